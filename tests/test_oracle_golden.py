@@ -1,0 +1,120 @@
+"""Pins the CPU oracle to the reference: every oracle function is checked
+against result dumps of the unmodified reference binaries (tests/golden/,
+made by tests/golden/make_golden.py).  No GPU needed."""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+CASES = ["tiny", "rmat10", "rmat12", "rmat16"]
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    rec = {k: z[k] for k in z.files}
+    n = int(rec["n"])
+    if "pairs" in rec:
+        pairs = rec["pairs"]
+    else:
+        scale = int(np.log2(n))
+        pairs = oracle.rmat_edges(scale, 16 * n, 1)
+    assert hashlib.sha256(pairs.tobytes()).hexdigest() == rec["pairs_sha256"].item().decode()
+    return n, pairs, rec
+
+
+@pytest.fixture(scope="module", params=CASES)
+def case(request):
+    n, pairs, rec = load(request.param)
+    return request.param, n, pairs, rec
+
+
+def test_generator_matches_stored_edges():
+    # the scale-16 fixture stores only a digest; load() regenerates and checks it
+    for name in CASES:
+        load(name)
+
+
+def test_pagerank_pull_quirk(case):
+    # pagerank_simple -m 2 -a 1: prev fixed at 0.15, serial fp32 sums in CSC order
+    name, n, pairs, rec = case
+    adj = oracle.build_adj(n, pairs)
+    got = oracle.pagerank_f32(adj, adj.out_deg(), 0.15, 10, swap=False)
+    np.testing.assert_array_equal(got.view(np.uint32), rec["pr_simple_pull"].view(np.uint32))
+
+
+def test_prgrid(case):
+    # prgrid_cilk -m 0: 10 iterations with swap, degrees counted twice
+    name, n, pairs, rec = case
+    P = oracle.default_p(n)
+    cell_ptr, gsrc, gdst = oracle.build_grid(n, pairs, P)
+    od, _ = oracle.degrees(n, pairs)
+    got = oracle.pagerank_grid_f32(n, P, cell_ptr, gsrc, gdst, 2 * od, 0.15, 10)
+    np.testing.assert_array_equal(got.view(np.uint32), rec["prgrid_m0"].view(np.uint32))
+    # the grid sum order equals the CSC order, so the CSR/CSC oracle agrees too
+    adj = oracle.build_adj(n, pairs)
+    got2 = oracle.pagerank_f32(adj, 2 * od, 0.15, 10, swap=True)
+    np.testing.assert_array_equal(got2.view(np.uint32), rec["prgrid_m0"].view(np.uint32))
+
+
+def test_bfs(case):
+    name, n, pairs, rec = case
+    adj = oracle.build_adj(n, pairs)
+    for r in rec["roots"]:
+        lv = oracle.bfs_levels(n, adj.out_ptr, adj.out_col, int(r))
+        np.testing.assert_array_equal(lv.astype(np.uint32), rec["bfsgrid_m0_p%d" % r])
+    # bfs_simple -m 8 (edge-centric): levels from root 0
+    lv0 = oracle.bfs_levels(n, adj.out_ptr, adj.out_col, 0)
+    np.testing.assert_array_equal(lv0.astype(np.uint32), rec["bfs_simple_m8"])
+    # bfs_simple -m 2 -u: visited counters; the visited set is the -u BFS reach
+    adju = oracle.build_adj(n, pairs, undirected=True)
+    lvu = oracle.bfs_levels(n, adju.out_ptr, adju.out_col, 0)
+    np.testing.assert_array_equal(lvu > 0, rec["bfs_simple_m2u"] > 0)
+
+
+def test_bfs_parents_form_tree(case):
+    name, n, pairs, rec = case
+    adj = oracle.build_adj(n, pairs)
+    for r in rec["roots"]:
+        lv, par = oracle.bfs_levels(n, adj.out_ptr, adj.out_col, int(r), parents=True)
+        assert oracle.bfs_tree_ok(n, adj.out_ptr, adj.out_col, int(r), lv, par)
+
+
+def test_sssp(case):
+    name, n, pairs, rec = case
+    adj = oracle.build_adj(n, pairs)
+    w = oracle.ref_weights(adj, "out")
+    for r in rec["roots"]:
+        d = oracle.sssp(n, adj.out_ptr, adj.out_col, w, int(r))
+        np.testing.assert_array_equal(d, rec["sssp_pull_p%d" % r])
+
+
+def test_wcc(case):
+    name, n, pairs, rec = case
+    lab = oracle.wcc(n, pairs)
+    np.testing.assert_array_equal(lab, rec["wcc_m2u"])
+    np.testing.assert_array_equal(lab, rec["wcc_m0"])
+    np.testing.assert_array_equal(lab, rec["wcc_m8"])
+
+
+def test_spmv_u32(case):
+    name, n, pairs, rec = case
+    adj = oracle.build_adj(n, pairs)
+    x = np.arange(n, dtype=np.uint32)
+    np.testing.assert_array_equal(oracle.spmv_u32(n, adj.in_ptr, adj.in_col, x, oracle.SPMV_PULL), rec["spmv_pull"])
+    np.testing.assert_array_equal(oracle.spmv_u32(n, adj.out_ptr, adj.out_col, x, oracle.SPMV_PUSH), rec["spmv_push"])
+    np.testing.assert_array_equal(oracle.spmv_u32(n, adj.out_ptr, adj.out_col, x, oracle.SPMV_EDGE), rec["spmv_m8"])
+
+
+def test_milli_floor_equals_integer_division():
+    # The reference scales x by the double 0.001 and truncates; for every u32 x
+    # that equals x // 1000 (the CUDA kernels use the integer form).  Checked on
+    # all multiples of 1000 and their neighbours plus a random sample.
+    k = np.arange(0, 4294968, dtype=np.uint64) * 1000
+    xs = np.concatenate([k, k + 1, k[1:] - 1, np.random.default_rng(0).integers(0, 2**32, 2_000_000)])
+    xs = xs[xs < 2**32].astype(np.uint64)
+    scaled = np.floor(0.001 * xs.astype(np.float64)).astype(np.uint64)
+    np.testing.assert_array_equal(scaled, xs // 1000)
