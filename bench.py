@@ -1,0 +1,262 @@
+"""Benchmark of the edge-traversal hot path on one GB300 (or N replicas).
+
+Default workload (the BFS/WCC configuration): undirected RMAT scale 24,
+edgefactor 16 (a=.57 b=.19 c=.19, seed 2), 16,777,216 vertices and
+536,870,912 adjacency entries after symmetrisation; one step = BFS from 64
+roots drawn uniformly from vertices with degree > 0 (seed 3), with int32
+levels and parents, plus min-id WCC.  value = GTEPS = (sum over roots of the
+out-degrees of reached vertices + input edges scanned by WCC) / step time.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  Inputs are larger than L2 (the CSR alone is
+2.1 GB), so no L2 flush is done between steps.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOAD = {"workload": "bfs64+wcc rmat24 undirected", "scale": 24, "edgefactor": 16, "seed": 2, "roots": 64,
+            "root_seed": 3, "undirected": True}
+METRIC, UNIT = "GTEPS", "GTEPS"
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return p["hbm_gbs"], "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """Samples nvidia-smi SM clocks and throttle reasons during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.samples = []
+        self.stop = threading.Event()
+        self.index = index
+        self.t = threading.Thread(target=self.run, daemon=True)
+
+    def run(self):
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                f = [x.strip() for x in out.stdout.strip().split(",")]
+                if len(f) == 6:
+                    self.samples.append(f)
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=10)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[2 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons}
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def run_ours(args):
+    import torch
+
+    import everythinggraph_gb300 as eg
+    from everythinggraph_gb300 import build
+
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    build.build_lib()
+    ctx = eg.Context(local)
+    W = dict(WORKLOAD)
+    if args.scale:
+        W["scale"] = args.scale
+    scale, ef = W["scale"], W["edgefactor"]
+    n = 1 << scale
+    m_in = ef * n
+    # ---- load: host pairs -> device -> CSR/CSC (timed separately, like init())
+    g = ctx.rmat(scale, m_in, W["seed"], undirected=True)
+    t0 = time.perf_counter()
+    g.build(eg.CSR | eg.CSC)
+    build_ms = g.info().build_ms
+    roots = g.sample_roots(W["roots"], W["root_seed"])
+    stream = torch.cuda.ExternalStream(ctx.stream)
+
+    def step(copy_out):
+        traversed = 0
+        for r in roots:
+            lv, par, st = g.bfs(int(r), parents=True, copy_out=copy_out)
+            if not copy_out:
+                pass
+            traversed += st.edges_traversed
+        lab, wst = g.wcc(copy_out=copy_out)
+        return traversed + m_in, wst
+
+    for _ in range(max(args.warmup, 0)):
+        step(False)
+    # ---- device-resident timed region
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    l0 = ctx.kernel_launches
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    edges = 0
+    with Clocks(local) as clk:
+        e0.record(stream)
+        for _ in range(args.steps):
+            te, _ = step(False)
+            edges += te
+        e1.record(stream)
+        torch.cuda.synchronize()
+    launches = ctx.kernel_launches - l0
+    ms = e0.elapsed_time(e1)
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    ms_step = ms / args.steps
+    value = edges * world / (ms / 1e3) / 1e9
+    # ---- end-to-end through the C ABI with host outputs (levels, parents, labels)
+    torch.cuda.synchronize()
+    te0 = time.perf_counter()
+    e_edges = 0
+    for _ in range(args.steps):
+        te, _ = step(True)
+        e_edges += te
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - te0
+    d2h = (W["roots"] * 2 * 4 * n + 8 * n)
+    h2d = W["roots"] * 4
+    # ---- per-kernel reports on the same graph size
+    kernels = {}
+    if not args.no_extras:
+        kernels = kernel_reports(ctx, eg, scale, args)
+    hbm, src = peaks()
+    dom = kernels.get("pagerank_pull_rmat%d" % scale)
+    roof = None
+    if dom:
+        roof = {"bound": "hbm", "achieved": dom["gbps"], "peak": hbm, "unit": "GB/s",
+                "frac": dom["gbps"] / hbm, "traffic": None, "kernel": "k_mp_rows<PrOp>", "peak_source": src}
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic (device RMAT generator)",
+        "config": dict(W, n=n, m_adjacency=2 * m_in, l2="inputs larger than L2 (CSR 2.1 GB)",
+                       parallelism="replicas" if world > 1 else "single"),
+        "e2e": {"value": e_edges * world / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "load": {"build_ms": build_ms},
+        "roofline": roof,
+        "clocks": clk.summary(),
+        "kernels": kernels,
+    }
+    if not args.no_cpu and rank == 0:
+        out["cpu_baseline"] = cpu_baseline(g, eg, roots, n, m_in, args)
+    g.free()
+    ctx.close()
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def kernel_reports(ctx, eg, scale, args):
+    """PageRank pull on the directed RMAT graph of the same scale (10 iterations)."""
+    import torch
+    rep = {}
+    n = 1 << scale
+    m = 16 * n
+    g = ctx.rmat(scale, m, 1).build(eg.CSR | eg.CSC)
+    g.pagerank(iterations=3, copy_out=False)
+    torch.cuda.synchronize()
+    _, st = g.pagerank(iterations=10, copy_out=False)
+    it_ms = st.ms / 10
+    bytes_it = 8 * m + 16 * n
+    rep["pagerank_pull_rmat%d" % scale] = {"ms_per_iter": it_ms, "gbps": bytes_it / (it_ms / 1e3) / 1e9,
+                                           "gteps": m / (it_ms / 1e3) / 1e9, "bytes_per_iter": bytes_it}
+    g.free()
+    return rep
+
+
+def cpu_baseline(g, eg, roots, n, m_in, args):
+    import oracle
+    oracle.build()
+    ptr, col = g.adj(eg.CSR)
+    threads = oracle.num_threads()
+    t0 = time.perf_counter()
+    traversed = 0
+    k = 0
+    od = np.diff(ptr.astype(np.int64))
+    for r in roots:
+        lv = oracle.bfs_levels(n, ptr, col, int(r))
+        traversed += int(od[lv > 0].sum())
+        k += 1
+        if time.perf_counter() - t0 > 15:
+            break
+    t1 = time.perf_counter()
+    return {"value": traversed / (t1 - t0) / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "%d of %d BFS roots on the same graph (serial oracle BFS)" % (k, len(roots))}
+
+
+def run_reference(args):
+    rank, world, local = dist_env()
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    print(json.dumps({"impl": "reference", "unavailable": "reference CPU arm not wired yet"}))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--scale", type=int, default=0)
+    ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,231 @@
+"""EverythingGraph edge-traversal hot path on GB300 (sm_103a).
+
+Python view of the C ABI in include/eg_gpu.h (libeg_gpu.so).  The C ABI is
+the product boundary; this module is a thin convenience layer used by the
+tests and the benchmark.  Every call runs CUDA kernels; there is no CPU path.
+
+    ctx = Context()
+    g = ctx.rmat(scale=20, m=16 << 20, seed=1)      # or ctx.from_pairs / from_file
+    g.build(CSR | CSC)
+    rank, st = g.pagerank(iterations=10)
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib as L
+from ._lib import EGError  # noqa: F401
+
+CSR, CSC, GRID = L.EG_LAYOUT_CSR, L.EG_LAYOUT_CSC, L.EG_LAYOUT_GRID
+UNDIRECTED = L.EG_UNDIRECTED
+UNREACHED_SSSP = 0xFFFFFFFE
+
+SPMV_KINDS = {"u32_pull": L.EG_SPMV_U32_PULL, "u32_push": L.EG_SPMV_U32_PUSH, "u32_edge": L.EG_SPMV_U32_EDGE,
+              "f32": L.EG_SPMV_F32, "f32_comp": L.EG_SPMV_F32_COMP, "f64": L.EG_SPMV_F64}
+
+
+def _ptr(a):
+    return ctypes.c_void_p(a.ctypes.data) if a is not None else ctypes.c_void_p(0)
+
+
+def lib():
+    return L.load()
+
+
+def weights(rule="ref", seed=0, lo=1, hi=255):
+    r = {"ref": L.EG_W_REF, "hash": L.EG_W_HASH, "unit": L.EG_W_UNIT}[rule]
+    return L.Weights(r, seed, lo, hi)
+
+
+class Context:
+    """One device, one stream (eg_open)."""
+
+    def __init__(self, device=0, hbm_budget=0):
+        self._h = ctypes.c_void_p()
+        L.check(lib().eg_open(device, hbm_budget, ctypes.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            lib().eg_close(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def stream(self):
+        return lib().eg_stream(self._h)
+
+    def sync(self):
+        L.check(lib().eg_sync(self._h))
+
+    @property
+    def bytes_in_use(self):
+        return lib().eg_bytes_in_use(self._h)
+
+    @property
+    def kernel_launches(self):
+        return lib().eg_kernel_launches(self._h)
+
+    def from_pairs(self, n, pairs, undirected=False):
+        pairs = np.ascontiguousarray(pairs, dtype=np.uint32)
+        h = ctypes.c_void_p()
+        L.check(lib().eg_graph_from_pairs(self._h, _ptr(pairs), len(pairs) // 2, n,
+                                          UNDIRECTED if undirected else 0, ctypes.byref(h)))
+        return Graph(self, h)
+
+    def from_device_pairs(self, n, dptr, m, undirected=False):
+        h = ctypes.c_void_p()
+        L.check(lib().eg_graph_from_device_pairs(self._h, ctypes.c_void_p(dptr), m, n,
+                                                 UNDIRECTED if undirected else 0, ctypes.byref(h)))
+        return Graph(self, h)
+
+    def from_file(self, path, n, undirected=False):
+        h = ctypes.c_void_p()
+        L.check(lib().eg_graph_from_file(self._h, path.encode(), n, UNDIRECTED if undirected else 0, ctypes.byref(h)))
+        return Graph(self, h)
+
+    def rmat(self, scale, m, seed, undirected=False):
+        h = ctypes.c_void_p()
+        L.check(lib().eg_graph_generate_rmat(self._h, scale, m, seed, UNDIRECTED if undirected else 0,
+                                             ctypes.byref(h)))
+        return Graph(self, h)
+
+    def er(self, n, m, seed, undirected=False):
+        h = ctypes.c_void_p()
+        L.check(lib().eg_graph_generate_er(self._h, n, m, seed, UNDIRECTED if undirected else 0, ctypes.byref(h)))
+        return Graph(self, h)
+
+
+class Graph:
+    def __init__(self, ctx, h):
+        self.ctx = ctx
+        self._h = h
+
+    def free(self):
+        if self._h:
+            lib().eg_graph_free(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+    # ---------------------------------------------------------------- layout
+    def build(self, layouts=CSR | CSC):
+        L.check(lib().eg_graph_build(self._h, layouts))
+        return self
+
+    def build_grid(self, P):
+        L.check(lib().eg_graph_build_grid(self._h, P))
+        return self
+
+    def info(self):
+        i = L.GraphInfo()
+        L.check(lib().eg_graph_get_info(self._h, ctypes.byref(i)))
+        return i
+
+    @property
+    def n(self):
+        return self.info().n
+
+    @property
+    def m(self):
+        return self.info().m
+
+    def adj(self, layout):
+        i = self.info()
+        ptr = np.empty(i.n + 1, dtype=np.uint32)
+        col = np.empty(i.m, dtype=np.uint32)
+        L.check(lib().eg_graph_copy_adj(self._h, layout, _ptr(ptr), _ptr(col)))
+        return ptr, col
+
+    def grid(self):
+        i = self.info()
+        cp = np.empty(i.grid_p * i.grid_p + 1, dtype=np.uint32)
+        s = np.empty(i.m, dtype=np.uint32)
+        d = np.empty(i.m, dtype=np.uint32)
+        L.check(lib().eg_graph_copy_grid(self._h, _ptr(cp), _ptr(s), _ptr(d)))
+        return cp, s, d
+
+    def degrees(self, out=True, inn=False):
+        n = self.n
+        od = np.empty(n, dtype=np.uint32) if out else None
+        idg = np.empty(n, dtype=np.uint32) if inn else None
+        L.check(lib().eg_graph_copy_degrees(self._h, _ptr(od), _ptr(idg)))
+        return od, idg
+
+    def device_ptr(self, which):
+        return lib().eg_graph_device_ptr(self._h, which)
+
+    def sample_roots(self, k, seed):
+        r = np.empty(k, dtype=np.uint32)
+        L.check(lib().eg_sample_roots(self._h, k, seed, _ptr(r)))
+        return r
+
+    # ---------------------------------------------------------------- algorithms
+    def pagerank(self, iterations=10, damping=0.85, prev_init=-1.0, swap=True, deg_multiplier=1, dangling=False,
+                 compensated=False, tolerance=0.0, copy_out=True):
+        o = L.PrOpts()
+        lib().eg_pr_opts_default(ctypes.byref(o))
+        o.iterations, o.damping, o.prev_init, o.swap = iterations, damping, prev_init, int(swap)
+        o.deg_multiplier, o.dangling, o.compensated, o.tolerance = deg_multiplier, int(dangling), int(compensated), tolerance
+        st = L.PrStats()
+        out = np.empty(self.n, dtype=np.float32) if copy_out else None
+        L.check(lib().eg_pagerank(self._h, ctypes.byref(o), _ptr(out), ctypes.byref(st)))
+        return out, st
+
+    def spmv(self, x, kind="u32_pull", value_seed=0, unit_values=False, copy_out=True):
+        k = SPMV_KINDS[kind]
+        xd = np.uint32 if kind.startswith("u32") else np.float32
+        x = np.ascontiguousarray(x, dtype=xd)
+        yd = np.float64 if kind == "f64" else xd
+        y = np.empty(self.n, dtype=yd) if copy_out else None
+        o = L.SpmvOpts(k, value_seed, int(unit_values))
+        ms = ctypes.c_float()
+        L.check(lib().eg_spmv(self._h, ctypes.byref(o), _ptr(x), _ptr(y), ctypes.byref(ms)))
+        return y, ms.value
+
+    def bfs(self, root, direction="auto", switch_divisor=20.0, parents=False, copy_out=True):
+        o = L.BfsOpts({"auto": L.EG_BFS_AUTO, "push": L.EG_BFS_PUSH_ONLY, "pull": L.EG_BFS_PULL_ONLY}[direction],
+                      switch_divisor)
+        n = self.n
+        lv = np.empty(n, dtype=np.int32) if copy_out else None
+        par = np.empty(n, dtype=np.int32) if parents else None
+        st = L.BfsStats()
+        L.check(lib().eg_bfs(self._h, root, ctypes.byref(o), _ptr(lv), _ptr(par), ctypes.byref(st)))
+        return (lv, par, st) if parents else (lv, st)
+
+    def bfs_multi(self, roots, copy_out=True):
+        roots = np.ascontiguousarray(roots, dtype=np.uint32)
+        n = self.n
+        out = np.empty((len(roots), n), dtype=np.int32) if copy_out else None
+        st = L.BfsStats()
+        L.check(lib().eg_bfs_multi(self._h, _ptr(roots), len(roots), _ptr(out), ctypes.byref(st)))
+        return out, st
+
+    def sssp(self, root, w=None, copy_out=True):
+        w = w or weights("ref")
+        out = np.empty(self.n, dtype=np.uint32) if copy_out else None
+        st = L.SsspStats()
+        L.check(lib().eg_sssp(self._h, root, ctypes.byref(w), _ptr(out), ctypes.byref(st)))
+        return out, st
+
+    def sssp_multi(self, roots, w=None, copy_out=True):
+        w = w or weights("ref")
+        roots = np.ascontiguousarray(roots, dtype=np.uint32)
+        out = np.empty((len(roots), self.n), dtype=np.uint32) if copy_out else None
+        st = L.SsspStats()
+        L.check(lib().eg_sssp_multi(self._h, _ptr(roots), len(roots), ctypes.byref(w), _ptr(out), ctypes.byref(st)))
+        return out, st
+
+    def wcc(self, copy_out=True):
+        out = np.empty(self.n, dtype=np.int64) if copy_out else None
+        st = L.WccStats()
+        L.check(lib().eg_wcc(self._h, _ptr(out), ctypes.byref(st)))
+        return out, st

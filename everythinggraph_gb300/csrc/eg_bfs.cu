@@ -1,0 +1,497 @@
+// Direction-optimising BFS with a bitmap frontier, and bit-sliced
+// multi-source BFS.
+//
+// Replaces bfs_simple.c (bfs_push 121-134, bfs_pull 104-120, the switch rule
+// 191-197) and bfsgrid_cilk.c (get_bfs 48-65, iterator 121-168).  The
+// reference's frontier is a byte map plus id lists (random.c:74-77,
+// buffer.c:62-297); here it is a bitmap in the style of Gemini's Bitmap
+// (bitmap.h:16-50), written one 32-bit word per warp with __ballot_sync, plus
+// a compacted id queue for push levels.
+//
+// Levels follow the reference: level[root] = 1, unreached = 0 (the value
+// bfsgrid_cilk and the edge-centric bfs_simple write into dist[]).
+#include <stdlib.h>
+#include <string.h>
+
+#include "eg_internal.cuh"
+
+namespace {
+
+struct BfsCounters {
+    unsigned long long next_deg;  // sum of out-degrees of the new frontier
+    uint32_t next_count;          // vertices in the new frontier
+    uint32_t qsize;               // entries in the next queue
+};
+
+__device__ __forceinline__ void warp_add_counters(BfsCounters *c, uint32_t cnt, unsigned long long deg) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        cnt += __shfl_down_sync(EG_FULL_MASK, cnt, o);
+        deg += __shfl_down_sync(EG_FULL_MASK, deg, o);
+    }
+    if ((threadIdx.x & 31) == 0 && cnt) {
+        atomicAdd(&c->next_count, cnt);
+        atomicAdd(&c->next_deg, deg);
+    }
+}
+
+__global__ void k_bfs_init(uint32_t n, int32_t *level, int32_t *parent, uint32_t *visited, uint32_t *cur_bm,
+                           uint32_t nw, uint32_t root, uint32_t *queue, const uint32_t *deg, BfsCounters *cnt) {
+    uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+        level[v] = v == root ? 1 : 0;
+        if (parent) parent[v] = v == root ? (int32_t)root : -1;
+    }
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += stride) {
+        uint32_t bit = (root >> 5) == w ? 1u << (root & 31) : 0u;
+        visited[w] = bit;
+        cur_bm[w] = bit;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        queue[0] = root;
+        cnt->next_count = 1;
+        cnt->qsize = 1;
+        cnt->next_deg = deg[root];
+    }
+}
+
+// Top-down step: one warp per frontier vertex, lanes over its out-list.
+// A vertex is claimed by the atomicOr that sets its visited bit.
+__global__ void __launch_bounds__(256) k_bfs_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+                                                  const uint32_t *__restrict__ deg, const uint32_t *__restrict__ queue,
+                                                  uint32_t qlen, uint32_t *visited, uint32_t *next_bm,
+                                                  uint32_t *next_queue, int32_t *level, int32_t *parent,
+                                                  int32_t next_level, BfsCounters *cnt) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t lt = eg_lanemask_lt();
+    for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < qlen; qi += warps) {
+        const uint32_t u = queue[qi];
+        const uint32_t b = ptr[u], e = ptr[u + 1];
+        for (uint32_t p0 = b; p0 < e; p0 += 32) {
+            const uint32_t p = p0 + lane;
+            bool claimed = false;
+            uint32_t v = 0;
+            if (p < e) {
+                v = col[p];
+                const uint32_t bit = 1u << (v & 31);
+                if (!(__ldcg(visited + (v >> 5)) & bit)) {
+                    uint32_t old = atomicOr(visited + (v >> 5), bit);
+                    if (!(old & bit)) {
+                        claimed = true;
+                        level[v] = next_level;
+                        if (parent) parent[v] = (int32_t)u;
+                        atomicOr(next_bm + (v >> 5), bit);
+                    }
+                }
+            }
+            const uint32_t ball = __ballot_sync(EG_FULL_MASK, claimed);
+            if (ball) {
+                uint32_t base = 0;
+                if (lane == 0) base = atomicAdd(&cnt->qsize, __popc(ball));
+                base = __shfl_sync(EG_FULL_MASK, base, 0);
+                if (claimed) next_queue[base + __popc(ball & lt)] = v;
+                unsigned long long d = claimed ? deg[v] : 0ull;
+                uint32_t c = claimed ? 1u : 0u;
+                warp_add_counters(cnt, c, d);
+            }
+        }
+    }
+}
+
+// Bottom-up step: one thread per vertex, warps over 32 consecutive vertices
+// (one bitmap word).  An unvisited vertex scans its in-list and stops at the
+// first neighbour in the frontier.  The new frontier word is the warp ballot.
+__global__ void __launch_bounds__(256) k_bfs_pull(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+                                                  const uint32_t *__restrict__ deg, uint32_t n,
+                                                  const uint32_t *__restrict__ cur_bm, uint32_t *visited,
+                                                  uint32_t *next_bm, int32_t *level, int32_t *parent,
+                                                  int32_t next_level, BfsCounters *cnt) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nw = (n + 31) >> 5;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += warps) {
+        const uint32_t vis = visited[w];
+        if (vis == EG_FULL_MASK) {
+            if (lane == 0) next_bm[w] = 0;
+            continue;
+        }
+        const uint32_t v = (w << 5) + lane;
+        bool found = false;
+        if (v < n && !(vis & (1u << lane))) {
+            const uint32_t b = ptr[v], e = ptr[v + 1];
+            for (uint32_t p = b; p < e; p++) {
+                const uint32_t u = col[p];
+                if (__ldg(cur_bm + (u >> 5)) & (1u << (u & 31))) {
+                    found = true;
+                    level[v] = next_level;
+                    if (parent) parent[v] = (int32_t)u;
+                    break;
+                }
+            }
+        }
+        const uint32_t ball = __ballot_sync(EG_FULL_MASK, found);
+        if (lane == 0) {
+            next_bm[w] = ball;
+            if (ball) visited[w] = vis | ball;
+        }
+        if (ball) warp_add_counters(cnt, found ? 1u : 0u, found ? (unsigned long long)deg[v] : 0ull);
+    }
+}
+
+// Bitmap -> id queue (ballot/popc compaction, one warp-aggregated atomic per word).
+__global__ void k_bm_to_queue(const uint32_t *__restrict__ bm, uint32_t n, uint32_t *queue, BfsCounters *cnt) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nw = (n + 31) >> 5;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t lt = eg_lanemask_lt();
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += warps) {
+        const uint32_t word = bm[w];
+        if (!word) continue;
+        const bool on = (word >> lane) & 1u;
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&cnt->qsize, __popc(word));
+        base = __shfl_sync(EG_FULL_MASK, base, 0);
+        if (on) queue[base + __popc(word & lt)] = (w << 5) + lane;
+    }
+}
+
+}  // namespace
+
+extern "C" void eg_bfs_opts_default(eg_bfs_opts *o) {
+    if (!o) return;
+    o->direction = EG_BFS_AUTO;
+    o->switch_divisor = 20.0;
+}
+
+static uint32_t blocks_for(eg_ctx *ctx, uint64_t threads) {
+    uint64_t b = (threads + 255) / 256;
+    uint64_t cap = (uint64_t)ctx->sm_count * 8;
+    if (b > cap) b = cap;
+    return b ? (uint32_t)b : 1u;
+}
+
+extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32_t *level_out, int32_t *parent_out,
+                      eg_bfs_stats *stats) {
+    if (!g) return eg_fail(EG_EINVAL, "NULL graph");
+    if (root >= g->n) return eg_fail(EG_EINVAL, "root %u >= n %u", root, g->n);
+    if (!(g->built & EG_LAYOUT_CSR)) return eg_fail(EG_ENOTBUILT, "BFS needs the CSR");
+    eg_bfs_opts o;
+    if (opts) o = *opts;
+    else eg_bfs_opts_default(&o);
+    const bool undirected = (g->flags & EG_UNDIRECTED) != 0;
+    eg_adj *in_adj = undirected ? &g->csr : ((g->built & EG_LAYOUT_CSC) ? &g->csc : nullptr);
+    if (!in_adj && o.direction != EG_BFS_PUSH_ONLY)
+        return eg_fail(EG_ENOTBUILT, "bottom-up BFS on a directed graph needs the CSC");
+    eg_ctx *ctx = g->ctx;
+    EG_CUDA(cudaSetDevice(ctx->device));
+    const uint32_t n = g->n;
+    const uint32_t nw = (n + 31) >> 5;
+    const bool want_parent = parent_out != nullptr;
+    EG_TRY(eg_buf_ensure(ctx, g->level, (uint64_t)n * 4));
+    if (want_parent) EG_TRY(eg_buf_ensure(ctx, g->parent, (uint64_t)n * 4));
+    // work: visited | bm0 | bm1 | queue0 | queue1 | counters
+    const uint64_t off_bm0 = (uint64_t)nw, off_bm1 = 2ull * nw, off_q0 = 3ull * nw, off_q1 = off_q0 + n,
+                   off_cnt = (off_q1 + n + 7) & ~7ull;
+    EG_TRY(eg_buf_ensure(ctx, g->bfs_work, (off_cnt + 8) * 4));
+    uint32_t *wk = bp<uint32_t>(g->bfs_work);
+    uint32_t *visited = wk, *bm[2] = {wk + off_bm0, wk + off_bm1}, *q[2] = {wk + off_q0, wk + off_q1};
+    BfsCounters *cnt = reinterpret_cast<BfsCounters *>(wk + off_cnt);
+    int32_t *level = bp<int32_t>(g->level);
+    int32_t *parent = want_parent ? bp<int32_t>(g->parent) : nullptr;
+    const uint32_t *deg = bp<uint32_t>(g->out_deg);
+    BfsCounters *h = (BfsCounters *)ctx->h_pinned;
+
+    EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    k_bfs_init<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(n, level, parent, visited, bm[0], nw, root, q[0], deg, cnt);
+    EG_LAUNCHED(ctx);
+    uint32_t count = 1, qlen = 1;
+    unsigned long long fdeg = 0;
+    EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(BfsCounters), cudaMemcpyDeviceToHost, ctx->stream));
+    EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    fdeg = h->next_deg;
+    int cur = 0;
+    bool have_queue = true;  // q[cur] lists the frontier
+    int32_t lvl = 1;
+    int pull_levels = 0;
+    uint64_t reached = 1, traversed = fdeg;
+    const double threshold = o.switch_divisor > 0 ? (double)g->m / o.switch_divisor : 0.0;
+    while (count > 0) {
+        bool pull;
+        if (o.direction == EG_BFS_PUSH_ONLY) pull = false;
+        else if (o.direction == EG_BFS_PULL_ONLY) pull = true;
+        else pull = (double)count + (double)fdeg > threshold;
+        const int nxt = cur ^ 1;
+        EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(BfsCounters), ctx->stream));
+        if (pull) {
+            k_bfs_pull<<<blocks_for(ctx, (uint64_t)nw * 32), 256, 0, ctx->stream>>>(
+                bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col), deg, n, bm[cur], visited, bm[nxt], level, parent,
+                lvl + 1, cnt);
+            EG_LAUNCHED(ctx);
+            pull_levels++;
+            have_queue = false;
+        } else {
+            if (!have_queue) {
+                k_bm_to_queue<<<blocks_for(ctx, (uint64_t)nw * 32), 256, 0, ctx->stream>>>(bm[cur], n, q[cur], cnt);
+                EG_LAUNCHED(ctx);
+                EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(BfsCounters), cudaMemcpyDeviceToHost, ctx->stream));
+                EG_CUDA(cudaStreamSynchronize(ctx->stream));
+                qlen = h->qsize;
+                EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(BfsCounters), ctx->stream));
+            }
+            EG_CUDA(cudaMemsetAsync(bm[nxt], 0, (uint64_t)nw * 4, ctx->stream));
+            k_bfs_push<<<blocks_for(ctx, (uint64_t)qlen * 32), 256, 0, ctx->stream>>>(
+                bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, q[cur], qlen, visited, bm[nxt], q[nxt], level,
+                parent, lvl + 1, cnt);
+            EG_LAUNCHED(ctx);
+            have_queue = true;
+        }
+        EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(BfsCounters), cudaMemcpyDeviceToHost, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        count = h->next_count;
+        fdeg = h->next_deg;
+        qlen = h->qsize;
+        reached += count;
+        traversed += fdeg;
+        cur = nxt;
+        lvl++;
+        if (lvl > (int32_t)n + 1) return eg_fail(EG_ETIMEOUT, "BFS did not terminate");
+    }
+    EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (level_out) EG_CUDA(cudaMemcpyAsync(level_out, level, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (want_parent) EG_CUDA(cudaMemcpyAsync(parent_out, parent, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (stats) {
+        stats->levels = lvl - 1;
+        stats->reached = (uint32_t)reached;
+        stats->edges_traversed = traversed;
+        stats->pull_levels = pull_levels;
+        EG_CUDA(cudaEventElapsedTime(&stats->ms, ctx->ev0, ctx->ev1));
+    }
+    return EG_OK;
+}
+
+// ============================================================== multi-source
+// Bit-sliced BFS: bit s of seen[v] / front[v] belongs to source s (k <= 64).
+namespace {
+struct MsCounters {
+    unsigned long long deg;   // sum of out-degrees of vertices with a nonzero new word
+    unsigned long long tdeg;  // sum over new (vertex, source) pairs of the vertex's out-degree
+    unsigned long long disc;  // new (vertex, source) pairs
+    uint32_t count;           // vertices with a nonzero new word
+    uint32_t pad;
+};
+
+__global__ void k_ms_init(uint32_t n, unsigned long long *seen, unsigned long long *front) {
+    uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+        seen[v] = 0ull;
+        front[v] = 0ull;
+    }
+}
+
+__global__ void k_ms_roots(const uint32_t *roots, int k, uint32_t n, unsigned long long *seen, unsigned long long *front,
+                           int32_t *levels) {
+    int s = threadIdx.x;
+    if (s < k) {
+        uint32_t r = roots[s];
+        atomicOr(seen + r, 1ull << s);
+        atomicOr(front + r, 1ull << s);
+        if (levels) levels[(uint64_t)s * n + r] = 1;
+    }
+}
+
+// Pull: a vertex ORs the frontier words of its in-neighbours, stopping early
+// once every source it still lacks has been found.
+__global__ void __launch_bounds__(256) k_ms_pull(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+                                                 uint32_t n, unsigned long long all,
+                                                 const unsigned long long *__restrict__ seen,
+                                                 const unsigned long long *__restrict__ front,
+                                                 unsigned long long *__restrict__ next) {
+    uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+        unsigned long long need = all & ~seen[v];
+        unsigned long long acc = 0ull;
+        if (need) {
+            const uint32_t b = ptr[v], e = ptr[v + 1];
+            for (uint32_t p = b; p < e; p++) {
+                acc |= __ldg(front + col[p]);
+                if ((acc & need) == need) break;
+            }
+        }
+        next[v] = acc & need;
+    }
+}
+
+// Push: one warp per vertex with a nonzero frontier word.
+__global__ void __launch_bounds__(256) k_ms_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+                                                 const uint32_t *__restrict__ queue, uint32_t qlen,
+                                                 const unsigned long long *__restrict__ seen,
+                                                 const unsigned long long *__restrict__ front,
+                                                 unsigned long long *__restrict__ next) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < qlen; qi += warps) {
+        const uint32_t u = queue[qi];
+        const unsigned long long f = front[u];
+        for (uint32_t p = ptr[u] + lane; p < ptr[u + 1]; p += 32) {
+            const uint32_t v = col[p];
+            const unsigned long long add = f & ~__ldcg(seen + v);
+            if (add && (__ldcg(next + v) & add) != add) atomicOr(next + v, add);
+        }
+    }
+}
+
+// Folds the new words into seen, records levels, makes them the frontier and
+// lists the frontier vertices for a following push step.
+__global__ void k_ms_fold(uint32_t n, int k, unsigned long long *seen, unsigned long long *front,
+                          unsigned long long *next, int clear_next, int32_t *levels, int32_t lvl,
+                          const uint32_t *__restrict__ deg, uint32_t *queue, MsCounters *cnt) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t lt = eg_lanemask_lt();
+    uint32_t stride = gridDim.x * blockDim.x;
+    // uniform trip count per warp for the ballots
+    for (uint32_t v0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); v0 < n; v0 += stride) {
+        const uint32_t v = v0 + lane;
+        unsigned long long x = 0ull;
+        if (v < n) {
+            x = next[v] & ~seen[v];
+            if (clear_next) next[v] = 0ull;
+            front[v] = x;
+            if (x) {
+                seen[v] |= x;
+                if (levels) {
+                    unsigned long long y = x;
+                    while (y) {
+                        int s = __ffsll((long long)y) - 1;
+                        y &= y - 1;
+                        levels[(uint64_t)s * n + v] = lvl;
+                    }
+                }
+            }
+        }
+        const uint32_t ball = __ballot_sync(EG_FULL_MASK, x != 0ull);
+        if (ball) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(&cnt->count, __popc(ball));
+            base = __shfl_sync(EG_FULL_MASK, base, 0);
+            unsigned long long d = x ? (unsigned long long)deg[v] : 0ull;
+            unsigned long long pc = (unsigned long long)__popcll((long long)x);
+            unsigned long long td = d * pc;
+            if (x) queue[base + __popc(ball & lt)] = v;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                d += __shfl_down_sync(EG_FULL_MASK, d, o);
+                td += __shfl_down_sync(EG_FULL_MASK, td, o);
+                pc += __shfl_down_sync(EG_FULL_MASK, pc, o);
+            }
+            if (lane == 0) {
+                atomicAdd(&cnt->deg, d);
+                atomicAdd(&cnt->tdeg, td);
+                atomicAdd(&cnt->disc, pc);
+            }
+        }
+    }
+}
+}  // namespace
+
+extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *levels_out, eg_bfs_stats *stats) {
+    if (!g || !roots) return eg_fail(EG_EINVAL, "NULL argument");
+    if (k < 1 || k > 64) return eg_fail(EG_EINVAL, "k=%d sources: bit-sliced BFS takes 1..64", k);
+    if (!(g->built & EG_LAYOUT_CSR)) return eg_fail(EG_ENOTBUILT, "BFS needs the CSR");
+    const bool undirected = (g->flags & EG_UNDIRECTED) != 0;
+    eg_adj *in_adj = undirected ? &g->csr : ((g->built & EG_LAYOUT_CSC) ? &g->csc : nullptr);
+    if (!in_adj) return eg_fail(EG_ENOTBUILT, "multi-source BFS on a directed graph needs the CSC");
+    for (int s = 0; s < k; s++)
+        if (roots[s] >= g->n) return eg_fail(EG_EINVAL, "root %u >= n", roots[s]);
+    eg_ctx *ctx = g->ctx;
+    EG_CUDA(cudaSetDevice(ctx->device));
+    const uint32_t n = g->n;
+    // work: seen | front | next (u64 each) | queue (u32) | roots | counters
+    const uint64_t words = 3ull * n;
+    const uint64_t bytes = words * 8 + (uint64_t)n * 4 + 64 * 4 + 64;
+    EG_TRY(eg_buf_ensure(ctx, g->msbfs_work, bytes));
+    unsigned long long *seen = bp<unsigned long long>(g->msbfs_work);
+    unsigned long long *front = seen + n, *next = seen + 2ull * n;
+    uint32_t *queue = reinterpret_cast<uint32_t *>(seen + 3ull * n);
+    uint32_t *d_roots = queue + n;
+    MsCounters *cnt = reinterpret_cast<MsCounters *>(d_roots + 64);
+    int32_t *levels = nullptr;
+    if (levels_out) {
+        EG_TRY(eg_buf_ensure(ctx, g->level, (uint64_t)k * n * 4));
+        levels = bp<int32_t>(g->level);
+    }
+    MsCounters *h = (MsCounters *)ctx->h_pinned;
+    const uint32_t *deg = bp<uint32_t>(g->out_deg);
+    const unsigned long long all = k == 64 ? ~0ull : ((1ull << k) - 1ull);
+    EG_CUDA(cudaMemcpyAsync(d_roots, roots, (uint64_t)k * 4, cudaMemcpyHostToDevice, ctx->stream));
+    EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    if (levels) EG_CUDA(cudaMemsetAsync(levels, 0, (uint64_t)k * n * 4, ctx->stream));
+    k_ms_init<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(n, seen, front);
+    EG_LAUNCHED(ctx);
+    EG_CUDA(cudaMemsetAsync(next, 0, (uint64_t)n * 8, ctx->stream));
+    k_ms_roots<<<1, 64, 0, ctx->stream>>>(d_roots, k, n, seen, front, levels);
+    EG_LAUNCHED(ctx);
+    // first frontier: the distinct roots
+    uint32_t count = 0;
+    unsigned long long fdeg = 0, rdeg = 0;
+    {
+        uint32_t *hq = (uint32_t *)malloc((size_t)k * 4);
+        uint32_t *hdeg = (uint32_t *)ctx->h_pinned + 1024;
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        for (int s = 0; s < k; s++) {
+            bool dup = false;
+            for (uint32_t i = 0; i < count; i++) dup |= hq[i] == roots[s];
+            if (!dup) hq[count++] = roots[s];
+        }
+        EG_CUDA(cudaMemcpy(queue, hq, (uint64_t)count * 4, cudaMemcpyHostToDevice));
+        for (uint32_t i = 0; i < count; i++) {
+            EG_CUDA(cudaMemcpy(hdeg, deg + hq[i], 4, cudaMemcpyDeviceToHost));
+            fdeg += *hdeg;
+            for (int s = 0; s < k; s++) rdeg += roots[s] == hq[i] ? *hdeg : 0u;
+        }
+        free(hq);
+    }
+    uint64_t reached = (uint64_t)k, traversed = rdeg;
+    int32_t lvl = 1;
+    int pull_levels = 0;
+    const double threshold = (double)g->m / 20.0;
+    while (count > 0) {
+        const bool pull = (double)count + (double)fdeg > threshold;
+        if (pull) {
+            k_ms_pull<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col),
+                                                                  n, all, seen, front, next);
+            EG_LAUNCHED(ctx);
+            pull_levels++;
+        } else {
+            k_ms_push<<<blocks_for(ctx, (uint64_t)count * 32), 256, 0, ctx->stream>>>(
+                bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), queue, count, seen, front, next);
+            EG_LAUNCHED(ctx);
+        }
+        EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(MsCounters), ctx->stream));
+        // after a push the next words were accumulated with atomics and must be
+        // cleared for the following level; after a pull they are overwritten
+        k_ms_fold<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(n, k, seen, front, next, 1, levels, lvl + 1, deg, queue,
+                                                              cnt);
+        EG_LAUNCHED(ctx);
+        EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(MsCounters), cudaMemcpyDeviceToHost, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        count = h->count;
+        fdeg = h->deg;
+        reached += h->disc;
+        traversed += h->tdeg;
+        lvl++;
+        if (lvl > (int32_t)n + 1) return eg_fail(EG_ETIMEOUT, "multi-source BFS did not terminate");
+    }
+    EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (levels_out) EG_CUDA(cudaMemcpyAsync(levels_out, levels, (uint64_t)k * n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (stats) {
+        stats->levels = lvl - 1;
+        stats->reached = (uint32_t)(reached > 0xffffffffull ? 0xffffffffull : reached);
+        stats->edges_traversed = traversed;
+        stats->pull_levels = pull_levels;
+        EG_CUDA(cudaEventElapsedTime(&stats->ms, ctx->ev0, ctx->ev1));
+    }
+    return EG_OK;
+}

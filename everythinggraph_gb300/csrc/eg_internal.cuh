@@ -1,0 +1,149 @@
+// Internal declarations shared by the CUDA translation units of libeg_gpu.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "eg_gpu.h"
+
+#define EG_FULL_MASK 0xffffffffu
+
+// ---------------------------------------------------------------- errors
+int eg_fail(int code, const char *fmt, ...);
+void eg_clear_error();
+
+#define EG_CUDA(call)                                                                               \
+    do {                                                                                            \
+        cudaError_t e_ = (call);                                                                    \
+        if (e_ != cudaSuccess)                                                                      \
+            return eg_fail(EG_ECUDA, "%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+#define EG_TRY(call)                 \
+    do {                             \
+        int rc_ = (call);            \
+        if (rc_ != EG_OK) return rc_; \
+    } while (0)
+
+// Checks the last launch and counts it.
+#define EG_LAUNCHED(ctx)                                                                           \
+    do {                                                                                           \
+        (ctx)->launches++;                                                                         \
+        cudaError_t e_ = cudaGetLastError();                                                       \
+        if (e_ != cudaSuccess)                                                                     \
+            return eg_fail(EG_ECUDA, "%s:%d launch: %s", __FILE__, __LINE__, cudaGetErrorString(e_)); \
+    } while (0)
+
+// ---------------------------------------------------------------- context
+struct eg_ctx {
+    int device;
+    int sm_count;
+    cudaStream_t stream;
+    uint64_t budget;
+    uint64_t in_use;
+    uint64_t launches;
+    void *h_pinned;  // 1 MiB pinned staging for small readbacks
+    cudaEvent_t ev0, ev1;
+};
+
+int eg_dmalloc(eg_ctx *ctx, void **p, uint64_t bytes);
+void eg_dfree(eg_ctx *ctx, void *p, uint64_t bytes);
+
+// A device buffer tracked against the context budget.
+struct eg_buf {
+    void *p = nullptr;
+    uint64_t bytes = 0;
+};
+int eg_buf_ensure(eg_ctx *ctx, eg_buf &b, uint64_t bytes);  // grows (contents lost)
+void eg_buf_free(eg_ctx *ctx, eg_buf &b);
+template <class T>
+static inline T *bp(const eg_buf &b) {
+    return (T *)b.p;
+}
+
+// ---------------------------------------------------------------- graph
+struct eg_adj {
+    eg_buf ptr;  // uint32[n+1]
+    eg_buf col;  // uint32[m]
+};
+
+// Merge-path schedule of one adjacency for one tile width.
+struct eg_mp_sched {
+    uint32_t items = 0;   // merge items per tile (threads * items per thread)
+    uint32_t ntiles = 0;  // tiles
+    eg_buf coord;         // uint2[ntiles+1]: (row, edge) at each tile start
+};
+
+struct eg_graph {
+    eg_ctx *ctx;
+    uint32_t n;
+    uint64_t m_in;  // input edges
+    uint64_t m;     // adjacency entries
+    unsigned flags;
+    unsigned built;
+    float build_ms;
+    eg_buf pairs;  // uint32[2*m_in]
+    eg_adj csr, csc;
+    eg_buf out_deg, in_deg;  // uint32[n]
+    // grid
+    uint32_t grid_p;
+    eg_buf cell_ptr, gsrc, gdst;
+    // schedules (CSC rows for PR/SpMV pull, CSR rows for push)
+    eg_mp_sched sched_csc, sched_csr;
+    // algorithm state, allocated on first use and reused
+    eg_buf rank, contrib0, contrib1, pr_part, pr_stats, mp_carry;
+    eg_buf level, parent, dist, label, spmv_x, spmv_y, spmv_vals;
+    uint64_t spmv_vals_seed;
+    int spmv_vals_kind;
+    eg_buf bfs_work;  // bitmaps, queues, counters
+    eg_buf msbfs_work;
+    eg_buf sssp_work;
+};
+
+// ---------------------------------------------------------------- helpers
+static inline uint32_t eg_div_up(uint64_t a, uint64_t b) { return (uint32_t)((a + b - 1) / b); }
+
+// device scan: out[i] = sum_{j<i} in[j] for i in [0, len]; out has len+1
+// entries (the last is the total).  in may equal out only if len+1 fits.
+int eg_exscan_u32(eg_ctx *ctx, const uint32_t *in, uint32_t *out, uint64_t len);
+// histogram of keys (values < n) into zeroed hist[n]
+int eg_histogram(eg_ctx *ctx, const uint32_t *keys, uint64_t len, uint32_t *hist);
+// stable LSD radix sort of (key, value) pairs by the low `bits` bits of key.
+// Sorted data ends in (k_out, v_out); the input arrays are overwritten.
+int eg_radix_sort(eg_ctx *ctx, uint32_t *k_in, uint32_t *v_in, uint32_t *k_tmp, uint32_t *v_tmp, uint64_t len,
+                  int bits, uint32_t **k_out, uint32_t **v_out);
+int eg_build_sched(eg_graph *g, eg_adj &adj, eg_mp_sched &s, uint32_t items);
+
+// ---------------------------------------------------------------- device utils
+#ifdef __CUDACC__
+__device__ __forceinline__ uint32_t eg_lanemask_lt() {
+    uint32_t r;
+    asm("mov.u32 %0, %%lanemask_lt;" : "=r"(r));
+    return r;
+}
+__device__ __forceinline__ uint32_t eg_ldg_nc(const uint32_t *p) {
+    uint32_t v;
+    asm volatile("ld.global.nc.u32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+}
+// SplitMix64 output function (Steele, Lea & Flood, OOPSLA 2014); the same
+// counter scheme as the CPU generator.
+__host__ __device__ __forceinline__ uint64_t eg_mix64(uint64_t z) {
+    z += 0x9E3779B97F4A7C15ull;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+__host__ __device__ __forceinline__ uint64_t eg_key(uint64_t seed, uint64_t idx) {
+    return eg_mix64(eg_mix64(seed) ^ idx);
+}
+__host__ __device__ __forceinline__ uint64_t eg_draw(uint64_t key, uint64_t j) {
+    return eg_mix64(key + j * 0x632BE59BD9B4E019ull);
+}
+// Symmetric per-edge hash of the endpoints, for weight and value rules.
+__host__ __device__ __forceinline__ uint64_t eg_edge_hash(uint64_t seed, uint32_t u, uint32_t v) {
+    uint32_t a = u < v ? u : v, b = u < v ? v : u;
+    return eg_draw(eg_key(seed, ((uint64_t)a << 32) | b), 0);
+}
+#endif

@@ -1,0 +1,262 @@
+// Merge-path row reduction over a CSR-shaped adjacency (ptr[n+1], col[m]).
+//
+// Rows and entries are merged into one sequence of n+m items (a row's end
+// follows its last entry); each CTA takes a fixed window of `T*IPT` items, so
+// work is balanced whatever the degree skew (RMAT hubs with 10^5..10^6
+// entries are spread over many CTAs; runs of empty rows cost one item each).
+// The windows' start coordinates are precomputed once per graph (schedule).
+//
+// Inside a CTA: row ends and entry values (gathered through col) are staged in
+// shared memory with coalesced 128-bit loads of col; every thread then walks
+// IPT consecutive items sequentially.  A row split between threads is summed
+// by the thread that sees its end, walking back over the partial sums of the
+// threads before it (fixed order, so results are deterministic).  A row split
+// between CTAs is finished by a fix-up kernel that adds the CTAs' partials in
+// CTA order.  Completed rows are written out by all threads in row order
+// (coalesced).
+//
+// The Op supplies: value type V, accumulator A,
+//   V gather(j, u)            value of entry j whose column is u
+//   A zero(), A add(A, V), A merge(A left, A right)
+//   R emit(row, A)            finishes a row; R (double2) is folded into a
+//                             per-CTA FP64 reduction when REDUCE is set
+#pragma once
+#include "eg_internal.cuh"
+
+#define EG_MP_NONE 0xffffffffu
+
+template <class A>
+struct eg_mp_carry {
+    uint32_t head_row;  // row finished in this CTA that began in an earlier CTA
+    uint32_t tail_row;  // row still open at the CTA's end (n if none)
+    A head_val;         // this CTA's partial of head_row
+    A tail_val;         // this CTA's partial of tail_row
+};
+
+__global__ void k_mp_schedule(const uint32_t *__restrict__ ptr, uint32_t n, uint32_t m, uint32_t items,
+                              uint32_t ntiles, uint2 *__restrict__ coord);
+
+template <int T, int IPT, class V, class A>
+struct eg_mp_smem {
+    static constexpr int W = T * IPT;
+    static constexpr size_t rowend_off = 0;
+    static constexpr size_t val_off = ((W + 2) * 4 + 15) & ~(size_t)15;
+    static constexpr size_t sum_off = (val_off + W * sizeof(V) + 15) & ~(size_t)15;
+    static constexpr size_t cval_off = (sum_off + W * sizeof(A) + 15) & ~(size_t)15;
+    static constexpr size_t crow_off = (cval_off + T * sizeof(A) + 15) & ~(size_t)15;
+    static constexpr size_t ccont_off = crow_off + T * 4;
+    static constexpr size_t bytes = (ccont_off + T + 15) & ~(size_t)15;
+};
+
+template <class Op, int T, int IPT, bool REDUCE>
+__global__ void __launch_bounds__(T) k_mp_rows(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+                                               uint32_t n, const uint2 *__restrict__ coord,
+                                               eg_mp_carry<typename Op::A> *__restrict__ carry,
+                                               double2 *__restrict__ part, Op op) {
+    using V = typename Op::V;
+    using A = typename Op::A;
+    using L = eg_mp_smem<T, IPT, V, A>;
+    constexpr int W = T * IPT;
+    extern __shared__ __align__(16) unsigned char smem[];
+    uint32_t *s_rowend = (uint32_t *)(smem + L::rowend_off);
+    V *s_val = (V *)(smem + L::val_off);
+    A *s_sum = (A *)(smem + L::sum_off);
+    A *s_cval = (A *)(smem + L::cval_off);
+    uint32_t *s_crow = (uint32_t *)(smem + L::crow_off);
+    unsigned char *s_ccont = smem + L::ccont_off;
+    __shared__ uint32_t s_head;
+    __shared__ A s_headval;
+    __shared__ double2 s_red[T / 32];
+
+    if (!op.active()) return;
+    op.setup();
+    const uint32_t tid = threadIdx.x;
+    const uint32_t c = blockIdx.x;
+    const uint2 c0 = coord[c], c1 = coord[c + 1];
+    const uint32_t i0 = c0.x, j0 = c0.y;
+    const uint32_t nrows = c1.x - i0, nedges = c1.y - j0;
+    const uint32_t rs0 = ptr[i0];  // ptr has n+1 entries; i0 <= n
+    if (tid == 0) s_head = EG_MP_NONE;
+
+    // stage row ends (relative to j0); the open row nrows gets its end too
+    for (uint32_t k = tid; k <= nrows; k += T) s_rowend[k] = (i0 + k < n) ? __ldg(ptr + i0 + k + 1) - j0 : 0xffffffffu;
+    // stage entry values: scalar head to a 16-byte boundary, uint4 body, tail
+    {
+        const uint32_t head = min((4u - (j0 & 3u)) & 3u, nedges);
+        if (tid < head) s_val[tid] = op.gather(j0 + tid, __ldg(col + j0 + tid));
+        const uint32_t nvec = (nedges - head) >> 2;
+        const uint4 *cv = reinterpret_cast<const uint4 *>(col + j0 + head);
+        for (uint32_t k = tid; k < nvec; k += T) {
+            uint4 q = __ldg(cv + k);
+            uint32_t b = head + 4 * k;
+            V a0 = op.gather(j0 + b, q.x), a1 = op.gather(j0 + b + 1, q.y);
+            V a2 = op.gather(j0 + b + 2, q.z), a3 = op.gather(j0 + b + 3, q.w);
+            s_val[b] = a0;
+            s_val[b + 1] = a1;
+            s_val[b + 2] = a2;
+            s_val[b + 3] = a3;
+        }
+        for (uint32_t k = head + 4 * nvec + tid; k < nedges; k += T) s_val[k] = op.gather(j0 + k, __ldg(col + j0 + k));
+    }
+    __syncthreads();
+
+    // merge-path search for this thread's first item
+    const uint32_t total = nrows + nedges;
+    const uint32_t d0 = min(tid * IPT, total), d1 = min(d0 + IPT, total);
+    uint32_t lo = d0 > nedges ? d0 - nedges : 0, hi = min(d0, nrows);
+    while (lo < hi) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (s_rowend[mid] <= d0 - mid - 1) lo = mid + 1;
+        else hi = mid;
+    }
+    uint32_t it = lo, jt = d0 - lo;
+    const uint32_t it_start = it;
+    // does this thread's first row begin before its first entry?
+    const bool start_cont = (it == 0) ? (rs0 < j0 + jt) : (s_rowend[it - 1] < jt);
+    A acc = op.zero();
+    A first_part = op.zero();
+    uint32_t first_row = EG_MP_NONE;
+#pragma unroll
+    for (int k = 0; k < IPT; k++) {
+        if (d0 + k < d1) {
+            if (s_rowend[it] <= jt) {
+                if (it == it_start && start_cont) {
+                    first_part = acc;
+                    first_row = it;
+                } else {
+                    s_sum[it] = acc;
+                }
+                acc = op.zero();
+                it++;
+            } else {
+                acc = op.add(acc, s_val[jt]);
+                jt++;
+            }
+        }
+    }
+    s_crow[tid] = it;
+    s_cval[tid] = acc;
+    s_ccont[tid] = (it == it_start) && start_cont;
+    __syncthreads();
+
+    // finish the first row of this thread if earlier threads hold parts of it
+    if (first_row != EG_MP_NONE) {
+        A tot = first_part;
+        int k = (int)tid - 1;
+        bool head = false;
+        for (;;) {
+            if (k < 0) {
+                head = true;
+                break;
+            }
+            tot = op.merge(s_cval[k], tot);
+            if (!s_ccont[k]) break;
+            k--;
+        }
+        if (head) {
+            s_head = first_row;  // always local row 0
+            s_headval = tot;
+        } else {
+            s_sum[first_row] = tot;
+        }
+    }
+    // the last thread collects the partial of the row left open at the CTA end
+    if (tid == T - 1) {
+        A tot = s_cval[T - 1];
+        int k = T - 1;
+        while (s_ccont[k] && k > 0) {
+            k--;
+            tot = op.merge(s_cval[k], tot);
+        }
+        carry[c].tail_row = i0 + nrows;
+        carry[c].tail_val = tot;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        carry[c].head_row = s_head == EG_MP_NONE ? EG_MP_NONE : i0;
+        if (s_head != EG_MP_NONE) carry[c].head_val = s_headval;
+    }
+    // write out completed rows in order
+    double2 red = make_double2(0.0, 0.0);
+    const uint32_t r0 = (s_head != EG_MP_NONE) ? 1u : 0u;
+    for (uint32_t r = r0 + tid; r < nrows; r += T) {
+        double2 x = op.emit(i0 + r, s_sum[r]);
+        if (REDUCE) {
+            red.x += x.x;
+            red.y += x.y;
+        }
+    }
+    if (REDUCE) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            red.x += __shfl_down_sync(EG_FULL_MASK, red.x, o);
+            red.y += __shfl_down_sync(EG_FULL_MASK, red.y, o);
+        }
+        if ((tid & 31) == 0) s_red[tid >> 5] = red;
+        __syncthreads();
+        if (tid == 0) {
+            double2 s = make_double2(0.0, 0.0);
+            for (int w = 0; w < T / 32; w++) {
+                s.x += s_red[w].x;
+                s.y += s_red[w].y;
+            }
+            part[c] = s;
+        }
+    }
+}
+
+// One thread per CTA: completes rows that span CTAs (CTA order, deterministic).
+template <class Op, bool REDUCE>
+__global__ void k_mp_fixup(const uint32_t *__restrict__ ptr, const uint2 *__restrict__ coord, uint32_t ntiles,
+                           const eg_mp_carry<typename Op::A> *__restrict__ carry, double2 *__restrict__ part, Op op) {
+    using A = typename Op::A;
+    __shared__ double2 s_red[8];
+    if (!op.active()) return;
+    op.setup();
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    double2 red = make_double2(0.0, 0.0);
+    if (c < ntiles) {
+        uint32_t row = carry[c].head_row;
+        if (row != EG_MP_NONE) {
+            A tot = carry[c].head_val;
+            const uint32_t rstart = ptr[row];
+            for (int k = (int)c - 1; k >= 0; k--) {
+                tot = op.merge(carry[k].tail_val, tot);
+                if (rstart >= coord[k].y) break;  // the row begins inside CTA k
+            }
+            red = op.emit(row, tot);
+        }
+    }
+    if (REDUCE) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            red.x += __shfl_down_sync(EG_FULL_MASK, red.x, o);
+            red.y += __shfl_down_sync(EG_FULL_MASK, red.y, o);
+        }
+        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = red;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double2 s = make_double2(0.0, 0.0);
+            for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+                s.x += s_red[w].x;
+                s.y += s_red[w].y;
+            }
+            part[blockIdx.x] = s;
+        }
+    }
+}
+
+// Compensated summation (Knuth's TwoSum) on fp32 pairs (sum, error).
+struct eg_f2sum {
+    __device__ __forceinline__ static float2 add(float2 a, float x) {
+        float s = __fadd_rn(a.x, x);
+        float bb = __fsub_rn(s, a.x);
+        float err = __fadd_rn(__fsub_rn(a.x, __fsub_rn(s, bb)), __fsub_rn(x, bb));
+        return make_float2(s, __fadd_rn(a.y, err));
+    }
+    __device__ __forceinline__ static float2 merge(float2 a, float2 b) {
+        float2 r = add(a, b.x);
+        r.y = __fadd_rn(r.y, b.y);
+        return r;
+    }
+};

@@ -1,0 +1,433 @@
+// Pull PageRank and SpMV as merge-path row reductions over the CSC (or CSR).
+//
+// Replaces pr_algo_pull and its iterator (pagerank_simple.c:72-84,110-133),
+// the grid PR loop (prgrid_cilk.c:62-76,111-141) whose per-destination sum
+// order equals the CSC order, and the SpMV loops (spmv.c:98-135).
+//
+// Per PageRank iteration the device runs three kernels:
+//   k_mp_rows<PrOp>   rank[v] = base + d * sum_{u in in(v)} contrib[u]
+//                     contrib'[v] = rank[v] / deg[v] (fused into the write)
+//   k_mp_fixup<PrOp>  rows that span CTAs
+//   k_pr_reduce       FP64 residual / dangling mass -> next base, stop flag
+// contrib[u] = prev[u] / (float)deg[u] is the reference's per-edge quotient
+// (pagerank_simple.c:78), computed once per vertex instead of once per edge.
+// Algorithmic bytes per iteration: 8 per entry (4 col + 4 gathered contrib)
+// and 16 per vertex (row end, degree, rank write, contrib write).
+#include <math.h>
+#include <stdlib.h>
+
+#include <type_traits>
+
+#include "eg_mp.cuh"
+
+#ifndef EG_MP_T
+#define EG_MP_T 256
+#endif
+#ifndef EG_MP_IPT
+#define EG_MP_IPT 8
+#endif
+
+// ============================================================== schedule
+__global__ void k_mp_schedule(const uint32_t *__restrict__ ptr, uint32_t n, uint32_t m, uint32_t items,
+                              uint32_t ntiles, uint2 *__restrict__ coord) {
+    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c > ntiles) return;
+    uint64_t total = (uint64_t)n + m;
+    uint64_t diag = (uint64_t)c * items;
+    if (diag > total) diag = total;
+    // merge-path search: first row index i such that ptr[i+1] > diag - i - 1
+    uint64_t lo = diag > m ? diag - m : 0, hi = diag < n ? diag : n;
+    while (lo < hi) {
+        uint64_t mid = (lo + hi) >> 1;
+        if ((uint64_t)ptr[mid + 1] <= diag - mid - 1) lo = mid + 1;
+        else hi = mid;
+    }
+    coord[c] = make_uint2((uint32_t)lo, (uint32_t)(diag - lo));
+}
+
+int eg_build_sched(eg_graph *g, eg_adj &adj, eg_mp_sched &s, uint32_t items) {
+    if (s.items == items && s.coord.p) return EG_OK;
+    eg_ctx *ctx = g->ctx;
+    uint64_t total = (uint64_t)g->n + g->m;
+    uint32_t ntiles = (uint32_t)((total + items - 1) / items);
+    if (ntiles == 0) ntiles = 1;
+    EG_TRY(eg_buf_ensure(ctx, s.coord, ((uint64_t)ntiles + 1) * sizeof(uint2)));
+    k_mp_schedule<<<eg_div_up(ntiles + 1, 256), 256, 0, ctx->stream>>>(bp<uint32_t>(adj.ptr), g->n, (uint32_t)g->m,
+                                                                      items, ntiles, bp<uint2>(s.coord));
+    EG_LAUNCHED(ctx);
+    s.items = items;
+    s.ntiles = ntiles;
+    return EG_OK;
+}
+
+// ============================================================== PR state
+struct eg_pr_dev {
+    float base;   // (1-d)/n (+ d * dangling / n)
+    int done;     // converged: remaining launches return at once
+    int iters;    // iterations that ran
+    int pad;
+    double residual;
+    double dangling;
+};
+
+template <bool COMP>
+struct PrOp {
+    using V = float;
+    using A = typename std::conditional<COMP, float2, float>::type;
+    const float *__restrict__ cin;
+    float *__restrict__ rank;
+    float *__restrict__ cout;
+    const uint32_t *__restrict__ deg;
+    const eg_pr_dev *st;
+    uint32_t mult;
+    float damping;
+    int residual;
+    float base;
+    __device__ __forceinline__ bool active() const { return st->done == 0; }
+    __device__ __forceinline__ void setup() { base = st->base; }
+    __device__ __forceinline__ V gather(uint32_t, uint32_t u) const { return __ldg(cin + u); }
+    __device__ __forceinline__ A zero() const {
+        if constexpr (COMP) return make_float2(0.f, 0.f);
+        else return 0.f;
+    }
+    __device__ __forceinline__ A add(A a, V x) const {
+        if constexpr (COMP) return eg_f2sum::add(a, x);
+        else return a + x;
+    }
+    __device__ __forceinline__ A merge(A a, A b) const {
+        if constexpr (COMP) return eg_f2sum::merge(a, b);
+        else return a + b;
+    }
+    __device__ __forceinline__ double2 emit(uint32_t v, A s) const {
+        float sum;
+        if constexpr (COMP) sum = s.x + s.y;
+        else sum = s;
+        float r = fmaf(damping, sum, base);
+        double res = 0.0;
+        if (residual) res = fabs((double)r - (double)rank[v]);
+        rank[v] = r;
+        uint32_t d = deg[v] * mult;
+        cout[v] = d ? __fdiv_rn(r, (float)d) : 0.f;
+        return make_double2(res, d ? 0.0 : (double)r);
+    }
+};
+
+// rank = prev_init, contrib = prev_init / deg; partial dangling mass
+__global__ void k_pr_init(uint32_t n, float prev_init, const uint32_t *__restrict__ deg, uint32_t mult,
+                          float *__restrict__ rank, float *__restrict__ contrib, double2 *__restrict__ part) {
+    __shared__ double s_red[8];
+    double dang = 0.0;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        uint32_t d = deg[v] * mult;
+        rank[v] = prev_init;
+        contrib[v] = d ? __fdiv_rn(prev_init, (float)d) : 0.f;
+        if (!d) dang += (double)prev_init;
+    }
+    for (int o = 16; o > 0; o >>= 1) dang += __shfl_down_sync(EG_FULL_MASK, dang, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = dang;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += s_red[w];
+        part[blockIdx.x] = make_double2(0.0, s);
+    }
+}
+
+// One block: deterministic FP64 sum of the partials, next base, stop test.
+__global__ void k_pr_reduce(const double2 *__restrict__ part, uint32_t nparts, eg_pr_dev *st, uint32_t n,
+                            float damping, int dangling, double tol, int count_iter) {
+    __shared__ double2 s[256];
+    if (st->done) return;
+    double2 acc = make_double2(0.0, 0.0);
+    for (uint32_t i = threadIdx.x; i < nparts; i += blockDim.x) {
+        acc.x += part[i].x;
+        acc.y += part[i].y;
+    }
+    s[threadIdx.x] = acc;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            s[threadIdx.x].x += s[threadIdx.x + w].x;
+            s[threadIdx.x].y += s[threadIdx.x + w].y;
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        double res = s[0].x, dang = s[0].y;
+        st->residual = res;
+        st->dangling = dang;
+        double b = (1.0 - (double)damping) / (double)n;
+        if (dangling) b += (double)damping * dang / (double)n;
+        st->base = (float)b;
+        if (count_iter) {
+            st->iters += 1;
+            if (tol > 0.0 && res < tol) st->done = 1;
+        }
+    }
+}
+
+template <class Op, bool REDUCE>
+static int mp_launch(eg_graph *g, eg_adj &adj, eg_mp_sched &s, eg_buf &carry_buf, double2 *part, const Op &op) {
+    eg_ctx *ctx = g->ctx;
+    using A = typename Op::A;
+    using L = eg_mp_smem<EG_MP_T, EG_MP_IPT, typename Op::V, A>;
+    auto kern = k_mp_rows<Op, EG_MP_T, EG_MP_IPT, REDUCE>;
+    static bool attr_set = false;
+    if (!attr_set) {
+        EG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::bytes));
+        attr_set = true;
+    }
+    EG_TRY(eg_buf_ensure(ctx, carry_buf, (uint64_t)s.ntiles * sizeof(eg_mp_carry<A>)));
+    kern<<<s.ntiles, EG_MP_T, L::bytes, ctx->stream>>>(bp<uint32_t>(adj.ptr), bp<uint32_t>(adj.col), g->n,
+                                                      bp<uint2>(s.coord), bp<eg_mp_carry<A>>(carry_buf), part, op);
+    EG_LAUNCHED(ctx);
+    uint32_t fb = eg_div_up(s.ntiles, 256);
+    k_mp_fixup<Op, REDUCE><<<fb, 256, 0, ctx->stream>>>(bp<uint32_t>(adj.ptr), bp<uint2>(s.coord), s.ntiles,
+                                                       bp<eg_mp_carry<A>>(carry_buf), part ? part + s.ntiles : nullptr,
+                                                       op);
+    EG_LAUNCHED(ctx);
+    return EG_OK;
+}
+
+extern "C" void eg_pr_opts_default(eg_pr_opts *o) {
+    if (!o) return;
+    o->iterations = 10;
+    o->damping = 0.85f;
+    o->prev_init = -1.0f;
+    o->swap = 1;
+    o->deg_multiplier = 1;
+    o->dangling = 0;
+    o->compensated = 0;
+    o->tolerance = 0.0;
+    o->use_graph = 0;
+}
+
+template <bool COMP, bool REDUCE>
+static int pr_iterations(eg_graph *g, const eg_pr_opts &o, eg_pr_dev *st, double2 *part, eg_buf &carry) {
+    eg_ctx *ctx = g->ctx;
+    uint32_t nparts = g->sched_csc.ntiles + eg_div_up(g->sched_csc.ntiles, 256);
+    for (int it = 0; it < o.iterations; it++) {
+        PrOp<COMP> op;
+        bool odd = o.swap && (it & 1);
+        op.cin = odd ? bp<float>(g->contrib1) : bp<float>(g->contrib0);
+        op.cout = odd ? bp<float>(g->contrib0) : bp<float>(g->contrib1);
+        op.rank = bp<float>(g->rank);
+        op.deg = bp<uint32_t>(g->out_deg);
+        op.st = st;
+        op.mult = o.deg_multiplier;
+        op.damping = o.damping;
+        op.residual = o.tolerance > 0.0;
+        op.base = 0.f;
+        EG_TRY((mp_launch<PrOp<COMP>, REDUCE>(g, g->csc, g->sched_csc, carry, part, op)));
+        k_pr_reduce<<<1, 256, 0, ctx->stream>>>(part, REDUCE ? nparts : 0, st, g->n, o.damping, o.dangling,
+                                                o.tolerance, 1);
+        EG_LAUNCHED(ctx);
+    }
+    return EG_OK;
+}
+
+extern "C" int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out, eg_pr_stats *stats) {
+    if (!g) return eg_fail(EG_EINVAL, "NULL graph");
+    eg_pr_opts o;
+    if (opts) o = *opts;
+    else eg_pr_opts_default(&o);
+    if (o.iterations < 0 || o.deg_multiplier == 0) return eg_fail(EG_EINVAL, "bad PageRank options");
+    if (!(g->built & EG_LAYOUT_CSC) || !(g->built & EG_LAYOUT_CSR))
+        return eg_fail(EG_ENOTBUILT, "PageRank needs the CSC (in-lists) and CSR (out-degrees)");
+    eg_ctx *ctx = g->ctx;
+    EG_CUDA(cudaSetDevice(ctx->device));
+    const uint32_t n = g->n;
+    EG_TRY(eg_build_sched(g, g->csc, g->sched_csc, EG_MP_T * EG_MP_IPT));
+    const uint32_t ntiles = g->sched_csc.ntiles;
+    const uint32_t nparts = ntiles + eg_div_up(ntiles, 256);
+    EG_TRY(eg_buf_ensure(ctx, g->rank, (uint64_t)n * 4));
+    EG_TRY(eg_buf_ensure(ctx, g->contrib0, (uint64_t)n * 4));
+    EG_TRY(eg_buf_ensure(ctx, g->contrib1, (uint64_t)n * 4));
+    EG_TRY(eg_buf_ensure(ctx, g->pr_part, ((uint64_t)nparts + 1024) * sizeof(double2)));
+    EG_TRY(eg_buf_ensure(ctx, g->pr_stats, sizeof(eg_pr_dev)));
+    eg_buf &carry = g->mp_carry;
+    eg_pr_dev *st = bp<eg_pr_dev>(g->pr_stats);
+    double2 *part = bp<double2>(g->pr_part);
+    EG_CUDA(cudaMemsetAsync(st, 0, sizeof(eg_pr_dev), ctx->stream));
+    EG_CUDA(cudaMemsetAsync(part, 0, ((uint64_t)nparts + 1024) * sizeof(double2), ctx->stream));
+    float prev_init = o.prev_init < 0.f ? 1.0f / (float)n : o.prev_init;
+    const bool reduce = o.tolerance > 0.0 || o.dangling;
+    uint32_t ib = eg_div_up(n, 256);
+    if (ib > 1024) ib = 1024;
+    k_pr_init<<<ib, 256, 0, ctx->stream>>>(n, prev_init, bp<uint32_t>(g->out_deg), o.deg_multiplier, bp<float>(g->rank),
+                                          bp<float>(g->contrib0), part);
+    EG_LAUNCHED(ctx);
+    k_pr_reduce<<<1, 256, 0, ctx->stream>>>(part, ib, st, n, o.damping, o.dangling, 0.0, 0);
+    EG_LAUNCHED(ctx);
+    EG_CUDA(cudaMemsetAsync(part, 0, ((uint64_t)nparts + 1024) * sizeof(double2), ctx->stream));
+    EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    if (o.compensated) {
+        if (reduce) EG_TRY((pr_iterations<true, true>(g, o, st, part, carry)));
+        else EG_TRY((pr_iterations<true, false>(g, o, st, part, carry)));
+    } else {
+        if (reduce) EG_TRY((pr_iterations<false, true>(g, o, st, part, carry)));
+        else EG_TRY((pr_iterations<false, false>(g, o, st, part, carry)));
+    }
+    EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    eg_pr_dev hst;
+    EG_CUDA(cudaMemcpyAsync(&hst, st, sizeof(hst), cudaMemcpyDeviceToHost, ctx->stream));
+    if (rank_out) EG_CUDA(cudaMemcpyAsync(rank_out, g->rank.p, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (stats) {
+        stats->iterations_run = hst.iters;
+        stats->residual = hst.residual;
+        stats->dangling_mass = hst.dangling;
+        EG_CUDA(cudaEventElapsedTime(&stats->ms, ctx->ev0, ctx->ev1));
+    }
+    return EG_OK;
+}
+
+// ============================================================== SpMV
+template <int MODE>  // 0: x/1000 (reference 0.001 scale), 1: x
+struct SpmvU32Op {
+    using V = uint32_t;
+    using A = uint32_t;
+    const uint32_t *__restrict__ x;
+    uint32_t *__restrict__ y;
+    __device__ __forceinline__ bool active() const { return true; }
+    __device__ __forceinline__ void setup() {}
+    __device__ __forceinline__ V gather(uint32_t, uint32_t u) const {
+        uint32_t xv = __ldg(x + u);
+        return MODE == 0 ? xv / 1000u : xv;
+    }
+    __device__ __forceinline__ A zero() const { return 0u; }
+    __device__ __forceinline__ A add(A a, V v) const { return a + v; }
+    __device__ __forceinline__ A merge(A a, A b) const { return a + b; }
+    __device__ __forceinline__ double2 emit(uint32_t v, A s) const {
+        y[v] = s;
+        return make_double2(0.0, 0.0);
+    }
+};
+
+template <bool COMP>
+struct SpmvF32Op {
+    using V = float;
+    using A = typename std::conditional<COMP, float2, float>::type;
+    const float *__restrict__ x;
+    const float *__restrict__ vals;
+    float *__restrict__ y;
+    __device__ __forceinline__ bool active() const { return true; }
+    __device__ __forceinline__ void setup() {}
+    __device__ __forceinline__ V gather(uint32_t j, uint32_t u) const { return __fmul_rn(__ldg(vals + j), __ldg(x + u)); }
+    __device__ __forceinline__ A zero() const {
+        if constexpr (COMP) return make_float2(0.f, 0.f);
+        else return 0.f;
+    }
+    __device__ __forceinline__ A add(A a, V v) const {
+        if constexpr (COMP) return eg_f2sum::add(a, v);
+        else return a + v;
+    }
+    __device__ __forceinline__ A merge(A a, A b) const {
+        if constexpr (COMP) return eg_f2sum::merge(a, b);
+        else return a + b;
+    }
+    __device__ __forceinline__ double2 emit(uint32_t v, A s) const {
+        if constexpr (COMP) y[v] = s.x + s.y;
+        else y[v] = s;
+        return make_double2(0.0, 0.0);
+    }
+};
+
+struct SpmvF64Op {
+    using V = double;
+    using A = double;
+    const float *__restrict__ x;
+    const float *__restrict__ vals;
+    double *__restrict__ y;
+    __device__ __forceinline__ bool active() const { return true; }
+    __device__ __forceinline__ void setup() {}
+    __device__ __forceinline__ V gather(uint32_t j, uint32_t u) const {
+        return __dmul_rn((double)__ldg(vals + j), (double)__ldg(x + u));
+    }
+    __device__ __forceinline__ A zero() const { return 0.0; }
+    __device__ __forceinline__ A add(A a, V v) const { return __dadd_rn(a, v); }
+    __device__ __forceinline__ A merge(A a, A b) const { return __dadd_rn(a, b); }
+    __device__ __forceinline__ double2 emit(uint32_t v, A s) const {
+        y[v] = s;
+        return make_double2(0.0, 0.0);
+    }
+};
+
+// Edge value of CSC entry p (row v, column u): U[0,1) hashed from the
+// unordered endpoint pair, or 1.
+__global__ void k_csc_values(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col, uint32_t n,
+                             uint64_t seed, int unit, float *__restrict__ vals) {
+    uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    uint32_t lane = threadIdx.x & 31;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps)
+        for (uint32_t p = ptr[v] + lane; p < ptr[v + 1]; p += 32) {
+            if (unit) vals[p] = 1.0f;
+            else vals[p] = (float)(eg_edge_hash(seed, col[p], v) >> 40) * (1.0f / 16777216.0f);
+        }
+}
+
+extern "C" int eg_spmv(eg_graph *g, const eg_spmv_opts *opts, const void *x, void *y, float *ms) {
+    if (!g || !opts || !x) return eg_fail(EG_EINVAL, "NULL argument");
+    const int kind = opts->kind;
+    if (kind < EG_SPMV_U32_PULL || kind > EG_SPMV_F64) return eg_fail(EG_EINVAL, "unknown SpMV kind %d", kind);
+    const bool pull = kind == EG_SPMV_U32_PULL || kind >= EG_SPMV_F32;
+    const unsigned need = pull ? EG_LAYOUT_CSC : EG_LAYOUT_CSR;
+    if (!(g->built & need)) return eg_fail(EG_ENOTBUILT, "SpMV kind %d needs layout %u", kind, need);
+    eg_ctx *ctx = g->ctx;
+    EG_CUDA(cudaSetDevice(ctx->device));
+    const uint32_t n = g->n;
+    eg_adj &adj = pull ? g->csc : g->csr;
+    eg_mp_sched &s = pull ? g->sched_csc : g->sched_csr;
+    EG_TRY(eg_build_sched(g, adj, s, EG_MP_T * EG_MP_IPT));
+    const size_t ysz = kind == EG_SPMV_F64 ? 8 : 4;
+    EG_TRY(eg_buf_ensure(ctx, g->spmv_x, (uint64_t)n * 4));
+    EG_TRY(eg_buf_ensure(ctx, g->spmv_y, (uint64_t)n * ysz));
+    EG_CUDA(cudaMemcpyAsync(g->spmv_x.p, x, (uint64_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    if (kind >= EG_SPMV_F32) {
+        int vk = opts->unit_values ? 1 : 2;
+        if (!g->spmv_vals.p || g->spmv_vals_kind != vk || (vk == 2 && g->spmv_vals_seed != opts->value_seed)) {
+            EG_TRY(eg_buf_ensure(ctx, g->spmv_vals, g->m * 4 + 16));
+            k_csc_values<<<eg_div_up((uint64_t)n * 32, 256) > 65535 ? 65535 : eg_div_up((uint64_t)n * 32, 256), 256, 0,
+                           ctx->stream>>>(bp<uint32_t>(g->csc.ptr), bp<uint32_t>(g->csc.col), n, opts->value_seed,
+                                          opts->unit_values, bp<float>(g->spmv_vals));
+            EG_LAUNCHED(ctx);
+            g->spmv_vals_kind = vk;
+            g->spmv_vals_seed = opts->value_seed;
+        }
+    }
+    eg_buf &carry = g->mp_carry;
+    EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    switch (kind) {
+        case EG_SPMV_U32_PULL:
+        case EG_SPMV_U32_PUSH: {
+            SpmvU32Op<0> op{bp<uint32_t>(g->spmv_x), bp<uint32_t>(g->spmv_y)};
+            EG_TRY((mp_launch<SpmvU32Op<0>, false>(g, adj, s, carry, nullptr, op)));
+            break;
+        }
+        case EG_SPMV_U32_EDGE: {
+            SpmvU32Op<1> op{bp<uint32_t>(g->spmv_x), bp<uint32_t>(g->spmv_y)};
+            EG_TRY((mp_launch<SpmvU32Op<1>, false>(g, adj, s, carry, nullptr, op)));
+            break;
+        }
+        case EG_SPMV_F32: {
+            SpmvF32Op<false> op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<float>(g->spmv_y)};
+            EG_TRY((mp_launch<SpmvF32Op<false>, false>(g, adj, s, carry, nullptr, op)));
+            break;
+        }
+        case EG_SPMV_F32_COMP: {
+            SpmvF32Op<true> op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<float>(g->spmv_y)};
+            EG_TRY((mp_launch<SpmvF32Op<true>, false>(g, adj, s, carry, nullptr, op)));
+            break;
+        }
+        case EG_SPMV_F64: {
+            SpmvF64Op op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<double>(g->spmv_y)};
+            EG_TRY((mp_launch<SpmvF64Op, false>(g, adj, s, carry, nullptr, op)));
+            break;
+        }
+    }
+    EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (y) EG_CUDA(cudaMemcpyAsync(y, g->spmv_y.p, (uint64_t)n * ysz, cudaMemcpyDeviceToHost, ctx->stream));
+    EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (ms) EG_CUDA(cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
+    return EG_OK;
+}

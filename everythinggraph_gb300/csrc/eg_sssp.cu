@@ -1,0 +1,368 @@
+// Single- and multi-source SSSP: frontier Bellman-Ford with atomicMin.
+//
+// Replaces sssp_pushpull.c: the push relax (sssp_algo, 39-56, which the
+// reference runs with unit weights) and the weighted pull relax
+// (sssp_algo_pull, 69-98) iterated to a fixed point (iterator, 127-190).  The
+// fixed point is the exact shortest-path distance, which is what both this
+// code and the reference's pull-only run (-a 1 -r) produce.  dist[root] = 0,
+// unreached = UINT32_MAX-1 (sssp_pushpull.c:8).
+//
+// Weights are computed from the edge's endpoints, like the reference's
+// CREATE_WEIGHT path (init_all.c:661-686): no weight array is stored or read.
+#include <stdlib.h>
+
+#include "eg_internal.cuh"
+
+#define EG_SSSP_INF 0xfffffffeu
+
+namespace {
+
+struct WRule {
+    int rule;
+    uint64_t seed;
+    uint32_t lo;
+    uint64_t span;
+    __device__ __forceinline__ uint32_t operator()(uint32_t u, uint32_t v) const {
+        if (rule == EG_W_REF) return (u % 10u) + (v % 10u);
+        if (rule == EG_W_UNIT) return 1u;
+        return lo + (uint32_t)(((eg_edge_hash(seed, u, v) >> 32) * span) >> 32);
+    }
+};
+
+struct SsspCounters {
+    unsigned long long relax;  // entries scanned
+    uint32_t qsize;
+    uint32_t pad;
+};
+
+__global__ void k_sssp_init(uint32_t n, uint32_t *dist, uint32_t root, uint32_t *queue, SsspCounters *cnt) {
+    uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) dist[v] = v == root ? 0u : EG_SSSP_INF;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        queue[0] = root;
+        cnt->qsize = 1;
+        cnt->relax = 0;
+    }
+}
+
+// One warp per frontier vertex; lanes relax its out-edges.  A vertex whose
+// distance drops is queued once per round (claimed through the next bitmap).
+__global__ void __launch_bounds__(256) k_sssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+                                                   const uint32_t *__restrict__ queue, uint32_t qlen, uint32_t *dist,
+                                                   uint32_t *next_bm, uint32_t *next_queue, WRule w,
+                                                   SsspCounters *cnt) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    const uint32_t lt = eg_lanemask_lt();
+    unsigned long long scanned = 0;
+    for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < qlen; qi += warps) {
+        const uint32_t u = queue[qi];
+        const uint32_t du = __ldcg(dist + u);
+        const uint32_t b = ptr[u], e = ptr[u + 1];
+        scanned += e - b;
+        for (uint32_t p0 = b; p0 < e; p0 += 32) {
+            const uint32_t p = p0 + lane;
+            bool q = false;
+            uint32_t v = 0;
+            if (p < e) {
+                v = col[p];
+                if (v != u) {  // self-loops skipped (sssp_pushpull.c:80)
+                    const uint64_t nd64 = (uint64_t)du + w(u, v);
+                    const uint32_t nd = nd64 < EG_SSSP_INF ? (uint32_t)nd64 : EG_SSSP_INF;
+                    if (nd < __ldcg(dist + v)) {
+                        const uint32_t old = atomicMin(dist + v, nd);
+                        if (nd < old) {
+                            const uint32_t bit = 1u << (v & 31);
+                            q = !(atomicOr(next_bm + (v >> 5), bit) & bit);
+                        }
+                    }
+                }
+            }
+            const uint32_t ball = __ballot_sync(EG_FULL_MASK, q);
+            if (ball) {
+                uint32_t base = 0;
+                if (lane == 0) base = atomicAdd(&cnt->qsize, __popc(ball));
+                base = __shfl_sync(EG_FULL_MASK, base, 0);
+                if (q) next_queue[base + __popc(ball & lt)] = v;
+            }
+        }
+    }
+    if (lane == 0 && scanned) atomicAdd(&cnt->relax, scanned);
+}
+
+// Clears the bitmap bits of the vertices in a queue.
+__global__ void k_clear_bits(const uint32_t *__restrict__ queue, uint32_t qlen, uint32_t *bm) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < qlen; i += gridDim.x * blockDim.x) {
+        uint32_t v = queue[i];
+        atomicAnd(bm + (v >> 5), ~(1u << (v & 31)));
+    }
+}
+
+__global__ void k_count_reached(const uint32_t *__restrict__ dist, uint64_t len, unsigned long long *out) {
+    unsigned long long c = 0;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < len; i += (uint64_t)gridDim.x * blockDim.x)
+        c += dist[i] != EG_SSSP_INF;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(EG_FULL_MASK, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
+}
+
+WRule make_rule(const eg_weights *w) {
+    WRule r;
+    r.rule = w ? w->rule : EG_W_REF;
+    r.seed = w ? w->seed : 0;
+    r.lo = w ? w->lo : 0;
+    r.span = w ? (uint64_t)w->hi - w->lo + 1 : 1;
+    return r;
+}
+
+uint32_t blocks_for(eg_ctx *ctx, uint64_t threads) {
+    uint64_t b = (threads + 255) / 256;
+    uint64_t cap = (uint64_t)ctx->sm_count * 8;
+    if (b > cap) b = cap;
+    return b ? (uint32_t)b : 1u;
+}
+
+int check_weights(const eg_weights *w) {
+    if (!w) return EG_OK;
+    if (w->rule != EG_W_REF && w->rule != EG_W_HASH && w->rule != EG_W_UNIT)
+        return eg_fail(EG_EINVAL, "unknown weight rule %d", w->rule);
+    if (w->rule == EG_W_HASH && w->hi < w->lo) return eg_fail(EG_EINVAL, "weight range hi < lo");
+    return EG_OK;
+}
+
+}  // namespace
+
+extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wts, uint32_t *dist_out, eg_sssp_stats *stats) {
+    if (!g) return eg_fail(EG_EINVAL, "NULL graph");
+    if (root >= g->n) return eg_fail(EG_EINVAL, "root %u >= n %u", root, g->n);
+    if (!(g->built & EG_LAYOUT_CSR)) return eg_fail(EG_ENOTBUILT, "SSSP needs the CSR");
+    EG_TRY(check_weights(wts));
+    eg_ctx *ctx = g->ctx;
+    EG_CUDA(cudaSetDevice(ctx->device));
+    const uint32_t n = g->n, nw = (n + 31) >> 5;
+    const WRule w = make_rule(wts);
+    EG_TRY(eg_buf_ensure(ctx, g->dist, (uint64_t)n * 4));
+    const uint64_t off_q0 = nw, off_q1 = off_q0 + n, off_cnt = (off_q1 + n + 7) & ~7ull;
+    EG_TRY(eg_buf_ensure(ctx, g->sssp_work, (off_cnt + 8) * 4));
+    uint32_t *wk = bp<uint32_t>(g->sssp_work);
+    uint32_t *bm = wk, *q[2] = {wk + off_q0, wk + off_q1};
+    SsspCounters *cnt = reinterpret_cast<SsspCounters *>(wk + off_cnt);
+    SsspCounters *h = (SsspCounters *)ctx->h_pinned;
+    uint32_t *dist = bp<uint32_t>(g->dist);
+    EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    EG_CUDA(cudaMemsetAsync(bm, 0, (uint64_t)nw * 4, ctx->stream));
+    k_sssp_init<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(n, dist, root, q[0], cnt);
+    EG_LAUNCHED(ctx);
+    uint32_t qlen = 1;
+    int cur = 0, rounds = 0;
+    unsigned long long relax = 0;
+    while (qlen > 0) {
+        const int nxt = cur ^ 1;
+        EG_CUDA(cudaMemsetAsync(&cnt->qsize, 0, 4, ctx->stream));
+        k_sssp_push<<<blocks_for(ctx, (uint64_t)qlen * 32), 256, 0, ctx->stream>>>(
+            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), q[cur], qlen, dist, bm, q[nxt], w, cnt);
+        EG_LAUNCHED(ctx);
+        EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(SsspCounters), cudaMemcpyDeviceToHost, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        qlen = h->qsize;
+        relax = h->relax;
+        // the new queue's bits must be clear before it produces the next one
+        if (qlen) {
+            k_clear_bits<<<blocks_for(ctx, qlen), 256, 0, ctx->stream>>>(q[nxt], qlen, bm);
+            EG_LAUNCHED(ctx);
+        }
+        cur = nxt;
+        rounds++;
+        if (rounds > (int)(4 * (uint64_t)n + 16)) return eg_fail(EG_ETIMEOUT, "SSSP did not converge");
+    }
+    EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (dist_out) EG_CUDA(cudaMemcpyAsync(dist_out, dist, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    unsigned long long *dcount = reinterpret_cast<unsigned long long *>(cnt) + 2;
+    if (stats) {
+        EG_CUDA(cudaMemsetAsync(dcount, 0, 8, ctx->stream));
+        k_count_reached<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(dist, n, dcount);
+        EG_LAUNCHED(ctx);
+        EG_CUDA(cudaMemcpyAsync(h, dcount, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (stats) {
+        stats->reached = (uint32_t) * (unsigned long long *)h;
+        stats->rounds = rounds;
+        stats->relaxations = relax;
+        EG_CUDA(cudaEventElapsedTime(&stats->ms, ctx->ev0, ctx->ev1));
+    }
+    return EG_OK;
+}
+
+// ============================================================== multi-source
+// dist is vertex-major: dist[v*k + s].  The frontier is a bit per
+// (vertex, source): act[v*KW + j] holds sources 32j..32j+31.  One warp takes
+// one (frontier vertex, source word) and walks the vertex's out-list; its 32
+// lanes relax 32 sources of the same edge (coalesced 128-byte rows).
+namespace {
+__global__ void k_msssp_init(uint32_t n, int k, uint32_t kw, uint32_t *dist, uint32_t *act0, uint32_t *act1) {
+    uint64_t total = (uint64_t)n * k;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x)
+        dist[i] = EG_SSSP_INF;
+    uint64_t tw = (uint64_t)n * kw;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < tw; i += (uint64_t)gridDim.x * blockDim.x) {
+        act0[i] = 0;
+        act1[i] = 0;
+    }
+}
+
+__global__ void k_msssp_roots(const uint32_t *roots, int k, uint32_t kw, uint32_t *dist, uint32_t *act,
+                              uint32_t *inq, uint32_t *queue, SsspCounters *cnt) {
+    for (int s = threadIdx.x; s < k; s += blockDim.x) {
+        uint32_t r = roots[s];
+        dist[(uint64_t)r * k + s] = 0;
+        atomicOr(act + (uint64_t)r * kw + (s >> 5), 1u << (s & 31));
+        uint32_t bit = 1u << (r & 31);
+        if (!(atomicOr(inq + (r >> 5), bit) & bit)) queue[atomicAdd(&cnt->qsize, 1u)] = r;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_msssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+                                                    const uint32_t *__restrict__ queue, uint32_t qlen, int k,
+                                                    uint32_t kw, uint32_t *dist, const uint32_t *__restrict__ act,
+                                                    uint32_t *next_act, uint32_t *next_inq, uint32_t *next_queue,
+                                                    WRule w, SsspCounters *cnt) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warps = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long scanned = 0;
+    const uint64_t items = (uint64_t)qlen * kw;
+    for (uint64_t it = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; it < items; it += warps) {
+        const uint32_t u = queue[it / kw];
+        const uint32_t j = (uint32_t)(it % kw);
+        const uint32_t a = act[(uint64_t)u * kw + j];
+        if (!a) continue;
+        const uint32_t s = j * 32 + lane;
+        const bool on = (a >> lane) & 1u;
+        const uint32_t du = on ? __ldcg(dist + (uint64_t)u * k + s) : EG_SSSP_INF;
+        const uint32_t b = ptr[u], e = ptr[u + 1];
+        if (lane == 0) scanned += (e - b) * (unsigned long long)__popc(a);
+        for (uint32_t p = b; p < e; p++) {
+            const uint32_t v = col[p];
+            if (v == u) continue;
+            bool improved = false;
+            if (on) {
+                const uint64_t nd64 = (uint64_t)du + w(u, v);
+                const uint32_t nd = nd64 < EG_SSSP_INF ? (uint32_t)nd64 : EG_SSSP_INF;
+                uint32_t *dp = dist + (uint64_t)v * k + s;
+                if (nd < __ldcg(dp)) improved = nd < atomicMin(dp, nd);
+            }
+            const uint32_t ball = __ballot_sync(EG_FULL_MASK, improved);
+            if (ball && lane == 0) {
+                atomicOr(next_act + (uint64_t)v * kw + j, ball);
+                const uint32_t bit = 1u << (v & 31);
+                if (!(atomicOr(next_inq + (v >> 5), bit) & bit)) next_queue[atomicAdd(&cnt->qsize, 1u)] = v;
+            }
+        }
+    }
+    if (lane == 0 && scanned) atomicAdd(&cnt->relax, scanned);
+}
+
+// Clears the frontier words and queued bits of the vertices in a queue.
+__global__ void k_msssp_clear(const uint32_t *__restrict__ queue, uint32_t qlen, uint32_t kw, uint32_t *act,
+                              uint32_t *inq) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < (uint64_t)qlen * kw;
+         i += (uint64_t)gridDim.x * blockDim.x) {
+        uint32_t v = queue[i / kw];
+        act[(uint64_t)v * kw + i % kw] = 0;
+        if (i % kw == 0) atomicAnd(inq + (v >> 5), ~(1u << (v & 31)));
+    }
+}
+
+__global__ void k_transpose_dist(const uint32_t *__restrict__ dvk, uint32_t n, int k, uint32_t *__restrict__ dkv) {
+    __shared__ uint32_t t[32][33];
+    uint32_t v0 = blockIdx.x * 32, s0 = blockIdx.y * 32;
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        uint32_t v = v0 + r, s = s0 + threadIdx.x;
+        t[r][threadIdx.x] = (v < n && s < (uint32_t)k) ? dvk[(uint64_t)v * k + s] : 0u;
+    }
+    __syncthreads();
+    for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+        uint32_t s = s0 + r, v = v0 + threadIdx.x;
+        if (v < n && s < (uint32_t)k) dkv[(uint64_t)s * n + v] = t[threadIdx.x][r];
+    }
+}
+}  // namespace
+
+extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg_weights *wts, uint32_t *dist_out,
+                             eg_sssp_stats *stats) {
+    if (!g || !roots) return eg_fail(EG_EINVAL, "NULL argument");
+    if (k < 1 || k > 1024) return eg_fail(EG_EINVAL, "k=%d: batched SSSP takes 1..1024 sources", k);
+    if (!(g->built & EG_LAYOUT_CSR)) return eg_fail(EG_ENOTBUILT, "SSSP needs the CSR");
+    EG_TRY(check_weights(wts));
+    for (int s = 0; s < k; s++)
+        if (roots[s] >= g->n) return eg_fail(EG_EINVAL, "root %u >= n", roots[s]);
+    eg_ctx *ctx = g->ctx;
+    EG_CUDA(cudaSetDevice(ctx->device));
+    const uint32_t n = g->n, nw = (n + 31) >> 5, kw = (uint32_t)((k + 31) / 32);
+    const WRule w = make_rule(wts);
+    // work: dist[n*k] | act0, act1 [n*kw] | inq0, inq1 [nw] | q0, q1 [n] | roots | counters
+    const uint64_t off_act0 = (uint64_t)n * k, off_act1 = off_act0 + (uint64_t)n * kw, off_inq0 = off_act1 + (uint64_t)n * kw,
+                   off_inq1 = off_inq0 + nw, off_q0 = off_inq1 + nw, off_q1 = off_q0 + n, off_roots = off_q1 + n,
+                   off_cnt = (off_roots + 1024 + 7) & ~7ull;
+    EG_TRY(eg_buf_ensure(ctx, g->sssp_work, (off_cnt + 8) * 4));
+    uint32_t *wk = bp<uint32_t>(g->sssp_work);
+    uint32_t *dist = wk, *act[2] = {wk + off_act0, wk + off_act1}, *inq[2] = {wk + off_inq0, wk + off_inq1},
+             *q[2] = {wk + off_q0, wk + off_q1}, *d_roots = wk + off_roots;
+    SsspCounters *cnt = reinterpret_cast<SsspCounters *>(wk + off_cnt);
+    SsspCounters *h = (SsspCounters *)ctx->h_pinned;
+    EG_CUDA(cudaMemcpyAsync(d_roots, roots, (uint64_t)k * 4, cudaMemcpyHostToDevice, ctx->stream));
+    EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    k_msssp_init<<<blocks_for(ctx, (uint64_t)n * k), 256, 0, ctx->stream>>>(n, k, kw, dist, act[0], act[1]);
+    EG_LAUNCHED(ctx);
+    EG_CUDA(cudaMemsetAsync(inq[0], 0, 2ull * nw * 4, ctx->stream));
+    EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(SsspCounters), ctx->stream));
+    k_msssp_roots<<<1, 256, 0, ctx->stream>>>(d_roots, k, kw, dist, act[0], inq[0], q[0], cnt);
+    EG_LAUNCHED(ctx);
+    EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(SsspCounters), cudaMemcpyDeviceToHost, ctx->stream));
+    EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    uint32_t qlen = h->qsize;
+    int cur = 0, rounds = 0;
+    unsigned long long relax = 0;
+    while (qlen > 0) {
+        const int nxt = cur ^ 1;
+        EG_CUDA(cudaMemsetAsync(&cnt->qsize, 0, 4, ctx->stream));
+        k_msssp_push<<<blocks_for(ctx, (uint64_t)qlen * kw * 32), 256, 0, ctx->stream>>>(
+            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), q[cur], qlen, k, kw, dist, act[cur], act[nxt], inq[nxt],
+            q[nxt], w, cnt);
+        EG_LAUNCHED(ctx);
+        // the current frontier's words and bits are cleared for reuse as "next"
+        k_msssp_clear<<<blocks_for(ctx, (uint64_t)qlen * kw), 256, 0, ctx->stream>>>(q[cur], qlen, kw, act[cur], inq[cur]);
+        EG_LAUNCHED(ctx);
+        EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(SsspCounters), cudaMemcpyDeviceToHost, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        qlen = h->qsize;
+        relax = h->relax;
+        cur = nxt;
+        rounds++;
+        if (rounds > (int)(4 * (uint64_t)n + 16)) return eg_fail(EG_ETIMEOUT, "batched SSSP did not converge");
+    }
+    EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (dist_out) {
+        EG_TRY(eg_buf_ensure(ctx, g->dist, (uint64_t)n * k * 4));
+        dim3 grid(eg_div_up(n, 32), eg_div_up((uint64_t)k, 32)), block(32, 8);
+        k_transpose_dist<<<grid, block, 0, ctx->stream>>>(dist, n, k, bp<uint32_t>(g->dist));
+        EG_LAUNCHED(ctx);
+        EG_CUDA(cudaMemcpyAsync(dist_out, g->dist.p, (uint64_t)n * k * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (stats) {
+        unsigned long long *dcount = reinterpret_cast<unsigned long long *>(cnt) + 2;
+        EG_CUDA(cudaMemsetAsync(dcount, 0, 8, ctx->stream));
+        k_count_reached<<<blocks_for(ctx, (uint64_t)n * k), 256, 0, ctx->stream>>>(dist, (uint64_t)n * k, dcount);
+        EG_LAUNCHED(ctx);
+        EG_CUDA(cudaMemcpyAsync(h, dcount, 8, cudaMemcpyDeviceToHost, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        unsigned long long rc = *(unsigned long long *)h;
+        stats->reached = (uint32_t)(rc > 0xffffffffull ? 0xffffffffull : rc);
+        stats->rounds = rounds;
+        stats->relaxations = relax;
+        EG_CUDA(cudaEventElapsedTime(&stats->ms, ctx->ev0, ctx->ev1));
+    }
+    return EG_OK;
+}

@@ -1,0 +1,113 @@
+// Weakly connected components with min-id labels.
+//
+// Replaces wcc.c: min-label propagation over adjacency lists (wcc_algo,
+// 30-42, with its pthread worklist 44-90) and over the grid and edge array
+// (193-261), whose fixed point labels every vertex with the minimum vertex id
+// of its component.
+//
+// GPU form: label propagation on component roots with pointer jumping.  Every
+// input edge hooks the larger of its two roots under the smaller one
+// (atomicCAS on the root's parent word), so a root is always the minimum id
+// of its tree; finds use path halving (pointer jumping), and a final pass
+// jumps every vertex to its root.  The result equals the reference's fixed
+// point bit for bit, independent of scheduling.
+#include "eg_internal.cuh"
+
+namespace {
+
+__device__ __forceinline__ uint32_t uf_find(uint32_t *par, uint32_t x) {
+    uint32_t p = __ldcg(par + x);
+    while (p != x) {
+        const uint32_t gp = __ldcg(par + p);
+        if (gp != p) par[x] = gp;  // halve the path; parents only ever decrease
+        x = p;
+        p = gp;
+    }
+    return x;
+}
+
+__global__ void k_wcc_init(uint32_t n, uint32_t *par) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) par[v] = v;
+}
+
+__global__ void k_wcc_hook(const uint32_t *__restrict__ pairs, uint64_t m, uint32_t *par, uint32_t *retries) {
+    uint32_t tries = 0;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint2 p = reinterpret_cast<const uint2 *>(pairs)[e];
+        uint32_t a = uf_find(par, p.x), b = uf_find(par, p.y);
+        while (a != b) {
+            if (a > b) {
+                uint32_t t = a;
+                a = b;
+                b = t;
+            }
+            // link root b (larger) under root a (smaller)
+            const uint32_t old = atomicCAS(par + b, b, a);
+            if (old == b) break;
+            tries++;
+            b = uf_find(par, old);
+            a = uf_find(par, a);
+        }
+    }
+    if (tries) atomicAdd(retries, tries);
+}
+
+__global__ void k_wcc_compress(uint32_t n, uint32_t *par, uint32_t *label, unsigned long long *roots) {
+    unsigned long long c = 0;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const uint32_t r = uf_find(par, v);
+        label[v] = r;
+        c += r == v;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(EG_FULL_MASK, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(roots, c);
+}
+
+__global__ void k_widen(const uint32_t *__restrict__ in, uint32_t n, long long *out) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) out[v] = in[v];
+}
+
+}  // namespace
+
+extern "C" int eg_wcc(eg_graph *g, int64_t *labels_out, eg_wcc_stats *stats) {
+    if (!g) return eg_fail(EG_EINVAL, "NULL graph");
+    eg_ctx *ctx = g->ctx;
+    EG_CUDA(cudaSetDevice(ctx->device));
+    const uint32_t n = g->n;
+    EG_TRY(eg_buf_ensure(ctx, g->label, (uint64_t)n * 4));
+    // work: parent[n] | counters | int64 staging for the host copy
+    const uint64_t off_cnt = ((uint64_t)n + 3) & ~3ull;
+    const uint64_t off_wide = off_cnt + 8;
+    EG_TRY(eg_buf_ensure(ctx, g->bfs_work, (off_wide + (labels_out ? 2ull * n : 0)) * 4));
+    uint32_t *par = bp<uint32_t>(g->bfs_work);
+    uint32_t *retries = par + off_cnt;
+    unsigned long long *roots = reinterpret_cast<unsigned long long *>(par + off_cnt + 2);
+    long long *wide = reinterpret_cast<long long *>(par + off_wide);
+    uint32_t blocks = (uint32_t)(ctx->sm_count * 8);
+    EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+    EG_CUDA(cudaMemsetAsync(retries, 0, 32, ctx->stream));
+    k_wcc_init<<<blocks, 256, 0, ctx->stream>>>(n, par);
+    EG_LAUNCHED(ctx);
+    if (g->m_in) {
+        k_wcc_hook<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->pairs), g->m_in, par, retries);
+        EG_LAUNCHED(ctx);
+    }
+    k_wcc_compress<<<blocks, 256, 0, ctx->stream>>>(n, par, bp<uint32_t>(g->label), roots);
+    EG_LAUNCHED(ctx);
+    EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    if (labels_out) {
+        k_widen<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->label), n, wide);
+        EG_LAUNCHED(ctx);
+        EG_CUDA(cudaMemcpyAsync(labels_out, wide, (uint64_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    unsigned long long *h = (unsigned long long *)ctx->h_pinned;
+    EG_CUDA(cudaMemcpyAsync(h, roots, 8, cudaMemcpyDeviceToHost, ctx->stream));
+    EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (stats) {
+        stats->components = (uint32_t)*h;
+        stats->rounds = 1;
+        EG_CUDA(cudaEventElapsedTime(&stats->ms, ctx->ev0, ctx->ev1));
+    }
+    return EG_OK;
+}

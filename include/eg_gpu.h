@@ -1,0 +1,251 @@
+/*
+ * eg_gpu.h - C ABI of the GB300 (sm_103a) edge-traversal library.
+ *
+ * Plain C types only: pointers, sizes, small option structs.  Every call
+ * returns an int status (EG_OK = 0, negative on error); eg_last_error()
+ * gives the message of the calling thread's last failure.  One context owns
+ * one CUDA stream on one device; calls on a context are not thread-safe.
+ * Host output arrays are caller-owned; a NULL host output leaves the result
+ * on the device (see eg_graph_device_ptr).
+ *
+ * Each entry point names the reference interface it replaces.  The reference
+ * is one process in shared memory whose loader fills globals
+ * (init_all.h:36-60) and whose algorithms are `struct algo_func` plug-ins
+ * (random.h:64-69) called construct -> reset -> main -> destruct
+ * (random.c:128-143).
+ */
+#ifndef EG_GPU_H
+#define EG_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define EG_OK 0
+#define EG_EINVAL (-1)    /* bad argument */
+#define EG_ECUDA (-2)     /* CUDA runtime error */
+#define EG_ENOMEM (-3)    /* device allocation failed or over the HBM budget */
+#define EG_EIO (-4)       /* input file unreadable or of odd size */
+#define EG_ETIMEOUT (-5)  /* a device-side wait hit its iteration limit */
+#define EG_ENOTBUILT (-6) /* the layout an algorithm needs was not built */
+#define EG_ERANGE (-7)    /* an edge endpoint is >= n */
+
+typedef struct eg_ctx eg_ctx;
+typedef struct eg_graph eg_graph;
+
+/* Message of the calling thread's last error ("" if none). */
+const char *eg_last_error(void);
+
+/* Library version string. */
+const char *eg_version(void);
+
+/* ---- context ------------------------------------------------------------ */
+/* Opens device `device` with one stream.  hbm_budget_bytes caps the bytes
+ * the context may allocate (0 = no cap).  Replaces the reference's thread
+ * setup (setWorkers, random.c:123 and parallel_ligra.h:49-57). */
+int eg_open(int device, uint64_t hbm_budget_bytes, eg_ctx **out);
+int eg_close(eg_ctx *ctx);
+/* The context's cudaStream_t, as void*. */
+void *eg_stream(eg_ctx *ctx);
+int eg_sync(eg_ctx *ctx);
+uint64_t eg_bytes_in_use(eg_ctx *ctx);
+/* Number of kernels this context has launched so far. */
+uint64_t eg_kernel_launches(eg_ctx *ctx);
+
+/* ---- graph input (replaces init(): init_all.c:791-893) ----------------- */
+#define EG_UNDIRECTED 1u /* -u: append reversed copies of every edge
+                            (init_all.c:171-175), doubling m (init_all.c:636) */
+
+/* From host pairs: 2*m uint32 values [src][dst] in file order. */
+int eg_graph_from_pairs(eg_ctx *ctx, const uint32_t *pairs, uint64_t m, uint32_t n, unsigned flags,
+                        eg_graph **out);
+/* From device pairs (copied; the caller keeps ownership). */
+int eg_graph_from_device_pairs(eg_ctx *ctx, const uint32_t *d_pairs, uint64_t m, uint32_t n,
+                               unsigned flags, eg_graph **out);
+/* From a binary [src][dst] uint32 file (init_all.c:812-822, 8-byte records). */
+int eg_graph_from_file(eg_ctx *ctx, const char *path, uint32_t n, unsigned flags, eg_graph **out);
+/* Synthetic graphs generated on the device (seeded, counter-based):
+ * RMAT(scale, a=.57,b=.19,c=.19,d=.05) with m edges, and Erdos-Renyi with n
+ * vertices and m uniform (src,dst) pairs. */
+int eg_graph_generate_rmat(eg_ctx *ctx, int scale, uint64_t m, uint64_t seed, unsigned flags,
+                           eg_graph **out);
+int eg_graph_generate_er(eg_ctx *ctx, uint32_t n, uint64_t m, uint64_t seed, unsigned flags,
+                         eg_graph **out);
+void eg_graph_free(eg_graph *g);
+
+/* ---- layouts (replaces init_adj_sort, init_all.c:629-790, and
+ * init_grid_sort, init_all.c:321-430) ------------------------------------ */
+#define EG_LAYOUT_CSR 1u /* out-lists, stable by src: each list in file order */
+#define EG_LAYOUT_CSC 2u /* in-lists: ascending src, ties in file order */
+#define EG_LAYOUT_GRID 4u
+
+int eg_graph_build(eg_graph *g, unsigned layouts);
+/* 2-D grid of P x P cells (reference partitioning, init_all.c:123-129):
+ * cells row-major by (src partition, dst partition), ascending src inside. */
+int eg_graph_build_grid(eg_graph *g, uint32_t P);
+
+typedef struct {
+    uint32_t n;
+    uint64_t m_input; /* edges in the input */
+    uint64_t m;       /* adjacency entries (2*m_input with EG_UNDIRECTED) */
+    unsigned layouts; /* EG_LAYOUT_* built so far */
+    uint32_t grid_p;
+    uint64_t device_bytes;
+    float build_ms; /* device time of the last eg_graph_build */
+} eg_graph_info;
+int eg_graph_get_info(eg_graph *g, eg_graph_info *info);
+/* Copies a built adjacency to the host: ptr has n+1 entries, col has m. */
+int eg_graph_copy_adj(eg_graph *g, unsigned layout, uint32_t *ptr, uint32_t *col);
+/* Grid copy: cell_ptr has P*P+1 entries, src/dst have m. */
+int eg_graph_copy_grid(eg_graph *g, uint32_t *cell_ptr, uint32_t *src, uint32_t *dst);
+/* Out-degree (CSR list lengths) and in-degree; either pointer may be NULL. */
+int eg_graph_copy_degrees(eg_graph *g, uint32_t *out_deg, uint32_t *in_deg);
+
+/* Device pointers of graph arrays and of the last result of each algorithm. */
+#define EG_DEV_CSR_PTR 1
+#define EG_DEV_CSR_COL 2
+#define EG_DEV_CSC_PTR 3
+#define EG_DEV_CSC_COL 4
+#define EG_DEV_OUT_DEG 5
+#define EG_DEV_RANK 10   /* float[n], last eg_pagerank */
+#define EG_DEV_LEVEL 11  /* int32[n], last eg_bfs */
+#define EG_DEV_PARENT 12 /* int32[n], last eg_bfs with parents */
+#define EG_DEV_DIST 13   /* uint32[n], last eg_sssp */
+#define EG_DEV_LABEL 14  /* uint32[n], last eg_wcc */
+#define EG_DEV_SPMV_Y 15 /* last eg_spmv output */
+void *eg_graph_device_ptr(eg_graph *g, int which);
+
+/* ---- PageRank (replaces pagerank_simple.c:72-84,110-133 and
+ * prgrid_cilk.c:62-76,111-141) --------------------------------------------
+ * Pull over the CSC: rank[v] = base + damping * sum_{u->v} prev[u]/deg[u],
+ * fp32 values, fp32 row sums (two-sum compensated when `compensated`).
+ * swap=1: prev = rank after every iteration (prgrid, pr_numa).  swap=0
+ * reproduces pagerank_simple's pull mode, where prev is never updated.
+ * deg_multiplier=2 reproduces the doubled degrees of the grid load modes
+ * (init_all.c:851-852).  prev_init < 0 means 1/n (the reference uses 0.15).
+ * dangling=1 spreads the mass of out-degree-0 vertices uniformly (FP64
+ * reduction on the device); 0 drops it like the reference.
+ * tolerance > 0 stops once the FP64 L1 change between iterates is below it. */
+typedef struct {
+    int iterations;
+    float damping;
+    float prev_init;
+    int swap;
+    uint32_t deg_multiplier;
+    int dangling;
+    int compensated;
+    double tolerance;
+    int use_graph; /* 1: replay the iteration as a captured CUDA graph */
+} eg_pr_opts;
+typedef struct {
+    int iterations_run;
+    double residual;      /* FP64 L1 change of the last iteration (if computed) */
+    double dangling_mass; /* FP64 mass on out-degree-0 vertices, last iterate */
+    float ms;             /* device time of the iterations */
+} eg_pr_stats;
+void eg_pr_opts_default(eg_pr_opts *o);
+int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out, eg_pr_stats *stats);
+
+/* ---- SpMV (replaces spmv.c:98-135) ---------------------------------------
+ * Row reductions over a built adjacency:
+ *  EG_SPMV_U32_PULL  y[v] = sum over in-edges u->v of x[u]/1000 (u32, wraps);
+ *                    the reference's pull mode with its 0.001 scale
+ *  EG_SPMV_U32_PUSH  y[u] = sum over out-edges u->v of x[v]/1000 (push mode)
+ *  EG_SPMV_U32_EDGE  y[u] = sum over out-edges u->v of x[v] (edge-array mode 8)
+ *  EG_SPMV_F32       y[v] = sum over in-edges of val(e)*x[u], fp32
+ *  EG_SPMV_F32_COMP  same with two-sum compensated row sums
+ *  EG_SPMV_F64       same in fp64 (the error reference on the device)
+ * val(e) is the edge value rule below (EG_SPMV_F* only). */
+#define EG_SPMV_U32_PULL 0
+#define EG_SPMV_U32_PUSH 1
+#define EG_SPMV_U32_EDGE 2
+#define EG_SPMV_F32 3
+#define EG_SPMV_F32_COMP 4
+#define EG_SPMV_F64 5
+typedef struct {
+    int kind;
+    uint64_t value_seed; /* val(e) = U[0,1) hashed from (seed, min(u,v), max(u,v)) */
+    int unit_values;     /* 1: val(e) = 1 */
+} eg_spmv_opts;
+/* x: host array of n (u32 for U32 kinds, f32 otherwise); y: host array of n
+ * (u32, f32 or f64 for EG_SPMV_F64), or NULL to keep y on the device. */
+int eg_spmv(eg_graph *g, const eg_spmv_opts *opts, const void *x, void *y, float *ms);
+
+/* ---- BFS (replaces bfs_simple.c:104-229 and bfsgrid_cilk.c:48-168) -------
+ * Direction-optimising BFS from `root` over the out-lists.  Levels follow
+ * the reference: level[root] = 1, reached vertices level+1 of their parent,
+ * unreached 0.  parent_out (optional): a BFS tree, parent[root] = root,
+ * -1 unreached.  Pull steps read the in-lists (CSC) of directed graphs and
+ * the CSR of undirected ones. */
+#define EG_BFS_AUTO 0
+#define EG_BFS_PUSH_ONLY 1
+#define EG_BFS_PULL_ONLY 2
+typedef struct {
+    int direction;
+    /* auto switches to pull when frontier size + frontier out-degree
+     * > m / switch_divisor (the reference uses 20, bfs_simple.c:191-197) */
+    double switch_divisor;
+} eg_bfs_opts;
+typedef struct {
+    int levels;
+    uint32_t reached;
+    uint64_t edges_traversed; /* sum of out-degrees of reached vertices */
+    int pull_levels;
+    float ms;
+} eg_bfs_stats;
+void eg_bfs_opts_default(eg_bfs_opts *o);
+int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32_t *level_out, int32_t *parent_out,
+           eg_bfs_stats *stats);
+
+/* Multi-source BFS, bit-sliced: up to 64 sources per 64-bit word per vertex,
+ * all advanced by one level per sweep.  levels_out: k*n int32, row s holds
+ * source s's levels (same convention as eg_bfs), or NULL. */
+int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *levels_out, eg_bfs_stats *stats);
+
+/* ---- SSSP (replaces sssp_pushpull.c:39-190) ------------------------------
+ * Exact shortest paths over the out-lists; dist[root] = 0, unreached =
+ * UINT32_MAX-1 (sssp_pushpull.c:8).  Weight rules, computed from the edge's
+ * endpoints like the reference's CREATE_WEIGHT path:
+ *   EG_W_REF   src%10 + dst%10 (init_all.c:661-686)
+ *   EG_W_HASH  lo + H(seed, min(u,v), max(u,v)) mod (hi-lo+1), symmetric */
+#define EG_W_REF 0
+#define EG_W_HASH 1
+#define EG_W_UNIT 2
+typedef struct {
+    int rule;
+    uint64_t seed;
+    uint32_t lo, hi;
+} eg_weights;
+typedef struct {
+    int rounds;
+    uint32_t reached;
+    uint64_t relaxations;
+    float ms;
+} eg_sssp_stats;
+int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *w, uint32_t *dist_out, eg_sssp_stats *stats);
+/* k sources in one batch; dist_out: k*n uint32 (row s for source s) or NULL. */
+int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg_weights *w, uint32_t *dist_out,
+                  eg_sssp_stats *stats);
+
+/* ---- WCC (replaces wcc.c:30-90,186-286) ----------------------------------
+ * Weakly connected components; label = the minimum vertex id of the
+ * component (the fixed point of the reference's min-label propagation). */
+typedef struct {
+    int rounds;
+    uint32_t components;
+    float ms;
+} eg_wcc_stats;
+int eg_wcc(eg_graph *g, int64_t *labels_out, eg_wcc_stats *stats);
+
+/* Samples k roots uniformly from vertices with out-degree > 0 (the same
+ * counter-based rule as the CPU generator). */
+int eg_sample_roots(eg_graph *g, int k, uint64_t seed, uint32_t *roots_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* EG_GPU_H */

@@ -268,3 +268,21 @@ def bfs_tree_ok(n, out_ptr, out_col, root, level, parent):
     keys = np.unique(src * n + out_col.astype(np.int64))
     q = ps.astype(np.int64) * n + vs.astype(np.int64)
     return bool(np.all(np.isin(q, keys)))
+
+
+def hash_weights(u, v, seed, lo, hi):
+    """u32 weights in [lo, hi] hashed from each (u, v) endpoint pair."""
+    u = np.ascontiguousarray(u, dtype=np.uint32)
+    v = np.ascontiguousarray(v, dtype=np.uint32)
+    out = np.empty(len(u), dtype=np.uint32)
+    lib().or_hash_weights(u64(len(u)), _p(u), _p(v), u64(seed), u32(lo), u32(hi), _p(out))
+    return out
+
+
+def hash_values(u, v, seed):
+    """fp32 values in [0, 1) hashed from each (u, v) endpoint pair."""
+    u = np.ascontiguousarray(u, dtype=np.uint32)
+    v = np.ascontiguousarray(v, dtype=np.uint32)
+    out = np.empty(len(u), dtype=np.float32)
+    lib().or_hash_values(u64(len(u)), _p(u), _p(v), u64(seed), _p(out))
+    return out

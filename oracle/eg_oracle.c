@@ -530,3 +530,22 @@ void or_set_threads(int t) {
     (void)t;
 #endif
 }
+
+/* Per-edge attributes hashed from the unordered endpoint pair (the weight and
+ * value rules of the CUDA library, restated for the checker). */
+static inline uint64_t or_edge_hash(uint64_t seed, uint32_t u, uint32_t v) {
+    uint32_t a = u < v ? u : v, b = u < v ? v : u;
+    return or_draw(or_key(seed, ((uint64_t)a << 32) | b), 0);
+}
+void or_hash_weights(uint64_t count, const uint32_t *u, const uint32_t *v, uint64_t seed, uint32_t lo,
+                     uint32_t hi, uint32_t *out) {
+    uint64_t span = (uint64_t)hi - lo + 1;
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)count; i++)
+        out[i] = lo + (uint32_t)(((or_edge_hash(seed, u[i], v[i]) >> 32) * span) >> 32);
+}
+void or_hash_values(uint64_t count, const uint32_t *u, const uint32_t *v, uint64_t seed, float *out) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)count; i++)
+        out[i] = (float)(or_edge_hash(seed, u[i], v[i]) >> 40) * (1.0f / 16777216.0f);
+}

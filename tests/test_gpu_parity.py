@@ -1,0 +1,332 @@
+"""GPU parity: the CUDA path, called through the C ABI, against the oracle
+and the reference's own dumps (tests/golden/).
+
+Integer outputs (layouts, BFS levels, SSSP distances, WCC labels, integer
+SpMV) must be bit-exact.  Floating-point outputs use the tolerances written
+below: against FP64, relative L1 error <= 1e-6 and max relative error <= 1e-5;
+against the reference's fp32 dumps (a different summation order), max
+relative error <= 2e-5.
+"""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+CASES = ["tiny", "rmat10", "rmat12", "rmat16"]
+PR_REL_L1 = 1e-6
+PR_MAX_REL = 1e-5
+PR_VS_REF32_MAX_REL = 2e-5
+
+
+def load(name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    rec = {k: z[k] for k in z.files}
+    n = int(rec["n"])
+    pairs = rec["pairs"] if "pairs" in rec else oracle.rmat_edges(int(np.log2(n)), 16 * n, 1)
+    assert hashlib.sha256(pairs.tobytes()).hexdigest() == rec["pairs_sha256"].item().decode()
+    return n, pairs, rec
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    import everythinggraph_gb300 as eg
+    from everythinggraph_gb300 import build
+    build.build_lib()
+    c = eg.Context(0)
+    yield c
+    c.close()
+
+
+@pytest.fixture(scope="module", params=CASES)
+def case(request, ctx):
+    import everythinggraph_gb300 as eg
+    n, pairs, rec = load(request.param)
+    g = ctx.from_pairs(n, pairs).build(eg.CSR | eg.CSC)
+    gu = ctx.from_pairs(n, pairs, undirected=True).build(eg.CSR | eg.CSC)
+    adj = oracle.build_adj(n, pairs)
+    adju = oracle.build_adj(n, pairs, undirected=True)
+    yield request.param, n, pairs, rec, g, gu, adj, adju
+    g.free()
+    gu.free()
+
+
+def rel_errors(got, ref):
+    got = got.astype(np.float64)
+    ref = ref.astype(np.float64)
+    l1 = np.abs(got - ref).sum() / max(np.abs(ref).sum(), 1e-300)
+    mx = (np.abs(got - ref) / np.maximum(np.abs(ref), 1e-30)).max() if len(ref) else 0.0
+    return l1, mx
+
+
+# ------------------------------------------------------------------ layouts
+def test_layouts_bit_exact(case):
+    import everythinggraph_gb300 as eg
+    name, n, pairs, rec, g, gu, adj, adju = case
+    for graph, a in ((g, adj), (gu, adju)):
+        ptr, col = graph.adj(eg.CSR)
+        np.testing.assert_array_equal(ptr, a.out_ptr)
+        np.testing.assert_array_equal(col, a.out_col)  # file order inside each list
+        ptr, col = graph.adj(eg.CSC)
+        np.testing.assert_array_equal(ptr, a.in_ptr)
+        np.testing.assert_array_equal(col, a.in_col)  # ascending src inside each list
+        od, idg = graph.degrees(True, True)
+        np.testing.assert_array_equal(od, a.out_deg())
+        np.testing.assert_array_equal(idg, a.in_deg())
+
+
+def test_grid_layout_bit_exact(case, ctx):
+    name, n, pairs, rec, g, gu, adj, adju = case
+    for P in sorted({oracle.default_p(n), 3, 7}):
+        if P > n:
+            continue
+        gg = ctx.from_pairs(n, pairs)
+        gg.build_grid(P)
+        cp, s, d = gg.grid()
+        rcp, rs, rd = oracle.build_grid(n, pairs, P)
+        np.testing.assert_array_equal(cp, rcp)
+        np.testing.assert_array_equal(s, rs)
+        np.testing.assert_array_equal(d, rd)
+        gg.free()
+
+
+def test_device_generators_match_cpu(ctx):
+    import everythinggraph_gb300 as eg
+    for scale, seed in ((10, 1), (12, 7)):
+        n = 1 << scale
+        g = ctx.rmat(scale, 16 * n, seed).build(eg.CSR)
+        a = oracle.build_adj(n, oracle.rmat_edges(scale, 16 * n, seed))
+        ptr, col = g.adj(eg.CSR)
+        np.testing.assert_array_equal(ptr, a.out_ptr)
+        np.testing.assert_array_equal(col, a.out_col)
+        g.free()
+    n, m = 5000, 40000
+    g = ctx.er(n, m, 4).build(eg.CSR)
+    a = oracle.build_adj(n, oracle.er_edges(n, m, 4))
+    ptr, col = g.adj(eg.CSR)
+    np.testing.assert_array_equal(col, a.out_col)
+    g.free()
+
+
+# ------------------------------------------------------------------ PageRank
+def test_pagerank_reference_pull_quirk(case):
+    # pagerank_simple -m 2 -a 1: prev stays 0.15, 10 identical iterations
+    name, n, pairs, rec, g, gu, adj, adju = case
+    got, st = g.pagerank(iterations=10, prev_init=0.15, swap=False)
+    l1, mx = rel_errors(got, rec["pr_simple_pull"])
+    assert mx <= PR_VS_REF32_MAX_REL, (l1, mx)
+
+
+def test_pagerank_prgrid_semantics(case):
+    # prgrid_cilk -m 0: 10 iterations with swap, degrees counted twice
+    name, n, pairs, rec, g, gu, adj, adju = case
+    for comp in (False, True):
+        got, st = g.pagerank(iterations=10, prev_init=0.15, swap=True, deg_multiplier=2, compensated=comp)
+        l1, mx = rel_errors(got, rec["prgrid_m0"])
+        assert mx <= PR_VS_REF32_MAX_REL, (comp, l1, mx)
+
+
+def test_pagerank_vs_fp64(case):
+    name, n, pairs, rec, g, gu, adj, adju = case
+    for dangling in (False, True):
+        ref = oracle.pagerank_f64(adj, adj.out_deg(), 1.0 / n, 10, dangling=dangling)
+        for comp in (False, True):
+            got, st = g.pagerank(iterations=10, dangling=dangling, compensated=comp)
+            l1, mx = rel_errors(got, ref)
+            assert l1 <= PR_REL_L1 and mx <= PR_MAX_REL, (dangling, comp, l1, mx)
+            assert st.iterations_run == 10
+
+
+def test_pagerank_tolerance_stops_early(case):
+    name, n, pairs, rec, g, gu, adj, adju = case
+    got, st = g.pagerank(iterations=200, tolerance=1e-6, dangling=True)
+    assert 1 <= st.iterations_run < 200
+    assert st.residual < 1e-6
+    assert abs(float(got.astype(np.float64).sum()) - 1.0) < 1e-4  # mass conserved with dangling redistribution
+
+
+# ------------------------------------------------------------------ SpMV
+def test_spmv_u32_bit_exact(case):
+    name, n, pairs, rec, g, gu, adj, adju = case
+    x = np.arange(n, dtype=np.uint32)
+    y, _ = g.spmv(x, "u32_pull")
+    np.testing.assert_array_equal(y, rec["spmv_pull"])
+    y, _ = g.spmv(x, "u32_push")
+    np.testing.assert_array_equal(y, rec["spmv_push"])
+    y, _ = g.spmv(x, "u32_edge")
+    np.testing.assert_array_equal(y, rec["spmv_m8"])
+    # random x with wrap-around
+    xr = np.random.default_rng(5).integers(0, 2**32, n, dtype=np.uint64).astype(np.uint32)
+    y, _ = g.spmv(xr, "u32_edge")
+    np.testing.assert_array_equal(y, oracle.spmv_u32(n, adj.out_ptr, adj.out_col, xr, oracle.SPMV_EDGE))
+
+
+def test_spmv_float_vs_fp64(case):
+    name, n, pairs, rec, g, gu, adj, adju = case
+    x = oracle.uniform_f32(n, 11)
+    # edge values are hashed from the endpoints; the oracle recomputes them
+    vals = oracle.hash_values(adj.in_col, adj.in_dst(), 9)
+    ref = oracle.spmv_f64(n, adj.in_ptr, adj.in_col, vals, x)
+    y64, _ = g.spmv(x, "f64", value_seed=9)
+    assert y64.dtype == np.float64
+    np.testing.assert_allclose(y64, ref, rtol=1e-12, atol=1e-300)
+    ones64 = oracle.spmv_f64(n, adj.in_ptr, adj.in_col, np.ones(adj.m, np.float32), x)
+    y1, _ = g.spmv(x, "f64", unit_values=True)
+    np.testing.assert_allclose(y1, ones64, rtol=1e-12, atol=1e-300)
+    nz = ref != 0
+    for kind in ("f32", "f32_comp"):
+        y, _ = g.spmv(x, kind, value_seed=9)
+        l1, mx = rel_errors(y[nz], ref[nz])
+        assert l1 <= 1e-6 and mx <= 1e-5, (kind, l1, mx)
+        assert np.all(y[~nz] == 0)
+
+
+# ------------------------------------------------------------------ BFS
+def test_bfs_levels_bit_exact(case):
+    name, n, pairs, rec, g, gu, adj, adju = case
+    for r in rec["roots"]:
+        for direction in ("auto", "push", "pull"):
+            lv, par, st = g.bfs(int(r), direction=direction, parents=True)
+            np.testing.assert_array_equal(lv.astype(np.uint32), rec["bfsgrid_m0_p%d" % r])
+            assert oracle.bfs_tree_ok(n, adj.out_ptr, adj.out_col, int(r), lv, par)
+    lv, st = g.bfs(0)
+    np.testing.assert_array_equal(lv.astype(np.uint32), rec["bfs_simple_m8"])
+    lvu, st = gu.bfs(0)
+    np.testing.assert_array_equal(lvu > 0, rec["bfs_simple_m2u"] > 0)
+    assert st.reached == int((lvu > 0).sum())
+
+
+def test_bfs_multi_matches_single(case):
+    name, n, pairs, rec, g, gu, adj, adju = case
+    od = adju.out_deg()
+    for k in (1, 5, 64):
+        roots = oracle.sample_roots(od, k, 3)
+        lv, st = gu.bfs_multi(roots)
+        for s, r in enumerate(roots):
+            ref = oracle.bfs_levels(n, adju.out_ptr, adju.out_col, int(r))
+            np.testing.assert_array_equal(lv[s], ref)
+
+
+# ------------------------------------------------------------------ SSSP
+def test_sssp_bit_exact(case):
+    import everythinggraph_gb300 as eg
+    name, n, pairs, rec, g, gu, adj, adju = case
+    for r in rec["roots"]:
+        d, st = g.sssp(int(r), eg.weights("ref"))
+        np.testing.assert_array_equal(d, rec["sssp_pull_p%d" % r])
+
+
+def test_sssp_hash_weights_and_batch(case):
+    import everythinggraph_gb300 as eg
+    name, n, pairs, rec, g, gu, adj, adju = case
+    w = eg.weights("hash", seed=6, lo=1, hi=255)
+    # the oracle gets the same per-entry weights (hash of the endpoints)
+    wa = oracle.hash_weights(adj.out_src(), adj.out_col, 6, 1, 255)
+    roots = oracle.sample_roots(adj.out_deg(), 7, 5)
+    dm, st = g.sssp_multi(roots, w)
+    for s, r in enumerate(roots):
+        ref = oracle.sssp(n, adj.out_ptr, adj.out_col, wa, int(r))
+        d1, _ = g.sssp(int(r), w)
+        np.testing.assert_array_equal(d1, ref)
+        np.testing.assert_array_equal(dm[s], ref)
+
+
+# ------------------------------------------------------------------ WCC
+def test_wcc_bit_exact(case):
+    name, n, pairs, rec, g, gu, adj, adju = case
+    lab, st = g.wcc()
+    np.testing.assert_array_equal(lab, rec["wcc_m2u"])
+    lab2, st2 = gu.wcc()
+    np.testing.assert_array_equal(lab2, rec["wcc_m0"])
+    assert st.components == len(np.unique(lab))
+
+
+# ------------------------------------------------------------------ edge cases
+def test_empty_and_tiny_graphs(ctx):
+    import everythinggraph_gb300 as eg
+    g = ctx.from_pairs(5, np.zeros(0, np.uint32)).build(eg.CSR | eg.CSC)
+    lv, st = g.bfs(3)
+    assert list(lv) == [0, 0, 0, 1, 0]
+    r, _ = g.pagerank(iterations=3)
+    np.testing.assert_allclose(r, np.full(5, 0.15 / 5, np.float32), rtol=1e-6)
+    lab, _ = g.wcc()
+    assert list(lab) == [0, 1, 2, 3, 4]
+    d, _ = g.sssp(2)
+    assert d[2] == 0 and (d[[0, 1, 3, 4]] == 0xFFFFFFFE).all()
+    g.free()
+    g1 = ctx.from_pairs(1, np.array([0, 0], np.uint32)).build(eg.CSR | eg.CSC)
+    lv, st = g1.bfs(0)
+    assert list(lv) == [1]
+    g1.free()
+
+
+def test_errors_are_reported(ctx):
+    import everythinggraph_gb300 as eg
+    g = ctx.from_pairs(4, np.array([0, 1, 1, 9], np.uint32))
+    with pytest.raises(eg.EGError) as e:
+        g.build()
+    assert e.value.code == -7  # EG_ERANGE: endpoint >= n
+    g.free()
+    g = ctx.from_pairs(4, np.array([0, 1, 1, 2], np.uint32))
+    with pytest.raises(eg.EGError) as e:
+        g.bfs(0)
+    assert e.value.code == -6  # layout not built
+    g.build()
+    with pytest.raises(eg.EGError) as e:
+        g.bfs(4)
+    assert e.value.code == -1
+    g.free()
+    small = eg.Context(0, hbm_budget=1 << 20)
+    with pytest.raises(eg.EGError) as e:
+        small.rmat(16, 1 << 20, 1)
+    assert e.value.code == -3  # over the HBM budget
+    small.close()
+
+
+# ------------------------------------------------------------------ larger, property checks
+@pytest.fixture(scope="module")
+def big(ctx):
+    import everythinggraph_gb300 as eg
+    g = ctx.rmat(20, 16 << 20, 2, undirected=True).build(eg.CSR | eg.CSC)
+    yield g
+    g.free()
+
+
+def test_big_bfs_properties(big):
+    import everythinggraph_gb300 as eg
+    ptr, col = big.adj(eg.CSR)
+    src = np.repeat(np.arange(len(ptr) - 1, dtype=np.int64), np.diff(ptr.astype(np.int64)))
+    roots = big.sample_roots(4, 3)
+    lvm, _ = big.bfs_multi(roots)
+    for s, r in enumerate(roots):
+        lv, par, st = big.bfs(int(r), parents=True)
+        np.testing.assert_array_equal(lv, lvm[s])
+        # every edge from a reached vertex reaches a vertex at most one level deeper
+        ls, ld = lv[src], lv[col]
+        assert np.all(ld[ls > 0] > 0) and np.all(ld[ls > 0] <= ls[ls > 0] + 1)
+        reached = np.nonzero(lv > 0)[0]
+        reached = reached[reached != r]
+        assert np.all(lv[par[reached]] == lv[reached] - 1)
+
+
+def test_big_wcc_and_sssp_properties(big):
+    import everythinggraph_gb300 as eg
+    ptr, col = big.adj(eg.CSR)
+    src = np.repeat(np.arange(len(ptr) - 1, dtype=np.int64), np.diff(ptr.astype(np.int64)))
+    lab, st = big.wcc()
+    assert np.all(lab[src] == lab[col])
+    assert np.all(lab <= np.arange(len(lab))) and np.all(lab[lab] == lab)
+    w = eg.weights("hash", seed=6, lo=1, hi=255)
+    wa = oracle.hash_weights(src.astype(np.uint32), col, 6, 1, 255).astype(np.int64)
+    r = int(big.sample_roots(1, 5)[0])
+    d, st = big.sssp(r, w)
+    d = d.astype(np.int64)
+    INF = 0xFFFFFFFE
+    ok = (d[src] != INF) & (src != col)
+    assert np.all(d[col][ok] <= d[src][ok] + wa[ok])  # no edge can still be relaxed
+    assert d[r] == 0
