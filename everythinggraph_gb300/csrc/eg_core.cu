@@ -593,6 +593,7 @@ static int build_adj_pair(eg_graph *g, bool want_csc) {
     uint32_t *ks = nullptr, *vs = nullptr;
     uint32_t *hbad = (uint32_t *)ctx->h_pinned;
     auto cleanup = [&]() {
+        cudaStreamSynchronize(ctx->stream);
         eg_buf_free(ctx, ka);
         eg_buf_free(ctx, va);
         eg_buf_free(ctx, kb);
@@ -734,14 +735,16 @@ extern "C" int eg_graph_build_grid(eg_graph *g, uint32_t P) {
     uint32_t psz = mod ? n / P + 1 : n / P;
     uint32_t split = mod * psz;
     uint64_t cells = (uint64_t)P * P;
-    eg_buf ka, va, kb, vb, rows;
+    eg_buf ka, va, kb, vb, rows, chist;
     int rc = EG_OK;
     auto cleanup = [&]() {
+        cudaStreamSynchronize(ctx->stream);
         eg_buf_free(ctx, ka);
         eg_buf_free(ctx, va);
         eg_buf_free(ctx, kb);
         eg_buf_free(ctx, vb);
         eg_buf_free(ctx, rows);
+        eg_buf_free(ctx, chist);
     };
 #define GTRY(x)            \
     do {                   \
@@ -773,11 +776,11 @@ extern "C" int eg_graph_build_grid(eg_graph *g, uint32_t P) {
                                                                 bp<uint32_t>(g->gsrc), bp<uint32_t>(g->gdst));
         ctx->launches++;
     }
-    // cell sizes -> offsets (reuse the rows buffer for the histogram)
-    GTRY(eg_buf_ensure(ctx, rows, (cells + 1) * 4));
-    if (cudaMemsetAsync(rows.p, 0, cells * 4, ctx->stream) != cudaSuccess) GTRY(eg_fail(EG_ECUDA, "memset"));
-    GTRY(eg_histogram(ctx, ks, M, bp<uint32_t>(rows)));
-    GTRY(eg_exscan_u32(ctx, bp<uint32_t>(rows), bp<uint32_t>(g->cell_ptr), cells));
+    // cell sizes -> offsets
+    GTRY(eg_buf_ensure(ctx, chist, (cells + 1) * 4));
+    if (cudaMemsetAsync(chist.p, 0, cells * 4, ctx->stream) != cudaSuccess) GTRY(eg_fail(EG_ECUDA, "memset"));
+    GTRY(eg_histogram(ctx, ks, M, bp<uint32_t>(chist)));
+    GTRY(eg_exscan_u32(ctx, bp<uint32_t>(chist), bp<uint32_t>(g->cell_ptr), cells));
     if (cudaStreamSynchronize(ctx->stream) != cudaSuccess)
         GTRY(eg_fail(EG_ECUDA, "grid build: %s", cudaGetErrorString(cudaGetLastError())));
 #undef GTRY

@@ -1,0 +1,27 @@
+/*
+ * Grid PageRank plug-in, replacing prgrid_cilk.c (current_algo, 188-190):
+ * ten iterations with prev = rank (prgrid_cilk.c:111-141), prev starting at
+ * 0.15 (98).  The grid load modes count degrees twice (init_all.c:851-852),
+ * so the divisor is doubled there, as in the reference.  The per-destination
+ * sum over the grid equals the CSC order, which is what the GPU reduces.
+ */
+#include "eg_host.h"
+
+static float *rank_h;
+
+static void g_construct(void) { rank_h = malloc((size_t)NB_NODES * sizeof(float)); }
+static void g_reset(struct node *n) { (void)n; }
+static void g_main(struct node *n) {
+    (void)n;
+    eg_pr_opts o;
+    eg_pr_opts_default(&o);
+    o.prev_init = 0.15f;
+    o.swap = 1;
+    o.deg_multiplier = (load_mode < 2 || load_mode >= 6) ? 2 : 1;
+    eg_pr_stats st;
+    if (eg_pagerank(eg_g, &o, rank_h, &st) != EG_OK) eg_die("pagerank");
+    printf("Iter %d time %f \n", st.iterations_run, st.ms / 1000.0);
+    eg_dump(rank_h, sizeof(float), NB_NODES);
+}
+static void g_destruct(void) { free(rank_h); }
+struct algo_func current_algo = {.reset = g_reset, .main = g_main, .construct = g_construct, .destruct = g_destruct};

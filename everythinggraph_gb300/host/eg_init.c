@@ -1,0 +1,41 @@
+/*
+ * Loader: replaces init() (init_all.c:791-893).  The file's [src][dst]
+ * records go to HBM and the layout selected by load_mode is built there:
+ *   0, 6      2-D grid (init_grid_sort) - plus CSR/CSC for the degree arrays
+ *   1         grid without sort: same device grid (the reference's
+ *             per-cell realloc lists are a host-side construction method)
+ *   2, 3      CSR + CSC by stable device radix sort (init_adj_sort)
+ *   4, 5      count sort / dynamic lists: the same device CSR + CSC
+ *   7, 8, 9   edge array: the device CSR (edge array sorted by src)
+ * -u appends the reversed edges for the adjacency modes only, as in the
+ * reference (init_all.c:636 doubles nb_edges only in init_adj_sort).
+ */
+#include <string.h>
+
+#include "eg_host.h"
+
+void init(int full) {
+    (void)full;
+    if (eg_open(0, 0, &eg_context) != EG_OK) eg_die("eg_open");
+    unsigned flags = 0;
+    int adjacency_mode = load_mode >= 2 && load_mode <= 5;
+    if (createUndir && adjacency_mode) flags |= EG_UNDIRECTED;
+    if (weighted_graph) {
+        fprintf(stderr, "-w (12-byte weighted records) is not supported by the GPU loader\n");
+        exit(1);
+    }
+    printf("Load start");
+    if (eg_graph_from_file(eg_context, filename, NB_NODES, flags, &eg_g) != EG_OK) eg_die("load");
+    eg_graph_info info;
+    eg_graph_get_info(eg_g, &info);
+    nb_edges = info.m;
+    printf("#NB edges = %llu\n", (unsigned long long)info.m_input);
+    unsigned layouts = EG_LAYOUT_CSR | EG_LAYOUT_CSC;
+    if (isSymmetric && adjacency_mode) layouts = EG_LAYOUT_CSR;
+    if (eg_graph_build(eg_g, layouts) != EG_OK) eg_die("build");
+    if (load_mode == 0 || load_mode == 1 || load_mode == 6) {
+        if (eg_graph_build_grid(eg_g, P) != EG_OK) eg_die("grid build");
+    }
+    eg_graph_get_info(eg_g, &info);
+    printf("#Device layout build time ( %f s )\n", info.build_ms / 1000.0);
+}

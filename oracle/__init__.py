@@ -286,3 +286,22 @@ def hash_values(u, v, seed):
     out = np.empty(len(u), dtype=np.float32)
     lib().or_hash_values(u64(len(u)), _p(u), _p(v), u64(seed), _p(out))
     return out
+
+
+def bfs_do(adj_out_ptr, adj_out_col, adj_in_ptr, adj_in_col, root):
+    """Multi-threaded direction-optimising BFS (levels, root = 1)."""
+    n = len(adj_out_ptr) - 1
+    level = np.empty(n, dtype=np.int32)
+    rc = lib().or_bfs_do(u32(n), _p(adj_out_ptr), _p(adj_out_col), _p(adj_in_ptr), _p(adj_in_col), u32(root),
+                         _p(level))
+    if rc != 0:
+        raise ValueError("root out of range")
+    return level
+
+
+def wcc_lp(out_ptr, out_col):
+    """Multi-threaded min-label propagation (wcc.c adjacency mode)."""
+    n = len(out_ptr) - 1
+    comp = np.empty(n, dtype=np.int64)
+    rounds = lib().or_wcc_lp(u32(n), _p(out_ptr), _p(out_col), _p(comp))
+    return comp, rounds

@@ -549,3 +549,117 @@ void or_hash_values(uint64_t count, const uint32_t *u, const uint32_t *v, uint64
     for (int64_t i = 0; i < (int64_t)count; i++)
         out[i] = (float)(or_edge_hash(seed, u[i], v[i]) >> 40) * (1.0f / 16777216.0f);
 }
+
+/* ------------------------------------------------------------------------ */
+/* Multi-threaded restatements of the reference's CPU loops, used as the
+ * timed CPU baseline (the reference binaries themselves need the reference
+ * sources, which are not shipped).
+ *
+ * or_bfs_do restates bfs_simple.c's iterator (136-229): push steps over the
+ * frontier's out-lists with a CAS on the next-frontier flag (bfs_push,
+ * 121-134), pull steps over unvisited vertices that stop at the first
+ * in-neighbour in the frontier (bfs_pull, 104-120), and the switch rule
+ * "pull iff items + frontier degree > m/20" (191-197).  Frontiers are byte
+ * maps as in random.c:74-77.  Writes levels (root = 1). */
+int or_bfs_do(uint32_t n, const uint32_t *out_ptr, const uint32_t *out_col, const uint32_t *in_ptr,
+              const uint32_t *in_col, uint32_t root, int32_t *level) {
+    if (root >= n) return -1;
+    uint64_t m = out_ptr[n];
+    unsigned char *cur = (unsigned char *)calloc(n, 1), *nxt = (unsigned char *)calloc(n, 1);
+    uint32_t *q = (uint32_t *)malloc((size_t)n * 4), *q2 = (uint32_t *)malloc((size_t)n * 4);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; i++) level[i] = 0;
+    level[root] = 1;
+    cur[root] = 1;
+    q[0] = root;
+    uint64_t qn = 1, items = 1, fdeg = out_ptr[root + 1] - out_ptr[root];
+    int pull = 0, have_q = 1;
+    int32_t lvl = 1;
+    while (items) {
+        pull = (double)items + (double)fdeg > (double)m / 20.0;
+        uint64_t cnt = 0, deg = 0, qn2 = 0;
+        if (!pull) {
+            if (!have_q) {
+                qn = 0;
+                for (uint32_t v = 0; v < n; v++)
+                    if (cur[v]) q[qn++] = v;
+            }
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : cnt, deg)
+            for (int64_t i = 0; i < (int64_t)qn; i++) {
+                uint32_t u = q[i];
+                for (uint32_t p = out_ptr[u]; p < out_ptr[u + 1]; p++) {
+                    uint32_t v = out_col[p];
+                    if (level[v] == 0 && __sync_bool_compare_and_swap(&level[v], 0, lvl + 1)) {
+                        nxt[v] = 1;
+                        uint64_t pos = __sync_fetch_and_add(&qn2, 1);
+                        q2[pos] = v;
+                        cnt++;
+                        deg += out_ptr[v + 1] - out_ptr[v];
+                    }
+                }
+            }
+            uint32_t *t = q; q = q2; q2 = t;
+            qn = qn2;
+            have_q = 1;
+        } else {
+#pragma omp parallel for schedule(dynamic, 1024) reduction(+ : cnt, deg)
+            for (int64_t v = 0; v < (int64_t)n; v++) {
+                if (level[v] != 0) continue;
+                for (uint32_t p = in_ptr[v]; p < in_ptr[v + 1]; p++) {
+                    if (cur[in_col[p]]) {
+                        level[v] = lvl + 1;
+                        nxt[v] = 1;
+                        cnt++;
+                        deg += out_ptr[v + 1] - out_ptr[v];
+                        break;
+                    }
+                }
+            }
+            have_q = 0;
+        }
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < (int64_t)n; i++) cur[i] = 0;
+        unsigned char *t = cur; cur = nxt; nxt = t;
+        items = cnt;
+        fdeg = deg;
+        lvl++;
+    }
+    free(cur); free(nxt); free(q); free(q2);
+    return 0;
+}
+
+/* or_wcc_lp restates wcc.c's adjacency-list mode (wcc.c:30-90, 262-277):
+ * every vertex starts active with its own id (wcc_reset, 128-135); each round
+ * relaxes the out-lists of the active vertices with writeMin and activates
+ * the vertices whose label dropped, until no vertex is active.  On a
+ * symmetric (-u) adjacency this is the min-id WCC labelling.  Returns rounds. */
+int or_wcc_lp(uint32_t n, const uint32_t *out_ptr, const uint32_t *out_col, int64_t *comp) {
+    unsigned char *act = (unsigned char *)malloc(n), *nact = (unsigned char *)calloc(n, 1);
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)n; i++) { comp[i] = i; act[i] = 1; }
+    int rounds = 0;
+    uint64_t active = n;
+    while (active) {
+        uint64_t nxt = 0;
+#pragma omp parallel for schedule(dynamic, 1024) reduction(+ : nxt)
+        for (int64_t u = 0; u < (int64_t)n; u++) {
+            if (!act[u]) continue;
+            int64_t cu = comp[u];
+            for (uint32_t p = out_ptr[u]; p < out_ptr[u + 1]; p++) {
+                uint32_t v = out_col[p];
+                int64_t c;
+                int changed = 0;
+                while ((c = comp[v]) > cu) {
+                    if (__sync_bool_compare_and_swap(&comp[v], c, cu)) { changed = 1; break; }
+                }
+                if (changed && __sync_bool_compare_and_swap(&nact[v], 0, 1)) nxt++;
+            }
+        }
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < (int64_t)n; i++) { act[i] = nact[i]; nact[i] = 0; }
+        active = nxt;
+        rounds++;
+    }
+    free(act); free(nact);
+    return rounds;
+}

@@ -1,0 +1,88 @@
+"""The C drop-in driver: same command line as the reference binaries, same
+plug-in order, result dumps compared with the reference's own dumps."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+import oracle
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+BIN = os.path.join(ROOT, "everythinggraph_gb300", "_build")
+
+
+@pytest.fixture(scope="module")
+def binaries():
+    from everythinggraph_gb300 import build
+    build.build_lib()
+    return build.build_host()
+
+
+def run(name, args, tmp_path, dtype, n):
+    out = str(tmp_path / ("%s.bin" % name))
+    env = dict(os.environ, EG_DUMP=out)
+    r = subprocess.run([os.path.join(BIN, name)] + args, env=env, capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stdout + r.stderr
+    a = np.fromfile(out, dtype=dtype)
+    assert a.size == n
+    return a, r.stdout
+
+
+def test_usage_without_gpu(binaries):
+    # argument errors are handled on the host before any device call
+    for exe in binaries:
+        r = subprocess.run([exe, "-h"], capture_output=True, text=True, timeout=30)
+        assert r.returncode == 255 and "Usage" in r.stdout
+        r = subprocess.run([exe, "-n", "10"], capture_output=True, text=True, timeout=30)
+        assert r.returncode == 255  # -f missing
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["tiny", "rmat10", "rmat12"])
+def test_driver_matches_reference_dumps(binaries, name, tmp_path):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    n = int(z["n"])
+    path = str(tmp_path / "g.bin")
+    z["pairs"].tofile(path)
+    f = ["-f", path, "-n", str(n)]
+    rank, out = run("eg_pagerank_simple", f + ["-m", "2", "-a", "1"], tmp_path, np.float32, n)
+    assert "Rank[0] = 0.15000" in out  # prev is never updated in pull mode
+    ref = z["pr_simple_pull"].astype(np.float64)
+    assert np.max(np.abs(rank - ref) / np.maximum(ref, 1e-30)) <= 2e-5
+    pr, _ = run("eg_prgrid_cilk", f + ["-m", "0"], tmp_path, np.float32, n)
+    ref = z["prgrid_m0"].astype(np.float64)
+    assert np.max(np.abs(pr - ref) / np.maximum(ref, 1e-30)) <= 2e-5
+    lv, _ = run("eg_bfs_simple", f + ["-m", "8"], tmp_path, np.int32, n)
+    np.testing.assert_array_equal(lv.astype(np.uint32), z["bfs_simple_m8"])
+    lv, _ = run("eg_bfs_simple", f + ["-m", "2", "-u"], tmp_path, np.int32, n)
+    np.testing.assert_array_equal(lv > 0, z["bfs_simple_m2u"] > 0)
+    for r in z["roots"]:
+        lv, _ = run("eg_bfsgrid_cilk", f + ["-m", "0", "-p", str(r)], tmp_path, np.int32, n)
+        np.testing.assert_array_equal(lv.astype(np.uint32), z["bfsgrid_m0_p%d" % r])
+        d, out = run("eg_sssp_pushpull", f + ["-m", "2", "-a", "1", "-r", "-p", str(r)], tmp_path, np.uint32, n)
+        np.testing.assert_array_equal(d, z["sssp_pull_p%d" % r])
+    for m, key, extra in (("2", "wcc_m2u", ["-u"]), ("0", "wcc_m0", []), ("8", "wcc_m8", [])):
+        lab, out = run("eg_wcc", f + ["-m", m] + extra, tmp_path, np.int64, n)
+        np.testing.assert_array_equal(lab, z[key])
+        assert "Total comp %d" % len(np.unique(lab)) in out
+    for args, key in ((["-m", "2", "-a", "1"], "spmv_pull"), (["-m", "2", "-a", "0"], "spmv_push"),
+                      (["-m", "8"], "spmv_m8")):
+        y, _ = run("eg_spmv", f + args, tmp_path, np.uint32, n)
+        np.testing.assert_array_equal(y, z[key])
+
+
+@pytest.mark.gpu
+def test_driver_rejects_bad_inputs(binaries, tmp_path):
+    bad = str(tmp_path / "odd.bin")
+    with open(bad, "wb") as fh:
+        fh.write(b"\x00" * 12)  # not a whole number of 8-byte records
+    r = subprocess.run([os.path.join(BIN, "eg_wcc"), "-f", bad, "-n", "4", "-m", "2"], capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode == 1 and "multiple of 8" in r.stderr
+    rng = str(tmp_path / "range.bin")
+    np.array([0, 1, 1, 7], np.uint32).tofile(rng)
+    r = subprocess.run([os.path.join(BIN, "eg_wcc"), "-f", rng, "-n", "4", "-m", "2"], capture_output=True, text=True,
+                       timeout=60)
+    assert r.returncode == 1 and ">= n" in r.stderr

@@ -118,3 +118,16 @@ def test_milli_floor_equals_integer_division():
     xs = xs[xs < 2**32].astype(np.uint64)
     scaled = np.floor(0.001 * xs.astype(np.float64)).astype(np.uint64)
     np.testing.assert_array_equal(scaled, xs // 1000)
+
+
+def test_parallel_ports(case):
+    # the multi-threaded ports used as the timed CPU baseline agree with the
+    # reference dumps too
+    name, n, pairs, rec = case
+    adj = oracle.build_adj(n, pairs)
+    for r in rec["roots"]:
+        lv = oracle.bfs_do(adj.out_ptr, adj.out_col, adj.in_ptr, adj.in_col, int(r))
+        np.testing.assert_array_equal(lv.astype(np.uint32), rec["bfsgrid_m0_p%d" % r])
+    adju = oracle.build_adj(n, pairs, undirected=True)
+    comp, rounds = oracle.wcc_lp(adju.out_ptr, adju.out_col)
+    np.testing.assert_array_equal(comp, rec["wcc_m2u"])
