@@ -9,11 +9,11 @@
 // Inside a CTA: row ends and entry values (gathered through col) are staged in
 // shared memory with coalesced 128-bit loads of col; every thread then walks
 // IPT consecutive items sequentially.  A row split between threads is summed
-// by the thread that sees its end, walking back over the partial sums of the
-// threads before it (fixed order, so results are deterministic).  A row split
-// between CTAs is finished by a fix-up kernel that adds the CTAs' partials in
-// CTA order.  Completed rows are written out by all threads in row order
-// (coalesced).
+// with a segmented scan over the threads' open-row partials (warp shuffles,
+// then across warps); a row split between CTAs is finished by a fix-up kernel
+// whose warps add the preceding CTAs' partials 32 at a time.  All reduction
+// orders are fixed, so results are deterministic.  Completed rows are written
+// out by all threads in row order (coalesced).
 //
 // The Op supplies: value type V, accumulator A,
 //   V gather(j, u)            value of entry j whose column is u
@@ -33,6 +33,33 @@ struct eg_mp_carry {
     A tail_val;         // this CTA's partial of tail_row
 };
 
+
+// Warp shuffles for the accumulator types (float, float2, double, uint32_t).
+template <class A>
+__device__ __forceinline__ A eg_shfl_up(A v, int off) {
+    return __shfl_up_sync(EG_FULL_MASK, v, off);
+}
+template <>
+__device__ __forceinline__ float2 eg_shfl_up<float2>(float2 v, int off) {
+    return make_float2(__shfl_up_sync(EG_FULL_MASK, v.x, off), __shfl_up_sync(EG_FULL_MASK, v.y, off));
+}
+template <class A>
+__device__ __forceinline__ A eg_shfl_down(A v, int off) {
+    return __shfl_down_sync(EG_FULL_MASK, v, off);
+}
+template <>
+__device__ __forceinline__ float2 eg_shfl_down<float2>(float2 v, int off) {
+    return make_float2(__shfl_down_sync(EG_FULL_MASK, v.x, off), __shfl_down_sync(EG_FULL_MASK, v.y, off));
+}
+template <class A>
+__device__ __forceinline__ A eg_shfl_idx(A v, int src) {
+    return __shfl_sync(EG_FULL_MASK, v, src);
+}
+template <>
+__device__ __forceinline__ float2 eg_shfl_idx<float2>(float2 v, int src) {
+    return make_float2(__shfl_sync(EG_FULL_MASK, v.x, src), __shfl_sync(EG_FULL_MASK, v.y, src));
+}
+
 __global__ void k_mp_schedule(const uint32_t *__restrict__ ptr, uint32_t n, uint32_t m, uint32_t items,
                               uint32_t ntiles, uint2 *__restrict__ coord);
 
@@ -44,8 +71,7 @@ struct eg_mp_smem {
     static constexpr size_t sum_off = (val_off + W * sizeof(V) + 15) & ~(size_t)15;
     static constexpr size_t cval_off = (sum_off + W * sizeof(A) + 15) & ~(size_t)15;
     static constexpr size_t crow_off = (cval_off + T * sizeof(A) + 15) & ~(size_t)15;
-    static constexpr size_t ccont_off = crow_off + T * 4;
-    static constexpr size_t bytes = (ccont_off + T + 15) & ~(size_t)15;
+    static constexpr size_t bytes = (crow_off + T * 4 + 15) & ~(size_t)15;
 };
 
 template <class Op, int T, int IPT, bool REDUCE>
@@ -63,10 +89,11 @@ __global__ void __launch_bounds__(T) k_mp_rows(const uint32_t *__restrict__ ptr,
     A *s_sum = (A *)(smem + L::sum_off);
     A *s_cval = (A *)(smem + L::cval_off);
     uint32_t *s_crow = (uint32_t *)(smem + L::crow_off);
-    unsigned char *s_ccont = smem + L::ccont_off;
     __shared__ uint32_t s_head;
     __shared__ A s_headval;
     __shared__ double2 s_red[T / 32];
+    __shared__ uint32_t s_wkey[T / 32], s_wfirst[T / 32];
+    __shared__ A s_wval[T / 32];
 
     if (!op.active()) return;
     op.setup();
@@ -134,42 +161,54 @@ __global__ void __launch_bounds__(T) k_mp_rows(const uint32_t *__restrict__ ptr,
             }
         }
     }
+    // Segmented inclusive scan of the threads' open-row partials, keyed by the
+    // open row (keys never decrease with the thread index, so equal keys form
+    // one run).  Fixed shuffle order: deterministic.
+    const uint32_t lane = tid & 31, warp = tid >> 5;
+    A v = acc;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const A pv = eg_shfl_up(v, off);
+        const uint32_t pk = __shfl_up_sync(EG_FULL_MASK, it, off);
+        if (lane >= (uint32_t)off && pk == it) v = op.merge(pv, v);
+    }
+    const uint32_t first_key = __shfl_sync(EG_FULL_MASK, it, 0);
+    if (lane == 31) {
+        s_wkey[warp] = it;
+        s_wval[warp] = v;
+        s_wfirst[warp] = first_key;
+    }
+    __syncthreads();
+    {
+        A ext = op.zero();
+        bool has = false;
+        for (int w2 = (int)warp - 1; w2 >= 0; w2--) {
+            if (s_wkey[w2] != it) break;
+            ext = has ? op.merge(s_wval[w2], ext) : s_wval[w2];
+            has = true;
+            if (s_wfirst[w2] != it) break;
+        }
+        if (has) v = op.merge(ext, v);
+    }
     s_crow[tid] = it;
-    s_cval[tid] = acc;
-    s_ccont[tid] = (it == it_start) && start_cont;
+    s_cval[tid] = v;
     __syncthreads();
 
-    // finish the first row of this thread if earlier threads hold parts of it
+    // finish this thread's first row if earlier threads hold parts of it; a
+    // row that began before the CTA is finished by the fix-up kernel
     if (first_row != EG_MP_NONE) {
         A tot = first_part;
-        int k = (int)tid - 1;
-        bool head = false;
-        for (;;) {
-            if (k < 0) {
-                head = true;
-                break;
-            }
-            tot = op.merge(s_cval[k], tot);
-            if (!s_ccont[k]) break;
-            k--;
-        }
-        if (head) {
-            s_head = first_row;  // always local row 0
+        if (tid > 0 && s_crow[tid - 1] == first_row) tot = op.merge(s_cval[tid - 1], tot);
+        if (first_row == 0 && rs0 < j0) {
+            s_head = 0;
             s_headval = tot;
         } else {
             s_sum[first_row] = tot;
         }
     }
-    // the last thread collects the partial of the row left open at the CTA end
     if (tid == T - 1) {
-        A tot = s_cval[T - 1];
-        int k = T - 1;
-        while (s_ccont[k] && k > 0) {
-            k--;
-            tot = op.merge(s_cval[k], tot);
-        }
         carry[c].tail_row = i0 + nrows;
-        carry[c].tail_val = tot;
+        carry[c].tail_val = v;
     }
     __syncthreads();
     if (tid == 0) {
@@ -205,35 +244,46 @@ __global__ void __launch_bounds__(T) k_mp_rows(const uint32_t *__restrict__ ptr,
     }
 }
 
-// One thread per CTA: completes rows that span CTAs (CTA order, deterministic).
+// One warp per CTA with a head row: completes rows that span CTAs by adding
+// the tail partials of the preceding CTAs, 32 CTAs per step (lanes in CTA
+// order, a fixed shuffle tree: deterministic).
 template <class Op, bool REDUCE>
 __global__ void k_mp_fixup(const uint32_t *__restrict__ ptr, const uint2 *__restrict__ coord, uint32_t ntiles,
                            const eg_mp_carry<typename Op::A> *__restrict__ carry, double2 *__restrict__ part, Op op) {
     using A = typename Op::A;
-    __shared__ double2 s_red[8];
+    __shared__ double2 s_red[32];
     if (!op.active()) return;
     op.setup();
-    uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     double2 red = make_double2(0.0, 0.0);
     if (c < ntiles) {
-        uint32_t row = carry[c].head_row;
+        const uint32_t row = carry[c].head_row;
         if (row != EG_MP_NONE) {
             A tot = carry[c].head_val;
             const uint32_t rstart = ptr[row];
-            for (int k = (int)c - 1; k >= 0; k--) {
-                tot = op.merge(carry[k].tail_val, tot);
-                if (rstart >= coord[k].y) break;  // the row begins inside CTA k
+            for (int base = (int)c - 1; base >= 0; base -= 32) {
+                const int k = base - (int)lane;
+                const bool valid = k >= 0;
+                const bool began = valid && rstart >= coord[k].y;  // the row begins inside CTA k
+                const uint32_t stop_mask = __ballot_sync(EG_FULL_MASK, began || !valid);
+                const int last = stop_mask ? __ffs(stop_mask) - 1 : 31;  // lanes 0..last contribute
+                A x = (valid && (int)lane <= last) ? carry[k].tail_val : op.zero();
+                // reduce lanes 0..31 (zeros past `last`) in a fixed tree, far-to-near order
+#pragma unroll
+                for (int off = 16; off > 0; off >>= 1) {
+                    const A y = eg_shfl_down(x, off);
+                    x = op.merge(y, x);
+                }
+                x = eg_shfl_idx(x, 0);
+                tot = op.merge(x, tot);
+                if (stop_mask) break;
             }
-            red = op.emit(row, tot);
+            if (lane == 0) red = op.emit(row, tot);
         }
     }
     if (REDUCE) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            red.x += __shfl_down_sync(EG_FULL_MASK, red.x, o);
-            red.y += __shfl_down_sync(EG_FULL_MASK, red.y, o);
-        }
-        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = red;
+        if (lane == 0) s_red[threadIdx.x >> 5] = red;
         __syncthreads();
         if (threadIdx.x == 0) {
             double2 s = make_double2(0.0, 0.0);

@@ -181,7 +181,7 @@ static int mp_launch(eg_graph *g, eg_adj &adj, eg_mp_sched &s, eg_buf &carry_buf
     kern<<<s.ntiles, EG_MP_T, L::bytes, ctx->stream>>>(bp<uint32_t>(adj.ptr), bp<uint32_t>(adj.col), g->n,
                                                       bp<uint2>(s.coord), bp<eg_mp_carry<A>>(carry_buf), part, op);
     EG_LAUNCHED(ctx);
-    uint32_t fb = eg_div_up(s.ntiles, 256);
+    uint32_t fb = eg_div_up((uint64_t)s.ntiles * 32, 256);
     k_mp_fixup<Op, REDUCE><<<fb, 256, 0, ctx->stream>>>(bp<uint32_t>(adj.ptr), bp<uint2>(s.coord), s.ntiles,
                                                        bp<eg_mp_carry<A>>(carry_buf), part ? part + s.ntiles : nullptr,
                                                        op);
@@ -205,7 +205,7 @@ extern "C" void eg_pr_opts_default(eg_pr_opts *o) {
 template <bool COMP, bool REDUCE>
 static int pr_iterations(eg_graph *g, const eg_pr_opts &o, eg_pr_dev *st, double2 *part, eg_buf &carry) {
     eg_ctx *ctx = g->ctx;
-    uint32_t nparts = g->sched_csc.ntiles + eg_div_up(g->sched_csc.ntiles, 256);
+    uint32_t nparts = g->sched_csc.ntiles + eg_div_up((uint64_t)g->sched_csc.ntiles * 32, 256);
     for (int it = 0; it < o.iterations; it++) {
         PrOp<COMP> op;
         bool odd = o.swap && (it & 1);
@@ -239,7 +239,7 @@ extern "C" int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out,
     const uint32_t n = g->n;
     EG_TRY(eg_build_sched(g, g->csc, g->sched_csc, EG_MP_T * EG_MP_IPT));
     const uint32_t ntiles = g->sched_csc.ntiles;
-    const uint32_t nparts = ntiles + eg_div_up(ntiles, 256);
+    const uint32_t nparts = ntiles + eg_div_up((uint64_t)ntiles * 32, 256);
     EG_TRY(eg_buf_ensure(ctx, g->rank, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->contrib0, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->contrib1, (uint64_t)n * 4));
