@@ -97,6 +97,7 @@ SIGNATURES = {
     "eg_sssp_multi": (c_int, [c_void_p, c_void_p, c_int, P(Weights), c_void_p, P(SsspStats)]),
     "eg_wcc": (c_int, [c_void_p, c_void_p, P(WccStats)]),
     "eg_sample_roots": (c_int, [c_void_p, c_int, c_u64, c_void_p]),
+    "eg_spmv_f32_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_u32, c_u64, c_void_p]),
 }
 
 _lib = None

@@ -241,6 +241,26 @@ typedef struct {
 } eg_wcc_stats;
 int eg_wcc(eg_graph *g, int64_t *labels_out, eg_wcc_stats *stats);
 
+/* ---- allocation-free SpMV ------------------------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory (a host callback, a plug-in inside a process whose allocator it does
+ * not own, a service that has handed HBM to its own pool): y[v] = sum over
+ * entries p of row v of vals[p] * x[col[p]] (fp32, vals NULL = all ones)
+ * over a caller-owned CSR-shaped array pair in device memory.  All pointers
+ * are device pointers; stream is a cudaStream_t (NULL = legacy default).
+ * The call allocates nothing: its scratch is a fixed 1.5 MiB array compiled
+ * into the library, held by every GPU that loads it until the process exits,
+ * which limits n + m to EG_NOALLOC_MAX_ITEMS (larger inputs are rejected
+ * with EG_EINVAL).  The first call on a device looks that array up with
+ * cudaGetSymbolAddress; make that first call before any stream capture.
+ * Every call on a device shares the array (it keeps the last call's
+ * contents; each call writes all it reads), so calls that overlap on the GPU
+ * race: serialise them on one stream.  Results equal eg_spmv's EG_SPMV_F32
+ * row sums (same kernel, same schedule). */
+#define EG_NOALLOC_MAX_ITEMS (65536ull * 2048ull)
+int eg_spmv_f32_noalloc(const uint32_t *d_ptr, const uint32_t *d_col, const float *d_vals, const float *d_x,
+                        float *d_y, uint32_t n, uint64_t m, void *stream);
+
 /* Samples k roots uniformly from vertices with out-degree > 0 (the same
  * counter-based rule as the CPU generator). */
 int eg_sample_roots(eg_graph *g, int k, uint64_t seed, uint32_t *roots_out);
