@@ -21,17 +21,40 @@ struct BfsCounters {
     unsigned long long next_deg;  // sum of out-degrees of the new frontier
     uint32_t next_count;          // vertices in the new frontier
     uint32_t qsize;               // entries in the next queue
+    uint32_t nbig;                // frontier vertices deferred to the cooperative kernel
+    uint32_t pad;
 };
 
-__device__ __forceinline__ void warp_add_counters(BfsCounters *c, uint32_t cnt, unsigned long long deg) {
+// Frontier vertices with more out-edges than this are expanded by the whole
+// grid (k_bfs_push_big) instead of one warp: an RMAT hub has 10^5..10^6.
+#define EG_BFS_BIG_DEG 2048u
+
+// Block-level reduction of per-thread counters: one atomic per block.
+__device__ __forceinline__ void block_add_counters(BfsCounters *c, uint32_t cnt, unsigned long long deg) {
+    __shared__ uint32_t s_cnt[32];
+    __shared__ unsigned long long s_deg[32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
         cnt += __shfl_down_sync(EG_FULL_MASK, cnt, o);
         deg += __shfl_down_sync(EG_FULL_MASK, deg, o);
     }
-    if ((threadIdx.x & 31) == 0 && cnt) {
-        atomicAdd(&c->next_count, cnt);
-        atomicAdd(&c->next_deg, deg);
+    const int w = threadIdx.x >> 5;
+    if ((threadIdx.x & 31) == 0) {
+        s_cnt[w] = cnt;
+        s_deg[w] = deg;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t tc = 0;
+        unsigned long long td = 0;
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+            tc += s_cnt[i];
+            td += s_deg[i];
+        }
+        if (tc) {
+            atomicAdd(&c->next_count, tc);
+            atomicAdd(&c->next_deg, td);
+        }
     }
 }
 
@@ -55,48 +78,101 @@ __global__ void k_bfs_init(uint32_t n, int32_t *level, int32_t *parent, uint32_t
     }
 }
 
+// Claims v for the next level if it is unvisited (atomicOr on its visited
+// bit); returns true for the one thread that set the bit.
+__device__ __forceinline__ bool bfs_claim(uint32_t v, uint32_t u, uint32_t *visited, uint32_t *next_bm, int32_t *level,
+                                          int32_t *parent, int32_t next_level) {
+    const uint32_t bit = 1u << (v & 31);
+    if (__ldcg(visited + (v >> 5)) & bit) return false;
+    const uint32_t old = atomicOr(visited + (v >> 5), bit);
+    if (old & bit) return false;
+    level[v] = next_level;
+    if (parent) parent[v] = (int32_t)u;
+    atomicOr(next_bm + (v >> 5), bit);
+    return true;
+}
+
+// Appends the claimed vertices of a warp to the next queue (one atomic per warp).
+__device__ __forceinline__ void warp_append(bool claimed, uint32_t v, uint32_t *next_queue, BfsCounters *cnt,
+                                            const uint32_t *__restrict__ deg, uint32_t &my_cnt,
+                                            unsigned long long &my_deg) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t ball = __ballot_sync(EG_FULL_MASK, claimed);
+    if (ball) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&cnt->qsize, __popc(ball));
+        base = __shfl_sync(EG_FULL_MASK, base, 0);
+        if (claimed) {
+            next_queue[base + __popc(ball & eg_lanemask_lt())] = v;
+            my_cnt++;
+            my_deg += deg[v];
+        }
+    }
+}
+
 // Top-down step: one warp per frontier vertex, lanes over its out-list.
-// A vertex is claimed by the atomicOr that sets its visited bit.
+// Vertices with more than EG_BFS_BIG_DEG out-edges go to a side list that
+// k_bfs_push_big expands with every thread of the grid.
 __global__ void __launch_bounds__(256) k_bfs_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
                                                   const uint32_t *__restrict__ deg, const uint32_t *__restrict__ queue,
                                                   uint32_t qlen, uint32_t *visited, uint32_t *next_bm,
                                                   uint32_t *next_queue, int32_t *level, int32_t *parent,
-                                                  int32_t next_level, BfsCounters *cnt) {
+                                                  int32_t next_level, BfsCounters *cnt, uint32_t *big) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t lt = eg_lanemask_lt();
+    uint32_t my_cnt = 0;
+    unsigned long long my_deg = 0;
+    // uniform trip count per warp (qi is the same for all lanes)
     for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < qlen; qi += warps) {
         const uint32_t u = queue[qi];
         const uint32_t b = ptr[u], e = ptr[u + 1];
+        if (e - b > EG_BFS_BIG_DEG) {
+            if (lane == 0) big[atomicAdd(&cnt->nbig, 1u)] = u;
+            continue;
+        }
         for (uint32_t p0 = b; p0 < e; p0 += 32) {
             const uint32_t p = p0 + lane;
             bool claimed = false;
             uint32_t v = 0;
             if (p < e) {
                 v = col[p];
-                const uint32_t bit = 1u << (v & 31);
-                if (!(__ldcg(visited + (v >> 5)) & bit)) {
-                    uint32_t old = atomicOr(visited + (v >> 5), bit);
-                    if (!(old & bit)) {
-                        claimed = true;
-                        level[v] = next_level;
-                        if (parent) parent[v] = (int32_t)u;
-                        atomicOr(next_bm + (v >> 5), bit);
-                    }
-                }
+                claimed = bfs_claim(v, u, visited, next_bm, level, parent, next_level);
             }
-            const uint32_t ball = __ballot_sync(EG_FULL_MASK, claimed);
-            if (ball) {
-                uint32_t base = 0;
-                if (lane == 0) base = atomicAdd(&cnt->qsize, __popc(ball));
-                base = __shfl_sync(EG_FULL_MASK, base, 0);
-                if (claimed) next_queue[base + __popc(ball & lt)] = v;
-                unsigned long long d = claimed ? deg[v] : 0ull;
-                uint32_t c = claimed ? 1u : 0u;
-                warp_add_counters(cnt, c, d);
-            }
+            warp_append(claimed, v, next_queue, cnt, deg, my_cnt, my_deg);
         }
     }
+    block_add_counters(cnt, my_cnt, my_deg);
+}
+
+// Expands the deferred high-degree frontier vertices: all threads of the
+// grid stride over each one's out-list in turn.
+__global__ void __launch_bounds__(256) k_bfs_push_big(const uint32_t *__restrict__ ptr,
+                                                      const uint32_t *__restrict__ col,
+                                                      const uint32_t *__restrict__ deg, const uint32_t *big,
+                                                      uint32_t *visited, uint32_t *next_bm, uint32_t *next_queue,
+                                                      int32_t *level, int32_t *parent, int32_t next_level,
+                                                      BfsCounters *cnt) {
+    const uint32_t nbig = *(volatile uint32_t *)&cnt->nbig;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nthreads = gridDim.x * blockDim.x;
+    uint32_t my_cnt = 0;
+    unsigned long long my_deg = 0;
+    for (uint32_t bi = 0; bi < nbig; bi++) {
+        const uint32_t u = big[bi];
+        const uint32_t b = ptr[u], e = ptr[u + 1];
+        // warp-uniform trip count: each warp covers 32 consecutive entries
+        for (uint32_t p0 = b + (tid & ~31u); p0 < e; p0 += nthreads) {
+            const uint32_t p = p0 + (threadIdx.x & 31);
+            bool claimed = false;
+            uint32_t v = 0;
+            if (p < e) {
+                v = col[p];
+                claimed = bfs_claim(v, u, visited, next_bm, level, parent, next_level);
+            }
+            warp_append(claimed, v, next_queue, cnt, deg, my_cnt, my_deg);
+        }
+    }
+    block_add_counters(cnt, my_cnt, my_deg);
 }
 
 // Bottom-up step: one thread per vertex, warps over 32 consecutive vertices
@@ -110,6 +186,8 @@ __global__ void __launch_bounds__(256) k_bfs_pull(const uint32_t *__restrict__ p
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t nw = (n + 31) >> 5;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    uint32_t my_cnt = 0;
+    unsigned long long my_deg = 0;
     for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += warps) {
         const uint32_t vis = visited[w];
         if (vis == EG_FULL_MASK) {
@@ -135,24 +213,52 @@ __global__ void __launch_bounds__(256) k_bfs_pull(const uint32_t *__restrict__ p
             next_bm[w] = ball;
             if (ball) visited[w] = vis | ball;
         }
-        if (ball) warp_add_counters(cnt, found ? 1u : 0u, found ? (unsigned long long)deg[v] : 0ull);
+        if (found) {
+            my_cnt++;
+            my_deg += deg[v];
+        }
     }
+    block_add_counters(cnt, my_cnt, my_deg);
 }
 
-// Bitmap -> id queue (ballot/popc compaction, one warp-aggregated atomic per word).
-__global__ void k_bm_to_queue(const uint32_t *__restrict__ bm, uint32_t n, uint32_t *queue, BfsCounters *cnt) {
-    const uint32_t lane = threadIdx.x & 31;
+// Bitmap -> id queue: each thread owns one word, a block-wide exclusive scan
+// of the words' popcounts places them, one atomic per block reserves space.
+__global__ void __launch_bounds__(256) k_bm_to_queue(const uint32_t *__restrict__ bm, uint32_t n, uint32_t *queue,
+                                                     BfsCounters *cnt) {
+    __shared__ uint32_t s_warp[8];
+    __shared__ uint32_t s_base;
     const uint32_t nw = (n + 31) >> 5;
-    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t lt = eg_lanemask_lt();
-    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += warps) {
-        const uint32_t word = bm[w];
-        if (!word) continue;
-        const bool on = (word >> lane) & 1u;
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(&cnt->qsize, __popc(word));
-        base = __shfl_sync(EG_FULL_MASK, base, 0);
-        if (on) queue[base + __popc(word & lt)] = (w << 5) + lane;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t w0 = blockIdx.x * blockDim.x; w0 < nw; w0 += gridDim.x * blockDim.x) {
+        const uint32_t w = w0 + threadIdx.x;
+        const uint32_t word = w < nw ? bm[w] : 0u;
+        const uint32_t c = __popc(word);
+        uint32_t x = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(EG_FULL_MASK, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31) s_warp[warp] = x;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (int i = 0; i < 8; i++) {
+                const uint32_t v = s_warp[i];
+                s_warp[i] = t;
+                t += v;
+            }
+            s_base = t ? atomicAdd(&cnt->qsize, t) : 0u;
+        }
+        __syncthreads();
+        uint32_t pos = s_base + s_warp[warp] + x - c;
+        uint32_t bits = word;
+        while (bits) {
+            const int b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            queue[pos++] = (w << 5) + (uint32_t)b;
+        }
+        __syncthreads();
     }
 }
 
@@ -190,12 +296,13 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
     const bool want_parent = parent_out != nullptr;
     EG_TRY(eg_buf_ensure(ctx, g->level, (uint64_t)n * 4));
     if (want_parent) EG_TRY(eg_buf_ensure(ctx, g->parent, (uint64_t)n * 4));
-    // work: visited | bm0 | bm1 | queue0 | queue1 | counters
+    // work: visited | bm0 | bm1 | queue0 | queue1 | big list | counters
     const uint64_t off_bm0 = (uint64_t)nw, off_bm1 = 2ull * nw, off_q0 = 3ull * nw, off_q1 = off_q0 + n,
-                   off_cnt = (off_q1 + n + 7) & ~7ull;
+                   off_big = off_q1 + n, off_cnt = (off_big + n + 7) & ~7ull;
     EG_TRY(eg_buf_ensure(ctx, g->bfs_work, (off_cnt + 8) * 4));
     uint32_t *wk = bp<uint32_t>(g->bfs_work);
     uint32_t *visited = wk, *bm[2] = {wk + off_bm0, wk + off_bm1}, *q[2] = {wk + off_q0, wk + off_q1};
+    uint32_t *big = wk + off_big;
     BfsCounters *cnt = reinterpret_cast<BfsCounters *>(wk + off_cnt);
     int32_t *level = bp<int32_t>(g->level);
     int32_t *parent = want_parent ? bp<int32_t>(g->parent) : nullptr;
@@ -242,8 +349,14 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
             EG_CUDA(cudaMemsetAsync(bm[nxt], 0, (uint64_t)nw * 4, ctx->stream));
             k_bfs_push<<<blocks_for(ctx, (uint64_t)qlen * 32), 256, 0, ctx->stream>>>(
                 bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, q[cur], qlen, visited, bm[nxt], q[nxt], level,
-                parent, lvl + 1, cnt);
+                parent, lvl + 1, cnt, big);
             EG_LAUNCHED(ctx);
+            if (fdeg > EG_BFS_BIG_DEG) {  // a frontier vertex may exceed the threshold
+                k_bfs_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, ctx->stream>>>(
+                    bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, big, visited, bm[nxt], q[nxt], level,
+                    parent, lvl + 1, cnt);
+                EG_LAUNCHED(ctx);
+            }
             have_queue = true;
         }
         EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(BfsCounters), cudaMemcpyDeviceToHost, ctx->stream));
@@ -279,7 +392,7 @@ struct MsCounters {
     unsigned long long tdeg;  // sum over new (vertex, source) pairs of the vertex's out-degree
     unsigned long long disc;  // new (vertex, source) pairs
     uint32_t count;           // vertices with a nonzero new word
-    uint32_t pad;
+    uint32_t nbig;            // frontier vertices deferred to k_ms_push_big
 };
 
 __global__ void k_ms_init(uint32_t n, unsigned long long *seen, unsigned long long *front) {
@@ -323,18 +436,46 @@ __global__ void __launch_bounds__(256) k_ms_pull(const uint32_t *__restrict__ pt
     }
 }
 
-// Push: one warp per vertex with a nonzero frontier word.
+// Push: one warp per vertex with a nonzero frontier word; vertices with more
+// than EG_BFS_BIG_DEG out-edges go to a side list for k_ms_push_big.
 __global__ void __launch_bounds__(256) k_ms_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
                                                  const uint32_t *__restrict__ queue, uint32_t qlen,
                                                  const unsigned long long *__restrict__ seen,
                                                  const unsigned long long *__restrict__ front,
-                                                 unsigned long long *__restrict__ next) {
+                                                 unsigned long long *__restrict__ next, uint32_t *big,
+                                                 MsCounters *cnt) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < qlen; qi += warps) {
         const uint32_t u = queue[qi];
+        const uint32_t b = ptr[u], e = ptr[u + 1];
+        if (e - b > EG_BFS_BIG_DEG) {
+            if (lane == 0) big[atomicAdd(&cnt->nbig, 1u)] = u;
+            continue;
+        }
         const unsigned long long f = front[u];
-        for (uint32_t p = ptr[u] + lane; p < ptr[u + 1]; p += 32) {
+        for (uint32_t p = b + lane; p < e; p += 32) {
+            const uint32_t v = col[p];
+            const unsigned long long add = f & ~__ldcg(seen + v);
+            if (add && (__ldcg(next + v) & add) != add) atomicOr(next + v, add);
+        }
+    }
+}
+
+// The deferred high-degree frontier vertices: every thread of the grid
+// strides over each one's out-list in turn.
+__global__ void __launch_bounds__(256) k_ms_push_big(const uint32_t *__restrict__ ptr,
+                                                     const uint32_t *__restrict__ col, const uint32_t *big,
+                                                     const unsigned long long *__restrict__ seen,
+                                                     const unsigned long long *__restrict__ front,
+                                                     unsigned long long *__restrict__ next, const MsCounters *cnt) {
+    const uint32_t nbig = *(volatile const uint32_t *)&cnt->nbig;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nthreads = gridDim.x * blockDim.x;
+    for (uint32_t bi = 0; bi < nbig; bi++) {
+        const uint32_t u = big[bi];
+        const unsigned long long f = front[u];
+        for (uint32_t p = ptr[u] + tid; p < ptr[u + 1]; p += nthreads) {
             const uint32_t v = col[p];
             const unsigned long long add = f & ~__ldcg(seen + v);
             if (add && (__ldcg(next + v) & add) != add) atomicOr(next + v, add);
@@ -407,14 +548,15 @@ extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *
     eg_ctx *ctx = g->ctx;
     EG_CUDA(cudaSetDevice(ctx->device));
     const uint32_t n = g->n;
-    // work: seen | front | next (u64 each) | queue (u32) | roots | counters
+    // work: seen | front | next (u64 each) | queue (u32) | big list (u32) | roots | counters
     const uint64_t words = 3ull * n;
-    const uint64_t bytes = words * 8 + (uint64_t)n * 4 + 64 * 4 + 64;
+    const uint64_t bytes = words * 8 + 2ull * n * 4 + 64 * 4 + 64;
     EG_TRY(eg_buf_ensure(ctx, g->msbfs_work, bytes));
     unsigned long long *seen = bp<unsigned long long>(g->msbfs_work);
     unsigned long long *front = seen + n, *next = seen + 2ull * n;
     uint32_t *queue = reinterpret_cast<uint32_t *>(seen + 3ull * n);
-    uint32_t *d_roots = queue + n;
+    uint32_t *big = queue + n;
+    uint32_t *d_roots = big + n;
     MsCounters *cnt = reinterpret_cast<MsCounters *>(d_roots + 64);
     int32_t *levels = nullptr;
     if (levels_out) {
@@ -458,6 +600,7 @@ extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *
     const double threshold = (double)g->m / 20.0;
     while (count > 0) {
         const bool pull = (double)count + (double)fdeg > threshold;
+        EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(MsCounters), ctx->stream));
         if (pull) {
             k_ms_pull<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col),
                                                                   n, all, seen, front, next);
@@ -465,10 +608,14 @@ extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *
             pull_levels++;
         } else {
             k_ms_push<<<blocks_for(ctx, (uint64_t)count * 32), 256, 0, ctx->stream>>>(
-                bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), queue, count, seen, front, next);
+                bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), queue, count, seen, front, next, big, cnt);
             EG_LAUNCHED(ctx);
+            if (fdeg > EG_BFS_BIG_DEG) {
+                k_ms_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, ctx->stream>>>(
+                    bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), big, seen, front, next, cnt);
+                EG_LAUNCHED(ctx);
+            }
         }
-        EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(MsCounters), ctx->stream));
         // after a push the next words were accumulated with atomics and must be
         // cleared for the following level; after a pull they are overwritten
         k_ms_fold<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(n, k, seen, front, next, 1, levels, lvl + 1, deg, queue,

@@ -32,8 +32,12 @@ struct WRule {
 struct SsspCounters {
     unsigned long long relax;  // entries scanned
     uint32_t qsize;
-    uint32_t pad;
+    uint32_t nbig;  // frontier vertices deferred to the grid-wide kernel
 };
+
+// Frontier vertices with more out-edges than this are relaxed by the whole
+// grid instead of one warp (RMAT hubs have 10^5..10^6 out-edges).
+#define EG_SSSP_BIG_DEG 2048u
 
 __global__ void k_sssp_init(uint32_t n, uint32_t *dist, uint32_t root, uint32_t *queue, SsspCounters *cnt) {
     uint32_t stride = gridDim.x * blockDim.x;
@@ -47,18 +51,72 @@ __global__ void k_sssp_init(uint32_t n, uint32_t *dist, uint32_t root, uint32_t 
 
 // One warp per frontier vertex; lanes relax its out-edges.  A vertex whose
 // distance drops is queued once per round (claimed through the next bitmap).
+__device__ __forceinline__ bool sssp_relax(uint32_t u, uint32_t du, uint32_t v, const WRule &w, uint32_t *dist,
+                                           uint32_t *next_bm) {
+    if (v == u) return false;  // self-loops skipped (sssp_pushpull.c:80)
+    const uint64_t nd64 = (uint64_t)du + w(u, v);
+    const uint32_t nd = nd64 < EG_SSSP_INF ? (uint32_t)nd64 : EG_SSSP_INF;
+    if (nd >= __ldcg(dist + v)) return false;
+    const uint32_t old = atomicMin(dist + v, nd);
+    if (nd >= old) return false;
+    const uint32_t bit = 1u << (v & 31);
+    return !(atomicOr(next_bm + (v >> 5), bit) & bit);
+}
+
+__device__ __forceinline__ void sssp_append(bool q, uint32_t v, uint32_t *next_queue, SsspCounters *cnt) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t ball = __ballot_sync(EG_FULL_MASK, q);
+    if (ball) {
+        uint32_t base = 0;
+        if (lane == 0) base = atomicAdd(&cnt->qsize, __popc(ball));
+        base = __shfl_sync(EG_FULL_MASK, base, 0);
+        if (q) next_queue[base + __popc(ball & eg_lanemask_lt())] = v;
+    }
+}
+
+// Relaxes the deferred high-degree frontier vertices with every thread.
+__global__ void __launch_bounds__(256) k_sssp_push_big(const uint32_t *__restrict__ ptr,
+                                                       const uint32_t *__restrict__ col, const uint32_t *big,
+                                                       uint32_t *dist, uint32_t *next_bm, uint32_t *next_queue,
+                                                       WRule w, SsspCounters *cnt) {
+    const uint32_t nbig = *(volatile uint32_t *)&cnt->nbig;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nthreads = gridDim.x * blockDim.x;
+    unsigned long long scanned = 0;
+    for (uint32_t bi = 0; bi < nbig; bi++) {
+        const uint32_t u = big[bi];
+        const uint32_t du = __ldcg(dist + u);
+        const uint32_t b = ptr[u], e = ptr[u + 1];
+        if (tid == 0) scanned += e - b;
+        for (uint32_t p0 = b + (tid & ~31u); p0 < e; p0 += nthreads) {
+            const uint32_t p = p0 + (threadIdx.x & 31);
+            bool q = false;
+            uint32_t v = 0;
+            if (p < e) {
+                v = col[p];
+                q = sssp_relax(u, du, v, w, dist, next_bm);
+            }
+            sssp_append(q, v, next_queue, cnt);
+        }
+    }
+    if (scanned) atomicAdd(&cnt->relax, scanned);
+}
+
 __global__ void __launch_bounds__(256) k_sssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
                                                    const uint32_t *__restrict__ queue, uint32_t qlen, uint32_t *dist,
                                                    uint32_t *next_bm, uint32_t *next_queue, WRule w,
-                                                   SsspCounters *cnt) {
+                                                   SsspCounters *cnt, uint32_t *big) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    const uint32_t lt = eg_lanemask_lt();
     unsigned long long scanned = 0;
     for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < qlen; qi += warps) {
         const uint32_t u = queue[qi];
         const uint32_t du = __ldcg(dist + u);
         const uint32_t b = ptr[u], e = ptr[u + 1];
+        if (e - b > EG_SSSP_BIG_DEG) {
+            if (lane == 0) big[atomicAdd(&cnt->nbig, 1u)] = u;
+            continue;
+        }
         scanned += e - b;
         for (uint32_t p0 = b; p0 < e; p0 += 32) {
             const uint32_t p = p0 + lane;
@@ -66,25 +124,9 @@ __global__ void __launch_bounds__(256) k_sssp_push(const uint32_t *__restrict__ 
             uint32_t v = 0;
             if (p < e) {
                 v = col[p];
-                if (v != u) {  // self-loops skipped (sssp_pushpull.c:80)
-                    const uint64_t nd64 = (uint64_t)du + w(u, v);
-                    const uint32_t nd = nd64 < EG_SSSP_INF ? (uint32_t)nd64 : EG_SSSP_INF;
-                    if (nd < __ldcg(dist + v)) {
-                        const uint32_t old = atomicMin(dist + v, nd);
-                        if (nd < old) {
-                            const uint32_t bit = 1u << (v & 31);
-                            q = !(atomicOr(next_bm + (v >> 5), bit) & bit);
-                        }
-                    }
-                }
+                q = sssp_relax(u, du, v, w, dist, next_bm);
             }
-            const uint32_t ball = __ballot_sync(EG_FULL_MASK, q);
-            if (ball) {
-                uint32_t base = 0;
-                if (lane == 0) base = atomicAdd(&cnt->qsize, __popc(ball));
-                base = __shfl_sync(EG_FULL_MASK, base, 0);
-                if (q) next_queue[base + __popc(ball & lt)] = v;
-            }
+            sssp_append(q, v, next_queue, cnt);
         }
     }
     if (lane == 0 && scanned) atomicAdd(&cnt->relax, scanned);
@@ -143,10 +185,10 @@ extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wts, uint32
     const uint32_t n = g->n, nw = (n + 31) >> 5;
     const WRule w = make_rule(wts);
     EG_TRY(eg_buf_ensure(ctx, g->dist, (uint64_t)n * 4));
-    const uint64_t off_q0 = nw, off_q1 = off_q0 + n, off_cnt = (off_q1 + n + 7) & ~7ull;
+    const uint64_t off_q0 = nw, off_q1 = off_q0 + n, off_big = off_q1 + n, off_cnt = (off_big + n + 7) & ~7ull;
     EG_TRY(eg_buf_ensure(ctx, g->sssp_work, (off_cnt + 8) * 4));
     uint32_t *wk = bp<uint32_t>(g->sssp_work);
-    uint32_t *bm = wk, *q[2] = {wk + off_q0, wk + off_q1};
+    uint32_t *bm = wk, *q[2] = {wk + off_q0, wk + off_q1}, *big = wk + off_big;
     SsspCounters *cnt = reinterpret_cast<SsspCounters *>(wk + off_cnt);
     SsspCounters *h = (SsspCounters *)ctx->h_pinned;
     uint32_t *dist = bp<uint32_t>(g->dist);
@@ -159,9 +201,13 @@ extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wts, uint32
     unsigned long long relax = 0;
     while (qlen > 0) {
         const int nxt = cur ^ 1;
-        EG_CUDA(cudaMemsetAsync(&cnt->qsize, 0, 4, ctx->stream));
+        EG_CUDA(cudaMemsetAsync(&cnt->qsize, 0, 8, ctx->stream));  // qsize and nbig
         k_sssp_push<<<blocks_for(ctx, (uint64_t)qlen * 32), 256, 0, ctx->stream>>>(
-            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), q[cur], qlen, dist, bm, q[nxt], w, cnt);
+            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), q[cur], qlen, dist, bm, q[nxt], w, cnt, big);
+        EG_LAUNCHED(ctx);
+        k_sssp_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr),
+                                                                              bp<uint32_t>(g->csr.col), big, dist, bm,
+                                                                              q[nxt], w, cnt);
         EG_LAUNCHED(ctx);
         EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(SsspCounters), cudaMemcpyDeviceToHost, ctx->stream));
         EG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -223,11 +269,31 @@ __global__ void k_msssp_roots(const uint32_t *roots, int k, uint32_t kw, uint32_
     }
 }
 
+// Relaxes the 32 sources of word j of frontier vertex u (du_lane: this lane's
+// source distance at u) along edge u->v; queues v when a distance dropped.
+__device__ __forceinline__ void msssp_edge(uint32_t u, uint32_t v, uint32_t j, uint32_t s, bool on, uint32_t du,
+                                           int k, uint32_t kw, const WRule &w, uint32_t *dist, uint32_t *next_act,
+                                           uint32_t *next_inq, uint32_t *next_queue, SsspCounters *cnt) {
+    bool improved = false;
+    if (on && v != u) {
+        const uint64_t nd64 = (uint64_t)du + w(u, v);
+        const uint32_t nd = nd64 < EG_SSSP_INF ? (uint32_t)nd64 : EG_SSSP_INF;
+        uint32_t *dp = dist + (uint64_t)v * k + s;
+        if (nd < __ldcg(dp)) improved = nd < atomicMin(dp, nd);
+    }
+    const uint32_t ball = __ballot_sync(EG_FULL_MASK, improved);
+    if (ball && (threadIdx.x & 31) == 0) {
+        atomicOr(next_act + (uint64_t)v * kw + j, ball);
+        const uint32_t bit = 1u << (v & 31);
+        if (!(atomicOr(next_inq + (v >> 5), bit) & bit)) next_queue[atomicAdd(&cnt->qsize, 1u)] = v;
+    }
+}
+
 __global__ void __launch_bounds__(256) k_msssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
                                                     const uint32_t *__restrict__ queue, uint32_t qlen, int k,
                                                     uint32_t kw, uint32_t *dist, const uint32_t *__restrict__ act,
                                                     uint32_t *next_act, uint32_t *next_inq, uint32_t *next_queue,
-                                                    WRule w, SsspCounters *cnt) {
+                                                    WRule w, SsspCounters *cnt, uint32_t *big) {
     const uint32_t lane = threadIdx.x & 31;
     const uint64_t warps = (gridDim.x * blockDim.x) >> 5;
     unsigned long long scanned = 0;
@@ -237,30 +303,46 @@ __global__ void __launch_bounds__(256) k_msssp_push(const uint32_t *__restrict__
         const uint32_t j = (uint32_t)(it % kw);
         const uint32_t a = act[(uint64_t)u * kw + j];
         if (!a) continue;
+        const uint32_t b = ptr[u], e = ptr[u + 1];
+        if (e - b > EG_SSSP_BIG_DEG) {
+            if (lane == 0) big[atomicAdd(&cnt->nbig, 1u)] = (uint32_t)((uint64_t)u * kw + j);
+            continue;
+        }
+        const uint32_t s = j * 32 + lane;
+        const bool on = (a >> lane) & 1u;
+        const uint32_t du = on ? __ldcg(dist + (uint64_t)u * k + s) : EG_SSSP_INF;
+        if (lane == 0) scanned += (e - b) * (unsigned long long)__popc(a);
+        for (uint32_t p = b; p < e; p++)
+            msssp_edge(u, col[p], j, s, on, du, k, kw, w, dist, next_act, next_inq, next_queue, cnt);
+    }
+    if (lane == 0 && scanned) atomicAdd(&cnt->relax, scanned);
+}
+
+// The deferred (high-degree vertex, source word) items: every warp of the
+// grid takes every (total warps)-th edge of each item.
+__global__ void __launch_bounds__(256) k_msssp_push_big(const uint32_t *__restrict__ ptr,
+                                                        const uint32_t *__restrict__ col, int k, uint32_t kw,
+                                                        uint32_t *dist, const uint32_t *__restrict__ act,
+                                                        uint32_t *next_act, uint32_t *next_inq, uint32_t *next_queue,
+                                                        WRule w, SsspCounters *cnt, const uint32_t *big) {
+    const uint32_t nbig = *(volatile uint32_t *)&cnt->nbig;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    unsigned long long scanned = 0;
+    for (uint32_t bi = 0; bi < nbig; bi++) {
+        const uint32_t item = big[bi];
+        const uint32_t u = item / kw, j = item % kw;
+        const uint32_t a = act[(uint64_t)u * kw + j];
         const uint32_t s = j * 32 + lane;
         const bool on = (a >> lane) & 1u;
         const uint32_t du = on ? __ldcg(dist + (uint64_t)u * k + s) : EG_SSSP_INF;
         const uint32_t b = ptr[u], e = ptr[u + 1];
-        if (lane == 0) scanned += (e - b) * (unsigned long long)__popc(a);
-        for (uint32_t p = b; p < e; p++) {
-            const uint32_t v = col[p];
-            if (v == u) continue;
-            bool improved = false;
-            if (on) {
-                const uint64_t nd64 = (uint64_t)du + w(u, v);
-                const uint32_t nd = nd64 < EG_SSSP_INF ? (uint32_t)nd64 : EG_SSSP_INF;
-                uint32_t *dp = dist + (uint64_t)v * k + s;
-                if (nd < __ldcg(dp)) improved = nd < atomicMin(dp, nd);
-            }
-            const uint32_t ball = __ballot_sync(EG_FULL_MASK, improved);
-            if (ball && lane == 0) {
-                atomicOr(next_act + (uint64_t)v * kw + j, ball);
-                const uint32_t bit = 1u << (v & 31);
-                if (!(atomicOr(next_inq + (v >> 5), bit) & bit)) next_queue[atomicAdd(&cnt->qsize, 1u)] = v;
-            }
-        }
+        if (gw == 0 && lane == 0) scanned += (e - b) * (unsigned long long)__popc(a);
+        for (uint32_t p = b + gw; p < e; p += warps)
+            msssp_edge(u, col[p], j, s, on, du, k, kw, w, dist, next_act, next_inq, next_queue, cnt);
     }
-    if (lane == 0 && scanned) atomicAdd(&cnt->relax, scanned);
+    if (scanned) atomicAdd(&cnt->relax, scanned);
 }
 
 // Clears the frontier words and queued bits of the vertices in a queue.
@@ -302,13 +384,14 @@ extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg
     const uint32_t n = g->n, nw = (n + 31) >> 5, kw = (uint32_t)((k + 31) / 32);
     const WRule w = make_rule(wts);
     // work: dist[n*k] | act0, act1 [n*kw] | inq0, inq1 [nw] | q0, q1 [n] | roots | counters
+    if ((uint64_t)n * kw >= 0xffffffffull) return eg_fail(EG_EINVAL, "n * ceil(k/32) must be < 2^32");
     const uint64_t off_act0 = (uint64_t)n * k, off_act1 = off_act0 + (uint64_t)n * kw, off_inq0 = off_act1 + (uint64_t)n * kw,
-                   off_inq1 = off_inq0 + nw, off_q0 = off_inq1 + nw, off_q1 = off_q0 + n, off_roots = off_q1 + n,
-                   off_cnt = (off_roots + 1024 + 7) & ~7ull;
+                   off_inq1 = off_inq0 + nw, off_q0 = off_inq1 + nw, off_q1 = off_q0 + n, off_big = off_q1 + n,
+                   off_roots = off_big + (uint64_t)n * kw, off_cnt = (off_roots + 1024 + 7) & ~7ull;
     EG_TRY(eg_buf_ensure(ctx, g->sssp_work, (off_cnt + 8) * 4));
     uint32_t *wk = bp<uint32_t>(g->sssp_work);
     uint32_t *dist = wk, *act[2] = {wk + off_act0, wk + off_act1}, *inq[2] = {wk + off_inq0, wk + off_inq1},
-             *q[2] = {wk + off_q0, wk + off_q1}, *d_roots = wk + off_roots;
+             *q[2] = {wk + off_q0, wk + off_q1}, *d_roots = wk + off_roots, *big = wk + off_big;
     SsspCounters *cnt = reinterpret_cast<SsspCounters *>(wk + off_cnt);
     SsspCounters *h = (SsspCounters *)ctx->h_pinned;
     EG_CUDA(cudaMemcpyAsync(d_roots, roots, (uint64_t)k * 4, cudaMemcpyHostToDevice, ctx->stream));
@@ -326,10 +409,14 @@ extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg
     unsigned long long relax = 0;
     while (qlen > 0) {
         const int nxt = cur ^ 1;
-        EG_CUDA(cudaMemsetAsync(&cnt->qsize, 0, 4, ctx->stream));
+        EG_CUDA(cudaMemsetAsync(&cnt->qsize, 0, 8, ctx->stream));  // qsize and nbig
         k_msssp_push<<<blocks_for(ctx, (uint64_t)qlen * kw * 32), 256, 0, ctx->stream>>>(
             bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), q[cur], qlen, k, kw, dist, act[cur], act[nxt], inq[nxt],
-            q[nxt], w, cnt);
+            q[nxt], w, cnt, big);
+        EG_LAUNCHED(ctx);
+        k_msssp_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, ctx->stream>>>(
+            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), k, kw, dist, act[cur], act[nxt], inq[nxt], q[nxt], w, cnt,
+            big);
         EG_LAUNCHED(ctx);
         // the current frontier's words and bits are cleared for reuse as "next"
         k_msssp_clear<<<blocks_for(ctx, (uint64_t)qlen * kw), 256, 0, ctx->stream>>>(q[cur], qlen, kw, act[cur], inq[cur]);
