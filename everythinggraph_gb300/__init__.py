@@ -193,10 +193,10 @@ class Graph:
 
     def bfs(self, root, direction="auto", switch_divisor=20.0, parents=False, copy_out=True):
         o = L.BfsOpts({"auto": L.EG_BFS_AUTO, "push": L.EG_BFS_PUSH_ONLY, "pull": L.EG_BFS_PULL_ONLY}[direction],
-                      switch_divisor)
+                      switch_divisor, int(parents))
         n = self.n
         lv = np.empty(n, dtype=np.int32) if copy_out else None
-        par = np.empty(n, dtype=np.int32) if parents else None
+        par = np.empty(n, dtype=np.int32) if (parents and copy_out) else None
         st = L.BfsStats()
         L.check(lib().eg_bfs(self._h, root, ctypes.byref(o), _ptr(lv), _ptr(par), ctypes.byref(st)))
         return (lv, par, st) if parents else (lv, st)

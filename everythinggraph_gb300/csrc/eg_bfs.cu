@@ -268,6 +268,7 @@ extern "C" void eg_bfs_opts_default(eg_bfs_opts *o) {
     if (!o) return;
     o->direction = EG_BFS_AUTO;
     o->switch_divisor = 20.0;
+    o->device_parents = 0;
 }
 
 static uint32_t blocks_for(eg_ctx *ctx, uint64_t threads) {
@@ -293,7 +294,7 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
     EG_CUDA(cudaSetDevice(ctx->device));
     const uint32_t n = g->n;
     const uint32_t nw = (n + 31) >> 5;
-    const bool want_parent = parent_out != nullptr;
+    const bool want_parent = parent_out != nullptr || o.device_parents;
     EG_TRY(eg_buf_ensure(ctx, g->level, (uint64_t)n * 4));
     if (want_parent) EG_TRY(eg_buf_ensure(ctx, g->parent, (uint64_t)n * 4));
     // work: visited | bm0 | bm1 | queue0 | queue1 | big list | counters
@@ -372,7 +373,7 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
     }
     EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     if (level_out) EG_CUDA(cudaMemcpyAsync(level_out, level, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    if (want_parent) EG_CUDA(cudaMemcpyAsync(parent_out, parent, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    if (parent_out) EG_CUDA(cudaMemcpyAsync(parent_out, parent, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
     EG_CUDA(cudaStreamSynchronize(ctx->stream));
     if (stats) {
         stats->levels = lvl - 1;

@@ -273,9 +273,10 @@ extern "C" void eg_graph_free(eg_graph *g) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     eg_buf *bufs[] = {&g->pairs,        &g->csr.ptr,     &g->csr.col,        &g->csc.ptr,      &g->csc.col,
+                      &g->csr.rid,      &g->csc.rid,
                       &g->out_deg,      &g->in_deg,      &g->cell_ptr,       &g->gsrc,         &g->gdst,
                       &g->sched_csc.coord, &g->sched_csr.coord, &g->rank,    &g->contrib0,     &g->contrib1,
-                      &g->pr_part,      &g->pr_stats,    &g->mp_carry,    &g->level,          &g->parent,       &g->dist,
+                      &g->pr_part,      &g->pr_stats,    &g->mp_carry,    &g->errflag,    &g->level,          &g->parent,       &g->dist,
                       &g->label,        &g->spmv_x,      &g->spmv_y,      &g->spmv_vals,      &g->bfs_work,     &g->msbfs_work,
                       &g->sssp_work};
     for (eg_buf *b : bufs) eg_buf_free(c, *b);
@@ -633,6 +634,9 @@ static int build_adj_pair(eg_graph *g, bool want_csc) {
     BTRY(eg_exscan_u32(ctx, bp<uint32_t>(g->out_deg), bp<uint32_t>(g->csr.ptr), n));
     if (M && cudaMemcpyAsync(g->csr.col.p, vs, M * 4, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess)
         BTRY(eg_fail(EG_ECUDA, "copy col"));
+    BTRY(eg_buf_ensure(ctx, g->csr.rid, M * 4 + 16));
+    if (M && cudaMemcpyAsync(g->csr.rid.p, ks, M * 4, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess)
+        BTRY(eg_fail(EG_ECUDA, "copy rid"));
     g->built |= EG_LAYOUT_CSR;
     if (want_csc) {
         // CSC: stable sort of the CSR entries by dst, value src.  The sorted
@@ -650,6 +654,9 @@ static int build_adj_pair(eg_graph *g, bool want_csc) {
         BTRY(eg_exscan_u32(ctx, bp<uint32_t>(g->in_deg), bp<uint32_t>(g->csc.ptr), n));
         if (M && cudaMemcpyAsync(g->csc.col.p, vs, M * 4, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess)
             BTRY(eg_fail(EG_ECUDA, "copy col"));
+        BTRY(eg_buf_ensure(ctx, g->csc.rid, M * 4 + 16));
+        if (M && cudaMemcpyAsync(g->csc.rid.p, ks, M * 4, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess)
+            BTRY(eg_fail(EG_ECUDA, "copy rid"));
         g->built |= EG_LAYOUT_CSC;
     }
     if (cudaStreamSynchronize(ctx->stream) != cudaSuccess)

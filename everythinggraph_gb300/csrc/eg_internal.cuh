@@ -66,6 +66,7 @@ static inline T *bp(const eg_buf &b) {
 struct eg_adj {
     eg_buf ptr;  // uint32[n+1]
     eg_buf col;  // uint32[m]
+    eg_buf rid;  // uint32[m]: row of each entry (COO form), kept from the sort
 };
 
 // Merge-path schedule of one adjacency for one tile width.
@@ -92,7 +93,7 @@ struct eg_graph {
     // schedules (CSC rows for PR/SpMV pull, CSR rows for push)
     eg_mp_sched sched_csc, sched_csr;
     // algorithm state, allocated on first use and reused
-    eg_buf rank, contrib0, contrib1, pr_part, pr_stats, mp_carry;
+    eg_buf rank, contrib0, contrib1, pr_part, pr_stats, mp_carry, errflag;
     eg_buf level, parent, dist, label, spmv_x, spmv_y, spmv_vals;
     uint64_t spmv_vals_seed;
     int spmv_vals_kind;

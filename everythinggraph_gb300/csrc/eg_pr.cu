@@ -189,6 +189,69 @@ static int mp_launch(eg_graph *g, eg_adj &adj, eg_mp_sched &s, eg_buf &carry_buf
     return EG_OK;
 }
 
+// Persistent TMA-staged variant: grid = resident CTAs (one wave), part[]
+// gets one FP64 partial per CTA then one per fix-up block.
+template <class Op, bool REDUCE>
+static int mpp_launch(eg_graph *g, eg_adj &adj, eg_mp_sched &s, eg_buf &carry_buf, double2 *part, int *err,
+                      const Op &op, uint32_t *grid_out) {
+    eg_ctx *ctx = g->ctx;
+    using A = typename Op::A;
+    using L = eg_mpp_smem<EG_MP_T, EG_MP_IPT, A>;
+    auto kern = k_mpp_rows<Op, EG_MP_T, EG_MP_IPT, REDUCE>;
+    static int per_sm = 0;
+    if (!per_sm) {
+        EG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::bytes));
+        EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, EG_MP_T, L::bytes));
+        if (per_sm < 1) return eg_fail(EG_ECUDA, "merge-path kernel does not fit on an SM");
+    }
+    EG_TRY(eg_buf_ensure(ctx, carry_buf, (uint64_t)s.ntiles * sizeof(eg_mp_carry<A>)));
+    uint32_t grid = (uint32_t)ctx->sm_count * (uint32_t)per_sm;
+    if (grid > s.ntiles) grid = s.ntiles;
+    *grid_out = grid;
+    kern<<<grid, EG_MP_T, L::bytes, ctx->stream>>>(bp<uint32_t>(adj.ptr), bp<uint32_t>(adj.col), g->n,
+                                                  bp<uint2>(s.coord), s.ntiles, bp<eg_mp_carry<A>>(carry_buf), part,
+                                                  err, op);
+    EG_LAUNCHED(ctx);
+    uint32_t fb = eg_div_up((uint64_t)s.ntiles * 32, 256);
+    k_mp_fixup<Op, REDUCE><<<fb, 256, 0, ctx->stream>>>(bp<uint32_t>(adj.ptr), bp<uint2>(s.coord), s.ntiles,
+                                                       bp<eg_mp_carry<A>>(carry_buf), part ? part + grid : nullptr,
+                                                       op);
+    EG_LAUNCHED(ctx);
+    return EG_OK;
+}
+
+// Row-id stream variant (k_coo_rows): one warp per TILE_E entries.  part[]
+// receives per-CTA partials of the main kernel, then of the empty-row kernel,
+// then of the fix-up; returns their count.
+#define EG_COO_TILE 2048
+#define EG_COO_U 4
+template <class Op, bool REDUCE>
+static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts) {
+    eg_ctx *ctx = g->ctx;
+    using A = typename Op::A;
+    const uint32_t m = (uint32_t)g->m;
+    const uint32_t ntiles = m ? eg_div_up(m, EG_COO_TILE) : 0;
+    EG_TRY(eg_buf_ensure(ctx, carry_buf, ((uint64_t)ntiles + 1) * sizeof(eg_mp_carry<A>)));
+    const uint32_t g1 = ntiles ? eg_div_up((uint64_t)ntiles * 32, 256) : 0;
+    uint32_t g2 = eg_div_up(g->n, 256);
+    if (g2 > (uint32_t)ctx->sm_count * 8) g2 = (uint32_t)ctx->sm_count * 8;
+    if (g1) {
+        k_coo_rows<Op, EG_COO_TILE, EG_COO_U, REDUCE><<<g1, 256, 0, ctx->stream>>>(
+            bp<uint32_t>(adj.rid), bp<uint32_t>(adj.col), m, ntiles, bp<eg_mp_carry<A>>(carry_buf), part, op);
+        EG_LAUNCHED(ctx);
+    }
+    k_coo_empty_rows<Op, REDUCE><<<g2, 256, 0, ctx->stream>>>(bp<uint32_t>(adj.ptr), g->n, part ? part + g1 : nullptr,
+                                                              op);
+    EG_LAUNCHED(ctx);
+    if (g1) {
+        k_coo_fixup<Op, EG_COO_TILE, REDUCE><<<g1, 256, 0, ctx->stream>>>(
+            bp<uint32_t>(adj.ptr), ntiles, bp<eg_mp_carry<A>>(carry_buf), part ? part + g1 + g2 : nullptr, op);
+        EG_LAUNCHED(ctx);
+    }
+    *nparts = g1 + g2 + g1;
+    return EG_OK;
+}
+
 extern "C" void eg_pr_opts_default(eg_pr_opts *o) {
     if (!o) return;
     o->iterations = 10;
@@ -205,7 +268,7 @@ extern "C" void eg_pr_opts_default(eg_pr_opts *o) {
 template <bool COMP, bool REDUCE>
 static int pr_iterations(eg_graph *g, const eg_pr_opts &o, eg_pr_dev *st, double2 *part, eg_buf &carry) {
     eg_ctx *ctx = g->ctx;
-    uint32_t nparts = g->sched_csc.ntiles + eg_div_up((uint64_t)g->sched_csc.ntiles * 32, 256);
+    uint32_t grid = 0;
     for (int it = 0; it < o.iterations; it++) {
         PrOp<COMP> op;
         bool odd = o.swap && (it & 1);
@@ -218,7 +281,9 @@ static int pr_iterations(eg_graph *g, const eg_pr_opts &o, eg_pr_dev *st, double
         op.damping = o.damping;
         op.residual = o.tolerance > 0.0;
         op.base = 0.f;
-        EG_TRY((mp_launch<PrOp<COMP>, REDUCE>(g, g->csc, g->sched_csc, carry, part, op)));
+        uint32_t nparts = 0;
+        EG_TRY((coo_launch<PrOp<COMP>, REDUCE>(g, g->csc, carry, part, op, &nparts)));
+        (void)grid;
         k_pr_reduce<<<1, 256, 0, ctx->stream>>>(part, REDUCE ? nparts : 0, st, g->n, o.damping, o.dangling,
                                                 o.tolerance, 1);
         EG_LAUNCHED(ctx);
@@ -239,12 +304,16 @@ extern "C" int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out,
     const uint32_t n = g->n;
     EG_TRY(eg_build_sched(g, g->csc, g->sched_csc, EG_MP_T * EG_MP_IPT));
     const uint32_t ntiles = g->sched_csc.ntiles;
-    const uint32_t nparts = ntiles + eg_div_up((uint64_t)ntiles * 32, 256);
+    const uint32_t coo_tiles = g->m ? eg_div_up(g->m, EG_COO_TILE) : 0;
+    const uint32_t nparts = ntiles + eg_div_up((uint64_t)ntiles * 32, 256) + 2 * eg_div_up((uint64_t)coo_tiles * 32, 256) +
+                            (uint32_t)ctx->sm_count * 8;
     EG_TRY(eg_buf_ensure(ctx, g->rank, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->contrib0, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->contrib1, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->pr_part, ((uint64_t)nparts + 1024) * sizeof(double2)));
     EG_TRY(eg_buf_ensure(ctx, g->pr_stats, sizeof(eg_pr_dev)));
+    EG_TRY(eg_buf_ensure(ctx, g->errflag, 16));
+    EG_CUDA(cudaMemsetAsync(g->errflag.p, 0, 16, ctx->stream));
     eg_buf &carry = g->mp_carry;
     eg_pr_dev *st = bp<eg_pr_dev>(g->pr_stats);
     double2 *part = bp<double2>(g->pr_part);
@@ -270,9 +339,12 @@ extern "C" int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out,
     }
     EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     eg_pr_dev hst;
+    int herr = 0;
     EG_CUDA(cudaMemcpyAsync(&hst, st, sizeof(hst), cudaMemcpyDeviceToHost, ctx->stream));
+    EG_CUDA(cudaMemcpyAsync(&herr, g->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     if (rank_out) EG_CUDA(cudaMemcpyAsync(rank_out, g->rank.p, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
     EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if (herr) return eg_fail(EG_ETIMEOUT, "PageRank: a tile copy did not complete (mbarrier wait limit)");
     if (stats) {
         stats->iterations_run = hst.iters;
         stats->residual = hst.residual;
@@ -396,32 +468,33 @@ extern "C" int eg_spmv(eg_graph *g, const eg_spmv_opts *opts, const void *x, voi
         }
     }
     eg_buf &carry = g->mp_carry;
+    uint32_t np = 0;
     EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     switch (kind) {
         case EG_SPMV_U32_PULL:
         case EG_SPMV_U32_PUSH: {
             SpmvU32Op<0> op{bp<uint32_t>(g->spmv_x), bp<uint32_t>(g->spmv_y)};
-            EG_TRY((mp_launch<SpmvU32Op<0>, false>(g, adj, s, carry, nullptr, op)));
+            EG_TRY((coo_launch<SpmvU32Op<0>, false>(g, adj, carry, nullptr, op, &np)));
             break;
         }
         case EG_SPMV_U32_EDGE: {
             SpmvU32Op<1> op{bp<uint32_t>(g->spmv_x), bp<uint32_t>(g->spmv_y)};
-            EG_TRY((mp_launch<SpmvU32Op<1>, false>(g, adj, s, carry, nullptr, op)));
+            EG_TRY((coo_launch<SpmvU32Op<1>, false>(g, adj, carry, nullptr, op, &np)));
             break;
         }
         case EG_SPMV_F32: {
             SpmvF32Op<false> op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<float>(g->spmv_y)};
-            EG_TRY((mp_launch<SpmvF32Op<false>, false>(g, adj, s, carry, nullptr, op)));
+            EG_TRY((coo_launch<SpmvF32Op<false>, false>(g, adj, carry, nullptr, op, &np)));
             break;
         }
         case EG_SPMV_F32_COMP: {
             SpmvF32Op<true> op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<float>(g->spmv_y)};
-            EG_TRY((mp_launch<SpmvF32Op<true>, false>(g, adj, s, carry, nullptr, op)));
+            EG_TRY((coo_launch<SpmvF32Op<true>, false>(g, adj, carry, nullptr, op, &np)));
             break;
         }
         case EG_SPMV_F64: {
             SpmvF64Op op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<double>(g->spmv_y)};
-            EG_TRY((mp_launch<SpmvF64Op, false>(g, adj, s, carry, nullptr, op)));
+            EG_TRY((coo_launch<SpmvF64Op, false>(g, adj, carry, nullptr, op, &np)));
             break;
         }
     }

@@ -6,12 +6,23 @@
 // of its component.
 //
 // GPU form: label propagation on component roots with pointer jumping.  Every
-// input edge hooks the larger of its two roots under the smaller one
-// (atomicCAS on the root's parent word), so a root is always the minimum id
-// of its tree; finds use path halving (pointer jumping), and a final pass
-// jumps every vertex to its root.  The result equals the reference's fixed
-// point bit for bit, independent of scheduling.
+// edge hooks the larger of its two roots under the smaller one (atomicCAS on
+// the root's parent word), so a root is always the minimum id of its tree;
+// finds use path halving (pointer jumping), and a final pass jumps every
+// vertex to its root.  The result equals the reference's fixed point bit for
+// bit, independent of scheduling.
+//
+// With the adjacency built, edges are hooked in two rounds (the sampling idea
+// of Sutton et al., "Optimizing parallel graph connectivity computation via
+// subgraph sampling", IPDPS 2018): first the first two entries of every list,
+// then, after a compression, the remaining entries of only those vertices
+// whose root is not the largest component's root (sampled), which on
+// power-law graphs skips most of the edges.
+#include <stdlib.h>
+
 #include "eg_internal.cuh"
+
+#define EG_WCC_NONE 0xffffffffu
 
 namespace {
 
@@ -24,6 +35,44 @@ __device__ __forceinline__ uint32_t uf_find(uint32_t *par, uint32_t x) {
         p = gp;
     }
     return x;
+}
+
+__device__ __forceinline__ void uf_link(uint32_t *par, uint32_t x, uint32_t y) {
+    uint32_t a = uf_find(par, x), b = uf_find(par, y);
+    while (a != b) {
+        if (a > b) {
+            const uint32_t t = a;
+            a = b;
+            b = t;
+        }
+        const uint32_t old = atomicCAS(par + b, b, a);
+        if (old == b) break;
+        b = uf_find(par, old);
+        a = uf_find(par, a);
+    }
+}
+
+// Hooks entries [lo, hi) of every list (first round: lo=0, hi=2) or, with
+// skip_root set, entries [lo, end) of vertices whose root is not skip_root.
+__global__ void k_wcc_lists(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col, uint32_t n,
+                            uint32_t lo, uint32_t hi, uint32_t skip_root, uint32_t *par) {
+    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+        if (skip_root != EG_WCC_NONE && uf_find(par, u) == skip_root) continue;
+        const uint32_t b = ptr[u], e = ptr[u + 1];
+        const uint32_t pe = (hi == EG_WCC_NONE || b + hi > e) ? e : b + hi;
+        for (uint32_t p = b + lo; p < pe; p++) uf_link(par, u, col[p]);
+    }
+}
+
+// Roots of 1024 vertices picked by a fixed hash (the largest component is the
+// most frequent root among them).
+__global__ void k_wcc_sample(const uint32_t *__restrict__ par, uint32_t n, uint32_t *out) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < 1024) out[i] = par[(uint32_t)(((eg_mix64((uint64_t)i + 0x51ed) >> 32) * (uint64_t)n) >> 32)];
+}
+
+__global__ void k_wcc_flatten(uint32_t n, uint32_t *par) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) par[v] = uf_find(par, v);
 }
 
 __global__ void k_wcc_init(uint32_t n, uint32_t *par) {
@@ -78,7 +127,8 @@ extern "C" int eg_wcc(eg_graph *g, int64_t *labels_out, eg_wcc_stats *stats) {
     EG_TRY(eg_buf_ensure(ctx, g->label, (uint64_t)n * 4));
     // work: parent[n] | counters | int64 staging for the host copy
     const uint64_t off_cnt = ((uint64_t)n + 3) & ~3ull;
-    const uint64_t off_wide = off_cnt + 8;
+    const uint64_t off_sample = off_cnt + 8;
+    const uint64_t off_wide = off_sample + 1024;
     EG_TRY(eg_buf_ensure(ctx, g->bfs_work, (off_wide + (labels_out ? 2ull * n : 0)) * 4));
     uint32_t *par = bp<uint32_t>(g->bfs_work);
     uint32_t *retries = par + off_cnt;
@@ -89,7 +139,54 @@ extern "C" int eg_wcc(eg_graph *g, int64_t *labels_out, eg_wcc_stats *stats) {
     EG_CUDA(cudaMemsetAsync(retries, 0, 32, ctx->stream));
     k_wcc_init<<<blocks, 256, 0, ctx->stream>>>(n, par);
     EG_LAUNCHED(ctx);
-    if (g->m_in) {
+    const bool have_csr = (g->built & EG_LAYOUT_CSR) != 0;
+    const bool sym = (g->flags & EG_UNDIRECTED) != 0;
+    const bool have_csc = (g->built & EG_LAYOUT_CSC) != 0;
+    int rounds = 1;
+    if (have_csr && (sym || have_csc) && n >= 1024) {
+        // round 1: two entries per list (both directions for a directed graph)
+        k_wcc_lists<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), n, 0, 2,
+                                                     EG_WCC_NONE, par);
+        EG_LAUNCHED(ctx);
+        if (!sym) {
+            k_wcc_lists<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), bp<uint32_t>(g->csc.col), n, 0, 2,
+                                                         EG_WCC_NONE, par);
+            EG_LAUNCHED(ctx);
+        }
+        k_wcc_flatten<<<blocks, 256, 0, ctx->stream>>>(n, par);
+        EG_LAUNCHED(ctx);
+        // the most frequent root among 1024 sampled vertices
+        uint32_t *dsample = par + off_sample;
+        k_wcc_sample<<<4, 256, 0, ctx->stream>>>(par, n, dsample);
+        EG_LAUNCHED(ctx);
+        uint32_t *hs = (uint32_t *)ctx->h_pinned;
+        EG_CUDA(cudaMemcpyAsync(hs, dsample, 1024 * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        qsort(hs, 1024, 4, [](const void *a, const void *b) -> int {
+            const uint32_t x = *(const uint32_t *)a, y = *(const uint32_t *)b;
+            return x < y ? -1 : x > y;
+        });
+        uint32_t best = hs[0], best_cnt = 0;
+        for (int i = 0; i < 1024;) {
+            int j = i;
+            while (j < 1024 && hs[j] == hs[i]) j++;
+            if ((uint32_t)(j - i) > best_cnt) {
+                best_cnt = (uint32_t)(j - i);
+                best = hs[i];
+            }
+            i = j;
+        }
+        // round 2: remaining entries of vertices outside the sampled component
+        k_wcc_lists<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), n, 2,
+                                                     EG_WCC_NONE, best, par);
+        EG_LAUNCHED(ctx);
+        if (!sym) {
+            k_wcc_lists<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), bp<uint32_t>(g->csc.col), n, 2,
+                                                         EG_WCC_NONE, best, par);
+            EG_LAUNCHED(ctx);
+        }
+        rounds = 2;
+    } else if (g->m_in) {
         k_wcc_hook<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->pairs), g->m_in, par, retries);
         EG_LAUNCHED(ctx);
     }
@@ -106,7 +203,7 @@ extern "C" int eg_wcc(eg_graph *g, int64_t *labels_out, eg_wcc_stats *stats) {
     EG_CUDA(cudaStreamSynchronize(ctx->stream));
     if (stats) {
         stats->components = (uint32_t)*h;
-        stats->rounds = 1;
+        stats->rounds = rounds;
         EG_CUDA(cudaEventElapsedTime(&stats->ms, ctx->ev0, ctx->ev1));
     }
     return EG_OK;

@@ -189,6 +189,9 @@ typedef struct {
     /* auto switches to pull when frontier size + frontier out-degree
      * > m / switch_divisor (the reference uses 20, bfs_simple.c:191-197) */
     double switch_divisor;
+    /* 1: compute parents on the device even when parent_out is NULL (read
+     * them later through eg_graph_device_ptr(g, EG_DEV_PARENT)) */
+    int device_parents;
 } eg_bfs_opts;
 typedef struct {
     int levels;
