@@ -191,9 +191,9 @@ class Graph:
         L.check(lib().eg_spmv(self._h, ctypes.byref(o), _ptr(x), _ptr(y), ctypes.byref(ms)))
         return y, ms.value
 
-    def bfs(self, root, direction="auto", switch_divisor=20.0, parents=False, copy_out=True):
+    def bfs(self, root, direction="auto", switch_divisor=20.0, parents=False, copy_out=True, host_loop=False):
         o = L.BfsOpts({"auto": L.EG_BFS_AUTO, "push": L.EG_BFS_PUSH_ONLY, "pull": L.EG_BFS_PULL_ONLY}[direction],
-                      switch_divisor, int(parents))
+                      switch_divisor, int(parents), int(host_loop))
         n = self.n
         lv = np.empty(n, dtype=np.int32) if copy_out else None
         par = np.empty(n, dtype=np.int32) if (parents and copy_out) else None

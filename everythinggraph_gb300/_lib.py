@@ -43,7 +43,7 @@ class SpmvOpts(ctypes.Structure):
 
 
 class BfsOpts(ctypes.Structure):
-    _fields_ = [("direction", c_int), ("switch_divisor", c_f64), ("device_parents", c_int)]
+    _fields_ = [("direction", c_int), ("switch_divisor", c_f64), ("device_parents", c_int), ("host_loop", c_int)]
 
 
 class BfsStats(ctypes.Structure):

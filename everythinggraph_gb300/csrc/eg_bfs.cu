@@ -262,6 +262,249 @@ __global__ void __launch_bounds__(256) k_bm_to_queue(const uint32_t *__restrict_
     }
 }
 
+
+// ---------------------------------------------------------------- device-driven levels
+// The level loop as a CUDA graph: a start kernel, then a while node whose
+// body runs one level (prep, push, push_big, pull, end).  Every kernel reads
+// the level's direction and buffer parity from BfsGState and returns at once
+// when it is not this level's step; the end kernel folds the counters,
+// picks the next direction with the reference's rule and clears the while
+// condition when the frontier is empty.
+struct BfsGState {
+    uint32_t parity;      // frontier buffers in use: bm[parity], q[parity]
+    uint32_t pull;        // this level runs bottom-up
+    uint32_t need_queue;  // the frontier exists only as a bitmap
+    uint32_t qlen;        // queue length when !need_queue
+    uint32_t qfill;       // queue length built by the prep kernel
+    uint32_t lvl;         // level of the current frontier (root = 1)
+    uint32_t levels, pull_levels;
+    uint32_t root, dirmode, n, err;
+    unsigned long long fdeg, reached, traversed;
+    double threshold;
+};
+
+__global__ void k_bfsg_start(BfsGState *st, const uint32_t *__restrict__ deg, int32_t *level, int32_t *parent,
+                             uint32_t *visited, uint32_t *bm0, uint32_t nw, uint32_t *q0, BfsCounters *cnt) {
+    const uint32_t n = st->n, root = st->root;
+    const uint32_t stride = gridDim.x * blockDim.x;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
+        level[v] = v == root ? 1 : 0;
+        if (parent) parent[v] = v == root ? (int32_t)root : -1;
+    }
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += stride) {
+        const uint32_t bit = (root >> 5) == w ? 1u << (root & 31) : 0u;
+        visited[w] = bit;
+        bm0[w] = bit;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        q0[0] = root;
+        const unsigned long long d = deg[root];
+        st->parity = 0;
+        st->need_queue = 0;
+        st->qlen = 1;
+        st->qfill = 0;
+        st->lvl = 1;
+        st->levels = 0;
+        st->pull_levels = 0;
+        st->err = 0;
+        st->fdeg = d;
+        st->reached = 1;
+        st->traversed = d;
+        st->pull = st->dirmode == EG_BFS_PULL_ONLY || (st->dirmode == EG_BFS_AUTO && 1.0 + (double)d > st->threshold);
+        cnt->next_deg = 0;
+        cnt->next_count = 0;
+        cnt->qsize = 0;
+        cnt->nbig = 0;
+    }
+}
+
+// Push levels: clear the next bitmap; after a pull level, list the frontier
+// (bitmap -> queue, one atomic per block).
+__global__ void __launch_bounds__(256) k_bfsg_prep(BfsGState *st, uint32_t *bm0, uint32_t *bm1, uint32_t *q0,
+                                                   uint32_t *q1, uint32_t nw) {
+    if (st->pull) return;
+    const uint32_t par = st->parity;
+    uint32_t *cur = par ? bm1 : bm0, *nxt = par ? bm0 : bm1, *q = par ? q1 : q0;
+    for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += gridDim.x * blockDim.x) nxt[w] = 0;
+    if (!st->need_queue) return;
+    __shared__ uint32_t s_warp[8];
+    __shared__ uint32_t s_base;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t w0 = blockIdx.x * blockDim.x; w0 < nw; w0 += gridDim.x * blockDim.x) {
+        const uint32_t w = w0 + threadIdx.x;
+        const uint32_t word = w < nw ? cur[w] : 0u;
+        const uint32_t c = __popc(word);
+        uint32_t x = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(EG_FULL_MASK, x, o);
+            if (lane >= (uint32_t)o) x += y;
+        }
+        if (lane == 31) s_warp[warp] = x;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            uint32_t t = 0;
+            for (int i = 0; i < 8; i++) {
+                const uint32_t v = s_warp[i];
+                s_warp[i] = t;
+                t += v;
+            }
+            s_base = t ? atomicAdd(&st->qfill, t) : 0u;
+        }
+        __syncthreads();
+        uint32_t pos = s_base + s_warp[warp] + x - c;
+        uint32_t bits = word;
+        while (bits) {
+            const int b = __ffs(bits) - 1;
+            bits &= bits - 1;
+            q[pos++] = (w << 5) + (uint32_t)b;
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) k_bfsg_push(const BfsGState *st, const uint32_t *__restrict__ ptr,
+                                                   const uint32_t *__restrict__ col, const uint32_t *__restrict__ deg,
+                                                   uint32_t *q0, uint32_t *q1, uint32_t *bm0, uint32_t *bm1,
+                                                   uint32_t *visited, int32_t *level, int32_t *parent,
+                                                   BfsCounters *cnt, uint32_t *big) {
+    if (st->pull) return;
+    const uint32_t par = st->parity;
+    const uint32_t qlen = st->need_queue ? st->qfill : st->qlen;
+    const uint32_t *queue = par ? q1 : q0;
+    uint32_t *next_queue = par ? q0 : q1, *next_bm = par ? bm0 : bm1;
+    const int32_t next_level = (int32_t)st->lvl + 1;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    uint32_t my_cnt = 0;
+    unsigned long long my_deg = 0;
+    for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < qlen; qi += warps) {
+        const uint32_t u = queue[qi];
+        const uint32_t b = ptr[u], e = ptr[u + 1];
+        if (e - b > EG_BFS_BIG_DEG) {
+            if (lane == 0) big[atomicAdd(&cnt->nbig, 1u)] = u;
+            continue;
+        }
+        for (uint32_t p0 = b; p0 < e; p0 += 32) {
+            const uint32_t p = p0 + lane;
+            bool claimed = false;
+            uint32_t v = 0;
+            if (p < e) {
+                v = col[p];
+                claimed = bfs_claim(v, u, visited, next_bm, level, parent, next_level);
+            }
+            warp_append(claimed, v, next_queue, cnt, deg, my_cnt, my_deg);
+        }
+    }
+    block_add_counters(cnt, my_cnt, my_deg);
+}
+
+__global__ void __launch_bounds__(256) k_bfsg_push_big(const BfsGState *st, const uint32_t *__restrict__ ptr,
+                                                       const uint32_t *__restrict__ col,
+                                                       const uint32_t *__restrict__ deg, const uint32_t *big,
+                                                       uint32_t *q0, uint32_t *q1, uint32_t *bm0, uint32_t *bm1,
+                                                       uint32_t *visited, int32_t *level, int32_t *parent,
+                                                       BfsCounters *cnt) {
+    if (st->pull) return;
+    const uint32_t nbig = *(volatile uint32_t *)&cnt->nbig;
+    if (!nbig) return;
+    const uint32_t par = st->parity;
+    uint32_t *next_queue = par ? q0 : q1, *next_bm = par ? bm0 : bm1;
+    const int32_t next_level = (int32_t)st->lvl + 1;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nthreads = gridDim.x * blockDim.x;
+    uint32_t my_cnt = 0;
+    unsigned long long my_deg = 0;
+    for (uint32_t bi = 0; bi < nbig; bi++) {
+        const uint32_t u = big[bi];
+        const uint32_t b = ptr[u], e = ptr[u + 1];
+        for (uint32_t p0 = b + (tid & ~31u); p0 < e; p0 += nthreads) {
+            const uint32_t p = p0 + (threadIdx.x & 31);
+            bool claimed = false;
+            uint32_t v = 0;
+            if (p < e) {
+                v = col[p];
+                claimed = bfs_claim(v, u, visited, next_bm, level, parent, next_level);
+            }
+            warp_append(claimed, v, next_queue, cnt, deg, my_cnt, my_deg);
+        }
+    }
+    block_add_counters(cnt, my_cnt, my_deg);
+}
+
+__global__ void __launch_bounds__(256) k_bfsg_pull(const BfsGState *st, const uint32_t *__restrict__ ptr,
+                                                   const uint32_t *__restrict__ col, const uint32_t *__restrict__ deg,
+                                                   uint32_t *bm0, uint32_t *bm1, uint32_t *visited, int32_t *level,
+                                                   int32_t *parent, BfsCounters *cnt) {
+    if (!st->pull) return;
+    const uint32_t n = st->n;
+    const uint32_t par = st->parity;
+    const uint32_t *cur_bm = par ? bm1 : bm0;
+    uint32_t *next_bm = par ? bm0 : bm1;
+    const int32_t next_level = (int32_t)st->lvl + 1;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t nw = (n + 31) >> 5;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    uint32_t my_cnt = 0;
+    unsigned long long my_deg = 0;
+    for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < nw; w += warps) {
+        const uint32_t vis = visited[w];
+        if (vis == EG_FULL_MASK) {
+            if (lane == 0) next_bm[w] = 0;
+            continue;
+        }
+        const uint32_t v = (w << 5) + lane;
+        bool found = false;
+        if (v < n && !(vis & (1u << lane))) {
+            const uint32_t b = ptr[v], e = ptr[v + 1];
+            for (uint32_t p = b; p < e; p++) {
+                const uint32_t u = col[p];
+                if (__ldcg(cur_bm + (u >> 5)) & (1u << (u & 31))) {
+                    found = true;
+                    level[v] = next_level;
+                    if (parent) parent[v] = (int32_t)u;
+                    break;
+                }
+            }
+        }
+        const uint32_t ball = __ballot_sync(EG_FULL_MASK, found);
+        if (lane == 0) {
+            next_bm[w] = ball;
+            if (ball) visited[w] = vis | ball;
+        }
+        if (found) {
+            my_cnt++;
+            my_deg += deg[v];
+        }
+    }
+    block_add_counters(cnt, my_cnt, my_deg);
+}
+
+__global__ void k_bfsg_end(BfsGState *st, BfsCounters *cnt, cudaGraphConditionalHandle handle) {
+    const uint32_t count = cnt->next_count;
+    const unsigned long long fdeg = cnt->next_deg;
+    st->levels += 1;
+    if (st->pull) st->pull_levels += 1;
+    st->reached += count;
+    st->traversed += fdeg;
+    if (count == 0 || st->lvl > st->n + 1) {
+        if (count != 0) st->err = 1;
+        cudaGraphSetConditional(handle, 0);
+        return;
+    }
+    st->need_queue = st->pull ? 1u : 0u;  // a pull level leaves only a bitmap
+    st->qlen = cnt->qsize;
+    st->qfill = 0;
+    st->parity ^= 1u;
+    st->lvl += 1;
+    st->fdeg = fdeg;
+    st->pull = st->dirmode == EG_BFS_PULL_ONLY ||
+               (st->dirmode == EG_BFS_AUTO && (double)count + (double)fdeg > st->threshold);
+    cnt->next_count = 0;
+    cnt->next_deg = 0;
+    cnt->qsize = 0;
+    cnt->nbig = 0;
+}
 }  // namespace
 
 extern "C" void eg_bfs_opts_default(eg_bfs_opts *o) {
@@ -269,6 +512,7 @@ extern "C" void eg_bfs_opts_default(eg_bfs_opts *o) {
     o->direction = EG_BFS_AUTO;
     o->switch_divisor = 20.0;
     o->device_parents = 0;
+    o->host_loop = 0;
 }
 
 static uint32_t blocks_for(eg_ctx *ctx, uint64_t threads) {
@@ -276,6 +520,59 @@ static uint32_t blocks_for(eg_ctx *ctx, uint64_t threads) {
     uint64_t cap = (uint64_t)ctx->sm_count * 8;
     if (b > cap) b = cap;
     return b ? (uint32_t)b : 1u;
+}
+
+// Captures the level loop of eg_bfs for the current buffers (see BfsGState).
+static int bfs_graph_build(eg_graph *g, eg_bfs_graph &bg, const void *const key[8], BfsGState *st,
+                           const uint32_t *deg, int32_t *level, int32_t *parent, uint32_t *visited, uint32_t *bm0,
+                           uint32_t *bm1, uint32_t *q0, uint32_t *q1, uint32_t *big, BfsCounters *cnt,
+                           const eg_adj *in_adj) {
+    eg_ctx *ctx = g->ctx;
+    const uint32_t n = g->n, nw = (n + 31) >> 5;
+    if (bg.exec) cudaGraphExecDestroy(bg.exec);
+    if (bg.graph) cudaGraphDestroy(bg.graph);
+    bg.exec = nullptr;
+    bg.graph = nullptr;
+    cudaGraph_t graph = nullptr;
+    EG_CUDA(cudaGraphCreate(&graph, 0));
+    bg.graph = graph;
+    const uint32_t blocks = (uint32_t)ctx->sm_count * 8;
+    // start kernel
+    EG_CUDA(cudaStreamBeginCaptureToGraph(ctx->stream, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    k_bfsg_start<<<blocks, 256, 0, ctx->stream>>>(st, deg, level, parent, visited, bm0, nw, q0, cnt);
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
+    if (ce != cudaSuccess) return eg_fail(EG_ECUDA, "BFS graph capture: %s", cudaGetErrorString(ce));
+    cudaGraphNode_t start_node;
+    size_t nnodes = 1;
+    EG_CUDA(cudaGraphGetNodes(graph, &start_node, &nnodes));
+    // while node
+    cudaGraphConditionalHandle handle;
+    EG_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    EG_CUDA(cudaGraphAddNode(&wnode, graph, &start_node, nullptr, 1, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    EG_CUDA(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    const uint32_t *iptr = in_adj ? bp<uint32_t>(in_adj->ptr) : nullptr;
+    const uint32_t *icol = in_adj ? bp<uint32_t>(in_adj->col) : nullptr;
+    k_bfsg_prep<<<blocks, 256, 0, ctx->stream>>>(st, bm0, bm1, q0, q1, nw);
+    k_bfsg_push<<<blocks, 256, 0, ctx->stream>>>(st, bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, q0, q1,
+                                                bm0, bm1, visited, level, parent, cnt, big);
+    k_bfsg_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, ctx->stream>>>(
+        st, bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, big, q0, q1, bm0, bm1, visited, level, parent, cnt);
+    if (iptr) k_bfsg_pull<<<blocks, 256, 0, ctx->stream>>>(st, iptr, icol, deg, bm0, bm1, visited, level, parent, cnt);
+    k_bfsg_end<<<1, 1, 0, ctx->stream>>>(st, cnt, handle);
+    ce = cudaStreamEndCapture(ctx->stream, &body);
+    if (ce != cudaSuccess) return eg_fail(EG_ECUDA, "BFS level capture: %s", cudaGetErrorString(ce));
+    cudaGraphExec_t exec = nullptr;
+    EG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    bg.exec = exec;
+    for (int i = 0; i < 8; i++) bg.key[i] = key[i];
+    return EG_OK;
 }
 
 extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32_t *level_out, int32_t *parent_out,
@@ -286,6 +583,7 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
     eg_bfs_opts o;
     if (opts) o = *opts;
     else eg_bfs_opts_default(&o);
+    if (o.direction < EG_BFS_AUTO || o.direction > EG_BFS_PULL_ONLY) return eg_fail(EG_EINVAL, "bad direction");
     const bool undirected = (g->flags & EG_UNDIRECTED) != 0;
     eg_adj *in_adj = undirected ? &g->csr : ((g->built & EG_LAYOUT_CSC) ? &g->csc : nullptr);
     if (!in_adj && o.direction != EG_BFS_PUSH_ONLY)
@@ -297,19 +595,59 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
     const bool want_parent = parent_out != nullptr || o.device_parents;
     EG_TRY(eg_buf_ensure(ctx, g->level, (uint64_t)n * 4));
     if (want_parent) EG_TRY(eg_buf_ensure(ctx, g->parent, (uint64_t)n * 4));
-    // work: visited | bm0 | bm1 | queue0 | queue1 | big list | counters
+    // work: visited | bm0 | bm1 | queue0 | queue1 | big list | counters | graph state
     const uint64_t off_bm0 = (uint64_t)nw, off_bm1 = 2ull * nw, off_q0 = 3ull * nw, off_q1 = off_q0 + n,
-                   off_big = off_q1 + n, off_cnt = (off_big + n + 7) & ~7ull;
-    EG_TRY(eg_buf_ensure(ctx, g->bfs_work, (off_cnt + 8) * 4));
+                   off_big = off_q1 + n, off_cnt = (off_big + n + 7) & ~7ull, off_st = off_cnt + 16;
+    EG_TRY(eg_buf_ensure(ctx, g->bfs_work, (off_st + 64) * 4));
     uint32_t *wk = bp<uint32_t>(g->bfs_work);
     uint32_t *visited = wk, *bm[2] = {wk + off_bm0, wk + off_bm1}, *q[2] = {wk + off_q0, wk + off_q1};
     uint32_t *big = wk + off_big;
     BfsCounters *cnt = reinterpret_cast<BfsCounters *>(wk + off_cnt);
+    BfsGState *gst = reinterpret_cast<BfsGState *>(wk + off_st);
     int32_t *level = bp<int32_t>(g->level);
     int32_t *parent = want_parent ? bp<int32_t>(g->parent) : nullptr;
     const uint32_t *deg = bp<uint32_t>(g->out_deg);
-    BfsCounters *h = (BfsCounters *)ctx->h_pinned;
+    const double threshold = o.switch_divisor > 0 ? (double)g->m / o.switch_divisor : 0.0;
 
+    if (!o.host_loop) {
+        eg_bfs_graph &bg = g->bfsg[want_parent ? 1 : 0];
+        const void *key[8] = {wk, level, parent, deg, g->csr.col.p, in_adj ? in_adj->col.p : nullptr, g->csr.ptr.p,
+                              (const void *)(uintptr_t)ctx->stream};
+        bool fresh = bg.exec != nullptr;
+        for (int i = 0; i < 8 && fresh; i++) fresh = bg.key[i] == key[i];
+        if (!fresh)
+            EG_TRY(bfs_graph_build(g, bg, key, gst, deg, level, parent, visited, bm[0], bm[1], q[0], q[1], big, cnt,
+                                   in_adj));
+        BfsGState *h = (BfsGState *)ctx->h_pinned;
+        memset(h, 0, sizeof(BfsGState));
+        h->root = root;
+        h->dirmode = (uint32_t)o.direction;
+        h->n = n;
+        h->threshold = threshold;
+        EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+        EG_CUDA(cudaMemcpyAsync(gst, h, sizeof(BfsGState), cudaMemcpyHostToDevice, ctx->stream));
+        EG_CUDA(cudaGraphLaunch(bg.exec, ctx->stream));
+        ctx->launches += 1;
+        EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+        if (level_out) EG_CUDA(cudaMemcpyAsync(level_out, level, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        if (parent_out)
+            EG_CUDA(cudaMemcpyAsync(parent_out, parent, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        BfsGState *hs = h + 1;
+        EG_CUDA(cudaMemcpyAsync(hs, gst, sizeof(BfsGState), cudaMemcpyDeviceToHost, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (hs->err) return eg_fail(EG_ETIMEOUT, "BFS did not terminate");
+        if (stats) {
+            stats->levels = (int)hs->levels;
+            stats->reached = (uint32_t)hs->reached;
+            stats->edges_traversed = hs->traversed;
+            stats->pull_levels = (int)hs->pull_levels;
+            EG_CUDA(cudaEventElapsedTime(&stats->ms, ctx->ev0, ctx->ev1));
+        }
+        return EG_OK;
+    }
+
+    // host-driven level loop
+    BfsCounters *h = (BfsCounters *)ctx->h_pinned;
     EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     k_bfs_init<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(n, level, parent, visited, bm[0], nw, root, q[0], deg, cnt);
     EG_LAUNCHED(ctx);
@@ -323,7 +661,6 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
     int32_t lvl = 1;
     int pull_levels = 0;
     uint64_t reached = 1, traversed = fdeg;
-    const double threshold = o.switch_divisor > 0 ? (double)g->m / o.switch_divisor : 0.0;
     while (count > 0) {
         bool pull;
         if (o.direction == EG_BFS_PUSH_ONLY) pull = false;

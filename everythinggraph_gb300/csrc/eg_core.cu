@@ -280,6 +280,10 @@ extern "C" void eg_graph_free(eg_graph *g) {
                       &g->label,        &g->spmv_x,      &g->spmv_y,      &g->spmv_vals,      &g->bfs_work,     &g->msbfs_work,
                       &g->sssp_work};
     for (eg_buf *b : bufs) eg_buf_free(c, *b);
+    for (eg_bfs_graph &bg : g->bfsg) {
+        if (bg.exec) cudaGraphExecDestroy(bg.exec);
+        if (bg.graph) cudaGraphDestroy(bg.graph);
+    }
     delete g;
 }
 

@@ -76,6 +76,14 @@ struct eg_mp_sched {
     eg_buf coord;         // uint2[ntiles+1]: (row, edge) at each tile start
 };
 
+// A BFS level loop captured as a CUDA graph with a device-side while node,
+// valid while the buffers it was captured with (key) stay in place.
+struct eg_bfs_graph {
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    const void *key[8] = {};
+};
+
 struct eg_graph {
     eg_ctx *ctx;
     uint32_t n;
@@ -100,6 +108,7 @@ struct eg_graph {
     eg_buf bfs_work;  // bitmaps, queues, counters
     eg_buf msbfs_work;
     eg_buf sssp_work;
+    eg_bfs_graph bfsg[2];  // without / with parents
 };
 
 // ---------------------------------------------------------------- helpers

@@ -777,3 +777,146 @@ __global__ void k_coo_empty_rows(const uint32_t *__restrict__ ptr, uint32_t n, d
         }
     }
 }
+
+// Four entries per lane: lane l of a warp holds entries base+4l .. base+4l+3
+// (128-bit loads of rid and col), sums the runs of equal rows among them
+// locally, and one segmented scan per 128 entries (flag form: a lane whose
+// last run starts inside it, or whose row differs from the previous lane's
+// last row, starts a segment) joins runs that cross lanes.  A run is emitted
+// by the lane holding its last entry; the run open after lane 31 is carried
+// to the next chunk.  Tiles are multiples of 128 entries, so only the last
+// tile has padding entries (row EG_MP_NONE, never emitted).
+template <class Op, int TILE_E, bool REDUCE>
+__global__ void __launch_bounds__(256) k_coo4_rows(const uint32_t *__restrict__ rid, const uint32_t *__restrict__ col,
+                                                   uint32_t m, uint32_t ntiles,
+                                                   eg_mp_carry<typename Op::A> *__restrict__ carry,
+                                                   double2 *__restrict__ part, Op op) {
+    static_assert(TILE_E % 128 == 0, "tiles hold whole chunks");
+    using V = typename Op::V;
+    using A = typename Op::A;
+    __shared__ double2 s_red[8];
+    if (!op.active()) return;
+    op.setup();
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    double2 red = make_double2(0.0, 0.0);
+    if (t < ntiles) {
+        const uint32_t E0 = t * (uint32_t)TILE_E;
+        const uint32_t E1 = min(E0 + (uint32_t)TILE_E, m);
+        const uint32_t first = __ldg(rid + E0);
+        const uint32_t head_row = (E0 > 0 && __ldg(rid + E0 - 1) == first) ? first : EG_MP_NONE;
+        const uint32_t tile_next = E1 < m ? __ldg(rid + E1) : EG_MP_NONE;
+        uint32_t crow = EG_MP_NONE;
+        A cval = op.zero();
+        bool head_done = false;
+        A head_val = op.zero();
+        auto finish = [&](uint32_t row, const A &val) {
+            if (row == EG_MP_NONE) return;
+            if (row == head_row) {
+                head_done = true;
+                head_val = val;
+                return;
+            }
+            const double2 d = op.emit(row, val);
+            if (REDUCE) {
+                red.x += d.x;
+                red.y += d.y;
+            }
+        };
+        for (uint32_t base = E0; base < E1; base += 128) {
+            const uint32_t e = base + 4 * lane;
+            uint32_t r[4], u[4];
+            if (e + 3 < E1) {
+                const uint4 rr = __ldg(reinterpret_cast<const uint4 *>(rid + e));
+                const uint4 cc = __ldg(reinterpret_cast<const uint4 *>(col + e));
+                r[0] = rr.x; r[1] = rr.y; r[2] = rr.z; r[3] = rr.w;
+                u[0] = cc.x; u[1] = cc.y; u[2] = cc.z; u[3] = cc.w;
+            } else {
+#pragma unroll
+                for (int k = 0; k < 4; k++) {
+                    const bool in = e + k < E1;
+                    r[k] = in ? __ldg(rid + e + k) : EG_MP_NONE;
+                    u[k] = in ? __ldg(col + e + k) : 0u;
+                }
+            }
+            V v[4];
+#pragma unroll
+            for (int k = 0; k < 4; k++) v[k] = r[k] != EG_MP_NONE ? op.gather(e + k, u[k]) : V();
+            // row of the entry after this lane's last one
+            uint32_t nxt = __shfl_down_sync(EG_FULL_MASK, r[0], 1);
+            if (lane == 31) nxt = base + 128 < E1 ? __ldg(rid + base + 128) : tile_next;
+            const uint32_t prev_last = __shfl_up_sync(EG_FULL_MASK, r[3], 1);
+            // local runs: head run (from entry 0), middle runs, tail run (to entry 3)
+            A hsum = op.add(op.zero(), v[0]);
+            A run = hsum;
+            bool multi = false;
+#pragma unroll
+            for (int k = 1; k < 4; k++) {
+                if (r[k] != r[k - 1]) {
+                    if (!multi) hsum = run;  // the head run closed at k-1
+                    else finish(r[k - 1], run);
+                    multi = true;
+                    run = op.add(op.zero(), v[k]);
+                } else {
+                    run = op.add(run, v[k]);
+                }
+            }
+            if (!multi) hsum = run;
+            // segmented scan of the tail runs across lanes
+            A x = run;
+            bool f = multi || lane == 0 || prev_last != r[0];
+            if (lane == 0 && !multi && r[0] == crow) x = op.merge(cval, x);
+#pragma unroll
+            for (int off = 1; off < 32; off <<= 1) {
+                const A px = eg_shfl_up(x, off);
+                const bool pf = __shfl_up_sync(EG_FULL_MASK, f, off);
+                if (lane >= (uint32_t)off) {
+                    if (!f) x = op.merge(px, x);
+                    f = f || pf;
+                }
+            }
+            // carry into this lane's head run (multi-run lanes)
+            const A prevS = eg_shfl_up(x, 1);
+            if (multi) {
+                A tot = hsum;
+                if (lane == 0) {
+                    if (r[0] == crow) tot = op.merge(cval, hsum);
+                } else if (prev_last == r[0]) {
+                    tot = op.merge(prevS, hsum);
+                }
+                finish(r[0], tot);
+            }
+            if (nxt != r[3]) finish(r[3], x);
+            crow = __shfl_sync(EG_FULL_MASK, r[3], 31);
+            cval = eg_shfl_idx(x, 31);
+        }
+        const uint32_t hmask = __ballot_sync(EG_FULL_MASK, head_done);
+        if (lane == 0) {
+            const bool tail_open = E1 < m && crow != EG_MP_NONE && tile_next == crow;
+            carry[t].tail_row = tail_open ? crow : EG_MP_NONE;
+            carry[t].tail_val = cval;
+            carry[t].head_row = hmask ? head_row : EG_MP_NONE;
+        }
+        if (hmask) {
+            const A hv = eg_shfl_idx(head_val, __ffs(hmask) - 1);
+            if (lane == 0) carry[t].head_val = hv;
+        }
+    }
+    if (REDUCE) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            red.x += __shfl_down_sync(EG_FULL_MASK, red.x, o);
+            red.y += __shfl_down_sync(EG_FULL_MASK, red.y, o);
+        }
+        if (lane == 0) s_red[threadIdx.x >> 5] = red;
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            double2 s = make_double2(0.0, 0.0);
+            for (int w = 0; w < 8; w++) {
+                s.x += s_red[w].x;
+                s.y += s_red[w].y;
+            }
+            part[blockIdx.x] = s;
+        }
+    }
+}

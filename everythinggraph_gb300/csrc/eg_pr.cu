@@ -220,7 +220,7 @@ static int mpp_launch(eg_graph *g, eg_adj &adj, eg_mp_sched &s, eg_buf &carry_bu
     return EG_OK;
 }
 
-// Row-id stream variant (k_coo_rows): one warp per TILE_E entries.  part[]
+// Row-id stream variant (k_coo4_rows): one warp per TILE_E entries.  part[]
 // receives per-CTA partials of the main kernel, then of the empty-row kernel,
 // then of the fix-up; returns their count.
 #define EG_COO_TILE 2048
@@ -236,7 +236,7 @@ static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part
     uint32_t g2 = eg_div_up(g->n, 256);
     if (g2 > (uint32_t)ctx->sm_count * 8) g2 = (uint32_t)ctx->sm_count * 8;
     if (g1) {
-        k_coo_rows<Op, EG_COO_TILE, EG_COO_U, REDUCE><<<g1, 256, 0, ctx->stream>>>(
+        k_coo4_rows<Op, EG_COO_TILE, REDUCE><<<g1, 256, 0, ctx->stream>>>(
             bp<uint32_t>(adj.rid), bp<uint32_t>(adj.col), m, ntiles, bp<eg_mp_carry<A>>(carry_buf), part, op);
         EG_LAUNCHED(ctx);
     }

@@ -192,6 +192,10 @@ typedef struct {
     /* 1: compute parents on the device even when parent_out is NULL (read
      * them later through eg_graph_device_ptr(g, EG_DEV_PARENT)) */
     int device_parents;
+    /* 0 (default): the level loop runs on the device as one CUDA graph with a
+     * conditional while node (no host round trip per level); 1: the host
+     * launches and synchronises every level */
+    int host_loop;
 } eg_bfs_opts;
 typedef struct {
     int levels;

@@ -191,9 +191,11 @@ def test_bfs_levels_bit_exact(case):
     name, n, pairs, rec, g, gu, adj, adju = case
     for r in rec["roots"]:
         for direction in ("auto", "push", "pull"):
-            lv, par, st = g.bfs(int(r), direction=direction, parents=True)
-            np.testing.assert_array_equal(lv.astype(np.uint32), rec["bfsgrid_m0_p%d" % r])
-            assert oracle.bfs_tree_ok(n, adj.out_ptr, adj.out_col, int(r), lv, par)
+            for host_loop in (False, True):  # device-driven graph loop and host-driven loop
+                lv, par, st = g.bfs(int(r), direction=direction, parents=True, host_loop=host_loop)
+                np.testing.assert_array_equal(lv.astype(np.uint32), rec["bfsgrid_m0_p%d" % r])
+                assert oracle.bfs_tree_ok(n, adj.out_ptr, adj.out_col, int(r), lv, par)
+                assert st.reached == int((lv > 0).sum())
     lv, st = g.bfs(0)
     np.testing.assert_array_equal(lv.astype(np.uint32), rec["bfs_simple_m8"])
     lvu, st = gu.bfs(0)
@@ -306,6 +308,9 @@ def test_big_bfs_properties(big):
     for s, r in enumerate(roots):
         lv, par, st = big.bfs(int(r), parents=True)
         np.testing.assert_array_equal(lv, lvm[s])
+        lvh, sth = big.bfs(int(r), host_loop=True)
+        np.testing.assert_array_equal(lv, lvh)
+        assert (st.levels, st.reached, st.edges_traversed) == (sth.levels, sth.reached, sth.edges_traversed)
         # every edge from a reached vertex reaches a vertex at most one level deeper
         ls, ld = lv[src], lv[col]
         assert np.all(ld[ls > 0] > 0) and np.all(ld[ls > 0] <= ls[ls > 0] + 1)
