@@ -224,6 +224,22 @@ class Graph:
         L.check(lib().eg_sssp_multi(self._h, _ptr(roots), len(roots), ctypes.byref(w), _ptr(out), ctypes.byref(st)))
         return out, st
 
+    def ppr(self, seed_lists, damping=0.85, tolerance=1e-6, max_iters=50, copy_out=True):
+        """Personalised PageRank for up to 32 queries (one seed list each)."""
+        nq = len(seed_lists)
+        offs = np.zeros(nq + 1, dtype=np.uint32)
+        offs[1:] = np.cumsum([len(s) for s in seed_lists])
+        seeds = np.ascontiguousarray(np.concatenate([np.asarray(s, dtype=np.uint32) for s in seed_lists]))
+        o = L.PprOpts()
+        o.damping, o.max_iters = damping, max_iters
+        tols = tolerance if isinstance(tolerance, (list, tuple, np.ndarray)) else [tolerance] * nq
+        for q in range(32):
+            o.tolerance[q] = float(tols[q]) if q < nq else 1.0
+        out = np.empty((nq, self.n), dtype=np.float32) if copy_out else None
+        st = L.PprStats()
+        L.check(lib().eg_ppr_multi(self._h, _ptr(seeds), _ptr(offs), nq, ctypes.byref(o), _ptr(out), ctypes.byref(st)))
+        return out, st
+
     def wcc(self, copy_out=True):
         out = np.empty(self.n, dtype=np.int64) if copy_out else None
         st = L.WccStats()

@@ -59,6 +59,14 @@ class SsspStats(ctypes.Structure):
     _fields_ = [("rounds", c_int), ("reached", c_u32), ("relaxations", c_u64), ("ms", c_f32)]
 
 
+class PprOpts(ctypes.Structure):
+    _fields_ = [("damping", c_f32), ("max_iters", c_int), ("tolerance", c_f32 * 32)]
+
+
+class PprStats(ctypes.Structure):
+    _fields_ = [("iterations", c_int * 32), ("residual", c_f64 * 32), ("sweeps", c_int), ("ms", c_f32)]
+
+
 class WccStats(ctypes.Structure):
     _fields_ = [("rounds", c_int), ("components", c_u32), ("ms", c_f32)]
 
@@ -97,6 +105,7 @@ SIGNATURES = {
     "eg_sssp_multi": (c_int, [c_void_p, c_void_p, c_int, P(Weights), c_void_p, P(SsspStats)]),
     "eg_wcc": (c_int, [c_void_p, c_void_p, P(WccStats)]),
     "eg_sample_roots": (c_int, [c_void_p, c_int, c_u64, c_void_p]),
+    "eg_ppr_multi": (c_int, [c_void_p, c_void_p, c_void_p, c_int, P(PprOpts), c_void_p, P(PprStats)]),
     "eg_spmv_f32_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_u32, c_u64, c_void_p]),
 }
 

@@ -273,12 +273,13 @@ extern "C" void eg_graph_free(eg_graph *g) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     eg_buf *bufs[] = {&g->pairs,        &g->csr.ptr,     &g->csr.col,        &g->csc.ptr,      &g->csc.col,
-                      &g->csr.rid,      &g->csc.rid,
+                      &g->csr.rid,      &g->csc.rid,     &g->csc_p.ptr,      &g->csc_p.col,    &g->csc_p.rid,
+                      &g->perm,         &g->deg_p,
                       &g->out_deg,      &g->in_deg,      &g->cell_ptr,       &g->gsrc,         &g->gdst,
                       &g->sched_csc.coord, &g->sched_csr.coord, &g->rank,    &g->contrib0,     &g->contrib1,
-                      &g->pr_part,      &g->pr_stats,    &g->mp_carry,    &g->errflag,    &g->level,          &g->parent,       &g->dist,
+                      &g->pr_part,      &g->pr_stats,    &g->mp_carry,    &g->errflag,     &g->rank_p,    &g->level,          &g->parent,       &g->dist,
                       &g->label,        &g->spmv_x,      &g->spmv_y,      &g->spmv_vals,      &g->bfs_work,     &g->msbfs_work,
-                      &g->sssp_work};
+                      &g->sssp_work,    &g->ppr_work};
     for (eg_buf *b : bufs) eg_buf_free(c, *b);
     for (eg_bfs_graph &bg : g->bfsg) {
         if (bg.exec) cudaGraphExecDestroy(bg.exec);
@@ -798,6 +799,102 @@ extern "C" int eg_graph_build_grid(eg_graph *g, uint32_t P) {
     cleanup();
     g->grid_p = P;
     g->built |= EG_LAYOUT_GRID;
+    return EG_OK;
+}
+
+// ---------------------------------------------------------------- relabelled CSC
+__global__ void k_relabel_keys(const uint32_t *__restrict__ deg, uint32_t n, uint32_t *keys, uint32_t *vals) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        keys[v] = ~deg[v];  // ascending key = descending degree; ties keep ascending id (stable sort)
+        vals[v] = v;
+    }
+}
+__global__ void k_relabel_perm(const uint32_t *__restrict__ order, const uint32_t *__restrict__ deg, uint32_t n,
+                               uint32_t *perm, uint32_t *deg_p) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t old = order[i];
+        perm[old] = i;
+        deg_p[i] = deg[old];
+    }
+}
+// CSC entry (row v, column u) -> (key perm[u], value perm[v])
+__global__ void k_relabel_entries(const uint32_t *__restrict__ rid, const uint32_t *__restrict__ col,
+                                  const uint32_t *__restrict__ perm, uint64_t m, uint32_t *keys, uint32_t *vals) {
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+        keys[e] = perm[col[e]];
+        vals[e] = perm[rid[e]];
+    }
+}
+
+int eg_build_relabeled_csc(eg_graph *g) {
+    if (g->relabeled) return EG_OK;
+    if (!(g->built & EG_LAYOUT_CSC) || !(g->built & EG_LAYOUT_CSR))
+        return eg_fail(EG_ENOTBUILT, "relabelled CSC needs the CSC and the out-degrees");
+    eg_ctx *ctx = g->ctx;
+    const uint32_t n = g->n;
+    const uint64_t M = g->m;
+    eg_buf ka, va, kb, vb;
+    int rc = EG_OK;
+    auto cleanup = [&]() {
+        cudaStreamSynchronize(ctx->stream);
+        eg_buf_free(ctx, ka);
+        eg_buf_free(ctx, va);
+        eg_buf_free(ctx, kb);
+        eg_buf_free(ctx, vb);
+    };
+#define RTRY(x)            \
+    do {                   \
+        rc = (x);          \
+        if (rc != EG_OK) { \
+            cleanup();     \
+            return rc;     \
+        }                  \
+    } while (0)
+    const uint64_t len = M > n ? M : n;
+    RTRY(eg_buf_ensure(ctx, ka, (len + 1) * 4));
+    RTRY(eg_buf_ensure(ctx, va, (len + 1) * 4));
+    RTRY(eg_buf_ensure(ctx, kb, (len + 1) * 4));
+    RTRY(eg_buf_ensure(ctx, vb, (len + 1) * 4));
+    RTRY(eg_buf_ensure(ctx, g->perm, (uint64_t)n * 4));
+    RTRY(eg_buf_ensure(ctx, g->deg_p, (uint64_t)n * 4));
+    uint32_t *ks, *vs;
+    k_relabel_keys<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(bp<uint32_t>(g->out_deg), n, bp<uint32_t>(ka),
+                                                             bp<uint32_t>(va));
+    ctx->launches++;
+    RTRY(eg_radix_sort(ctx, bp<uint32_t>(ka), bp<uint32_t>(va), bp<uint32_t>(kb), bp<uint32_t>(vb), n, 32, &ks, &vs));
+    k_relabel_perm<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(vs, bp<uint32_t>(g->out_deg), n, bp<uint32_t>(g->perm),
+                                                             bp<uint32_t>(g->deg_p));
+    ctx->launches++;
+    // entries in the new ids: stable sort by new src, then by new dst
+    if (M) {
+        k_relabel_entries<<<grid_for(ctx, M), 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.rid), bp<uint32_t>(g->csc.col),
+                                                                    bp<uint32_t>(g->perm), M, bp<uint32_t>(ka),
+                                                                    bp<uint32_t>(va));
+        ctx->launches++;
+    }
+    const int bits = n <= 1 ? 1 : 32 - __builtin_clz(n - 1);
+    RTRY(eg_radix_sort(ctx, bp<uint32_t>(ka), bp<uint32_t>(va), bp<uint32_t>(kb), bp<uint32_t>(vb), M, bits, &ks, &vs));
+    uint32_t *kt = (ks == bp<uint32_t>(ka)) ? bp<uint32_t>(kb) : bp<uint32_t>(ka);
+    uint32_t *vt = (ks == bp<uint32_t>(ka)) ? bp<uint32_t>(vb) : bp<uint32_t>(va);
+    RTRY(eg_radix_sort(ctx, vs, ks, kt, vt, M, bits, &ks, &vs));  // keys: new dst, values: new src
+    RTRY(eg_buf_ensure(ctx, g->csc_p.ptr, ((uint64_t)n + 1) * 4));
+    RTRY(eg_buf_ensure(ctx, g->csc_p.col, M * 4 + 16));
+    RTRY(eg_buf_ensure(ctx, g->csc_p.rid, M * 4 + 16));
+    if (M) {
+        if (cudaMemcpyAsync(g->csc_p.col.p, vs, M * 4, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess ||
+            cudaMemcpyAsync(g->csc_p.rid.p, ks, M * 4, cudaMemcpyDeviceToDevice, ctx->stream) != cudaSuccess)
+            RTRY(eg_fail(EG_ECUDA, "relabel copy"));
+    }
+    // row pointers from the row histogram (reuse kb/vb: no longer needed)
+    uint32_t *hist = bp<uint32_t>(ka);  // stream order: the copies above have read ks/vs first
+    if (cudaMemsetAsync(hist, 0, (uint64_t)n * 4, ctx->stream) != cudaSuccess) RTRY(eg_fail(EG_ECUDA, "memset"));
+    RTRY(eg_histogram(ctx, bp<uint32_t>(g->csc_p.rid), M, hist));
+    RTRY(eg_exscan_u32(ctx, hist, bp<uint32_t>(g->csc_p.ptr), n));
+    if (cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        RTRY(eg_fail(EG_ECUDA, "relabel: %s", cudaGetErrorString(cudaGetLastError())));
+#undef RTRY
+    cleanup();
+    g->relabeled = true;
     return EG_OK;
 }
 

@@ -95,19 +95,25 @@ struct eg_graph {
     eg_buf pairs;  // uint32[2*m_in]
     eg_adj csr, csc;
     eg_buf out_deg, in_deg;  // uint32[n]
+    // PageRank's copy of the CSC with vertices relabelled by descending
+    // out-degree (hot sources contiguous): perm[old] = new, deg_p[new]
+    eg_adj csc_p;
+    eg_buf perm, deg_p;
+    bool relabeled = false;
     // grid
     uint32_t grid_p;
     eg_buf cell_ptr, gsrc, gdst;
     // schedules (CSC rows for PR/SpMV pull, CSR rows for push)
     eg_mp_sched sched_csc, sched_csr;
     // algorithm state, allocated on first use and reused
-    eg_buf rank, contrib0, contrib1, pr_part, pr_stats, mp_carry, errflag;
+    eg_buf rank, rank_p, contrib0, contrib1, pr_part, pr_stats, mp_carry, errflag;
     eg_buf level, parent, dist, label, spmv_x, spmv_y, spmv_vals;
     uint64_t spmv_vals_seed;
     int spmv_vals_kind;
     eg_buf bfs_work;  // bitmaps, queues, counters
     eg_buf msbfs_work;
     eg_buf sssp_work;
+    eg_buf ppr_work;
     eg_bfs_graph bfsg[2];  // without / with parents
 };
 
@@ -124,6 +130,8 @@ int eg_histogram(eg_ctx *ctx, const uint32_t *keys, uint64_t len, uint32_t *hist
 int eg_radix_sort(eg_ctx *ctx, uint32_t *k_in, uint32_t *v_in, uint32_t *k_tmp, uint32_t *v_tmp, uint64_t len,
                   int bits, uint32_t **k_out, uint32_t **v_out);
 int eg_build_sched(eg_graph *g, eg_adj &adj, eg_mp_sched &s, uint32_t items);
+// builds g->csc_p / perm / deg_p from the CSC and out-degrees (once)
+int eg_build_relabeled_csc(eg_graph *g);
 
 // ---------------------------------------------------------------- device utils
 #ifdef __CUDACC__

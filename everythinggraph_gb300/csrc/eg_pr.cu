@@ -4,6 +4,10 @@
 // the grid PR loop (prgrid_cilk.c:62-76,111-141) whose per-destination sum
 // order equals the CSC order, and the SpMV loops (spmv.c:98-135).
 //
+// PageRank runs on a copy of the CSC whose vertices are relabelled by
+// descending out-degree (built once, eg_build_relabeled_csc): the most
+// gathered contrib entries are then contiguous, so they share cache sectors
+// and stay in L1; ranks are mapped back to the original ids at the end.
 // Per PageRank iteration the device runs three kernels:
 //   k_mp_rows<PrOp>   rank[v] = base + d * sum_{u in in(v)} contrib[u]
 //                     contrib'[v] = rank[v] / deg[v] (fused into the write)
@@ -131,6 +135,11 @@ __global__ void k_pr_init(uint32_t n, float prev_init, const uint32_t *__restric
         for (int w = 0; w < (int)(blockDim.x >> 5); w++) s += s_red[w];
         part[blockIdx.x] = make_double2(0.0, s);
     }
+}
+
+__global__ void k_pr_unpermute(const float *__restrict__ rank_p, const uint32_t *__restrict__ perm, uint32_t n,
+                               float *__restrict__ rank) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) rank[v] = rank_p[perm[v]];
 }
 
 // One block: deterministic FP64 sum of the partials, next base, stop test.
@@ -274,15 +283,15 @@ static int pr_iterations(eg_graph *g, const eg_pr_opts &o, eg_pr_dev *st, double
         bool odd = o.swap && (it & 1);
         op.cin = odd ? bp<float>(g->contrib1) : bp<float>(g->contrib0);
         op.cout = odd ? bp<float>(g->contrib0) : bp<float>(g->contrib1);
-        op.rank = bp<float>(g->rank);
-        op.deg = bp<uint32_t>(g->out_deg);
+        op.rank = bp<float>(g->rank_p);
+        op.deg = bp<uint32_t>(g->deg_p);
         op.st = st;
         op.mult = o.deg_multiplier;
         op.damping = o.damping;
         op.residual = o.tolerance > 0.0;
         op.base = 0.f;
         uint32_t nparts = 0;
-        EG_TRY((coo_launch<PrOp<COMP>, REDUCE>(g, g->csc, carry, part, op, &nparts)));
+        EG_TRY((coo_launch<PrOp<COMP>, REDUCE>(g, g->csc_p, carry, part, op, &nparts)));
         (void)grid;
         k_pr_reduce<<<1, 256, 0, ctx->stream>>>(part, REDUCE ? nparts : 0, st, g->n, o.damping, o.dangling,
                                                 o.tolerance, 1);
@@ -307,7 +316,9 @@ extern "C" int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out,
     const uint32_t coo_tiles = g->m ? eg_div_up(g->m, EG_COO_TILE) : 0;
     const uint32_t nparts = ntiles + eg_div_up((uint64_t)ntiles * 32, 256) + 2 * eg_div_up((uint64_t)coo_tiles * 32, 256) +
                             (uint32_t)ctx->sm_count * 8;
+    EG_TRY(eg_build_relabeled_csc(g));
     EG_TRY(eg_buf_ensure(ctx, g->rank, (uint64_t)n * 4));
+    EG_TRY(eg_buf_ensure(ctx, g->rank_p, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->contrib0, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->contrib1, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->pr_part, ((uint64_t)nparts + 1024) * sizeof(double2)));
@@ -323,8 +334,8 @@ extern "C" int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out,
     const bool reduce = o.tolerance > 0.0 || o.dangling;
     uint32_t ib = eg_div_up(n, 256);
     if (ib > 1024) ib = 1024;
-    k_pr_init<<<ib, 256, 0, ctx->stream>>>(n, prev_init, bp<uint32_t>(g->out_deg), o.deg_multiplier, bp<float>(g->rank),
-                                          bp<float>(g->contrib0), part);
+    k_pr_init<<<ib, 256, 0, ctx->stream>>>(n, prev_init, bp<uint32_t>(g->deg_p), o.deg_multiplier,
+                                          bp<float>(g->rank_p), bp<float>(g->contrib0), part);
     EG_LAUNCHED(ctx);
     k_pr_reduce<<<1, 256, 0, ctx->stream>>>(part, ib, st, n, o.damping, o.dangling, 0.0, 0);
     EG_LAUNCHED(ctx);
@@ -338,6 +349,9 @@ extern "C" int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out,
         else EG_TRY((pr_iterations<false, false>(g, o, st, part, carry)));
     }
     EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    // ranks back to the original vertex ids
+    k_pr_unpermute<<<ib, 256, 0, ctx->stream>>>(bp<float>(g->rank_p), bp<uint32_t>(g->perm), n, bp<float>(g->rank));
+    EG_LAUNCHED(ctx);
     eg_pr_dev hst;
     int herr = 0;
     EG_CUDA(cudaMemcpyAsync(&hst, st, sizeof(hst), cudaMemcpyDeviceToHost, ctx->stream));

@@ -248,6 +248,29 @@ typedef struct {
 } eg_wcc_stats;
 int eg_wcc(eg_graph *g, int64_t *labels_out, eg_wcc_stats *stats);
 
+/* ---- personalised PageRank, batched ---------------------------------------
+ * No counterpart in the reference (which runs one global PageRank; the
+ * iteration is pr_numa.c:245-277,396 with teleport to a seed set).  Up to 32
+ * queries per call, query q seeded by seeds[seed_offsets[q] ..
+ * seed_offsets[q+1]): x' = d * A^T D^-1 x + (1 - d + d * dangling(x)) * t,
+ * t uniform over the seeds, x0 = t.  Query q stops when the FP64 L1 change
+ * of its vector is below tolerance[q] or after max_iters.  Each query's
+ * result is bit-identical alone or in any batch.  ranks_out: nq*n floats
+ * (row q for query q) or NULL. */
+typedef struct {
+    float damping;
+    int max_iters;
+    float tolerance[32];
+} eg_ppr_opts;
+typedef struct {
+    int iterations[32];
+    double residual[32];
+    int sweeps; /* batch iterations run */
+    float ms;
+} eg_ppr_stats;
+int eg_ppr_multi(eg_graph *g, const uint32_t *seeds, const uint32_t *seed_offsets, int nq, const eg_ppr_opts *opts,
+                 float *ranks_out, eg_ppr_stats *stats);
+
 /* ---- allocation-free SpMV ------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory (a host callback, a plug-in inside a process whose allocator it does

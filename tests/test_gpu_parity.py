@@ -335,3 +335,23 @@ def test_big_wcc_and_sssp_properties(big):
     ok = (d[src] != INF) & (src != col)
     assert np.all(d[col][ok] <= d[src][ok] + wa[ok])  # no edge can still be relaxed
     assert d[r] == 0
+
+
+# ------------------------------------------------------------------ personalised PageRank
+def test_ppr_batch_vs_fp64_and_alone(case):
+    name, n, pairs, rec, g, gu, adj, adju = case
+    rng = np.random.default_rng(7)
+    nz = np.nonzero(adj.out_deg() > 0)[0]
+    seed_lists = [rng.choice(nz, size=int(rng.integers(1, 9))).astype(np.uint32) for _ in range(12)]
+    tols = [1e-4, 1e-5, 1e-6, 1e-7] * 3
+    R, st = g.ppr(seed_lists, tolerance=tols, max_iters=50)
+    for q, seeds in enumerate(seed_lists):
+        ref, it_ref = oracle.ppr_f64(adj, adj.out_deg(), seeds, tol=tols[q], max_iters=50)
+        l1 = np.abs(R[q] - ref).sum() / np.abs(ref).sum()
+        assert l1 <= 1e-5, (q, l1)
+        assert abs(st.iterations[q] - it_ref) <= 1, (q, st.iterations[q], it_ref)
+    # each query alone gives the same bits as in the batch
+    for q in (0, 5, 11):
+        Ra, sta = g.ppr([seed_lists[q]], tolerance=[tols[q]], max_iters=50)
+        np.testing.assert_array_equal(Ra[0].view(np.uint32), R[q].view(np.uint32))
+        assert sta.iterations[0] == st.iterations[q]
