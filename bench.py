@@ -213,6 +213,72 @@ def kernel_reports(ctx, eg, scale, args):
     return rep
 
 
+def serve_report(ctx, eg, scale, rate, nq, seed=7, plain_sample=40):
+    """Serving workload: Poisson arrivals at `rate` qps of 60% BFS, 25% SSSP
+    (u32 weights U[1,255]), 15% personalised PageRank (1-8 seeds, tolerance
+    10^U(-7,-4), <= 50 iterations) on the resident undirected RMAT graph;
+    p50/p99 latency (arrival -> completion) and QPS, next to the QPS of the
+    plain one-query-at-a-time kernels on a sample of the same queries."""
+    import torch
+    n = 1 << scale
+    g = ctx.rmat(scale, 16 * n, 2, undirected=True).build(eg.CSR | eg.CSC)
+    od, _ = g.degrees(True, False)
+    nz = np.nonzero(od > 0)[0].astype(np.uint32)
+    rng = np.random.default_rng(seed)
+    kinds = rng.choice(3, size=nq, p=[0.60, 0.25, 0.15])
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, size=nq))
+    qs = []
+    for i in range(nq):
+        if kinds[i] == 0:
+            qs.append(("bfs", int(rng.choice(nz)), None, 0.0))
+        elif kinds[i] == 1:
+            qs.append(("sssp", int(rng.choice(nz)), None, 0.0))
+        else:
+            k = int(rng.integers(1, 9))
+            qs.append(("ppr", 0, [int(x) for x in rng.choice(nz, size=k)], float(10 ** rng.uniform(-7, -4))))
+    w = eg.weights("hash", seed=6, lo=1, hi=255)
+    srv = eg.Server(g, hbm_budget=64 << 30, weights_=w)
+    torch.cuda.synchronize()
+    t_start = srv.info()["clock_s"]
+    arrivals = arrivals + t_start
+    done = []
+    i = 0
+    while len(done) < nq:
+        now = srv.info()["clock_s"]
+        while i < nq and arrivals[i] <= now:
+            kind, src, seeds, tol = qs[i]
+            if kind == "ppr":
+                srv.submit("ppr", seeds=seeds, tol=tol, arrival=float(arrivals[i]))
+            else:
+                srv.submit(kind, source=src, arrival=float(arrivals[i]))
+            i += 1
+        active = srv.step()
+        done.extend(srv.poll())
+        if active == 0 and i < nq:  # idle: wait for the next arrival
+            time.sleep(max(0.0, min(0.001, arrivals[i] - srv.info()["clock_s"])))
+    info = srv.info()
+    srv.close()
+    lat = np.array([r.done_s - r.arrival_s for r in done]) * 1e3
+    span = max(r.done_s for r in done) - arrivals[0]
+    # plain kernels, one query at a time, on a sample of the same mix
+    samp = list(range(min(plain_sample, nq)))
+    t0 = time.perf_counter()
+    for j in samp:
+        kind, src, seeds, tol = qs[j]
+        if kind == "bfs":
+            g.bfs(src, copy_out=False)
+        elif kind == "sssp":
+            g.sssp(src, w, copy_out=False)
+        else:
+            g.ppr([seeds], tolerance=tol, copy_out=False)
+    plain_qps = len(samp) / (time.perf_counter() - t0)
+    g.free()
+    qps = nq / span
+    return {"workload": "serve rmat%d undirected, %d queries, Poisson %g qps offered" % (scale, nq, rate),
+            "qps": qps, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "plain_qps": plain_qps, "speedup_vs_plain": qps / plain_qps, "slots": info}
+
+
 def cpu_baseline(g, eg, roots, n, m_in, args):
     """The multi-threaded CPU port of the reference loops (bfs_simple's
     direction-optimising iterator, wcc's label propagation) on a bounded
@@ -292,8 +358,18 @@ def main():
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--pr-only", action="store_true", help="only the PageRank pull report (profiling)")
+    ap.add_argument("--serve-only", action="store_true", help="only the serving report")
+    ap.add_argument("--rate", type=float, default=20000.0)
+    ap.add_argument("--queries", type=int, default=2000)
     args = ap.parse_args()
-    if args.pr_only:
+    if args.serve_only:
+        import everythinggraph_gb300 as eg
+        from everythinggraph_gb300 import build
+        build.build_lib()
+        ctx = eg.Context(0)
+        print(json.dumps(serve_report(ctx, eg, args.scale or 24, args.rate, args.queries)))
+        ctx.close()
+    elif args.pr_only:
         import everythinggraph_gb300 as eg
         from everythinggraph_gb300 import build
         build.build_lib()

@@ -245,3 +245,66 @@ class Graph:
         st = L.WccStats()
         L.check(lib().eg_wcc(self._h, _ptr(out), ctypes.byref(st)))
         return out, st
+
+
+class Server:
+    """Continuous-batching query server over a resident graph (eg_serve_*)."""
+
+    KINDS = {"bfs": L.EG_Q_BFS, "sssp": L.EG_Q_SSSP, "ppr": L.EG_Q_PPR}
+
+    def __init__(self, graph, hbm_budget=64 << 30, weights_=None, keep_results=False, max_bfs=64, max_sssp=64,
+                 max_ppr=32, ppr_max_iters=50):
+        self.graph = graph
+        o = L.ServeOpts()
+        lib().eg_serve_opts_default(ctypes.byref(o))
+        o.hbm_budget, o.keep_results = hbm_budget, int(keep_results)
+        o.max_bfs, o.max_sssp, o.max_ppr, o.ppr_max_iters = max_bfs, max_sssp, max_ppr, ppr_max_iters
+        if weights_ is not None:
+            o.weights = weights_
+        self._h = ctypes.c_void_p()
+        L.check(lib().eg_serve_open(graph._h, ctypes.byref(o), ctypes.byref(self._h)))
+
+    def close(self):
+        if self._h:
+            lib().eg_serve_close(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, kind, source=0, seeds=(), tol=1e-6, arrival=0.0):
+        q = L.Query()
+        q.kind = self.KINDS[kind]
+        q.source = source
+        q.nseeds = len(seeds)
+        for i, s_ in enumerate(seeds):
+            q.seeds[i] = int(s_)
+        q.tol, q.arrival_s = tol, arrival
+        qid = ctypes.c_uint64()
+        L.check(lib().eg_serve_submit(self._h, ctypes.byref(q), ctypes.byref(qid)))
+        return qid.value
+
+    def step(self):
+        a = ctypes.c_int()
+        L.check(lib().eg_serve_step(self._h, ctypes.byref(a)))
+        return a.value
+
+    def poll(self, max_results=4096):
+        buf = (L.QueryResult * max_results)()
+        c = ctypes.c_int()
+        L.check(lib().eg_serve_poll(self._h, buf, max_results, ctypes.byref(c)))
+        return [buf[i] for i in range(c.value)]
+
+    def take_result(self):
+        n = self.graph.n
+        out = np.empty(n, dtype=np.uint32)
+        L.check(lib().eg_serve_take_result(self._h, _ptr(out), n))
+        return out
+
+    def info(self):
+        b, s_, p, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()
+        L.check(lib().eg_serve_info(self._h, ctypes.byref(b), ctypes.byref(s_), ctypes.byref(p), ctypes.byref(t)))
+        return {"bfs_slots": b.value, "sssp_slots": s_.value, "ppr_slots": p.value, "clock_s": t.value}

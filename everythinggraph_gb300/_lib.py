@@ -21,6 +21,7 @@ EG_DEV_RANK, EG_DEV_LEVEL, EG_DEV_PARENT, EG_DEV_DIST, EG_DEV_LABEL, EG_DEV_SPMV
 EG_SPMV_U32_PULL, EG_SPMV_U32_PUSH, EG_SPMV_U32_EDGE, EG_SPMV_F32, EG_SPMV_F32_COMP, EG_SPMV_F64 = 0, 1, 2, 3, 4, 5
 EG_BFS_AUTO, EG_BFS_PUSH_ONLY, EG_BFS_PULL_ONLY = 0, 1, 2
 EG_W_REF, EG_W_HASH, EG_W_UNIT = 0, 1, 2
+EG_Q_BFS, EG_Q_SSSP, EG_Q_PPR = 1, 2, 3
 
 
 class GraphInfo(ctypes.Structure):
@@ -67,6 +68,21 @@ class PprStats(ctypes.Structure):
     _fields_ = [("iterations", c_int * 32), ("residual", c_f64 * 32), ("sweeps", c_int), ("ms", c_f32)]
 
 
+class Query(ctypes.Structure):
+    _fields_ = [("kind", c_int), ("source", c_u32), ("nseeds", c_u32), ("seeds", c_u32 * 8), ("tol", c_f32),
+                ("arrival_s", c_f64)]
+
+
+class QueryResult(ctypes.Structure):
+    _fields_ = [("id", c_u64), ("kind", c_int), ("arrival_s", c_f64), ("admit_s", c_f64), ("done_s", c_f64),
+                ("reached", c_u32), ("depth", c_u32), ("iterations", c_int), ("value", c_f64)]
+
+
+class ServeOpts(ctypes.Structure):
+    _fields_ = [("hbm_budget", c_u64), ("max_bfs", c_int), ("max_sssp", c_int), ("max_ppr", c_int),
+                ("weights", Weights), ("ppr_damping", c_f32), ("ppr_max_iters", c_int), ("keep_results", c_int)]
+
+
 class WccStats(ctypes.Structure):
     _fields_ = [("rounds", c_int), ("components", c_u32), ("ms", c_f32)]
 
@@ -106,6 +122,14 @@ SIGNATURES = {
     "eg_wcc": (c_int, [c_void_p, c_void_p, P(WccStats)]),
     "eg_sample_roots": (c_int, [c_void_p, c_int, c_u64, c_void_p]),
     "eg_ppr_multi": (c_int, [c_void_p, c_void_p, c_void_p, c_int, P(PprOpts), c_void_p, P(PprStats)]),
+    "eg_serve_opts_default": (None, [P(ServeOpts)]),
+    "eg_serve_open": (c_int, [c_void_p, P(ServeOpts), P(c_void_p)]),
+    "eg_serve_submit": (c_int, [c_void_p, P(Query), P(c_u64)]),
+    "eg_serve_step": (c_int, [c_void_p, P(c_int)]),
+    "eg_serve_poll": (c_int, [c_void_p, c_void_p, c_int, P(c_int)]),
+    "eg_serve_take_result": (c_int, [c_void_p, c_void_p, c_u32]),
+    "eg_serve_info": (c_int, [c_void_p, P(c_int), P(c_int), P(c_int), P(c_f64)]),
+    "eg_serve_close": (c_int, [c_void_p]),
     "eg_spmv_f32_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_u32, c_u64, c_void_p]),
 }
 

@@ -585,7 +585,9 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
     else eg_bfs_opts_default(&o);
     if (o.direction < EG_BFS_AUTO || o.direction > EG_BFS_PULL_ONLY) return eg_fail(EG_EINVAL, "bad direction");
     const bool undirected = (g->flags & EG_UNDIRECTED) != 0;
-    eg_adj *in_adj = undirected ? &g->csr : ((g->built & EG_LAYOUT_CSC) ? &g->csc : nullptr);
+    // in-lists: the CSC when built (sorted by source id, so RMAT hubs come first
+    // and bottom-up scans stop early); an undirected CSR is its own transpose
+    eg_adj *in_adj = (g->built & EG_LAYOUT_CSC) ? &g->csc : (undirected ? &g->csr : nullptr);
     if (!in_adj && o.direction != EG_BFS_PUSH_ONLY)
         return eg_fail(EG_ENOTBUILT, "bottom-up BFS on a directed graph needs the CSC");
     eg_ctx *ctx = g->ctx;
@@ -879,7 +881,9 @@ extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *
     if (k < 1 || k > 64) return eg_fail(EG_EINVAL, "k=%d sources: bit-sliced BFS takes 1..64", k);
     if (!(g->built & EG_LAYOUT_CSR)) return eg_fail(EG_ENOTBUILT, "BFS needs the CSR");
     const bool undirected = (g->flags & EG_UNDIRECTED) != 0;
-    eg_adj *in_adj = undirected ? &g->csr : ((g->built & EG_LAYOUT_CSC) ? &g->csc : nullptr);
+    // in-lists: the CSC when built (sorted by source id, so RMAT hubs come first
+    // and bottom-up scans stop early); an undirected CSR is its own transpose
+    eg_adj *in_adj = (g->built & EG_LAYOUT_CSC) ? &g->csc : (undirected ? &g->csr : nullptr);
     if (!in_adj) return eg_fail(EG_ENOTBUILT, "multi-source BFS on a directed graph needs the CSC");
     for (int s = 0; s < k; s++)
         if (roots[s] >= g->n) return eg_fail(EG_EINVAL, "root %u >= n", roots[s]);

@@ -1,0 +1,212 @@
+// Kernels of the batched personalised PageRank (see eg_ppr.cu), shared with
+// the query server.  Internal linkage: each translation unit has its copy.
+#pragma once
+#include "eg_internal.cuh"
+
+#define EG_PPR_LANES 32
+#define EG_PPR_TILE 1024
+#define EG_PPR_NONE 0xffffffffu
+
+namespace {
+
+struct PprQ {  // per-query state (device)
+    double residual;
+    double dangling;
+    float tol;
+    int iters;
+    int max_iters;
+    int done;
+    int nseeds;
+    int active;  // lane in use
+};
+
+// Y[v][q] = sum over CSC entries of row v of X[u][q], for the rows whose
+// entries lie in this warp's tile; rows open at the tile ends go to carries.
+__global__ void __launch_bounds__(256) k_ppr_rows(const uint32_t *__restrict__ rid, const uint32_t *__restrict__ col,
+                                                  uint32_t m, uint32_t ntiles, const float *__restrict__ X,
+                                                  float *__restrict__ Y, float *__restrict__ head_val,
+                                                  float *__restrict__ tail_val, uint32_t *__restrict__ head_row) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (t >= ntiles) return;
+    const uint32_t E0 = t * EG_PPR_TILE, E1 = min(E0 + EG_PPR_TILE, m);
+    const uint32_t first = __ldg(rid + E0);
+    const uint32_t hrow = (E0 > 0 && __ldg(rid + E0 - 1) == first) ? first : EG_PPR_NONE;
+    const uint32_t tnext = E1 < m ? __ldg(rid + E1) : EG_PPR_NONE;
+    float acc = 0.f;
+    uint32_t cur = first;
+    bool hdone = false;
+    float hval = 0.f;
+    for (uint32_t base = E0; base < E1; base += 32) {
+        const uint32_t e = base + lane;
+        const uint32_t my_r = e < E1 ? __ldg(rid + e) : EG_PPR_NONE;
+        const uint32_t my_c = e < E1 ? __ldg(col + e) : 0u;
+        const uint32_t cnt = min(32u, E1 - base);
+        for (uint32_t j = 0; j < cnt; j++) {
+            const uint32_t r = __shfl_sync(EG_FULL_MASK, my_r, j);
+            const uint32_t u = __shfl_sync(EG_FULL_MASK, my_c, j);
+            if (r != cur) {  // row `cur` ended inside the tile
+                if (cur == hrow) {
+                    hdone = true;
+                    hval = acc;
+                } else {
+                    Y[(uint64_t)cur * EG_PPR_LANES + lane] = acc;
+                }
+                acc = 0.f;
+                cur = r;
+            }
+            acc += __ldg(X + (uint64_t)u * EG_PPR_LANES + lane);
+        }
+    }
+    // the last row: complete if the next tile starts another row
+    if (tnext != cur) {
+        if (cur == hrow) {
+            hdone = true;
+            hval = acc;
+        } else {
+            Y[(uint64_t)cur * EG_PPR_LANES + lane] = acc;
+        }
+        tail_val[(uint64_t)t * EG_PPR_LANES + lane] = 0.f;
+    } else {
+        tail_val[(uint64_t)t * EG_PPR_LANES + lane] = acc;
+    }
+    if (lane == 0) head_row[t] = hdone ? hrow : EG_PPR_NONE;
+    if (hdone) head_val[(uint64_t)t * EG_PPR_LANES + lane] = hval;
+}
+
+// Rows split between tiles: a warp per tile with a head row adds the tails of
+// the preceding tiles (nearest first is irrelevant: the order is fixed).
+__global__ void k_ppr_fixup(const uint32_t *__restrict__ ptr, uint32_t ntiles, const uint32_t *__restrict__ head_row,
+                            const float *__restrict__ head_val, const float *__restrict__ tail_val,
+                            float *__restrict__ Y) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (t >= ntiles) return;
+    const uint32_t row = head_row[t];
+    if (row == EG_PPR_NONE) return;
+    const uint32_t rstart = ptr[row];
+    float tot = 0.f;
+    for (int k = (int)t - 1; k >= 0; k--) {
+        tot += tail_val[(uint64_t)k * EG_PPR_LANES + lane];
+        if (rstart >= (uint32_t)k * EG_PPR_TILE) break;  // the row begins in tile k
+    }
+    tot += head_val[(uint64_t)t * EG_PPR_LANES + lane];
+    Y[(uint64_t)row * EG_PPR_LANES + lane] = tot;
+}
+
+// Rows without in-edges sum to zero.
+__global__ void k_ppr_empty(const uint32_t *__restrict__ ptr, uint32_t n, float *__restrict__ Y) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps)
+        if (ptr[v] == ptr[v + 1]) Y[(uint64_t)v * EG_PPR_LANES + lane] = 0.f;
+}
+
+// Teleport plus returned dangling mass at the seeds: Y[s][q] += c_q / d so that
+// d * Y carries (1 - d + d * dangling_q) / nseeds_q at every seed occurrence.
+// Query q's seeds are seeds[sbeg[q] .. send[q]).
+__global__ void k_ppr_seeds(const uint32_t *__restrict__ seeds, const uint32_t *__restrict__ sbeg,
+                            const uint32_t *__restrict__ send, int nq, const PprQ *__restrict__ qs, float d,
+                            float *__restrict__ Y) {
+    const int q = threadIdx.x;
+    if (q >= nq || !qs[q].active || qs[q].done) return;
+    const float c = (float)(((1.0 - (double)d) + (double)d * qs[q].dangling) / ((double)qs[q].nseeds * (double)d));
+    for (uint32_t i = sbeg[q]; i < send[q]; i++) Y[(uint64_t)seeds[i] * EG_PPR_LANES + q] += c;
+}
+
+// R = d * Y, X = R / deg; per-block FP64 partials of |R - R_old| and of the
+// mass on out-degree-0 vertices, per query.
+__global__ void __launch_bounds__(256) k_ppr_finish(const float *__restrict__ Y, const uint32_t *__restrict__ deg,
+                                                    uint32_t n, float d, const PprQ *__restrict__ qs,
+                                                    float *__restrict__ R, float *__restrict__ X,
+                                                    double2 *__restrict__ part) {
+    __shared__ double2 s_part[8][EG_PPR_LANES];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const bool live = qs[lane].active && !qs[lane].done;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    double res = 0.0, dang = 0.0;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
+        if (!live) continue;
+        const uint64_t i = (uint64_t)v * EG_PPR_LANES + lane;
+        const float r = d * Y[i];
+        res += fabs((double)r - (double)R[i]);
+        R[i] = r;
+        const uint32_t dv = deg[v];
+        X[i] = dv ? __fdiv_rn(r, (float)dv) : 0.f;
+        if (!dv) dang += (double)r;
+    }
+    s_part[warp][lane] = make_double2(res, dang);
+    __syncthreads();
+    if (warp == 0) {
+        double2 s = make_double2(0.0, 0.0);
+        for (int w = 0; w < 8; w++) {
+            s.x += s_part[w][lane].x;
+            s.y += s_part[w][lane].y;
+        }
+        part[(uint64_t)blockIdx.x * EG_PPR_LANES + lane] = s;
+    }
+}
+
+// Per query: fixed-order FP64 sum of the block partials, stop test.
+__global__ void k_ppr_reduce(const double2 *__restrict__ part, uint32_t nblocks, PprQ *qs, int count_iter) {
+    const int q = threadIdx.x;
+    if (q >= EG_PPR_LANES) return;
+    PprQ &s = qs[q];
+    if (!s.active || s.done) return;
+    double res = 0.0, dang = 0.0;
+    for (uint32_t b = 0; b < nblocks; b++) {
+        res += part[(uint64_t)b * EG_PPR_LANES + q].x;
+        dang += part[(uint64_t)b * EG_PPR_LANES + q].y;
+    }
+    s.dangling = dang;
+    if (count_iter) {
+        s.residual = res;
+        s.iters += 1;
+        if (res < (double)s.tol || s.iters >= s.max_iters) s.done = 1;
+    }
+}
+
+// Zero the columns of the lanes in `mask` (every lane: mask = ~0).
+__global__ void k_ppr_init(uint32_t n, uint32_t mask, float *R, float *X) {
+    const uint64_t total = (uint64_t)n * EG_PPR_LANES;
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x) {
+        if (!((mask >> (i & 31)) & 1u)) continue;
+        R[i] = 0.f;
+        X[i] = 0.f;
+    }
+}
+// Lanes in `mask` start from R = t: their columns must be zero on entry.
+__global__ void k_ppr_init_seeds(const uint32_t *__restrict__ seeds, const uint32_t *__restrict__ sbeg,
+                                 const uint32_t *__restrict__ send, uint32_t mask, const PprQ *qs,
+                                 const uint32_t *__restrict__ deg, float *R, float *X) {
+    const int q = threadIdx.x;
+    if (q >= EG_PPR_LANES || !((mask >> q) & 1u) || !qs[q].active) return;
+    const float w = 1.0f / (float)qs[q].nseeds;
+    for (uint32_t i = sbeg[q]; i < send[q]; i++) R[(uint64_t)seeds[i] * EG_PPR_LANES + q] += w;
+    for (uint32_t i = sbeg[q]; i < send[q]; i++) {
+        const uint32_t s = seeds[i];
+        const uint32_t dv = deg[s];
+        X[(uint64_t)s * EG_PPR_LANES + q] = dv ? __fdiv_rn(R[(uint64_t)s * EG_PPR_LANES + q], (float)dv) : 0.f;
+    }
+}
+__global__ void k_ppr_init_dangling(const uint32_t *__restrict__ seeds, const uint32_t *__restrict__ sbeg,
+                                    const uint32_t *__restrict__ send, uint32_t mask,
+                                    const uint32_t *__restrict__ deg, const float *R, PprQ *qs) {
+    const int q = threadIdx.x;
+    if (q >= EG_PPR_LANES || !((mask >> q) & 1u) || !qs[q].active) return;
+    double dang = 0.0;
+    for (uint32_t i = sbeg[q]; i < send[q]; i++) {
+        const uint32_t s = seeds[i];
+        bool first = true;  // count each distinct seed once
+        for (uint32_t j = sbeg[q]; j < i; j++) first &= seeds[j] != s;
+        if (first && deg[s] == 0) dang += (double)R[(uint64_t)s * EG_PPR_LANES + q];
+    }
+    qs[q].dangling = dang;
+}
+
+__global__ void k_ppr_extract(const float *__restrict__ R, uint32_t n, int q, float *__restrict__ out) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        out[v] = R[(uint64_t)v * EG_PPR_LANES + q];
+}
+
+}  // namespace

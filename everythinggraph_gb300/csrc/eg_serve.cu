@@ -1,0 +1,885 @@
+// Query server: continuous batching of BFS, SSSP and personalised-PageRank
+// queries over one resident graph.
+//
+// No counterpart in the reference (it runs one algorithm per process).  Each
+// query kind has an engine with a fixed number of slots whose state lives in
+// HBM for the server's lifetime:
+//   BFS   64 slots, bit-sliced: bit s of seen[v]/front[v] (u64) is slot s
+//   SSSP  64 slots, dist[v][s] vertex-major, per-(vertex, slot) frontier bits
+//   PPR   32 lanes, x[v][q] vertex-major (the eg_ppr_multi iteration)
+// A scheduler tick admits queued queries into free slots (slot counts are
+// capped by the HBM budget), advances every engine that has live slots by one
+// step (one BFS level, one Bellman-Ford round, one PPR iteration) and retires
+// the slots whose query finished.  A slot's arithmetic never reads another
+// slot's values, so a query's result does not depend on what else is in the
+// batch.  Each engine's step is the same code whatever the slot occupancy.
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+
+#include <algorithm>
+#include <deque>
+#include <vector>
+
+#include "eg_ppr.cuh"
+
+#define SV_INF 0xfffffffeu
+#define SV_BFS_SLOTS 64
+#define SV_SSSP_SLOTS 64
+#define SV_PPR_LANES 32
+#define SV_BIG_DEG 2048u
+
+namespace {
+
+double now_s() {
+    struct timespec t;
+    clock_gettime(CLOCK_MONOTONIC, &t);
+    return (double)t.tv_sec + 1e-9 * (double)t.tv_nsec;
+}
+
+struct SvCounters {
+    unsigned long long deg;         // out-degree sum of the new frontier
+    unsigned long long newmask;     // BFS: slots that discovered vertices this level
+    unsigned long long actmask[4];  // SSSP: slots still relaxing (bits of the next frontier)
+    uint32_t count;                 // vertices in the new frontier
+    uint32_t qsize;
+    uint32_t nbig;
+    uint32_t pad;
+};
+
+// ------------------------------------------------------------------ BFS engine
+__global__ void k_sv_bfs_admit(const uint32_t *roots, const uint32_t *slots, int k, uint32_t n,
+                               unsigned long long *seen, unsigned long long *front, int32_t *levels) {
+    const int i = threadIdx.x;
+    if (i < k) {
+        const uint32_t r = roots[i], s = slots[i];
+        atomicOr(seen + r, 1ull << s);
+        atomicOr(front + r, 1ull << s);
+        levels[(uint64_t)s * n + r] = 1;
+    }
+}
+
+// pull: OR the frontier words of the in-neighbours (early exit when every
+// missing slot is found)
+__global__ void __launch_bounds__(256) k_sv_bfs_pull(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+                                                     uint32_t n, unsigned long long live,
+                                                     const unsigned long long *__restrict__ seen,
+                                                     const unsigned long long *__restrict__ front,
+                                                     unsigned long long *__restrict__ next) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const unsigned long long need = live & ~seen[v];
+        unsigned long long acc = 0ull;
+        if (need) {
+            for (uint32_t p = ptr[v]; p < ptr[v + 1]; p++) {
+                acc |= __ldg(front + col[p]);
+                if ((acc & need) == need) break;
+            }
+        }
+        next[v] = acc & need;
+    }
+}
+
+__global__ void k_sv_front_queue(const unsigned long long *__restrict__ front, uint32_t n, uint32_t *queue,
+                                 SvCounters *cnt) {
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t v0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); v0 < n; v0 += gridDim.x * blockDim.x) {
+        const uint32_t v = v0 + lane;
+        const bool on = v < n && front[v] != 0ull;
+        const uint32_t ball = __ballot_sync(EG_FULL_MASK, on);
+        if (ball) {
+            uint32_t base = 0;
+            if (lane == 0) base = atomicAdd(&cnt->qsize, __popc(ball));
+            base = __shfl_sync(EG_FULL_MASK, base, 0);
+            if (on) queue[base + __popc(ball & eg_lanemask_lt())] = v;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_sv_bfs_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+                                                     const uint32_t *__restrict__ queue, const SvCounters *qc,
+                                                     const unsigned long long *__restrict__ seen,
+                                                     const unsigned long long *__restrict__ front,
+                                                     unsigned long long *__restrict__ next, uint32_t *big,
+                                                     SvCounters *cnt) {
+    const uint32_t qlen = qc->qsize;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < qlen; qi += warps) {
+        const uint32_t u = queue[qi];
+        const uint32_t b = ptr[u], e = ptr[u + 1];
+        if (e - b > SV_BIG_DEG) {
+            if (lane == 0) big[atomicAdd(&cnt->nbig, 1u)] = u;
+            continue;
+        }
+        const unsigned long long f = front[u];
+        for (uint32_t p = b + lane; p < e; p += 32) {
+            const uint32_t v = col[p];
+            const unsigned long long add = f & ~__ldcg(seen + v);
+            if (add && (__ldcg(next + v) & add) != add) atomicOr(next + v, add);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) k_sv_bfs_push_big(const uint32_t *__restrict__ ptr,
+                                                         const uint32_t *__restrict__ col, const uint32_t *big,
+                                                         const unsigned long long *__restrict__ seen,
+                                                         const unsigned long long *__restrict__ front,
+                                                         unsigned long long *__restrict__ next, const SvCounters *cnt) {
+    const uint32_t nbig = *(volatile const uint32_t *)&cnt->nbig;
+    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
+    for (uint32_t bi = 0; bi < nbig; bi++) {
+        const uint32_t u = big[bi];
+        const unsigned long long f = front[u];
+        for (uint32_t p = ptr[u] + tid; p < ptr[u + 1]; p += nt) {
+            const uint32_t v = col[p];
+            const unsigned long long add = f & ~__ldcg(seen + v);
+            if (add && (__ldcg(next + v) & add) != add) atomicOr(next + v, add);
+        }
+    }
+}
+
+// seen |= new, levels of the new bits = slot level + 1, front = new, next = 0
+__global__ void k_sv_bfs_fold(uint32_t n, unsigned long long *seen, unsigned long long *front,
+                              unsigned long long *next, int32_t *levels, const int32_t *__restrict__ slot_level,
+                              const uint32_t *__restrict__ deg, SvCounters *cnt) {
+    unsigned long long my_new = 0ull, my_deg = 0ull;
+    uint32_t my_cnt = 0;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const unsigned long long x = next[v] & ~seen[v];
+        next[v] = 0ull;
+        front[v] = x;
+        if (x) {
+            seen[v] |= x;
+            my_new |= x;
+            my_cnt++;
+            my_deg += deg[v];
+            unsigned long long y = x;
+            while (y) {
+                const int s = __ffsll((long long)y) - 1;
+                y &= y - 1;
+                levels[(uint64_t)s * n + v] = slot_level[s] + 1;
+            }
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        my_new |= __shfl_down_sync(EG_FULL_MASK, my_new, o);
+        my_deg += __shfl_down_sync(EG_FULL_MASK, my_deg, o);
+        my_cnt += __shfl_down_sync(EG_FULL_MASK, my_cnt, o);
+    }
+    if ((threadIdx.x & 31) == 0 && my_cnt) {
+        atomicOr(&cnt->newmask, my_new);
+        atomicAdd(&cnt->deg, my_deg);
+        atomicAdd(&cnt->count, my_cnt);
+    }
+}
+
+// retiring slots: clear their bits everywhere
+__global__ void k_sv_bfs_clear(uint32_t n, unsigned long long keep, unsigned long long *seen,
+                               unsigned long long *front) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        seen[v] &= keep;
+        front[v] &= keep;
+    }
+}
+
+// reached count and deepest level of a slot's level row
+__global__ void k_sv_level_summary(const int32_t *__restrict__ row, uint32_t n, unsigned long long *out) {
+    unsigned long long c = 0, mx = 0;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const int32_t l = row[v];
+        c += l > 0;
+        mx = l > (int32_t)mx ? (unsigned long long)l : mx;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        c += __shfl_down_sync(EG_FULL_MASK, c, o);
+        mx = max(mx, __shfl_down_sync(EG_FULL_MASK, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out, c);
+        atomicMax(out + 1, mx);
+    }
+}
+
+// ------------------------------------------------------------------ SSSP engine
+struct SvW {
+    int rule;
+    uint64_t seed;
+    uint32_t lo;
+    uint64_t span;
+    __device__ __forceinline__ uint32_t operator()(uint32_t u, uint32_t v) const {
+        if (rule == EG_W_REF) return (u % 10u) + (v % 10u);
+        if (rule == EG_W_UNIT) return 1u;
+        return lo + (uint32_t)(((eg_edge_hash(seed, u, v) >> 32) * span) >> 32);
+    }
+};
+
+__global__ void k_sv_sssp_admit(const uint32_t *roots, const uint32_t *slots, int k, uint32_t *dist, uint32_t *act,
+                                uint32_t *inq, uint32_t *queue, SvCounters *cnt) {
+    const int i = threadIdx.x;
+    if (i < k) {
+        const uint32_t r = roots[i], s = slots[i];
+        dist[(uint64_t)r * SV_SSSP_SLOTS + s] = 0;
+        atomicOr(act + (uint64_t)r * 2 + (s >> 5), 1u << (s & 31));
+        const uint32_t bit = 1u << (r & 31);
+        if (!(atomicOr(inq + (r >> 5), bit) & bit)) queue[atomicAdd(&cnt->qsize, 1u)] = r;
+    }
+}
+
+__device__ __forceinline__ void sv_relax(uint32_t u, uint32_t v, uint32_t j, uint32_t s, bool on, uint32_t du,
+                                         const SvW &w, uint32_t *dist, uint32_t *next_act, uint32_t *next_inq,
+                                         uint32_t *next_queue, SvCounters *cnt) {
+    bool improved = false;
+    if (on && v != u) {
+        const uint64_t nd64 = (uint64_t)du + w(u, v);
+        const uint32_t nd = nd64 < SV_INF ? (uint32_t)nd64 : SV_INF;
+        uint32_t *dp = dist + (uint64_t)v * SV_SSSP_SLOTS + s;
+        if (nd < __ldcg(dp)) improved = nd < atomicMin(dp, nd);
+    }
+    const uint32_t ball = __ballot_sync(EG_FULL_MASK, improved);
+    if (ball && (threadIdx.x & 31) == 0) {
+        atomicOr(next_act + (uint64_t)v * 2 + j, ball);
+        atomicOr(&cnt->actmask[j], (unsigned long long)ball);
+        const uint32_t bit = 1u << (v & 31);
+        if (!(atomicOr(next_inq + (v >> 5), bit) & bit)) next_queue[atomicAdd(&cnt->qsize, 1u)] = v;
+    }
+}
+
+__global__ void __launch_bounds__(256) k_sv_sssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+                                                      const uint32_t *__restrict__ queue, const SvCounters *qc,
+                                                      uint32_t *dist, const uint32_t *__restrict__ act,
+                                                      uint32_t *next_act, uint32_t *next_inq, uint32_t *next_queue,
+                                                      SvW w, SvCounters *cnt, uint32_t *big) {
+    const uint32_t qlen = qc->qsize;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint64_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint64_t it = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; it < 2ull * qlen; it += warps) {
+        const uint32_t u = queue[it >> 1];
+        const uint32_t j = (uint32_t)(it & 1);
+        const uint32_t a = act[(uint64_t)u * 2 + j];
+        if (!a) continue;
+        const uint32_t b = ptr[u], e = ptr[u + 1];
+        if (e - b > SV_BIG_DEG) {
+            if (lane == 0) big[atomicAdd(&cnt->nbig, 1u)] = u * 2 + j;
+            continue;
+        }
+        const uint32_t s = j * 32 + lane;
+        const bool on = (a >> lane) & 1u;
+        const uint32_t du = on ? __ldcg(dist + (uint64_t)u * SV_SSSP_SLOTS + s) : SV_INF;
+        for (uint32_t p = b; p < e; p++) sv_relax(u, col[p], j, s, on, du, w, dist, next_act, next_inq, next_queue, cnt);
+    }
+}
+
+__global__ void __launch_bounds__(256) k_sv_sssp_push_big(const uint32_t *__restrict__ ptr,
+                                                          const uint32_t *__restrict__ col, uint32_t *dist,
+                                                          const uint32_t *__restrict__ act, uint32_t *next_act,
+                                                          uint32_t *next_inq, uint32_t *next_queue, SvW w,
+                                                          SvCounters *cnt, const uint32_t *big) {
+    const uint32_t nbig = *(volatile uint32_t *)&cnt->nbig;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t bi = 0; bi < nbig; bi++) {
+        const uint32_t u = big[bi] >> 1, j = big[bi] & 1;
+        const uint32_t a = act[(uint64_t)u * 2 + j];
+        const uint32_t s = j * 32 + lane;
+        const bool on = (a >> lane) & 1u;
+        const uint32_t du = on ? __ldcg(dist + (uint64_t)u * SV_SSSP_SLOTS + s) : SV_INF;
+        for (uint32_t p = ptr[u] + gw; p < ptr[u + 1]; p += warps)
+            sv_relax(u, col[p], j, s, on, du, w, dist, next_act, next_inq, next_queue, cnt);
+    }
+}
+
+__global__ void k_sv_sssp_clear_frontier(const uint32_t *__restrict__ queue, const SvCounters *qc, uint32_t *act,
+                                         uint32_t *inq) {
+    const uint32_t qlen = qc->qsize;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < qlen; i += gridDim.x * blockDim.x) {
+        const uint32_t v = queue[i];
+        act[(uint64_t)v * 2] = 0;
+        act[(uint64_t)v * 2 + 1] = 0;
+        atomicAnd(inq + (v >> 5), ~(1u << (v & 31)));
+    }
+}
+
+__global__ void k_sv_sssp_reset(uint32_t n, unsigned long long mask, uint32_t *dist) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        unsigned long long y = mask;
+        while (y) {
+            const int s = __ffsll((long long)y) - 1;
+            y &= y - 1;
+            dist[(uint64_t)v * SV_SSSP_SLOTS + s] = SV_INF;
+        }
+    }
+}
+
+__global__ void k_sv_dist_summary(const uint32_t *__restrict__ dist, uint32_t n, uint32_t s, unsigned long long *out) {
+    unsigned long long c = 0, mx = 0;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const uint32_t d = dist[(uint64_t)v * SV_SSSP_SLOTS + s];
+        if (d != SV_INF) {
+            c++;
+            mx = d > mx ? d : mx;
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        c += __shfl_down_sync(EG_FULL_MASK, c, o);
+        mx = max(mx, __shfl_down_sync(EG_FULL_MASK, mx, o));
+    }
+    if ((threadIdx.x & 31) == 0) {
+        atomicAdd(out, c);
+        atomicMax(out + 1, mx);
+    }
+}
+
+__global__ void k_sv_column(const uint32_t *__restrict__ m, uint32_t n, uint32_t width, uint32_t s, uint32_t *out) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        out[v] = m[(uint64_t)v * width + s];
+}
+
+// ------------------------------------------------------------------ PPR engine
+// Uses the batched PPR kernels (eg_ppr.cuh); lane q's seeds sit at
+// seeds[8q .. 8q + nseeds).
+__global__ void k_sv_ppr_column(const float *__restrict__ R, uint32_t n, uint32_t q, float *out, double *sum) {
+    double s = 0.0;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const float r = R[(uint64_t)v * EG_PPR_LANES + q];
+        if (out) out[v] = r;
+        s += (double)r;
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(EG_FULL_MASK, s, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(sum, s);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ server
+struct Pending {
+    uint64_t id;
+    eg_query q;
+};
+
+struct eg_server {
+    eg_graph *g;
+    eg_serve_opts opts;
+    uint64_t next_id = 1;
+    std::deque<Pending> queue;
+    std::vector<eg_query_result> done;
+    std::vector<std::vector<uint32_t>> kept;  // per result (keep_results): full result as u32 words
+    double t0;
+    int bfs_cap, sssp_cap, ppr_cap;
+    // BFS engine
+    eg_buf bfs_buf;
+    unsigned long long bfs_seen_mask = 0;  // slots in use
+    int32_t bfs_level[SV_BFS_SLOTS];
+    uint64_t bfs_id[SV_BFS_SLOTS];
+    double bfs_admit[SV_BFS_SLOTS], bfs_arrival[SV_BFS_SLOTS];
+    unsigned long long bfs_count = 0, bfs_fdeg = 0;
+    // SSSP engine
+    eg_buf sssp_buf;
+    unsigned long long sssp_mask = 0;
+    uint64_t sssp_id[SV_SSSP_SLOTS];
+    double sssp_admit[SV_SSSP_SLOTS], sssp_arrival[SV_SSSP_SLOTS];
+    int sssp_cur = 0;
+    int sssp_rounds[SV_SSSP_SLOTS];
+    // PPR engine
+    eg_buf ppr_buf;
+    uint32_t ppr_mask = 0;
+    uint64_t ppr_id[SV_PPR_LANES];
+    double ppr_admit[SV_PPR_LANES], ppr_arrival[SV_PPR_LANES];
+    eg_buf small;  // counters, admission lists, summaries (device)
+    uint64_t ticks = 0;
+};
+
+static uint32_t sv_blocks(eg_ctx *ctx, uint64_t threads) {
+    uint64_t b = (threads + 255) / 256;
+    const uint64_t cap = (uint64_t)ctx->sm_count * 8;
+    return (uint32_t)(b > cap ? cap : (b ? b : 1));
+}
+
+extern "C" void eg_serve_opts_default(eg_serve_opts *o) {
+    if (!o) return;
+    memset(o, 0, sizeof(*o));
+    o->hbm_budget = 64ull << 30;
+    o->max_bfs = SV_BFS_SLOTS;
+    o->max_sssp = SV_SSSP_SLOTS;
+    o->max_ppr = SV_PPR_LANES;
+    o->weights.rule = EG_W_HASH;
+    o->weights.seed = 6;
+    o->weights.lo = 1;
+    o->weights.hi = 255;
+    o->ppr_damping = 0.85f;
+    o->ppr_max_iters = 50;
+    o->keep_results = 0;
+}
+
+// Device bytes per slot of each engine (the admission cost of one query).
+static void sv_slot_bytes(uint32_t n, uint64_t *bfs, uint64_t *sssp, uint64_t *ppr) {
+    *bfs = (uint64_t)n * 4;        // level row
+    *sssp = (uint64_t)n * 4;       // dist column
+    *ppr = (uint64_t)n * 4 * 3;    // R, X, Y columns
+}
+
+extern "C" int eg_serve_open(eg_graph *g, const eg_serve_opts *opts, eg_server **out) {
+    if (!g || !out) return eg_fail(EG_EINVAL, "NULL argument");
+    if (!(g->built & EG_LAYOUT_CSR) || !(g->built & EG_LAYOUT_CSC))
+        return eg_fail(EG_ENOTBUILT, "the server needs the CSR and the CSC");
+    eg_serve_opts o;
+    if (opts) o = *opts;
+    else eg_serve_opts_default(&o);
+    eg_ctx *ctx = g->ctx;
+    const uint32_t n = g->n;
+    uint64_t sb, ss, sp;
+    sv_slot_bytes(n, &sb, &ss, &sp);
+    // shared per-engine state, then as many slots as the budget allows
+    const uint64_t shared_bfs = (uint64_t)n * 8 * 3 + (uint64_t)n * 8;
+    const uint64_t shared_sssp = (uint64_t)n * 8 * 2 + (uint64_t)n * 4 * 2 + (uint64_t)n * 4 * 3;
+    const uint64_t shared_ppr = 0;
+    const uint64_t base = shared_bfs + shared_sssp + shared_ppr;
+    if (o.hbm_budget && o.hbm_budget < base + sb + ss + sp)
+        return eg_fail(EG_ENOMEM, "HBM budget %llu below one slot of each engine (%llu)", (unsigned long long)o.hbm_budget,
+                       (unsigned long long)(base + sb + ss + sp));
+    const uint64_t avail = o.hbm_budget ? o.hbm_budget - base : ~0ull;
+    // split the budget evenly in bytes between the three engines
+    auto cap = [&](int want, int hard, uint64_t per) {
+        int c = want < 1 ? 1 : (want > hard ? hard : want);
+        uint64_t lim = avail / 3 / per;
+        if ((uint64_t)c > lim) c = (int)(lim < 1 ? 1 : lim);
+        return c;
+    };
+    eg_server *s = new eg_server();
+    s->g = g;
+    s->opts = o;
+    s->bfs_cap = cap(o.max_bfs, SV_BFS_SLOTS, sb);
+    s->sssp_cap = cap(o.max_sssp, SV_SSSP_SLOTS, ss);
+    s->ppr_cap = cap(o.max_ppr, SV_PPR_LANES, sp);
+    int rc = EG_OK;
+    // BFS: seen | front | next (u64) | queue+big (u32 x 2n) | levels (64 rows)
+    if (rc == EG_OK) rc = eg_buf_ensure(ctx, s->bfs_buf, (uint64_t)n * 8 * 3 + (uint64_t)n * 8 + (uint64_t)SV_BFS_SLOTS * n * 4);
+    // SSSP: dist [n][64] | act x2 [n][2] | inq x2 | queue x2 | big
+    if (rc == EG_OK)
+        rc = eg_buf_ensure(ctx, s->sssp_buf, (uint64_t)n * 4 * SV_SSSP_SLOTS + (uint64_t)n * 8 * 2 + (uint64_t)((n + 31) / 32) * 4 * 2 +
+                                                 (uint64_t)n * 4 * 3);
+    // PPR: R, X, Y [n][32] | parts
+    const uint64_t ptiles = g->m ? (g->m + EG_PPR_TILE - 1) / EG_PPR_TILE : 0;
+    if (rc == EG_OK)
+        rc = eg_buf_ensure(ctx, s->ppr_buf, (uint64_t)n * 4 * EG_PPR_LANES * 3 + ptiles * EG_PPR_LANES * 4 * 2 +
+                                                 ((ptiles + 63) & ~63ull) * 4 + (uint64_t)ctx->sm_count * 4 * 32 * 16 + 256);
+    if (rc == EG_OK) rc = eg_buf_ensure(ctx, s->small, 64 * 1024);
+    if (rc != EG_OK) {
+        eg_buf_free(ctx, s->bfs_buf);
+        eg_buf_free(ctx, s->sssp_buf);
+        eg_buf_free(ctx, s->ppr_buf);
+        eg_buf_free(ctx, s->small);
+        delete s;
+        return rc;
+    }
+    // initial state
+    unsigned char *bb = bp<unsigned char>(s->bfs_buf);
+    EG_CUDA(cudaMemsetAsync(bb, 0, (uint64_t)n * 8 * 3, ctx->stream));
+    EG_CUDA(cudaMemsetAsync(bb + (uint64_t)n * 8 * 4, 0, (uint64_t)SV_BFS_SLOTS * n * 4, ctx->stream));
+    unsigned char *sbuf = bp<unsigned char>(s->sssp_buf);
+    EG_CUDA(cudaMemsetAsync(sbuf, 0xff, (uint64_t)n * 4 * SV_SSSP_SLOTS, ctx->stream));  // reset below to SV_INF
+    k_sv_sssp_reset<<<sv_blocks(ctx, (uint64_t)n * SV_SSSP_SLOTS), 256, 0, ctx->stream>>>(n, ~0ull, (uint32_t *)sbuf);
+    ctx->launches++;
+    EG_CUDA(cudaMemsetAsync(sbuf + (uint64_t)n * 4 * SV_SSSP_SLOTS, 0,
+                            (uint64_t)n * 8 * 2 + (uint64_t)((n + 31) / 32) * 4 * 2, ctx->stream));
+    EG_CUDA(cudaMemsetAsync(s->small.p, 0, 64 * 1024, ctx->stream));
+    EG_CUDA(cudaMemsetAsync(s->ppr_buf.p, 0, (uint64_t)n * 4 * EG_PPR_LANES * 2, ctx->stream));
+    if (n >= 0x80000000u) return eg_fail(EG_EINVAL, "the server takes n < 2^31");
+    EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    s->t0 = now_s();
+    *out = s;
+    return EG_OK;
+}
+
+extern "C" int eg_serve_close(eg_server *s) {
+    if (!s) return EG_OK;
+    eg_ctx *ctx = s->g->ctx;
+    cudaStreamSynchronize(ctx->stream);
+    eg_buf_free(ctx, s->bfs_buf);
+    eg_buf_free(ctx, s->sssp_buf);
+    eg_buf_free(ctx, s->ppr_buf);
+    eg_buf_free(ctx, s->small);
+    delete s;
+    return EG_OK;
+}
+
+extern "C" int eg_serve_submit(eg_server *s, const eg_query *q, uint64_t *id_out) {
+    if (!s || !q) return eg_fail(EG_EINVAL, "NULL argument");
+    const uint32_t n = s->g->n;
+    if (q->kind == EG_Q_BFS || q->kind == EG_Q_SSSP) {
+        if (q->source >= n) return eg_fail(EG_EINVAL, "source %u >= n", q->source);
+    } else if (q->kind == EG_Q_PPR) {
+        if (q->nseeds < 1 || q->nseeds > 8) return eg_fail(EG_EINVAL, "a PPR query has 1..8 seeds");
+        for (uint32_t i = 0; i < q->nseeds; i++)
+            if (q->seeds[i] >= n) return eg_fail(EG_EINVAL, "seed %u >= n", q->seeds[i]);
+    } else {
+        return eg_fail(EG_EINVAL, "unknown query kind %d", q->kind);
+    }
+    Pending p;
+    p.id = s->next_id++;
+    p.q = *q;
+    if (p.q.arrival_s <= 0.0) p.q.arrival_s = now_s() - s->t0;
+    s->queue.push_back(p);
+    if (id_out) *id_out = p.id;
+    return EG_OK;
+}
+
+static void sv_finish(eg_server *s, uint64_t id, int kind, double arrival, double admit, uint32_t reached,
+                      uint32_t depth, int iters, double value) {
+    eg_query_result r;
+    memset(&r, 0, sizeof(r));
+    r.id = id;
+    r.kind = kind;
+    r.arrival_s = arrival;
+    r.admit_s = admit;
+    r.done_s = now_s() - s->t0;
+    r.reached = reached;
+    r.depth = depth;
+    r.iterations = iters;
+    r.value = value;
+    s->done.push_back(r);
+}
+
+// One scheduler tick.
+extern "C" int eg_serve_step(eg_server *s, int *active_out) {
+    if (!s) return eg_fail(EG_EINVAL, "NULL server");
+    eg_graph *g = s->g;
+    eg_ctx *ctx = g->ctx;
+    EG_CUDA(cudaSetDevice(ctx->device));
+    const uint32_t n = g->n;
+    const double m = (double)g->m;
+    const uint32_t nw = (n + 31) / 32;
+    unsigned char *small = bp<unsigned char>(s->small);
+    SvCounters *bcnt = (SvCounters *)small, *scnt = (SvCounters *)(small + 256);
+    uint32_t *adm_roots = (uint32_t *)(small + 1024), *adm_slots = (uint32_t *)(small + 2048);
+    int32_t *d_slot_level = (int32_t *)(small + 3072);
+    PprQ *d_ppr = (PprQ *)(small + 4096);                 // 32 x PprQ
+    uint32_t *d_pseeds = (uint32_t *)(small + 8192);      // 8 per lane
+    uint32_t *d_sbeg = (uint32_t *)(small + 9216), *d_send = (uint32_t *)(small + 9344);
+    unsigned long long *d_sum = (unsigned long long *)(small + 12544);
+    unsigned char *hs = (unsigned char *)ctx->h_pinned;
+    s->ticks++;
+
+    // ---------------- admission (FIFO per kind into free slots)
+    std::vector<uint32_t> broots, bslots, sroots, sslots;
+    uint32_t new_ppr = 0;
+    PprQ ppr_new[SV_PPR_LANES];
+    uint32_t ppr_seeds_new[SV_PPR_LANES][8];
+    for (auto it = s->queue.begin(); it != s->queue.end();) {
+        const eg_query &q = it->q;
+        bool took = false;
+        const double tnow = now_s() - s->t0;
+        if (q.kind == EG_Q_BFS) {
+            for (int sl = 0; sl < s->bfs_cap; sl++)
+                if (!((s->bfs_seen_mask >> sl) & 1ull) && std::find(bslots.begin(), bslots.end(), (uint32_t)sl) == bslots.end()) {
+                    broots.push_back(q.source);
+                    bslots.push_back((uint32_t)sl);
+                    s->bfs_id[sl] = it->id;
+                    s->bfs_arrival[sl] = q.arrival_s;
+                    s->bfs_admit[sl] = tnow;
+                    took = true;
+                    break;
+                }
+        } else if (q.kind == EG_Q_SSSP) {
+            for (int sl = 0; sl < s->sssp_cap; sl++)
+                if (!((s->sssp_mask >> sl) & 1ull) && std::find(sslots.begin(), sslots.end(), (uint32_t)sl) == sslots.end()) {
+                    sroots.push_back(q.source);
+                    sslots.push_back((uint32_t)sl);
+                    s->sssp_id[sl] = it->id;
+                    s->sssp_arrival[sl] = q.arrival_s;
+                    s->sssp_admit[sl] = tnow;
+                    s->sssp_rounds[sl] = 0;
+                    took = true;
+                    break;
+                }
+        } else {
+            for (int sl = 0; sl < s->ppr_cap; sl++)
+                if (!((s->ppr_mask >> sl) & 1u) && !((new_ppr >> sl) & 1u)) {
+                    PprQ &p = ppr_new[sl];
+                    memset(&p, 0, sizeof(p));
+                    p.tol = q.tol > 0 ? q.tol : 1e-6f;
+                    p.max_iters = s->opts.ppr_max_iters;
+                    p.active = 1;
+                    p.nseeds = (int)q.nseeds;
+                    for (uint32_t k = 0; k < q.nseeds; k++) ppr_seeds_new[sl][k] = q.seeds[k];
+                    new_ppr |= 1u << sl;
+                    s->ppr_id[sl] = it->id;
+                    s->ppr_arrival[sl] = q.arrival_s;
+                    s->ppr_admit[sl] = tnow;
+                    took = true;
+                    break;
+                }
+        }
+        if (took) it = s->queue.erase(it);
+        else ++it;
+    }
+    unsigned long long *seen = bp<unsigned long long>(s->bfs_buf);
+    unsigned long long *front = seen + n, *next = seen + 2ull * n;
+    uint32_t *bq = reinterpret_cast<uint32_t *>(seen + 3ull * n), *bbig = bq + n;
+    int32_t *levels = reinterpret_cast<int32_t *>(bbig + n);
+    const uint32_t *deg = bp<uint32_t>(g->out_deg);
+    // ---------------- BFS: admit, then one level for all live slots
+    if (!broots.empty()) {
+        EG_CUDA(cudaMemcpyAsync(adm_roots, broots.data(), broots.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+        EG_CUDA(cudaMemcpyAsync(adm_slots, bslots.data(), bslots.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+        k_sv_bfs_admit<<<1, 64, 0, ctx->stream>>>(adm_roots, adm_slots, (int)broots.size(), n, seen, front, levels);
+        EG_LAUNCHED(ctx);
+        for (size_t i = 0; i < bslots.size(); i++) {
+            s->bfs_seen_mask |= 1ull << bslots[i];
+            s->bfs_level[bslots[i]] = 1;
+            s->bfs_fdeg += 1;  // keeps the first step of new roots in push mode unless the frontier is large
+        }
+    }
+    const unsigned long long live = s->bfs_seen_mask;
+    unsigned long long bfs_done = 0;
+    if (live) {
+        EG_CUDA(cudaMemcpyAsync(d_slot_level, s->bfs_level, sizeof(s->bfs_level), cudaMemcpyHostToDevice, ctx->stream));
+        EG_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(SvCounters), ctx->stream));
+        const bool pull = (double)s->bfs_count + (double)s->bfs_fdeg > m / 20.0;
+        if (pull) {
+            k_sv_bfs_pull<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), bp<uint32_t>(g->csc.col), n,
+                                                                     live, seen, front, next);
+            EG_LAUNCHED(ctx);
+        } else {
+            k_sv_front_queue<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(front, n, bq, bcnt);
+            EG_LAUNCHED(ctx);
+            k_sv_bfs_push<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr),
+                                                                               bp<uint32_t>(g->csr.col), bq, bcnt,
+                                                                               seen, front, next, bbig, bcnt);
+            EG_LAUNCHED(ctx);
+            k_sv_bfs_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, ctx->stream>>>(
+                bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), bbig, seen, front, next, bcnt);
+            EG_LAUNCHED(ctx);
+            EG_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(SvCounters), ctx->stream));
+        }
+        k_sv_bfs_fold<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(n, seen, front, next, levels, d_slot_level, deg, bcnt);
+        EG_LAUNCHED(ctx);
+        SvCounters *hc = (SvCounters *)hs;
+        EG_CUDA(cudaMemcpyAsync(hc, bcnt, sizeof(SvCounters), cudaMemcpyDeviceToHost, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        s->bfs_count = hc->count;
+        s->bfs_fdeg = hc->deg;
+        for (int sl = 0; sl < SV_BFS_SLOTS; sl++)
+            if ((live >> sl) & 1ull) s->bfs_level[sl] += 1;
+        bfs_done = live & ~hc->newmask;  // no discovery this level: finished
+    }
+    // ---------------- SSSP: admit, then one round for all live slots
+    uint32_t *dist = bp<uint32_t>(s->sssp_buf);
+    uint32_t *act0 = dist + (uint64_t)n * SV_SSSP_SLOTS, *act1 = act0 + 2ull * n;
+    uint32_t *inq0 = act1 + 2ull * n, *inq1 = inq0 + nw;
+    uint32_t *sq0 = inq1 + nw, *sq1 = sq0 + n, *sbig = sq1 + n;
+    uint32_t *act[2] = {act0, act1}, *inq[2] = {inq0, inq1}, *sq[2] = {sq0, sq1};
+    SvCounters *scur = scnt, *snext = (SvCounters *)(small + 512);
+    // scnt holds the current queue size (qsize); snext collects the next one
+    if (!sroots.empty()) {
+        EG_CUDA(cudaMemcpyAsync(adm_roots + 128, sroots.data(), sroots.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+        EG_CUDA(cudaMemcpyAsync(adm_slots + 128, sslots.data(), sslots.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+        const int c = s->sssp_cur;
+        k_sv_sssp_admit<<<1, 64, 0, ctx->stream>>>(adm_roots + 128, adm_slots + 128, (int)sroots.size(), dist, act[c],
+                                                   inq[c], sq[c], scur);
+        EG_LAUNCHED(ctx);
+        for (size_t i = 0; i < sslots.size(); i++) s->sssp_mask |= 1ull << sslots[i];
+    }
+    unsigned long long sssp_done = 0;
+    if (s->sssp_mask) {
+        const int c = s->sssp_cur, nx = c ^ 1;
+        SvW w;
+        w.rule = s->opts.weights.rule;
+        w.seed = s->opts.weights.seed;
+        w.lo = s->opts.weights.lo;
+        w.span = (uint64_t)s->opts.weights.hi - s->opts.weights.lo + 1;
+        EG_CUDA(cudaMemsetAsync(snext, 0, sizeof(SvCounters), ctx->stream));
+        k_sv_sssp_push<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
+            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), sq[c], scur, dist, act[c], act[nx], inq[nx], sq[nx], w,
+            snext, sbig);
+        EG_LAUNCHED(ctx);
+        k_sv_sssp_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, ctx->stream>>>(
+            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), dist, act[c], act[nx], inq[nx], sq[nx], w, snext, sbig);
+        EG_LAUNCHED(ctx);
+        k_sv_sssp_clear_frontier<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(sq[c], scur, act[c], inq[c]);
+        EG_LAUNCHED(ctx);
+        EG_CUDA(cudaMemcpyAsync(scur, snext, sizeof(SvCounters), cudaMemcpyDeviceToDevice, ctx->stream));
+        SvCounters *hc = (SvCounters *)(hs + 256);
+        EG_CUDA(cudaMemcpyAsync(hc, snext, sizeof(SvCounters), cudaMemcpyDeviceToHost, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        const unsigned long long still = hc->actmask[0] | (hc->actmask[1] << 32);
+        for (int sl = 0; sl < SV_SSSP_SLOTS; sl++)
+            if ((s->sssp_mask >> sl) & 1ull) s->sssp_rounds[sl] += 1;
+        sssp_done = s->sssp_mask & ~still;
+        s->sssp_cur = nx;
+    }
+    // ---------------- PPR: admit lanes, then one iteration for all live lanes
+    float *R = bp<float>(s->ppr_buf), *X = R + (uint64_t)n * EG_PPR_LANES, *Y = X + (uint64_t)n * EG_PPR_LANES;
+    const uint32_t pm = (uint32_t)g->m;
+    const uint32_t ptiles = pm ? eg_div_up(pm, EG_PPR_TILE) : 0;
+    float *phv = Y + (uint64_t)n * EG_PPR_LANES, *ptv = phv + (uint64_t)ptiles * EG_PPR_LANES;
+    uint32_t *phr = reinterpret_cast<uint32_t *>(ptv + (uint64_t)ptiles * EG_PPR_LANES);
+    double2 *ppart = reinterpret_cast<double2 *>(phr + ((ptiles + 63) & ~63u));
+    PprQ *hp = (PprQ *)(hs + 1024);
+    if (new_ppr) {
+        EG_CUDA(cudaMemcpyAsync(hp, d_ppr, sizeof(PprQ) * EG_PPR_LANES, cudaMemcpyDeviceToHost, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        uint32_t *hseeds = (uint32_t *)(hs + 4096), *hbeg = hseeds + 256, *hend = hbeg + 32;
+        EG_CUDA(cudaMemcpyAsync(hseeds, d_pseeds, 256 * 4, cudaMemcpyDeviceToHost, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        for (int q = 0; q < EG_PPR_LANES; q++) {
+            hbeg[q] = 8u * q;
+            if ((new_ppr >> q) & 1u) {
+                hp[q] = ppr_new[q];
+                for (int k = 0; k < hp[q].nseeds; k++) hseeds[8 * q + k] = ppr_seeds_new[q][k];
+            }
+            hend[q] = 8u * q + (hp[q].active ? (uint32_t)hp[q].nseeds : 0u);
+        }
+        EG_CUDA(cudaMemcpyAsync(d_ppr, hp, sizeof(PprQ) * EG_PPR_LANES, cudaMemcpyHostToDevice, ctx->stream));
+        EG_CUDA(cudaMemcpyAsync(d_pseeds, hseeds, 256 * 4, cudaMemcpyHostToDevice, ctx->stream));
+        EG_CUDA(cudaMemcpyAsync(d_sbeg, hbeg, 32 * 4, cudaMemcpyHostToDevice, ctx->stream));
+        EG_CUDA(cudaMemcpyAsync(d_send, hend, 32 * 4, cudaMemcpyHostToDevice, ctx->stream));
+        k_ppr_init<<<sv_blocks(ctx, (uint64_t)n * 32), 256, 0, ctx->stream>>>(n, new_ppr, R, X);
+        EG_LAUNCHED(ctx);
+        k_ppr_init_seeds<<<1, 32, 0, ctx->stream>>>(d_pseeds, d_sbeg, d_send, new_ppr, d_ppr, deg, R, X);
+        EG_LAUNCHED(ctx);
+        k_ppr_init_dangling<<<1, 32, 0, ctx->stream>>>(d_pseeds, d_sbeg, d_send, new_ppr, deg, R, d_ppr);
+        EG_LAUNCHED(ctx);
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));  // the host staging above is reused below
+        s->ppr_mask |= new_ppr;
+    }
+    uint32_t ppr_done = 0;
+    if (s->ppr_mask) {
+        const uint32_t fb = (uint32_t)ctx->sm_count * 4;
+        const uint32_t rb = ptiles ? eg_div_up((uint64_t)ptiles * 32, 256) : 0;
+        if (rb) {
+            k_ppr_rows<<<rb, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.rid), bp<uint32_t>(g->csc.col), pm, ptiles, X, Y,
+                                                    phv, ptv, phr);
+            EG_LAUNCHED(ctx);
+            k_ppr_fixup<<<rb, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), ptiles, phr, phv, ptv, Y);
+            EG_LAUNCHED(ctx);
+        }
+        k_ppr_empty<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), n, Y);
+        EG_LAUNCHED(ctx);
+        k_ppr_seeds<<<1, 32, 0, ctx->stream>>>(d_pseeds, d_sbeg, d_send, 32, d_ppr, s->opts.ppr_damping, Y);
+        EG_LAUNCHED(ctx);
+        k_ppr_finish<<<fb, 256, 0, ctx->stream>>>(Y, deg, n, s->opts.ppr_damping, d_ppr, R, X, ppart);
+        EG_LAUNCHED(ctx);
+        k_ppr_reduce<<<1, 32, 0, ctx->stream>>>(ppart, fb, d_ppr, 1);
+        EG_LAUNCHED(ctx);
+        EG_CUDA(cudaMemcpyAsync(hp, d_ppr, sizeof(PprQ) * EG_PPR_LANES, cudaMemcpyDeviceToHost, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        for (int q = 0; q < EG_PPR_LANES; q++)
+            if (hp[q].active && hp[q].done) ppr_done |= 1u << q;
+        ppr_done &= s->ppr_mask;
+    }
+    // ---------------- retire
+    if (bfs_done) {
+        for (int sl = 0; sl < SV_BFS_SLOTS; sl++) {
+            if (!((bfs_done >> sl) & 1ull)) continue;
+            int32_t *row = levels + (uint64_t)sl * n;
+            EG_CUDA(cudaMemsetAsync(d_sum, 0, 16, ctx->stream));
+            k_sv_level_summary<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(row, n, d_sum);
+            EG_LAUNCHED(ctx);
+            unsigned long long *hsum = (unsigned long long *)(hs + 9000 + 64);
+            EG_CUDA(cudaMemcpyAsync(hsum, d_sum, 16, cudaMemcpyDeviceToHost, ctx->stream));
+            std::vector<uint32_t> keep;
+            if (s->opts.keep_results) {
+                keep.resize(n);
+                EG_CUDA(cudaMemcpyAsync(keep.data(), row, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+            }
+            EG_CUDA(cudaStreamSynchronize(ctx->stream));
+            sv_finish(s, s->bfs_id[sl], EG_Q_BFS, s->bfs_arrival[sl], s->bfs_admit[sl], (uint32_t)hsum[0],
+                      (uint32_t)hsum[1], s->bfs_level[sl] - 1, 0.0);
+            if (s->opts.keep_results) s->kept.push_back(std::move(keep));
+            EG_CUDA(cudaMemsetAsync(row, 0, (uint64_t)n * 4, ctx->stream));
+        }
+        k_sv_bfs_clear<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(n, ~bfs_done, seen, front);
+        EG_LAUNCHED(ctx);
+        s->bfs_seen_mask &= ~bfs_done;
+    }
+    if (sssp_done) {
+        for (int sl = 0; sl < SV_SSSP_SLOTS; sl++) {
+            if (!((sssp_done >> sl) & 1ull)) continue;
+            EG_CUDA(cudaMemsetAsync(d_sum, 0, 16, ctx->stream));
+            k_sv_dist_summary<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(dist, n, (uint32_t)sl, d_sum);
+            EG_LAUNCHED(ctx);
+            unsigned long long *hsum = (unsigned long long *)(hs + 9000 + 64);
+            EG_CUDA(cudaMemcpyAsync(hsum, d_sum, 16, cudaMemcpyDeviceToHost, ctx->stream));
+            std::vector<uint32_t> keep;
+            if (s->opts.keep_results) {
+                keep.resize(n);
+                uint32_t *col = bp<uint32_t>(g->spmv_y);
+                EG_TRY(eg_buf_ensure(ctx, g->spmv_y, (uint64_t)n * 8));
+                col = bp<uint32_t>(g->spmv_y);
+                k_sv_column<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(dist, n, SV_SSSP_SLOTS, (uint32_t)sl, col);
+                EG_LAUNCHED(ctx);
+                EG_CUDA(cudaMemcpyAsync(keep.data(), col, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+            }
+            EG_CUDA(cudaStreamSynchronize(ctx->stream));
+            sv_finish(s, s->sssp_id[sl], EG_Q_SSSP, s->sssp_arrival[sl], s->sssp_admit[sl], (uint32_t)hsum[0],
+                      (uint32_t)hsum[1], s->sssp_rounds[sl], 0.0);
+            if (s->opts.keep_results) s->kept.push_back(std::move(keep));
+        }
+        k_sv_sssp_reset<<<sv_blocks(ctx, (uint64_t)n * SV_SSSP_SLOTS), 256, 0, ctx->stream>>>(n, sssp_done, dist);
+        EG_LAUNCHED(ctx);
+        s->sssp_mask &= ~sssp_done;
+    }
+    if (ppr_done) {
+        for (int q = 0; q < EG_PPR_LANES; q++) {
+            if (!((ppr_done >> q) & 1u)) continue;
+            double *dsum = reinterpret_cast<double *>(d_sum);
+            EG_CUDA(cudaMemsetAsync(dsum, 0, 16, ctx->stream));
+            std::vector<uint32_t> keep;
+            float *col = nullptr;
+            if (s->opts.keep_results) {
+                keep.resize(n);
+                EG_TRY(eg_buf_ensure(ctx, g->spmv_y, (uint64_t)n * 8));
+                col = bp<float>(g->spmv_y);
+            }
+            k_sv_ppr_column<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(R, n, (uint32_t)q, col, dsum);
+            EG_LAUNCHED(ctx);
+            double *hsum = (double *)(hs + 9000 + 64);
+            EG_CUDA(cudaMemcpyAsync(hsum, dsum, 8, cudaMemcpyDeviceToHost, ctx->stream));
+            if (col) EG_CUDA(cudaMemcpyAsync(keep.data(), col, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
+            EG_CUDA(cudaStreamSynchronize(ctx->stream));
+            sv_finish(s, s->ppr_id[q], EG_Q_PPR, s->ppr_arrival[q], s->ppr_admit[q], 0u, 0u, hp[q].iters, *hsum);
+            if (s->opts.keep_results) s->kept.push_back(std::move(keep));
+            hp[q].active = 0;
+            hp[q].done = 0;
+        }
+        EG_CUDA(cudaMemcpyAsync(d_ppr, hp, sizeof(PprQ) * EG_PPR_LANES, cudaMemcpyHostToDevice, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        s->ppr_mask &= ~ppr_done;
+    }
+    if (active_out)
+        *active_out = __builtin_popcountll(s->bfs_seen_mask) + __builtin_popcountll(s->sssp_mask) +
+                      __builtin_popcount(s->ppr_mask) + (int)s->queue.size();
+    return EG_OK;
+}
+
+extern "C" int eg_serve_poll(eg_server *s, eg_query_result *out, int max, int *count) {
+    if (!s || !count) return eg_fail(EG_EINVAL, "NULL argument");
+    int c = (int)s->done.size();
+    if (c > max) c = max;
+    for (int i = 0; i < c; i++) out[i] = s->done[i];
+    s->done.erase(s->done.begin(), s->done.begin() + c);
+    *count = c;
+    return EG_OK;
+}
+
+extern "C" int eg_serve_take_result(eg_server *s, uint32_t *out, uint32_t n) {
+    if (!s || !out) return eg_fail(EG_EINVAL, "NULL argument");
+    if (s->kept.empty()) return eg_fail(EG_EINVAL, "no kept result (keep_results off or none left)");
+    if (n != s->g->n) return eg_fail(EG_EINVAL, "buffer holds %u, the graph has %u vertices", n, s->g->n);
+    memcpy(out, s->kept.front().data(), (size_t)n * 4);
+    s->kept.erase(s->kept.begin());
+    return EG_OK;
+}
+
+extern "C" int eg_serve_info(eg_server *s, int *bfs_slots, int *sssp_slots, int *ppr_slots, double *clock_s) {
+    if (!s) return eg_fail(EG_EINVAL, "NULL server");
+    if (bfs_slots) *bfs_slots = s->bfs_cap;
+    if (sssp_slots) *sssp_slots = s->sssp_cap;
+    if (ppr_slots) *ppr_slots = s->ppr_cap;
+    if (clock_s) *clock_s = now_s() - s->t0;
+    return EG_OK;
+}

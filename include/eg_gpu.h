@@ -271,6 +271,58 @@ typedef struct {
 int eg_ppr_multi(eg_graph *g, const uint32_t *seeds, const uint32_t *seed_offsets, int nq, const eg_ppr_opts *opts,
                  float *ranks_out, eg_ppr_stats *stats);
 
+/* ---- query server (continuous batching) ----------------------------------
+ * No counterpart in the reference (one algorithm per process).  A server
+ * keeps the graph and every admitted query's state in HBM.  eg_serve_step is
+ * one scheduler tick: queued queries are admitted into free slots (64 BFS,
+ * 64 SSSP, 32 PPR at most; fewer when hbm_budget cannot hold their state),
+ * every engine with live slots advances one step (one BFS level, one
+ * Bellman-Ford round, one PPR iteration), finished queries are retired.
+ * Queries join and leave between ticks; a slot's arithmetic never reads
+ * another slot's values, so results do not depend on the mix.  Results stay
+ * on the device; eg_serve_poll returns a summary per finished query, and
+ * with keep_results the full result (levels, distances, or fp32 ranks as
+ * u32 words) is kept in host memory in completion order. */
+#define EG_Q_BFS 1
+#define EG_Q_SSSP 2
+#define EG_Q_PPR 3
+typedef struct eg_server eg_server;
+typedef struct {
+    int kind;
+    uint32_t source;   /* BFS / SSSP */
+    uint32_t nseeds;   /* PPR: 1..8 */
+    uint32_t seeds[8];
+    float tol;         /* PPR tolerance (<= 0: 1e-6) */
+    double arrival_s;  /* arrival time on the server clock (<= 0: now) */
+} eg_query;
+typedef struct {
+    uint64_t id;
+    int kind;
+    double arrival_s, admit_s, done_s; /* server clock, seconds */
+    uint32_t reached;                  /* BFS/SSSP: vertices reached */
+    uint32_t depth;                    /* BFS: deepest level; SSSP: largest distance */
+    int iterations;                    /* levels / rounds / PPR iterations */
+    double value;                      /* PPR: sum of the rank vector */
+} eg_query_result;
+typedef struct {
+    uint64_t hbm_budget; /* bytes of per-query state the server may hold */
+    int max_bfs, max_sssp, max_ppr;
+    eg_weights weights;  /* SSSP weight rule */
+    float ppr_damping;
+    int ppr_max_iters;
+    int keep_results;
+} eg_serve_opts;
+void eg_serve_opts_default(eg_serve_opts *o);
+int eg_serve_open(eg_graph *g, const eg_serve_opts *opts, eg_server **out);
+int eg_serve_submit(eg_server *s, const eg_query *q, uint64_t *id_out);
+/* active_out: queries admitted or queued after the tick */
+int eg_serve_step(eg_server *s, int *active_out);
+int eg_serve_poll(eg_server *s, eg_query_result *out, int max, int *count);
+/* next kept full result (n u32 words), in completion order */
+int eg_serve_take_result(eg_server *s, uint32_t *out, uint32_t n);
+int eg_serve_info(eg_server *s, int *bfs_slots, int *sssp_slots, int *ppr_slots, double *clock_s);
+int eg_serve_close(eg_server *s);
+
 /* ---- allocation-free SpMV ------------------------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device
  * memory (a host callback, a plug-in inside a process whose allocator it does

@@ -355,3 +355,65 @@ def test_ppr_batch_vs_fp64_and_alone(case):
         Ra, sta = g.ppr([seed_lists[q]], tolerance=[tols[q]], max_iters=50)
         np.testing.assert_array_equal(Ra[0].view(np.uint32), R[q].view(np.uint32))
         assert sta.iterations[0] == st.iterations[q]
+
+
+# ------------------------------------------------------------------ query server
+@pytest.mark.parametrize("budget_slots", [64, 3])
+def test_server_results_equal_standalone(ctx, budget_slots):
+    """Mixed BFS/SSSP/PPR queries arriving over several ticks: every result
+    equals the same query run alone by the plain kernels."""
+    import everythinggraph_gb300 as eg
+    n, pairs, rec = load("rmat12")
+    g = ctx.from_pairs(n, pairs, undirected=True).build(eg.CSR | eg.CSC)
+    w = eg.weights("hash", seed=6, lo=1, hi=255)
+    per_slot = n * 4 * 3
+    budget = 0 if budget_slots == 64 else (n * 8 * 4 + n * 8 * 2 + (n // 32) * 8 + n * 12 + n * 16 + 3 * budget_slots * per_slot)
+    srv = eg.Server(g, hbm_budget=budget, weights_=w, keep_results=True)
+    info = srv.info()
+    if budget_slots != 64:
+        assert info["bfs_slots"] < 64 and info["ppr_slots"] < 32
+    rng = np.random.default_rng(11)
+    nz = np.nonzero(np.diff(g.adj(eg.CSR)[0].astype(np.int64)) > 0)[0]
+    queries = {}
+    results = {}
+    for wave in range(6):
+        for _ in range(int(rng.integers(3, 9))):
+            r = float(rng.random())
+            if r < 0.6:
+                src = int(rng.choice(nz))
+                queries[srv.submit("bfs", source=src)] = ("bfs", src)
+            elif r < 0.85:
+                src = int(rng.choice(nz))
+                queries[srv.submit("sssp", source=src)] = ("sssp", src)
+            else:
+                seeds = [int(x) for x in rng.choice(nz, size=int(rng.integers(1, 9)))]
+                queries[srv.submit("ppr", seeds=seeds, tol=1e-6)] = ("ppr", seeds)
+        for _ in range(int(rng.integers(1, 4))):
+            srv.step()
+            for res in srv.poll():
+                results[res.id] = (res, srv.take_result())
+    for _ in range(500):
+        if srv.step() == 0:
+            break
+        for res in srv.poll():
+            results[res.id] = (res, srv.take_result())
+    for res in srv.poll():
+        results[res.id] = (res, srv.take_result())
+    assert set(results) == set(queries)
+    for qid, (kind, arg) in queries.items():
+        res, full = results[qid]
+        if kind == "bfs":
+            lv, st = g.bfs(arg)
+            np.testing.assert_array_equal(full.view(np.int32), lv)
+            assert res.reached == st.reached
+        elif kind == "sssp":
+            d, st = g.sssp(arg, w)
+            np.testing.assert_array_equal(full, d)
+            assert res.reached == st.reached
+        else:
+            R, st = g.ppr([arg], tolerance=1e-6)
+            np.testing.assert_array_equal(full, R[0].view(np.uint32))
+            assert res.iterations == st.iterations[0]
+        assert res.arrival_s <= res.admit_s <= res.done_s
+    srv.close()
+    g.free()
