@@ -28,6 +28,11 @@ sys.path.insert(0, ROOT)
 WORKLOAD = {"workload": "bfs64+wcc rmat24 undirected", "scale": 24, "edgefactor": 16, "seed": 2, "roots": 64,
             "root_seed": 3, "undirected": True}
 METRIC, UNIT = "GTEPS", "GTEPS"
+# DRAM bytes (read + write) of one row-kernel launch per CSC entry, from an
+# ncu capture of PageRank on directed RMAT-22 (the kernel's traffic grows with
+# the entries); the summary and its command are in
+# profiles/k_coo4_rows_pagerank_rmat22.md.
+PR_ROWS_DRAM_BYTES_PER_ENTRY = 593.69e6 / 67108864
 
 
 def peaks():
@@ -166,13 +171,31 @@ def run_ours(args):
     # ---- per-kernel reports on the same graph size
     kernels = {}
     if not args.no_extras:
-        kernels = kernel_reports(ctx, eg, scale, args)
+        try:
+            kernels["msbfs_64_roots"] = msbfs_report(g, roots)
+        except Exception as ex:  # reported, not fatal for the headline
+            kernels["msbfs_64_roots"] = {"error": str(ex)}
+        try:
+            kernels["serve"] = serve_report(ctx, eg, scale, args.rate, args.queries, g=g)
+        except Exception as ex:
+            kernels["serve"] = {"error": str(ex)}
+        kernels.update(kernel_reports(ctx, eg, scale, args))
+        for name, fn in (("spmv_er25", lambda: spmv_report(ctx, eg, 25 if scale >= 24 else scale, 32)),
+                         ("sssp_rmat23_256", lambda: sssp_report(ctx, eg, 23 if scale >= 24 else scale - 1))):
+            try:
+                kernels[name] = fn()
+            except Exception as ex:
+                kernels[name] = {"error": str(ex)}
     hbm, src = peaks()
     dom = kernels.get("pagerank_pull_rmat%d" % scale)
     roof = None
     if dom:
-        roof = {"bound": "hbm", "achieved": dom["gbps"], "peak": hbm, "unit": "GB/s",
-                "frac": dom["gbps"] / hbm, "traffic": None, "kernel": "k_mp_rows<PrOp>", "peak_source": src}
+        roof = {"bound": "hbm", "achieved": dom["row_kernel_gbps"], "peak": hbm, "unit": "GB/s",
+                "frac": dom["row_kernel_gbps"] / hbm,
+                "traffic": PR_ROWS_DRAM_BYTES_PER_ENTRY * dom["m"] if PR_ROWS_DRAM_BYTES_PER_ENTRY else None,
+                "kernel": "k_coov_rows<PrOp<0>, %d, %d> (PageRank pull, RMAT-%d directed)"
+                          % (dom["schedule"]["tile_entries"], dom["schedule"]["entries_per_lane"], scale),
+                "algorithmic_bytes": dom["bytes_per_iter"], "peak_source": src}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
@@ -202,26 +225,113 @@ def kernel_reports(ctx, eg, scale, args):
     n = 1 << scale
     m = 16 * n
     g = ctx.rmat(scale, m, 1).build(eg.CSR | eg.CSC)
+    cands, chosen = g.tune()  # row-kernel schedule for this graph
     g.pagerank(iterations=3, copy_out=False)
     torch.cuda.synchronize()
     _, st = g.pagerank(iterations=10, copy_out=False)
+    _, stg = g.pagerank(iterations=10, copy_out=False, use_graph=True)
+    _, stg = g.pagerank(iterations=10, copy_out=False, use_graph=True)
     it_ms = st.ms / 10
     bytes_it = 8 * m + 16 * n
-    rep["pagerank_pull_rmat%d" % scale] = {"ms_per_iter": it_ms, "gbps": bytes_it / (it_ms / 1e3) / 1e9,
-                                           "gteps": m / (it_ms / 1e3) / 1e9, "bytes_per_iter": bytes_it}
+    rep["pagerank_pull_rmat%d" % scale] = {
+        "ms_per_iter": it_ms, "gbps": bytes_it / (it_ms / 1e3) / 1e9, "gteps": m / (it_ms / 1e3) / 1e9,
+        "row_kernel_ms": st.row_kernel_ms, "row_kernel_gbps": bytes_it / (st.row_kernel_ms / 1e3) / 1e9,
+        "ms_per_iter_graph_replay": stg.ms / 10, "bytes_per_iter": bytes_it,
+        "bytes_rule": "8 per CSC entry (row id + column) + 16 per vertex (contribution, degree, rank, next contribution)",
+        "build_ms": g.info().build_ms, "m": m,
+        "schedule": {"tile_entries": cands[chosen][0], "entries_per_lane": cands[chosen][1],
+                     "candidates_ms": [[t, u, ms] for t, u, ms in cands]}}
     g.free()
     return rep
 
 
-def serve_report(ctx, eg, scale, rate, nq, seed=7, plain_sample=40):
+def spmv_report(ctx, eg, log_n=25, degree=32):
+    """SpMV over an Erdos-Renyi graph (2^25 vertices, 32 out-edges each, seed 4):
+    fp32 values U[0,1) hashed from the endpoints, x U[0,1) (seed 11); fp32,
+    fp32 two-sum and fp64, with max-relative and L1 error against fp64; the
+    64x64 grid layout built on the device beside it."""
+    import oracle
+    n = 1 << log_n
+    m = degree * n
+    g = ctx.er(n, m, 4).build(eg.CSR | eg.CSC)
+    x = oracle.uniform_f32(n, 11)
+    y64, _ = g.spmv(x, "f64", value_seed=9)
+    out = {"workload": "ER n=2^%d m=%d" % (log_n, m), "build_ms": g.info().build_ms}
+    nz = y64 != 0
+    for kind in ("f32", "f32_comp", "f64"):
+        g.spmv(x, kind, value_seed=9, copy_out=False)
+        y, ms = g.spmv(x, kind, value_seed=9)
+        bytes_ = 12 * m + (16 if kind == "f64" else 12) * n
+        rec = {"ms": ms, "gbps": bytes_ / (ms / 1e3) / 1e9, "gflops": 2 * m / (ms / 1e3) / 1e9}
+        if kind != "f64":
+            d = np.abs(y.astype(np.float64) - y64)
+            rec["max_rel_err"] = float((d[nz] / np.abs(y64[nz])).max())
+            rec["l1_rel_err"] = float(d.sum() / np.abs(y64).sum())
+        out[kind] = rec
+    # PageRank over the same graph, 10 iterations
+    _, st = g.pagerank(iterations=10, copy_out=False)
+    out["pagerank_ms_per_iter"] = st.ms / 10
+    g.free()
+    gg = ctx.er(n, m, 4)
+    import time as _t
+    t0 = _t.perf_counter()
+    gg.build_grid(64)
+    out["grid64_build_s"] = _t.perf_counter() - t0
+    gg.free()
+    return out
+
+
+def sssp_report(ctx, eg, scale=23, k=256, singles=16):
+    """Batched SSSP on RMAT-23 (seed 5), u32 weights U[1,255] hashed from the
+    endpoints: k sources in one batch versus single-source launches (a sample
+    of `singles`, scaled to k)."""
+    n = 1 << scale
+    g = ctx.rmat(scale, 16 * n, 5).build(eg.CSR)
+    roots = g.sample_roots(k, 6)
+    w = eg.weights("hash", seed=6, lo=1, hi=255)
+    g.sssp_multi(roots[:8], w, copy_out=False)
+    _, stb = g.sssp_multi(roots, w, copy_out=False)
+    t1 = 0.0
+    for r in roots[:singles]:
+        _, st = g.sssp(int(r), w, copy_out=False)
+        t1 += st.ms
+    per_single = t1 / singles
+    wf = eg.weights("f32", seed=6)
+    _, stf = g.sssp_multi(roots, wf, copy_out=False)
+    g.free()
+    return {"workload": "rmat%d, %d sources" % (scale, k), "batched_ms": stb.ms, "single_ms_each": per_single,
+            "runs_per_s_batched": k / (stb.ms / 1e3), "runs_per_s_single": 1e3 / per_single,
+            "speedup": per_single * k / stb.ms, "rounds_batched": stb.rounds,
+            "gteps_batched": stb.relaxations / (stb.ms / 1e3) / 1e9,
+            "f32_weights_batched_ms": stf.ms, "f32_rounds_batched": stf.rounds}
+
+
+def msbfs_report(g, roots):
+    """Bit-sliced BFS of all roots in one batch versus the same roots one by one."""
+    g.bfs_multi(roots[:4], copy_out=False)
+    _, stm = g.bfs_multi(roots, copy_out=False)
+    t1 = 0.0
+    for r in roots[:16]:
+        _, st = g.bfs(int(r), copy_out=False)
+        t1 += st.ms
+    per_single = t1 / 16
+    return {"batched_ms": stm.ms, "single_ms_each": per_single, "gteps_batched": stm.edges_traversed / (stm.ms / 1e3) / 1e9,
+            "speedup": per_single * len(roots) / stm.ms}
+
+
+def serve_report(ctx, eg, scale, rate, nq, seed=7, plain_sample=40, g=None):
     """Serving workload: Poisson arrivals at `rate` qps of 60% BFS, 25% SSSP
     (u32 weights U[1,255]), 15% personalised PageRank (1-8 seeds, tolerance
     10^U(-7,-4), <= 50 iterations) on the resident undirected RMAT graph;
     p50/p99 latency (arrival -> completion) and QPS, next to the QPS of the
-    plain one-query-at-a-time kernels on a sample of the same queries."""
+    plain one-query-at-a-time kernels on a sample of the same queries (BFS:
+    the direction-optimising BFS; SSSP: the single-source frontier
+    Bellman-Ford; PPR: the PageRank row kernel with a seed teleport)."""
     import torch
     n = 1 << scale
-    g = ctx.rmat(scale, 16 * n, 2, undirected=True).build(eg.CSR | eg.CSC)
+    own = g is None
+    if own:
+        g = ctx.rmat(scale, 16 * n, 2, undirected=True).build(eg.CSR | eg.CSC)
     od, _ = g.degrees(True, False)
     nz = np.nonzero(od > 0)[0].astype(np.uint32)
     rng = np.random.default_rng(seed)
@@ -270,9 +380,10 @@ def serve_report(ctx, eg, scale, rate, nq, seed=7, plain_sample=40):
         elif kind == "sssp":
             g.sssp(src, w, copy_out=False)
         else:
-            g.ppr([seeds], tolerance=tol, copy_out=False)
+            g.ppr_single(seeds, tolerance=tol, copy_out=False)
     plain_qps = len(samp) / (time.perf_counter() - t0)
-    g.free()
+    if own:
+        g.free()
     qps = nq / span
     return {"workload": "serve rmat%d undirected, %d queries, Poisson %g qps offered" % (scale, nq, rate),
             "qps": qps, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
@@ -360,7 +471,7 @@ def main():
     ap.add_argument("--pr-only", action="store_true", help="only the PageRank pull report (profiling)")
     ap.add_argument("--serve-only", action="store_true", help="only the serving report")
     ap.add_argument("--rate", type=float, default=20000.0)
-    ap.add_argument("--queries", type=int, default=2000)
+    ap.add_argument("--queries", type=int, default=1000)
     args = ap.parse_args()
     if args.serve_only:
         import everythinggraph_gb300 as eg

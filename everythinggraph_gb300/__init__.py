@@ -33,7 +33,9 @@ def lib():
 
 
 def weights(rule="ref", seed=0, lo=1, hi=255):
-    r = {"ref": L.EG_W_REF, "hash": L.EG_W_HASH, "unit": L.EG_W_UNIT}[rule]
+    """SSSP weight rule: "ref" (src%10+dst%10), "hash" (u32 in [lo, hi]),
+    "unit", or "f32" (fp32 in (0, 1]; distances come back as float32)."""
+    r = {"ref": L.EG_W_REF, "hash": L.EG_W_HASH, "unit": L.EG_W_UNIT, "f32": L.EG_W_HASH_F32}[rule]
     return L.Weights(r, seed, lo, hi)
 
 
@@ -163,6 +165,17 @@ class Graph:
     def device_ptr(self, which):
         return lib().eg_graph_device_ptr(self._h, which)
 
+    def tune(self):
+        """Times the row-kernel schedules on this graph and keeps the fastest;
+        returns [(tile entries, entries per lane, ms per iteration)] and the
+        chosen index."""
+        r = L.TuneResult()
+        L.check(lib().eg_graph_tune(self._h, ctypes.byref(r)))
+        return [(r.tile_entries[i], r.entries_per_lane[i], r.ms[i]) for i in range(r.ncand)], r.chosen
+
+    def set_row_schedule(self, tile_entries, entries_per_lane):
+        L.check(lib().eg_graph_set_row_schedule(self._h, tile_entries, entries_per_lane))
+
     def sample_roots(self, k, seed):
         r = np.empty(k, dtype=np.uint32)
         L.check(lib().eg_sample_roots(self._h, k, seed, _ptr(r)))
@@ -170,11 +183,12 @@ class Graph:
 
     # ---------------------------------------------------------------- algorithms
     def pagerank(self, iterations=10, damping=0.85, prev_init=-1.0, swap=True, deg_multiplier=1, dangling=False,
-                 compensated=False, tolerance=0.0, copy_out=True):
+                 compensated=False, tolerance=0.0, copy_out=True, use_graph=False):
         o = L.PrOpts()
         lib().eg_pr_opts_default(ctypes.byref(o))
         o.iterations, o.damping, o.prev_init, o.swap = iterations, damping, prev_init, int(swap)
         o.deg_multiplier, o.dangling, o.compensated, o.tolerance = deg_multiplier, int(dangling), int(compensated), tolerance
+        o.use_graph = int(use_graph)
         st = L.PrStats()
         out = np.empty(self.n, dtype=np.float32) if copy_out else None
         L.check(lib().eg_pagerank(self._h, ctypes.byref(o), _ptr(out), ctypes.byref(st)))
@@ -214,6 +228,8 @@ class Graph:
         out = np.empty(self.n, dtype=np.uint32) if copy_out else None
         st = L.SsspStats()
         L.check(lib().eg_sssp(self._h, root, ctypes.byref(w), _ptr(out), ctypes.byref(st)))
+        if out is not None and w.rule == L.EG_W_HASH_F32:
+            out = out.view(np.float32)
         return out, st
 
     def sssp_multi(self, roots, w=None, copy_out=True):
@@ -222,6 +238,8 @@ class Graph:
         out = np.empty((len(roots), self.n), dtype=np.uint32) if copy_out else None
         st = L.SsspStats()
         L.check(lib().eg_sssp_multi(self._h, _ptr(roots), len(roots), ctypes.byref(w), _ptr(out), ctypes.byref(st)))
+        if out is not None and w.rule == L.EG_W_HASH_F32:
+            out = out.view(np.float32)
         return out, st
 
     def ppr(self, seed_lists, damping=0.85, tolerance=1e-6, max_iters=50, copy_out=True):
@@ -238,6 +256,18 @@ class Graph:
         out = np.empty((nq, self.n), dtype=np.float32) if copy_out else None
         st = L.PprStats()
         L.check(lib().eg_ppr_multi(self._h, _ptr(seeds), _ptr(offs), nq, ctypes.byref(o), _ptr(out), ctypes.byref(st)))
+        return out, st
+
+    def ppr_single(self, seeds, damping=0.85, tolerance=1e-6, max_iters=50, copy_out=True):
+        """One personalised PageRank query on the plain PageRank row kernel."""
+        seeds = np.ascontiguousarray(seeds, dtype=np.uint32)
+        o = L.PprOpts()
+        o.damping, o.max_iters = damping, max_iters
+        for q in range(32):
+            o.tolerance[q] = tolerance
+        out = np.empty(self.n, dtype=np.float32) if copy_out else None
+        st = L.PprStats()
+        L.check(lib().eg_ppr(self._h, _ptr(seeds), len(seeds), ctypes.byref(o), _ptr(out), ctypes.byref(st)))
         return out, st
 
     def wcc(self, copy_out=True):

@@ -20,7 +20,7 @@ EG_DEV_CSR_PTR, EG_DEV_CSR_COL, EG_DEV_CSC_PTR, EG_DEV_CSC_COL, EG_DEV_OUT_DEG =
 EG_DEV_RANK, EG_DEV_LEVEL, EG_DEV_PARENT, EG_DEV_DIST, EG_DEV_LABEL, EG_DEV_SPMV_Y = 10, 11, 12, 13, 14, 15
 EG_SPMV_U32_PULL, EG_SPMV_U32_PUSH, EG_SPMV_U32_EDGE, EG_SPMV_F32, EG_SPMV_F32_COMP, EG_SPMV_F64 = 0, 1, 2, 3, 4, 5
 EG_BFS_AUTO, EG_BFS_PUSH_ONLY, EG_BFS_PULL_ONLY = 0, 1, 2
-EG_W_REF, EG_W_HASH, EG_W_UNIT = 0, 1, 2
+EG_W_REF, EG_W_HASH, EG_W_UNIT, EG_W_HASH_F32 = 0, 1, 2, 3
 EG_Q_BFS, EG_Q_SSSP, EG_Q_PPR = 1, 2, 3
 
 
@@ -36,7 +36,13 @@ class PrOpts(ctypes.Structure):
 
 
 class PrStats(ctypes.Structure):
-    _fields_ = [("iterations_run", c_int), ("residual", c_f64), ("dangling_mass", c_f64), ("ms", c_f32)]
+    _fields_ = [("iterations_run", c_int), ("residual", c_f64), ("dangling_mass", c_f64), ("ms", c_f32),
+                ("row_kernel_ms", c_f32)]
+
+
+class TuneResult(ctypes.Structure):
+    _fields_ = [("ncand", c_int), ("chosen", c_int), ("tile_entries", c_int * 8), ("entries_per_lane", c_int * 8),
+                ("ms", c_f32 * 8)]
 
 
 class SpmvOpts(ctypes.Structure):
@@ -122,6 +128,9 @@ SIGNATURES = {
     "eg_wcc": (c_int, [c_void_p, c_void_p, P(WccStats)]),
     "eg_sample_roots": (c_int, [c_void_p, c_int, c_u64, c_void_p]),
     "eg_ppr_multi": (c_int, [c_void_p, c_void_p, c_void_p, c_int, P(PprOpts), c_void_p, P(PprStats)]),
+    "eg_graph_tune": (c_int, [c_void_p, P(TuneResult)]),
+    "eg_graph_set_row_schedule": (c_int, [c_void_p, c_int, c_int]),
+    "eg_ppr": (c_int, [c_void_p, c_void_p, c_u32, P(PprOpts), c_void_p, P(PprStats)]),
     "eg_serve_opts_default": (None, [P(ServeOpts)]),
     "eg_serve_open": (c_int, [c_void_p, P(ServeOpts), P(c_void_p)]),
     "eg_serve_submit": (c_int, [c_void_p, P(Query), P(c_u64)]),

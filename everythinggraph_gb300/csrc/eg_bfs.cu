@@ -14,6 +14,7 @@
 #include <string.h>
 
 #include "eg_internal.cuh"
+#include "eg_mspull.cuh"
 
 namespace {
 
@@ -756,26 +757,6 @@ __global__ void k_ms_roots(const uint32_t *roots, int k, uint32_t n, unsigned lo
 
 // Pull: a vertex ORs the frontier words of its in-neighbours, stopping early
 // once every source it still lacks has been found.
-__global__ void __launch_bounds__(256) k_ms_pull(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
-                                                 uint32_t n, unsigned long long all,
-                                                 const unsigned long long *__restrict__ seen,
-                                                 const unsigned long long *__restrict__ front,
-                                                 unsigned long long *__restrict__ next) {
-    uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
-        unsigned long long need = all & ~seen[v];
-        unsigned long long acc = 0ull;
-        if (need) {
-            const uint32_t b = ptr[v], e = ptr[v + 1];
-            for (uint32_t p = b; p < e; p++) {
-                acc |= __ldg(front + col[p]);
-                if ((acc & need) == need) break;
-            }
-        }
-        next[v] = acc & need;
-    }
-}
-
 // Push: one warp per vertex with a nonzero frontier word; vertices with more
 // than EG_BFS_BIG_DEG out-edges go to a side list for k_ms_push_big.
 __global__ void __launch_bounds__(256) k_ms_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
@@ -944,8 +925,13 @@ extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *
         const bool pull = (double)count + (double)fdeg > threshold;
         EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(MsCounters), ctx->stream));
         if (pull) {
-            k_ms_pull<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col),
-                                                                  n, all, seen, front, next);
+            // the heavy list reuses the push side list (idle in a pull level)
+            k_msp_light<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(bp<uint32_t>(in_adj->ptr),
+                                                                    bp<uint32_t>(in_adj->col), n, all, seen, front, next,
+                                                                    big, &cnt->nbig);
+            EG_LAUNCHED(ctx);
+            k_msp_heavy<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
+                bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col), all, seen, front, next, big, &cnt->nbig);
             EG_LAUNCHED(ctx);
             pull_levels++;
         } else {

@@ -43,6 +43,7 @@ extern "C" int eg_open(int device, uint64_t hbm_budget_bytes, eg_ctx **out) {
     EG_CUDA(cudaMallocHost(&c->h_pinned, 1 << 20));
     EG_CUDA(cudaEventCreate(&c->ev0));
     EG_CUDA(cudaEventCreate(&c->ev1));
+    for (cudaEvent_t &e : c->evk) EG_CUDA(cudaEventCreate(&e));
     *out = c;
     return EG_OK;
 }
@@ -53,6 +54,7 @@ extern "C" int eg_close(eg_ctx *c) {
     cudaStreamSynchronize(c->stream);
     cudaEventDestroy(c->ev0);
     cudaEventDestroy(c->ev1);
+    for (cudaEvent_t e : c->evk) cudaEventDestroy(e);
     cudaFreeHost(c->h_pinned);
     cudaStreamDestroy(c->stream);
     delete c;
@@ -285,6 +287,8 @@ extern "C" void eg_graph_free(eg_graph *g) {
         if (bg.exec) cudaGraphExecDestroy(bg.exec);
         if (bg.graph) cudaGraphDestroy(bg.graph);
     }
+    if (g->prg.exec) cudaGraphExecDestroy(g->prg.exec);
+    if (g->prg.graph) cudaGraphDestroy(g->prg.graph);
     delete g;
 }
 

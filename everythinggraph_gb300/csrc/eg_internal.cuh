@@ -36,6 +36,7 @@ void eg_clear_error();
     } while (0)
 
 // ---------------------------------------------------------------- context
+#define EG_KEV 8  // kernel launches timed individually per call
 struct eg_ctx {
     int device;
     int sm_count;
@@ -45,6 +46,7 @@ struct eg_ctx {
     uint64_t launches;
     void *h_pinned;  // 1 MiB pinned staging for small readbacks
     cudaEvent_t ev0, ev1;
+    cudaEvent_t evk[2 * EG_KEV];  // begin/end pairs around single kernel launches
 };
 
 int eg_dmalloc(eg_ctx *ctx, void **p, uint64_t bytes);
@@ -115,6 +117,9 @@ struct eg_graph {
     eg_buf sssp_work;
     eg_buf ppr_work;
     eg_bfs_graph bfsg[2];  // without / with parents
+    eg_bfs_graph prg;      // PageRank iterations (key: options and buffers)
+    int row_cfg = 0;       // row-kernel schedule (entries per warp tile, per lane)
+    uint64_t prk[16] = {};
 };
 
 // ---------------------------------------------------------------- helpers
@@ -163,5 +168,41 @@ __host__ __device__ __forceinline__ uint64_t eg_draw(uint64_t key, uint64_t j) {
 __host__ __device__ __forceinline__ uint64_t eg_edge_hash(uint64_t seed, uint32_t u, uint32_t v) {
     uint32_t a = u < v ? u : v, b = u < v ? v : u;
     return eg_draw(eg_key(seed, ((uint64_t)a << 32) | b), 0);
+}
+
+// SSSP edge weights computed from the endpoints (no weight array), and the
+// extension of a path distance by one edge in the rule's encoding: u32 sums
+// saturating at EG_SSSP_INF, or fp32 sums (bit patterns, which order like
+// the values for non-negative floats; unreached = +inf).
+#define EG_SSSP_INF 0xfffffffeu
+#define EG_SSSP_INF_F32 0x7f800000u
+struct eg_wrule {
+    int rule;
+    uint64_t seed;
+    uint32_t lo;
+    uint64_t span;
+    __host__ __device__ __forceinline__ uint32_t inf() const {
+        return rule == EG_W_HASH_F32 ? EG_SSSP_INF_F32 : EG_SSSP_INF;
+    }
+    __device__ __forceinline__ uint32_t extend(uint32_t du, uint32_t u, uint32_t v) const {
+        if (rule == EG_W_HASH_F32) {
+            const float w = (float)((eg_edge_hash(seed, u, v) >> 40) + 1) * (1.0f / 16777216.0f);
+            return __float_as_uint(__fadd_rn(__uint_as_float(du), w));
+        }
+        uint32_t w;
+        if (rule == EG_W_REF) w = (u % 10u) + (v % 10u);
+        else if (rule == EG_W_UNIT) w = 1u;
+        else w = lo + (uint32_t)(((eg_edge_hash(seed, u, v) >> 32) * span) >> 32);
+        const uint64_t nd = (uint64_t)du + w;
+        return nd < EG_SSSP_INF ? (uint32_t)nd : EG_SSSP_INF;
+    }
+};
+static inline eg_wrule eg_make_wrule(const eg_weights *w) {
+    eg_wrule r;
+    r.rule = w ? w->rule : EG_W_REF;
+    r.seed = w ? w->seed : 0;
+    r.lo = w ? w->lo : 0;
+    r.span = w ? (uint64_t)w->hi - w->lo + 1 : 1;
+    return r;
 }
 #endif

@@ -778,20 +778,23 @@ __global__ void k_coo_empty_rows(const uint32_t *__restrict__ ptr, uint32_t n, d
     }
 }
 
-// Four entries per lane: lane l of a warp holds entries base+4l .. base+4l+3
-// (128-bit loads of rid and col), sums the runs of equal rows among them
-// locally, and one segmented scan per 128 entries (flag form: a lane whose
-// last run starts inside it, or whose row differs from the previous lane's
-// last row, starts a segment) joins runs that cross lanes.  A run is emitted
-// by the lane holding its last entry; the run open after lane 31 is carried
-// to the next chunk.  Tiles are multiples of 128 entries, so only the last
-// tile has padding entries (row EG_MP_NONE, never emitted).
-template <class Op, int TILE_E, bool REDUCE>
-__global__ void __launch_bounds__(256) k_coo4_rows(const uint32_t *__restrict__ rid, const uint32_t *__restrict__ col,
+// U entries per lane (U = 4 or 8): lane l of a warp holds entries
+// base+U*l .. base+U*l+U-1 (128-bit loads of rid and col), sums the runs of
+// equal rows among them locally, and one segmented scan per 32*U entries
+// (flag form: a lane whose last run starts inside it, or whose row differs
+// from the previous lane's last row, starts a segment) joins runs that cross
+// lanes.  A run is emitted by the lane holding its last entry; the run open
+// after lane 31 is carried to the next chunk.  Tiles are multiples of 32*U
+// entries, so only the last tile has padding entries (row EG_MP_NONE, never
+// emitted).
+template <class Op, int TILE_E, int U, bool REDUCE>
+__global__ void __launch_bounds__(256) k_coov_rows(const uint32_t *__restrict__ rid, const uint32_t *__restrict__ col,
                                                    uint32_t m, uint32_t ntiles,
                                                    eg_mp_carry<typename Op::A> *__restrict__ carry,
                                                    double2 *__restrict__ part, Op op) {
-    static_assert(TILE_E % 128 == 0, "tiles hold whole chunks");
+    static_assert(U == 4 || U == 8, "4 or 8 entries per lane");
+    static_assert(TILE_E % (32 * U) == 0, "tiles hold whole chunks");
+    constexpr uint32_t CH = 32u * U;  // entries per chunk
     using V = typename Op::V;
     using A = typename Op::A;
     __shared__ double2 s_red[8];
@@ -823,35 +826,38 @@ __global__ void __launch_bounds__(256) k_coo4_rows(const uint32_t *__restrict__ 
                 red.y += d.y;
             }
         };
-        for (uint32_t base = E0; base < E1; base += 128) {
-            const uint32_t e = base + 4 * lane;
-            uint32_t r[4], u[4];
-            if (e + 3 < E1) {
-                const uint4 rr = __ldg(reinterpret_cast<const uint4 *>(rid + e));
-                const uint4 cc = __ldg(reinterpret_cast<const uint4 *>(col + e));
-                r[0] = rr.x; r[1] = rr.y; r[2] = rr.z; r[3] = rr.w;
-                u[0] = cc.x; u[1] = cc.y; u[2] = cc.z; u[3] = cc.w;
+        for (uint32_t base = E0; base < E1; base += CH) {
+            const uint32_t e = base + U * lane;
+            uint32_t r[U], u[U];
+            if (e + U - 1 < E1) {
+#pragma unroll
+                for (int h = 0; h < U / 4; h++) {
+                    const uint4 rr = __ldg(reinterpret_cast<const uint4 *>(rid + e) + h);
+                    const uint4 cc = __ldg(reinterpret_cast<const uint4 *>(col + e) + h);
+                    r[4 * h] = rr.x; r[4 * h + 1] = rr.y; r[4 * h + 2] = rr.z; r[4 * h + 3] = rr.w;
+                    u[4 * h] = cc.x; u[4 * h + 1] = cc.y; u[4 * h + 2] = cc.z; u[4 * h + 3] = cc.w;
+                }
             } else {
 #pragma unroll
-                for (int k = 0; k < 4; k++) {
+                for (int k = 0; k < U; k++) {
                     const bool in = e + k < E1;
                     r[k] = in ? __ldg(rid + e + k) : EG_MP_NONE;
                     u[k] = in ? __ldg(col + e + k) : 0u;
                 }
             }
-            V v[4];
+            V v[U];
 #pragma unroll
-            for (int k = 0; k < 4; k++) v[k] = r[k] != EG_MP_NONE ? op.gather(e + k, u[k]) : V();
+            for (int k = 0; k < U; k++) v[k] = r[k] != EG_MP_NONE ? op.gather(e + k, u[k]) : V();
             // row of the entry after this lane's last one
             uint32_t nxt = __shfl_down_sync(EG_FULL_MASK, r[0], 1);
-            if (lane == 31) nxt = base + 128 < E1 ? __ldg(rid + base + 128) : tile_next;
-            const uint32_t prev_last = __shfl_up_sync(EG_FULL_MASK, r[3], 1);
-            // local runs: head run (from entry 0), middle runs, tail run (to entry 3)
+            if (lane == 31) nxt = base + CH < E1 ? __ldg(rid + base + CH) : tile_next;
+            const uint32_t prev_last = __shfl_up_sync(EG_FULL_MASK, r[U - 1], 1);
+            // local runs: head run (from entry 0), middle runs, tail run (to entry U-1)
             A hsum = op.add(op.zero(), v[0]);
             A run = hsum;
             bool multi = false;
 #pragma unroll
-            for (int k = 1; k < 4; k++) {
+            for (int k = 1; k < U; k++) {
                 if (r[k] != r[k - 1]) {
                     if (!multi) hsum = run;  // the head run closed at k-1
                     else finish(r[k - 1], run);
@@ -886,8 +892,8 @@ __global__ void __launch_bounds__(256) k_coo4_rows(const uint32_t *__restrict__ 
                 }
                 finish(r[0], tot);
             }
-            if (nxt != r[3]) finish(r[3], x);
-            crow = __shfl_sync(EG_FULL_MASK, r[3], 31);
+            if (nxt != r[U - 1]) finish(r[U - 1], x);
+            crow = __shfl_sync(EG_FULL_MASK, r[U - 1], 31);
             cval = eg_shfl_idx(x, 31);
         }
         const uint32_t hmask = __ballot_sync(EG_FULL_MASK, head_done);

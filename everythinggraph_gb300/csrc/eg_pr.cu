@@ -19,6 +19,7 @@
 // and 16 per vertex (row end, degree, rank write, contrib write).
 #include <math.h>
 #include <stdlib.h>
+#include <string.h>
 
 #include <type_traits>
 
@@ -74,6 +75,22 @@ struct eg_pr_dev {
     double dangling;
 };
 
+// Teleport set of a single personalised PageRank query: up to
+// EG_PPR1_SEEDS distinct vertices (relabelled ids) with their multiplicity.
+#define EG_PPR1_SEEDS 8
+struct PprSeeds {
+    uint32_t count;  // distinct seeds; 0 = uniform teleport (plain PageRank)
+    uint32_t id[EG_PPR1_SEEDS];
+    float mult[EG_PPR1_SEEDS];
+    __device__ __forceinline__ float weight(uint32_t v) const {
+        float w = 0.f;
+#pragma unroll
+        for (int i = 0; i < EG_PPR1_SEEDS; i++)
+            if (i < (int)count && v == id[i]) w = mult[i];
+        return w;
+    }
+};
+
 template <bool COMP>
 struct PrOp {
     using V = float;
@@ -87,6 +104,7 @@ struct PrOp {
     float damping;
     int residual;
     float base;
+    PprSeeds seeds;
     __device__ __forceinline__ bool active() const { return st->done == 0; }
     __device__ __forceinline__ void setup() { base = st->base; }
     __device__ __forceinline__ V gather(uint32_t, uint32_t u) const { return __ldg(cin + u); }
@@ -106,7 +124,9 @@ struct PrOp {
         float sum;
         if constexpr (COMP) sum = s.x + s.y;
         else sum = s;
-        float r = fmaf(damping, sum, base);
+        // teleport: base on every vertex, or base x multiplicity on the seeds
+        const float b = seeds.count ? base * seeds.weight(v) : base;
+        float r = fmaf(damping, sum, b);
         double res = 0.0;
         if (residual) res = fabs((double)r - (double)rank[v]);
         rank[v] = r;
@@ -137,13 +157,40 @@ __global__ void k_pr_init(uint32_t n, float prev_init, const uint32_t *__restric
     }
 }
 
+// Personalised start vector: multiplicity / total seeds on the seeds, 0 elsewhere.
+__global__ void k_ppr1_init(uint32_t n, PprSeeds seeds, float inv_total, const uint32_t *__restrict__ deg,
+                            float *__restrict__ rank, float *__restrict__ contrib, double2 *__restrict__ part) {
+    __shared__ double s_red[8];
+    double dang = 0.0;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const uint32_t d = deg[v];
+        const float r = seeds.weight(v) * inv_total;
+        rank[v] = r;
+        contrib[v] = d ? __fdiv_rn(r, (float)d) : 0.f;
+        if (!d) dang += (double)r;
+    }
+    for (int o = 16; o > 0; o >>= 1) dang += __shfl_down_sync(EG_FULL_MASK, dang, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = dang;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s_red[w];
+        part[blockIdx.x] = make_double2(0.0, t);
+    }
+}
+
+__global__ void k_map_ids(const uint32_t *__restrict__ perm, const uint32_t *__restrict__ in, uint32_t k,
+                          uint32_t *__restrict__ out) {
+    for (uint32_t i = threadIdx.x; i < k; i += blockDim.x) out[i] = perm[in[i]];
+}
+
 __global__ void k_pr_unpermute(const float *__restrict__ rank_p, const uint32_t *__restrict__ perm, uint32_t n,
                                float *__restrict__ rank) {
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) rank[v] = rank_p[perm[v]];
 }
 
 // One block: deterministic FP64 sum of the partials, next base, stop test.
-__global__ void k_pr_reduce(const double2 *__restrict__ part, uint32_t nparts, eg_pr_dev *st, uint32_t n,
+__global__ void k_pr_reduce(const double2 *__restrict__ part, uint32_t nparts, eg_pr_dev *st, double tele_div,
                             float damping, int dangling, double tol, int count_iter) {
     __shared__ double2 s[256];
     if (st->done) return;
@@ -165,8 +212,8 @@ __global__ void k_pr_reduce(const double2 *__restrict__ part, uint32_t nparts, e
         double res = s[0].x, dang = s[0].y;
         st->residual = res;
         st->dangling = dang;
-        double b = (1.0 - (double)damping) / (double)n;
-        if (dangling) b += (double)damping * dang / (double)n;
+        double b = (1.0 - (double)damping) / tele_div;
+        if (dangling) b += (double)damping * dang / tele_div;
         st->base = (float)b;
         if (count_iter) {
             st->iters += 1;
@@ -229,36 +276,55 @@ static int mpp_launch(eg_graph *g, eg_adj &adj, eg_mp_sched &s, eg_buf &carry_bu
     return EG_OK;
 }
 
-// Row-id stream variant (k_coo4_rows): one warp per TILE_E entries.  part[]
-// receives per-CTA partials of the main kernel, then of the empty-row kernel,
-// then of the fix-up; returns their count.
-#define EG_COO_TILE 2048
-#define EG_COO_U 4
-template <class Op, bool REDUCE>
-static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts) {
+// Row-id stream kernel (k_coov_rows): one warp per TILE entries, U entries
+// per lane.  part[] receives per-CTA partials of the main kernel, then of the
+// empty-row kernel, then of the fix-up; returns their count.  The schedule
+// (TILE, U) is the graph's row_cfg, picked by eg_graph_tune.
+#define EG_COO_TILE_MIN 1024
+#define EG_ROW_CFGS 5
+static const int kRowTile[EG_ROW_CFGS] = {2048, 1024, 4096, 2048, 4096};
+static const int kRowU[EG_ROW_CFGS] = {4, 4, 4, 8, 8};
+
+template <class Op, int TILE, int U, bool REDUCE>
+static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts,
+                        cudaEvent_t ev_begin, cudaEvent_t ev_end) {
     eg_ctx *ctx = g->ctx;
     using A = typename Op::A;
     const uint32_t m = (uint32_t)g->m;
-    const uint32_t ntiles = m ? eg_div_up(m, EG_COO_TILE) : 0;
+    const uint32_t ntiles = m ? eg_div_up(m, TILE) : 0;
     EG_TRY(eg_buf_ensure(ctx, carry_buf, ((uint64_t)ntiles + 1) * sizeof(eg_mp_carry<A>)));
     const uint32_t g1 = ntiles ? eg_div_up((uint64_t)ntiles * 32, 256) : 0;
     uint32_t g2 = eg_div_up(g->n, 256);
     if (g2 > (uint32_t)ctx->sm_count * 8) g2 = (uint32_t)ctx->sm_count * 8;
     if (g1) {
-        k_coo4_rows<Op, EG_COO_TILE, REDUCE><<<g1, 256, 0, ctx->stream>>>(
+        if (ev_begin) EG_CUDA(cudaEventRecord(ev_begin, ctx->stream));
+        k_coov_rows<Op, TILE, U, REDUCE><<<g1, 256, 0, ctx->stream>>>(
             bp<uint32_t>(adj.rid), bp<uint32_t>(adj.col), m, ntiles, bp<eg_mp_carry<A>>(carry_buf), part, op);
         EG_LAUNCHED(ctx);
+        if (ev_end) EG_CUDA(cudaEventRecord(ev_end, ctx->stream));
     }
     k_coo_empty_rows<Op, REDUCE><<<g2, 256, 0, ctx->stream>>>(bp<uint32_t>(adj.ptr), g->n, part ? part + g1 : nullptr,
                                                               op);
     EG_LAUNCHED(ctx);
     if (g1) {
-        k_coo_fixup<Op, EG_COO_TILE, REDUCE><<<g1, 256, 0, ctx->stream>>>(
+        k_coo_fixup<Op, TILE, REDUCE><<<g1, 256, 0, ctx->stream>>>(
             bp<uint32_t>(adj.ptr), ntiles, bp<eg_mp_carry<A>>(carry_buf), part ? part + g1 + g2 : nullptr, op);
         EG_LAUNCHED(ctx);
     }
     *nparts = g1 + g2 + g1;
     return EG_OK;
+}
+
+template <class Op, bool REDUCE>
+static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts,
+                      cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr) {
+    switch (g->row_cfg) {
+    case 1: return coo_launch_t<Op, 1024, 4, REDUCE>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
+    case 2: return coo_launch_t<Op, 4096, 4, REDUCE>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
+    case 3: return coo_launch_t<Op, 2048, 8, REDUCE>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
+    case 4: return coo_launch_t<Op, 4096, 8, REDUCE>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
+    default: return coo_launch_t<Op, 2048, 4, REDUCE>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
+    }
 }
 
 extern "C" void eg_pr_opts_default(eg_pr_opts *o) {
@@ -274,10 +340,12 @@ extern "C" void eg_pr_opts_default(eg_pr_opts *o) {
     o->use_graph = 0;
 }
 
+// Launches every iteration; with `timed`, the row kernels of the first
+// EG_KEV iterations are bracketed by the context's kernel events.
 template <bool COMP, bool REDUCE>
-static int pr_iterations(eg_graph *g, const eg_pr_opts &o, eg_pr_dev *st, double2 *part, eg_buf &carry) {
+static int pr_iterations(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, double tele_div, eg_pr_dev *st,
+                         double2 *part, eg_buf &carry, bool timed) {
     eg_ctx *ctx = g->ctx;
-    uint32_t grid = 0;
     for (int it = 0; it < o.iterations; it++) {
         PrOp<COMP> op;
         bool odd = o.swap && (it & 1);
@@ -290,39 +358,91 @@ static int pr_iterations(eg_graph *g, const eg_pr_opts &o, eg_pr_dev *st, double
         op.damping = o.damping;
         op.residual = o.tolerance > 0.0;
         op.base = 0.f;
+        op.seeds = ps;
         uint32_t nparts = 0;
-        EG_TRY((coo_launch<PrOp<COMP>, REDUCE>(g, g->csc_p, carry, part, op, &nparts)));
-        (void)grid;
-        k_pr_reduce<<<1, 256, 0, ctx->stream>>>(part, REDUCE ? nparts : 0, st, g->n, o.damping, o.dangling,
+        const bool t = timed && it < EG_KEV;
+        EG_TRY((coo_launch<PrOp<COMP>, REDUCE>(g, g->csc_p, carry, part, op, &nparts, t ? ctx->evk[2 * it] : nullptr,
+                                                t ? ctx->evk[2 * it + 1] : nullptr)));
+        k_pr_reduce<<<1, 256, 0, ctx->stream>>>(part, REDUCE ? nparts : 0, st, tele_div, o.damping, o.dangling,
                                                 o.tolerance, 1);
         EG_LAUNCHED(ctx);
     }
     return EG_OK;
 }
 
-extern "C" int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out, eg_pr_stats *stats) {
-    if (!g) return eg_fail(EG_EINVAL, "NULL graph");
-    eg_pr_opts o;
-    if (opts) o = *opts;
-    else eg_pr_opts_default(&o);
-    if (o.iterations < 0 || o.deg_multiplier == 0) return eg_fail(EG_EINVAL, "bad PageRank options");
-    if (!(g->built & EG_LAYOUT_CSC) || !(g->built & EG_LAYOUT_CSR))
-        return eg_fail(EG_ENOTBUILT, "PageRank needs the CSC (in-lists) and CSR (out-degrees)");
+static int pr_dispatch(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, double tele_div, bool reduce,
+                       eg_pr_dev *st, double2 *part, eg_buf &carry, bool timed) {
+    if (o.compensated) {
+        if (reduce) return pr_iterations<true, true>(g, o, ps, tele_div, st, part, carry, timed);
+        return pr_iterations<true, false>(g, o, ps, tele_div, st, part, carry, timed);
+    }
+    if (reduce) return pr_iterations<false, true>(g, o, ps, tele_div, st, part, carry, timed);
+    return pr_iterations<false, false>(g, o, ps, tele_div, st, part, carry, timed);
+}
+
+// The iteration loop of plain PageRank captured once as a CUDA graph and
+// replayed while the options and the buffers it was captured with stay the same.
+static int pr_graph(eg_graph *g, const eg_pr_opts &o, bool reduce, eg_pr_dev *st, double2 *part, eg_buf &carry) {
     eg_ctx *ctx = g->ctx;
-    EG_CUDA(cudaSetDevice(ctx->device));
+    uint64_t key[16] = {};
+    key[0] = (uint64_t)o.iterations;
+    key[1] = (uint64_t)o.swap | ((uint64_t)o.compensated << 1) | ((uint64_t)reduce << 2) | ((uint64_t)o.dangling << 3);
+    uint32_t dbits;
+    memcpy(&dbits, &o.damping, 4);
+    key[2] = dbits | ((uint64_t)o.deg_multiplier << 32);
+    memcpy(&key[3], &o.tolerance, 8);
+    key[4] = (uint64_t)(uintptr_t)g->contrib0.p;
+    key[5] = (uint64_t)(uintptr_t)g->contrib1.p;
+    key[6] = (uint64_t)(uintptr_t)g->rank_p.p;
+    key[7] = (uint64_t)(uintptr_t)g->deg_p.p;
+    key[8] = (uint64_t)(uintptr_t)st;
+    key[9] = (uint64_t)(uintptr_t)part;
+    key[10] = (uint64_t)(uintptr_t)carry.p;
+    key[11] = (uint64_t)(uintptr_t)g->csc_p.rid.p;
+    key[12] = (uint64_t)(uintptr_t)g->csc_p.col.p;
+    key[13] = (uint64_t)(uintptr_t)g->csc_p.ptr.p;
+    key[14] = g->m ^ ((uint64_t)g->row_cfg << 56);
+    key[15] = (uint64_t)ctx->stream ^ 0x5052ull;
+    if (g->prg.exec && !memcmp(key, g->prk, sizeof(key))) return EG_OK;
+    if (g->prg.exec) cudaGraphExecDestroy(g->prg.exec);
+    if (g->prg.graph) cudaGraphDestroy(g->prg.graph);
+    g->prg.exec = nullptr;
+    g->prg.graph = nullptr;
+    // the carries must be allocated before capture (no allocation inside it)
+    EG_TRY(eg_buf_ensure(ctx, carry,
+                         ((uint64_t)(g->m ? eg_div_up(g->m, EG_COO_TILE_MIN) : 0) + 1) * sizeof(eg_mp_carry<double>)));
+    key[10] = (uint64_t)(uintptr_t)carry.p;
+    PprSeeds none;
+    memset(&none, 0, sizeof(none));
+    EG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int rc = pr_dispatch(g, o, none, (double)g->n, reduce, st, part, carry, false);
+    cudaGraph_t gr = nullptr;
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &gr);
+    if (rc != EG_OK) {
+        if (gr) cudaGraphDestroy(gr);
+        return rc;
+    }
+    if (e != cudaSuccess) return eg_fail(EG_ECUDA, "PageRank capture: %s", cudaGetErrorString(e));
+    g->prg.graph = gr;
+    EG_CUDA(cudaGraphInstantiate(&g->prg.exec, gr, 0));
+    memcpy(g->prk, key, sizeof(key));
+    return EG_OK;
+}
+
+// Shared by eg_pagerank and eg_ppr: the iterations over the relabelled CSC,
+// then the ranks back in the original vertex order.  `ps` (in relabelled
+// ids) selects the personalised teleport; its total multiplicity divides it.
+static int pr_run(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, uint32_t seed_total, float *rank_out,
+                  eg_pr_stats *stats) {
+    eg_ctx *ctx = g->ctx;
     const uint32_t n = g->n;
-    EG_TRY(eg_build_sched(g, g->csc, g->sched_csc, EG_MP_T * EG_MP_IPT));
-    const uint32_t ntiles = g->sched_csc.ntiles;
-    const uint32_t coo_tiles = g->m ? eg_div_up(g->m, EG_COO_TILE) : 0;
-    const uint32_t nparts = ntiles + eg_div_up((uint64_t)ntiles * 32, 256) + 2 * eg_div_up((uint64_t)coo_tiles * 32, 256) +
-                            (uint32_t)ctx->sm_count * 8;
-    EG_TRY(eg_build_relabeled_csc(g));
+    const uint32_t coo_tiles = g->m ? eg_div_up(g->m, EG_COO_TILE_MIN) : 0;  // the most tiles of any schedule
+    const uint32_t nparts = 2 * eg_div_up((uint64_t)coo_tiles * 32, 256) + (uint32_t)ctx->sm_count * 8;
     EG_TRY(eg_buf_ensure(ctx, g->rank, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->rank_p, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->contrib0, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->contrib1, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->pr_part, ((uint64_t)nparts + 1024) * sizeof(double2)));
-    EG_TRY(eg_buf_ensure(ctx, g->pr_stats, sizeof(eg_pr_dev)));
     EG_TRY(eg_buf_ensure(ctx, g->errflag, 16));
     EG_CUDA(cudaMemsetAsync(g->errflag.p, 0, 16, ctx->stream));
     eg_buf &carry = g->mp_carry;
@@ -330,23 +450,30 @@ extern "C" int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out,
     double2 *part = bp<double2>(g->pr_part);
     EG_CUDA(cudaMemsetAsync(st, 0, sizeof(eg_pr_dev), ctx->stream));
     EG_CUDA(cudaMemsetAsync(part, 0, ((uint64_t)nparts + 1024) * sizeof(double2), ctx->stream));
-    float prev_init = o.prev_init < 0.f ? 1.0f / (float)n : o.prev_init;
+    const bool ppr = ps.count > 0;
+    const double tele_div = ppr ? (double)seed_total : (double)n;
     const bool reduce = o.tolerance > 0.0 || o.dangling;
     uint32_t ib = eg_div_up(n, 256);
     if (ib > 1024) ib = 1024;
-    k_pr_init<<<ib, 256, 0, ctx->stream>>>(n, prev_init, bp<uint32_t>(g->deg_p), o.deg_multiplier,
-                                          bp<float>(g->rank_p), bp<float>(g->contrib0), part);
+    if (ppr) {
+        k_ppr1_init<<<ib, 256, 0, ctx->stream>>>(n, ps, (float)(1.0 / (double)seed_total), bp<uint32_t>(g->deg_p),
+                                                bp<float>(g->rank_p), bp<float>(g->contrib0), part);
+    } else {
+        const float prev_init = o.prev_init < 0.f ? 1.0f / (float)n : o.prev_init;
+        k_pr_init<<<ib, 256, 0, ctx->stream>>>(n, prev_init, bp<uint32_t>(g->deg_p), o.deg_multiplier,
+                                              bp<float>(g->rank_p), bp<float>(g->contrib0), part);
+    }
     EG_LAUNCHED(ctx);
-    k_pr_reduce<<<1, 256, 0, ctx->stream>>>(part, ib, st, n, o.damping, o.dangling, 0.0, 0);
+    k_pr_reduce<<<1, 256, 0, ctx->stream>>>(part, ib, st, tele_div, o.damping, o.dangling, 0.0, 0);
     EG_LAUNCHED(ctx);
     EG_CUDA(cudaMemsetAsync(part, 0, ((uint64_t)nparts + 1024) * sizeof(double2), ctx->stream));
+    const bool graph = o.use_graph && !ppr;
+    if (graph) EG_TRY(pr_graph(g, o, reduce, st, part, carry));
     EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-    if (o.compensated) {
-        if (reduce) EG_TRY((pr_iterations<true, true>(g, o, st, part, carry)));
-        else EG_TRY((pr_iterations<true, false>(g, o, st, part, carry)));
+    if (graph) {
+        if (o.iterations > 0) EG_CUDA(cudaGraphLaunch(g->prg.exec, ctx->stream));
     } else {
-        if (reduce) EG_TRY((pr_iterations<false, true>(g, o, st, part, carry)));
-        else EG_TRY((pr_iterations<false, false>(g, o, st, part, carry)));
+        EG_TRY(pr_dispatch(g, o, ps, tele_div, reduce, st, part, carry, true));
     }
     EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     // ranks back to the original vertex ids
@@ -364,6 +491,131 @@ extern "C" int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out,
         stats->residual = hst.residual;
         stats->dangling_mass = hst.dangling;
         EG_CUDA(cudaEventElapsedTime(&stats->ms, ctx->ev0, ctx->ev1));
+        stats->row_kernel_ms = 0.f;
+        int timed = graph || !g->m ? 0 : (o.iterations < EG_KEV ? o.iterations : EG_KEV);
+        if (timed > hst.iters) timed = hst.iters;  // converged launches return at once
+        for (int i = 0; i < timed; i++) {
+            float t = 0.f;
+            EG_CUDA(cudaEventElapsedTime(&t, ctx->evk[2 * i], ctx->evk[2 * i + 1]));
+            stats->row_kernel_ms += t / (float)timed;
+        }
+    }
+    return EG_OK;
+}
+
+static int pr_prepare(eg_graph *g) {
+    if (!(g->built & EG_LAYOUT_CSC) || !(g->built & EG_LAYOUT_CSR))
+        return eg_fail(EG_ENOTBUILT, "PageRank needs the CSC (in-lists) and CSR (out-degrees)");
+    EG_CUDA(cudaSetDevice(g->ctx->device));
+    EG_TRY(eg_build_relabeled_csc(g));
+    EG_TRY(eg_buf_ensure(g->ctx, g->pr_stats, 512));
+    return EG_OK;
+}
+
+extern "C" int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out, eg_pr_stats *stats) {
+    if (!g) return eg_fail(EG_EINVAL, "NULL graph");
+    eg_pr_opts o;
+    if (opts) o = *opts;
+    else eg_pr_opts_default(&o);
+    if (o.iterations < 0 || o.deg_multiplier == 0) return eg_fail(EG_EINVAL, "bad PageRank options");
+    EG_TRY(pr_prepare(g));
+    PprSeeds none;
+    memset(&none, 0, sizeof(none));
+    return pr_run(g, o, none, 0, rank_out, stats);
+}
+
+// ============================================================== autotuner
+extern "C" int eg_graph_set_row_schedule(eg_graph *g, int tile_entries, int entries_per_lane) {
+    if (!g) return eg_fail(EG_EINVAL, "NULL graph");
+    for (int c = 0; c < EG_ROW_CFGS; c++)
+        if (kRowTile[c] == tile_entries && kRowU[c] == entries_per_lane) {
+            g->row_cfg = c;
+            return EG_OK;
+        }
+    return eg_fail(EG_EINVAL, "no row schedule with %d entries per warp tile and %d per lane", tile_entries,
+                   entries_per_lane);
+}
+
+extern "C" int eg_graph_tune(eg_graph *g, eg_tune_result *out) {
+    if (!g) return eg_fail(EG_EINVAL, "NULL graph");
+    EG_TRY(pr_prepare(g));
+    eg_pr_opts o;
+    eg_pr_opts_default(&o);
+    o.iterations = 6;
+    PprSeeds none;
+    memset(&none, 0, sizeof(none));
+    eg_tune_result r;
+    memset(&r, 0, sizeof(r));
+    r.ncand = EG_ROW_CFGS;
+    int best = 0;
+    for (int c = 0; c < EG_ROW_CFGS; c++) {
+        g->row_cfg = c;
+        eg_pr_stats st;
+        EG_TRY(pr_run(g, o, none, 0, nullptr, &st));  // warm-up (caches, carries)
+        EG_TRY(pr_run(g, o, none, 0, nullptr, &st));
+        r.tile_entries[c] = kRowTile[c];
+        r.entries_per_lane[c] = kRowU[c];
+        r.ms[c] = st.row_kernel_ms;
+        if (st.row_kernel_ms < r.ms[best]) best = c;
+    }
+    g->row_cfg = best;
+    r.chosen = best;
+    if (out) *out = r;
+    return EG_OK;
+}
+
+extern "C" int eg_ppr(eg_graph *g, const uint32_t *seeds, uint32_t nseeds, const eg_ppr_opts *opts, float *rank_out,
+                      eg_ppr_stats *stats) {
+    if (!g || !seeds) return eg_fail(EG_EINVAL, "NULL argument");
+    if (nseeds < 1) return eg_fail(EG_EINVAL, "a query needs a seed");
+    eg_ppr_opts po;
+    if (opts) po = *opts;
+    else {
+        po.damping = 0.85f;
+        po.max_iters = 50;
+        for (int q = 0; q < 32; q++) po.tolerance[q] = 1e-6f;
+    }
+    if (po.max_iters < 1 || !(po.damping > 0.f && po.damping < 1.f)) return eg_fail(EG_EINVAL, "bad PPR options");
+    // distinct seeds with their multiplicity
+    PprSeeds ps;
+    memset(&ps, 0, sizeof(ps));
+    for (uint32_t i = 0; i < nseeds; i++) {
+        if (seeds[i] >= g->n) return eg_fail(EG_EINVAL, "seed %u >= n", seeds[i]);
+        uint32_t j = 0;
+        while (j < ps.count && ps.id[j] != seeds[i]) j++;
+        if (j == ps.count) {
+            if (ps.count == EG_PPR1_SEEDS) return eg_fail(EG_EINVAL, "at most %d distinct seeds", EG_PPR1_SEEDS);
+            ps.id[ps.count++] = seeds[i];
+        }
+        ps.mult[j] += 1.f;
+    }
+    EG_TRY(pr_prepare(g));
+    eg_ctx *ctx = g->ctx;
+    // seed ids into the relabelled order
+    uint32_t *d_ids = reinterpret_cast<uint32_t *>(static_cast<char *>(g->pr_stats.p) + 256);
+    uint32_t *h = (uint32_t *)ctx->h_pinned;
+    memcpy(h, ps.id, sizeof(ps.id));
+    EG_CUDA(cudaMemcpyAsync(d_ids, h, sizeof(ps.id), cudaMemcpyHostToDevice, ctx->stream));
+    k_map_ids<<<1, 32, 0, ctx->stream>>>(bp<uint32_t>(g->perm), d_ids, ps.count, d_ids + EG_PPR1_SEEDS);
+    EG_LAUNCHED(ctx);
+    EG_CUDA(cudaMemcpyAsync(h, d_ids + EG_PPR1_SEEDS, sizeof(ps.id), cudaMemcpyDeviceToHost, ctx->stream));
+    EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    memcpy(ps.id, h, ps.count * sizeof(uint32_t));
+    eg_pr_opts o;
+    eg_pr_opts_default(&o);
+    o.iterations = po.max_iters;
+    o.damping = po.damping;
+    o.swap = 1;
+    o.dangling = 1;  // the mass on out-degree-0 vertices returns to the seeds
+    o.tolerance = po.tolerance[0] > 0.f ? (double)po.tolerance[0] : 0.0;
+    eg_pr_stats s;
+    EG_TRY(pr_run(g, o, ps, nseeds, rank_out, &s));
+    if (stats) {
+        memset(stats, 0, sizeof(*stats));
+        stats->iterations[0] = s.iterations_run;
+        stats->residual[0] = s.residual;
+        stats->sweeps = s.iterations_run;
+        stats->ms = s.ms;
     }
     return EG_OK;
 }

@@ -21,6 +21,7 @@
 #include <deque>
 #include <vector>
 
+#include "eg_mspull.cuh"
 #include "eg_ppr.cuh"
 
 #define SV_INF 0xfffffffeu
@@ -61,24 +62,6 @@ __global__ void k_sv_bfs_admit(const uint32_t *roots, const uint32_t *slots, int
 
 // pull: OR the frontier words of the in-neighbours (early exit when every
 // missing slot is found)
-__global__ void __launch_bounds__(256) k_sv_bfs_pull(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
-                                                     uint32_t n, unsigned long long live,
-                                                     const unsigned long long *__restrict__ seen,
-                                                     const unsigned long long *__restrict__ front,
-                                                     unsigned long long *__restrict__ next) {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-        const unsigned long long need = live & ~seen[v];
-        unsigned long long acc = 0ull;
-        if (need) {
-            for (uint32_t p = ptr[v]; p < ptr[v + 1]; p++) {
-                acc |= __ldg(front + col[p]);
-                if ((acc & need) == need) break;
-            }
-        }
-        next[v] = acc & need;
-    }
-}
-
 __global__ void k_sv_front_queue(const unsigned long long *__restrict__ front, uint32_t n, uint32_t *queue,
                                  SvCounters *cnt) {
     const uint32_t lane = threadIdx.x & 31;
@@ -203,17 +186,7 @@ __global__ void k_sv_level_summary(const int32_t *__restrict__ row, uint32_t n, 
 }
 
 // ------------------------------------------------------------------ SSSP engine
-struct SvW {
-    int rule;
-    uint64_t seed;
-    uint32_t lo;
-    uint64_t span;
-    __device__ __forceinline__ uint32_t operator()(uint32_t u, uint32_t v) const {
-        if (rule == EG_W_REF) return (u % 10u) + (v % 10u);
-        if (rule == EG_W_UNIT) return 1u;
-        return lo + (uint32_t)(((eg_edge_hash(seed, u, v) >> 32) * span) >> 32);
-    }
-};
+using SvW = eg_wrule;  // integer rules only (the server keeps u32 distances)
 
 __global__ void k_sv_sssp_admit(const uint32_t *roots, const uint32_t *slots, int k, uint32_t *dist, uint32_t *act,
                                 uint32_t *inq, uint32_t *queue, SvCounters *cnt) {
@@ -232,8 +205,7 @@ __device__ __forceinline__ void sv_relax(uint32_t u, uint32_t v, uint32_t j, uin
                                          uint32_t *next_queue, SvCounters *cnt) {
     bool improved = false;
     if (on && v != u) {
-        const uint64_t nd64 = (uint64_t)du + w(u, v);
-        const uint32_t nd = nd64 < SV_INF ? (uint32_t)nd64 : SV_INF;
+        const uint32_t nd = w.extend(du, u, v);
         uint32_t *dp = dist + (uint64_t)v * SV_SSSP_SLOTS + s;
         if (nd < __ldcg(dp)) improved = nd < atomicMin(dp, nd);
     }
@@ -390,6 +362,11 @@ struct eg_server {
     double ppr_admit[SV_PPR_LANES], ppr_arrival[SV_PPR_LANES];
     eg_buf small;  // counters, admission lists, summaries (device)
     uint64_t ticks = 0;
+    // device time per engine step (events around each engine's launches)
+    cudaEvent_t ev[6] = {};
+    double eng_ms[3] = {0.0, 0.0, 0.0};
+    uint64_t eng_steps[3] = {0, 0, 0};
+    uint64_t admitted[3] = {0, 0, 0}, completed[3] = {0, 0, 0};
 };
 
 static uint32_t sv_blocks(eg_ctx *ctx, uint64_t threads) {
@@ -428,6 +405,9 @@ extern "C" int eg_serve_open(eg_graph *g, const eg_serve_opts *opts, eg_server *
     eg_serve_opts o;
     if (opts) o = *opts;
     else eg_serve_opts_default(&o);
+    if (o.weights.rule != EG_W_REF && o.weights.rule != EG_W_HASH && o.weights.rule != EG_W_UNIT)
+        return eg_fail(EG_EINVAL, "the server takes integer weight rules (EG_W_REF, EG_W_HASH, EG_W_UNIT)");
+    if (o.weights.rule == EG_W_HASH && o.weights.hi < o.weights.lo) return eg_fail(EG_EINVAL, "weight range hi < lo");
     eg_ctx *ctx = g->ctx;
     const uint32_t n = g->n;
     uint64_t sb, ss, sp;
@@ -541,6 +521,7 @@ static void sv_finish(eg_server *s, uint64_t id, int kind, double arrival, doubl
     r.iterations = iters;
     r.value = value;
     s->done.push_back(r);
+    s->completed[kind - 1]++;
 }
 
 // One scheduler tick.
@@ -640,8 +621,11 @@ extern "C" int eg_serve_step(eg_server *s, int *active_out) {
         EG_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(SvCounters), ctx->stream));
         const bool pull = (double)s->bfs_count + (double)s->bfs_fdeg > m / 20.0;
         if (pull) {
-            k_sv_bfs_pull<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), bp<uint32_t>(g->csc.col), n,
-                                                                     live, seen, front, next);
+            k_msp_light<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), bp<uint32_t>(g->csc.col),
+                                                                   n, live, seen, front, next, bbig, &bcnt->nbig);
+            EG_LAUNCHED(ctx);
+            k_msp_heavy<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
+                bp<uint32_t>(g->csc.ptr), bp<uint32_t>(g->csc.col), live, seen, front, next, bbig, &bcnt->nbig);
             EG_LAUNCHED(ctx);
         } else {
             k_sv_front_queue<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(front, n, bq, bcnt);

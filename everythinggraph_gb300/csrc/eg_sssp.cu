@@ -13,21 +13,9 @@
 
 #include "eg_internal.cuh"
 
-#define EG_SSSP_INF 0xfffffffeu
-
 namespace {
 
-struct WRule {
-    int rule;
-    uint64_t seed;
-    uint32_t lo;
-    uint64_t span;
-    __device__ __forceinline__ uint32_t operator()(uint32_t u, uint32_t v) const {
-        if (rule == EG_W_REF) return (u % 10u) + (v % 10u);
-        if (rule == EG_W_UNIT) return 1u;
-        return lo + (uint32_t)(((eg_edge_hash(seed, u, v) >> 32) * span) >> 32);
-    }
-};
+using WRule = eg_wrule;
 
 struct SsspCounters {
     unsigned long long relax;  // entries scanned
@@ -39,9 +27,10 @@ struct SsspCounters {
 // grid instead of one warp (RMAT hubs have 10^5..10^6 out-edges).
 #define EG_SSSP_BIG_DEG 2048u
 
-__global__ void k_sssp_init(uint32_t n, uint32_t *dist, uint32_t root, uint32_t *queue, SsspCounters *cnt) {
+__global__ void k_sssp_init(uint32_t n, uint32_t *dist, uint32_t root, uint32_t *queue, SsspCounters *cnt,
+                            uint32_t inf) {
     uint32_t stride = gridDim.x * blockDim.x;
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) dist[v] = v == root ? 0u : EG_SSSP_INF;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) dist[v] = v == root ? 0u : inf;
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         queue[0] = root;
         cnt->qsize = 1;
@@ -54,8 +43,7 @@ __global__ void k_sssp_init(uint32_t n, uint32_t *dist, uint32_t root, uint32_t 
 __device__ __forceinline__ bool sssp_relax(uint32_t u, uint32_t du, uint32_t v, const WRule &w, uint32_t *dist,
                                            uint32_t *next_bm) {
     if (v == u) return false;  // self-loops skipped (sssp_pushpull.c:80)
-    const uint64_t nd64 = (uint64_t)du + w(u, v);
-    const uint32_t nd = nd64 < EG_SSSP_INF ? (uint32_t)nd64 : EG_SSSP_INF;
+    const uint32_t nd = w.extend(du, u, v);
     if (nd >= __ldcg(dist + v)) return false;
     const uint32_t old = atomicMin(dist + v, nd);
     if (nd >= old) return false;
@@ -140,22 +128,14 @@ __global__ void k_clear_bits(const uint32_t *__restrict__ queue, uint32_t qlen, 
     }
 }
 
-__global__ void k_count_reached(const uint32_t *__restrict__ dist, uint64_t len, unsigned long long *out) {
+__global__ void k_count_reached(const uint32_t *__restrict__ dist, uint64_t len, unsigned long long *out,
+                                uint32_t inf) {
     unsigned long long c = 0;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < len; i += (uint64_t)gridDim.x * blockDim.x)
-        c += dist[i] != EG_SSSP_INF;
+        c += dist[i] != inf;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(EG_FULL_MASK, c, o);
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
-}
-
-WRule make_rule(const eg_weights *w) {
-    WRule r;
-    r.rule = w ? w->rule : EG_W_REF;
-    r.seed = w ? w->seed : 0;
-    r.lo = w ? w->lo : 0;
-    r.span = w ? (uint64_t)w->hi - w->lo + 1 : 1;
-    return r;
 }
 
 uint32_t blocks_for(eg_ctx *ctx, uint64_t threads) {
@@ -167,7 +147,7 @@ uint32_t blocks_for(eg_ctx *ctx, uint64_t threads) {
 
 int check_weights(const eg_weights *w) {
     if (!w) return EG_OK;
-    if (w->rule != EG_W_REF && w->rule != EG_W_HASH && w->rule != EG_W_UNIT)
+    if (w->rule != EG_W_REF && w->rule != EG_W_HASH && w->rule != EG_W_UNIT && w->rule != EG_W_HASH_F32)
         return eg_fail(EG_EINVAL, "unknown weight rule %d", w->rule);
     if (w->rule == EG_W_HASH && w->hi < w->lo) return eg_fail(EG_EINVAL, "weight range hi < lo");
     return EG_OK;
@@ -183,7 +163,7 @@ extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wts, uint32
     eg_ctx *ctx = g->ctx;
     EG_CUDA(cudaSetDevice(ctx->device));
     const uint32_t n = g->n, nw = (n + 31) >> 5;
-    const WRule w = make_rule(wts);
+    const WRule w = eg_make_wrule(wts);
     EG_TRY(eg_buf_ensure(ctx, g->dist, (uint64_t)n * 4));
     const uint64_t off_q0 = nw, off_q1 = off_q0 + n, off_big = off_q1 + n, off_cnt = (off_big + n + 7) & ~7ull;
     EG_TRY(eg_buf_ensure(ctx, g->sssp_work, (off_cnt + 8) * 4));
@@ -194,7 +174,7 @@ extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wts, uint32
     uint32_t *dist = bp<uint32_t>(g->dist);
     EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     EG_CUDA(cudaMemsetAsync(bm, 0, (uint64_t)nw * 4, ctx->stream));
-    k_sssp_init<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(n, dist, root, q[0], cnt);
+    k_sssp_init<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(n, dist, root, q[0], cnt, w.inf());
     EG_LAUNCHED(ctx);
     uint32_t qlen = 1;
     int cur = 0, rounds = 0;
@@ -227,7 +207,7 @@ extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wts, uint32
     unsigned long long *dcount = reinterpret_cast<unsigned long long *>(cnt) + 2;
     if (stats) {
         EG_CUDA(cudaMemsetAsync(dcount, 0, 8, ctx->stream));
-        k_count_reached<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(dist, n, dcount);
+        k_count_reached<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(dist, n, dcount, w.inf());
         EG_LAUNCHED(ctx);
         EG_CUDA(cudaMemcpyAsync(h, dcount, 8, cudaMemcpyDeviceToHost, ctx->stream));
     }
@@ -247,10 +227,11 @@ extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wts, uint32
 // one (frontier vertex, source word) and walks the vertex's out-list; its 32
 // lanes relax 32 sources of the same edge (coalesced 128-byte rows).
 namespace {
-__global__ void k_msssp_init(uint32_t n, int k, uint32_t kw, uint32_t *dist, uint32_t *act0, uint32_t *act1) {
+__global__ void k_msssp_init(uint32_t n, int k, uint32_t kw, uint32_t *dist, uint32_t *act0, uint32_t *act1,
+                             uint32_t inf) {
     uint64_t total = (uint64_t)n * k;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < total; i += (uint64_t)gridDim.x * blockDim.x)
-        dist[i] = EG_SSSP_INF;
+        dist[i] = inf;
     uint64_t tw = (uint64_t)n * kw;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < tw; i += (uint64_t)gridDim.x * blockDim.x) {
         act0[i] = 0;
@@ -276,8 +257,7 @@ __device__ __forceinline__ void msssp_edge(uint32_t u, uint32_t v, uint32_t j, u
                                            uint32_t *next_inq, uint32_t *next_queue, SsspCounters *cnt) {
     bool improved = false;
     if (on && v != u) {
-        const uint64_t nd64 = (uint64_t)du + w(u, v);
-        const uint32_t nd = nd64 < EG_SSSP_INF ? (uint32_t)nd64 : EG_SSSP_INF;
+        const uint32_t nd = w.extend(du, u, v);
         uint32_t *dp = dist + (uint64_t)v * k + s;
         if (nd < __ldcg(dp)) improved = nd < atomicMin(dp, nd);
     }
@@ -382,7 +362,7 @@ extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg
     eg_ctx *ctx = g->ctx;
     EG_CUDA(cudaSetDevice(ctx->device));
     const uint32_t n = g->n, nw = (n + 31) >> 5, kw = (uint32_t)((k + 31) / 32);
-    const WRule w = make_rule(wts);
+    const WRule w = eg_make_wrule(wts);
     // work: dist[n*k] | act0, act1 [n*kw] | inq0, inq1 [nw] | q0, q1 [n] | roots | counters
     if ((uint64_t)n * kw >= 0xffffffffull) return eg_fail(EG_EINVAL, "n * ceil(k/32) must be < 2^32");
     const uint64_t off_act0 = (uint64_t)n * k, off_act1 = off_act0 + (uint64_t)n * kw, off_inq0 = off_act1 + (uint64_t)n * kw,
@@ -396,7 +376,7 @@ extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg
     SsspCounters *h = (SsspCounters *)ctx->h_pinned;
     EG_CUDA(cudaMemcpyAsync(d_roots, roots, (uint64_t)k * 4, cudaMemcpyHostToDevice, ctx->stream));
     EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-    k_msssp_init<<<blocks_for(ctx, (uint64_t)n * k), 256, 0, ctx->stream>>>(n, k, kw, dist, act[0], act[1]);
+    k_msssp_init<<<blocks_for(ctx, (uint64_t)n * k), 256, 0, ctx->stream>>>(n, k, kw, dist, act[0], act[1], w.inf());
     EG_LAUNCHED(ctx);
     EG_CUDA(cudaMemsetAsync(inq[0], 0, 2ull * nw * 4, ctx->stream));
     EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(SsspCounters), ctx->stream));
@@ -441,7 +421,8 @@ extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg
     if (stats) {
         unsigned long long *dcount = reinterpret_cast<unsigned long long *>(cnt) + 2;
         EG_CUDA(cudaMemsetAsync(dcount, 0, 8, ctx->stream));
-        k_count_reached<<<blocks_for(ctx, (uint64_t)n * k), 256, 0, ctx->stream>>>(dist, (uint64_t)n * k, dcount);
+        k_count_reached<<<blocks_for(ctx, (uint64_t)n * k), 256, 0, ctx->stream>>>(dist, (uint64_t)n * k, dcount,
+                                                                                   w.inf());
         EG_LAUNCHED(ctx);
         EG_CUDA(cudaMemcpyAsync(h, dcount, 8, cudaMemcpyDeviceToHost, ctx->stream));
         EG_CUDA(cudaStreamSynchronize(ctx->stream));

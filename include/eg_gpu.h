@@ -146,9 +146,29 @@ typedef struct {
     double residual;      /* FP64 L1 change of the last iteration (if computed) */
     double dangling_mass; /* FP64 mass on out-degree-0 vertices, last iterate */
     float ms;             /* device time of the iterations */
+    float row_kernel_ms;  /* mean device time of one row-sum kernel launch (up to
+                             the first 8 iterations; 0 when use_graph) */
 } eg_pr_stats;
 void eg_pr_opts_default(eg_pr_opts *o);
 int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out, eg_pr_stats *stats);
+
+/* ---- row-kernel autotuner (no reference counterpart) ---------------------
+ * The PageRank/SpMV row kernel walks the CSC as warp tiles of 1024, 2048 or
+ * 4096 entries with 4 or 8 entries per lane.  eg_graph_tune times every
+ * schedule on this graph (two 6-iteration PageRank runs each, CUDA events
+ * around the row kernel) and keeps the fastest for eg_pagerank, eg_ppr and
+ * eg_spmv on this graph; eg_graph_set_row_schedule picks one by hand.  The
+ * default is 2048 x 4.  Schedules change only how rows are split between
+ * warps, i.e. the fp32 summation order. */
+typedef struct {
+    int ncand;
+    int chosen;               /* index of the schedule kept */
+    int tile_entries[8];
+    int entries_per_lane[8];
+    float ms[8];              /* mean row-kernel time per iteration */
+} eg_tune_result;
+int eg_graph_tune(eg_graph *g, eg_tune_result *out);
+int eg_graph_set_row_schedule(eg_graph *g, int tile_entries, int entries_per_lane);
 
 /* ---- SpMV (replaces spmv.c:98-135) ---------------------------------------
  * Row reductions over a built adjacency:
@@ -218,10 +238,16 @@ int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *levels_out,
  * UINT32_MAX-1 (sssp_pushpull.c:8).  Weight rules, computed from the edge's
  * endpoints like the reference's CREATE_WEIGHT path:
  *   EG_W_REF   src%10 + dst%10 (init_all.c:661-686)
- *   EG_W_HASH  lo + H(seed, min(u,v), max(u,v)) mod (hi-lo+1), symmetric */
+ *   EG_W_HASH  lo + H(seed, min(u,v), max(u,v)) mod (hi-lo+1), symmetric
+ *   EG_W_UNIT  1 (hop counts)
+ *   EG_W_HASH_F32  fp32 weights in (0,1]: ((H >> 40) + 1) / 2^24; the path
+ *              sums are rounded to fp32 like the reference's float add
+ *              (sssp_pushpull.c:81), and dist_out holds fp32 bit patterns
+ *              (unreached = +inf, 0x7f800000).  Not accepted by the server. */
 #define EG_W_REF 0
 #define EG_W_HASH 1
 #define EG_W_UNIT 2
+#define EG_W_HASH_F32 3
 typedef struct {
     int rule;
     uint64_t seed;
@@ -270,6 +296,13 @@ typedef struct {
 } eg_ppr_stats;
 int eg_ppr_multi(eg_graph *g, const uint32_t *seeds, const uint32_t *seed_offsets, int nq, const eg_ppr_opts *opts,
                  float *ranks_out, eg_ppr_stats *stats);
+/* One personalised PageRank query on the plain PageRank row kernel (the
+ * one-query-at-a-time path): the same iteration with the teleport and the
+ * dangling mass sent to at most 8 distinct seeds (repeats count with their
+ * multiplicity); stops on opts->tolerance[0] or max_iters.  Fills
+ * iterations[0], residual[0], sweeps and ms of the stats. */
+int eg_ppr(eg_graph *g, const uint32_t *seeds, uint32_t nseeds, const eg_ppr_opts *opts, float *rank_out,
+           eg_ppr_stats *stats);
 
 /* ---- query server (continuous batching) ----------------------------------
  * No counterpart in the reference (one algorithm per process).  A server

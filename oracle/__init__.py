@@ -228,6 +228,16 @@ def sssp(n, ptr, col, w, root):
     return dist
 
 
+def sssp_f32(n, ptr, col, w, root):
+    """fp32-weight SSSP; returns the fp32 distances (unreached = +inf)."""
+    w = np.ascontiguousarray(w, dtype=np.float32)
+    dist = np.empty(n, dtype=np.uint32)
+    rc = lib().or_sssp_f32(u32(n), _p(ptr), _p(col), _p(w), u32(root), _p(dist))
+    if rc != 0:
+        raise ValueError("root out of range")
+    return dist.view(np.float32)
+
+
 def wcc(n, pairs):
     pairs = np.ascontiguousarray(pairs, dtype=np.uint32)
     labels = np.empty(n, dtype=np.int64)
@@ -276,6 +286,15 @@ def hash_weights(u, v, seed, lo, hi):
     v = np.ascontiguousarray(v, dtype=np.uint32)
     out = np.empty(len(u), dtype=np.uint32)
     lib().or_hash_weights(u64(len(u)), _p(u), _p(v), u64(seed), u32(lo), u32(hi), _p(out))
+    return out
+
+
+def hash_weights_f32(u, v, seed):
+    """fp32 weights in (0, 1] hashed from each (u, v) endpoint pair."""
+    u = np.ascontiguousarray(u, dtype=np.uint32)
+    v = np.ascontiguousarray(v, dtype=np.uint32)
+    out = np.empty(len(u), dtype=np.float32)
+    lib().or_hash_weights_f32(u64(len(u)), _p(u), _p(v), u64(seed), _p(out))
     return out
 
 

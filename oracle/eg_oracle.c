@@ -481,6 +481,43 @@ int or_sssp(uint32_t n, const uint32_t *ptr, const uint32_t *col, const uint32_t
     return 0;
 }
 
+/* SSSP with fp32 weights and fp32 path sums (the reference's pull relax adds
+ * in float, sssp_pushpull.c:81): Dijkstra where extending a path rounds
+ * d[u] + w to fp32.  Rounded addition of w >= 0 is monotone and never
+ * decreases d, so Dijkstra and Bellman-Ford reach the same least fixed point.
+ * Distances are returned as fp32 bit patterns (unreached = +inf), which order
+ * like the floats for non-negative values. */
+int or_sssp_f32(uint32_t n, const uint32_t *ptr, const uint32_t *col, const float *w, uint32_t root,
+                uint32_t *dist_bits) {
+    if (root >= n) return -1;
+    uint64_t m = ptr[n];
+    or_hitem *h = (or_hitem *)malloc((size_t)(m + 1) * sizeof(or_hitem));
+    uint64_t sz = 0;
+    const uint32_t inf = 0x7f800000u;
+    for (uint32_t i = 0; i < n; i++) dist_bits[i] = inf;
+    dist_bits[root] = 0;
+    or_heap_push(h, &sz, (or_hitem){0, root});
+    while (sz) {
+        or_hitem it = or_heap_pop(h, &sz);
+        if (it.d != dist_bits[it.v]) continue;
+        float du;
+        memcpy(&du, &it.d, 4);
+        for (uint32_t p = ptr[it.v]; p < ptr[it.v + 1]; p++) {
+            uint32_t v = col[p];
+            if (v == it.v) continue;
+            float ndv = du + w[p];
+            uint32_t nb;
+            memcpy(&nb, &ndv, 4);
+            if (nb < dist_bits[v]) {
+                dist_bits[v] = nb;
+                or_heap_push(h, &sz, (or_hitem){nb, v});
+            }
+        }
+    }
+    free(h);
+    return 0;
+}
+
 /* WCC: min-label propagation (wcc.c:30-42 on -u adjacency lists, and the grid
  * and edge-array sweeps wcc.c:193-261 that relax both endpoints) converges to
  * the minimum vertex id of each weakly connected component.  Restated with
@@ -543,6 +580,12 @@ void or_hash_weights(uint64_t count, const uint32_t *u, const uint32_t *v, uint6
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < (int64_t)count; i++)
         out[i] = lo + (uint32_t)(((or_edge_hash(seed, u[i], v[i]) >> 32) * span) >> 32);
+}
+/* fp32 weights in (0, 1]: (top 24 hash bits + 1) / 2^24, exact in fp32. */
+void or_hash_weights_f32(uint64_t count, const uint32_t *u, const uint32_t *v, uint64_t seed, float *out) {
+#pragma omp parallel for schedule(static)
+    for (int64_t i = 0; i < (int64_t)count; i++)
+        out[i] = (float)((or_edge_hash(seed, u[i], v[i]) >> 40) + 1) * (1.0f / 16777216.0f);
 }
 void or_hash_values(uint64_t count, const uint32_t *u, const uint32_t *v, uint64_t seed, float *out) {
 #pragma omp parallel for schedule(static)

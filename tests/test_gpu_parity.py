@@ -142,6 +142,44 @@ def test_pagerank_vs_fp64(case):
             assert st.iterations_run == 10
 
 
+def test_pagerank_graph_replay_matches_stream(case):
+    # the captured iteration loop gives the same bits as the launched one,
+    # on a first capture, a replay, and a re-capture after the options change
+    name, n, pairs, rec, g, gu, adj, adju = case
+    for comp, dangling in ((False, False), (False, False), (True, True), (False, False)):
+        a, sa = g.pagerank(iterations=7, compensated=comp, dangling=dangling)
+        b, sb = g.pagerank(iterations=7, compensated=comp, dangling=dangling, use_graph=True)
+        np.testing.assert_array_equal(a, b)
+        assert sb.iterations_run == 7
+        assert sa.row_kernel_ms > 0 and sb.row_kernel_ms == 0
+
+
+def test_row_schedules_and_autotuner(case):
+    # every row-kernel schedule stays within the FP64 tolerance, for PageRank
+    # and the fp32 SpMV; the tuner keeps one of them
+    name, n, pairs, rec, g, gu, adj, adju = case
+    ref = oracle.pagerank_f64(adj, adj.out_deg(), 1.0 / n, 10, dangling=True)
+    x = oracle.uniform_f32(n, 11)
+    vals = oracle.hash_values(adj.in_col, adj.in_dst(), 9)
+    y_ref = oracle.spmv_f64(n, adj.in_ptr, adj.in_col, vals, x)
+    for tile, u in ((1024, 4), (2048, 4), (4096, 4), (2048, 8), (4096, 8)):
+        g.set_row_schedule(tile, u)
+        got, st = g.pagerank(iterations=10, dangling=True)
+        l1, mx = rel_errors(got, ref)
+        assert l1 <= PR_REL_L1 and mx <= PR_MAX_REL, (tile, u, l1, mx)
+        y, _ = g.spmv(x, "f32_comp", value_seed=9)
+        l1, mx = rel_errors(y, y_ref)
+        assert l1 <= PR_REL_L1, (tile, u, l1)
+    with pytest.raises(RuntimeError):
+        g.set_row_schedule(512, 4)
+    cands, chosen = g.tune()
+    assert len(cands) == 5 and 0 <= chosen < 5
+    if n > 1000:
+        assert all(ms > 0 for _, _, ms in cands)
+    assert cands[chosen][2] == min(ms for _, _, ms in cands)
+    g.set_row_schedule(2048, 4)
+
+
 def test_pagerank_tolerance_stops_early(case):
     name, n, pairs, rec, g, gu, adj, adju = case
     got, st = g.pagerank(iterations=200, tolerance=1e-6, dangling=True)
@@ -236,6 +274,25 @@ def test_sssp_hash_weights_and_batch(case):
         d1, _ = g.sssp(int(r), w)
         np.testing.assert_array_equal(d1, ref)
         np.testing.assert_array_equal(dm[s], ref)
+
+
+def test_sssp_f32_weights_bit_exact(case):
+    # fp32 weights in (0, 1] with fp32 path sums: the least fixed point is
+    # unique, so the GPU's relaxation order cannot change a bit
+    import everythinggraph_gb300 as eg
+    name, n, pairs, rec, g, gu, adj, adju = case
+    w = eg.weights("f32", seed=6)
+    wa = oracle.hash_weights_f32(adj.out_src(), adj.out_col, 6)
+    assert wa.min() > 0 and wa.max() <= 1
+    roots = oracle.sample_roots(adj.out_deg(), 5, 9)
+    dm, st = g.sssp_multi(roots, w)
+    assert dm.dtype == np.float32
+    for s, r in enumerate(roots):
+        ref = oracle.sssp_f32(n, adj.out_ptr, adj.out_col, wa, int(r))
+        d1, st1 = g.sssp(int(r), w)
+        np.testing.assert_array_equal(d1.view(np.uint32), ref.view(np.uint32))
+        np.testing.assert_array_equal(dm[s].view(np.uint32), ref.view(np.uint32))
+        assert st1.reached == int(np.isfinite(ref).sum())
 
 
 # ------------------------------------------------------------------ WCC
@@ -355,6 +412,25 @@ def test_ppr_batch_vs_fp64_and_alone(case):
         Ra, sta = g.ppr([seed_lists[q]], tolerance=[tols[q]], max_iters=50)
         np.testing.assert_array_equal(Ra[0].view(np.uint32), R[q].view(np.uint32))
         assert sta.iterations[0] == st.iterations[q]
+
+
+def test_ppr_single_query_path(case):
+    # the plain one-query path (PageRank row kernel with a seed teleport)
+    # against FP64, with repeated seeds counted by multiplicity
+    name, n, pairs, rec, g, gu, adj, adju = case
+    rng = np.random.default_rng(11)
+    nz = np.nonzero(adj.out_deg() > 0)[0]
+    for k, tol in ((1, 1e-4), (3, 1e-6), (8, 1e-7)):
+        seeds = rng.choice(nz, size=k).astype(np.uint32)
+        if k == 3:
+            seeds[2] = seeds[0]
+        ref, it_ref = oracle.ppr_f64(adj, adj.out_deg(), seeds, tol=tol, max_iters=50)
+        got, st = g.ppr_single(seeds, tolerance=tol, max_iters=50)
+        l1 = np.abs(got - ref).sum() / np.abs(ref).sum()
+        assert l1 <= 1e-5, (k, l1)
+        assert abs(st.iterations[0] - it_ref) <= 1, (k, st.iterations[0], it_ref)
+    with pytest.raises(RuntimeError):
+        g.ppr_single(np.arange(9, dtype=np.uint32))  # more than 8 distinct seeds
 
 
 # ------------------------------------------------------------------ query server

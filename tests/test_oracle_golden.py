@@ -92,6 +92,40 @@ def test_sssp(case):
         np.testing.assert_array_equal(d, rec["sssp_pull_p%d" % r])
 
 
+def test_sssp_f32(case):
+    # (1) with the reference's integer weights as floats the fp32 path sums are
+    # exact, so the fp32 Dijkstra must reproduce the reference's dumps (its pull
+    # relax adds in float); (2) with hashed fp32 weights it must equal an
+    # independent float32 Bellman-Ford fixed point
+    name, n, pairs, rec = case
+    adj = oracle.build_adj(n, pairs)
+    w = oracle.ref_weights(adj, "out").astype(np.float32)
+    for r in rec["roots"]:
+        d = oracle.sssp_f32(n, adj.out_ptr, adj.out_col, w, int(r))
+        ref = rec["sssp_pull_p%d" % r]
+        np.testing.assert_array_equal(np.isinf(d), ref == 0xFFFFFFFE)
+        np.testing.assert_array_equal(d[~np.isinf(d)], ref[ref != 0xFFFFFFFE].astype(np.float32))
+    if n > 5000:
+        return
+    wf = oracle.hash_weights_f32(adj.out_src(), adj.out_col, 6)
+    assert wf.min() > 0 and wf.max() <= 1
+    src, dst = adj.out_src(), adj.out_col
+    keep = src != dst
+    src, dst, wf = src[keep], dst[keep], wf[keep]
+    for r in rec["roots"]:
+        d = np.full(n, np.inf, dtype=np.float32)
+        d[int(r)] = 0
+        while True:
+            cand = (d[src] + wf).astype(np.float32)
+            nd = d.copy()
+            np.minimum.at(nd, dst, cand)
+            if np.array_equal(nd, d):
+                break
+            d = nd
+        got = oracle.sssp_f32(n, adj.out_ptr, adj.out_col, oracle.hash_weights_f32(adj.out_src(), adj.out_col, 6), int(r))
+        np.testing.assert_array_equal(got.view(np.uint32), d.view(np.uint32))
+
+
 def test_wcc(case):
     name, n, pairs, rec = case
     lab = oracle.wcc(n, pairs)
