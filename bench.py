@@ -367,6 +367,7 @@ def serve_report(ctx, eg, scale, rate, nq, seed=7, plain_sample=40, g=None):
         if active == 0 and i < nq:  # idle: wait for the next arrival
             time.sleep(max(0.0, min(0.001, arrivals[i] - srv.info()["clock_s"])))
     info = srv.info()
+    info["stats"] = srv.stats()
     srv.close()
     lat = np.array([r.done_s - r.arrival_s for r in done]) * 1e3
     span = max(r.done_s for r in done) - arrivals[0]

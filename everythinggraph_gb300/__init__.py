@@ -10,6 +10,7 @@ tests and the benchmark.  Every call runs CUDA kernels; there is no CPU path.
     rank, st = g.pagerank(iterations=10)
 """
 import ctypes
+import weakref
 
 import numpy as np
 
@@ -44,11 +45,23 @@ class Context:
 
     def __init__(self, device=0, hbm_budget=0):
         self._h = ctypes.c_void_p()
+        self._children = weakref.WeakSet()  # graphs and servers, freed before the context
         L.check(lib().eg_open(device, hbm_budget, ctypes.byref(self._h)))
+
+    def _adopt(self, obj):
+        self._children.add(obj)
+        return obj
 
     def close(self):
         if self._h:
-            lib().eg_close(self._h)
+            kids = list(self._children)
+            for k in kids:
+                if isinstance(k, Server):
+                    k.close()
+            for k in kids:
+                if isinstance(k, Graph):
+                    k.free()
+            L.check(lib().eg_close(self._h))
             self._h = ctypes.c_void_p()
 
     def __del__(self):
@@ -85,9 +98,12 @@ class Context:
                                                  UNDIRECTED if undirected else 0, ctypes.byref(h)))
         return Graph(self, h)
 
-    def from_file(self, path, n, undirected=False):
+    def from_file(self, path, n, undirected=False, weighted=False):
+        """Binary [src][dst] u32 records, or 12-byte [src][dst][f32 weight]
+        records with weighted=True (-w; the weights are skipped)."""
         h = ctypes.c_void_p()
-        L.check(lib().eg_graph_from_file(self._h, path.encode(), n, UNDIRECTED if undirected else 0, ctypes.byref(h)))
+        flags = (UNDIRECTED if undirected else 0) | (L.EG_WEIGHTED_FILE if weighted else 0)
+        L.check(lib().eg_graph_from_file(self._h, path.encode(), n, flags, ctypes.byref(h)))
         return Graph(self, h)
 
     def rmat(self, scale, m, seed, undirected=False):
@@ -106,6 +122,7 @@ class Graph:
     def __init__(self, ctx, h):
         self.ctx = ctx
         self._h = h
+        ctx._adopt(self)
 
     def free(self):
         if self._h:
@@ -293,6 +310,7 @@ class Server:
             o.weights = weights_
         self._h = ctypes.c_void_p()
         L.check(lib().eg_serve_open(graph._h, ctypes.byref(o), ctypes.byref(self._h)))
+        graph.ctx._adopt(self)
 
     def close(self):
         if self._h:
@@ -333,6 +351,14 @@ class Server:
         out = np.empty(n, dtype=np.uint32)
         L.check(lib().eg_serve_take_result(self._h, _ptr(out), n))
         return out
+
+    def stats(self):
+        st = L.ServeStats()
+        L.check(lib().eg_serve_stats(self._h, ctypes.byref(st)))
+        names = ("bfs", "sssp", "ppr")
+        return {"ticks": st.ticks, "queued": st.queued,
+                "engines": {names[e]: {"device_ms": st.engine_ms[e], "steps": st.engine_steps[e],
+                                       "admitted": st.admitted[e], "completed": st.completed[e]} for e in range(3)}}
 
     def info(self):
         b, s_, p, t = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_double()

@@ -21,6 +21,7 @@ EG_DEV_RANK, EG_DEV_LEVEL, EG_DEV_PARENT, EG_DEV_DIST, EG_DEV_LABEL, EG_DEV_SPMV
 EG_SPMV_U32_PULL, EG_SPMV_U32_PUSH, EG_SPMV_U32_EDGE, EG_SPMV_F32, EG_SPMV_F32_COMP, EG_SPMV_F64 = 0, 1, 2, 3, 4, 5
 EG_BFS_AUTO, EG_BFS_PUSH_ONLY, EG_BFS_PULL_ONLY = 0, 1, 2
 EG_W_REF, EG_W_HASH, EG_W_UNIT, EG_W_HASH_F32 = 0, 1, 2, 3
+EG_WEIGHTED_FILE = 2
 EG_Q_BFS, EG_Q_SSSP, EG_Q_PPR = 1, 2, 3
 
 
@@ -38,6 +39,11 @@ class PrOpts(ctypes.Structure):
 class PrStats(ctypes.Structure):
     _fields_ = [("iterations_run", c_int), ("residual", c_f64), ("dangling_mass", c_f64), ("ms", c_f32),
                 ("row_kernel_ms", c_f32)]
+
+
+class ServeStats(ctypes.Structure):
+    _fields_ = [("ticks", c_u64), ("queued", c_u64), ("engine_ms", c_f64 * 3), ("engine_steps", c_u64 * 3),
+                ("admitted", c_u64 * 3), ("completed", c_u64 * 3)]
 
 
 class TuneResult(ctypes.Structure):
@@ -132,6 +138,7 @@ SIGNATURES = {
     "eg_graph_set_row_schedule": (c_int, [c_void_p, c_int, c_int]),
     "eg_ppr": (c_int, [c_void_p, c_void_p, c_u32, P(PprOpts), c_void_p, P(PprStats)]),
     "eg_serve_opts_default": (None, [P(ServeOpts)]),
+    "eg_serve_stats": (c_int, [c_void_p, P(ServeStats)]),
     "eg_serve_open": (c_int, [c_void_p, P(ServeOpts), P(c_void_p)]),
     "eg_serve_submit": (c_int, [c_void_p, P(Query), P(c_u64)]),
     "eg_serve_step": (c_int, [c_void_p, P(c_int)]),

@@ -50,6 +50,7 @@ extern "C" int eg_open(int device, uint64_t hbm_budget_bytes, eg_ctx **out) {
 
 extern "C" int eg_close(eg_ctx *c) {
     if (!c) return EG_OK;
+    if (c->live_graphs > 0) return eg_fail(EG_EINVAL, "eg_close: %d graphs are still open", c->live_graphs);
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     cudaEventDestroy(c->ev0);
@@ -152,6 +153,7 @@ static int graph_alloc(eg_ctx *ctx, uint64_t m, uint32_t n, unsigned flags, eg_g
     if (n == 0xffffffffu) return eg_fail(EG_EINVAL, "n must be < 2^32-1");
     eg_graph *g = new eg_graph();
     g->ctx = ctx;
+    ctx->live_graphs++;
     g->n = n;
     g->m_in = m;
     g->m = M;
@@ -160,6 +162,7 @@ static int graph_alloc(eg_ctx *ctx, uint64_t m, uint32_t n, unsigned flags, eg_g
     g->grid_p = 0;
     int rc = eg_buf_ensure(ctx, g->pairs, 2 * m * sizeof(uint32_t));
     if (rc != EG_OK) {
+        ctx->live_graphs--;
         delete g;
         return rc;
     }
@@ -202,29 +205,37 @@ extern "C" int eg_graph_from_file(eg_ctx *ctx, const char *path, uint32_t n, uns
         fclose(f);
         return eg_fail(EG_EIO, "cannot stat %s", path);
     }
-    if (sb.st_size % 8 != 0) {
+    const uint64_t rec = (flags & EG_WEIGHTED_FILE) ? 12 : 8;  // bytes per record
+    if ((uint64_t)sb.st_size % rec != 0) {
         fclose(f);
-        return eg_fail(EG_EIO, "%s: size %lld is not a multiple of 8 bytes", path, (long long)sb.st_size);
+        return eg_fail(EG_EIO, "%s: size %lld is not a multiple of %d bytes", path, (long long)sb.st_size, (int)rec);
     }
-    uint64_t m = (uint64_t)sb.st_size / 8;
+    uint64_t m = (uint64_t)sb.st_size / rec;
     int rc = graph_alloc(ctx, m, n, flags, out);
     if (rc != EG_OK) {
         fclose(f);
         return rc;
     }
     eg_graph *g = *out;
-    // stream the file through pinned staging in 1 MiB pieces
-    uint64_t done = 0, total = (uint64_t)sb.st_size;
-    while (done < total) {
-        size_t want = (size_t)((total - done) < (1u << 20) ? (total - done) : (1u << 20));
-        size_t got = fread(ctx->h_pinned, 1, want, f);
-        if (got != want) {
+    // stream the file through the 1 MiB pinned staging; 12-byte records are
+    // compacted to [src][dst] pairs in place (pair i lands at 8i <= 12i)
+    const uint64_t per = (1u << 20) / rec;  // records per piece
+    uint64_t done = 0;
+    while (done < m) {
+        const uint64_t cnt = m - done < per ? m - done : per;
+        const size_t got = fread(ctx->h_pinned, 1, (size_t)(cnt * rec), f);
+        if (got != cnt * rec) {
             fclose(f);
             eg_graph_free(g);
             *out = nullptr;
             return eg_fail(EG_EIO, "%s: short read", path);
         }
-        cudaError_t e = cudaMemcpyAsync((char *)g->pairs.p + done, ctx->h_pinned, got, cudaMemcpyHostToDevice, ctx->stream);
+        if (rec == 12) {
+            unsigned char *b = (unsigned char *)ctx->h_pinned;
+            for (uint64_t i = 0; i < cnt; i++) memmove(b + 8 * i, b + 12 * i, 8);
+        }
+        cudaError_t e = cudaMemcpyAsync((char *)g->pairs.p + done * 8, ctx->h_pinned, cnt * 8, cudaMemcpyHostToDevice,
+                                        ctx->stream);
         if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
         if (e != cudaSuccess) {
             fclose(f);
@@ -232,7 +243,7 @@ extern "C" int eg_graph_from_file(eg_ctx *ctx, const char *path, uint32_t n, uns
             *out = nullptr;
             return eg_fail(EG_ECUDA, "file H2D: %s", cudaGetErrorString(e));
         }
-        done += got;
+        done += cnt;
     }
     fclose(f);
     return EG_OK;
@@ -278,8 +289,8 @@ extern "C" void eg_graph_free(eg_graph *g) {
                       &g->csr.rid,      &g->csc.rid,     &g->csc_p.ptr,      &g->csc_p.col,    &g->csc_p.rid,
                       &g->perm,         &g->deg_p,
                       &g->out_deg,      &g->in_deg,      &g->cell_ptr,       &g->gsrc,         &g->gdst,
-                      &g->sched_csc.coord, &g->sched_csr.coord, &g->rank,    &g->contrib0,     &g->contrib1,
-                      &g->pr_part,      &g->pr_stats,    &g->mp_carry,    &g->errflag,     &g->rank_p,    &g->level,          &g->parent,       &g->dist,
+                      &g->rank,    &g->contrib0,     &g->contrib1,
+                      &g->pr_part,      &g->pr_stats,    &g->mp_carry,    &g->errflag,     &g->rank_p,    &g->rank_q,    &g->level,          &g->parent,       &g->dist,
                       &g->label,        &g->spmv_x,      &g->spmv_y,      &g->spmv_vals,      &g->bfs_work,     &g->msbfs_work,
                       &g->sssp_work,    &g->ppr_work};
     for (eg_buf *b : bufs) eg_buf_free(c, *b);
@@ -289,6 +300,7 @@ extern "C" void eg_graph_free(eg_graph *g) {
     }
     if (g->prg.exec) cudaGraphExecDestroy(g->prg.exec);
     if (g->prg.graph) cudaGraphDestroy(g->prg.graph);
+    c->live_graphs--;
     delete g;
 }
 

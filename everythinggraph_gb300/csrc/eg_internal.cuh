@@ -47,6 +47,7 @@ struct eg_ctx {
     void *h_pinned;  // 1 MiB pinned staging for small readbacks
     cudaEvent_t ev0, ev1;
     cudaEvent_t evk[2 * EG_KEV];  // begin/end pairs around single kernel launches
+    int live_graphs;              // eg_close refuses while graphs are alive
 };
 
 int eg_dmalloc(eg_ctx *ctx, void **p, uint64_t bytes);
@@ -71,12 +72,6 @@ struct eg_adj {
     eg_buf rid;  // uint32[m]: row of each entry (COO form), kept from the sort
 };
 
-// Merge-path schedule of one adjacency for one tile width.
-struct eg_mp_sched {
-    uint32_t items = 0;   // merge items per tile (threads * items per thread)
-    uint32_t ntiles = 0;  // tiles
-    eg_buf coord;         // uint2[ntiles+1]: (row, edge) at each tile start
-};
 
 // A BFS level loop captured as a CUDA graph with a device-side while node,
 // valid while the buffers it was captured with (key) stay in place.
@@ -105,10 +100,8 @@ struct eg_graph {
     // grid
     uint32_t grid_p;
     eg_buf cell_ptr, gsrc, gdst;
-    // schedules (CSC rows for PR/SpMV pull, CSR rows for push)
-    eg_mp_sched sched_csc, sched_csr;
     // algorithm state, allocated on first use and reused
-    eg_buf rank, rank_p, contrib0, contrib1, pr_part, pr_stats, mp_carry, errflag;
+    eg_buf rank, rank_p, rank_q, contrib0, contrib1, pr_part, pr_stats, mp_carry, errflag;
     eg_buf level, parent, dist, label, spmv_x, spmv_y, spmv_vals;
     uint64_t spmv_vals_seed;
     int spmv_vals_kind;
@@ -134,7 +127,6 @@ int eg_histogram(eg_ctx *ctx, const uint32_t *keys, uint64_t len, uint32_t *hist
 // Sorted data ends in (k_out, v_out); the input arrays are overwritten.
 int eg_radix_sort(eg_ctx *ctx, uint32_t *k_in, uint32_t *v_in, uint32_t *k_tmp, uint32_t *v_tmp, uint64_t len,
                   int bits, uint32_t **k_out, uint32_t **v_out);
-int eg_build_sched(eg_graph *g, eg_adj &adj, eg_mp_sched &s, uint32_t items);
 // builds g->csc_p / perm / deg_p from the CSC and out-degrees (once)
 int eg_build_relabeled_csc(eg_graph *g);
 
@@ -170,6 +162,29 @@ __host__ __device__ __forceinline__ uint64_t eg_edge_hash(uint64_t seed, uint32_
     return eg_draw(eg_key(seed, ((uint64_t)a << 32) | b), 0);
 }
 
+// Two running sums (e.g. a residual and a dangling mass) kept by one thread
+// as fp32 (sum, error) pairs (Knuth's TwoSum) and widened to FP64 once per
+// thread before the FP64 block reduction.  FP64 instructions issue at a small
+// fraction of the fp32 rate on this GPU, and per-row sums often run in
+// divergent code (one lane per finished row), so per-row FP64 adds would
+// dominate the kernels that carry them.
+struct eg_red2 {
+    float s0 = 0.f, c0 = 0.f, s1 = 0.f, c1 = 0.f;
+    __device__ __forceinline__ static void two_sum(float &s, float &c, float x) {
+        const float t = s + x;
+        const float bp = t - s;
+        c += (s - (t - bp)) + (x - bp);
+        s = t;
+    }
+    __device__ __forceinline__ void add(float2 d) {
+        two_sum(s0, c0, d.x);
+        two_sum(s1, c1, d.y);
+    }
+    __device__ __forceinline__ double2 wide() const {
+        return make_double2((double)s0 + (double)c0, (double)s1 + (double)c1);
+    }
+};
+
 // SSSP edge weights computed from the endpoints (no weight array), and the
 // extension of a path distance by one edge in the rule's encoding: u32 sums
 // saturating at EG_SSSP_INF, or fp32 sums (bit patterns, which order like
@@ -184,18 +199,21 @@ struct eg_wrule {
     __host__ __device__ __forceinline__ uint32_t inf() const {
         return rule == EG_W_HASH_F32 ? EG_SSSP_INF_F32 : EG_SSSP_INF;
     }
-    __device__ __forceinline__ uint32_t extend(uint32_t du, uint32_t u, uint32_t v) const {
-        if (rule == EG_W_HASH_F32) {
-            const float w = (float)((eg_edge_hash(seed, u, v) >> 40) + 1) * (1.0f / 16777216.0f);
-            return __float_as_uint(__fadd_rn(__uint_as_float(du), w));
-        }
-        uint32_t w;
-        if (rule == EG_W_REF) w = (u % 10u) + (v % 10u);
-        else if (rule == EG_W_UNIT) w = 1u;
-        else w = lo + (uint32_t)(((eg_edge_hash(seed, u, v) >> 32) * span) >> 32);
+    // the edge's weight in the rule's encoding (fp32 bits for EG_W_HASH_F32)
+    __device__ __forceinline__ uint32_t weight(uint32_t u, uint32_t v) const {
+        if (rule == EG_W_HASH_F32)
+            return __float_as_uint((float)((eg_edge_hash(seed, u, v) >> 40) + 1) * (1.0f / 16777216.0f));
+        if (rule == EG_W_REF) return (u % 10u) + (v % 10u);
+        if (rule == EG_W_UNIT) return 1u;
+        return lo + (uint32_t)(((eg_edge_hash(seed, u, v) >> 32) * span) >> 32);
+    }
+    // path distance du extended by an edge of weight w
+    __device__ __forceinline__ uint32_t add(uint32_t du, uint32_t w) const {
+        if (rule == EG_W_HASH_F32) return __float_as_uint(__fadd_rn(__uint_as_float(du), __uint_as_float(w)));
         const uint64_t nd = (uint64_t)du + w;
         return nd < EG_SSSP_INF ? (uint32_t)nd : EG_SSSP_INF;
     }
+    __device__ __forceinline__ uint32_t extend(uint32_t du, uint32_t u, uint32_t v) const { return add(du, weight(u, v)); }
 };
 static inline eg_wrule eg_make_wrule(const eg_weights *w) {
     eg_wrule r;

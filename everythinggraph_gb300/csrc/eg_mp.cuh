@@ -18,8 +18,10 @@
 // The Op supplies: value type V, accumulator A,
 //   V gather(j, u)            value of entry j whose column is u
 //   A zero(), A add(A, V), A merge(A left, A right)
-//   R emit(row, A)            finishes a row; R (double2) is folded into a
-//                             per-CTA FP64 reduction when REDUCE is set
+//   float2 emit(row, A)       finishes a row; the two partials it returns
+//                             (PageRank: |change|, dangling mass) are summed
+//                             per thread as fp32 TwoSum pairs (eg_red2), then
+//                             per CTA in FP64, when REDUCE is set
 #pragma once
 #include "eg_internal.cuh"
 
@@ -215,16 +217,14 @@ __global__ void __launch_bounds__(T) k_mp_rows(const uint32_t *__restrict__ ptr,
         if (s_head != EG_MP_NONE) carry[c].head_val = s_headval;
     }
     // write out completed rows in order
-    double2 red = make_double2(0.0, 0.0);
+    eg_red2 redf;
     const uint32_t r0 = (s_head != EG_MP_NONE) ? 1u : 0u;
     for (uint32_t r = r0 + tid; r < nrows; r += T) {
-        double2 x = op.emit(i0 + r, s_sum[r]);
-        if (REDUCE) {
-            red.x += x.x;
-            red.y += x.y;
-        }
+        const float2 x = op.emit(i0 + r, s_sum[r]);
+        if (REDUCE) redf.add(x);
     }
     if (REDUCE) {
+        double2 red = redf.wide();
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             red.x += __shfl_down_sync(EG_FULL_MASK, red.x, o);
@@ -255,7 +255,7 @@ __global__ void k_mp_fixup(const uint32_t *__restrict__ ptr, const uint2 *__rest
     op.setup();
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    double2 red = make_double2(0.0, 0.0);
+    eg_red2 redf;
     if (c < ntiles) {
         const uint32_t row = carry[c].head_row;
         if (row != EG_MP_NONE) {
@@ -278,11 +278,11 @@ __global__ void k_mp_fixup(const uint32_t *__restrict__ ptr, const uint2 *__rest
                 tot = op.merge(x, tot);
                 if (stop_mask) break;
             }
-            if (lane == 0) red = op.emit(row, tot);
+            if (lane == 0) redf.add(op.emit(row, tot));
         }
     }
     if (REDUCE) {
-        if (lane == 0) s_red[threadIdx.x >> 5] = red;
+        if (lane == 0) s_red[threadIdx.x >> 5] = redf.wide();
         __syncthreads();
         if (threadIdx.x == 0) {
             double2 s = make_double2(0.0, 0.0);
@@ -310,387 +310,12 @@ struct eg_f2sum {
     }
 };
 
-// ============================================================== TMA-staged variant
-// Persistent CTAs walk tiles c = blockIdx.x, blockIdx.x + gridDim.x, ...  One
-// thread stages the next tile's row ends and column indices into shared
-// memory with cp.async.bulk (TMA, completion on an mbarrier) while the CTA
-// works on the current tile (double buffer).  Each thread then reads its own
-// entries' columns from shared memory and gathers their values straight into
-// registers (all gathers of a thread in flight together), walks its IPT items,
-// and the carries are joined as in k_mp_rows.  Every mbarrier wait is
-// bounded: on timeout the CTA raises *err and stops.
-#define EG_MPP_SPIN_LIMIT (1u << 24)
-
-__device__ __forceinline__ uint32_t eg_smem_addr(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-__device__ __forceinline__ void eg_mbar_init(uint64_t *bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(eg_smem_addr(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void eg_fence_mbar_init() {
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void eg_fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
-__device__ __forceinline__ void eg_mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(eg_smem_addr(bar)), "r"(bytes)
-                 : "memory");
-}
-// 1-D bulk copy global -> shared; dst, src 16-byte aligned, bytes % 16 == 0.
-__device__ __forceinline__ void eg_bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-            eg_smem_addr(dst)),
-        "l"(src), "r"(bytes), "r"(eg_smem_addr(bar))
-        : "memory");
-}
-// Bounded wait for the phase `parity` of an mbarrier; false on timeout.
-__device__ __forceinline__ bool eg_mbar_wait(uint64_t *bar, uint32_t parity) {
-    const uint32_t a = eg_smem_addr(bar);
-    for (uint32_t i = 0; i < EG_MPP_SPIN_LIMIT; i++) {
-        uint32_t done;
-        asm volatile(
-            "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-            "selp.u32 %0, 1, 0, p;\n\t}"
-            : "=r"(done)
-            : "r"(a), "r"(parity)
-            : "memory");
-        if (done) return true;
-    }
-    return false;
-}
-
-template <int T, int IPT, class A>
-struct eg_mpp_smem {
-    static constexpr int W = T * IPT;
-    static constexpr int SLOT = W + 8;  // aligned slices take at most W + 7 words
-    static constexpr size_t re_off = 0;                                   // 2 x SLOT u32
-    static constexpr size_t col_off = re_off + 2 * SLOT * 4;              // 2 x SLOT u32
-    static constexpr size_t sum_off = (col_off + 2 * SLOT * 4 + 15) & ~(size_t)15;
-    static constexpr size_t cval_off = (sum_off + W * sizeof(A) + 15) & ~(size_t)15;
-    static constexpr size_t crow_off = (cval_off + T * sizeof(A) + 15) & ~(size_t)15;
-    static constexpr size_t bytes = (crow_off + T * 4 + 15) & ~(size_t)15;
-};
-
-// Issues the bulk copies of tile c into stage buffers (row ends of rows
-// i0..i0+nrows, i.e. ptr[i0+1 .. i0+nrows+1], and col[j0 .. j1)), widened
-// to 16-byte boundaries; the arrays are padded past their ends.
-__device__ __forceinline__ void eg_mpp_issue(const uint32_t *ptr, const uint32_t *col, const uint2 *coord, uint32_t c,
-                                             uint32_t *re_buf, uint32_t *col_buf, uint64_t *bar) {
-    const uint2 c0 = coord[c], c1 = coord[c + 1];
-    const uint32_t ra = (c0.x + 1) & ~3u, rb = (c1.x + 2 + 3) & ~3u;
-    const uint32_t ca = c0.y & ~3u, cb = (c1.y + 3) & ~3u;
-    const uint32_t rbytes = (rb - ra) * 4, cbytes = (cb - ca) * 4;
-    eg_mbar_expect_tx(bar, rbytes + cbytes);
-    eg_bulk_g2s(re_buf, ptr + ra, rbytes, bar);
-    if (cbytes) eg_bulk_g2s(col_buf, col + ca, cbytes, bar);
-}
-
-template <class Op, int T, int IPT, bool REDUCE>
-__global__ void __launch_bounds__(T) k_mpp_rows(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
-                                                uint32_t n, const uint2 *__restrict__ coord, uint32_t ntiles,
-                                                eg_mp_carry<typename Op::A> *__restrict__ carry,
-                                                double2 *__restrict__ part, int *err, Op op) {
-    using V = typename Op::V;
-    using A = typename Op::A;
-    using L = eg_mpp_smem<T, IPT, A>;
-    extern __shared__ __align__(16) unsigned char smem[];
-    uint32_t *s_re = (uint32_t *)(smem + L::re_off);
-    uint32_t *s_col = (uint32_t *)(smem + L::col_off);
-    A *s_sum = (A *)(smem + L::sum_off);
-    A *s_cval = (A *)(smem + L::cval_off);
-    uint32_t *s_crow = (uint32_t *)(smem + L::crow_off);
-    __shared__ __align__(8) uint64_t s_bar[2];
-    __shared__ uint32_t s_head;
-    __shared__ A s_headval;
-    __shared__ uint32_t s_wkey[T / 32], s_wfirst[T / 32];
-    __shared__ A s_wval[T / 32];
-    __shared__ double2 s_red[T / 32];
-
-    if (!op.active()) return;
-    op.setup();
-    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-    if (tid == 0) {
-        eg_mbar_init(&s_bar[0], 1);
-        eg_mbar_init(&s_bar[1], 1);
-        eg_fence_mbar_init();
-    }
-    __syncthreads();
-    uint32_t c = blockIdx.x;
-    if (tid == 0 && c < ntiles) eg_mpp_issue(ptr, col, coord, c, s_re, s_col, &s_bar[0]);
-    double2 red = make_double2(0.0, 0.0);
-    uint32_t phases = 0;  // bit s: parity of stage s's next completion
-    int stage = 0;
-    for (; c < ntiles; c += gridDim.x) {
-        // next tile's copy goes into the other stage (released by the
-        // __syncthreads that ended the previous iteration)
-        const uint32_t cn = c + gridDim.x;
-        if (tid == 0 && cn < ntiles) {
-            eg_fence_proxy_async();
-            eg_mpp_issue(ptr, col, coord, cn, s_re + (stage ^ 1) * L::SLOT, s_col + (stage ^ 1) * L::SLOT,
-                         &s_bar[stage ^ 1]);
-        }
-        const uint2 c0 = coord[c], c1 = coord[c + 1];
-        const uint32_t i0 = c0.x, j0 = c0.y;
-        const uint32_t nrows = c1.x - i0, nedges = c1.y - j0;
-        const uint32_t rs0 = __ldg(ptr + i0);
-        const uint32_t roff = (i0 + 1) - ((i0 + 1) & ~3u);  // s_re index of row i0's end
-        const uint32_t coff = j0 & 3u;                       // s_col index of entry j0
-        const bool ok = eg_mbar_wait(&s_bar[stage], (phases >> stage) & 1u);
-        if (__syncthreads_or(!ok)) {
-            if (tid == 0) {
-                atomicExch(err, 1);
-                // let a copy already issued into the other stage land first
-                if (cn < ntiles) eg_mbar_wait(&s_bar[stage ^ 1], (phases >> (stage ^ 1)) & 1u);
-            }
-            return;
-        }
-        phases ^= 1u << stage;
-        const uint32_t *re = s_re + stage * L::SLOT + roff;
-        const uint32_t *cl = s_col + stage * L::SLOT + coff;
-        // relative row end of local row r (the open row past the last vertex never ends)
-        auto rowend = [&](uint32_t r) -> uint32_t { return (i0 + r < n) ? re[r] - j0 : 0xffffffffu; };
-        if (tid == 0) s_head = EG_MP_NONE;
-
-        const uint32_t total = nrows + nedges;
-        const uint32_t d0 = min(tid * IPT, total), d1 = min(d0 + IPT, total);
-        // merge-path searches for this thread's first and one-past-last item
-        uint32_t lo = d0 > nedges ? d0 - nedges : 0, hi = min(d0, nrows);
-        while (lo < hi) {
-            const uint32_t mid = (lo + hi) >> 1;
-            if (rowend(mid) <= d0 - mid - 1) lo = mid + 1;
-            else hi = mid;
-        }
-        uint32_t it = lo, jt = d0 - lo;
-        uint32_t lo2 = d1 > nedges ? d1 - nedges : 0, hi2 = min(d1, nrows);
-        while (lo2 < hi2) {
-            const uint32_t mid = (lo2 + hi2) >> 1;
-            if (rowend(mid) <= d1 - mid - 1) lo2 = mid + 1;
-            else hi2 = mid;
-        }
-        const uint32_t ne = (d1 - lo2) - jt;  // entries among this thread's items
-        // gather this thread's entries into registers, all loads in flight
-        V v[IPT];
-#pragma unroll
-        for (int k = 0; k < IPT; k++) v[k] = (uint32_t)k < ne ? op.gather(j0 + jt + k, cl[jt + k]) : V();
-        const uint32_t it_start = it;
-        const bool start_cont = (it == 0) ? (rs0 < j0 + jt) : (rowend(it - 1) < jt);
-        A acc = op.zero();
-        A first_part = op.zero();
-        uint32_t first_row = EG_MP_NONE;
-        uint32_t nre = it < nrows ? rowend(it) : 0xffffffffu;  // end of the current row
-#pragma unroll
-        for (int k = 0; k < IPT; k++) {
-            if (d0 + k < d1) {
-                if (nre <= jt) {
-                    if (it == it_start && start_cont) {
-                        first_part = acc;
-                        first_row = it;
-                    } else {
-                        s_sum[it] = acc;
-                    }
-                    acc = op.zero();
-                    it++;
-                    nre = it < nrows ? rowend(it) : 0xffffffffu;
-                } else {
-                    acc = op.add(acc, v[0]);
-#pragma unroll
-                    for (int q = 0; q < IPT - 1; q++) v[q] = v[q + 1];
-                    jt++;
-                }
-            }
-        }
-        // segmented scan of the open-row partials (as in k_mp_rows)
-        A sv = acc;
-#pragma unroll
-        for (int off = 1; off < 32; off <<= 1) {
-            const A pv = eg_shfl_up(sv, off);
-            const uint32_t pk = __shfl_up_sync(EG_FULL_MASK, it, off);
-            if (lane >= (uint32_t)off && pk == it) sv = op.merge(pv, sv);
-        }
-        const uint32_t first_key = __shfl_sync(EG_FULL_MASK, it, 0);
-        if (lane == 31) {
-            s_wkey[warp] = it;
-            s_wval[warp] = sv;
-            s_wfirst[warp] = first_key;
-        }
-        __syncthreads();
-        {
-            A ext = op.zero();
-            bool has = false;
-            for (int w2 = (int)warp - 1; w2 >= 0; w2--) {
-                if (s_wkey[w2] != it) break;
-                ext = has ? op.merge(s_wval[w2], ext) : s_wval[w2];
-                has = true;
-                if (s_wfirst[w2] != it) break;
-            }
-            if (has) sv = op.merge(ext, sv);
-        }
-        s_crow[tid] = it;
-        s_cval[tid] = sv;
-        __syncthreads();
-        if (first_row != EG_MP_NONE) {
-            A tot = first_part;
-            if (tid > 0 && s_crow[tid - 1] == first_row) tot = op.merge(s_cval[tid - 1], tot);
-            if (first_row == 0 && rs0 < j0) {
-                s_head = 0;
-                s_headval = tot;
-            } else {
-                s_sum[first_row] = tot;
-            }
-        }
-        if (tid == T - 1) {
-            carry[c].tail_row = i0 + nrows;
-            carry[c].tail_val = sv;
-        }
-        __syncthreads();
-        if (tid == 0) {
-            carry[c].head_row = s_head == EG_MP_NONE ? EG_MP_NONE : i0;
-            if (s_head != EG_MP_NONE) carry[c].head_val = s_headval;
-        }
-        const uint32_t r0 = (s_head != EG_MP_NONE) ? 1u : 0u;
-        for (uint32_t r = r0 + tid; r < nrows; r += T) {
-            const double2 x = op.emit(i0 + r, s_sum[r]);
-            if (REDUCE) {
-                red.x += x.x;
-                red.y += x.y;
-            }
-        }
-        __syncthreads();  // stage buffers and s_sum are free again
-        stage ^= 1;
-    }
-    if (REDUCE) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            red.x += __shfl_down_sync(EG_FULL_MASK, red.x, o);
-            red.y += __shfl_down_sync(EG_FULL_MASK, red.y, o);
-        }
-        if (lane == 0) s_red[warp] = red;
-        __syncthreads();
-        if (tid == 0) {
-            double2 s = make_double2(0.0, 0.0);
-            for (int w = 0; w < T / 32; w++) {
-                s.x += s_red[w].x;
-                s.y += s_red[w].y;
-            }
-            part[blockIdx.x] = s;
-        }
-    }
-}
-
 // ============================================================== row-id stream variant
 // Entries carry their row id (rid[e], the COO form of the CSR/CSC, built once
-// per graph).  Each warp owns a fixed range of TILE_E entries and walks it in
-// chunks of 32: lane l loads entry e = base + l (coalesced col and rid),
-// gathers its value, and a segmented inclusive scan by row over the 32 lanes
-// (5 shuffle steps, fixed order) sums each row's run; the lane holding the
-// last entry of a row emits it.  The row open at the end of a chunk is
-// carried in registers to the next chunk; rows split between warps are
-// finished by k_coo_fixup (same head/tail scheme as the merge-path kernels).
-// Rows without entries are written by k_coo_empty_rows.  No shared memory,
-// no block barriers in the main loop: all lanes work in parallel.
-template <class Op, int TILE_E, int U, bool REDUCE>
-__global__ void __launch_bounds__(256) k_coo_rows(const uint32_t *__restrict__ rid, const uint32_t *__restrict__ col,
-                                                  uint32_t m, uint32_t ntiles,
-                                                  eg_mp_carry<typename Op::A> *__restrict__ carry,
-                                                  double2 *__restrict__ part, Op op) {
-    using V = typename Op::V;
-    using A = typename Op::A;
-    __shared__ double2 s_red[8];
-    if (!op.active()) return;
-    op.setup();
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // warp tile
-    double2 red = make_double2(0.0, 0.0);
-    if (t < ntiles) {
-        const uint32_t E0 = t * (uint32_t)TILE_E;
-        const uint32_t E1 = min(E0 + (uint32_t)TILE_E, m);
-        // a row open at E0 that began before the tile is the head: not emitted here
-        const uint32_t head_row = (E0 > 0 && __ldg(rid + E0 - 1) == __ldg(rid + E0)) ? __ldg(rid + E0) : EG_MP_NONE;
-        uint32_t crow = EG_MP_NONE;  // row carried from the previous chunk
-        A cval = op.zero();
-        bool head_done = false;
-        A head_val = op.zero();
-        for (uint32_t base = E0; base < E1; base += 32u * U) {
-            uint32_t r[U], u[U];
-            V v[U];
-#pragma unroll
-            for (int k = 0; k < U; k++) {
-                const uint32_t e = base + 32u * k + lane;
-                r[k] = e < E1 ? __ldg(rid + e) : EG_MP_NONE;
-                u[k] = e < E1 ? __ldg(col + e) : 0u;
-            }
-#pragma unroll
-            for (int k = 0; k < U; k++) {
-                const uint32_t e = base + 32u * k + lane;
-                v[k] = e < E1 ? op.gather(e, u[k]) : V();
-            }
-#pragma unroll
-            for (int k = 0; k < U; k++) {
-                const uint32_t e0 = base + 32u * k;
-                if (e0 >= E1) break;
-                const uint32_t row = r[k];
-                A x = op.add(op.zero(), v[k]);
-                if (lane == 0 && row == crow) x = op.merge(cval, x);
-#pragma unroll
-                for (int off = 1; off < 32; off <<= 1) {
-                    const A px = eg_shfl_up(x, off);
-                    const uint32_t pr = __shfl_up_sync(EG_FULL_MASK, row, off);
-                    if (lane >= (uint32_t)off && pr == row) x = op.merge(px, x);
-                }
-                // the row after this entry (for lane 31: the next chunk's first entry)
-                uint32_t nrow = __shfl_down_sync(EG_FULL_MASK, row, 1);
-                if (lane == 31) nrow = (e0 + 32 < E1) ? __ldg(rid + e0 + 32) : EG_MP_NONE;
-                const uint32_t e = e0 + lane;
-                bool last = e < E1 && nrow != row;  // ends a run inside the tile
-                if (last && e + 1 >= E1) last = (E1 == m) || __ldg(rid + E1) != row;  // row ends at the tile end?
-                if (last) {
-                    if (row == head_row) {
-                        head_done = true;
-                        head_val = x;
-                    } else {
-                        const double2 d = op.emit(row, x);
-                        if (REDUCE) {
-                            red.x += d.x;
-                            red.y += d.y;
-                        }
-                    }
-                }
-                crow = __shfl_sync(EG_FULL_MASK, row, 31);
-                cval = eg_shfl_idx(x, 31);
-            }
-        }
-        // head: the lane that finished it holds the value; tail: the open row at E1
-        const uint32_t hmask = __ballot_sync(EG_FULL_MASK, head_done);
-        if (lane == 0) {
-            const bool tail_open = E1 < m && crow != EG_MP_NONE && __ldg(rid + E1) == crow;
-            carry[t].tail_row = tail_open ? crow : EG_MP_NONE;
-            carry[t].tail_val = cval;
-            carry[t].head_row = hmask ? head_row : EG_MP_NONE;
-        }
-        if (hmask) {
-            const A hv = eg_shfl_idx(head_val, __ffs(hmask) - 1);
-            if (lane == 0) carry[t].head_val = hv;
-        }
-    }
-    if (REDUCE) {
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            red.x += __shfl_down_sync(EG_FULL_MASK, red.x, o);
-            red.y += __shfl_down_sync(EG_FULL_MASK, red.y, o);
-        }
-        if (lane == 0) s_red[threadIdx.x >> 5] = red;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double2 s = make_double2(0.0, 0.0);
-            for (int w = 0; w < 8; w++) {
-                s.x += s_red[w].x;
-                s.y += s_red[w].y;
-            }
-            part[blockIdx.x] = s;
-        }
-    }
-}
+// per graph), so a warp can own a fixed range of entries and find row
+// boundaries by comparing neighbouring row ids.  Rows split between warps are
+// finished by k_coo_fixup (same head/tail scheme as the merge-path kernels);
+// rows without entries are written by k_coo_empty_rows.
 
 // Rows split between warp tiles: one warp per tile with a head row adds the
 // tails of the preceding tiles, 32 per step (as k_mp_fixup).
@@ -704,7 +329,7 @@ __global__ void k_coo_fixup(const uint32_t *__restrict__ ptr, uint32_t ntiles,
     op.setup();
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    double2 red = make_double2(0.0, 0.0);
+    eg_red2 redf;
     if (c < ntiles) {
         const uint32_t row = carry[c].head_row;
         if (row != EG_MP_NONE) {
@@ -726,11 +351,11 @@ __global__ void k_coo_fixup(const uint32_t *__restrict__ ptr, uint32_t ntiles,
                 tot = op.merge(x, tot);
                 if (stop_mask) break;
             }
-            if (lane == 0) red = op.emit(row, tot);
+            if (lane == 0) redf.add(op.emit(row, tot));
         }
     }
     if (REDUCE) {
-        if (lane == 0) s_red[threadIdx.x >> 5] = red;
+        if (lane == 0) s_red[threadIdx.x >> 5] = redf.wide();
         __syncthreads();
         if (threadIdx.x == 0) {
             double2 s = make_double2(0.0, 0.0);
@@ -749,17 +374,15 @@ __global__ void k_coo_empty_rows(const uint32_t *__restrict__ ptr, uint32_t n, d
     __shared__ double2 s_red[8];
     if (!op.active()) return;
     op.setup();
-    double2 red = make_double2(0.0, 0.0);
+    eg_red2 redf;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
         if (__ldg(ptr + v) == __ldg(ptr + v + 1)) {
-            const double2 d = op.emit(v, op.zero());
-            if (REDUCE) {
-                red.x += d.x;
-                red.y += d.y;
-            }
+            const float2 d = op.emit(v, op.zero());
+            if (REDUCE) redf.add(d);
         }
     }
     if (REDUCE) {
+        double2 red = redf.wide();
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             red.x += __shfl_down_sync(EG_FULL_MASK, red.x, o);
@@ -802,7 +425,7 @@ __global__ void __launch_bounds__(256) k_coov_rows(const uint32_t *__restrict__ 
     op.setup();
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    double2 red = make_double2(0.0, 0.0);
+    eg_red2 redf;
     if (t < ntiles) {
         const uint32_t E0 = t * (uint32_t)TILE_E;
         const uint32_t E1 = min(E0 + (uint32_t)TILE_E, m);
@@ -820,11 +443,8 @@ __global__ void __launch_bounds__(256) k_coov_rows(const uint32_t *__restrict__ 
                 head_val = val;
                 return;
             }
-            const double2 d = op.emit(row, val);
-            if (REDUCE) {
-                red.x += d.x;
-                red.y += d.y;
-            }
+            const float2 d = op.emit(row, val);
+            if (REDUCE) redf.add(d);
         };
         for (uint32_t base = E0; base < E1; base += CH) {
             const uint32_t e = base + U * lane;
@@ -909,6 +529,7 @@ __global__ void __launch_bounds__(256) k_coov_rows(const uint32_t *__restrict__ 
         }
     }
     if (REDUCE) {
+        double2 red = redf.wide();
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
             red.x += __shfl_down_sync(EG_FULL_MASK, red.x, o);

@@ -46,9 +46,9 @@ struct NoallocSpmvOp {
     __device__ __forceinline__ A zero() const { return 0.f; }
     __device__ __forceinline__ A add(A a, V v) const { return a + v; }
     __device__ __forceinline__ A merge(A a, A b) const { return a + b; }
-    __device__ __forceinline__ double2 emit(uint32_t v, A s) const {
+    __device__ __forceinline__ float2 emit(uint32_t v, A s) const {
         y[v] = s;
-        return make_double2(0.0, 0.0);
+        return make_float2(0.f, 0.f);
     }
 };
 

@@ -124,18 +124,18 @@ __global__ void __launch_bounds__(256) k_ppr_finish(const float *__restrict__ Y,
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const bool live = qs[lane].active && !qs[lane].done;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    double res = 0.0, dang = 0.0;
+    eg_red2 acc;  // fp32 TwoSum pairs per lane, widened once (FP64 issues slowly)
     for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
         if (!live) continue;
         const uint64_t i = (uint64_t)v * EG_PPR_LANES + lane;
         const float r = d * Y[i];
-        res += fabs((double)r - (double)R[i]);
+        const float old = R[i];
         R[i] = r;
         const uint32_t dv = deg[v];
         X[i] = dv ? __fdiv_rn(r, (float)dv) : 0.f;
-        if (!dv) dang += (double)r;
+        acc.add(make_float2(fabsf(r - old), dv ? 0.f : r));
     }
-    s_part[warp][lane] = make_double2(res, dang);
+    s_part[warp][lane] = acc.wide();
     __syncthreads();
     if (warp == 0) {
         double2 s = make_double2(0.0, 0.0);

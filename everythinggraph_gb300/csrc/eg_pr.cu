@@ -25,14 +25,7 @@
 
 #include "eg_mp.cuh"
 
-#ifndef EG_MP_T
-#define EG_MP_T 256
-#endif
-#ifndef EG_MP_IPT
-#define EG_MP_IPT 8
-#endif
-
-// ============================================================== schedule
+// ============================================================== merge-path schedule (eg_noalloc.cu)
 __global__ void k_mp_schedule(const uint32_t *__restrict__ ptr, uint32_t n, uint32_t m, uint32_t items,
                               uint32_t ntiles, uint2 *__restrict__ coord) {
     uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
@@ -48,21 +41,6 @@ __global__ void k_mp_schedule(const uint32_t *__restrict__ ptr, uint32_t n, uint
         else hi = mid;
     }
     coord[c] = make_uint2((uint32_t)lo, (uint32_t)(diag - lo));
-}
-
-int eg_build_sched(eg_graph *g, eg_adj &adj, eg_mp_sched &s, uint32_t items) {
-    if (s.items == items && s.coord.p) return EG_OK;
-    eg_ctx *ctx = g->ctx;
-    uint64_t total = (uint64_t)g->n + g->m;
-    uint32_t ntiles = (uint32_t)((total + items - 1) / items);
-    if (ntiles == 0) ntiles = 1;
-    EG_TRY(eg_buf_ensure(ctx, s.coord, ((uint64_t)ntiles + 1) * sizeof(uint2)));
-    k_mp_schedule<<<eg_div_up(ntiles + 1, 256), 256, 0, ctx->stream>>>(bp<uint32_t>(adj.ptr), g->n, (uint32_t)g->m,
-                                                                      items, ntiles, bp<uint2>(s.coord));
-    EG_LAUNCHED(ctx);
-    s.items = items;
-    s.ntiles = ntiles;
-    return EG_OK;
 }
 
 // ============================================================== PR state
@@ -102,7 +80,6 @@ struct PrOp {
     const eg_pr_dev *st;
     uint32_t mult;
     float damping;
-    int residual;
     float base;
     PprSeeds seeds;
     __device__ __forceinline__ bool active() const { return st->done == 0; }
@@ -120,19 +97,17 @@ struct PrOp {
         if constexpr (COMP) return eg_f2sum::merge(a, b);
         else return a + b;
     }
-    __device__ __forceinline__ double2 emit(uint32_t v, A s) const {
+    __device__ __forceinline__ float2 emit(uint32_t v, A s) const {
         float sum;
         if constexpr (COMP) sum = s.x + s.y;
         else sum = s;
         // teleport: base on every vertex, or base x multiplicity on the seeds
         const float b = seeds.count ? base * seeds.weight(v) : base;
         float r = fmaf(damping, sum, b);
-        double res = 0.0;
-        if (residual) res = fabs((double)r - (double)rank[v]);
         rank[v] = r;
         uint32_t d = deg[v] * mult;
         cout[v] = d ? __fdiv_rn(r, (float)d) : 0.f;
-        return make_double2(res, d ? 0.0 : (double)r);
+        return make_float2(0.f, d ? 0.f : r);  // (residual: k_pr_residual, dangling mass)
     }
 };
 
@@ -179,14 +154,39 @@ __global__ void k_ppr1_init(uint32_t n, PprSeeds seeds, float inv_total, const u
     }
 }
 
+// L1 change between two rank vectors, per-block FP64 partials in .x (the
+// stop test's residual); skipped once the run has converged.
+__global__ void k_pr_residual(const float *__restrict__ cur, const float *__restrict__ prev, uint32_t n,
+                              const eg_pr_dev *st, double2 *__restrict__ part) {
+    __shared__ double s_red[8];
+    if (st->done) return;
+    eg_red2 acc;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        acc.add(make_float2(fabsf(__ldg(cur + v) - __ldg(prev + v)), 0.f));
+    double r = acc.wide().x;
+    for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(EG_FULL_MASK, r, o);
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = r;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0.0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) t += s_red[w];
+        part[blockIdx.x] = make_double2(t, 0.0);
+    }
+}
+
 __global__ void k_map_ids(const uint32_t *__restrict__ perm, const uint32_t *__restrict__ in, uint32_t k,
                           uint32_t *__restrict__ out) {
     for (uint32_t i = threadIdx.x; i < k; i += blockDim.x) out[i] = perm[in[i]];
 }
 
-__global__ void k_pr_unpermute(const float *__restrict__ rank_p, const uint32_t *__restrict__ perm, uint32_t n,
+// Iteration `it` writes its ranks to buffer B when `it` is even and to A when
+// it is odd (the start vector is in A), so the last iteration that ran (the
+// stop test may end the run early) left its ranks in B if st->iters is odd.
+__global__ void k_pr_unpermute(const float *__restrict__ rank_a, const float *__restrict__ rank_b,
+                               const eg_pr_dev *st, const uint32_t *__restrict__ perm, uint32_t n,
                                float *__restrict__ rank) {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) rank[v] = rank_p[perm[v]];
+    const float *src = (st->iters & 1) ? rank_b : rank_a;
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) rank[v] = src[perm[v]];
 }
 
 // One block: deterministic FP64 sum of the partials, next base, stop test.
@@ -222,65 +222,13 @@ __global__ void k_pr_reduce(const double2 *__restrict__ part, uint32_t nparts, e
     }
 }
 
-template <class Op, bool REDUCE>
-static int mp_launch(eg_graph *g, eg_adj &adj, eg_mp_sched &s, eg_buf &carry_buf, double2 *part, const Op &op) {
-    eg_ctx *ctx = g->ctx;
-    using A = typename Op::A;
-    using L = eg_mp_smem<EG_MP_T, EG_MP_IPT, typename Op::V, A>;
-    auto kern = k_mp_rows<Op, EG_MP_T, EG_MP_IPT, REDUCE>;
-    static bool attr_set = false;
-    if (!attr_set) {
-        EG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::bytes));
-        attr_set = true;
-    }
-    EG_TRY(eg_buf_ensure(ctx, carry_buf, (uint64_t)s.ntiles * sizeof(eg_mp_carry<A>)));
-    kern<<<s.ntiles, EG_MP_T, L::bytes, ctx->stream>>>(bp<uint32_t>(adj.ptr), bp<uint32_t>(adj.col), g->n,
-                                                      bp<uint2>(s.coord), bp<eg_mp_carry<A>>(carry_buf), part, op);
-    EG_LAUNCHED(ctx);
-    uint32_t fb = eg_div_up((uint64_t)s.ntiles * 32, 256);
-    k_mp_fixup<Op, REDUCE><<<fb, 256, 0, ctx->stream>>>(bp<uint32_t>(adj.ptr), bp<uint2>(s.coord), s.ntiles,
-                                                       bp<eg_mp_carry<A>>(carry_buf), part ? part + s.ntiles : nullptr,
-                                                       op);
-    EG_LAUNCHED(ctx);
-    return EG_OK;
-}
-
-// Persistent TMA-staged variant: grid = resident CTAs (one wave), part[]
-// gets one FP64 partial per CTA then one per fix-up block.
-template <class Op, bool REDUCE>
-static int mpp_launch(eg_graph *g, eg_adj &adj, eg_mp_sched &s, eg_buf &carry_buf, double2 *part, int *err,
-                      const Op &op, uint32_t *grid_out) {
-    eg_ctx *ctx = g->ctx;
-    using A = typename Op::A;
-    using L = eg_mpp_smem<EG_MP_T, EG_MP_IPT, A>;
-    auto kern = k_mpp_rows<Op, EG_MP_T, EG_MP_IPT, REDUCE>;
-    static int per_sm = 0;
-    if (!per_sm) {
-        EG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L::bytes));
-        EG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, EG_MP_T, L::bytes));
-        if (per_sm < 1) return eg_fail(EG_ECUDA, "merge-path kernel does not fit on an SM");
-    }
-    EG_TRY(eg_buf_ensure(ctx, carry_buf, (uint64_t)s.ntiles * sizeof(eg_mp_carry<A>)));
-    uint32_t grid = (uint32_t)ctx->sm_count * (uint32_t)per_sm;
-    if (grid > s.ntiles) grid = s.ntiles;
-    *grid_out = grid;
-    kern<<<grid, EG_MP_T, L::bytes, ctx->stream>>>(bp<uint32_t>(adj.ptr), bp<uint32_t>(adj.col), g->n,
-                                                  bp<uint2>(s.coord), s.ntiles, bp<eg_mp_carry<A>>(carry_buf), part,
-                                                  err, op);
-    EG_LAUNCHED(ctx);
-    uint32_t fb = eg_div_up((uint64_t)s.ntiles * 32, 256);
-    k_mp_fixup<Op, REDUCE><<<fb, 256, 0, ctx->stream>>>(bp<uint32_t>(adj.ptr), bp<uint2>(s.coord), s.ntiles,
-                                                       bp<eg_mp_carry<A>>(carry_buf), part ? part + grid : nullptr,
-                                                       op);
-    EG_LAUNCHED(ctx);
-    return EG_OK;
-}
-
 // Row-id stream kernel (k_coov_rows): one warp per TILE entries, U entries
 // per lane.  part[] receives per-CTA partials of the main kernel, then of the
 // empty-row kernel, then of the fix-up; returns their count.  The schedule
 // (TILE, U) is the graph's row_cfg, picked by eg_graph_tune.
 #define EG_COO_TILE_MIN 1024
+#define EG_PR_CHECK 4  // iterations between reads of the stop flag
+#define EG_PR_RES_BLOCKS 1024
 #define EG_ROW_CFGS 5
 static const int kRowTile[EG_ROW_CFGS] = {2048, 1024, 4096, 2048, 4096};
 static const int kRowU[EG_ROW_CFGS] = {4, 4, 4, 8, 8};
@@ -344,25 +292,31 @@ extern "C" void eg_pr_opts_default(eg_pr_opts *o) {
 // EG_KEV iterations are bracketed by the context's kernel events.
 template <bool COMP, bool REDUCE>
 static int pr_iterations(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, double tele_div, eg_pr_dev *st,
-                         double2 *part, eg_buf &carry, bool timed) {
+                         double2 *part, eg_buf &carry, bool timed, int it0, int it1) {
     eg_ctx *ctx = g->ctx;
-    for (int it = 0; it < o.iterations; it++) {
+    for (int it = it0; it < it1; it++) {
         PrOp<COMP> op;
         bool odd = o.swap && (it & 1);
         op.cin = odd ? bp<float>(g->contrib1) : bp<float>(g->contrib0);
         op.cout = odd ? bp<float>(g->contrib0) : bp<float>(g->contrib1);
-        op.rank = bp<float>(g->rank_p);
+        float *rank_new = (it & 1) ? bp<float>(g->rank_p) : bp<float>(g->rank_q);
+        const float *rank_old = (it & 1) ? bp<float>(g->rank_q) : bp<float>(g->rank_p);
+        op.rank = rank_new;
         op.deg = bp<uint32_t>(g->deg_p);
         op.st = st;
         op.mult = o.deg_multiplier;
         op.damping = o.damping;
-        op.residual = o.tolerance > 0.0;
         op.base = 0.f;
         op.seeds = ps;
         uint32_t nparts = 0;
         const bool t = timed && it < EG_KEV;
         EG_TRY((coo_launch<PrOp<COMP>, REDUCE>(g, g->csc_p, carry, part, op, &nparts, t ? ctx->evk[2 * it] : nullptr,
                                                 t ? ctx->evk[2 * it + 1] : nullptr)));
+        if (o.tolerance > 0.0) {  // the L1 change, after the row kernels (coalesced, 8 bytes per vertex)
+            k_pr_residual<<<EG_PR_RES_BLOCKS, 256, 0, ctx->stream>>>(rank_new, rank_old, g->n, st, part + nparts);
+            EG_LAUNCHED(ctx);
+            nparts += EG_PR_RES_BLOCKS;
+        }
         k_pr_reduce<<<1, 256, 0, ctx->stream>>>(part, REDUCE ? nparts : 0, st, tele_div, o.damping, o.dangling,
                                                 o.tolerance, 1);
         EG_LAUNCHED(ctx);
@@ -370,14 +324,15 @@ static int pr_iterations(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, d
     return EG_OK;
 }
 
+// Iterations [it0, it1).
 static int pr_dispatch(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, double tele_div, bool reduce,
-                       eg_pr_dev *st, double2 *part, eg_buf &carry, bool timed) {
+                       eg_pr_dev *st, double2 *part, eg_buf &carry, bool timed, int it0, int it1) {
     if (o.compensated) {
-        if (reduce) return pr_iterations<true, true>(g, o, ps, tele_div, st, part, carry, timed);
-        return pr_iterations<true, false>(g, o, ps, tele_div, st, part, carry, timed);
+        if (reduce) return pr_iterations<true, true>(g, o, ps, tele_div, st, part, carry, timed, it0, it1);
+        return pr_iterations<true, false>(g, o, ps, tele_div, st, part, carry, timed, it0, it1);
     }
-    if (reduce) return pr_iterations<false, true>(g, o, ps, tele_div, st, part, carry, timed);
-    return pr_iterations<false, false>(g, o, ps, tele_div, st, part, carry, timed);
+    if (reduce) return pr_iterations<false, true>(g, o, ps, tele_div, st, part, carry, timed, it0, it1);
+    return pr_iterations<false, false>(g, o, ps, tele_div, st, part, carry, timed, it0, it1);
 }
 
 // The iteration loop of plain PageRank captured once as a CUDA graph and
@@ -393,7 +348,7 @@ static int pr_graph(eg_graph *g, const eg_pr_opts &o, bool reduce, eg_pr_dev *st
     memcpy(&key[3], &o.tolerance, 8);
     key[4] = (uint64_t)(uintptr_t)g->contrib0.p;
     key[5] = (uint64_t)(uintptr_t)g->contrib1.p;
-    key[6] = (uint64_t)(uintptr_t)g->rank_p.p;
+    key[6] = (uint64_t)(uintptr_t)g->rank_p.p ^ ((uint64_t)(uintptr_t)g->rank_q.p << 1);
     key[7] = (uint64_t)(uintptr_t)g->deg_p.p;
     key[8] = (uint64_t)(uintptr_t)st;
     key[9] = (uint64_t)(uintptr_t)part;
@@ -415,7 +370,7 @@ static int pr_graph(eg_graph *g, const eg_pr_opts &o, bool reduce, eg_pr_dev *st
     PprSeeds none;
     memset(&none, 0, sizeof(none));
     EG_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-    int rc = pr_dispatch(g, o, none, (double)g->n, reduce, st, part, carry, false);
+    int rc = pr_dispatch(g, o, none, (double)g->n, reduce, st, part, carry, false, 0, o.iterations);
     cudaGraph_t gr = nullptr;
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &gr);
     if (rc != EG_OK) {
@@ -437,14 +392,13 @@ static int pr_run(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, uint32_t
     eg_ctx *ctx = g->ctx;
     const uint32_t n = g->n;
     const uint32_t coo_tiles = g->m ? eg_div_up(g->m, EG_COO_TILE_MIN) : 0;  // the most tiles of any schedule
-    const uint32_t nparts = 2 * eg_div_up((uint64_t)coo_tiles * 32, 256) + (uint32_t)ctx->sm_count * 8;
+    const uint32_t nparts = 2 * eg_div_up((uint64_t)coo_tiles * 32, 256) + (uint32_t)ctx->sm_count * 8 + EG_PR_RES_BLOCKS;
     EG_TRY(eg_buf_ensure(ctx, g->rank, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->rank_p, (uint64_t)n * 4));
+    EG_TRY(eg_buf_ensure(ctx, g->rank_q, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->contrib0, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->contrib1, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->pr_part, ((uint64_t)nparts + 1024) * sizeof(double2)));
-    EG_TRY(eg_buf_ensure(ctx, g->errflag, 16));
-    EG_CUDA(cudaMemsetAsync(g->errflag.p, 0, 16, ctx->stream));
     eg_buf &carry = g->mp_carry;
     eg_pr_dev *st = bp<eg_pr_dev>(g->pr_stats);
     double2 *part = bp<double2>(g->pr_part);
@@ -473,19 +427,29 @@ static int pr_run(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, uint32_t
     if (graph) {
         if (o.iterations > 0) EG_CUDA(cudaGraphLaunch(g->prg.exec, ctx->stream));
     } else {
-        EG_TRY(pr_dispatch(g, o, ps, tele_div, reduce, st, part, carry, true));
+        // with a tolerance, the stop flag is read every EG_PR_CHECK iterations so
+        // that converged runs do not keep launching no-op iterations
+        const int chunk = o.tolerance > 0.0 ? EG_PR_CHECK : (o.iterations > 0 ? o.iterations : 1);
+        int *hdone = (int *)ctx->h_pinned;
+        for (int it0 = 0; it0 < o.iterations; it0 += chunk) {
+            const int it1 = it0 + chunk < o.iterations ? it0 + chunk : o.iterations;
+            EG_TRY(pr_dispatch(g, o, ps, tele_div, reduce, st, part, carry, true, it0, it1));
+            if (o.tolerance > 0.0 && it1 < o.iterations) {
+                EG_CUDA(cudaMemcpyAsync(hdone, &st->done, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+                EG_CUDA(cudaStreamSynchronize(ctx->stream));
+                if (*hdone) break;
+            }
+        }
     }
     EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     // ranks back to the original vertex ids
-    k_pr_unpermute<<<ib, 256, 0, ctx->stream>>>(bp<float>(g->rank_p), bp<uint32_t>(g->perm), n, bp<float>(g->rank));
+    k_pr_unpermute<<<ib, 256, 0, ctx->stream>>>(bp<float>(g->rank_p), bp<float>(g->rank_q), st, bp<uint32_t>(g->perm),
+                                                n, bp<float>(g->rank));
     EG_LAUNCHED(ctx);
     eg_pr_dev hst;
-    int herr = 0;
     EG_CUDA(cudaMemcpyAsync(&hst, st, sizeof(hst), cudaMemcpyDeviceToHost, ctx->stream));
-    EG_CUDA(cudaMemcpyAsync(&herr, g->errflag.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
     if (rank_out) EG_CUDA(cudaMemcpyAsync(rank_out, g->rank.p, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
     EG_CUDA(cudaStreamSynchronize(ctx->stream));
-    if (herr) return eg_fail(EG_ETIMEOUT, "PageRank: a tile copy did not complete (mbarrier wait limit)");
     if (stats) {
         stats->iterations_run = hst.iters;
         stats->residual = hst.residual;
@@ -636,9 +600,9 @@ struct SpmvU32Op {
     __device__ __forceinline__ A zero() const { return 0u; }
     __device__ __forceinline__ A add(A a, V v) const { return a + v; }
     __device__ __forceinline__ A merge(A a, A b) const { return a + b; }
-    __device__ __forceinline__ double2 emit(uint32_t v, A s) const {
+    __device__ __forceinline__ float2 emit(uint32_t v, A s) const {
         y[v] = s;
-        return make_double2(0.0, 0.0);
+        return make_float2(0.f, 0.f);
     }
 };
 
@@ -664,10 +628,10 @@ struct SpmvF32Op {
         if constexpr (COMP) return eg_f2sum::merge(a, b);
         else return a + b;
     }
-    __device__ __forceinline__ double2 emit(uint32_t v, A s) const {
+    __device__ __forceinline__ float2 emit(uint32_t v, A s) const {
         if constexpr (COMP) y[v] = s.x + s.y;
         else y[v] = s;
-        return make_double2(0.0, 0.0);
+        return make_float2(0.f, 0.f);
     }
 };
 
@@ -685,9 +649,9 @@ struct SpmvF64Op {
     __device__ __forceinline__ A zero() const { return 0.0; }
     __device__ __forceinline__ A add(A a, V v) const { return __dadd_rn(a, v); }
     __device__ __forceinline__ A merge(A a, A b) const { return __dadd_rn(a, b); }
-    __device__ __forceinline__ double2 emit(uint32_t v, A s) const {
+    __device__ __forceinline__ float2 emit(uint32_t v, A s) const {
         y[v] = s;
-        return make_double2(0.0, 0.0);
+        return make_float2(0.f, 0.f);
     }
 };
 
@@ -715,8 +679,6 @@ extern "C" int eg_spmv(eg_graph *g, const eg_spmv_opts *opts, const void *x, voi
     EG_CUDA(cudaSetDevice(ctx->device));
     const uint32_t n = g->n;
     eg_adj &adj = pull ? g->csc : g->csr;
-    eg_mp_sched &s = pull ? g->sched_csc : g->sched_csr;
-    EG_TRY(eg_build_sched(g, adj, s, EG_MP_T * EG_MP_IPT));
     const size_t ysz = kind == EG_SPMV_F64 ? 8 : 4;
     EG_TRY(eg_buf_ensure(ctx, g->spmv_x, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->spmv_y, (uint64_t)n * ysz));

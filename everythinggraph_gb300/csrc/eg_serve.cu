@@ -21,6 +21,8 @@
 #include <deque>
 #include <vector>
 
+#include "eg_bigwork.cuh"
+#include "eg_mrelax.cuh"
 #include "eg_mspull.cuh"
 #include "eg_ppr.cuh"
 
@@ -200,23 +202,18 @@ __global__ void k_sv_sssp_admit(const uint32_t *roots, const uint32_t *slots, in
     }
 }
 
-__device__ __forceinline__ void sv_relax(uint32_t u, uint32_t v, uint32_t j, uint32_t s, bool on, uint32_t du,
-                                         const SvW &w, uint32_t *dist, uint32_t *next_act, uint32_t *next_inq,
-                                         uint32_t *next_queue, SvCounters *cnt) {
-    bool improved = false;
-    if (on && v != u) {
-        const uint32_t nd = w.extend(du, u, v);
-        uint32_t *dp = dist + (uint64_t)v * SV_SSSP_SLOTS + s;
-        if (nd < __ldcg(dp)) improved = nd < atomicMin(dp, nd);
-    }
-    const uint32_t ball = __ballot_sync(EG_FULL_MASK, improved);
-    if (ball && (threadIdx.x & 31) == 0) {
+// Records v in the next frontier for the slots in `ball` of word j.
+struct SvSink {
+    uint32_t j;
+    uint32_t *next_act, *next_inq, *next_queue;
+    SvCounters *cnt;
+    __device__ __forceinline__ void operator()(uint32_t v, uint32_t ball) {
         atomicOr(next_act + (uint64_t)v * 2 + j, ball);
         atomicOr(&cnt->actmask[j], (unsigned long long)ball);
         const uint32_t bit = 1u << (v & 31);
         if (!(atomicOr(next_inq + (v >> 5), bit) & bit)) next_queue[atomicAdd(&cnt->qsize, 1u)] = v;
     }
-}
+};
 
 __global__ void __launch_bounds__(256) k_sv_sssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
                                                       const uint32_t *__restrict__ queue, const SvCounters *qc,
@@ -238,27 +235,38 @@ __global__ void __launch_bounds__(256) k_sv_sssp_push(const uint32_t *__restrict
         }
         const uint32_t s = j * 32 + lane;
         const bool on = (a >> lane) & 1u;
-        const uint32_t du = on ? __ldcg(dist + (uint64_t)u * SV_SSSP_SLOTS + s) : SV_INF;
-        for (uint32_t p = b; p < e; p++) sv_relax(u, col[p], j, s, on, du, w, dist, next_act, next_inq, next_queue, cnt);
+        const uint32_t du = on ? __ldcg(dist + (uint64_t)u * SV_SSSP_SLOTS + s) : 0u;
+        SvSink sink{j, next_act, next_inq, next_queue, cnt};
+        eg_mrelax_span(u, b, e, col, w, on, du, s, SV_SSSP_SLOTS, dist, sink);
     }
 }
 
+// Deferred (hub, word) items in chunks of SV_SSSP_CHUNK edges, one CTA per
+// chunk, one warp per 32 edges of it.
+#define SV_SSSP_CHUNK 256u
 __global__ void __launch_bounds__(256) k_sv_sssp_push_big(const uint32_t *__restrict__ ptr,
                                                           const uint32_t *__restrict__ col, uint32_t *dist,
                                                           const uint32_t *__restrict__ act, uint32_t *next_act,
                                                           uint32_t *next_inq, uint32_t *next_queue, SvW w,
-                                                          SvCounters *cnt, const uint32_t *big) {
+                                                          SvCounters *cnt, const uint32_t *big,
+                                                          const uint32_t *__restrict__ bigoff) {
     const uint32_t nbig = *(volatile uint32_t *)&cnt->nbig;
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t bi = 0; bi < nbig; bi++) {
-        const uint32_t u = big[bi] >> 1, j = big[bi] & 1;
+    if (!nbig) return;
+    const uint32_t total = bigoff[nbig];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
+        const uint32_t i = eg_big_item(bigoff, nbig, c);
+        const uint32_t u = big[i] >> 1, j = big[i] & 1;
         const uint32_t a = act[(uint64_t)u * 2 + j];
         const uint32_t s = j * 32 + lane;
         const bool on = (a >> lane) & 1u;
-        const uint32_t du = on ? __ldcg(dist + (uint64_t)u * SV_SSSP_SLOTS + s) : SV_INF;
-        for (uint32_t p = ptr[u] + gw; p < ptr[u + 1]; p += warps)
-            sv_relax(u, col[p], j, s, on, du, w, dist, next_act, next_inq, next_queue, cnt);
+        const uint32_t du = on ? __ldcg(dist + (uint64_t)u * SV_SSSP_SLOTS + s) : 0u;
+        const uint32_t ve = ptr[u + 1];
+        const uint32_t b = ptr[u] + (c - bigoff[i]) * SV_SSSP_CHUNK + 32u * warp;
+        if (b < ve) {
+            SvSink sink{j, next_act, next_inq, next_queue, cnt};
+            eg_mrelax_span(u, b, ve - b > 32 ? b + 32 : ve, col, w, on, du, s, SV_SSSP_SLOTS, dist, sink);
+        }
     }
 }
 
@@ -360,13 +368,29 @@ struct eg_server {
     uint32_t ppr_mask = 0;
     uint64_t ppr_id[SV_PPR_LANES];
     double ppr_admit[SV_PPR_LANES], ppr_arrival[SV_PPR_LANES];
+    PprQ *hq = nullptr;                  // host mirror of the lanes' state (pinned, updated every iteration)
+    uint32_t pseeds[SV_PPR_LANES * 8] = {};  // seeds of each lane (8 per lane)
+    uint32_t pnseeds[SV_PPR_LANES] = {};
     eg_buf small;  // counters, admission lists, summaries (device)
     uint64_t ticks = 0;
-    // device time per engine step (events around each engine's launches)
-    cudaEvent_t ev[6] = {};
+    // engines run on their own streams; a step is in flight until its event completes
+    cudaStream_t st[3] = {};
+    cudaEvent_t ev_begin[3] = {}, ev_end[3] = {};
+    bool inflight[3] = {false, false, false};
+    unsigned long long step_mask[3] = {0, 0, 0};  // slots live in the step in flight
+    unsigned char *hpin = nullptr;                // pinned host staging, a region per engine
     double eng_ms[3] = {0.0, 0.0, 0.0};
     uint64_t eng_steps[3] = {0, 0, 0};
     uint64_t admitted[3] = {0, 0, 0}, completed[3] = {0, 0, 0};
+};
+
+// Device small-buffer layout (bytes) and host staging layout (bytes).
+enum : uint32_t {
+    SM_BCNT = 0, SM_SCNT = 256, SM_SNEXT = 512, SM_BROOTS = 1024, SM_SROOTS = 1536, SM_BSLOTS = 2048,
+    SM_SSLOTS = 2560, SM_BLEVEL = 3072, SM_PPRQ = 4096, SM_PSEEDS = 8192, SM_PSBEG = 9216, SM_PSEND = 9344,
+    SM_SUM = 12544,  // 64 bytes per engine
+    HP_BCNT = 0, HP_SCNT = 256, HP_PPRQ = 1024, HP_PSEEDS = 4096, HP_SUM = 8192,  // 64 per engine
+    HP_BADM = 12288, HP_SADM = 13312, HP_BLEVEL = 14336, HP_BYTES = 16384
 };
 
 static uint32_t sv_blocks(eg_ctx *ctx, uint64_t threads) {
@@ -414,7 +438,7 @@ extern "C" int eg_serve_open(eg_graph *g, const eg_serve_opts *opts, eg_server *
     sv_slot_bytes(n, &sb, &ss, &sp);
     // shared per-engine state, then as many slots as the budget allows
     const uint64_t shared_bfs = (uint64_t)n * 8 * 3 + (uint64_t)n * 8;
-    const uint64_t shared_sssp = (uint64_t)n * 8 * 2 + (uint64_t)n * 4 * 2 + (uint64_t)n * 4 * 3;
+    const uint64_t shared_sssp = (uint64_t)n * 8 * 2 + (uint64_t)n * 4 * 2 + (uint64_t)n * 4 * 4;
     const uint64_t shared_ppr = 0;
     const uint64_t base = shared_bfs + shared_sssp + shared_ppr;
     if (o.hbm_budget && o.hbm_budget < base + sb + ss + sp)
@@ -437,17 +461,33 @@ extern "C" int eg_serve_open(eg_graph *g, const eg_serve_opts *opts, eg_server *
     int rc = EG_OK;
     // BFS: seen | front | next (u64) | queue+big (u32 x 2n) | levels (64 rows)
     if (rc == EG_OK) rc = eg_buf_ensure(ctx, s->bfs_buf, (uint64_t)n * 8 * 3 + (uint64_t)n * 8 + (uint64_t)SV_BFS_SLOTS * n * 4);
-    // SSSP: dist [n][64] | act x2 [n][2] | inq x2 | queue x2 | big
+    // SSSP: dist [n][64] | act x2 [n][2] | inq x2 | queue x2 | big | big chunk offsets
     if (rc == EG_OK)
         rc = eg_buf_ensure(ctx, s->sssp_buf, (uint64_t)n * 4 * SV_SSSP_SLOTS + (uint64_t)n * 8 * 2 + (uint64_t)((n + 31) / 32) * 4 * 2 +
-                                                 (uint64_t)n * 4 * 3);
+                                                 (uint64_t)n * 4 * 4 + 4);
     // PPR: R, X, Y [n][32] | parts
     const uint64_t ptiles = g->m ? (g->m + EG_PPR_TILE - 1) / EG_PPR_TILE : 0;
     if (rc == EG_OK)
         rc = eg_buf_ensure(ctx, s->ppr_buf, (uint64_t)n * 4 * EG_PPR_LANES * 3 + ptiles * EG_PPR_LANES * 4 * 2 +
                                                  ((ptiles + 63) & ~63ull) * 4 + (uint64_t)ctx->sm_count * 4 * 32 * 16 + 256);
     if (rc == EG_OK) rc = eg_buf_ensure(ctx, s->small, 64 * 1024);
+    for (int e = 0; e < 3 && rc == EG_OK; e++) {
+        if (cudaStreamCreateWithFlags(&s->st[e], cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreate(&s->ev_begin[e]) != cudaSuccess || cudaEventCreate(&s->ev_end[e]) != cudaSuccess)
+            rc = eg_fail(EG_ECUDA, "server streams/events");
+    }
+    if (rc == EG_OK && cudaMallocHost(&s->hpin, HP_BYTES) != cudaSuccess) rc = eg_fail(EG_ECUDA, "server staging");
+    if (rc == EG_OK) {
+        s->hq = (PprQ *)(s->hpin + HP_PPRQ);
+        memset(s->hpin, 0, HP_BYTES);
+    }
     if (rc != EG_OK) {
+        for (int e = 0; e < 3; e++) {
+            if (s->st[e]) cudaStreamDestroy(s->st[e]);
+            if (s->ev_begin[e]) cudaEventDestroy(s->ev_begin[e]);
+            if (s->ev_end[e]) cudaEventDestroy(s->ev_end[e]);
+        }
+        if (s->hpin) cudaFreeHost(s->hpin);
         eg_buf_free(ctx, s->bfs_buf);
         eg_buf_free(ctx, s->sssp_buf);
         eg_buf_free(ctx, s->ppr_buf);
@@ -478,6 +518,13 @@ extern "C" int eg_serve_close(eg_server *s) {
     if (!s) return EG_OK;
     eg_ctx *ctx = s->g->ctx;
     cudaStreamSynchronize(ctx->stream);
+    for (int e = 0; e < 3; e++) {
+        cudaStreamSynchronize(s->st[e]);
+        cudaStreamDestroy(s->st[e]);
+        cudaEventDestroy(s->ev_begin[e]);
+        cudaEventDestroy(s->ev_end[e]);
+    }
+    cudaFreeHost(s->hpin);
     eg_buf_free(ctx, s->bfs_buf);
     eg_buf_free(ctx, s->sssp_buf);
     eg_buf_free(ctx, s->ppr_buf);
@@ -524,294 +571,308 @@ static void sv_finish(eg_server *s, uint64_t id, int kind, double arrival, doubl
     s->completed[kind - 1]++;
 }
 
-// One scheduler tick.
-extern "C" int eg_serve_step(eg_server *s, int *active_out) {
-    if (!s) return eg_fail(EG_EINVAL, "NULL server");
+// ---------------------------------------------------------------- engines
+// Each engine (BFS, SSSP, PPR) advances on its own stream: a step (one BFS
+// level, one Bellman-Ford round, one PPR iteration over all live slots) is
+// launched, its counters are copied to pinned host memory behind it, and an
+// event marks its end.  eg_serve_step polls the events: an engine whose step
+// finished has its finished slots retired and its free slots refilled from
+// the queue, then its next step is launched.  Engines never wait for one
+// another, so a slow Bellman-Ford round does not hold back BFS levels.
+enum { E_BFS = 0, E_SSSP = 1, E_PPR = 2 };
+
+static int sv_poll(eg_server *s, int e, bool *ready) {
+    *ready = false;
+    if (!s->inflight[e]) return EG_OK;
+    const cudaError_t q = cudaEventQuery(s->ev_end[e]);
+    if (q == cudaErrorNotReady) return EG_OK;
+    if (q != cudaSuccess) return eg_fail(EG_ECUDA, "server engine %d: %s", e, cudaGetErrorString(q));
+    float ms = 0.f;
+    EG_CUDA(cudaEventElapsedTime(&ms, s->ev_begin[e], s->ev_end[e]));
+    s->eng_ms[e] += ms;
+    s->eng_steps[e]++;
+    s->inflight[e] = false;
+    *ready = true;
+    return EG_OK;
+}
+
+// ---- BFS
+static int sv_bfs_retire(eg_server *s, unsigned long long done) {
     eg_graph *g = s->g;
     eg_ctx *ctx = g->ctx;
-    EG_CUDA(cudaSetDevice(ctx->device));
     const uint32_t n = g->n;
-    const double m = (double)g->m;
-    const uint32_t nw = (n + 31) / 32;
-    unsigned char *small = bp<unsigned char>(s->small);
-    SvCounters *bcnt = (SvCounters *)small, *scnt = (SvCounters *)(small + 256);
-    uint32_t *adm_roots = (uint32_t *)(small + 1024), *adm_slots = (uint32_t *)(small + 2048);
-    int32_t *d_slot_level = (int32_t *)(small + 3072);
-    PprQ *d_ppr = (PprQ *)(small + 4096);                 // 32 x PprQ
-    uint32_t *d_pseeds = (uint32_t *)(small + 8192);      // 8 per lane
-    uint32_t *d_sbeg = (uint32_t *)(small + 9216), *d_send = (uint32_t *)(small + 9344);
-    unsigned long long *d_sum = (unsigned long long *)(small + 12544);
-    unsigned char *hs = (unsigned char *)ctx->h_pinned;
-    s->ticks++;
-
-    // ---------------- admission (FIFO per kind into free slots)
-    std::vector<uint32_t> broots, bslots, sroots, sslots;
-    uint32_t new_ppr = 0;
-    PprQ ppr_new[SV_PPR_LANES];
-    uint32_t ppr_seeds_new[SV_PPR_LANES][8];
-    for (auto it = s->queue.begin(); it != s->queue.end();) {
-        const eg_query &q = it->q;
-        bool took = false;
-        const double tnow = now_s() - s->t0;
-        if (q.kind == EG_Q_BFS) {
-            for (int sl = 0; sl < s->bfs_cap; sl++)
-                if (!((s->bfs_seen_mask >> sl) & 1ull) && std::find(bslots.begin(), bslots.end(), (uint32_t)sl) == bslots.end()) {
-                    broots.push_back(q.source);
-                    bslots.push_back((uint32_t)sl);
-                    s->bfs_id[sl] = it->id;
-                    s->bfs_arrival[sl] = q.arrival_s;
-                    s->bfs_admit[sl] = tnow;
-                    took = true;
-                    break;
-                }
-        } else if (q.kind == EG_Q_SSSP) {
-            for (int sl = 0; sl < s->sssp_cap; sl++)
-                if (!((s->sssp_mask >> sl) & 1ull) && std::find(sslots.begin(), sslots.end(), (uint32_t)sl) == sslots.end()) {
-                    sroots.push_back(q.source);
-                    sslots.push_back((uint32_t)sl);
-                    s->sssp_id[sl] = it->id;
-                    s->sssp_arrival[sl] = q.arrival_s;
-                    s->sssp_admit[sl] = tnow;
-                    s->sssp_rounds[sl] = 0;
-                    took = true;
-                    break;
-                }
-        } else {
-            for (int sl = 0; sl < s->ppr_cap; sl++)
-                if (!((s->ppr_mask >> sl) & 1u) && !((new_ppr >> sl) & 1u)) {
-                    PprQ &p = ppr_new[sl];
-                    memset(&p, 0, sizeof(p));
-                    p.tol = q.tol > 0 ? q.tol : 1e-6f;
-                    p.max_iters = s->opts.ppr_max_iters;
-                    p.active = 1;
-                    p.nseeds = (int)q.nseeds;
-                    for (uint32_t k = 0; k < q.nseeds; k++) ppr_seeds_new[sl][k] = q.seeds[k];
-                    new_ppr |= 1u << sl;
-                    s->ppr_id[sl] = it->id;
-                    s->ppr_arrival[sl] = q.arrival_s;
-                    s->ppr_admit[sl] = tnow;
-                    took = true;
-                    break;
-                }
+    cudaStream_t st = s->st[E_BFS];
+    unsigned long long *seen = bp<unsigned long long>(s->bfs_buf);
+    unsigned long long *front = seen + n;
+    int32_t *levels = reinterpret_cast<int32_t *>(reinterpret_cast<uint32_t *>(seen + 3ull * n) + 2ull * n);
+    unsigned long long *d_sum = (unsigned long long *)(bp<unsigned char>(s->small) + SM_SUM);
+    unsigned long long *hsum = (unsigned long long *)(s->hpin + HP_SUM);
+    for (int sl = 0; sl < SV_BFS_SLOTS; sl++) {
+        if (!((done >> sl) & 1ull)) continue;
+        int32_t *row = levels + (uint64_t)sl * n;
+        EG_CUDA(cudaMemsetAsync(d_sum, 0, 16, st));
+        k_sv_level_summary<<<sv_blocks(ctx, n), 256, 0, st>>>(row, n, d_sum);
+        EG_LAUNCHED(ctx);
+        EG_CUDA(cudaMemcpyAsync(hsum, d_sum, 16, cudaMemcpyDeviceToHost, st));
+        std::vector<uint32_t> keep;
+        if (s->opts.keep_results) {
+            keep.resize(n);
+            EG_CUDA(cudaMemcpyAsync(keep.data(), row, (uint64_t)n * 4, cudaMemcpyDeviceToHost, st));
         }
-        if (took) it = s->queue.erase(it);
-        else ++it;
+        EG_CUDA(cudaStreamSynchronize(st));
+        sv_finish(s, s->bfs_id[sl], EG_Q_BFS, s->bfs_arrival[sl], s->bfs_admit[sl], (uint32_t)hsum[0],
+                  (uint32_t)hsum[1], s->bfs_level[sl] - 1, 0.0);
+        if (s->opts.keep_results) s->kept.push_back(std::move(keep));
+        EG_CUDA(cudaMemsetAsync(row, 0, (uint64_t)n * 4, st));
+    }
+    k_sv_bfs_clear<<<sv_blocks(ctx, n), 256, 0, st>>>(n, ~done, seen, front);
+    EG_LAUNCHED(ctx);
+    s->bfs_seen_mask &= ~done;
+    return EG_OK;
+}
+
+static int sv_bfs_advance(eg_server *s, bool *progress) {
+    bool ready;
+    EG_TRY(sv_poll(s, E_BFS, &ready));
+    if (ready) {
+        const SvCounters *hc = (const SvCounters *)(s->hpin + HP_BCNT);
+        const unsigned long long live = s->step_mask[E_BFS];
+        s->bfs_count = hc->count;
+        s->bfs_fdeg = hc->deg;
+        for (int sl = 0; sl < SV_BFS_SLOTS; sl++)
+            if ((live >> sl) & 1ull) s->bfs_level[sl] += 1;
+        const unsigned long long done = live & ~hc->newmask;  // no discovery this level: finished
+        if (done) EG_TRY(sv_bfs_retire(s, done));
+        *progress = true;
+    }
+    if (s->inflight[E_BFS]) return EG_OK;
+    eg_graph *g = s->g;
+    eg_ctx *ctx = g->ctx;
+    const uint32_t n = g->n;
+    cudaStream_t st = s->st[E_BFS];
+    unsigned char *small = bp<unsigned char>(s->small);
+    SvCounters *bcnt = (SvCounters *)(small + SM_BCNT);
+    // admission: FIFO into free slots
+    uint32_t *hroots = (uint32_t *)(s->hpin + HP_BADM), *hslots = hroots + 64;
+    int nadm = 0;
+    unsigned long long taken = 0;
+    const double tnow = now_s() - s->t0;
+    for (auto it = s->queue.begin(); it != s->queue.end();) {
+        if (it->q.kind != EG_Q_BFS) {
+            ++it;
+            continue;
+        }
+        int sl = 0;
+        while (sl < s->bfs_cap && (((s->bfs_seen_mask | taken) >> sl) & 1ull)) sl++;
+        if (sl >= s->bfs_cap) break;
+        taken |= 1ull << sl;
+        hroots[nadm] = it->q.source;
+        hslots[nadm] = (uint32_t)sl;
+        nadm++;
+        s->bfs_id[sl] = it->id;
+        s->bfs_arrival[sl] = it->q.arrival_s;
+        s->bfs_admit[sl] = tnow;
+        it = s->queue.erase(it);
     }
     unsigned long long *seen = bp<unsigned long long>(s->bfs_buf);
     unsigned long long *front = seen + n, *next = seen + 2ull * n;
     uint32_t *bq = reinterpret_cast<uint32_t *>(seen + 3ull * n), *bbig = bq + n;
     int32_t *levels = reinterpret_cast<int32_t *>(bbig + n);
     const uint32_t *deg = bp<uint32_t>(g->out_deg);
-    // ---------------- BFS: admit, then one level for all live slots
-    if (!broots.empty()) {
-        EG_CUDA(cudaMemcpyAsync(adm_roots, broots.data(), broots.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-        EG_CUDA(cudaMemcpyAsync(adm_slots, bslots.data(), bslots.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-        k_sv_bfs_admit<<<1, 64, 0, ctx->stream>>>(adm_roots, adm_slots, (int)broots.size(), n, seen, front, levels);
+    if (nadm) {
+        EG_CUDA(cudaMemcpyAsync(small + SM_BROOTS, hroots, (uint64_t)nadm * 4, cudaMemcpyHostToDevice, st));
+        EG_CUDA(cudaMemcpyAsync(small + SM_BSLOTS, hslots, (uint64_t)nadm * 4, cudaMemcpyHostToDevice, st));
+        k_sv_bfs_admit<<<1, 64, 0, st>>>((const uint32_t *)(small + SM_BROOTS), (const uint32_t *)(small + SM_BSLOTS), nadm,
+                                         n, seen, front, levels);
         EG_LAUNCHED(ctx);
-        for (size_t i = 0; i < bslots.size(); i++) {
-            s->bfs_seen_mask |= 1ull << bslots[i];
-            s->bfs_level[bslots[i]] = 1;
+        for (int i = 0; i < nadm; i++) {
+            s->bfs_seen_mask |= 1ull << hslots[i];
+            s->bfs_level[hslots[i]] = 1;
             s->bfs_fdeg += 1;  // keeps the first step of new roots in push mode unless the frontier is large
         }
+        s->admitted[E_BFS] += nadm;
+        *progress = true;
     }
     const unsigned long long live = s->bfs_seen_mask;
-    unsigned long long bfs_done = 0;
-    if (live) {
-        EG_CUDA(cudaMemcpyAsync(d_slot_level, s->bfs_level, sizeof(s->bfs_level), cudaMemcpyHostToDevice, ctx->stream));
-        EG_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(SvCounters), ctx->stream));
-        const bool pull = (double)s->bfs_count + (double)s->bfs_fdeg > m / 20.0;
-        if (pull) {
-            k_msp_light<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), bp<uint32_t>(g->csc.col),
-                                                                   n, live, seen, front, next, bbig, &bcnt->nbig);
-            EG_LAUNCHED(ctx);
-            k_msp_heavy<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
-                bp<uint32_t>(g->csc.ptr), bp<uint32_t>(g->csc.col), live, seen, front, next, bbig, &bcnt->nbig);
-            EG_LAUNCHED(ctx);
-        } else {
-            k_sv_front_queue<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(front, n, bq, bcnt);
-            EG_LAUNCHED(ctx);
-            k_sv_bfs_push<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr),
-                                                                               bp<uint32_t>(g->csr.col), bq, bcnt,
-                                                                               seen, front, next, bbig, bcnt);
-            EG_LAUNCHED(ctx);
-            k_sv_bfs_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, ctx->stream>>>(
-                bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), bbig, seen, front, next, bcnt);
-            EG_LAUNCHED(ctx);
-            EG_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(SvCounters), ctx->stream));
-        }
-        k_sv_bfs_fold<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(n, seen, front, next, levels, d_slot_level, deg, bcnt);
+    if (!live) return EG_OK;
+    int32_t *hlev = (int32_t *)(s->hpin + HP_BLEVEL);
+    memcpy(hlev, s->bfs_level, sizeof(s->bfs_level));
+    EG_CUDA(cudaEventRecord(s->ev_begin[E_BFS], st));
+    EG_CUDA(cudaMemcpyAsync(small + SM_BLEVEL, hlev, sizeof(s->bfs_level), cudaMemcpyHostToDevice, st));
+    EG_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(SvCounters), st));
+    const bool pull = (double)s->bfs_count + (double)s->bfs_fdeg > (double)g->m / 20.0;
+    if (pull) {
+        k_msp_light<<<sv_blocks(ctx, n), 256, 0, st>>>(bp<uint32_t>(g->csc.ptr), bp<uint32_t>(g->csc.col), n, live, seen,
+                                                       front, next, bbig, &bcnt->nbig);
         EG_LAUNCHED(ctx);
-        SvCounters *hc = (SvCounters *)hs;
-        EG_CUDA(cudaMemcpyAsync(hc, bcnt, sizeof(SvCounters), cudaMemcpyDeviceToHost, ctx->stream));
-        EG_CUDA(cudaStreamSynchronize(ctx->stream));
-        s->bfs_count = hc->count;
-        s->bfs_fdeg = hc->deg;
-        for (int sl = 0; sl < SV_BFS_SLOTS; sl++)
-            if ((live >> sl) & 1ull) s->bfs_level[sl] += 1;
-        bfs_done = live & ~hc->newmask;  // no discovery this level: finished
+        k_msp_heavy<<<(uint32_t)ctx->sm_count * 8, 256, 0, st>>>(bp<uint32_t>(g->csc.ptr), bp<uint32_t>(g->csc.col), live,
+                                                                 seen, front, next, bbig, &bcnt->nbig);
+        EG_LAUNCHED(ctx);
+    } else {
+        k_sv_front_queue<<<sv_blocks(ctx, n), 256, 0, st>>>(front, n, bq, bcnt);
+        EG_LAUNCHED(ctx);
+        k_sv_bfs_push<<<(uint32_t)ctx->sm_count * 8, 256, 0, st>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), bq,
+                                                                   bcnt, seen, front, next, bbig, bcnt);
+        EG_LAUNCHED(ctx);
+        k_sv_bfs_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, st>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col),
+                                                                       bbig, seen, front, next, bcnt);
+        EG_LAUNCHED(ctx);
     }
-    // ---------------- SSSP: admit, then one round for all live slots
+    EG_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(SvCounters), st));
+    k_sv_bfs_fold<<<sv_blocks(ctx, n), 256, 0, st>>>(n, seen, front, next, levels, (const int32_t *)(small + SM_BLEVEL),
+                                                     deg, bcnt);
+    EG_LAUNCHED(ctx);
+    EG_CUDA(cudaMemcpyAsync(s->hpin + HP_BCNT, bcnt, sizeof(SvCounters), cudaMemcpyDeviceToHost, st));
+    EG_CUDA(cudaEventRecord(s->ev_end[E_BFS], st));
+    s->inflight[E_BFS] = true;
+    s->step_mask[E_BFS] = live;
+    *progress = true;
+    return EG_OK;
+}
+
+// ---- SSSP
+static int sv_sssp_retire(eg_server *s, unsigned long long done) {
+    eg_graph *g = s->g;
+    eg_ctx *ctx = g->ctx;
+    const uint32_t n = g->n;
+    cudaStream_t st = s->st[E_SSSP];
+    uint32_t *dist = bp<uint32_t>(s->sssp_buf);
+    unsigned long long *d_sum = (unsigned long long *)(bp<unsigned char>(s->small) + SM_SUM + 64);
+    unsigned long long *hsum = (unsigned long long *)(s->hpin + HP_SUM + 64);
+    for (int sl = 0; sl < SV_SSSP_SLOTS; sl++) {
+        if (!((done >> sl) & 1ull)) continue;
+        EG_CUDA(cudaMemsetAsync(d_sum, 0, 16, st));
+        k_sv_dist_summary<<<sv_blocks(ctx, n), 256, 0, st>>>(dist, n, (uint32_t)sl, d_sum);
+        EG_LAUNCHED(ctx);
+        EG_CUDA(cudaMemcpyAsync(hsum, d_sum, 16, cudaMemcpyDeviceToHost, st));
+        std::vector<uint32_t> keep;
+        if (s->opts.keep_results) {
+            keep.resize(n);
+            EG_TRY(eg_buf_ensure(ctx, g->spmv_y, (uint64_t)n * 8));
+            uint32_t *col = bp<uint32_t>(g->spmv_y);
+            k_sv_column<<<sv_blocks(ctx, n), 256, 0, st>>>(dist, n, SV_SSSP_SLOTS, (uint32_t)sl, col);
+            EG_LAUNCHED(ctx);
+            EG_CUDA(cudaMemcpyAsync(keep.data(), col, (uint64_t)n * 4, cudaMemcpyDeviceToHost, st));
+        }
+        EG_CUDA(cudaStreamSynchronize(st));
+        sv_finish(s, s->sssp_id[sl], EG_Q_SSSP, s->sssp_arrival[sl], s->sssp_admit[sl], (uint32_t)hsum[0],
+                  (uint32_t)hsum[1], s->sssp_rounds[sl], 0.0);
+        if (s->opts.keep_results) s->kept.push_back(std::move(keep));
+    }
+    k_sv_sssp_reset<<<sv_blocks(ctx, (uint64_t)n * SV_SSSP_SLOTS), 256, 0, st>>>(n, done, dist);
+    EG_LAUNCHED(ctx);
+    s->sssp_mask &= ~done;
+    return EG_OK;
+}
+
+static int sv_sssp_advance(eg_server *s, bool *progress) {
+    bool ready;
+    EG_TRY(sv_poll(s, E_SSSP, &ready));
+    if (ready) {
+        const SvCounters *hc = (const SvCounters *)(s->hpin + HP_SCNT);
+        const unsigned long long live = s->step_mask[E_SSSP];
+        const unsigned long long still = hc->actmask[0] | (hc->actmask[1] << 32);
+        for (int sl = 0; sl < SV_SSSP_SLOTS; sl++)
+            if ((live >> sl) & 1ull) s->sssp_rounds[sl] += 1;
+        const unsigned long long done = live & ~still;
+        if (done) EG_TRY(sv_sssp_retire(s, done));
+        *progress = true;
+    }
+    if (s->inflight[E_SSSP]) return EG_OK;
+    eg_graph *g = s->g;
+    eg_ctx *ctx = g->ctx;
+    const uint32_t n = g->n, nw = (n + 31) / 32;
+    cudaStream_t st = s->st[E_SSSP];
+    unsigned char *small = bp<unsigned char>(s->small);
+    SvCounters *scur = (SvCounters *)(small + SM_SCNT), *snext = (SvCounters *)(small + SM_SNEXT);
     uint32_t *dist = bp<uint32_t>(s->sssp_buf);
     uint32_t *act0 = dist + (uint64_t)n * SV_SSSP_SLOTS, *act1 = act0 + 2ull * n;
     uint32_t *inq0 = act1 + 2ull * n, *inq1 = inq0 + nw;
-    uint32_t *sq0 = inq1 + nw, *sq1 = sq0 + n, *sbig = sq1 + n;
+    uint32_t *sq0 = inq1 + nw, *sq1 = sq0 + n, *sbig = sq1 + n, *sbigoff = sbig + n;
     uint32_t *act[2] = {act0, act1}, *inq[2] = {inq0, inq1}, *sq[2] = {sq0, sq1};
-    SvCounters *scur = scnt, *snext = (SvCounters *)(small + 512);
-    // scnt holds the current queue size (qsize); snext collects the next one
-    if (!sroots.empty()) {
-        EG_CUDA(cudaMemcpyAsync(adm_roots + 128, sroots.data(), sroots.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-        EG_CUDA(cudaMemcpyAsync(adm_slots + 128, sslots.data(), sslots.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-        const int c = s->sssp_cur;
-        k_sv_sssp_admit<<<1, 64, 0, ctx->stream>>>(adm_roots + 128, adm_slots + 128, (int)sroots.size(), dist, act[c],
-                                                   inq[c], sq[c], scur);
-        EG_LAUNCHED(ctx);
-        for (size_t i = 0; i < sslots.size(); i++) s->sssp_mask |= 1ull << sslots[i];
+    uint32_t *hroots = (uint32_t *)(s->hpin + HP_SADM), *hslots = hroots + 64;
+    int nadm = 0;
+    unsigned long long taken = 0;
+    const double tnow = now_s() - s->t0;
+    for (auto it = s->queue.begin(); it != s->queue.end();) {
+        if (it->q.kind != EG_Q_SSSP) {
+            ++it;
+            continue;
+        }
+        int sl = 0;
+        while (sl < s->sssp_cap && (((s->sssp_mask | taken) >> sl) & 1ull)) sl++;
+        if (sl >= s->sssp_cap) break;
+        taken |= 1ull << sl;
+        hroots[nadm] = it->q.source;
+        hslots[nadm] = (uint32_t)sl;
+        nadm++;
+        s->sssp_id[sl] = it->id;
+        s->sssp_arrival[sl] = it->q.arrival_s;
+        s->sssp_admit[sl] = tnow;
+        s->sssp_rounds[sl] = 0;
+        it = s->queue.erase(it);
     }
-    unsigned long long sssp_done = 0;
-    if (s->sssp_mask) {
-        const int c = s->sssp_cur, nx = c ^ 1;
-        SvW w;
-        w.rule = s->opts.weights.rule;
-        w.seed = s->opts.weights.seed;
-        w.lo = s->opts.weights.lo;
-        w.span = (uint64_t)s->opts.weights.hi - s->opts.weights.lo + 1;
-        EG_CUDA(cudaMemsetAsync(snext, 0, sizeof(SvCounters), ctx->stream));
-        k_sv_sssp_push<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
-            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), sq[c], scur, dist, act[c], act[nx], inq[nx], sq[nx], w,
-            snext, sbig);
+    const int c = s->sssp_cur, nx = c ^ 1;
+    if (nadm) {
+        EG_CUDA(cudaMemcpyAsync(small + SM_SROOTS, hroots, (uint64_t)nadm * 4, cudaMemcpyHostToDevice, st));
+        EG_CUDA(cudaMemcpyAsync(small + SM_SSLOTS, hslots, (uint64_t)nadm * 4, cudaMemcpyHostToDevice, st));
+        k_sv_sssp_admit<<<1, 64, 0, st>>>((const uint32_t *)(small + SM_SROOTS), (const uint32_t *)(small + SM_SSLOTS),
+                                          nadm, dist, act[c], inq[c], sq[c], scur);
         EG_LAUNCHED(ctx);
-        k_sv_sssp_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, ctx->stream>>>(
-            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), dist, act[c], act[nx], inq[nx], sq[nx], w, snext, sbig);
-        EG_LAUNCHED(ctx);
-        k_sv_sssp_clear_frontier<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(sq[c], scur, act[c], inq[c]);
-        EG_LAUNCHED(ctx);
-        EG_CUDA(cudaMemcpyAsync(scur, snext, sizeof(SvCounters), cudaMemcpyDeviceToDevice, ctx->stream));
-        SvCounters *hc = (SvCounters *)(hs + 256);
-        EG_CUDA(cudaMemcpyAsync(hc, snext, sizeof(SvCounters), cudaMemcpyDeviceToHost, ctx->stream));
-        EG_CUDA(cudaStreamSynchronize(ctx->stream));
-        const unsigned long long still = hc->actmask[0] | (hc->actmask[1] << 32);
-        for (int sl = 0; sl < SV_SSSP_SLOTS; sl++)
-            if ((s->sssp_mask >> sl) & 1ull) s->sssp_rounds[sl] += 1;
-        sssp_done = s->sssp_mask & ~still;
-        s->sssp_cur = nx;
+        for (int i = 0; i < nadm; i++) s->sssp_mask |= 1ull << hslots[i];
+        s->admitted[E_SSSP] += nadm;
+        *progress = true;
     }
-    // ---------------- PPR: admit lanes, then one iteration for all live lanes
+    if (!s->sssp_mask) return EG_OK;
+    SvW w = eg_make_wrule(&s->opts.weights);
+    EG_CUDA(cudaEventRecord(s->ev_begin[E_SSSP], st));
+    EG_CUDA(cudaMemsetAsync(snext, 0, sizeof(SvCounters), st));
+    k_sv_sssp_push<<<(uint32_t)ctx->sm_count * 8, 256, 0, st>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), sq[c],
+                                                                scur, dist, act[c], act[nx], inq[nx], sq[nx], w, snext,
+                                                                sbig);
+    EG_LAUNCHED(ctx);
+    k_big_offsets<<<1, 1024, 0, st>>>(sbig, &snext->nbig, 2u, bp<uint32_t>(g->csr.ptr), SV_SSSP_CHUNK, sbigoff);
+    EG_LAUNCHED(ctx);
+    k_sv_sssp_push_big<<<(uint32_t)ctx->sm_count * 8, 256, 0, st>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col),
+                                                                    dist, act[c], act[nx], inq[nx], sq[nx], w, snext,
+                                                                    sbig, sbigoff);
+    EG_LAUNCHED(ctx);
+    k_sv_sssp_clear_frontier<<<sv_blocks(ctx, n), 256, 0, st>>>(sq[c], scur, act[c], inq[c]);
+    EG_LAUNCHED(ctx);
+    EG_CUDA(cudaMemcpyAsync(scur, snext, sizeof(SvCounters), cudaMemcpyDeviceToDevice, st));
+    EG_CUDA(cudaMemcpyAsync(s->hpin + HP_SCNT, snext, sizeof(SvCounters), cudaMemcpyDeviceToHost, st));
+    EG_CUDA(cudaEventRecord(s->ev_end[E_SSSP], st));
+    s->sssp_cur = nx;
+    s->inflight[E_SSSP] = true;
+    s->step_mask[E_SSSP] = s->sssp_mask;
+    *progress = true;
+    return EG_OK;
+}
+
+// ---- PPR
+static int sv_ppr_advance(eg_server *s, bool *progress) {
+    bool ready;
+    EG_TRY(sv_poll(s, E_PPR, &ready));
+    eg_graph *g = s->g;
+    eg_ctx *ctx = g->ctx;
+    const uint32_t n = g->n;
+    cudaStream_t st = s->st[E_PPR];
+    unsigned char *small = bp<unsigned char>(s->small);
+    PprQ *d_ppr = (PprQ *)(small + SM_PPRQ);
+    uint32_t *d_pseeds = (uint32_t *)(small + SM_PSEEDS);
+    uint32_t *d_sbeg = (uint32_t *)(small + SM_PSBEG), *d_send = (uint32_t *)(small + SM_PSEND);
     float *R = bp<float>(s->ppr_buf), *X = R + (uint64_t)n * EG_PPR_LANES, *Y = X + (uint64_t)n * EG_PPR_LANES;
-    const uint32_t pm = (uint32_t)g->m;
-    const uint32_t ptiles = pm ? eg_div_up(pm, EG_PPR_TILE) : 0;
-    float *phv = Y + (uint64_t)n * EG_PPR_LANES, *ptv = phv + (uint64_t)ptiles * EG_PPR_LANES;
-    uint32_t *phr = reinterpret_cast<uint32_t *>(ptv + (uint64_t)ptiles * EG_PPR_LANES);
-    double2 *ppart = reinterpret_cast<double2 *>(phr + ((ptiles + 63) & ~63u));
-    PprQ *hp = (PprQ *)(hs + 1024);
-    if (new_ppr) {
-        EG_CUDA(cudaMemcpyAsync(hp, d_ppr, sizeof(PprQ) * EG_PPR_LANES, cudaMemcpyDeviceToHost, ctx->stream));
-        EG_CUDA(cudaStreamSynchronize(ctx->stream));
-        uint32_t *hseeds = (uint32_t *)(hs + 4096), *hbeg = hseeds + 256, *hend = hbeg + 32;
-        EG_CUDA(cudaMemcpyAsync(hseeds, d_pseeds, 256 * 4, cudaMemcpyDeviceToHost, ctx->stream));
-        EG_CUDA(cudaStreamSynchronize(ctx->stream));
-        for (int q = 0; q < EG_PPR_LANES; q++) {
-            hbeg[q] = 8u * q;
-            if ((new_ppr >> q) & 1u) {
-                hp[q] = ppr_new[q];
-                for (int k = 0; k < hp[q].nseeds; k++) hseeds[8 * q + k] = ppr_seeds_new[q][k];
-            }
-            hend[q] = 8u * q + (hp[q].active ? (uint32_t)hp[q].nseeds : 0u);
-        }
-        EG_CUDA(cudaMemcpyAsync(d_ppr, hp, sizeof(PprQ) * EG_PPR_LANES, cudaMemcpyHostToDevice, ctx->stream));
-        EG_CUDA(cudaMemcpyAsync(d_pseeds, hseeds, 256 * 4, cudaMemcpyHostToDevice, ctx->stream));
-        EG_CUDA(cudaMemcpyAsync(d_sbeg, hbeg, 32 * 4, cudaMemcpyHostToDevice, ctx->stream));
-        EG_CUDA(cudaMemcpyAsync(d_send, hend, 32 * 4, cudaMemcpyHostToDevice, ctx->stream));
-        k_ppr_init<<<sv_blocks(ctx, (uint64_t)n * 32), 256, 0, ctx->stream>>>(n, new_ppr, R, X);
-        EG_LAUNCHED(ctx);
-        k_ppr_init_seeds<<<1, 32, 0, ctx->stream>>>(d_pseeds, d_sbeg, d_send, new_ppr, d_ppr, deg, R, X);
-        EG_LAUNCHED(ctx);
-        k_ppr_init_dangling<<<1, 32, 0, ctx->stream>>>(d_pseeds, d_sbeg, d_send, new_ppr, deg, R, d_ppr);
-        EG_LAUNCHED(ctx);
-        EG_CUDA(cudaStreamSynchronize(ctx->stream));  // the host staging above is reused below
-        s->ppr_mask |= new_ppr;
-    }
-    uint32_t ppr_done = 0;
-    if (s->ppr_mask) {
-        const uint32_t fb = (uint32_t)ctx->sm_count * 4;
-        const uint32_t rb = ptiles ? eg_div_up((uint64_t)ptiles * 32, 256) : 0;
-        if (rb) {
-            k_ppr_rows<<<rb, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.rid), bp<uint32_t>(g->csc.col), pm, ptiles, X, Y,
-                                                    phv, ptv, phr);
-            EG_LAUNCHED(ctx);
-            k_ppr_fixup<<<rb, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), ptiles, phr, phv, ptv, Y);
-            EG_LAUNCHED(ctx);
-        }
-        k_ppr_empty<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), n, Y);
-        EG_LAUNCHED(ctx);
-        k_ppr_seeds<<<1, 32, 0, ctx->stream>>>(d_pseeds, d_sbeg, d_send, 32, d_ppr, s->opts.ppr_damping, Y);
-        EG_LAUNCHED(ctx);
-        k_ppr_finish<<<fb, 256, 0, ctx->stream>>>(Y, deg, n, s->opts.ppr_damping, d_ppr, R, X, ppart);
-        EG_LAUNCHED(ctx);
-        k_ppr_reduce<<<1, 32, 0, ctx->stream>>>(ppart, fb, d_ppr, 1);
-        EG_LAUNCHED(ctx);
-        EG_CUDA(cudaMemcpyAsync(hp, d_ppr, sizeof(PprQ) * EG_PPR_LANES, cudaMemcpyDeviceToHost, ctx->stream));
-        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    PprQ *hp = s->hq;
+    bool upload = false;
+    if (ready) {
+        uint32_t done = 0;
         for (int q = 0; q < EG_PPR_LANES; q++)
-            if (hp[q].active && hp[q].done) ppr_done |= 1u << q;
-        ppr_done &= s->ppr_mask;
-    }
-    // ---------------- retire
-    if (bfs_done) {
-        for (int sl = 0; sl < SV_BFS_SLOTS; sl++) {
-            if (!((bfs_done >> sl) & 1ull)) continue;
-            int32_t *row = levels + (uint64_t)sl * n;
-            EG_CUDA(cudaMemsetAsync(d_sum, 0, 16, ctx->stream));
-            k_sv_level_summary<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(row, n, d_sum);
-            EG_LAUNCHED(ctx);
-            unsigned long long *hsum = (unsigned long long *)(hs + 9000 + 64);
-            EG_CUDA(cudaMemcpyAsync(hsum, d_sum, 16, cudaMemcpyDeviceToHost, ctx->stream));
-            std::vector<uint32_t> keep;
-            if (s->opts.keep_results) {
-                keep.resize(n);
-                EG_CUDA(cudaMemcpyAsync(keep.data(), row, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
-            }
-            EG_CUDA(cudaStreamSynchronize(ctx->stream));
-            sv_finish(s, s->bfs_id[sl], EG_Q_BFS, s->bfs_arrival[sl], s->bfs_admit[sl], (uint32_t)hsum[0],
-                      (uint32_t)hsum[1], s->bfs_level[sl] - 1, 0.0);
-            if (s->opts.keep_results) s->kept.push_back(std::move(keep));
-            EG_CUDA(cudaMemsetAsync(row, 0, (uint64_t)n * 4, ctx->stream));
-        }
-        k_sv_bfs_clear<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(n, ~bfs_done, seen, front);
-        EG_LAUNCHED(ctx);
-        s->bfs_seen_mask &= ~bfs_done;
-    }
-    if (sssp_done) {
-        for (int sl = 0; sl < SV_SSSP_SLOTS; sl++) {
-            if (!((sssp_done >> sl) & 1ull)) continue;
-            EG_CUDA(cudaMemsetAsync(d_sum, 0, 16, ctx->stream));
-            k_sv_dist_summary<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(dist, n, (uint32_t)sl, d_sum);
-            EG_LAUNCHED(ctx);
-            unsigned long long *hsum = (unsigned long long *)(hs + 9000 + 64);
-            EG_CUDA(cudaMemcpyAsync(hsum, d_sum, 16, cudaMemcpyDeviceToHost, ctx->stream));
-            std::vector<uint32_t> keep;
-            if (s->opts.keep_results) {
-                keep.resize(n);
-                uint32_t *col = bp<uint32_t>(g->spmv_y);
-                EG_TRY(eg_buf_ensure(ctx, g->spmv_y, (uint64_t)n * 8));
-                col = bp<uint32_t>(g->spmv_y);
-                k_sv_column<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(dist, n, SV_SSSP_SLOTS, (uint32_t)sl, col);
-                EG_LAUNCHED(ctx);
-                EG_CUDA(cudaMemcpyAsync(keep.data(), col, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
-            }
-            EG_CUDA(cudaStreamSynchronize(ctx->stream));
-            sv_finish(s, s->sssp_id[sl], EG_Q_SSSP, s->sssp_arrival[sl], s->sssp_admit[sl], (uint32_t)hsum[0],
-                      (uint32_t)hsum[1], s->sssp_rounds[sl], 0.0);
-            if (s->opts.keep_results) s->kept.push_back(std::move(keep));
-        }
-        k_sv_sssp_reset<<<sv_blocks(ctx, (uint64_t)n * SV_SSSP_SLOTS), 256, 0, ctx->stream>>>(n, sssp_done, dist);
-        EG_LAUNCHED(ctx);
-        s->sssp_mask &= ~sssp_done;
-    }
-    if (ppr_done) {
+            if (((s->ppr_mask >> q) & 1u) && hp[q].active && hp[q].done) done |= 1u << q;
         for (int q = 0; q < EG_PPR_LANES; q++) {
-            if (!((ppr_done >> q) & 1u)) continue;
-            double *dsum = reinterpret_cast<double *>(d_sum);
-            EG_CUDA(cudaMemsetAsync(dsum, 0, 16, ctx->stream));
+            if (!((done >> q) & 1u)) continue;
+            double *dsum = (double *)(small + SM_SUM + 128);
+            double *hsum = (double *)(s->hpin + HP_SUM + 128);
+            EG_CUDA(cudaMemsetAsync(dsum, 0, 16, st));
             std::vector<uint32_t> keep;
             float *col = nullptr;
             if (s->opts.keep_results) {
@@ -819,24 +880,137 @@ extern "C" int eg_serve_step(eg_server *s, int *active_out) {
                 EG_TRY(eg_buf_ensure(ctx, g->spmv_y, (uint64_t)n * 8));
                 col = bp<float>(g->spmv_y);
             }
-            k_sv_ppr_column<<<sv_blocks(ctx, n), 256, 0, ctx->stream>>>(R, n, (uint32_t)q, col, dsum);
+            k_sv_ppr_column<<<sv_blocks(ctx, n), 256, 0, st>>>(R, n, (uint32_t)q, col, dsum);
             EG_LAUNCHED(ctx);
-            double *hsum = (double *)(hs + 9000 + 64);
-            EG_CUDA(cudaMemcpyAsync(hsum, dsum, 8, cudaMemcpyDeviceToHost, ctx->stream));
-            if (col) EG_CUDA(cudaMemcpyAsync(keep.data(), col, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
-            EG_CUDA(cudaStreamSynchronize(ctx->stream));
+            EG_CUDA(cudaMemcpyAsync(hsum, dsum, 8, cudaMemcpyDeviceToHost, st));
+            if (col) EG_CUDA(cudaMemcpyAsync(keep.data(), col, (uint64_t)n * 4, cudaMemcpyDeviceToHost, st));
+            EG_CUDA(cudaStreamSynchronize(st));
             sv_finish(s, s->ppr_id[q], EG_Q_PPR, s->ppr_arrival[q], s->ppr_admit[q], 0u, 0u, hp[q].iters, *hsum);
             if (s->opts.keep_results) s->kept.push_back(std::move(keep));
             hp[q].active = 0;
             hp[q].done = 0;
+            s->pnseeds[q] = 0;
         }
-        EG_CUDA(cudaMemcpyAsync(d_ppr, hp, sizeof(PprQ) * EG_PPR_LANES, cudaMemcpyHostToDevice, ctx->stream));
-        EG_CUDA(cudaStreamSynchronize(ctx->stream));
-        s->ppr_mask &= ~ppr_done;
+        s->ppr_mask &= ~done;
+        upload = done != 0;
+        *progress = true;
+    }
+    if (s->inflight[E_PPR]) return EG_OK;
+    uint32_t new_ppr = 0;
+    const double tnow = now_s() - s->t0;
+    for (auto it = s->queue.begin(); it != s->queue.end();) {
+        if (it->q.kind != EG_Q_PPR) {
+            ++it;
+            continue;
+        }
+        int sl = 0;
+        while (sl < s->ppr_cap && (((s->ppr_mask | new_ppr) >> sl) & 1u)) sl++;
+        if (sl >= s->ppr_cap) break;
+        const eg_query &q = it->q;
+        PprQ &p = hp[sl];
+        memset(&p, 0, sizeof(p));
+        p.tol = q.tol > 0 ? q.tol : 1e-6f;
+        p.max_iters = s->opts.ppr_max_iters;
+        p.active = 1;
+        p.nseeds = (int)q.nseeds;
+        for (uint32_t k = 0; k < q.nseeds; k++) s->pseeds[8 * sl + k] = q.seeds[k];
+        s->pnseeds[sl] = q.nseeds;
+        new_ppr |= 1u << sl;
+        s->ppr_id[sl] = it->id;
+        s->ppr_arrival[sl] = q.arrival_s;
+        s->ppr_admit[sl] = tnow;
+        it = s->queue.erase(it);
+    }
+    if (new_ppr || upload) {
+        uint32_t *hseeds = (uint32_t *)(s->hpin + HP_PSEEDS), *hbeg = hseeds + 256, *hend = hbeg + 32;
+        for (int q = 0; q < EG_PPR_LANES; q++) {
+            hbeg[q] = 8u * q;
+            hend[q] = 8u * q + (hp[q].active ? s->pnseeds[q] : 0u);
+            for (int k = 0; k < 8; k++) hseeds[8 * q + k] = s->pseeds[8 * q + k];
+        }
+        EG_CUDA(cudaMemcpyAsync(d_ppr, hp, sizeof(PprQ) * EG_PPR_LANES, cudaMemcpyHostToDevice, st));
+        EG_CUDA(cudaMemcpyAsync(d_pseeds, hseeds, 256 * 4, cudaMemcpyHostToDevice, st));
+        EG_CUDA(cudaMemcpyAsync(d_sbeg, hbeg, 32 * 4, cudaMemcpyHostToDevice, st));
+        EG_CUDA(cudaMemcpyAsync(d_send, hend, 32 * 4, cudaMemcpyHostToDevice, st));
+    }
+    const uint32_t *deg = bp<uint32_t>(g->out_deg);
+    if (new_ppr) {
+        k_ppr_init<<<sv_blocks(ctx, (uint64_t)n * 32), 256, 0, st>>>(n, new_ppr, R, X);
+        EG_LAUNCHED(ctx);
+        k_ppr_init_seeds<<<1, 32, 0, st>>>(d_pseeds, d_sbeg, d_send, new_ppr, d_ppr, deg, R, X);
+        EG_LAUNCHED(ctx);
+        k_ppr_init_dangling<<<1, 32, 0, st>>>(d_pseeds, d_sbeg, d_send, new_ppr, deg, R, d_ppr);
+        EG_LAUNCHED(ctx);
+        s->ppr_mask |= new_ppr;
+        s->admitted[E_PPR] += __builtin_popcount(new_ppr);
+        *progress = true;
+    }
+    if (!s->ppr_mask) return EG_OK;
+    const uint32_t pm = (uint32_t)g->m;
+    const uint32_t ptiles = pm ? eg_div_up(pm, EG_PPR_TILE) : 0;
+    float *phv = Y + (uint64_t)n * EG_PPR_LANES, *ptv = phv + (uint64_t)ptiles * EG_PPR_LANES;
+    uint32_t *phr = reinterpret_cast<uint32_t *>(ptv + (uint64_t)ptiles * EG_PPR_LANES);
+    double2 *ppart = reinterpret_cast<double2 *>(phr + ((ptiles + 63) & ~63u));
+    const uint32_t fb = (uint32_t)ctx->sm_count * 4;
+    const uint32_t rb = ptiles ? eg_div_up((uint64_t)ptiles * 32, 256) : 0;
+    EG_CUDA(cudaEventRecord(s->ev_begin[E_PPR], st));
+    if (rb) {
+        k_ppr_rows<<<rb, 256, 0, st>>>(bp<uint32_t>(g->csc.rid), bp<uint32_t>(g->csc.col), pm, ptiles, X, Y, phv, ptv, phr);
+        EG_LAUNCHED(ctx);
+        k_ppr_fixup<<<rb, 256, 0, st>>>(bp<uint32_t>(g->csc.ptr), ptiles, phr, phv, ptv, Y);
+        EG_LAUNCHED(ctx);
+    }
+    k_ppr_empty<<<(uint32_t)ctx->sm_count * 8, 256, 0, st>>>(bp<uint32_t>(g->csc.ptr), n, Y);
+    EG_LAUNCHED(ctx);
+    k_ppr_seeds<<<1, 32, 0, st>>>(d_pseeds, d_sbeg, d_send, 32, d_ppr, s->opts.ppr_damping, Y);
+    EG_LAUNCHED(ctx);
+    k_ppr_finish<<<fb, 256, 0, st>>>(Y, deg, n, s->opts.ppr_damping, d_ppr, R, X, ppart);
+    EG_LAUNCHED(ctx);
+    k_ppr_reduce<<<1, 32, 0, st>>>(ppart, fb, d_ppr, 1);
+    EG_LAUNCHED(ctx);
+    EG_CUDA(cudaMemcpyAsync(hp, d_ppr, sizeof(PprQ) * EG_PPR_LANES, cudaMemcpyDeviceToHost, st));
+    EG_CUDA(cudaEventRecord(s->ev_end[E_PPR], st));
+    s->inflight[E_PPR] = true;
+    s->step_mask[E_PPR] = s->ppr_mask;
+    *progress = true;
+    return EG_OK;
+}
+
+// One scheduler pass: every engine whose step has finished is retired,
+// refilled and relaunched.  When no engine was ready the call waits briefly
+// (about a millisecond at most) so that a polling caller does not spin the host.
+extern "C" int eg_serve_step(eg_server *s, int *active_out) {
+    if (!s) return eg_fail(EG_EINVAL, "NULL server");
+    EG_CUDA(cudaSetDevice(s->g->ctx->device));
+    s->ticks++;
+    bool progress = false;
+    for (int spin = 0; spin < 20 && !progress; spin++) {
+        EG_TRY(sv_bfs_advance(s, &progress));
+        EG_TRY(sv_sssp_advance(s, &progress));
+        EG_TRY(sv_ppr_advance(s, &progress));
+        if (!progress) {
+            if (!s->inflight[E_BFS] && !s->inflight[E_SSSP] && !s->inflight[E_PPR]) break;  // idle
+            struct timespec ts = {0, 1000};
+            nanosleep(&ts, nullptr);
+        }
     }
     if (active_out)
         *active_out = __builtin_popcountll(s->bfs_seen_mask) + __builtin_popcountll(s->sssp_mask) +
                       __builtin_popcount(s->ppr_mask) + (int)s->queue.size();
+    return EG_OK;
+}
+
+extern "C" int eg_serve_stats(eg_server *s, eg_serve_stats_t *out) {
+    if (!s || !out) return eg_fail(EG_EINVAL, "NULL argument");
+    memset(out, 0, sizeof(*out));
+    out->ticks = s->ticks;
+    for (int e = 0; e < 3; e++) {
+        out->engine_ms[e] = s->eng_ms[e];
+        out->engine_steps[e] = s->eng_steps[e];
+        out->admitted[e] = s->admitted[e];
+        out->completed[e] = s->completed[e];
+    }
+    out->queued = s->queue.size();
     return EG_OK;
 }
 

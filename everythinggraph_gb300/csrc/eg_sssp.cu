@@ -12,6 +12,8 @@
 #include <stdlib.h>
 
 #include "eg_internal.cuh"
+#include "eg_bigwork.cuh"
+#include "eg_mrelax.cuh"
 
 namespace {
 
@@ -62,21 +64,27 @@ __device__ __forceinline__ void sssp_append(bool q, uint32_t v, uint32_t *next_q
     }
 }
 
-// Relaxes the deferred high-degree frontier vertices with every thread.
+// Relaxes the deferred high-degree frontier vertices: chunks of
+// EG_SSSP_CHUNK edges shared out over the grid (one CTA per chunk).
+#define EG_SSSP_CHUNK 2048u
 __global__ void __launch_bounds__(256) k_sssp_push_big(const uint32_t *__restrict__ ptr,
                                                        const uint32_t *__restrict__ col, const uint32_t *big,
-                                                       uint32_t *dist, uint32_t *next_bm, uint32_t *next_queue,
-                                                       WRule w, SsspCounters *cnt) {
+                                                       const uint32_t *__restrict__ bigoff, uint32_t *dist,
+                                                       uint32_t *next_bm, uint32_t *next_queue, WRule w,
+                                                       SsspCounters *cnt) {
     const uint32_t nbig = *(volatile uint32_t *)&cnt->nbig;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nthreads = gridDim.x * blockDim.x;
+    if (!nbig) return;
+    const uint32_t total = bigoff[nbig];
     unsigned long long scanned = 0;
-    for (uint32_t bi = 0; bi < nbig; bi++) {
-        const uint32_t u = big[bi];
+    for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
+        const uint32_t i = eg_big_item(bigoff, nbig, c);
+        const uint32_t u = big[i];
         const uint32_t du = __ldcg(dist + u);
-        const uint32_t b = ptr[u], e = ptr[u + 1];
-        if (tid == 0) scanned += e - b;
-        for (uint32_t p0 = b + (tid & ~31u); p0 < e; p0 += nthreads) {
+        const uint32_t vb = ptr[u], ve = ptr[u + 1];
+        const uint32_t b = vb + (c - bigoff[i]) * EG_SSSP_CHUNK;
+        const uint32_t e = ve - b > EG_SSSP_CHUNK ? b + EG_SSSP_CHUNK : ve;
+        if (threadIdx.x == 0) scanned += e - b;
+        for (uint32_t p0 = b + (threadIdx.x & ~31u); p0 < e; p0 += blockDim.x) {
             const uint32_t p = p0 + (threadIdx.x & 31);
             bool q = false;
             uint32_t v = 0;
@@ -165,10 +173,11 @@ extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wts, uint32
     const uint32_t n = g->n, nw = (n + 31) >> 5;
     const WRule w = eg_make_wrule(wts);
     EG_TRY(eg_buf_ensure(ctx, g->dist, (uint64_t)n * 4));
-    const uint64_t off_q0 = nw, off_q1 = off_q0 + n, off_big = off_q1 + n, off_cnt = (off_big + n + 7) & ~7ull;
+    const uint64_t off_q0 = nw, off_q1 = off_q0 + n, off_big = off_q1 + n, off_bigoff = off_big + n,
+                   off_cnt = (off_bigoff + n + 1 + 7) & ~7ull;
     EG_TRY(eg_buf_ensure(ctx, g->sssp_work, (off_cnt + 8) * 4));
     uint32_t *wk = bp<uint32_t>(g->sssp_work);
-    uint32_t *bm = wk, *q[2] = {wk + off_q0, wk + off_q1}, *big = wk + off_big;
+    uint32_t *bm = wk, *q[2] = {wk + off_q0, wk + off_q1}, *big = wk + off_big, *bigoff = wk + off_bigoff;
     SsspCounters *cnt = reinterpret_cast<SsspCounters *>(wk + off_cnt);
     SsspCounters *h = (SsspCounters *)ctx->h_pinned;
     uint32_t *dist = bp<uint32_t>(g->dist);
@@ -185,9 +194,12 @@ extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wts, uint32
         k_sssp_push<<<blocks_for(ctx, (uint64_t)qlen * 32), 256, 0, ctx->stream>>>(
             bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), q[cur], qlen, dist, bm, q[nxt], w, cnt, big);
         EG_LAUNCHED(ctx);
-        k_sssp_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr),
-                                                                              bp<uint32_t>(g->csr.col), big, dist, bm,
-                                                                              q[nxt], w, cnt);
+        k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, 1u, bp<uint32_t>(g->csr.ptr), EG_SSSP_CHUNK,
+                                                   bigoff);
+        EG_LAUNCHED(ctx);
+        k_sssp_push_big<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr),
+                                                                              bp<uint32_t>(g->csr.col), big, bigoff,
+                                                                              dist, bm, q[nxt], w, cnt);
         EG_LAUNCHED(ctx);
         EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(SsspCounters), cudaMemcpyDeviceToHost, ctx->stream));
         EG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -250,24 +262,17 @@ __global__ void k_msssp_roots(const uint32_t *roots, int k, uint32_t kw, uint32_
     }
 }
 
-// Relaxes the 32 sources of word j of frontier vertex u (du_lane: this lane's
-// source distance at u) along edge u->v; queues v when a distance dropped.
-__device__ __forceinline__ void msssp_edge(uint32_t u, uint32_t v, uint32_t j, uint32_t s, bool on, uint32_t du,
-                                           int k, uint32_t kw, const WRule &w, uint32_t *dist, uint32_t *next_act,
-                                           uint32_t *next_inq, uint32_t *next_queue, SsspCounters *cnt) {
-    bool improved = false;
-    if (on && v != u) {
-        const uint32_t nd = w.extend(du, u, v);
-        uint32_t *dp = dist + (uint64_t)v * k + s;
-        if (nd < __ldcg(dp)) improved = nd < atomicMin(dp, nd);
-    }
-    const uint32_t ball = __ballot_sync(EG_FULL_MASK, improved);
-    if (ball && (threadIdx.x & 31) == 0) {
+// Records v in the next frontier for the sources in `ball` of word j.
+struct MsSink {
+    uint32_t j, kw;
+    uint32_t *next_act, *next_inq, *next_queue;
+    SsspCounters *cnt;
+    __device__ __forceinline__ void operator()(uint32_t v, uint32_t ball) {
         atomicOr(next_act + (uint64_t)v * kw + j, ball);
         const uint32_t bit = 1u << (v & 31);
         if (!(atomicOr(next_inq + (v >> 5), bit) & bit)) next_queue[atomicAdd(&cnt->qsize, 1u)] = v;
     }
-}
+};
 
 __global__ void __launch_bounds__(256) k_msssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
                                                     const uint32_t *__restrict__ queue, uint32_t qlen, int k,
@@ -290,37 +295,45 @@ __global__ void __launch_bounds__(256) k_msssp_push(const uint32_t *__restrict__
         }
         const uint32_t s = j * 32 + lane;
         const bool on = (a >> lane) & 1u;
-        const uint32_t du = on ? __ldcg(dist + (uint64_t)u * k + s) : EG_SSSP_INF;
+        const uint32_t du = on ? __ldcg(dist + (uint64_t)u * k + s) : 0u;
         if (lane == 0) scanned += (e - b) * (unsigned long long)__popc(a);
-        for (uint32_t p = b; p < e; p++)
-            msssp_edge(u, col[p], j, s, on, du, k, kw, w, dist, next_act, next_inq, next_queue, cnt);
+        MsSink sink{j, kw, next_act, next_inq, next_queue, cnt};
+        eg_mrelax_span(u, b, e, col, w, on, du, s, (uint32_t)k, dist, sink);
     }
     if (lane == 0 && scanned) atomicAdd(&cnt->relax, scanned);
 }
 
-// The deferred (high-degree vertex, source word) items: every warp of the
-// grid takes every (total warps)-th edge of each item.
+// The deferred (high-degree vertex, source word) items: chunks of
+// EG_MSSSP_CHUNK edges shared out over the grid, one CTA per chunk, one warp
+// per 32 edges of it.
+#define EG_MSSSP_CHUNK 256u
 __global__ void __launch_bounds__(256) k_msssp_push_big(const uint32_t *__restrict__ ptr,
                                                         const uint32_t *__restrict__ col, int k, uint32_t kw,
                                                         uint32_t *dist, const uint32_t *__restrict__ act,
                                                         uint32_t *next_act, uint32_t *next_inq, uint32_t *next_queue,
-                                                        WRule w, SsspCounters *cnt, const uint32_t *big) {
+                                                        WRule w, SsspCounters *cnt, const uint32_t *big,
+                                                        const uint32_t *__restrict__ bigoff) {
     const uint32_t nbig = *(volatile uint32_t *)&cnt->nbig;
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    if (!nbig) return;
+    const uint32_t total = bigoff[nbig];
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long scanned = 0;
-    for (uint32_t bi = 0; bi < nbig; bi++) {
-        const uint32_t item = big[bi];
+    for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
+        const uint32_t i = eg_big_item(bigoff, nbig, c);
+        const uint32_t item = big[i];
         const uint32_t u = item / kw, j = item % kw;
         const uint32_t a = act[(uint64_t)u * kw + j];
         const uint32_t s = j * 32 + lane;
         const bool on = (a >> lane) & 1u;
-        const uint32_t du = on ? __ldcg(dist + (uint64_t)u * k + s) : EG_SSSP_INF;
-        const uint32_t b = ptr[u], e = ptr[u + 1];
-        if (gw == 0 && lane == 0) scanned += (e - b) * (unsigned long long)__popc(a);
-        for (uint32_t p = b + gw; p < e; p += warps)
-            msssp_edge(u, col[p], j, s, on, du, k, kw, w, dist, next_act, next_inq, next_queue, cnt);
+        const uint32_t du = on ? __ldcg(dist + (uint64_t)u * k + s) : 0u;
+        const uint32_t vb = ptr[u], ve = ptr[u + 1];
+        const uint32_t off = c - bigoff[i];
+        if (off == 0 && threadIdx.x == 0) scanned += (ve - vb) * (unsigned long long)__popc(a);
+        const uint32_t b = vb + off * EG_MSSSP_CHUNK + 32u * warp;
+        if (b < ve) {
+            MsSink sink{j, kw, next_act, next_inq, next_queue, cnt};
+            eg_mrelax_span(u, b, ve - b > 32 ? b + 32 : ve, col, w, on, du, s, (uint32_t)k, dist, sink);
+        }
     }
     if (scanned) atomicAdd(&cnt->relax, scanned);
 }
@@ -367,11 +380,13 @@ extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg
     if ((uint64_t)n * kw >= 0xffffffffull) return eg_fail(EG_EINVAL, "n * ceil(k/32) must be < 2^32");
     const uint64_t off_act0 = (uint64_t)n * k, off_act1 = off_act0 + (uint64_t)n * kw, off_inq0 = off_act1 + (uint64_t)n * kw,
                    off_inq1 = off_inq0 + nw, off_q0 = off_inq1 + nw, off_q1 = off_q0 + n, off_big = off_q1 + n,
-                   off_roots = off_big + (uint64_t)n * kw, off_cnt = (off_roots + 1024 + 7) & ~7ull;
+                   off_bigoff = off_big + (uint64_t)n * kw, off_roots = off_bigoff + (uint64_t)n * kw + 1,
+                   off_cnt = (off_roots + 1024 + 7) & ~7ull;
     EG_TRY(eg_buf_ensure(ctx, g->sssp_work, (off_cnt + 8) * 4));
     uint32_t *wk = bp<uint32_t>(g->sssp_work);
     uint32_t *dist = wk, *act[2] = {wk + off_act0, wk + off_act1}, *inq[2] = {wk + off_inq0, wk + off_inq1},
-             *q[2] = {wk + off_q0, wk + off_q1}, *d_roots = wk + off_roots, *big = wk + off_big;
+             *q[2] = {wk + off_q0, wk + off_q1}, *d_roots = wk + off_roots, *big = wk + off_big,
+             *bigoff = wk + off_bigoff;
     SsspCounters *cnt = reinterpret_cast<SsspCounters *>(wk + off_cnt);
     SsspCounters *h = (SsspCounters *)ctx->h_pinned;
     EG_CUDA(cudaMemcpyAsync(d_roots, roots, (uint64_t)k * 4, cudaMemcpyHostToDevice, ctx->stream));
@@ -394,9 +409,12 @@ extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg
             bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), q[cur], qlen, k, kw, dist, act[cur], act[nxt], inq[nxt],
             q[nxt], w, cnt, big);
         EG_LAUNCHED(ctx);
-        k_msssp_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, ctx->stream>>>(
+        k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, kw, bp<uint32_t>(g->csr.ptr), EG_MSSSP_CHUNK,
+                                                   bigoff);
+        EG_LAUNCHED(ctx);
+        k_msssp_push_big<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
             bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), k, kw, dist, act[cur], act[nxt], inq[nxt], q[nxt], w, cnt,
-            big);
+            big, bigoff);
         EG_LAUNCHED(ctx);
         // the current frontier's words and bits are cleared for reuse as "next"
         k_msssp_clear<<<blocks_for(ctx, (uint64_t)qlen * kw), 256, 0, ctx->stream>>>(q[cur], qlen, kw, act[cur], inq[cur]);

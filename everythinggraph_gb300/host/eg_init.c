@@ -20,10 +20,7 @@ void init(int full) {
     unsigned flags = 0;
     int adjacency_mode = load_mode >= 2 && load_mode <= 5;
     if (createUndir && adjacency_mode) flags |= EG_UNDIRECTED;
-    if (weighted_graph) {
-        fprintf(stderr, "-w (12-byte weighted records) is not supported by the GPU loader\n");
-        exit(1);
-    }
+    if (weighted_graph) flags |= EG_WEIGHTED_FILE;  // 12-byte records, weights skipped
     printf("Load start");
     if (eg_graph_from_file(eg_context, filename, NB_NODES, flags, &eg_g) != EG_OK) eg_die("load");
     eg_graph_info info;

@@ -48,7 +48,8 @@ const char *eg_version(void);
  * the context may allocate (0 = no cap).  Replaces the reference's thread
  * setup (setWorkers, random.c:123 and parallel_ligra.h:49-57). */
 int eg_open(int device, uint64_t hbm_budget_bytes, eg_ctx **out);
-int eg_close(eg_ctx *ctx);
+int eg_close(eg_ctx *ctx); /* EG_EINVAL (context kept) while graphs are open:
+                              free every graph (and server) first */
 /* The context's cudaStream_t, as void*. */
 void *eg_stream(eg_ctx *ctx);
 int eg_sync(eg_ctx *ctx);
@@ -59,6 +60,12 @@ uint64_t eg_kernel_launches(eg_ctx *ctx);
 /* ---- graph input (replaces init(): init_all.c:791-893) ----------------- */
 #define EG_UNDIRECTED 1u /* -u: append reversed copies of every edge
                             (init_all.c:171-175), doubling m (init_all.c:636) */
+#define EG_WEIGHTED_FILE 2u /* -w: the file holds 12-byte [src][dst][f32 weight]
+                               records (struct input, init_all.h:8-14;
+                               item_size, init_all.c:43-49).  The weights are
+                               skipped: the adjacency build overwrites them
+                               with the CREATE_WEIGHT rule (init_all.c:661-686),
+                               which the SSSP weight rules restate. */
 
 /* From host pairs: 2*m uint32 values [src][dst] in file order. */
 int eg_graph_from_pairs(eg_ctx *ctx, const uint32_t *pairs, uint64_t m, uint32_t n, unsigned flags,
@@ -307,10 +314,12 @@ int eg_ppr(eg_graph *g, const uint32_t *seeds, uint32_t nseeds, const eg_ppr_opt
 /* ---- query server (continuous batching) ----------------------------------
  * No counterpart in the reference (one algorithm per process).  A server
  * keeps the graph and every admitted query's state in HBM.  eg_serve_step is
- * one scheduler tick: queued queries are admitted into free slots (64 BFS,
- * 64 SSSP, 32 PPR at most; fewer when hbm_budget cannot hold their state),
- * every engine with live slots advances one step (one BFS level, one
- * Bellman-Ford round, one PPR iteration), finished queries are retired.
+ * one scheduler pass.  The three engines (64 BFS slots, 64 SSSP slots, 32
+ * PPR lanes at most; fewer when hbm_budget cannot hold their state) run on
+ * their own CUDA streams; an engine whose step (one BFS level, one
+ * Bellman-Ford round, one PPR iteration over all its live slots) has
+ * finished retires its finished queries, admits queued ones into the freed
+ * slots and launches its next step, without waiting for the other engines.
  * Queries join and leave between ticks; a slot's arithmetic never reads
  * another slot's values, so results do not depend on the mix.  Results stay
  * on the device; eg_serve_poll returns a summary per finished query, and
@@ -354,6 +363,18 @@ int eg_serve_poll(eg_server *s, eg_query_result *out, int max, int *count);
 /* next kept full result (n u32 words), in completion order */
 int eg_serve_take_result(eg_server *s, uint32_t *out, uint32_t n);
 int eg_serve_info(eg_server *s, int *bfs_slots, int *sssp_slots, int *ppr_slots, double *clock_s);
+/* Per-engine counters since eg_serve_open: index 0 BFS, 1 SSSP, 2 PPR.
+ * engine_ms is the device time of the engine's steps (CUDA events on the
+ * engine's stream; engines overlap, so the three can sum past wall time). */
+typedef struct {
+    uint64_t ticks;
+    uint64_t queued;
+    double engine_ms[3];
+    uint64_t engine_steps[3];
+    uint64_t admitted[3];
+    uint64_t completed[3];
+} eg_serve_stats_t;
+int eg_serve_stats(eg_server *s, eg_serve_stats_t *out);
 int eg_serve_close(eg_server *s);
 
 /* ---- allocation-free SpMV ------------------------------------------------

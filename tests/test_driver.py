@@ -74,6 +74,34 @@ def test_driver_matches_reference_dumps(binaries, name, tmp_path):
 
 
 @pytest.mark.gpu
+def test_driver_weighted_records(binaries, tmp_path):
+    # -w: 12-byte [src][dst][f32 weight] records; the weights are replaced by
+    # the CREATE_WEIGHT rule, so every result equals the 8-byte file's
+    z = np.load(os.path.join(GOLDEN, "rmat10.npz"))
+    n = int(z["n"])
+    pairs = z["pairs"].reshape(-1, 2)
+    rec = np.zeros((len(pairs), 3), np.uint32)
+    rec[:, :2] = pairs
+    rec[:, 2] = np.random.default_rng(1).random(len(pairs), dtype=np.float32).view(np.uint32)
+    path = str(tmp_path / "w.bin")
+    rec.tofile(path)
+    f = ["-f", path, "-n", str(n), "-w"]
+    r = int(z["roots"][0])
+    d, _ = run("eg_sssp_pushpull", f + ["-m", "2", "-a", "1", "-r", "-p", str(r)], tmp_path, np.uint32, n)
+    np.testing.assert_array_equal(d, z["sssp_pull_p%d" % r])
+    lab, _ = run("eg_wcc", f + ["-m", "2", "-u"], tmp_path, np.int64, n)
+    np.testing.assert_array_equal(lab, z["wcc_m2u"])
+    lv, _ = run("eg_bfsgrid_cilk", f + ["-m", "0", "-p", str(r)], tmp_path, np.int32, n)
+    np.testing.assert_array_equal(lv.astype(np.uint32), z["bfsgrid_m0_p%d" % r])
+    odd = str(tmp_path / "w_odd.bin")
+    with open(odd, "wb") as fh:
+        fh.write(b"\x00" * 16)  # not a whole number of 12-byte records
+    res = subprocess.run([os.path.join(BIN, "eg_wcc"), "-f", odd, "-n", "4", "-m", "2", "-w"], capture_output=True,
+                         text=True, timeout=60)
+    assert res.returncode == 1 and "multiple of 12" in res.stderr
+
+
+@pytest.mark.gpu
 def test_driver_rejects_bad_inputs(binaries, tmp_path):
     bad = str(tmp_path / "odd.bin")
     with open(bad, "wb") as fh:
