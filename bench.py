@@ -181,7 +181,8 @@ def run_ours(args):
             kernels["serve"] = {"error": str(ex)}
         kernels.update(kernel_reports(ctx, eg, scale, args))
         for name, fn in (("spmv_er25", lambda: spmv_report(ctx, eg, 25 if scale >= 24 else scale, 32)),
-                         ("sssp_rmat23_256", lambda: sssp_report(ctx, eg, 23 if scale >= 24 else scale - 1))):
+                         ("sssp_rmat23_256", lambda: sssp_report(ctx, eg, 23 if scale >= 24 else scale - 1)),
+                         ("ppr_32_queries", lambda: ppr_report(ctx, eg, scale))):
             try:
                 kernels[name] = fn()
             except Exception as ex:
@@ -460,6 +461,56 @@ def run_reference(args):
     print(json.dumps(out))
 
 
+def ppr_report(ctx, eg, scale=24, nq=32, seed=7):
+    """Personalised PageRank on the undirected RMAT graph: nq queries (1-8
+    seeds, tolerance 1e-6, <= 50 iterations) in one 32-lane batch versus the
+    same queries one at a time on the PageRank row kernel."""
+    n = 1 << scale
+    g = ctx.rmat(scale, 16 * n, 2, undirected=True).build(eg.CSR | eg.CSC)
+    od, _ = g.degrees(True, False)
+    nz = np.nonzero(od > 0)[0]
+    rng = np.random.default_rng(seed)
+    seeds = [rng.choice(nz, int(rng.integers(1, 9))).astype(np.uint32) for _ in range(nq)]
+    g.ppr(seeds[:2], tolerance=1e-6, copy_out=False)
+    _, stb = g.ppr(seeds, tolerance=1e-6, max_iters=50, copy_out=False)
+    t1, its = 0.0, 0
+    for sd in seeds[:8]:
+        _, st = g.ppr_single(sd, tolerance=1e-6, max_iters=50, copy_out=False)
+        t1 += st.ms
+        its += st.sweeps
+    g.free()
+    per_single = t1 / 8
+    return {"workload": "ppr rmat%d undirected, %d queries" % (scale, nq), "batched_ms": stb.ms,
+            "sweeps": stb.sweeps, "ms_per_sweep": stb.ms / max(stb.sweeps, 1), "single_ms_each": per_single,
+            "single_iters_each": its / 8, "speedup": per_single * nq / stb.ms}
+
+
+def only_report(name, args):
+    """One report alone (profiling and quick checks)."""
+    import everythinggraph_gb300 as eg
+    from everythinggraph_gb300 import build
+    build.build_lib()
+    ctx = eg.Context(0)
+    scale = args.scale or 24
+    if name == "serve":
+        out = serve_report(ctx, eg, scale, args.rate, args.queries)
+    elif name == "pr":
+        out = kernel_reports(ctx, eg, scale, args)
+    elif name == "spmv":
+        out = spmv_report(ctx, eg, args.scale or 25, 32)
+    elif name == "sssp":
+        out = sssp_report(ctx, eg, args.scale or 23)
+    elif name == "ppr":
+        out = ppr_report(ctx, eg, scale)
+    else:  # msbfs
+        n = 1 << scale
+        g = ctx.rmat(scale, 16 * n, 2, undirected=True).build(eg.CSR | eg.CSC)
+        out = msbfs_report(g, g.sample_roots(64, 3))
+        g.free()
+    print(json.dumps(out))
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -471,23 +522,13 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--pr-only", action="store_true", help="only the PageRank pull report (profiling)")
     ap.add_argument("--serve-only", action="store_true", help="only the serving report")
+    ap.add_argument("--only", choices=["pr", "spmv", "sssp", "msbfs", "ppr", "serve"],
+                    help="only one kernel report (profiling)")
     ap.add_argument("--rate", type=float, default=20000.0)
     ap.add_argument("--queries", type=int, default=1000)
     args = ap.parse_args()
-    if args.serve_only:
-        import everythinggraph_gb300 as eg
-        from everythinggraph_gb300 import build
-        build.build_lib()
-        ctx = eg.Context(0)
-        print(json.dumps(serve_report(ctx, eg, args.scale or 24, args.rate, args.queries)))
-        ctx.close()
-    elif args.pr_only:
-        import everythinggraph_gb300 as eg
-        from everythinggraph_gb300 import build
-        build.build_lib()
-        ctx = eg.Context(0)
-        print(json.dumps(kernel_reports(ctx, eg, args.scale or 24, args)))
-        ctx.close()
+    if args.only or args.serve_only or args.pr_only:
+        only_report(args.only or ("serve" if args.serve_only else "pr"), args)
     elif args.impl == "reference":
         run_reference(args)
     else:

@@ -292,7 +292,7 @@ extern "C" void eg_graph_free(eg_graph *g) {
                       &g->rank,    &g->contrib0,     &g->contrib1,
                       &g->pr_part,      &g->pr_stats,    &g->mp_carry,    &g->errflag,     &g->rank_p,    &g->rank_q,    &g->level,          &g->parent,       &g->dist,
                       &g->label,        &g->spmv_x,      &g->spmv_y,      &g->spmv_vals,      &g->bfs_work,     &g->msbfs_work,
-                      &g->sssp_work,    &g->ppr_work};
+                      &g->sssp_work,    &g->ppr_work,    &g->wts};
     for (eg_buf *b : bufs) eg_buf_free(c, *b);
     for (eg_bfs_graph &bg : g->bfsg) {
         if (bg.exec) cudaGraphExecDestroy(bg.exec);

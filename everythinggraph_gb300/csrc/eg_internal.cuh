@@ -112,6 +112,10 @@ struct eg_graph {
     eg_bfs_graph bfsg[2];  // without / with parents
     eg_bfs_graph prg;      // PageRank iterations (key: options and buffers)
     int row_cfg = 0;       // row-kernel schedule (entries per warp tile, per lane)
+    // SSSP edge weights of the CSR entries for one rule, materialised on first
+    // use (the reference stores them in its edge records, init_all.c:661-686)
+    eg_buf wts;
+    uint64_t wts_key[3] = {~0ull, ~0ull, ~0ull};
     uint64_t prk[16] = {};
 };
 
@@ -215,6 +219,12 @@ struct eg_wrule {
     }
     __device__ __forceinline__ uint32_t extend(uint32_t du, uint32_t u, uint32_t v) const { return add(du, weight(u, v)); }
 };
+struct eg_graph;
+// The CSR-order weight array of rule w, computed once per rule and kept in
+// the graph (replaced when another rule is asked for).
+int eg_edge_weights(eg_graph *g, const eg_wrule &w, const uint32_t **out);
+// Writes rule w's CSR-order weights to out[m] on the context's stream.
+int eg_fill_weights(eg_graph *g, const eg_wrule &w, uint32_t *out);
 static inline eg_wrule eg_make_wrule(const eg_weights *w) {
     eg_wrule r;
     r.rule = w ? w->rule : EG_W_REF;

@@ -42,20 +42,33 @@ __global__ void __launch_bounds__(256) k_ppr_rows(const uint32_t *__restrict__ r
         const uint32_t my_r = e < E1 ? __ldg(rid + e) : EG_PPR_NONE;
         const uint32_t my_c = e < E1 ? __ldg(col + e) : 0u;
         const uint32_t cnt = min(32u, E1 - base);
-        for (uint32_t j = 0; j < cnt; j++) {
-            const uint32_t r = __shfl_sync(EG_FULL_MASK, my_r, j);
-            const uint32_t u = __shfl_sync(EG_FULL_MASK, my_c, j);
-            if (r != cur) {  // row `cur` ended inside the tile
-                if (cur == hrow) {
-                    hdone = true;
-                    hval = acc;
-                } else {
-                    Y[(uint64_t)cur * EG_PPR_LANES + lane] = acc;
-                }
-                acc = 0.f;
-                cur = r;
+        // 8 entries per step: their 8 row loads are issued before any is
+        // added, then added in entry order (the same order as one at a time)
+        for (uint32_t j0 = 0; j0 < cnt; j0 += 8) {
+            uint32_t rr[8];
+            float xv[8];
+#pragma unroll
+            for (uint32_t q = 0; q < 8; q++) {
+                const uint32_t j = j0 + q;
+                rr[q] = __shfl_sync(EG_FULL_MASK, my_r, j & 31);
+                const uint32_t u = __shfl_sync(EG_FULL_MASK, my_c, j & 31);
+                xv[q] = j < cnt ? __ldg(X + (uint64_t)u * EG_PPR_LANES + lane) : 0.f;
             }
-            acc += __ldg(X + (uint64_t)u * EG_PPR_LANES + lane);
+#pragma unroll
+            for (uint32_t q = 0; q < 8; q++) {
+                if (j0 + q >= cnt) break;
+                if (rr[q] != cur) {  // row `cur` ended inside the tile
+                    if (cur == hrow) {
+                        hdone = true;
+                        hval = acc;
+                    } else {
+                        Y[(uint64_t)cur * EG_PPR_LANES + lane] = acc;
+                    }
+                    acc = 0.f;
+                    cur = rr[q];
+                }
+                acc += xv[q];
+            }
         }
     }
     // the last row: complete if the next tile starts another row

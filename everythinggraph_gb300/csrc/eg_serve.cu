@@ -202,50 +202,57 @@ __global__ void k_sv_sssp_admit(const uint32_t *roots, const uint32_t *slots, in
     }
 }
 
-// Records v in the next frontier for the slots in `ball` of word j.
+// Records v in the next frontier for slots of word j (eg_mrelax's Sink);
+// actmask collects the slots that improved anything this round.
 struct SvSink {
     uint32_t j;
     uint32_t *next_act, *next_inq, *next_queue;
     SvCounters *cnt;
-    __device__ __forceinline__ void operator()(uint32_t v, uint32_t ball) {
+    __device__ __forceinline__ bool enqueue_bit(uint32_t v) {
+        const uint32_t bit = 1u << (v & 31);
+        return !(atomicOr(next_inq + (v >> 5), bit) & bit);
+    }
+    __device__ __forceinline__ void row(uint32_t v, uint32_t ball) {
         atomicOr(next_act + (uint64_t)v * 2 + j, ball);
         atomicOr(&cnt->actmask[j], (unsigned long long)ball);
-        const uint32_t bit = 1u << (v & 31);
-        if (!(atomicOr(next_inq + (v >> 5), bit) & bit)) next_queue[atomicAdd(&cnt->qsize, 1u)] = v;
+        if (enqueue_bit(v)) next_queue[atomicAdd(&cnt->qsize, 1u)] = v;
     }
+    __device__ __forceinline__ bool mark(uint32_t v, uint32_t bit) {
+        atomicOr(next_act + (uint64_t)v * 2 + j, bit);
+        return enqueue_bit(v);
+    }
+    __device__ __forceinline__ void append(bool q, uint32_t v) {
+        const uint32_t ball = __ballot_sync(EG_FULL_MASK, q);
+        if (!ball) return;
+        uint32_t base = 0;
+        if ((threadIdx.x & 31) == 0) base = atomicAdd(&cnt->qsize, (uint32_t)__popc(ball));
+        base = __shfl_sync(EG_FULL_MASK, base, 0);
+        if (q) next_queue[base + __popc(ball & eg_lanemask_lt())] = v;
+    }
+    __device__ __forceinline__ void any(uint32_t bit) { atomicOr(&cnt->actmask[j], (unsigned long long)bit); }
 };
 
 __global__ void __launch_bounds__(256) k_sv_sssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
-                                                      const uint32_t *__restrict__ queue, const SvCounters *qc,
+                                                      const uint32_t *__restrict__ wts, const uint32_t *__restrict__ queue, const SvCounters *qc,
                                                       uint32_t *dist, const uint32_t *__restrict__ act,
                                                       uint32_t *next_act, uint32_t *next_inq, uint32_t *next_queue,
                                                       SvW w, SvCounters *cnt, uint32_t *big) {
     const uint32_t qlen = qc->qsize;
-    const uint32_t lane = threadIdx.x & 31;
-    const uint64_t warps = (gridDim.x * blockDim.x) >> 5;
-    for (uint64_t it = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; it < 2ull * qlen; it += warps) {
-        const uint32_t u = queue[it >> 1];
-        const uint32_t j = (uint32_t)(it & 1);
-        const uint32_t a = act[(uint64_t)u * 2 + j];
-        if (!a) continue;
-        const uint32_t b = ptr[u], e = ptr[u + 1];
-        if (e - b > SV_BIG_DEG) {
-            if (lane == 0) big[atomicAdd(&cnt->nbig, 1u)] = u * 2 + j;
-            continue;
-        }
-        const uint32_t s = j * 32 + lane;
-        const bool on = (a >> lane) & 1u;
-        const uint32_t du = on ? __ldcg(dist + (uint64_t)u * SV_SSSP_SLOTS + s) : 0u;
-        SvSink sink{j, next_act, next_inq, next_queue, cnt};
-        eg_mrelax_span(u, b, e, col, w, on, du, s, SV_SSSP_SLOTS, dist, sink);
-    }
+    const uint64_t warps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
+    unsigned long long scanned = 0;
+    SvSink sink{0, next_act, next_inq, next_queue, cnt};
+    for (uint64_t base = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * 32; base < 2ull * qlen;
+         base += warps * 32)
+        eg_mrelax_items(base, 2ull * qlen, queue, 2u, ptr, col, wts, w, SV_SSSP_SLOTS, dist, act, SV_BIG_DEG, big,
+                        &cnt->nbig, sink, scanned);
 }
 
 // Deferred (hub, word) items in chunks of SV_SSSP_CHUNK edges, one CTA per
 // chunk, one warp per 32 edges of it.
 #define SV_SSSP_CHUNK 256u
 __global__ void __launch_bounds__(256) k_sv_sssp_push_big(const uint32_t *__restrict__ ptr,
-                                                          const uint32_t *__restrict__ col, uint32_t *dist,
+                                                          const uint32_t *__restrict__ col,
+                                                          const uint32_t *__restrict__ wts, uint32_t *dist,
                                                           const uint32_t *__restrict__ act, uint32_t *next_act,
                                                           uint32_t *next_inq, uint32_t *next_queue, SvW w,
                                                           SvCounters *cnt, const uint32_t *big,
@@ -265,7 +272,7 @@ __global__ void __launch_bounds__(256) k_sv_sssp_push_big(const uint32_t *__rest
         const uint32_t b = ptr[u] + (c - bigoff[i]) * SV_SSSP_CHUNK + 32u * warp;
         if (b < ve) {
             SvSink sink{j, next_act, next_inq, next_queue, cnt};
-            eg_mrelax_span(u, b, ve - b > 32 ? b + 32 : ve, col, w, on, du, s, SV_SSSP_SLOTS, dist, sink);
+            eg_mrelax(u, b, ve - b > 32 ? b + 32 : ve, col, wts, w, a, du, j, SV_SSSP_SLOTS, dist, sink);
         }
     }
 }
@@ -368,6 +375,8 @@ struct eg_server {
     uint32_t ppr_mask = 0;
     uint64_t ppr_id[SV_PPR_LANES];
     double ppr_admit[SV_PPR_LANES], ppr_arrival[SV_PPR_LANES];
+    eg_buf wts_buf;                      // SSSP weights of the CSR entries (the server's own copy)
+    const uint32_t *wts = nullptr;
     PprQ *hq = nullptr;                  // host mirror of the lanes' state (pinned, updated every iteration)
     uint32_t pseeds[SV_PPR_LANES * 8] = {};  // seeds of each lane (8 per lane)
     uint32_t pnseeds[SV_PPR_LANES] = {};
@@ -471,6 +480,9 @@ extern "C" int eg_serve_open(eg_graph *g, const eg_serve_opts *opts, eg_server *
         rc = eg_buf_ensure(ctx, s->ppr_buf, (uint64_t)n * 4 * EG_PPR_LANES * 3 + ptiles * EG_PPR_LANES * 4 * 2 +
                                                  ((ptiles + 63) & ~63ull) * 4 + (uint64_t)ctx->sm_count * 4 * 32 * 16 + 256);
     if (rc == EG_OK) rc = eg_buf_ensure(ctx, s->small, 64 * 1024);
+    if (rc == EG_OK) rc = eg_buf_ensure(ctx, s->wts_buf, g->m * 4 + 16);
+    if (rc == EG_OK) rc = eg_fill_weights(g, eg_make_wrule(&o.weights), bp<uint32_t>(s->wts_buf));
+    if (rc == EG_OK) s->wts = bp<uint32_t>(s->wts_buf);
     for (int e = 0; e < 3 && rc == EG_OK; e++) {
         if (cudaStreamCreateWithFlags(&s->st[e], cudaStreamNonBlocking) != cudaSuccess ||
             cudaEventCreate(&s->ev_begin[e]) != cudaSuccess || cudaEventCreate(&s->ev_end[e]) != cudaSuccess)
@@ -492,6 +504,7 @@ extern "C" int eg_serve_open(eg_graph *g, const eg_serve_opts *opts, eg_server *
         eg_buf_free(ctx, s->sssp_buf);
         eg_buf_free(ctx, s->ppr_buf);
         eg_buf_free(ctx, s->small);
+        eg_buf_free(ctx, s->wts_buf);
         delete s;
         return rc;
     }
@@ -529,6 +542,7 @@ extern "C" int eg_serve_close(eg_server *s) {
     eg_buf_free(ctx, s->sssp_buf);
     eg_buf_free(ctx, s->ppr_buf);
     eg_buf_free(ctx, s->small);
+    eg_buf_free(ctx, s->wts_buf);
     delete s;
     return EG_OK;
 }
@@ -825,16 +839,17 @@ static int sv_sssp_advance(eg_server *s, bool *progress) {
     }
     if (!s->sssp_mask) return EG_OK;
     SvW w = eg_make_wrule(&s->opts.weights);
+    const uint32_t *wts = s->wts;
     EG_CUDA(cudaEventRecord(s->ev_begin[E_SSSP], st));
     EG_CUDA(cudaMemsetAsync(snext, 0, sizeof(SvCounters), st));
-    k_sv_sssp_push<<<(uint32_t)ctx->sm_count * 8, 256, 0, st>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), sq[c],
-                                                                scur, dist, act[c], act[nx], inq[nx], sq[nx], w, snext,
-                                                                sbig);
+    k_sv_sssp_push<<<(uint32_t)ctx->sm_count * 8, 256, 0, st>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), wts,
+                                                                sq[c], scur, dist, act[c], act[nx], inq[nx], sq[nx], w,
+                                                                snext, sbig);
     EG_LAUNCHED(ctx);
     k_big_offsets<<<1, 1024, 0, st>>>(sbig, &snext->nbig, 2u, bp<uint32_t>(g->csr.ptr), SV_SSSP_CHUNK, sbigoff);
     EG_LAUNCHED(ctx);
     k_sv_sssp_push_big<<<(uint32_t)ctx->sm_count * 8, 256, 0, st>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col),
-                                                                    dist, act[c], act[nx], inq[nx], sq[nx], w, snext,
+                                                                    wts, dist, act[c], act[nx], inq[nx], sq[nx], w, snext,
                                                                     sbig, sbigoff);
     EG_LAUNCHED(ctx);
     k_sv_sssp_clear_frontier<<<sv_blocks(ctx, n), 256, 0, st>>>(sq[c], scur, act[c], inq[c]);

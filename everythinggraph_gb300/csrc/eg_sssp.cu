@@ -10,6 +10,7 @@
 // Weights are computed from the edge's endpoints, like the reference's
 // CREATE_WEIGHT path (init_all.c:661-686): no weight array is stored or read.
 #include <stdlib.h>
+#include <string.h>
 
 #include "eg_internal.cuh"
 #include "eg_bigwork.cuh"
@@ -22,7 +23,8 @@ using WRule = eg_wrule;
 struct SsspCounters {
     unsigned long long relax;  // entries scanned
     uint32_t qsize;
-    uint32_t nbig;  // frontier vertices deferred to the grid-wide kernel
+    uint32_t nbig;             // frontier vertices deferred to the grid-wide kernel
+    unsigned long long reached;
 };
 
 // Frontier vertices with more out-edges than this are relaxed by the whole
@@ -42,10 +44,11 @@ __global__ void k_sssp_init(uint32_t n, uint32_t *dist, uint32_t root, uint32_t 
 
 // One warp per frontier vertex; lanes relax its out-edges.  A vertex whose
 // distance drops is queued once per round (claimed through the next bitmap).
-__device__ __forceinline__ bool sssp_relax(uint32_t u, uint32_t du, uint32_t v, const WRule &w, uint32_t *dist,
+__device__ __forceinline__ bool sssp_relax(uint32_t u, uint32_t du, uint32_t v, uint32_t wt, const WRule &w,
+                                           uint32_t *dist,
                                            uint32_t *next_bm) {
     if (v == u) return false;  // self-loops skipped (sssp_pushpull.c:80)
-    const uint32_t nd = w.extend(du, u, v);
+    const uint32_t nd = w.add(du, wt);
     if (nd >= __ldcg(dist + v)) return false;
     const uint32_t old = atomicMin(dist + v, nd);
     if (nd >= old) return false;
@@ -68,7 +71,8 @@ __device__ __forceinline__ void sssp_append(bool q, uint32_t v, uint32_t *next_q
 // EG_SSSP_CHUNK edges shared out over the grid (one CTA per chunk).
 #define EG_SSSP_CHUNK 2048u
 __global__ void __launch_bounds__(256) k_sssp_push_big(const uint32_t *__restrict__ ptr,
-                                                       const uint32_t *__restrict__ col, const uint32_t *big,
+                                                       const uint32_t *__restrict__ col,
+                                                       const uint32_t *__restrict__ wts, const uint32_t *big,
                                                        const uint32_t *__restrict__ bigoff, uint32_t *dist,
                                                        uint32_t *next_bm, uint32_t *next_queue, WRule w,
                                                        SsspCounters *cnt) {
@@ -90,7 +94,7 @@ __global__ void __launch_bounds__(256) k_sssp_push_big(const uint32_t *__restric
             uint32_t v = 0;
             if (p < e) {
                 v = col[p];
-                q = sssp_relax(u, du, v, w, dist, next_bm);
+                q = sssp_relax(u, du, v, __ldg(wts + p), w, dist, next_bm);
             }
             sssp_append(q, v, next_queue, cnt);
         }
@@ -99,7 +103,7 @@ __global__ void __launch_bounds__(256) k_sssp_push_big(const uint32_t *__restric
 }
 
 __global__ void __launch_bounds__(256) k_sssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
-                                                   const uint32_t *__restrict__ queue, uint32_t qlen, uint32_t *dist,
+                                                   const uint32_t *__restrict__ wts, const uint32_t *__restrict__ queue, uint32_t qlen, uint32_t *dist,
                                                    uint32_t *next_bm, uint32_t *next_queue, WRule w,
                                                    SsspCounters *cnt, uint32_t *big) {
     const uint32_t lane = threadIdx.x & 31;
@@ -120,7 +124,7 @@ __global__ void __launch_bounds__(256) k_sssp_push(const uint32_t *__restrict__ 
             uint32_t v = 0;
             if (p < e) {
                 v = col[p];
-                q = sssp_relax(u, du, v, w, dist, next_bm);
+                q = sssp_relax(u, du, v, __ldg(wts + p), w, dist, next_bm);
             }
             sssp_append(q, v, next_queue, cnt);
         }
@@ -146,6 +150,12 @@ __global__ void k_count_reached(const uint32_t *__restrict__ dist, uint64_t len,
     if ((threadIdx.x & 31) == 0 && c) atomicAdd(out, c);
 }
 
+__global__ void k_edge_weights(const uint32_t *__restrict__ rid, const uint32_t *__restrict__ col, uint32_t m,
+                               WRule w, uint32_t *__restrict__ out) {
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < m; p += gridDim.x * blockDim.x)
+        out[p] = w.weight(__ldg(rid + p), __ldg(col + p));
+}
+
 uint32_t blocks_for(eg_ctx *ctx, uint64_t threads) {
     uint64_t b = (threads + 255) / 256;
     uint64_t cap = (uint64_t)ctx->sm_count * 8;
@@ -163,15 +173,42 @@ int check_weights(const eg_weights *w) {
 
 }  // namespace
 
-extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wts, uint32_t *dist_out, eg_sssp_stats *stats) {
+int eg_fill_weights(eg_graph *g, const eg_wrule &w, uint32_t *out) {
+    eg_ctx *ctx = g->ctx;
+    const eg_adj &a = g->csr;
+    if (g->m) {
+        k_edge_weights<<<blocks_for(ctx, g->m), 256, 0, ctx->stream>>>(bp<uint32_t>(a.rid), bp<uint32_t>(a.col),
+                                                                      (uint32_t)g->m, w, out);
+        EG_LAUNCHED(ctx);
+    }
+    return EG_OK;
+}
+
+int eg_edge_weights(eg_graph *g, const eg_wrule &w, const uint32_t **out) {
+    const uint64_t key[3] = {(uint64_t)w.rule, w.seed, ((uint64_t)w.lo << 32) ^ w.span};
+    if (g->wts.p && !memcmp(key, g->wts_key, sizeof(key))) {
+        *out = bp<uint32_t>(g->wts);
+        return EG_OK;
+    }
+    EG_TRY(eg_buf_ensure(g->ctx, g->wts, g->m * 4 + 16));
+    EG_TRY(eg_fill_weights(g, w, bp<uint32_t>(g->wts)));
+    memcpy(g->wts_key, key, sizeof(key));
+    *out = bp<uint32_t>(g->wts);
+    return EG_OK;
+}
+
+extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wrule_in, uint32_t *dist_out,
+                       eg_sssp_stats *stats) {
     if (!g) return eg_fail(EG_EINVAL, "NULL graph");
     if (root >= g->n) return eg_fail(EG_EINVAL, "root %u >= n %u", root, g->n);
     if (!(g->built & EG_LAYOUT_CSR)) return eg_fail(EG_ENOTBUILT, "SSSP needs the CSR");
-    EG_TRY(check_weights(wts));
+    EG_TRY(check_weights(wrule_in));
     eg_ctx *ctx = g->ctx;
     EG_CUDA(cudaSetDevice(ctx->device));
     const uint32_t n = g->n, nw = (n + 31) >> 5;
-    const WRule w = eg_make_wrule(wts);
+    const WRule w = eg_make_wrule(wrule_in);
+    const uint32_t *wts = nullptr;
+    EG_TRY(eg_edge_weights(g, w, &wts));
     EG_TRY(eg_buf_ensure(ctx, g->dist, (uint64_t)n * 4));
     const uint64_t off_q0 = nw, off_q1 = off_q0 + n, off_big = off_q1 + n, off_bigoff = off_big + n,
                    off_cnt = (off_bigoff + n + 1 + 7) & ~7ull;
@@ -192,13 +229,13 @@ extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wts, uint32
         const int nxt = cur ^ 1;
         EG_CUDA(cudaMemsetAsync(&cnt->qsize, 0, 8, ctx->stream));  // qsize and nbig
         k_sssp_push<<<blocks_for(ctx, (uint64_t)qlen * 32), 256, 0, ctx->stream>>>(
-            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), q[cur], qlen, dist, bm, q[nxt], w, cnt, big);
+            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), wts, q[cur], qlen, dist, bm, q[nxt], w, cnt, big);
         EG_LAUNCHED(ctx);
         k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, 1u, bp<uint32_t>(g->csr.ptr), EG_SSSP_CHUNK,
                                                    bigoff);
         EG_LAUNCHED(ctx);
         k_sssp_push_big<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr),
-                                                                              bp<uint32_t>(g->csr.col), big, bigoff,
+                                                                              bp<uint32_t>(g->csr.col), wts, big, bigoff,
                                                                               dist, bm, q[nxt], w, cnt);
         EG_LAUNCHED(ctx);
         EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(SsspCounters), cudaMemcpyDeviceToHost, ctx->stream));
@@ -216,7 +253,7 @@ extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wts, uint32
     }
     EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     if (dist_out) EG_CUDA(cudaMemcpyAsync(dist_out, dist, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
-    unsigned long long *dcount = reinterpret_cast<unsigned long long *>(cnt) + 2;
+    unsigned long long *dcount = &cnt->reached;
     if (stats) {
         EG_CUDA(cudaMemsetAsync(dcount, 0, 8, ctx->stream));
         k_count_reached<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(dist, n, dcount, w.inf());
@@ -262,44 +299,47 @@ __global__ void k_msssp_roots(const uint32_t *roots, int k, uint32_t kw, uint32_
     }
 }
 
-// Records v in the next frontier for the sources in `ball` of word j.
+// Records v in the next frontier for sources of word j (eg_mrelax's Sink).
 struct MsSink {
     uint32_t j, kw;
     uint32_t *next_act, *next_inq, *next_queue;
     SsspCounters *cnt;
-    __device__ __forceinline__ void operator()(uint32_t v, uint32_t ball) {
-        atomicOr(next_act + (uint64_t)v * kw + j, ball);
+    __device__ __forceinline__ bool enqueue_bit(uint32_t v) {
         const uint32_t bit = 1u << (v & 31);
-        if (!(atomicOr(next_inq + (v >> 5), bit) & bit)) next_queue[atomicAdd(&cnt->qsize, 1u)] = v;
+        return !(atomicOr(next_inq + (v >> 5), bit) & bit);
     }
+    __device__ __forceinline__ void row(uint32_t v, uint32_t ball) {
+        atomicOr(next_act + (uint64_t)v * kw + j, ball);
+        if (enqueue_bit(v)) next_queue[atomicAdd(&cnt->qsize, 1u)] = v;
+    }
+    __device__ __forceinline__ bool mark(uint32_t v, uint32_t bit) {
+        atomicOr(next_act + (uint64_t)v * kw + j, bit);
+        return enqueue_bit(v);
+    }
+    __device__ __forceinline__ void append(bool q, uint32_t v) {
+        const uint32_t ball = __ballot_sync(EG_FULL_MASK, q);
+        if (!ball) return;
+        uint32_t base = 0;
+        if ((threadIdx.x & 31) == 0) base = atomicAdd(&cnt->qsize, (uint32_t)__popc(ball));
+        base = __shfl_sync(EG_FULL_MASK, base, 0);
+        if (q) next_queue[base + __popc(ball & eg_lanemask_lt())] = v;
+    }
+    __device__ __forceinline__ void any(uint32_t) {}
 };
 
 __global__ void __launch_bounds__(256) k_msssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
-                                                    const uint32_t *__restrict__ queue, uint32_t qlen, int k,
+                                                    const uint32_t *__restrict__ wts, const uint32_t *__restrict__ queue, uint32_t qlen, int k,
                                                     uint32_t kw, uint32_t *dist, const uint32_t *__restrict__ act,
                                                     uint32_t *next_act, uint32_t *next_inq, uint32_t *next_queue,
                                                     WRule w, SsspCounters *cnt, uint32_t *big) {
     const uint32_t lane = threadIdx.x & 31;
-    const uint64_t warps = (gridDim.x * blockDim.x) >> 5;
+    const uint64_t warps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
     unsigned long long scanned = 0;
     const uint64_t items = (uint64_t)qlen * kw;
-    for (uint64_t it = (blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5; it < items; it += warps) {
-        const uint32_t u = queue[it / kw];
-        const uint32_t j = (uint32_t)(it % kw);
-        const uint32_t a = act[(uint64_t)u * kw + j];
-        if (!a) continue;
-        const uint32_t b = ptr[u], e = ptr[u + 1];
-        if (e - b > EG_SSSP_BIG_DEG) {
-            if (lane == 0) big[atomicAdd(&cnt->nbig, 1u)] = (uint32_t)((uint64_t)u * kw + j);
-            continue;
-        }
-        const uint32_t s = j * 32 + lane;
-        const bool on = (a >> lane) & 1u;
-        const uint32_t du = on ? __ldcg(dist + (uint64_t)u * k + s) : 0u;
-        if (lane == 0) scanned += (e - b) * (unsigned long long)__popc(a);
-        MsSink sink{j, kw, next_act, next_inq, next_queue, cnt};
-        eg_mrelax_span(u, b, e, col, w, on, du, s, (uint32_t)k, dist, sink);
-    }
+    MsSink sink{0, kw, next_act, next_inq, next_queue, cnt};
+    for (uint64_t base = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * 32; base < items; base += warps * 32)
+        eg_mrelax_items(base, items, queue, kw, ptr, col, wts, w, (uint32_t)k, dist, act, EG_SSSP_BIG_DEG, big,
+                        &cnt->nbig, sink, scanned);
     if (lane == 0 && scanned) atomicAdd(&cnt->relax, scanned);
 }
 
@@ -308,7 +348,8 @@ __global__ void __launch_bounds__(256) k_msssp_push(const uint32_t *__restrict__
 // per 32 edges of it.
 #define EG_MSSSP_CHUNK 256u
 __global__ void __launch_bounds__(256) k_msssp_push_big(const uint32_t *__restrict__ ptr,
-                                                        const uint32_t *__restrict__ col, int k, uint32_t kw,
+                                                        const uint32_t *__restrict__ col,
+                                                        const uint32_t *__restrict__ wts, int k, uint32_t kw,
                                                         uint32_t *dist, const uint32_t *__restrict__ act,
                                                         uint32_t *next_act, uint32_t *next_inq, uint32_t *next_queue,
                                                         WRule w, SsspCounters *cnt, const uint32_t *big,
@@ -332,7 +373,7 @@ __global__ void __launch_bounds__(256) k_msssp_push_big(const uint32_t *__restri
         const uint32_t b = vb + off * EG_MSSSP_CHUNK + 32u * warp;
         if (b < ve) {
             MsSink sink{j, kw, next_act, next_inq, next_queue, cnt};
-            eg_mrelax_span(u, b, ve - b > 32 ? b + 32 : ve, col, w, on, du, s, (uint32_t)k, dist, sink);
+            eg_mrelax(u, b, ve - b > 32 ? b + 32 : ve, col, wts, w, a, du, j, (uint32_t)k, dist, sink);
         }
     }
     if (scanned) atomicAdd(&cnt->relax, scanned);
@@ -364,18 +405,20 @@ __global__ void k_transpose_dist(const uint32_t *__restrict__ dvk, uint32_t n, i
 }
 }  // namespace
 
-extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg_weights *wts, uint32_t *dist_out,
-                             eg_sssp_stats *stats) {
+extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg_weights *wrule_in,
+                             uint32_t *dist_out, eg_sssp_stats *stats) {
     if (!g || !roots) return eg_fail(EG_EINVAL, "NULL argument");
     if (k < 1 || k > 1024) return eg_fail(EG_EINVAL, "k=%d: batched SSSP takes 1..1024 sources", k);
     if (!(g->built & EG_LAYOUT_CSR)) return eg_fail(EG_ENOTBUILT, "SSSP needs the CSR");
-    EG_TRY(check_weights(wts));
+    EG_TRY(check_weights(wrule_in));
     for (int s = 0; s < k; s++)
         if (roots[s] >= g->n) return eg_fail(EG_EINVAL, "root %u >= n", roots[s]);
     eg_ctx *ctx = g->ctx;
     EG_CUDA(cudaSetDevice(ctx->device));
     const uint32_t n = g->n, nw = (n + 31) >> 5, kw = (uint32_t)((k + 31) / 32);
-    const WRule w = eg_make_wrule(wts);
+    const WRule w = eg_make_wrule(wrule_in);
+    const uint32_t *wts = nullptr;
+    EG_TRY(eg_edge_weights(g, w, &wts));
     // work: dist[n*k] | act0, act1 [n*kw] | inq0, inq1 [nw] | q0, q1 [n] | roots | counters
     if ((uint64_t)n * kw >= 0xffffffffull) return eg_fail(EG_EINVAL, "n * ceil(k/32) must be < 2^32");
     const uint64_t off_act0 = (uint64_t)n * k, off_act1 = off_act0 + (uint64_t)n * kw, off_inq0 = off_act1 + (uint64_t)n * kw,
@@ -405,16 +448,16 @@ extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg
     while (qlen > 0) {
         const int nxt = cur ^ 1;
         EG_CUDA(cudaMemsetAsync(&cnt->qsize, 0, 8, ctx->stream));  // qsize and nbig
-        k_msssp_push<<<blocks_for(ctx, (uint64_t)qlen * kw * 32), 256, 0, ctx->stream>>>(
-            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), q[cur], qlen, k, kw, dist, act[cur], act[nxt], inq[nxt],
+        k_msssp_push<<<blocks_for(ctx, (uint64_t)qlen * kw), 256, 0, ctx->stream>>>(
+            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), wts, q[cur], qlen, k, kw, dist, act[cur], act[nxt], inq[nxt],
             q[nxt], w, cnt, big);
         EG_LAUNCHED(ctx);
         k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, kw, bp<uint32_t>(g->csr.ptr), EG_MSSSP_CHUNK,
                                                    bigoff);
         EG_LAUNCHED(ctx);
         k_msssp_push_big<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
-            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), k, kw, dist, act[cur], act[nxt], inq[nxt], q[nxt], w, cnt,
-            big, bigoff);
+            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), wts, k, kw, dist, act[cur], act[nxt], inq[nxt], q[nxt], w,
+            cnt, big, bigoff);
         EG_LAUNCHED(ctx);
         // the current frontier's words and bits are cleared for reuse as "next"
         k_msssp_clear<<<blocks_for(ctx, (uint64_t)qlen * kw), 256, 0, ctx->stream>>>(q[cur], qlen, kw, act[cur], inq[cur]);
@@ -437,7 +480,7 @@ extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg
     }
     EG_CUDA(cudaStreamSynchronize(ctx->stream));
     if (stats) {
-        unsigned long long *dcount = reinterpret_cast<unsigned long long *>(cnt) + 2;
+        unsigned long long *dcount = &cnt->reached;
         EG_CUDA(cudaMemsetAsync(dcount, 0, 8, ctx->stream));
         k_count_reached<<<blocks_for(ctx, (uint64_t)n * k), 256, 0, ctx->stream>>>(dist, (uint64_t)n * k, dcount,
                                                                                    w.inf());
