@@ -31,8 +31,8 @@ METRIC, UNIT = "GTEPS", "GTEPS"
 # DRAM bytes (read + write) of one row-kernel launch per CSC entry, from an
 # ncu capture of PageRank on directed RMAT-22 (the kernel's traffic grows with
 # the entries); the summary and its command are in
-# profiles/k_coo4_rows_pagerank_rmat22.md.
-PR_ROWS_DRAM_BYTES_PER_ENTRY = 593.69e6 / 67108864
+# profiles/k_coov_rows_pagerank_rmat22.md.
+PR_ROWS_DRAM_BYTES_PER_ENTRY = 588.27e6 / 67108864
 
 
 def peaks():
