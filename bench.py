@@ -194,8 +194,9 @@ def run_ours(args):
         roof = {"bound": "hbm", "achieved": dom["row_kernel_gbps"], "peak": hbm, "unit": "GB/s",
                 "frac": dom["row_kernel_gbps"] / hbm,
                 "traffic": PR_ROWS_DRAM_BYTES_PER_ENTRY * dom["m"] if PR_ROWS_DRAM_BYTES_PER_ENTRY else None,
-                "kernel": "k_coov_rows<PrOp<0>, %d, %d> (PageRank pull, RMAT-%d directed)"
-                          % (dom["schedule"]["tile_entries"], dom["schedule"]["entries_per_lane"], scale),
+                "kernel": "k_coov_rows<PrOp<0>, %d, %d> prefetch=%d min_blocks=%d (PageRank pull, RMAT-%d directed)"
+                          % (dom["schedule"]["tile"], dom["schedule"]["per_lane"], dom["schedule"]["prefetch"],
+                             dom["schedule"]["min_blocks"], scale),
                 "algorithmic_bytes": dom["bytes_per_iter"], "peak_source": src}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -240,8 +241,7 @@ def kernel_reports(ctx, eg, scale, args):
         "ms_per_iter_graph_replay": stg.ms / 10, "bytes_per_iter": bytes_it,
         "bytes_rule": "8 per CSC entry (row id + column) + 16 per vertex (contribution, degree, rank, next contribution)",
         "build_ms": g.info().build_ms, "m": m,
-        "schedule": {"tile_entries": cands[chosen][0], "entries_per_lane": cands[chosen][1],
-                     "candidates_ms": [[t, u, ms] for t, u, ms in cands]}}
+        "schedule": dict(cands[chosen], candidates=cands)}
     g.free()
     return rep
 

@@ -184,14 +184,16 @@ class Graph:
 
     def tune(self):
         """Times the row-kernel schedules on this graph and keeps the fastest;
-        returns [(tile entries, entries per lane, ms per iteration)] and the
-        chosen index."""
+        returns [{tile, per_lane, prefetch, min_blocks, ms}] and the chosen
+        index."""
         r = L.TuneResult()
         L.check(lib().eg_graph_tune(self._h, ctypes.byref(r)))
-        return [(r.tile_entries[i], r.entries_per_lane[i], r.ms[i]) for i in range(r.ncand)], r.chosen
+        cands = [{"tile": r.tile_entries[i], "per_lane": r.entries_per_lane[i], "prefetch": r.prefetch[i],
+                  "min_blocks": r.min_blocks[i], "ms": r.ms[i]} for i in range(r.ncand)]
+        return cands, r.chosen
 
-    def set_row_schedule(self, tile_entries, entries_per_lane):
-        L.check(lib().eg_graph_set_row_schedule(self._h, tile_entries, entries_per_lane))
+    def set_row_schedule(self, index):
+        L.check(lib().eg_graph_set_row_schedule(self._h, index))
 
     def sample_roots(self, k, seed):
         r = np.empty(k, dtype=np.uint32)

@@ -48,7 +48,7 @@ class ServeStats(ctypes.Structure):
 
 class TuneResult(ctypes.Structure):
     _fields_ = [("ncand", c_int), ("chosen", c_int), ("tile_entries", c_int * 8), ("entries_per_lane", c_int * 8),
-                ("ms", c_f32 * 8)]
+                ("prefetch", c_int * 8), ("min_blocks", c_int * 8), ("ms", c_f32 * 8)]
 
 
 class SpmvOpts(ctypes.Structure):
@@ -135,7 +135,7 @@ SIGNATURES = {
     "eg_sample_roots": (c_int, [c_void_p, c_int, c_u64, c_void_p]),
     "eg_ppr_multi": (c_int, [c_void_p, c_void_p, c_void_p, c_int, P(PprOpts), c_void_p, P(PprStats)]),
     "eg_graph_tune": (c_int, [c_void_p, P(TuneResult)]),
-    "eg_graph_set_row_schedule": (c_int, [c_void_p, c_int, c_int]),
+    "eg_graph_set_row_schedule": (c_int, [c_void_p, c_int]),
     "eg_ppr": (c_int, [c_void_p, c_void_p, c_u32, P(PprOpts), c_void_p, P(PprStats)]),
     "eg_serve_opts_default": (None, [P(ServeOpts)]),
     "eg_serve_stats": (c_int, [c_void_p, P(ServeStats)]),

@@ -401,6 +401,31 @@ __global__ void k_coo_empty_rows(const uint32_t *__restrict__ ptr, uint32_t n, d
     }
 }
 
+// The chunk of a warp tile starting at cb: lane l's entries cb+U*l ..
+// cb+U*l+U-1 (128-bit loads), rows past the tile end E1 set to EG_MP_NONE.
+template <int U>
+__device__ __forceinline__ void eg_coov_load(const uint32_t *__restrict__ rid, const uint32_t *__restrict__ col,
+                                             uint32_t cb, uint32_t E1, uint32_t lane, uint32_t (&r)[U],
+                                             uint32_t (&u)[U]) {
+    const uint32_t e = cb + U * lane;
+    if (e + U - 1 < E1) {
+#pragma unroll
+        for (int h = 0; h < U / 4; h++) {
+            const uint4 rr = __ldg(reinterpret_cast<const uint4 *>(rid + e) + h);
+            const uint4 cc = __ldg(reinterpret_cast<const uint4 *>(col + e) + h);
+            r[4 * h] = rr.x; r[4 * h + 1] = rr.y; r[4 * h + 2] = rr.z; r[4 * h + 3] = rr.w;
+            u[4 * h] = cc.x; u[4 * h + 1] = cc.y; u[4 * h + 2] = cc.z; u[4 * h + 3] = cc.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            const bool in = e + k < E1;
+            r[k] = in ? __ldg(rid + e + k) : EG_MP_NONE;
+            u[k] = in ? __ldg(col + e + k) : 0u;
+        }
+    }
+}
+
 // U entries per lane (U = 4 or 8): lane l of a warp holds entries
 // base+U*l .. base+U*l+U-1 (128-bit loads of rid and col), sums the runs of
 // equal rows among them locally, and one segmented scan per 32*U entries
@@ -410,11 +435,16 @@ __global__ void k_coo_empty_rows(const uint32_t *__restrict__ ptr, uint32_t n, d
 // after lane 31 is carried to the next chunk.  Tiles are multiples of 32*U
 // entries, so only the last tile has padding entries (row EG_MP_NONE, never
 // emitted).
-template <class Op, int TILE_E, int U, bool REDUCE>
-__global__ void __launch_bounds__(256) k_coov_rows(const uint32_t *__restrict__ rid, const uint32_t *__restrict__ col,
-                                                   uint32_t m, uint32_t ntiles,
-                                                   eg_mp_carry<typename Op::A> *__restrict__ carry,
-                                                   double2 *__restrict__ part, Op op) {
+//
+// PF: the next chunk's rid/col words are loaded before the current chunk's
+// gathers, so the streaming loads of one chunk overlap the gathers and scan
+// of the previous one.  MINB: resident CTAs per SM asked of the compiler,
+// which bounds the registers per thread (6: 42, 8: every warp slot, 32).
+template <class Op, int TILE_E, int U, bool REDUCE, bool PF = false, int MINB = 6>
+__global__ void __launch_bounds__(256, MINB) k_coov_rows(const uint32_t *__restrict__ rid,
+                                                         const uint32_t *__restrict__ col, uint32_t m, uint32_t ntiles,
+                                                         eg_mp_carry<typename Op::A> *__restrict__ carry,
+                                                         double2 *__restrict__ part, Op op) {
     static_assert(U == 4 || U == 8, "4 or 8 entries per lane");
     static_assert(TILE_E % (32 * U) == 0, "tiles hold whole chunks");
     constexpr uint32_t CH = 32u * U;  // entries per chunk
@@ -446,24 +476,20 @@ __global__ void __launch_bounds__(256) k_coov_rows(const uint32_t *__restrict__ 
             const float2 d = op.emit(row, val);
             if (REDUCE) redf.add(d);
         };
+        uint32_t rn[U], un[U];  // prefetched next chunk (PF)
+        if (PF) eg_coov_load<U>(rid, col, E0, E1, lane, rn, un);
         for (uint32_t base = E0; base < E1; base += CH) {
             const uint32_t e = base + U * lane;
             uint32_t r[U], u[U];
-            if (e + U - 1 < E1) {
-#pragma unroll
-                for (int h = 0; h < U / 4; h++) {
-                    const uint4 rr = __ldg(reinterpret_cast<const uint4 *>(rid + e) + h);
-                    const uint4 cc = __ldg(reinterpret_cast<const uint4 *>(col + e) + h);
-                    r[4 * h] = rr.x; r[4 * h + 1] = rr.y; r[4 * h + 2] = rr.z; r[4 * h + 3] = rr.w;
-                    u[4 * h] = cc.x; u[4 * h + 1] = cc.y; u[4 * h + 2] = cc.z; u[4 * h + 3] = cc.w;
-                }
-            } else {
+            if (PF) {
 #pragma unroll
                 for (int k = 0; k < U; k++) {
-                    const bool in = e + k < E1;
-                    r[k] = in ? __ldg(rid + e + k) : EG_MP_NONE;
-                    u[k] = in ? __ldg(col + e + k) : 0u;
+                    r[k] = rn[k];
+                    u[k] = un[k];
                 }
+                if (base + CH < E1) eg_coov_load<U>(rid, col, base + CH, E1, lane, rn, un);
+            } else {
+                eg_coov_load<U>(rid, col, base, E1, lane, r, u);
             }
             V v[U];
 #pragma unroll

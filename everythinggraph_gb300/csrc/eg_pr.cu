@@ -226,14 +226,19 @@ __global__ void k_pr_reduce(const double2 *__restrict__ part, uint32_t nparts, e
 // per lane.  part[] receives per-CTA partials of the main kernel, then of the
 // empty-row kernel, then of the fix-up; returns their count.  The schedule
 // (TILE, U) is the graph's row_cfg, picked by eg_graph_tune.
-#define EG_COO_TILE_MIN 1024
+#define EG_COO_TILE_MIN 512
 #define EG_PR_CHECK 4  // iterations between reads of the stop flag
 #define EG_PR_RES_BLOCKS 1024
-#define EG_ROW_CFGS 5
-static const int kRowTile[EG_ROW_CFGS] = {2048, 1024, 4096, 2048, 4096};
-static const int kRowU[EG_ROW_CFGS] = {4, 4, 4, 8, 8};
+#define EG_ROW_CFGS 8
+struct RowCfg {
+    int tile, u, pf, minb;
+};
+// min_blocks bounds the registers: 6 resident CTAs of 256 threads leave 42
+// registers per thread, 5 leave 51, 4 leave 64, 8 leave 32.
+static const RowCfg kRowCfg[EG_ROW_CFGS] = {{1024, 4, 1, 5}, {2048, 4, 0, 6}, {2048, 4, 1, 5}, {1024, 4, 1, 6},
+                                            {512, 4, 1, 5},  {1024, 8, 1, 4}, {1024, 4, 0, 8}, {2048, 8, 0, 5}};
 
-template <class Op, int TILE, int U, bool REDUCE>
+template <class Op, int TILE, int U, bool REDUCE, bool PF, int MINB>
 static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts,
                         cudaEvent_t ev_begin, cudaEvent_t ev_end) {
     eg_ctx *ctx = g->ctx;
@@ -246,7 +251,7 @@ static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *pa
     if (g2 > (uint32_t)ctx->sm_count * 8) g2 = (uint32_t)ctx->sm_count * 8;
     if (g1) {
         if (ev_begin) EG_CUDA(cudaEventRecord(ev_begin, ctx->stream));
-        k_coov_rows<Op, TILE, U, REDUCE><<<g1, 256, 0, ctx->stream>>>(
+        k_coov_rows<Op, TILE, U, REDUCE, PF, MINB><<<g1, 256, 0, ctx->stream>>>(
             bp<uint32_t>(adj.rid), bp<uint32_t>(adj.col), m, ntiles, bp<eg_mp_carry<A>>(carry_buf), part, op);
         EG_LAUNCHED(ctx);
         if (ev_end) EG_CUDA(cudaEventRecord(ev_end, ctx->stream));
@@ -266,13 +271,19 @@ static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *pa
 template <class Op, bool REDUCE>
 static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts,
                       cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr) {
+#define EG_ROW_CASE(i, T, U, PF, MB) \
+    case i: return coo_launch_t<Op, T, U, REDUCE, PF, MB>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
     switch (g->row_cfg) {
-    case 1: return coo_launch_t<Op, 1024, 4, REDUCE>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
-    case 2: return coo_launch_t<Op, 4096, 4, REDUCE>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
-    case 3: return coo_launch_t<Op, 2048, 8, REDUCE>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
-    case 4: return coo_launch_t<Op, 4096, 8, REDUCE>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
-    default: return coo_launch_t<Op, 2048, 4, REDUCE>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
+        EG_ROW_CASE(1, 2048, 4, false, 6)
+        EG_ROW_CASE(2, 2048, 4, true, 5)
+        EG_ROW_CASE(3, 1024, 4, true, 6)
+        EG_ROW_CASE(4, 512, 4, true, 5)
+        EG_ROW_CASE(5, 1024, 8, true, 4)
+        EG_ROW_CASE(6, 1024, 4, false, 8)
+        EG_ROW_CASE(7, 2048, 8, false, 5)
+        default: return coo_launch_t<Op, 1024, 4, REDUCE, true, 5>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
     }
+#undef EG_ROW_CASE
 }
 
 extern "C" void eg_pr_opts_default(eg_pr_opts *o) {
@@ -489,15 +500,11 @@ extern "C" int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out,
 }
 
 // ============================================================== autotuner
-extern "C" int eg_graph_set_row_schedule(eg_graph *g, int tile_entries, int entries_per_lane) {
+extern "C" int eg_graph_set_row_schedule(eg_graph *g, int index) {
     if (!g) return eg_fail(EG_EINVAL, "NULL graph");
-    for (int c = 0; c < EG_ROW_CFGS; c++)
-        if (kRowTile[c] == tile_entries && kRowU[c] == entries_per_lane) {
-            g->row_cfg = c;
-            return EG_OK;
-        }
-    return eg_fail(EG_EINVAL, "no row schedule with %d entries per warp tile and %d per lane", tile_entries,
-                   entries_per_lane);
+    if (index < 0 || index >= EG_ROW_CFGS) return eg_fail(EG_EINVAL, "row schedule %d of %d", index, EG_ROW_CFGS);
+    g->row_cfg = index;
+    return EG_OK;
 }
 
 extern "C" int eg_graph_tune(eg_graph *g, eg_tune_result *out) {
@@ -517,8 +524,10 @@ extern "C" int eg_graph_tune(eg_graph *g, eg_tune_result *out) {
         eg_pr_stats st;
         EG_TRY(pr_run(g, o, none, 0, nullptr, &st));  // warm-up (caches, carries)
         EG_TRY(pr_run(g, o, none, 0, nullptr, &st));
-        r.tile_entries[c] = kRowTile[c];
-        r.entries_per_lane[c] = kRowU[c];
+        r.tile_entries[c] = kRowCfg[c].tile;
+        r.entries_per_lane[c] = kRowCfg[c].u;
+        r.prefetch[c] = kRowCfg[c].pf;
+        r.min_blocks[c] = kRowCfg[c].minb;
         r.ms[c] = st.row_kernel_ms;
         if (st.row_kernel_ms < r.ms[best]) best = c;
     }

@@ -160,22 +160,26 @@ void eg_pr_opts_default(eg_pr_opts *o);
 int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out, eg_pr_stats *stats);
 
 /* ---- row-kernel autotuner (no reference counterpart) ---------------------
- * The PageRank/SpMV row kernel walks the CSC as warp tiles of 1024, 2048 or
- * 4096 entries with 4 or 8 entries per lane.  eg_graph_tune times every
- * schedule on this graph (two 6-iteration PageRank runs each, CUDA events
- * around the row kernel) and keeps the fastest for eg_pagerank, eg_ppr and
- * eg_spmv on this graph; eg_graph_set_row_schedule picks one by hand.  The
- * default is 2048 x 4.  Schedules change only how rows are split between
- * warps, i.e. the fp32 summation order. */
+ * The PageRank/SpMV row kernel walks the CSC as warp tiles of 512, 1024 or
+ * 2048 entries with 4 or 8 entries per lane, optionally loading the next
+ * chunk's indices ahead (prefetch), with min_blocks resident CTAs per SM
+ * bounding its registers.
+ * eg_graph_tune times every schedule on this graph (two 6-iteration PageRank
+ * runs each, CUDA events around the row kernel) and keeps the fastest for
+ * eg_pagerank, eg_ppr and eg_spmv on this graph; eg_graph_set_row_schedule
+ * picks one by index (0 = 1024 x 4 with prefetch, the default).  Schedules change only
+ * how rows are split between warps, i.e. the fp32 summation order. */
 typedef struct {
     int ncand;
     int chosen;               /* index of the schedule kept */
     int tile_entries[8];
     int entries_per_lane[8];
+    int prefetch[8];
+    int min_blocks[8];
     float ms[8];              /* mean row-kernel time per iteration */
 } eg_tune_result;
 int eg_graph_tune(eg_graph *g, eg_tune_result *out);
-int eg_graph_set_row_schedule(eg_graph *g, int tile_entries, int entries_per_lane);
+int eg_graph_set_row_schedule(eg_graph *g, int index);
 
 /* ---- SpMV (replaces spmv.c:98-135) ---------------------------------------
  * Row reductions over a built adjacency:
