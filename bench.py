@@ -272,13 +272,26 @@ def spmv_report(ctx, eg, log_n=25, degree=32):
     # PageRank over the same graph, 10 iterations
     _, st = g.pagerank(iterations=10, copy_out=False)
     out["pagerank_ms_per_iter"] = st.ms / 10
-    g.free()
-    gg = ctx.er(n, m, 4)
+    # the 64 x 64 grid layout and the grid kernels (cells in L2-sized blocks)
     import time as _t
     t0 = _t.perf_counter()
-    gg.build_grid(64)
+    g.build_grid(64)
     out["grid64_build_s"] = _t.perf_counter() - t0
-    gg.free()
+    grid = {}
+    for kind in ("f32", "f64"):
+        g.spmv(x, kind, value_seed=9, copy_out=False, grid=True)
+        y, ms = g.spmv(x, kind, value_seed=9, grid=True)
+        bytes_ = 12 * m + (16 if kind == "f64" else 12) * n
+        rec = {"ms": ms, "gbps": bytes_ / (ms / 1e3) / 1e9}
+        if kind == "f32":
+            d = np.abs(y.astype(np.float64) - y64)
+            rec["max_rel_err"] = float((d[nz] / np.abs(y64[nz])).max())
+            rec["l1_rel_err"] = float(d.sum() / np.abs(y64).sum())
+        grid[kind] = rec
+    _, st = g.pagerank(iterations=10, copy_out=False, grid=True)
+    grid["pagerank_ms_per_iter"] = st.ms / 10
+    out["grid64"] = grid
+    g.free()
     return out
 
 

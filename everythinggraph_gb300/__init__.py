@@ -202,24 +202,25 @@ class Graph:
 
     # ---------------------------------------------------------------- algorithms
     def pagerank(self, iterations=10, damping=0.85, prev_init=-1.0, swap=True, deg_multiplier=1, dangling=False,
-                 compensated=False, tolerance=0.0, copy_out=True, use_graph=False):
+                 compensated=False, tolerance=0.0, copy_out=True, use_graph=False, grid=False):
         o = L.PrOpts()
         lib().eg_pr_opts_default(ctypes.byref(o))
         o.iterations, o.damping, o.prev_init, o.swap = iterations, damping, prev_init, int(swap)
         o.deg_multiplier, o.dangling, o.compensated, o.tolerance = deg_multiplier, int(dangling), int(compensated), tolerance
         o.use_graph = int(use_graph)
+        o.grid = int(grid)
         st = L.PrStats()
         out = np.empty(self.n, dtype=np.float32) if copy_out else None
         L.check(lib().eg_pagerank(self._h, ctypes.byref(o), _ptr(out), ctypes.byref(st)))
         return out, st
 
-    def spmv(self, x, kind="u32_pull", value_seed=0, unit_values=False, copy_out=True):
+    def spmv(self, x, kind="u32_pull", value_seed=0, unit_values=False, copy_out=True, grid=False):
         k = SPMV_KINDS[kind]
         xd = np.uint32 if kind.startswith("u32") else np.float32
         x = np.ascontiguousarray(x, dtype=xd)
         yd = np.float64 if kind == "f64" else xd
         y = np.empty(self.n, dtype=yd) if copy_out else None
-        o = L.SpmvOpts(k, value_seed, int(unit_values))
+        o = L.SpmvOpts(k, value_seed, int(unit_values), int(grid))
         ms = ctypes.c_float()
         L.check(lib().eg_spmv(self._h, ctypes.byref(o), _ptr(x), _ptr(y), ctypes.byref(ms)))
         return y, ms.value

@@ -33,7 +33,7 @@ class GraphInfo(ctypes.Structure):
 class PrOpts(ctypes.Structure):
     _fields_ = [("iterations", c_int), ("damping", c_f32), ("prev_init", c_f32), ("swap", c_int),
                 ("deg_multiplier", c_u32), ("dangling", c_int), ("compensated", c_int), ("tolerance", c_f64),
-                ("use_graph", c_int)]
+                ("use_graph", c_int), ("grid", c_int)]
 
 
 class PrStats(ctypes.Structure):
@@ -52,7 +52,7 @@ class TuneResult(ctypes.Structure):
 
 
 class SpmvOpts(ctypes.Structure):
-    _fields_ = [("kind", c_int), ("value_seed", c_u64), ("unit_values", c_int)]
+    _fields_ = [("kind", c_int), ("value_seed", c_u64), ("unit_values", c_int), ("grid", c_int)]
 
 
 class BfsOpts(ctypes.Structure):

@@ -292,7 +292,8 @@ extern "C" void eg_graph_free(eg_graph *g) {
                       &g->rank,    &g->contrib0,     &g->contrib1,
                       &g->pr_part,      &g->pr_stats,    &g->mp_carry,    &g->errflag,     &g->rank_p,    &g->rank_q,    &g->level,          &g->parent,       &g->dist,
                       &g->label,        &g->spmv_x,      &g->spmv_y,      &g->spmv_vals,      &g->bfs_work,     &g->msbfs_work,
-                      &g->sssp_work,    &g->ppr_work,    &g->wts};
+                      &g->sssp_work,    &g->ppr_work,    &g->wts,
+                      &g->grid_order,   &g->grid_units,  &g->grid_off,    &g->grid_vals,   &g->grid_acc};
     for (eg_buf *b : bufs) eg_buf_free(c, *b);
     for (eg_bfs_graph &bg : g->bfsg) {
         if (bg.exec) cudaGraphExecDestroy(bg.exec);
@@ -815,6 +816,8 @@ extern "C" int eg_graph_build_grid(eg_graph *g, uint32_t P) {
     cleanup();
     g->grid_p = P;
     g->built |= EG_LAYOUT_GRID;
+    g->grid_order_p = 0;  // cell order and edge values follow the new cells
+    g->grid_vals_kind = 0;
     return EG_OK;
 }
 

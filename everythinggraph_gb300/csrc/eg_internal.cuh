@@ -100,6 +100,12 @@ struct eg_graph {
     // grid
     uint32_t grid_p;
     eg_buf cell_ptr, gsrc, gdst;
+    // grid SpMV/PageRank: cell visiting order, work-unit offsets, edge values,
+    // accumulators (eg_grid.cu)
+    eg_buf grid_order, grid_units, grid_off, grid_vals, grid_acc;
+    uint32_t grid_order_p = 0, grid_block = 0;
+    int grid_vals_kind = 0;
+    uint64_t grid_vals_seed = 0;
     // algorithm state, allocated on first use and reused
     eg_buf rank, rank_p, rank_q, contrib0, contrib1, pr_part, pr_stats, mp_carry, errflag;
     eg_buf level, parent, dist, label, spmv_x, spmv_y, spmv_vals;
@@ -220,6 +226,9 @@ struct eg_wrule {
     __device__ __forceinline__ uint32_t extend(uint32_t du, uint32_t u, uint32_t v) const { return add(du, weight(u, v)); }
 };
 struct eg_graph;
+// SpMV / PageRank over the 2-D grid layout (eg_grid.cu).
+int eg_grid_spmv(eg_graph *g, int kind, uint64_t value_seed, int unit_values, const void *d_x, void *d_y);
+int eg_grid_pagerank(eg_graph *g, const eg_pr_opts &o, float *rank_out, eg_pr_stats *stats);
 // The CSR-order weight array of rule w, computed once per rule and kept in
 // the graph (replaced when another rule is asked for).
 int eg_edge_weights(eg_graph *g, const eg_wrule &w, const uint32_t **out);

@@ -297,6 +297,7 @@ extern "C" void eg_pr_opts_default(eg_pr_opts *o) {
     o->compensated = 0;
     o->tolerance = 0.0;
     o->use_graph = 0;
+    o->grid = 0;
 }
 
 // Launches every iteration; with `timed`, the row kernels of the first
@@ -493,6 +494,10 @@ extern "C" int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out,
     if (opts) o = *opts;
     else eg_pr_opts_default(&o);
     if (o.iterations < 0 || o.deg_multiplier == 0) return eg_fail(EG_EINVAL, "bad PageRank options");
+    if (o.grid) {
+        EG_CUDA(cudaSetDevice(g->ctx->device));
+        return eg_grid_pagerank(g, o, rank_out, stats);
+    }
     EG_TRY(pr_prepare(g));
     PprSeeds none;
     memset(&none, 0, sizeof(none));
@@ -682,7 +687,7 @@ extern "C" int eg_spmv(eg_graph *g, const eg_spmv_opts *opts, const void *x, voi
     const int kind = opts->kind;
     if (kind < EG_SPMV_U32_PULL || kind > EG_SPMV_F64) return eg_fail(EG_EINVAL, "unknown SpMV kind %d", kind);
     const bool pull = kind == EG_SPMV_U32_PULL || kind >= EG_SPMV_F32;
-    const unsigned need = pull ? EG_LAYOUT_CSC : EG_LAYOUT_CSR;
+    const unsigned need = opts->grid ? EG_LAYOUT_GRID : (pull ? EG_LAYOUT_CSC : EG_LAYOUT_CSR);
     if (!(g->built & need)) return eg_fail(EG_ENOTBUILT, "SpMV kind %d needs layout %u", kind, need);
     eg_ctx *ctx = g->ctx;
     EG_CUDA(cudaSetDevice(ctx->device));
@@ -692,6 +697,15 @@ extern "C" int eg_spmv(eg_graph *g, const eg_spmv_opts *opts, const void *x, voi
     EG_TRY(eg_buf_ensure(ctx, g->spmv_x, (uint64_t)n * 4));
     EG_TRY(eg_buf_ensure(ctx, g->spmv_y, (uint64_t)n * ysz));
     EG_CUDA(cudaMemcpyAsync(g->spmv_x.p, x, (uint64_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    if (opts->grid) {
+        EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
+        EG_TRY(eg_grid_spmv(g, kind, opts->value_seed, opts->unit_values, g->spmv_x.p, g->spmv_y.p));
+        EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+        if (y) EG_CUDA(cudaMemcpyAsync(y, g->spmv_y.p, (uint64_t)n * ysz, cudaMemcpyDeviceToHost, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (ms) EG_CUDA(cudaEventElapsedTime(ms, ctx->ev0, ctx->ev1));
+        return EG_OK;
+    }
     if (kind >= EG_SPMV_F32) {
         int vk = opts->unit_values ? 1 : 2;
         if (!g->spmv_vals.p || g->spmv_vals_kind != vk || (vk == 2 && g->spmv_vals_seed != opts->value_seed)) {

@@ -147,6 +147,9 @@ typedef struct {
     int compensated;
     double tolerance;
     int use_graph; /* 1: replay the iteration as a captured CUDA graph */
+    int grid;      /* 1: iterate over the 2-D grid layout (prgrid_cilk.c:62-141):
+                      cells in L2-sized blocks, sums by atomic adds (not in a
+                      fixed order); needs eg_graph_build_grid and the CSR */
 } eg_pr_opts;
 typedef struct {
     int iterations_run;
@@ -201,6 +204,9 @@ typedef struct {
     int kind;
     uint64_t value_seed; /* val(e) = U[0,1) hashed from (seed, min(u,v), max(u,v)) */
     int unit_values;     /* 1: val(e) = 1 */
+    int grid;            /* 1: over the 2-D grid layout (spmv.c's grid modes):
+                            cells in L2-sized blocks, y by atomic adds (u32
+                            exact; f32/f64 not in a fixed order; no F32_COMP) */
 } eg_spmv_opts;
 /* x: host array of n (u32 for U32 kinds, f32 otherwise); y: host array of n
  * (u32, f32 or f64 for EG_SPMV_F64), or NULL to keep y on the device. */
