@@ -118,6 +118,7 @@ def run_ours(args):
     t0 = time.perf_counter()
     g.build(eg.CSR | eg.CSC)
     build_ms = g.info().build_ms
+    g.tune()  # row schedule and BFS level-loop form for this graph (untimed setup)
     roots = g.sample_roots(W["roots"], W["root_seed"])
     stream = torch.cuda.ExternalStream(ctx.stream)
 
@@ -207,7 +208,7 @@ def run_ours(args):
         "e2e": {"value": e_edges * world / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
-        "load": {"build_ms": build_ms},
+        "load": {"build_ms": build_ms, "bfs_tuning": g.bfs_tuning},
         "roofline": roof,
         "clocks": clk.summary(),
         "kernels": kernels,
@@ -498,6 +499,32 @@ def ppr_report(ctx, eg, scale=24, nq=32, seed=7):
             "single_iters_each": its / 8, "speedup": per_single * nq / stb.ms}
 
 
+def bfs_report(ctx, eg, scale=24, roots=16):
+    """Single-source BFS (levels + parents) on the undirected RMAT graph: the
+    CUDA-graph level loop and the host-driven loop (the same kernels launched
+    level by level, which a profiler can capture one by one), plus WCC."""
+    n = 1 << scale
+    g = ctx.rmat(scale, 16 * n, 2, undirected=True).build(eg.CSR | eg.CSC)
+    rs = g.sample_roots(roots, 3)
+    out = {"workload": "bfs rmat%d undirected, %d roots" % (scale, roots)}
+    for name, host_loop in (("graph_loop", False), ("host_loop", True)):
+        g.bfs(int(rs[0]), parents=True, copy_out=False, host_loop=host_loop)
+        ms, te, lv, pl = 0.0, 0, 0, 0
+        for r in rs:
+            _, _, st = g.bfs(int(r), parents=True, copy_out=False, host_loop=host_loop)
+            ms += st.ms
+            te += st.edges_traversed
+            lv += st.levels
+            pl += st.pull_levels
+        out[name] = {"ms_per_bfs": ms / roots, "gteps": te / (ms / 1e3) / 1e9, "levels": lv / roots,
+                     "pull_levels": pl / roots}
+    g.wcc(copy_out=False)
+    _, st = g.wcc(copy_out=False)
+    out["wcc"] = {"ms": st.ms, "components": st.components, "rounds": st.rounds}
+    g.free()
+    return out
+
+
 def only_report(name, args):
     """One report alone (profiling and quick checks)."""
     import everythinggraph_gb300 as eg
@@ -515,6 +542,8 @@ def only_report(name, args):
         out = sssp_report(ctx, eg, args.scale or 23)
     elif name == "ppr":
         out = ppr_report(ctx, eg, scale)
+    elif name == "bfs":
+        out = bfs_report(ctx, eg, scale)
     else:  # msbfs
         n = 1 << scale
         g = ctx.rmat(scale, 16 * n, 2, undirected=True).build(eg.CSR | eg.CSC)
@@ -535,7 +564,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--pr-only", action="store_true", help="only the PageRank pull report (profiling)")
     ap.add_argument("--serve-only", action="store_true", help="only the serving report")
-    ap.add_argument("--only", choices=["pr", "spmv", "sssp", "msbfs", "ppr", "serve"],
+    ap.add_argument("--only", choices=["pr", "spmv", "sssp", "msbfs", "ppr", "bfs", "serve"],
                     help="only one kernel report (profiling)")
     ap.add_argument("--rate", type=float, default=20000.0)
     ap.add_argument("--queries", type=int, default=1000)

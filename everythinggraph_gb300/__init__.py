@@ -190,6 +190,7 @@ class Graph:
         L.check(lib().eg_graph_tune(self._h, ctypes.byref(r)))
         cands = [{"tile": r.tile_entries[i], "per_lane": r.entries_per_lane[i], "prefetch": r.prefetch[i],
                   "min_blocks": r.min_blocks[i], "ms": r.ms[i]} for i in range(r.ncand)]
+        self.bfs_tuning = {"graph_ms": r.bfs_graph_ms, "host_ms": r.bfs_host_ms, "host_loop": r.bfs_host_loop}
         return cands, r.chosen
 
     def set_row_schedule(self, index):
@@ -225,9 +226,12 @@ class Graph:
         L.check(lib().eg_spmv(self._h, ctypes.byref(o), _ptr(x), _ptr(y), ctypes.byref(ms)))
         return y, ms.value
 
-    def bfs(self, root, direction="auto", switch_divisor=20.0, parents=False, copy_out=True, host_loop=False):
+    def bfs(self, root, direction="auto", switch_divisor=20.0, parents=False, copy_out=True, host_loop=None):
+        """host_loop: None = the form eg_graph_tune kept (else the CUDA graph),
+        False = CUDA-graph level loop, True = host-driven level loop."""
+        hl = -1 if host_loop is None else int(bool(host_loop))
         o = L.BfsOpts({"auto": L.EG_BFS_AUTO, "push": L.EG_BFS_PUSH_ONLY, "pull": L.EG_BFS_PULL_ONLY}[direction],
-                      switch_divisor, int(parents), int(host_loop))
+                      switch_divisor, int(parents), hl)
         n = self.n
         lv = np.empty(n, dtype=np.int32) if copy_out else None
         par = np.empty(n, dtype=np.int32) if (parents and copy_out) else None

@@ -48,7 +48,8 @@ class ServeStats(ctypes.Structure):
 
 class TuneResult(ctypes.Structure):
     _fields_ = [("ncand", c_int), ("chosen", c_int), ("tile_entries", c_int * 8), ("entries_per_lane", c_int * 8),
-                ("prefetch", c_int * 8), ("min_blocks", c_int * 8), ("ms", c_f32 * 8)]
+                ("prefetch", c_int * 8), ("min_blocks", c_int * 8), ("ms", c_f32 * 8), ("bfs_graph_ms", c_f32),
+                ("bfs_host_ms", c_f32), ("bfs_host_loop", c_int)]
 
 
 class SpmvOpts(ctypes.Structure):

@@ -13,6 +13,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include "eg_bigwork.cuh"
 #include "eg_internal.cuh"
 #include "eg_mspull.cuh"
 
@@ -29,6 +30,7 @@ struct BfsCounters {
 // Frontier vertices with more out-edges than this are expanded by the whole
 // grid (k_bfs_push_big) instead of one warp: an RMAT hub has 10^5..10^6.
 #define EG_BFS_BIG_DEG 2048u
+#define EG_BFS_CHUNK 4096u  // edges of a deferred hub per CTA work unit
 
 // Block-level reduction of per-thread counters: one atomic per block.
 __device__ __forceinline__ void block_add_counters(BfsCounters *c, uint32_t cnt, unsigned long long deg) {
@@ -150,19 +152,19 @@ __global__ void __launch_bounds__(256) k_bfs_push(const uint32_t *__restrict__ p
 __global__ void __launch_bounds__(256) k_bfs_push_big(const uint32_t *__restrict__ ptr,
                                                       const uint32_t *__restrict__ col,
                                                       const uint32_t *__restrict__ deg, const uint32_t *big,
-                                                      uint32_t *visited, uint32_t *next_bm, uint32_t *next_queue,
-                                                      int32_t *level, int32_t *parent, int32_t next_level,
-                                                      BfsCounters *cnt) {
+                                                      const uint32_t *__restrict__ bigoff, uint32_t *visited,
+                                                      uint32_t *next_bm, uint32_t *next_queue, int32_t *level,
+                                                      int32_t *parent, int32_t next_level, BfsCounters *cnt) {
     const uint32_t nbig = *(volatile uint32_t *)&cnt->nbig;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nthreads = gridDim.x * blockDim.x;
     uint32_t my_cnt = 0;
     unsigned long long my_deg = 0;
-    for (uint32_t bi = 0; bi < nbig; bi++) {
-        const uint32_t u = big[bi];
-        const uint32_t b = ptr[u], e = ptr[u + 1];
+    const uint32_t total = nbig ? bigoff[nbig] : 0u;
+    for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
+        const uint32_t i = eg_big_item(bigoff, nbig, c);
+        const uint32_t u = big[i];
+        const uint32_t b = ptr[u] + (c - bigoff[i]) * EG_BFS_CHUNK, e = min(ptr[u + 1], b + EG_BFS_CHUNK);
         // warp-uniform trip count: each warp covers 32 consecutive entries
-        for (uint32_t p0 = b + (tid & ~31u); p0 < e; p0 += nthreads) {
+        for (uint32_t p0 = b + (threadIdx.x & ~31u); p0 < e; p0 += blockDim.x) {
             const uint32_t p = p0 + (threadIdx.x & 31);
             bool claimed = false;
             uint32_t v = 0;
@@ -403,23 +405,23 @@ __global__ void __launch_bounds__(256) k_bfsg_push(const BfsGState *st, const ui
 __global__ void __launch_bounds__(256) k_bfsg_push_big(const BfsGState *st, const uint32_t *__restrict__ ptr,
                                                        const uint32_t *__restrict__ col,
                                                        const uint32_t *__restrict__ deg, const uint32_t *big,
-                                                       uint32_t *q0, uint32_t *q1, uint32_t *bm0, uint32_t *bm1,
-                                                       uint32_t *visited, int32_t *level, int32_t *parent,
-                                                       BfsCounters *cnt) {
+                                                       const uint32_t *__restrict__ bigoff, uint32_t *q0, uint32_t *q1,
+                                                       uint32_t *bm0, uint32_t *bm1, uint32_t *visited, int32_t *level,
+                                                       int32_t *parent, BfsCounters *cnt) {
     if (st->pull) return;
     const uint32_t nbig = *(volatile uint32_t *)&cnt->nbig;
     if (!nbig) return;
     const uint32_t par = st->parity;
     uint32_t *next_queue = par ? q0 : q1, *next_bm = par ? bm0 : bm1;
     const int32_t next_level = (int32_t)st->lvl + 1;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nthreads = gridDim.x * blockDim.x;
     uint32_t my_cnt = 0;
     unsigned long long my_deg = 0;
-    for (uint32_t bi = 0; bi < nbig; bi++) {
-        const uint32_t u = big[bi];
-        const uint32_t b = ptr[u], e = ptr[u + 1];
-        for (uint32_t p0 = b + (tid & ~31u); p0 < e; p0 += nthreads) {
+    const uint32_t total = bigoff[nbig];
+    for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
+        const uint32_t i = eg_big_item(bigoff, nbig, c);
+        const uint32_t u = big[i];
+        const uint32_t b = ptr[u] + (c - bigoff[i]) * EG_BFS_CHUNK, e = min(ptr[u + 1], b + EG_BFS_CHUNK);
+        for (uint32_t p0 = b + (threadIdx.x & ~31u); p0 < e; p0 += blockDim.x) {
             const uint32_t p = p0 + (threadIdx.x & 31);
             bool claimed = false;
             uint32_t v = 0;
@@ -513,7 +515,7 @@ extern "C" void eg_bfs_opts_default(eg_bfs_opts *o) {
     o->direction = EG_BFS_AUTO;
     o->switch_divisor = 20.0;
     o->device_parents = 0;
-    o->host_loop = 0;
+    o->host_loop = -1;
 }
 
 static uint32_t blocks_for(eg_ctx *ctx, uint64_t threads) {
@@ -526,8 +528,8 @@ static uint32_t blocks_for(eg_ctx *ctx, uint64_t threads) {
 // Captures the level loop of eg_bfs for the current buffers (see BfsGState).
 static int bfs_graph_build(eg_graph *g, eg_bfs_graph &bg, const void *const key[8], BfsGState *st,
                            const uint32_t *deg, int32_t *level, int32_t *parent, uint32_t *visited, uint32_t *bm0,
-                           uint32_t *bm1, uint32_t *q0, uint32_t *q1, uint32_t *big, BfsCounters *cnt,
-                           const eg_adj *in_adj) {
+                           uint32_t *bm1, uint32_t *q0, uint32_t *q1, uint32_t *big, uint32_t *bigoff,
+                           BfsCounters *cnt, const eg_adj *in_adj) {
     eg_ctx *ctx = g->ctx;
     const uint32_t n = g->n, nw = (n + 31) >> 5;
     if (bg.exec) cudaGraphExecDestroy(bg.exec);
@@ -563,8 +565,9 @@ static int bfs_graph_build(eg_graph *g, eg_bfs_graph &bg, const void *const key[
     k_bfsg_prep<<<blocks, 256, 0, ctx->stream>>>(st, bm0, bm1, q0, q1, nw);
     k_bfsg_push<<<blocks, 256, 0, ctx->stream>>>(st, bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, q0, q1,
                                                 bm0, bm1, visited, level, parent, cnt, big);
-    k_bfsg_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, ctx->stream>>>(
-        st, bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, big, q0, q1, bm0, bm1, visited, level, parent, cnt);
+    k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, 1u, bp<uint32_t>(g->csr.ptr), EG_BFS_CHUNK, bigoff);
+    k_bfsg_push_big<<<blocks, 256, 0, ctx->stream>>>(st, bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, big,
+                                                    bigoff, q0, q1, bm0, bm1, visited, level, parent, cnt);
     if (iptr) k_bfsg_pull<<<blocks, 256, 0, ctx->stream>>>(st, iptr, icol, deg, bm0, bm1, visited, level, parent, cnt);
     k_bfsg_end<<<1, 1, 0, ctx->stream>>>(st, cnt, handle);
     ce = cudaStreamEndCapture(ctx->stream, &body);
@@ -600,11 +603,12 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
     if (want_parent) EG_TRY(eg_buf_ensure(ctx, g->parent, (uint64_t)n * 4));
     // work: visited | bm0 | bm1 | queue0 | queue1 | big list | counters | graph state
     const uint64_t off_bm0 = (uint64_t)nw, off_bm1 = 2ull * nw, off_q0 = 3ull * nw, off_q1 = off_q0 + n,
-                   off_big = off_q1 + n, off_cnt = (off_big + n + 7) & ~7ull, off_st = off_cnt + 16;
+                   off_big = off_q1 + n, off_bigoff = off_big + n, off_cnt = (off_bigoff + n + 1 + 7) & ~7ull,
+                   off_st = off_cnt + 16;
     EG_TRY(eg_buf_ensure(ctx, g->bfs_work, (off_st + 64) * 4));
     uint32_t *wk = bp<uint32_t>(g->bfs_work);
     uint32_t *visited = wk, *bm[2] = {wk + off_bm0, wk + off_bm1}, *q[2] = {wk + off_q0, wk + off_q1};
-    uint32_t *big = wk + off_big;
+    uint32_t *big = wk + off_big, *bigoff = wk + off_bigoff;
     BfsCounters *cnt = reinterpret_cast<BfsCounters *>(wk + off_cnt);
     BfsGState *gst = reinterpret_cast<BfsGState *>(wk + off_st);
     int32_t *level = bp<int32_t>(g->level);
@@ -612,15 +616,16 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
     const uint32_t *deg = bp<uint32_t>(g->out_deg);
     const double threshold = o.switch_divisor > 0 ? (double)g->m / o.switch_divisor : 0.0;
 
-    if (!o.host_loop) {
+    const bool host_loop = o.host_loop < 0 ? g->bfs_host_loop != 0 : o.host_loop != 0;
+    if (!host_loop) {
         eg_bfs_graph &bg = g->bfsg[want_parent ? 1 : 0];
         const void *key[8] = {wk, level, parent, deg, g->csr.col.p, in_adj ? in_adj->col.p : nullptr, g->csr.ptr.p,
                               (const void *)(uintptr_t)ctx->stream};
         bool fresh = bg.exec != nullptr;
         for (int i = 0; i < 8 && fresh; i++) fresh = bg.key[i] == key[i];
         if (!fresh)
-            EG_TRY(bfs_graph_build(g, bg, key, gst, deg, level, parent, visited, bm[0], bm[1], q[0], q[1], big, cnt,
-                                   in_adj));
+            EG_TRY(bfs_graph_build(g, bg, key, gst, deg, level, parent, visited, bm[0], bm[1], q[0], q[1], big, bigoff,
+                                   cnt, in_adj));
         BfsGState *h = (BfsGState *)ctx->h_pinned;
         memset(h, 0, sizeof(BfsGState));
         h->root = root;
@@ -693,9 +698,12 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
                 parent, lvl + 1, cnt, big);
             EG_LAUNCHED(ctx);
             if (fdeg > EG_BFS_BIG_DEG) {  // a frontier vertex may exceed the threshold
-                k_bfs_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, ctx->stream>>>(
-                    bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, big, visited, bm[nxt], q[nxt], level,
-                    parent, lvl + 1, cnt);
+                k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, 1u, bp<uint32_t>(g->csr.ptr), EG_BFS_CHUNK,
+                                                           bigoff);
+                EG_LAUNCHED(ctx);
+                k_bfs_push_big<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
+                    bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, big, bigoff, visited, bm[nxt], q[nxt],
+                    level, parent, lvl + 1, cnt);
                 EG_LAUNCHED(ctx);
             }
             have_queue = true;
@@ -787,16 +795,19 @@ __global__ void __launch_bounds__(256) k_ms_push(const uint32_t *__restrict__ pt
 // strides over each one's out-list in turn.
 __global__ void __launch_bounds__(256) k_ms_push_big(const uint32_t *__restrict__ ptr,
                                                      const uint32_t *__restrict__ col, const uint32_t *big,
+                                                     const uint32_t *__restrict__ bigoff,
                                                      const unsigned long long *__restrict__ seen,
                                                      const unsigned long long *__restrict__ front,
                                                      unsigned long long *__restrict__ next, const MsCounters *cnt) {
     const uint32_t nbig = *(volatile const uint32_t *)&cnt->nbig;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nthreads = gridDim.x * blockDim.x;
-    for (uint32_t bi = 0; bi < nbig; bi++) {
-        const uint32_t u = big[bi];
+    if (!nbig) return;
+    const uint32_t total = bigoff[nbig];
+    for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
+        const uint32_t i = eg_big_item(bigoff, nbig, c);
+        const uint32_t u = big[i];
         const unsigned long long f = front[u];
-        for (uint32_t p = ptr[u] + tid; p < ptr[u + 1]; p += nthreads) {
+        const uint32_t b = ptr[u] + (c - bigoff[i]) * EG_BFS_CHUNK, e = min(ptr[u + 1], b + EG_BFS_CHUNK);
+        for (uint32_t p = b + threadIdx.x; p < e; p += blockDim.x) {
             const uint32_t v = col[p];
             const unsigned long long add = f & ~__ldcg(seen + v);
             if (add && (__ldcg(next + v) & add) != add) atomicOr(next + v, add);
@@ -871,9 +882,9 @@ extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *
     eg_ctx *ctx = g->ctx;
     EG_CUDA(cudaSetDevice(ctx->device));
     const uint32_t n = g->n;
-    // work: seen | front | next (u64 each) | queue (u32) | big list (u32) | roots | counters
+    // work: seen | front | next (u64 each) | queue (u32) | big list (u32) | roots | counters | big chunk offsets
     const uint64_t words = 3ull * n;
-    const uint64_t bytes = words * 8 + 2ull * n * 4 + 64 * 4 + 64;
+    const uint64_t bytes = words * 8 + 2ull * n * 4 + 64 * 4 + 64 + ((uint64_t)n + 1) * 4;
     EG_TRY(eg_buf_ensure(ctx, g->msbfs_work, bytes));
     unsigned long long *seen = bp<unsigned long long>(g->msbfs_work);
     unsigned long long *front = seen + n, *next = seen + 2ull * n;
@@ -881,6 +892,7 @@ extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *
     uint32_t *big = queue + n;
     uint32_t *d_roots = big + n;
     MsCounters *cnt = reinterpret_cast<MsCounters *>(d_roots + 64);
+    uint32_t *bigoff = d_roots + 64 + 16;
     int32_t *levels = nullptr;
     if (levels_out) {
         EG_TRY(eg_buf_ensure(ctx, g->level, (uint64_t)k * n * 4));
@@ -939,8 +951,11 @@ extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *
                 bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), queue, count, seen, front, next, big, cnt);
             EG_LAUNCHED(ctx);
             if (fdeg > EG_BFS_BIG_DEG) {
-                k_ms_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, ctx->stream>>>(
-                    bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), big, seen, front, next, cnt);
+                k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, 1u, bp<uint32_t>(g->csr.ptr), EG_BFS_CHUNK,
+                                                           bigoff);
+                EG_LAUNCHED(ctx);
+                k_ms_push_big<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
+                    bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), big, bigoff, seen, front, next, cnt);
                 EG_LAUNCHED(ctx);
             }
         }
@@ -968,5 +983,28 @@ extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *
         stats->pull_levels = pull_levels;
         EG_CUDA(cudaEventElapsedTime(&stats->ms, ctx->ev0, ctx->ev1));
     }
+    return EG_OK;
+}
+
+int eg_bfs_tune(eg_graph *g, float *ms_graph, float *ms_host, int *host_loop) {
+    uint32_t roots[4];
+    EG_TRY(eg_sample_roots(g, 4, 12345, roots));
+    float t[2] = {0.f, 0.f};
+    for (int form = 0; form < 2; form++) {
+        eg_bfs_opts o;
+        eg_bfs_opts_default(&o);
+        o.host_loop = form;
+        o.device_parents = 1;
+        eg_bfs_stats st;
+        EG_TRY(eg_bfs(g, roots[0], &o, nullptr, nullptr, &st));  // warm-up (graph capture, buffers)
+        for (int r = 0; r < 4; r++) {
+            EG_TRY(eg_bfs(g, roots[r], &o, nullptr, nullptr, &st));
+            t[form] += st.ms / 4.f;
+        }
+    }
+    g->bfs_host_loop = t[1] < t[0] ? 1 : 0;
+    *ms_graph = t[0];
+    *ms_host = t[1];
+    *host_loop = g->bfs_host_loop;
     return EG_OK;
 }

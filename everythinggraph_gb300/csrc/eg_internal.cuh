@@ -118,6 +118,7 @@ struct eg_graph {
     eg_bfs_graph bfsg[2];  // without / with parents
     eg_bfs_graph prg;      // PageRank iterations (key: options and buffers)
     int row_cfg = 0;       // row-kernel schedule (entries per warp tile, per lane)
+    int bfs_host_loop = 0; // BFS level-loop form eg_bfs uses by default (eg_graph_tune)
     // SSSP edge weights of the CSR entries for one rule, materialised on first
     // use (the reference stores them in its edge records, init_all.c:661-686)
     eg_buf wts;
@@ -226,6 +227,8 @@ struct eg_wrule {
     __device__ __forceinline__ uint32_t extend(uint32_t du, uint32_t u, uint32_t v) const { return add(du, weight(u, v)); }
 };
 struct eg_graph;
+// Times eg_bfs's two level-loop forms on a few sampled roots (eg_bfs.cu).
+int eg_bfs_tune(eg_graph *g, float *ms_graph, float *ms_host, int *host_loop);
 // SpMV / PageRank over the 2-D grid layout (eg_grid.cu).
 int eg_grid_spmv(eg_graph *g, int kind, uint64_t value_seed, int unit_values, const void *d_x, void *d_y);
 int eg_grid_pagerank(eg_graph *g, const eg_pr_opts &o, float *rank_out, eg_pr_stats *stats);

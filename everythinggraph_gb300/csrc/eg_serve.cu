@@ -105,17 +105,22 @@ __global__ void __launch_bounds__(256) k_sv_bfs_push(const uint32_t *__restrict_
     }
 }
 
+#define SV_BFS_CHUNK 4096u  // edges of a deferred hub per CTA work unit
 __global__ void __launch_bounds__(256) k_sv_bfs_push_big(const uint32_t *__restrict__ ptr,
                                                          const uint32_t *__restrict__ col, const uint32_t *big,
+                                                         const uint32_t *__restrict__ bigoff,
                                                          const unsigned long long *__restrict__ seen,
                                                          const unsigned long long *__restrict__ front,
                                                          unsigned long long *__restrict__ next, const SvCounters *cnt) {
     const uint32_t nbig = *(volatile const uint32_t *)&cnt->nbig;
-    const uint32_t tid = blockIdx.x * blockDim.x + threadIdx.x, nt = gridDim.x * blockDim.x;
-    for (uint32_t bi = 0; bi < nbig; bi++) {
-        const uint32_t u = big[bi];
+    if (!nbig) return;
+    const uint32_t total = bigoff[nbig];
+    for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
+        const uint32_t i = eg_big_item(bigoff, nbig, c);
+        const uint32_t u = big[i];
         const unsigned long long f = front[u];
-        for (uint32_t p = ptr[u] + tid; p < ptr[u + 1]; p += nt) {
+        const uint32_t b = ptr[u] + (c - bigoff[i]) * SV_BFS_CHUNK, e = min(ptr[u + 1], b + SV_BFS_CHUNK);
+        for (uint32_t p = b + threadIdx.x; p < e; p += blockDim.x) {
             const uint32_t v = col[p];
             const unsigned long long add = f & ~__ldcg(seen + v);
             if (add && (__ldcg(next + v) & add) != add) atomicOr(next + v, add);
@@ -446,7 +451,7 @@ extern "C" int eg_serve_open(eg_graph *g, const eg_serve_opts *opts, eg_server *
     uint64_t sb, ss, sp;
     sv_slot_bytes(n, &sb, &ss, &sp);
     // shared per-engine state, then as many slots as the budget allows
-    const uint64_t shared_bfs = (uint64_t)n * 8 * 3 + (uint64_t)n * 8;
+    const uint64_t shared_bfs = (uint64_t)n * 8 * 3 + (uint64_t)n * 8 + ((uint64_t)n + 1) * 4;
     const uint64_t shared_sssp = (uint64_t)n * 8 * 2 + (uint64_t)n * 4 * 2 + (uint64_t)n * 4 * 4;
     const uint64_t shared_ppr = 0;
     const uint64_t base = shared_bfs + shared_sssp + shared_ppr;
@@ -468,8 +473,10 @@ extern "C" int eg_serve_open(eg_graph *g, const eg_serve_opts *opts, eg_server *
     s->sssp_cap = cap(o.max_sssp, SV_SSSP_SLOTS, ss);
     s->ppr_cap = cap(o.max_ppr, SV_PPR_LANES, sp);
     int rc = EG_OK;
-    // BFS: seen | front | next (u64) | queue+big (u32 x 2n) | levels (64 rows)
-    if (rc == EG_OK) rc = eg_buf_ensure(ctx, s->bfs_buf, (uint64_t)n * 8 * 3 + (uint64_t)n * 8 + (uint64_t)SV_BFS_SLOTS * n * 4);
+    // BFS: seen | front | next (u64) | queue+big (u32 x 2n) | levels (64 rows) | big chunk offsets
+    if (rc == EG_OK)
+        rc = eg_buf_ensure(ctx, s->bfs_buf, (uint64_t)n * 8 * 3 + (uint64_t)n * 8 + (uint64_t)SV_BFS_SLOTS * n * 4 +
+                                                ((uint64_t)n + 1) * 4);
     // SSSP: dist [n][64] | act x2 [n][2] | inq x2 | queue x2 | big | big chunk offsets
     if (rc == EG_OK)
         rc = eg_buf_ensure(ctx, s->sssp_buf, (uint64_t)n * 4 * SV_SSSP_SLOTS + (uint64_t)n * 8 * 2 + (uint64_t)((n + 31) / 32) * 4 * 2 +
@@ -692,6 +699,7 @@ static int sv_bfs_advance(eg_server *s, bool *progress) {
     unsigned long long *front = seen + n, *next = seen + 2ull * n;
     uint32_t *bq = reinterpret_cast<uint32_t *>(seen + 3ull * n), *bbig = bq + n;
     int32_t *levels = reinterpret_cast<int32_t *>(bbig + n);
+    uint32_t *bbigoff = reinterpret_cast<uint32_t *>(levels + (uint64_t)SV_BFS_SLOTS * n);
     const uint32_t *deg = bp<uint32_t>(g->out_deg);
     if (nadm) {
         EG_CUDA(cudaMemcpyAsync(small + SM_BROOTS, hroots, (uint64_t)nadm * 4, cudaMemcpyHostToDevice, st));
@@ -728,8 +736,10 @@ static int sv_bfs_advance(eg_server *s, bool *progress) {
         k_sv_bfs_push<<<(uint32_t)ctx->sm_count * 8, 256, 0, st>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), bq,
                                                                    bcnt, seen, front, next, bbig, bcnt);
         EG_LAUNCHED(ctx);
-        k_sv_bfs_push_big<<<(uint32_t)ctx->sm_count * 4, 256, 0, st>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col),
-                                                                       bbig, seen, front, next, bcnt);
+        k_big_offsets<<<1, 1024, 0, st>>>(bbig, &bcnt->nbig, 1u, bp<uint32_t>(g->csr.ptr), SV_BFS_CHUNK, bbigoff);
+        EG_LAUNCHED(ctx);
+        k_sv_bfs_push_big<<<(uint32_t)ctx->sm_count * 8, 256, 0, st>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col),
+                                                                       bbig, bbigoff, seen, front, next, bcnt);
         EG_LAUNCHED(ctx);
     }
     EG_CUDA(cudaMemsetAsync(bcnt, 0, sizeof(SvCounters), st));

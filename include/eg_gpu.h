@@ -180,6 +180,11 @@ typedef struct {
     int prefetch[8];
     int min_blocks[8];
     float ms[8];              /* mean row-kernel time per iteration */
+    /* BFS level loop (when the graph has a CSR): mean ms per BFS over 4
+     * sampled roots for the CUDA-graph and the host-driven loop, and the
+     * form kept for eg_bfs's host_loop = -1 */
+    float bfs_graph_ms, bfs_host_ms;
+    int bfs_host_loop;
 } eg_tune_result;
 int eg_graph_tune(eg_graph *g, eg_tune_result *out);
 int eg_graph_set_row_schedule(eg_graph *g, int index);
@@ -229,9 +234,11 @@ typedef struct {
     /* 1: compute parents on the device even when parent_out is NULL (read
      * them later through eg_graph_device_ptr(g, EG_DEV_PARENT)) */
     int device_parents;
-    /* 0 (default): the level loop runs on the device as one CUDA graph with a
+    /* 0: the level loop runs on the device as one CUDA graph with a
      * conditional while node (no host round trip per level); 1: the host
-     * launches and synchronises every level */
+     * launches and synchronises every level, each kernel on a grid sized to
+     * its frontier; -1 (default): the form eg_graph_tune found faster on
+     * this graph, else the graph */
     int host_loop;
 } eg_bfs_opts;
 typedef struct {
