@@ -752,15 +752,71 @@ __global__ void k_ms_init(uint32_t n, unsigned long long *seen, unsigned long lo
     }
 }
 
+// Device state of the multi-source level loop (one CUDA graph, see
+// msbfs_graph_build): the frontier's size and out-degree sum, the direction
+// chosen for the level, and the totals for the stats.
+struct MsGState {
+    uint32_t count;  // vertices in the frontier
+    int32_t lvl;     // level of the frontier (roots: 1)
+    int pull;        // this level runs bottom-up
+    int pull_levels;
+    unsigned long long fdeg;       // out-degree sum of the frontier's vertices
+    unsigned long long reached;    // (vertex, source) pairs reached
+    unsigned long long traversed;  // sum over those pairs of the vertex's out-degree
+    unsigned long long m;          // adjacency entries (switch rule)
+    uint32_t n;
+    uint32_t pad;
+};
+
+// Roots: seen/front bits, level 1, and the first frontier (distinct roots)
+// with its statistics.  One block of 64 threads.
 __global__ void k_ms_roots(const uint32_t *roots, int k, uint32_t n, unsigned long long *seen, unsigned long long *front,
-                           int32_t *levels) {
-    int s = threadIdx.x;
-    if (s < k) {
-        uint32_t r = roots[s];
-        atomicOr(seen + r, 1ull << s);
-        atomicOr(front + r, 1ull << s);
-        if (levels) levels[(uint64_t)s * n + r] = 1;
+                           int32_t *levels, const uint32_t *__restrict__ deg, uint32_t *queue, MsGState *st,
+                           unsigned long long m) {
+    __shared__ unsigned int s_count;
+    __shared__ unsigned long long s_fdeg, s_rdeg;
+    const int s = threadIdx.x;
+    if (s == 0) {
+        s_count = 0;
+        s_fdeg = 0;
+        s_rdeg = 0;
     }
+    __syncthreads();
+    if (s < k) {
+        const uint32_t r = roots[s];
+        atomicOr(seen + r, 1ull << s);
+        const unsigned long long was = atomicOr(front + r, 1ull << s);
+        if (levels) levels[(uint64_t)s * n + r] = 1;
+        const unsigned long long d = deg[r];
+        atomicAdd(&s_rdeg, d);
+        if (!was) {  // the first source at this vertex lists it
+            queue[atomicAdd(&s_count, 1u)] = r;
+            atomicAdd(&s_fdeg, d);
+        }
+    }
+    __syncthreads();
+    if (s == 0) {
+        st->count = s_count;
+        st->lvl = 1;
+        st->pull = 0;
+        st->pull_levels = 0;
+        st->fdeg = s_fdeg;
+        st->reached = (unsigned long long)k;
+        st->traversed = s_rdeg;
+        st->m = m;
+        st->n = n;
+    }
+}
+
+// Level start: the reference's switch rule (bfs_simple.c:191-197) on the
+// frontier's size and out-degrees, and cleared level counters.
+__global__ void k_msg_prep(MsGState *st, MsCounters *cnt) {
+    st->pull = (double)st->count + (double)st->fdeg > (double)st->m / 20.0;
+    cnt->deg = 0;
+    cnt->tdeg = 0;
+    cnt->disc = 0;
+    cnt->count = 0;
+    cnt->nbig = 0;
 }
 
 // Pull: a vertex ORs the frontier words of its in-neighbours, stopping early
@@ -768,11 +824,13 @@ __global__ void k_ms_roots(const uint32_t *roots, int k, uint32_t n, unsigned lo
 // Push: one warp per vertex with a nonzero frontier word; vertices with more
 // than EG_BFS_BIG_DEG out-edges go to a side list for k_ms_push_big.
 __global__ void __launch_bounds__(256) k_ms_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
-                                                 const uint32_t *__restrict__ queue, uint32_t qlen,
+                                                 const uint32_t *__restrict__ queue, const MsGState *st,
                                                  const unsigned long long *__restrict__ seen,
                                                  const unsigned long long *__restrict__ front,
                                                  unsigned long long *__restrict__ next, uint32_t *big,
                                                  MsCounters *cnt) {
+    if (st->pull) return;
+    const uint32_t qlen = st->count;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < qlen; qi += warps) {
@@ -815,11 +873,25 @@ __global__ void __launch_bounds__(256) k_ms_push_big(const uint32_t *__restrict_
     }
 }
 
+// Level end: the new frontier's counters into the loop state; the while node
+// repeats the level body while the frontier is non-empty (and at most n + 1
+// levels, a bound the loop can never need).
+__global__ void k_msg_end(MsGState *st, const MsCounters *cnt, cudaGraphConditionalHandle handle) {
+    st->count = cnt->count;
+    st->fdeg = cnt->deg;
+    st->reached += cnt->disc;
+    st->traversed += cnt->tdeg;
+    st->pull_levels += st->pull;
+    st->lvl += 1;
+    cudaGraphSetConditional(handle, (cnt->count > 0 && (uint32_t)st->lvl <= st->n + 1) ? 1u : 0u);
+}
+
 // Folds the new words into seen, records levels, makes them the frontier and
 // lists the frontier vertices for a following push step.
 __global__ void k_ms_fold(uint32_t n, int k, unsigned long long *seen, unsigned long long *front,
-                          unsigned long long *next, int clear_next, int32_t *levels, int32_t lvl,
+                          unsigned long long *next, int clear_next, int32_t *levels, const MsGState *st,
                           const uint32_t *__restrict__ deg, uint32_t *queue, MsCounters *cnt) {
+    const int32_t lvl = st->lvl + 1;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t lt = eg_lanemask_lt();
     uint32_t stride = gridDim.x * blockDim.x;
@@ -868,6 +940,59 @@ __global__ void k_ms_fold(uint32_t n, int k, unsigned long long *seen, unsigned 
 }
 }  // namespace
 
+// The level loop of eg_bfs_multi as one CUDA graph: a while node whose body
+// is prep (direction), push (+ hubs in chunks) or the two-part pull, fold,
+// and end (counters into the state, loop condition).  Valid while the
+// buffers and k it was captured with (key) stay the same.
+static int msbfs_graph_build(eg_graph *g, const void *const key[8], const eg_adj *in_adj, int k,
+                             unsigned long long all, unsigned long long *seen, unsigned long long *front,
+                             unsigned long long *next, uint32_t *queue, uint32_t *big, uint32_t *bigoff, int32_t *levels,
+                             MsGState *st, MsCounters *cnt) {
+    eg_ctx *ctx = g->ctx;
+    eg_bfs_graph &bg = g->msg;
+    const uint32_t n = g->n;
+    const uint32_t *deg = bp<uint32_t>(g->out_deg);
+    if (bg.exec) cudaGraphExecDestroy(bg.exec);
+    if (bg.graph) cudaGraphDestroy(bg.graph);
+    bg.exec = nullptr;
+    bg.graph = nullptr;
+    cudaGraph_t graph = nullptr;
+    EG_CUDA(cudaGraphCreate(&graph, 0));
+    bg.graph = graph;
+    cudaGraphConditionalHandle handle;
+    EG_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    EG_CUDA(cudaGraphAddNode(&wnode, graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    const uint32_t blocks = (uint32_t)ctx->sm_count * 8;
+    EG_CUDA(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    k_msg_prep<<<1, 1, 0, ctx->stream>>>(st, cnt);
+    k_ms_push<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), queue, st, seen,
+                                               front, next, big, cnt);
+    k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, 1u, bp<uint32_t>(g->csr.ptr), EG_BFS_CHUNK, bigoff);
+    k_ms_push_big<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), big, bigoff,
+                                                   seen, front, next, cnt);
+    // the heavy list reuses the push side list (idle in a pull level)
+    k_msp_light<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col), n, all, seen,
+                                                 front, next, big, &cnt->nbig, &st->pull);
+    k_msp_heavy<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col), all, seen, front,
+                                                 next, big, &cnt->nbig, &st->pull);
+    k_ms_fold<<<blocks, 256, 0, ctx->stream>>>(n, k, seen, front, next, 1, levels, st, deg, queue, cnt);
+    k_msg_end<<<1, 1, 0, ctx->stream>>>(st, cnt, handle);
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &body);
+    if (ce != cudaSuccess) return eg_fail(EG_ECUDA, "multi-source BFS capture: %s", cudaGetErrorString(ce));
+    cudaGraphExec_t exec = nullptr;
+    EG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    bg.exec = exec;
+    for (int i = 0; i < 8; i++) bg.key[i] = key[i];
+    return EG_OK;
+}
+
 extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *levels_out, eg_bfs_stats *stats) {
     if (!g || !roots) return eg_fail(EG_EINVAL, "NULL argument");
     if (k < 1 || k > 64) return eg_fail(EG_EINVAL, "k=%d sources: bit-sliced BFS takes 1..64", k);
@@ -882,9 +1007,9 @@ extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *
     eg_ctx *ctx = g->ctx;
     EG_CUDA(cudaSetDevice(ctx->device));
     const uint32_t n = g->n;
-    // work: seen | front | next (u64 each) | queue (u32) | big list (u32) | roots | counters | big chunk offsets
-    const uint64_t words = 3ull * n;
-    const uint64_t bytes = words * 8 + 2ull * n * 4 + 64 * 4 + 64 + ((uint64_t)n + 1) * 4;
+    // work: seen | front | next (u64 each) | queue (u32) | big list (u32) | roots | counters | state |
+    //       big chunk offsets
+    const uint64_t bytes = 3ull * n * 8 + 2ull * n * 4 + 64 * 4 + 64 + 64 + ((uint64_t)n + 1) * 4;
     EG_TRY(eg_buf_ensure(ctx, g->msbfs_work, bytes));
     unsigned long long *seen = bp<unsigned long long>(g->msbfs_work);
     unsigned long long *front = seen + n, *next = seen + 2ull * n;
@@ -892,95 +1017,42 @@ extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *
     uint32_t *big = queue + n;
     uint32_t *d_roots = big + n;
     MsCounters *cnt = reinterpret_cast<MsCounters *>(d_roots + 64);
-    uint32_t *bigoff = d_roots + 64 + 16;
+    MsGState *st = reinterpret_cast<MsGState *>(d_roots + 64 + 16);
+    uint32_t *bigoff = d_roots + 64 + 32;
     int32_t *levels = nullptr;
     if (levels_out) {
         EG_TRY(eg_buf_ensure(ctx, g->level, (uint64_t)k * n * 4));
         levels = bp<int32_t>(g->level);
     }
-    MsCounters *h = (MsCounters *)ctx->h_pinned;
     const uint32_t *deg = bp<uint32_t>(g->out_deg);
     const unsigned long long all = k == 64 ? ~0ull : ((1ull << k) - 1ull);
+    const void *key[8] = {g->msbfs_work.p, levels, g->csr.col.p, in_adj->col.p, (const void *)(uintptr_t)k, g->csr.ptr.p,
+                          in_adj->ptr.p, g->out_deg.p};
+    bool same = g->msg.exec != nullptr;
+    for (int i = 0; i < 8 && same; i++) same = g->msg.key[i] == key[i];
+    if (!same)
+        EG_TRY(msbfs_graph_build(g, key, in_adj, k, all, seen, front, next, queue, big, bigoff, levels, st, cnt));
     EG_CUDA(cudaMemcpyAsync(d_roots, roots, (uint64_t)k * 4, cudaMemcpyHostToDevice, ctx->stream));
     EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
     if (levels) EG_CUDA(cudaMemsetAsync(levels, 0, (uint64_t)k * n * 4, ctx->stream));
     k_ms_init<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(n, seen, front);
     EG_LAUNCHED(ctx);
     EG_CUDA(cudaMemsetAsync(next, 0, (uint64_t)n * 8, ctx->stream));
-    k_ms_roots<<<1, 64, 0, ctx->stream>>>(d_roots, k, n, seen, front, levels);
+    k_ms_roots<<<1, 64, 0, ctx->stream>>>(d_roots, k, n, seen, front, levels, deg, queue, st, g->m);
     EG_LAUNCHED(ctx);
-    // first frontier: the distinct roots
-    uint32_t count = 0;
-    unsigned long long fdeg = 0, rdeg = 0;
-    {
-        uint32_t *hq = (uint32_t *)malloc((size_t)k * 4);
-        uint32_t *hdeg = (uint32_t *)ctx->h_pinned + 1024;
-        EG_CUDA(cudaStreamSynchronize(ctx->stream));
-        for (int s = 0; s < k; s++) {
-            bool dup = false;
-            for (uint32_t i = 0; i < count; i++) dup |= hq[i] == roots[s];
-            if (!dup) hq[count++] = roots[s];
-        }
-        EG_CUDA(cudaMemcpy(queue, hq, (uint64_t)count * 4, cudaMemcpyHostToDevice));
-        for (uint32_t i = 0; i < count; i++) {
-            EG_CUDA(cudaMemcpy(hdeg, deg + hq[i], 4, cudaMemcpyDeviceToHost));
-            fdeg += *hdeg;
-            for (int s = 0; s < k; s++) rdeg += roots[s] == hq[i] ? *hdeg : 0u;
-        }
-        free(hq);
-    }
-    uint64_t reached = (uint64_t)k, traversed = rdeg;
-    int32_t lvl = 1;
-    int pull_levels = 0;
-    const double threshold = (double)g->m / 20.0;
-    while (count > 0) {
-        const bool pull = (double)count + (double)fdeg > threshold;
-        EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(MsCounters), ctx->stream));
-        if (pull) {
-            // the heavy list reuses the push side list (idle in a pull level)
-            k_msp_light<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(bp<uint32_t>(in_adj->ptr),
-                                                                    bp<uint32_t>(in_adj->col), n, all, seen, front, next,
-                                                                    big, &cnt->nbig);
-            EG_LAUNCHED(ctx);
-            k_msp_heavy<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
-                bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col), all, seen, front, next, big, &cnt->nbig);
-            EG_LAUNCHED(ctx);
-            pull_levels++;
-        } else {
-            k_ms_push<<<blocks_for(ctx, (uint64_t)count * 32), 256, 0, ctx->stream>>>(
-                bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), queue, count, seen, front, next, big, cnt);
-            EG_LAUNCHED(ctx);
-            if (fdeg > EG_BFS_BIG_DEG) {
-                k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, 1u, bp<uint32_t>(g->csr.ptr), EG_BFS_CHUNK,
-                                                           bigoff);
-                EG_LAUNCHED(ctx);
-                k_ms_push_big<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
-                    bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), big, bigoff, seen, front, next, cnt);
-                EG_LAUNCHED(ctx);
-            }
-        }
-        // after a push the next words were accumulated with atomics and must be
-        // cleared for the following level; after a pull they are overwritten
-        k_ms_fold<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(n, k, seen, front, next, 1, levels, lvl + 1, deg, queue,
-                                                              cnt);
-        EG_LAUNCHED(ctx);
-        EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(MsCounters), cudaMemcpyDeviceToHost, ctx->stream));
-        EG_CUDA(cudaStreamSynchronize(ctx->stream));
-        count = h->count;
-        fdeg = h->deg;
-        reached += h->disc;
-        traversed += h->tdeg;
-        lvl++;
-        if (lvl > (int32_t)n + 1) return eg_fail(EG_ETIMEOUT, "multi-source BFS did not terminate");
-    }
+    EG_CUDA(cudaGraphLaunch(g->msg.exec, ctx->stream));
+    ctx->launches++;
     EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
+    MsGState *h = (MsGState *)ctx->h_pinned;
+    EG_CUDA(cudaMemcpyAsync(h, st, sizeof(MsGState), cudaMemcpyDeviceToHost, ctx->stream));
     if (levels_out) EG_CUDA(cudaMemcpyAsync(levels_out, levels, (uint64_t)k * n * 4, cudaMemcpyDeviceToHost, ctx->stream));
     EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    if ((uint32_t)h->lvl > n + 1) return eg_fail(EG_ETIMEOUT, "multi-source BFS did not terminate");
     if (stats) {
-        stats->levels = lvl - 1;
-        stats->reached = (uint32_t)(reached > 0xffffffffull ? 0xffffffffull : reached);
-        stats->edges_traversed = traversed;
-        stats->pull_levels = pull_levels;
+        stats->levels = h->lvl - 1;
+        stats->reached = (uint32_t)(h->reached > 0xffffffffull ? 0xffffffffull : h->reached);
+        stats->edges_traversed = h->traversed;
+        stats->pull_levels = h->pull_levels;
         EG_CUDA(cudaEventElapsedTime(&stats->ms, ctx->ev0, ctx->ev1));
     }
     return EG_OK;

@@ -299,8 +299,10 @@ extern "C" void eg_graph_free(eg_graph *g) {
         if (bg.exec) cudaGraphExecDestroy(bg.exec);
         if (bg.graph) cudaGraphDestroy(bg.graph);
     }
-    if (g->prg.exec) cudaGraphExecDestroy(g->prg.exec);
-    if (g->prg.graph) cudaGraphDestroy(g->prg.graph);
+    for (eg_bfs_graph *bg : {&g->prg, &g->msg}) {
+        if (bg->exec) cudaGraphExecDestroy(bg->exec);
+        if (bg->graph) cudaGraphDestroy(bg->graph);
+    }
     c->live_graphs--;
     delete g;
 }

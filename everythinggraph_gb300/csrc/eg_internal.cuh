@@ -117,6 +117,7 @@ struct eg_graph {
     eg_buf ppr_work;
     eg_bfs_graph bfsg[2];  // without / with parents
     eg_bfs_graph prg;      // PageRank iterations (key: options and buffers)
+    eg_bfs_graph msg;      // multi-source BFS level loop
     int row_cfg = 0;       // row-kernel schedule (entries per warp tile, per lane)
     int bfs_host_loop = 0; // BFS level-loop form eg_bfs uses by default (eg_graph_tune)
     // SSSP edge weights of the CSR entries for one rule, materialised on first

@@ -26,7 +26,8 @@ __global__ void __launch_bounds__(256) k_msp_light(const uint32_t *__restrict__ 
                                                    const unsigned long long *__restrict__ seen,
                                                    const unsigned long long *__restrict__ front,
                                                    unsigned long long *__restrict__ next, uint32_t *__restrict__ heavy,
-                                                   uint32_t *heavy_count) {
+                                                   uint32_t *heavy_count, const int *gate = nullptr) {
+    if (gate && !*gate) return;  // a device-driven loop chose push for this level
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t stride = gridDim.x * blockDim.x;
     // uniform trip count per warp for the ballot
@@ -61,8 +62,10 @@ __global__ void __launch_bounds__(256) k_msp_heavy(const uint32_t *__restrict__ 
                                                    unsigned long long all, const unsigned long long *__restrict__ seen,
                                                    const unsigned long long *__restrict__ front,
                                                    unsigned long long *__restrict__ next,
-                                                   const uint32_t *__restrict__ heavy, const uint32_t *heavy_count) {
+                                                   const uint32_t *__restrict__ heavy, const uint32_t *heavy_count,
+                                                   const int *gate = nullptr) {
     __shared__ unsigned long long s_acc;
+    if (gate && !*gate) return;
     const uint32_t nh = *(volatile const uint32_t *)heavy_count;
     const uint32_t lane = threadIdx.x & 31;
     for (uint32_t i = blockIdx.x; i < nh; i += gridDim.x) {
