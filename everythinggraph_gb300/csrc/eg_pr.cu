@@ -1,22 +1,26 @@
-// Pull PageRank and SpMV as merge-path row reductions over the CSC (or CSR).
+// Pull PageRank, personalised PageRank (one query) and SpMV as row
+// reductions over the CSC (or CSR), plus the row-schedule autotuner.
 //
 // Replaces pr_algo_pull and its iterator (pagerank_simple.c:72-84,110-133),
 // the grid PR loop (prgrid_cilk.c:62-76,111-141) whose per-destination sum
-// order equals the CSC order, and the SpMV loops (spmv.c:98-135).
+// order equals the CSC order (the grid-cell form is eg_grid.cu), and the SpMV
+// loops (spmv.c:98-135).
 //
 // PageRank runs on a copy of the CSC whose vertices are relabelled by
 // descending out-degree (built once, eg_build_relabeled_csc): the most
 // gathered contrib entries are then contiguous, so they share cache sectors
 // and stay in L1; ranks are mapped back to the original ids at the end.
-// Per PageRank iteration the device runs three kernels:
-//   k_mp_rows<PrOp>   rank[v] = base + d * sum_{u in in(v)} contrib[u]
-//                     contrib'[v] = rank[v] / deg[v] (fused into the write)
-//   k_mp_fixup<PrOp>  rows that span CTAs
-//   k_pr_reduce       FP64 residual / dangling mass -> next base, stop flag
+// Per PageRank iteration the device runs:
+//   k_coov_rows<PrOp>      rank[v] = base + d * sum_{u in in(v)} contrib[u],
+//                          contrib'[v] = rank[v] / deg[v] (fused into the write);
+//                          warp tiles of row-id/column pairs (eg_mp.cuh)
+//   k_coo_empty_rows, k_coo_fixup   rows without entries, rows split between tiles
+//   k_pr_residual          (with a tolerance) the L1 change, coalesced
+//   k_pr_reduce            FP64 residual / dangling mass -> next base, stop flag
 // contrib[u] = prev[u] / (float)deg[u] is the reference's per-edge quotient
 // (pagerank_simple.c:78), computed once per vertex instead of once per edge.
-// Algorithmic bytes per iteration: 8 per entry (4 col + 4 gathered contrib)
-// and 16 per vertex (row end, degree, rank write, contrib write).
+// Algorithmic bytes per iteration: 8 per entry (row id + column) and 16 per
+// vertex (gathered contribution, degree, rank write, contribution write).
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
