@@ -177,7 +177,7 @@ def run_ours(args):
         except Exception as ex:  # reported, not fatal for the headline
             kernels["msbfs_64_roots"] = {"error": str(ex)}
         try:
-            kernels["serve"] = serve_report(ctx, eg, scale, args.rate, args.queries, g=g)
+            kernels["serve"] = serve_report(ctx, eg, scale, args.rate, args.queries, g=g, exclusive=args.serve_exclusive, gang=not args.serve_no_gang)
         except Exception as ex:
             kernels["serve"] = {"error": str(ex)}
         kernels.update(kernel_reports(ctx, eg, scale, args))
@@ -334,7 +334,7 @@ def msbfs_report(g, roots):
             "speedup": per_single * len(roots) / stm.ms}
 
 
-def serve_report(ctx, eg, scale, rate, nq, seed=7, plain_sample=40, g=None):
+def serve_report(ctx, eg, scale, rate, nq, seed=7, plain_sample=40, g=None, exclusive=False, gang=True):
     """Serving workload: Poisson arrivals at `rate` qps of 60% BFS, 25% SSSP
     (u32 weights U[1,255]), 15% personalised PageRank (1-8 seeds, tolerance
     10^U(-7,-4), <= 50 iterations) on the resident undirected RMAT graph;
@@ -362,7 +362,7 @@ def serve_report(ctx, eg, scale, rate, nq, seed=7, plain_sample=40, g=None):
             k = int(rng.integers(1, 9))
             qs.append(("ppr", 0, [int(x) for x in rng.choice(nz, size=k)], float(10 ** rng.uniform(-7, -4))))
     w = eg.weights("hash", seed=6, lo=1, hi=255)
-    srv = eg.Server(g, hbm_budget=64 << 30, weights_=w)
+    srv = eg.Server(g, hbm_budget=64 << 30, weights_=w, exclusive=exclusive, gang=gang)
     torch.cuda.synchronize()
     t_start = srv.info()["clock_s"]
     arrivals = arrivals + t_start
@@ -402,6 +402,7 @@ def serve_report(ctx, eg, scale, rate, nq, seed=7, plain_sample=40, g=None):
         g.free()
     qps = nq / span
     return {"workload": "serve rmat%d undirected, %d queries, Poisson %g qps offered" % (scale, nq, rate),
+            "engines": "exclusive" if exclusive else "concurrent", "sssp_gang": gang,
             "qps": qps, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "plain_qps": plain_qps, "speedup_vs_plain": qps / plain_qps, "slots": info}
 
@@ -533,7 +534,7 @@ def only_report(name, args):
     ctx = eg.Context(0)
     scale = args.scale or 24
     if name == "serve":
-        out = serve_report(ctx, eg, scale, args.rate, args.queries)
+        out = serve_report(ctx, eg, scale, args.rate, args.queries, exclusive=args.serve_exclusive, gang=not args.serve_no_gang)
     elif name == "pr":
         out = kernel_reports(ctx, eg, scale, args)
     elif name == "spmv":
@@ -568,6 +569,10 @@ def main():
                     help="only one kernel report (profiling)")
     ap.add_argument("--rate", type=float, default=20000.0)
     ap.add_argument("--queries", type=int, default=1000)
+    ap.add_argument("--serve-no-gang", action="store_true",
+                    help="query server admits SSSP queries into any free slot instead of 32-source gangs")
+    ap.add_argument("--serve-exclusive", action="store_true",
+                    help="query server runs one engine step at a time instead of overlapping them")
     args = ap.parse_args()
     if args.only or args.serve_only or args.pr_only:
         only_report(args.only or ("serve" if args.serve_only else "pr"), args)

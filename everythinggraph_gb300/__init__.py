@@ -307,12 +307,13 @@ class Server:
     KINDS = {"bfs": L.EG_Q_BFS, "sssp": L.EG_Q_SSSP, "ppr": L.EG_Q_PPR}
 
     def __init__(self, graph, hbm_budget=64 << 30, weights_=None, keep_results=False, max_bfs=64, max_sssp=64,
-                 max_ppr=32, ppr_max_iters=50):
+                 max_ppr=32, ppr_max_iters=50, exclusive=False, gang=True):
         self.graph = graph
         o = L.ServeOpts()
         lib().eg_serve_opts_default(ctypes.byref(o))
         o.hbm_budget, o.keep_results = hbm_budget, int(keep_results)
         o.max_bfs, o.max_sssp, o.max_ppr, o.ppr_max_iters = max_bfs, max_sssp, max_ppr, ppr_max_iters
+        o.exclusive, o.gang = int(exclusive), int(gang)
         if weights_ is not None:
             o.weights = weights_
         self._h = ctypes.c_void_p()

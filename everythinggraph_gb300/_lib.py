@@ -93,7 +93,8 @@ class QueryResult(ctypes.Structure):
 
 class ServeOpts(ctypes.Structure):
     _fields_ = [("hbm_budget", c_u64), ("max_bfs", c_int), ("max_sssp", c_int), ("max_ppr", c_int),
-                ("weights", Weights), ("ppr_damping", c_f32), ("ppr_max_iters", c_int), ("keep_results", c_int)]
+                ("weights", Weights), ("ppr_damping", c_f32), ("ppr_max_iters", c_int), ("keep_results", c_int),
+                ("exclusive", c_int), ("gang", c_int)]
 
 
 class WccStats(ctypes.Structure):

@@ -304,24 +304,39 @@ __global__ void k_sv_sssp_reset(uint32_t n, unsigned long long mask, uint32_t *d
     }
 }
 
-__global__ void k_sv_dist_summary(const uint32_t *__restrict__ dist, uint32_t n, uint32_t s, unsigned long long *out) {
-    unsigned long long c = 0, mx = 0;
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-        const uint32_t d = dist[(uint64_t)v * SV_SSSP_SLOTS + s];
-        if (d != SV_INF) {
-            c++;
-            mx = d > mx ? d : mx;
+// reached count and largest distance of every slot in `done`, two words per
+// slot in out[]: a warp takes 32 vertices and walks the done slots, so slots
+// that share a 32-byte sector of a vertex row reuse it from L1
+__global__ void __launch_bounds__(256) k_sv_dist_summary(const uint32_t *__restrict__ dist, uint32_t n,
+                                                         unsigned long long done, unsigned long long *out) {
+    __shared__ unsigned long long s_c[SV_SSSP_SLOTS];
+    __shared__ unsigned int s_m[SV_SSSP_SLOTS];
+    for (uint32_t i = threadIdx.x; i < SV_SSSP_SLOTS; i += blockDim.x) {
+        s_c[i] = 0;
+        s_m[i] = 0;
+    }
+    __syncthreads();
+    const uint32_t lane = threadIdx.x & 31;
+    for (uint32_t v0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); v0 < n; v0 += gridDim.x * blockDim.x) {
+        const uint32_t v = v0 + lane;
+        for (unsigned long long y = done; y; y &= y - 1) {
+            const int sl = __ffsll((long long)y) - 1;
+            const uint32_t d = v < n ? dist[(uint64_t)v * SV_SSSP_SLOTS + sl] : SV_INF;
+            const bool r = d != SV_INF;
+            const uint32_t c = (uint32_t)__popc(__ballot_sync(EG_FULL_MASK, r));
+            const uint32_t m = __reduce_max_sync(EG_FULL_MASK, r ? d : 0u);
+            if (lane == 0 && c) {
+                atomicAdd(&s_c[sl], (unsigned long long)c);
+                atomicMax(&s_m[sl], m);
+            }
         }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        c += __shfl_down_sync(EG_FULL_MASK, c, o);
-        mx = max(mx, __shfl_down_sync(EG_FULL_MASK, mx, o));
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicAdd(out, c);
-        atomicMax(out + 1, mx);
-    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < SV_SSSP_SLOTS; i += blockDim.x)
+        if (((done >> i) & 1ull) && s_c[i]) {
+            atomicAdd(out + 2 * i, s_c[i]);
+            atomicMax(out + 2 * i + 1, (unsigned long long)s_m[i]);
+        }
 }
 
 __global__ void k_sv_column(const uint32_t *__restrict__ m, uint32_t n, uint32_t width, uint32_t s, uint32_t *out) {
@@ -391,6 +406,8 @@ struct eg_server {
     cudaStream_t st[3] = {};
     cudaEvent_t ev_begin[3] = {}, ev_end[3] = {};
     bool inflight[3] = {false, false, false};
+    int turn = 0;            // engine offered the GPU first at the next launch
+    bool ppr_dirty = false;  // host lane table changed since its last upload
     unsigned long long step_mask[3] = {0, 0, 0};  // slots live in the step in flight
     unsigned char *hpin = nullptr;                // pinned host staging, a region per engine
     double eng_ms[3] = {0.0, 0.0, 0.0};
@@ -403,8 +420,9 @@ enum : uint32_t {
     SM_BCNT = 0, SM_SCNT = 256, SM_SNEXT = 512, SM_BROOTS = 1024, SM_SROOTS = 1536, SM_BSLOTS = 2048,
     SM_SSLOTS = 2560, SM_BLEVEL = 3072, SM_PPRQ = 4096, SM_PSEEDS = 8192, SM_PSBEG = 9216, SM_PSEND = 9344,
     SM_SUM = 12544,  // 64 bytes per engine
+    SM_RSUM = 16384,  // retire summaries: 16 bytes per slot, BFS then SSSP
     HP_BCNT = 0, HP_SCNT = 256, HP_PPRQ = 1024, HP_PSEEDS = 4096, HP_SUM = 8192,  // 64 per engine
-    HP_BADM = 12288, HP_SADM = 13312, HP_BLEVEL = 14336, HP_BYTES = 16384
+    HP_BADM = 12288, HP_SADM = 13312, HP_BLEVEL = 14336, HP_RSUM = 16384, HP_BYTES = 20480
 };
 
 static uint32_t sv_blocks(eg_ctx *ctx, uint64_t threads) {
@@ -427,6 +445,8 @@ extern "C" void eg_serve_opts_default(eg_serve_opts *o) {
     o->ppr_damping = 0.85f;
     o->ppr_max_iters = 50;
     o->keep_results = 0;
+    o->exclusive = 0;
+    o->gang = 1;
 }
 
 // Device bytes per slot of each engine (the admission cost of one query).
@@ -626,25 +646,29 @@ static int sv_bfs_retire(eg_server *s, unsigned long long done) {
     unsigned long long *seen = bp<unsigned long long>(s->bfs_buf);
     unsigned long long *front = seen + n;
     int32_t *levels = reinterpret_cast<int32_t *>(reinterpret_cast<uint32_t *>(seen + 3ull * n) + 2ull * n);
-    unsigned long long *d_sum = (unsigned long long *)(bp<unsigned char>(s->small) + SM_SUM);
-    unsigned long long *hsum = (unsigned long long *)(s->hpin + HP_SUM);
+    unsigned long long *d_sum = (unsigned long long *)(bp<unsigned char>(s->small) + SM_RSUM);
+    unsigned long long *hsum = (unsigned long long *)(s->hpin + HP_RSUM);
+    std::vector<std::vector<uint32_t>> keep;
+    EG_CUDA(cudaMemsetAsync(d_sum, 0, 16 * SV_BFS_SLOTS, st));
     for (int sl = 0; sl < SV_BFS_SLOTS; sl++) {
         if (!((done >> sl) & 1ull)) continue;
         int32_t *row = levels + (uint64_t)sl * n;
-        EG_CUDA(cudaMemsetAsync(d_sum, 0, 16, st));
-        k_sv_level_summary<<<sv_blocks(ctx, n), 256, 0, st>>>(row, n, d_sum);
+        k_sv_level_summary<<<sv_blocks(ctx, n), 256, 0, st>>>(row, n, d_sum + 2 * sl);
         EG_LAUNCHED(ctx);
-        EG_CUDA(cudaMemcpyAsync(hsum, d_sum, 16, cudaMemcpyDeviceToHost, st));
-        std::vector<uint32_t> keep;
         if (s->opts.keep_results) {
-            keep.resize(n);
-            EG_CUDA(cudaMemcpyAsync(keep.data(), row, (uint64_t)n * 4, cudaMemcpyDeviceToHost, st));
+            keep.emplace_back(n);
+            EG_CUDA(cudaMemcpyAsync(keep.back().data(), row, (uint64_t)n * 4, cudaMemcpyDeviceToHost, st));
         }
-        EG_CUDA(cudaStreamSynchronize(st));
-        sv_finish(s, s->bfs_id[sl], EG_Q_BFS, s->bfs_arrival[sl], s->bfs_admit[sl], (uint32_t)hsum[0],
-                  (uint32_t)hsum[1], s->bfs_level[sl] - 1, 0.0);
-        if (s->opts.keep_results) s->kept.push_back(std::move(keep));
         EG_CUDA(cudaMemsetAsync(row, 0, (uint64_t)n * 4, st));
+    }
+    EG_CUDA(cudaMemcpyAsync(hsum, d_sum, 16 * SV_BFS_SLOTS, cudaMemcpyDeviceToHost, st));
+    EG_CUDA(cudaStreamSynchronize(st));  // one wait for every retiring slot
+    size_t k = 0;
+    for (int sl = 0; sl < SV_BFS_SLOTS; sl++) {
+        if (!((done >> sl) & 1ull)) continue;
+        sv_finish(s, s->bfs_id[sl], EG_Q_BFS, s->bfs_arrival[sl], s->bfs_admit[sl], (uint32_t)hsum[2 * sl],
+                  (uint32_t)hsum[2 * sl + 1], s->bfs_level[sl] - 1, 0.0);
+        if (s->opts.keep_results) s->kept.push_back(std::move(keep[k++]));
     }
     k_sv_bfs_clear<<<sv_blocks(ctx, n), 256, 0, st>>>(n, ~done, seen, front);
     EG_LAUNCHED(ctx);
@@ -652,7 +676,7 @@ static int sv_bfs_retire(eg_server *s, unsigned long long done) {
     return EG_OK;
 }
 
-static int sv_bfs_advance(eg_server *s, bool *progress) {
+static int sv_bfs_advance(eg_server *s, bool *progress, bool launch, bool *launched) {
     bool ready;
     EG_TRY(sv_poll(s, E_BFS, &ready));
     if (ready) {
@@ -666,7 +690,7 @@ static int sv_bfs_advance(eg_server *s, bool *progress) {
         if (done) EG_TRY(sv_bfs_retire(s, done));
         *progress = true;
     }
-    if (s->inflight[E_BFS]) return EG_OK;
+    if (!launch || s->inflight[E_BFS]) return EG_OK;
     eg_graph *g = s->g;
     eg_ctx *ctx = g->ctx;
     const uint32_t n = g->n;
@@ -749,6 +773,7 @@ static int sv_bfs_advance(eg_server *s, bool *progress) {
     EG_CUDA(cudaMemcpyAsync(s->hpin + HP_BCNT, bcnt, sizeof(SvCounters), cudaMemcpyDeviceToHost, st));
     EG_CUDA(cudaEventRecord(s->ev_end[E_BFS], st));
     s->inflight[E_BFS] = true;
+    *launched = true;
     s->step_mask[E_BFS] = live;
     *progress = true;
     return EG_OK;
@@ -761,27 +786,32 @@ static int sv_sssp_retire(eg_server *s, unsigned long long done) {
     const uint32_t n = g->n;
     cudaStream_t st = s->st[E_SSSP];
     uint32_t *dist = bp<uint32_t>(s->sssp_buf);
-    unsigned long long *d_sum = (unsigned long long *)(bp<unsigned char>(s->small) + SM_SUM + 64);
-    unsigned long long *hsum = (unsigned long long *)(s->hpin + HP_SUM + 64);
-    for (int sl = 0; sl < SV_SSSP_SLOTS; sl++) {
-        if (!((done >> sl) & 1ull)) continue;
-        EG_CUDA(cudaMemsetAsync(d_sum, 0, 16, st));
-        k_sv_dist_summary<<<sv_blocks(ctx, n), 256, 0, st>>>(dist, n, (uint32_t)sl, d_sum);
-        EG_LAUNCHED(ctx);
-        EG_CUDA(cudaMemcpyAsync(hsum, d_sum, 16, cudaMemcpyDeviceToHost, st));
-        std::vector<uint32_t> keep;
-        if (s->opts.keep_results) {
-            keep.resize(n);
-            EG_TRY(eg_buf_ensure(ctx, g->spmv_y, (uint64_t)n * 8));
-            uint32_t *col = bp<uint32_t>(g->spmv_y);
+    unsigned long long *d_sum = (unsigned long long *)(bp<unsigned char>(s->small) + SM_RSUM + 16 * SV_BFS_SLOTS);
+    unsigned long long *hsum = (unsigned long long *)(s->hpin + HP_RSUM + 16 * SV_BFS_SLOTS);
+    EG_CUDA(cudaMemsetAsync(d_sum, 0, 16 * SV_SSSP_SLOTS, st));
+    k_sv_dist_summary<<<sv_blocks(ctx, n), 256, 0, st>>>(dist, n, done, d_sum);
+    EG_LAUNCHED(ctx);
+    std::vector<std::vector<uint32_t>> keep;
+    if (s->opts.keep_results) {
+        EG_TRY(eg_buf_ensure(ctx, g->spmv_y, (uint64_t)n * 8));
+        uint32_t *col = bp<uint32_t>(g->spmv_y);
+        for (int sl = 0; sl < SV_SSSP_SLOTS; sl++) {
+            if (!((done >> sl) & 1ull)) continue;
+            keep.emplace_back(n);
             k_sv_column<<<sv_blocks(ctx, n), 256, 0, st>>>(dist, n, SV_SSSP_SLOTS, (uint32_t)sl, col);
             EG_LAUNCHED(ctx);
-            EG_CUDA(cudaMemcpyAsync(keep.data(), col, (uint64_t)n * 4, cudaMemcpyDeviceToHost, st));
+            EG_CUDA(cudaMemcpyAsync(keep.back().data(), col, (uint64_t)n * 4, cudaMemcpyDeviceToHost, st));
+            EG_CUDA(cudaStreamSynchronize(st));  // col is reused by the next slot
         }
-        EG_CUDA(cudaStreamSynchronize(st));
-        sv_finish(s, s->sssp_id[sl], EG_Q_SSSP, s->sssp_arrival[sl], s->sssp_admit[sl], (uint32_t)hsum[0],
-                  (uint32_t)hsum[1], s->sssp_rounds[sl], 0.0);
-        if (s->opts.keep_results) s->kept.push_back(std::move(keep));
+    }
+    EG_CUDA(cudaMemcpyAsync(hsum, d_sum, 16 * SV_SSSP_SLOTS, cudaMemcpyDeviceToHost, st));
+    EG_CUDA(cudaStreamSynchronize(st));  // one wait for every retiring slot
+    size_t k = 0;
+    for (int sl = 0; sl < SV_SSSP_SLOTS; sl++) {
+        if (!((done >> sl) & 1ull)) continue;
+        sv_finish(s, s->sssp_id[sl], EG_Q_SSSP, s->sssp_arrival[sl], s->sssp_admit[sl], (uint32_t)hsum[2 * sl],
+                  (uint32_t)hsum[2 * sl + 1], s->sssp_rounds[sl], 0.0);
+        if (s->opts.keep_results) s->kept.push_back(std::move(keep[k++]));
     }
     k_sv_sssp_reset<<<sv_blocks(ctx, (uint64_t)n * SV_SSSP_SLOTS), 256, 0, st>>>(n, done, dist);
     EG_LAUNCHED(ctx);
@@ -789,7 +819,7 @@ static int sv_sssp_retire(eg_server *s, unsigned long long done) {
     return EG_OK;
 }
 
-static int sv_sssp_advance(eg_server *s, bool *progress) {
+static int sv_sssp_advance(eg_server *s, bool *progress, bool launch, bool *launched) {
     bool ready;
     EG_TRY(sv_poll(s, E_SSSP, &ready));
     if (ready) {
@@ -802,7 +832,7 @@ static int sv_sssp_advance(eg_server *s, bool *progress) {
         if (done) EG_TRY(sv_sssp_retire(s, done));
         *progress = true;
     }
-    if (s->inflight[E_SSSP]) return EG_OK;
+    if (!launch || s->inflight[E_SSSP]) return EG_OK;
     eg_graph *g = s->g;
     eg_ctx *ctx = g->ctx;
     const uint32_t n = g->n, nw = (n + 31) / 32;
@@ -818,13 +848,18 @@ static int sv_sssp_advance(eg_server *s, bool *progress) {
     int nadm = 0;
     unsigned long long taken = 0;
     const double tnow = now_s() - s->t0;
+    // gang admission: a 32-source word with a live source takes no new one
+    unsigned long long closed = s->sssp_mask;
+    if (s->opts.gang)
+        for (int j = 0; j < 2; j++)
+            if ((s->sssp_mask >> (32 * j)) & 0xffffffffull) closed |= 0xffffffffull << (32 * j);
     for (auto it = s->queue.begin(); it != s->queue.end();) {
         if (it->q.kind != EG_Q_SSSP) {
             ++it;
             continue;
         }
         int sl = 0;
-        while (sl < s->sssp_cap && (((s->sssp_mask | taken) >> sl) & 1ull)) sl++;
+        while (sl < s->sssp_cap && (((closed | taken) >> sl) & 1ull)) sl++;
         if (sl >= s->sssp_cap) break;
         taken |= 1ull << sl;
         hroots[nadm] = it->q.source;
@@ -869,13 +904,14 @@ static int sv_sssp_advance(eg_server *s, bool *progress) {
     EG_CUDA(cudaEventRecord(s->ev_end[E_SSSP], st));
     s->sssp_cur = nx;
     s->inflight[E_SSSP] = true;
+    *launched = true;
     s->step_mask[E_SSSP] = s->sssp_mask;
     *progress = true;
     return EG_OK;
 }
 
 // ---- PPR
-static int sv_ppr_advance(eg_server *s, bool *progress) {
+static int sv_ppr_advance(eg_server *s, bool *progress, bool launch, bool *launched) {
     bool ready;
     EG_TRY(sv_poll(s, E_PPR, &ready));
     eg_graph *g = s->g;
@@ -888,39 +924,47 @@ static int sv_ppr_advance(eg_server *s, bool *progress) {
     uint32_t *d_sbeg = (uint32_t *)(small + SM_PSBEG), *d_send = (uint32_t *)(small + SM_PSEND);
     float *R = bp<float>(s->ppr_buf), *X = R + (uint64_t)n * EG_PPR_LANES, *Y = X + (uint64_t)n * EG_PPR_LANES;
     PprQ *hp = s->hq;
-    bool upload = false;
     if (ready) {
         uint32_t done = 0;
         for (int q = 0; q < EG_PPR_LANES; q++)
             if (((s->ppr_mask >> q) & 1u) && hp[q].active && hp[q].done) done |= 1u << q;
+        double *dsum = (double *)(small + SM_RSUM + 16 * (SV_BFS_SLOTS + SV_SSSP_SLOTS));
+        double *hsum = (double *)(s->hpin + HP_RSUM + 16 * (SV_BFS_SLOTS + SV_SSSP_SLOTS));
+        std::vector<std::vector<uint32_t>> keep;
+        if (done) EG_CUDA(cudaMemsetAsync(dsum, 0, 8 * EG_PPR_LANES, st));
         for (int q = 0; q < EG_PPR_LANES; q++) {
             if (!((done >> q) & 1u)) continue;
-            double *dsum = (double *)(small + SM_SUM + 128);
-            double *hsum = (double *)(s->hpin + HP_SUM + 128);
-            EG_CUDA(cudaMemsetAsync(dsum, 0, 16, st));
-            std::vector<uint32_t> keep;
             float *col = nullptr;
             if (s->opts.keep_results) {
-                keep.resize(n);
                 EG_TRY(eg_buf_ensure(ctx, g->spmv_y, (uint64_t)n * 8));
                 col = bp<float>(g->spmv_y);
+                keep.emplace_back(n);
             }
-            k_sv_ppr_column<<<sv_blocks(ctx, n), 256, 0, st>>>(R, n, (uint32_t)q, col, dsum);
+            k_sv_ppr_column<<<sv_blocks(ctx, n), 256, 0, st>>>(R, n, (uint32_t)q, col, dsum + q);
             EG_LAUNCHED(ctx);
-            EG_CUDA(cudaMemcpyAsync(hsum, dsum, 8, cudaMemcpyDeviceToHost, st));
-            if (col) EG_CUDA(cudaMemcpyAsync(keep.data(), col, (uint64_t)n * 4, cudaMemcpyDeviceToHost, st));
-            EG_CUDA(cudaStreamSynchronize(st));
-            sv_finish(s, s->ppr_id[q], EG_Q_PPR, s->ppr_arrival[q], s->ppr_admit[q], 0u, 0u, hp[q].iters, *hsum);
-            if (s->opts.keep_results) s->kept.push_back(std::move(keep));
+            if (col) {
+                EG_CUDA(cudaMemcpyAsync(keep.back().data(), col, (uint64_t)n * 4, cudaMemcpyDeviceToHost, st));
+                EG_CUDA(cudaStreamSynchronize(st));  // col is reused by the next lane
+            }
+        }
+        if (done) {
+            EG_CUDA(cudaMemcpyAsync(hsum, dsum, 8 * EG_PPR_LANES, cudaMemcpyDeviceToHost, st));
+            EG_CUDA(cudaStreamSynchronize(st));  // one wait for every retiring lane
+        }
+        size_t kk = 0;
+        for (int q = 0; q < EG_PPR_LANES; q++) {
+            if (!((done >> q) & 1u)) continue;
+            sv_finish(s, s->ppr_id[q], EG_Q_PPR, s->ppr_arrival[q], s->ppr_admit[q], 0u, 0u, hp[q].iters, hsum[q]);
+            if (s->opts.keep_results) s->kept.push_back(std::move(keep[kk++]));
             hp[q].active = 0;
             hp[q].done = 0;
             s->pnseeds[q] = 0;
         }
         s->ppr_mask &= ~done;
-        upload = done != 0;
+        if (done) s->ppr_dirty = true;  // the lane table goes up with the next launch
         *progress = true;
     }
-    if (s->inflight[E_PPR]) return EG_OK;
+    if (!launch || s->inflight[E_PPR]) return EG_OK;
     uint32_t new_ppr = 0;
     const double tnow = now_s() - s->t0;
     for (auto it = s->queue.begin(); it != s->queue.end();) {
@@ -946,7 +990,8 @@ static int sv_ppr_advance(eg_server *s, bool *progress) {
         s->ppr_admit[sl] = tnow;
         it = s->queue.erase(it);
     }
-    if (new_ppr || upload) {
+    if (new_ppr || s->ppr_dirty) {
+        s->ppr_dirty = false;
         uint32_t *hseeds = (uint32_t *)(s->hpin + HP_PSEEDS), *hbeg = hseeds + 256, *hend = hbeg + 32;
         for (int q = 0; q < EG_PPR_LANES; q++) {
             hbeg[q] = 8u * q;
@@ -996,6 +1041,7 @@ static int sv_ppr_advance(eg_server *s, bool *progress) {
     EG_CUDA(cudaMemcpyAsync(hp, d_ppr, sizeof(PprQ) * EG_PPR_LANES, cudaMemcpyDeviceToHost, st));
     EG_CUDA(cudaEventRecord(s->ev_end[E_PPR], st));
     s->inflight[E_PPR] = true;
+    *launched = true;
     s->step_mask[E_PPR] = s->ppr_mask;
     *progress = true;
     return EG_OK;
@@ -1009,10 +1055,18 @@ extern "C" int eg_serve_step(eg_server *s, int *active_out) {
     EG_CUDA(cudaSetDevice(s->g->ctx->device));
     s->ticks++;
     bool progress = false;
+    typedef int (*advance_fn)(eg_server *, bool *, bool, bool *);
+    static const advance_fn adv[3] = {sv_bfs_advance, sv_sssp_advance, sv_ppr_advance};
     for (int spin = 0; spin < 20 && !progress; spin++) {
-        EG_TRY(sv_bfs_advance(s, &progress));
-        EG_TRY(sv_sssp_advance(s, &progress));
-        EG_TRY(sv_ppr_advance(s, &progress));
+        bool launched = false;
+        for (int e = 0; e < 3; e++) EG_TRY(adv[e](s, &progress, false, &launched));  // retire finished steps
+        for (int t = 0; t < 3; t++) {  // refill and launch, engines taking turns first
+            const int e = (s->turn + t) % 3;
+            if (s->opts.exclusive && (s->inflight[E_BFS] || s->inflight[E_SSSP] || s->inflight[E_PPR])) break;
+            launched = false;
+            EG_TRY(adv[e](s, &progress, true, &launched));
+            if (launched) s->turn = (e + 1) % 3;
+        }
         if (!progress) {
             if (!s->inflight[E_BFS] && !s->inflight[E_SSSP] && !s->inflight[E_PPR]) break;  // idle
             struct timespec ts = {0, 1000};

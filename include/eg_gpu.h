@@ -370,6 +370,15 @@ typedef struct {
     float ppr_damping;
     int ppr_max_iters;
     int keep_results;
+    int exclusive;       /* 1: one engine step on the GPU at a time (engines
+                            take turns, each step gets the whole GPU and L2);
+                            0 (default): the engines' steps overlap */
+    int gang;            /* 1 (default): SSSP queries enter in gangs: a word
+                            of 32 source slots is refilled only once all of
+                            its sources have finished, so the sources that
+                            share a word stay in step and relax dense rows;
+                            0: a free slot takes the next query at once
+                            (lower latency under light load) */
 } eg_serve_opts;
 void eg_serve_opts_default(eg_serve_opts *o);
 int eg_serve_open(eg_graph *g, const eg_serve_opts *opts, eg_server **out);

@@ -469,8 +469,9 @@ def test_ppr_single_query_path(case):
 
 
 # ------------------------------------------------------------------ query server
-@pytest.mark.parametrize("budget_slots", [64, 3])
-def test_server_results_equal_standalone(ctx, budget_slots):
+@pytest.mark.parametrize("budget_slots,exclusive,gang", [(64, False, True), (3, False, True), (64, True, True),
+                                                         (64, False, False)])
+def test_server_results_equal_standalone(ctx, budget_slots, exclusive, gang):
     """Mixed BFS/SSSP/PPR queries arriving over several ticks: every result
     equals the same query run alone by the plain kernels."""
     import everythinggraph_gb300 as eg
@@ -479,7 +480,7 @@ def test_server_results_equal_standalone(ctx, budget_slots):
     w = eg.weights("hash", seed=6, lo=1, hi=255)
     per_slot = n * 4 * 3
     budget = 0 if budget_slots == 64 else (n * 8 * 4 + n * 8 * 2 + (n // 32) * 8 + n * 12 + n * 16 + 3 * budget_slots * per_slot)
-    srv = eg.Server(g, hbm_budget=budget, weights_=w, keep_results=True)
+    srv = eg.Server(g, hbm_budget=budget, weights_=w, keep_results=True, exclusive=exclusive, gang=gang)
     info = srv.info()
     if budget_slots != 64:
         assert info["bfs_slots"] < 64 and info["ppr_slots"] < 32
