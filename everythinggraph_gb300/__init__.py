@@ -184,12 +184,13 @@ class Graph:
 
     def tune(self):
         """Times the row-kernel schedules on this graph and keeps the fastest;
-        returns [{tile, per_lane, prefetch, min_blocks, ms}] and the chosen
-        index."""
+        returns [{tile, per_lane, prefetch, min_blocks, cache_hint, ms}] and
+        the chosen index."""
         r = L.TuneResult()
         L.check(lib().eg_graph_tune(self._h, ctypes.byref(r)))
         cands = [{"tile": r.tile_entries[i], "per_lane": r.entries_per_lane[i], "prefetch": r.prefetch[i],
-                  "min_blocks": r.min_blocks[i], "ms": r.ms[i]} for i in range(r.ncand)]
+                  "min_blocks": r.min_blocks[i], "cache_hint": r.cache_hint[i],
+                  "ms": r.ms[i]} for i in range(r.ncand)]
         self.bfs_tuning = {"graph_ms": r.bfs_graph_ms, "host_ms": r.bfs_host_ms, "host_loop": r.bfs_host_loop}
         return cands, r.chosen
 

@@ -401,18 +401,40 @@ __global__ void k_coo_empty_rows(const uint32_t *__restrict__ ptr, uint32_t n, d
     }
 }
 
+// 128-bit streaming load of the row-id / column words.  HINT 1: the words
+// are not kept in L1 and are the first evicted from L2, which leaves both
+// caches to the gathered vector (the words are read once per pass).
+template <int HINT>
+__device__ __forceinline__ uint4 eg_stream_ld4(const uint32_t *p, uint64_t pol) {
+    if constexpr (HINT == 0) {
+        return __ldg(reinterpret_cast<const uint4 *>(p));
+    } else {
+        uint4 v;
+        asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v4.u32 {%0, %1, %2, %3}, [%4], %5;"
+            : "=r"(v.x), "=r"(v.y), "=r"(v.z), "=r"(v.w)
+            : "l"(p), "l"(pol));
+        return v;
+    }
+}
+
+__device__ __forceinline__ uint64_t eg_l2_evict_first_policy() {
+    uint64_t pol;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
 // The chunk of a warp tile starting at cb: lane l's entries cb+U*l ..
 // cb+U*l+U-1 (128-bit loads), rows past the tile end E1 set to EG_MP_NONE.
-template <int U>
+template <int U, int HINT = 0>
 __device__ __forceinline__ void eg_coov_load(const uint32_t *__restrict__ rid, const uint32_t *__restrict__ col,
                                              uint32_t cb, uint32_t E1, uint32_t lane, uint32_t (&r)[U],
-                                             uint32_t (&u)[U]) {
+                                             uint32_t (&u)[U], uint64_t pol = 0) {
     const uint32_t e = cb + U * lane;
     if (e + U - 1 < E1) {
 #pragma unroll
         for (int h = 0; h < U / 4; h++) {
-            const uint4 rr = __ldg(reinterpret_cast<const uint4 *>(rid + e) + h);
-            const uint4 cc = __ldg(reinterpret_cast<const uint4 *>(col + e) + h);
+            const uint4 rr = eg_stream_ld4<HINT>(rid + e + 4 * h, pol);
+            const uint4 cc = eg_stream_ld4<HINT>(col + e + 4 * h, pol);
             r[4 * h] = rr.x; r[4 * h + 1] = rr.y; r[4 * h + 2] = rr.z; r[4 * h + 3] = rr.w;
             u[4 * h] = cc.x; u[4 * h + 1] = cc.y; u[4 * h + 2] = cc.z; u[4 * h + 3] = cc.w;
         }
@@ -423,6 +445,136 @@ __device__ __forceinline__ void eg_coov_load(const uint32_t *__restrict__ rid, c
             r[k] = in ? __ldg(rid + e + k) : EG_MP_NONE;
             u[k] = in ? __ldg(col + e + k) : 0u;
         }
+    }
+}
+
+// Block sum of the emitted (residual, dangling) pairs into part[blockIdx.x].
+__device__ __forceinline__ void eg_coov_reduce(const eg_red2 &redf, double2 *s_red, uint32_t nwarps,
+                                               double2 *__restrict__ part) {
+    double2 red = redf.wide();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        red.x += __shfl_down_sync(EG_FULL_MASK, red.x, o);
+        red.y += __shfl_down_sync(EG_FULL_MASK, red.y, o);
+    }
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = red;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double2 sum = make_double2(0.0, 0.0);
+        for (uint32_t w = 0; w < nwarps; w++) {
+            sum.x += s_red[w].x;
+            sum.y += s_red[w].y;
+        }
+        part[blockIdx.x] = sum;
+    }
+}
+
+// One warp tile t of the row-id stream (the body of k_coov_rows);
+// `gather(e, u)` returns the value of entry e, source u.
+template <class Op, int TILE_E, int U, bool REDUCE, bool PF, int HINT, class G>
+__device__ __forceinline__ void eg_coov_tile(uint32_t t, const uint32_t *__restrict__ rid,
+                                             const uint32_t *__restrict__ col, uint32_t m,
+                                             eg_mp_carry<typename Op::A> *__restrict__ carry, const Op &op,
+                                             eg_red2 &redf, const G &gather, uint64_t pol) {
+    constexpr uint32_t CH = 32u * U;  // entries per chunk
+    using V = typename Op::V;
+    using A = typename Op::A;
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t E0 = t * (uint32_t)TILE_E;
+    const uint32_t E1 = min(E0 + (uint32_t)TILE_E, m);
+    const uint32_t first = __ldg(rid + E0);
+    const uint32_t head_row = (E0 > 0 && __ldg(rid + E0 - 1) == first) ? first : EG_MP_NONE;
+    const uint32_t tile_next = E1 < m ? __ldg(rid + E1) : EG_MP_NONE;
+    uint32_t crow = EG_MP_NONE;
+    A cval = op.zero();
+    bool head_done = false;
+    A head_val = op.zero();
+    auto finish = [&](uint32_t row, const A &val) {
+        if (row == EG_MP_NONE) return;
+        if (row == head_row) {
+            head_done = true;
+            head_val = val;
+            return;
+        }
+        const float2 d = op.emit(row, val);
+        if (REDUCE) redf.add(d);
+    };
+    uint32_t rn[U], un[U];  // prefetched next chunk (PF)
+    if (PF) eg_coov_load<U, HINT>(rid, col, E0, E1, lane, rn, un, pol);
+    for (uint32_t base = E0; base < E1; base += CH) {
+        const uint32_t e = base + U * lane;
+        uint32_t r[U], u[U];
+        if (PF) {
+#pragma unroll
+            for (int k = 0; k < U; k++) {
+                r[k] = rn[k];
+                u[k] = un[k];
+            }
+            if (base + CH < E1) eg_coov_load<U, HINT>(rid, col, base + CH, E1, lane, rn, un, pol);
+        } else {
+            eg_coov_load<U, HINT>(rid, col, base, E1, lane, r, u, pol);
+        }
+        V v[U];
+#pragma unroll
+        for (int k = 0; k < U; k++) v[k] = r[k] != EG_MP_NONE ? gather(e + k, u[k]) : V();
+        // row of the entry after this lane's last one
+        uint32_t nxt = __shfl_down_sync(EG_FULL_MASK, r[0], 1);
+        if (lane == 31) nxt = base + CH < E1 ? __ldg(rid + base + CH) : tile_next;
+        const uint32_t prev_last = __shfl_up_sync(EG_FULL_MASK, r[U - 1], 1);
+        // local runs: head run (from entry 0), middle runs, tail run (to entry U-1)
+        A hsum = op.add(op.zero(), v[0]);
+        A run = hsum;
+        bool multi = false;
+#pragma unroll
+        for (int k = 1; k < U; k++) {
+            if (r[k] != r[k - 1]) {
+                if (!multi) hsum = run;  // the head run closed at k-1
+                else finish(r[k - 1], run);
+                multi = true;
+                run = op.add(op.zero(), v[k]);
+            } else {
+                run = op.add(run, v[k]);
+            }
+        }
+        if (!multi) hsum = run;
+        // segmented scan of the tail runs across lanes
+        A x = run;
+        bool f = multi || lane == 0 || prev_last != r[0];
+        if (lane == 0 && !multi && r[0] == crow) x = op.merge(cval, x);
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            const A px = eg_shfl_up(x, off);
+            const bool pf = __shfl_up_sync(EG_FULL_MASK, f, off);
+            if (lane >= (uint32_t)off) {
+                if (!f) x = op.merge(px, x);
+                f = f || pf;
+            }
+        }
+        // carry into this lane's head run (multi-run lanes)
+        const A prevS = eg_shfl_up(x, 1);
+        if (multi) {
+            A tot = hsum;
+            if (lane == 0) {
+                if (r[0] == crow) tot = op.merge(cval, hsum);
+            } else if (prev_last == r[0]) {
+                tot = op.merge(prevS, hsum);
+            }
+            finish(r[0], tot);
+        }
+        if (nxt != r[U - 1]) finish(r[U - 1], x);
+        crow = __shfl_sync(EG_FULL_MASK, r[U - 1], 31);
+        cval = eg_shfl_idx(x, 31);
+    }
+    const uint32_t hmask = __ballot_sync(EG_FULL_MASK, head_done);
+    if (lane == 0) {
+        const bool tail_open = E1 < m && crow != EG_MP_NONE && tile_next == crow;
+        carry[t].tail_row = tail_open ? crow : EG_MP_NONE;
+        carry[t].tail_val = cval;
+        carry[t].head_row = hmask ? head_row : EG_MP_NONE;
+    }
+    if (hmask) {
+        const A hv = eg_shfl_idx(head_val, __ffs(hmask) - 1);
+        if (lane == 0) carry[t].head_val = hv;
     }
 }
 
@@ -440,136 +592,22 @@ __device__ __forceinline__ void eg_coov_load(const uint32_t *__restrict__ rid, c
 // gathers, so the streaming loads of one chunk overlap the gathers and scan
 // of the previous one.  MINB: resident CTAs per SM asked of the compiler,
 // which bounds the registers per thread (6: 42, 8: every warp slot, 32).
-template <class Op, int TILE_E, int U, bool REDUCE, bool PF = false, int MINB = 6>
+// HINT: cache hints on the streamed words (eg_stream_ld4).
+template <class Op, int TILE_E, int U, bool REDUCE, bool PF = false, int MINB = 6, int HINT = 0>
 __global__ void __launch_bounds__(256, MINB) k_coov_rows(const uint32_t *__restrict__ rid,
                                                          const uint32_t *__restrict__ col, uint32_t m, uint32_t ntiles,
                                                          eg_mp_carry<typename Op::A> *__restrict__ carry,
                                                          double2 *__restrict__ part, Op op) {
     static_assert(U == 4 || U == 8, "4 or 8 entries per lane");
     static_assert(TILE_E % (32 * U) == 0, "tiles hold whole chunks");
-    constexpr uint32_t CH = 32u * U;  // entries per chunk
-    using V = typename Op::V;
-    using A = typename Op::A;
     __shared__ double2 s_red[8];
     if (!op.active()) return;
     op.setup();
-    const uint32_t lane = threadIdx.x & 31;
     const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint64_t pol = HINT ? eg_l2_evict_first_policy() : 0;
     eg_red2 redf;
-    if (t < ntiles) {
-        const uint32_t E0 = t * (uint32_t)TILE_E;
-        const uint32_t E1 = min(E0 + (uint32_t)TILE_E, m);
-        const uint32_t first = __ldg(rid + E0);
-        const uint32_t head_row = (E0 > 0 && __ldg(rid + E0 - 1) == first) ? first : EG_MP_NONE;
-        const uint32_t tile_next = E1 < m ? __ldg(rid + E1) : EG_MP_NONE;
-        uint32_t crow = EG_MP_NONE;
-        A cval = op.zero();
-        bool head_done = false;
-        A head_val = op.zero();
-        auto finish = [&](uint32_t row, const A &val) {
-            if (row == EG_MP_NONE) return;
-            if (row == head_row) {
-                head_done = true;
-                head_val = val;
-                return;
-            }
-            const float2 d = op.emit(row, val);
-            if (REDUCE) redf.add(d);
-        };
-        uint32_t rn[U], un[U];  // prefetched next chunk (PF)
-        if (PF) eg_coov_load<U>(rid, col, E0, E1, lane, rn, un);
-        for (uint32_t base = E0; base < E1; base += CH) {
-            const uint32_t e = base + U * lane;
-            uint32_t r[U], u[U];
-            if (PF) {
-#pragma unroll
-                for (int k = 0; k < U; k++) {
-                    r[k] = rn[k];
-                    u[k] = un[k];
-                }
-                if (base + CH < E1) eg_coov_load<U>(rid, col, base + CH, E1, lane, rn, un);
-            } else {
-                eg_coov_load<U>(rid, col, base, E1, lane, r, u);
-            }
-            V v[U];
-#pragma unroll
-            for (int k = 0; k < U; k++) v[k] = r[k] != EG_MP_NONE ? op.gather(e + k, u[k]) : V();
-            // row of the entry after this lane's last one
-            uint32_t nxt = __shfl_down_sync(EG_FULL_MASK, r[0], 1);
-            if (lane == 31) nxt = base + CH < E1 ? __ldg(rid + base + CH) : tile_next;
-            const uint32_t prev_last = __shfl_up_sync(EG_FULL_MASK, r[U - 1], 1);
-            // local runs: head run (from entry 0), middle runs, tail run (to entry U-1)
-            A hsum = op.add(op.zero(), v[0]);
-            A run = hsum;
-            bool multi = false;
-#pragma unroll
-            for (int k = 1; k < U; k++) {
-                if (r[k] != r[k - 1]) {
-                    if (!multi) hsum = run;  // the head run closed at k-1
-                    else finish(r[k - 1], run);
-                    multi = true;
-                    run = op.add(op.zero(), v[k]);
-                } else {
-                    run = op.add(run, v[k]);
-                }
-            }
-            if (!multi) hsum = run;
-            // segmented scan of the tail runs across lanes
-            A x = run;
-            bool f = multi || lane == 0 || prev_last != r[0];
-            if (lane == 0 && !multi && r[0] == crow) x = op.merge(cval, x);
-#pragma unroll
-            for (int off = 1; off < 32; off <<= 1) {
-                const A px = eg_shfl_up(x, off);
-                const bool pf = __shfl_up_sync(EG_FULL_MASK, f, off);
-                if (lane >= (uint32_t)off) {
-                    if (!f) x = op.merge(px, x);
-                    f = f || pf;
-                }
-            }
-            // carry into this lane's head run (multi-run lanes)
-            const A prevS = eg_shfl_up(x, 1);
-            if (multi) {
-                A tot = hsum;
-                if (lane == 0) {
-                    if (r[0] == crow) tot = op.merge(cval, hsum);
-                } else if (prev_last == r[0]) {
-                    tot = op.merge(prevS, hsum);
-                }
-                finish(r[0], tot);
-            }
-            if (nxt != r[U - 1]) finish(r[U - 1], x);
-            crow = __shfl_sync(EG_FULL_MASK, r[U - 1], 31);
-            cval = eg_shfl_idx(x, 31);
-        }
-        const uint32_t hmask = __ballot_sync(EG_FULL_MASK, head_done);
-        if (lane == 0) {
-            const bool tail_open = E1 < m && crow != EG_MP_NONE && tile_next == crow;
-            carry[t].tail_row = tail_open ? crow : EG_MP_NONE;
-            carry[t].tail_val = cval;
-            carry[t].head_row = hmask ? head_row : EG_MP_NONE;
-        }
-        if (hmask) {
-            const A hv = eg_shfl_idx(head_val, __ffs(hmask) - 1);
-            if (lane == 0) carry[t].head_val = hv;
-        }
-    }
-    if (REDUCE) {
-        double2 red = redf.wide();
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            red.x += __shfl_down_sync(EG_FULL_MASK, red.x, o);
-            red.y += __shfl_down_sync(EG_FULL_MASK, red.y, o);
-        }
-        if (lane == 0) s_red[threadIdx.x >> 5] = red;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double2 s = make_double2(0.0, 0.0);
-            for (int w = 0; w < 8; w++) {
-                s.x += s_red[w].x;
-                s.y += s_red[w].y;
-            }
-            part[blockIdx.x] = s;
-        }
-    }
+    if (t < ntiles)
+        eg_coov_tile<Op, TILE_E, U, REDUCE, PF, HINT>(
+            t, rid, col, m, carry, op, redf, [&](uint32_t e, uint32_t u) { return op.gather(e, u); }, pol);
+    if (REDUCE) eg_coov_reduce(redf, s_red, 8, part);
 }

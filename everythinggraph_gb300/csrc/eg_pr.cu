@@ -229,20 +229,23 @@ __global__ void k_pr_reduce(const double2 *__restrict__ part, uint32_t nparts, e
 // Row-id stream kernel (k_coov_rows): one warp per TILE entries, U entries
 // per lane.  part[] receives per-CTA partials of the main kernel, then of the
 // empty-row kernel, then of the fix-up; returns their count.  The schedule
-// (TILE, U) is the graph's row_cfg, picked by eg_graph_tune.
+// (TILE, U, ...) is the graph's row_cfg, picked by eg_graph_tune; `hint`
+// keeps the streamed row ids and columns out of L1 and first in line for L2
+// eviction.
 #define EG_COO_TILE_MIN 512
 #define EG_PR_CHECK 4  // iterations between reads of the stop flag
 #define EG_PR_RES_BLOCKS 1024
-#define EG_ROW_CFGS 8
+#define EG_ROW_CFGS 10
 struct RowCfg {
-    int tile, u, pf, minb;
+    int tile, u, pf, minb, hint;
 };
 // min_blocks bounds the registers: 6 resident CTAs of 256 threads leave 42
 // registers per thread, 5 leave 51, 4 leave 64, 8 leave 32.
-static const RowCfg kRowCfg[EG_ROW_CFGS] = {{1024, 4, 1, 5}, {2048, 4, 0, 6}, {2048, 4, 1, 5}, {1024, 4, 1, 6},
-                                            {512, 4, 1, 5},  {1024, 8, 1, 4}, {1024, 4, 0, 8}, {2048, 8, 0, 5}};
+static const RowCfg kRowCfg[EG_ROW_CFGS] = {
+    {1024, 4, 1, 5, 0}, {2048, 4, 0, 6, 0}, {2048, 4, 1, 5, 0}, {1024, 4, 1, 6, 0}, {512, 4, 1, 5, 0},
+    {1024, 8, 1, 4, 0}, {1024, 4, 0, 8, 0}, {2048, 8, 0, 5, 0}, {1024, 4, 1, 5, 1}, {2048, 4, 1, 5, 1}};
 
-template <class Op, int TILE, int U, bool REDUCE, bool PF, int MINB>
+template <class Op, int TILE, int U, bool REDUCE, bool PF, int MINB, int HINT = 0>
 static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts,
                         cudaEvent_t ev_begin, cudaEvent_t ev_end) {
     eg_ctx *ctx = g->ctx;
@@ -250,41 +253,44 @@ static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *pa
     const uint32_t m = (uint32_t)g->m;
     const uint32_t ntiles = m ? eg_div_up(m, TILE) : 0;
     EG_TRY(eg_buf_ensure(ctx, carry_buf, ((uint64_t)ntiles + 1) * sizeof(eg_mp_carry<A>)));
-    const uint32_t g1 = ntiles ? eg_div_up((uint64_t)ntiles * 32, 256) : 0;
+    const uint32_t gf = ntiles ? eg_div_up((uint64_t)ntiles * 32, 256) : 0;  // one warp per tile
+    const uint32_t g1 = gf;
     uint32_t g2 = eg_div_up(g->n, 256);
     if (g2 > (uint32_t)ctx->sm_count * 8) g2 = (uint32_t)ctx->sm_count * 8;
     if (g1) {
         if (ev_begin) EG_CUDA(cudaEventRecord(ev_begin, ctx->stream));
-        k_coov_rows<Op, TILE, U, REDUCE, PF, MINB><<<g1, 256, 0, ctx->stream>>>(
-            bp<uint32_t>(adj.rid), bp<uint32_t>(adj.col), m, ntiles, bp<eg_mp_carry<A>>(carry_buf), part, op);
+        k_coov_rows<Op, TILE, U, REDUCE, PF, MINB, HINT><<<g1, 256, 0, ctx->stream>>>(
+                bp<uint32_t>(adj.rid), bp<uint32_t>(adj.col), m, ntiles, bp<eg_mp_carry<A>>(carry_buf), part, op);
         EG_LAUNCHED(ctx);
         if (ev_end) EG_CUDA(cudaEventRecord(ev_end, ctx->stream));
     }
     k_coo_empty_rows<Op, REDUCE><<<g2, 256, 0, ctx->stream>>>(bp<uint32_t>(adj.ptr), g->n, part ? part + g1 : nullptr,
                                                               op);
     EG_LAUNCHED(ctx);
-    if (g1) {
-        k_coo_fixup<Op, TILE, REDUCE><<<g1, 256, 0, ctx->stream>>>(
+    if (gf) {
+        k_coo_fixup<Op, TILE, REDUCE><<<gf, 256, 0, ctx->stream>>>(
             bp<uint32_t>(adj.ptr), ntiles, bp<eg_mp_carry<A>>(carry_buf), part ? part + g1 + g2 : nullptr, op);
         EG_LAUNCHED(ctx);
     }
-    *nparts = g1 + g2 + g1;
+    *nparts = g1 + g2 + gf;
     return EG_OK;
 }
 
 template <class Op, bool REDUCE>
 static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts,
                       cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr) {
-#define EG_ROW_CASE(i, T, U, PF, MB) \
-    case i: return coo_launch_t<Op, T, U, REDUCE, PF, MB>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
+#define EG_ROW_CASE(i, T, U, PF, MB, H) \
+    case i: return coo_launch_t<Op, T, U, REDUCE, PF, MB, H>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
     switch (g->row_cfg) {
-        EG_ROW_CASE(1, 2048, 4, false, 6)
-        EG_ROW_CASE(2, 2048, 4, true, 5)
-        EG_ROW_CASE(3, 1024, 4, true, 6)
-        EG_ROW_CASE(4, 512, 4, true, 5)
-        EG_ROW_CASE(5, 1024, 8, true, 4)
-        EG_ROW_CASE(6, 1024, 4, false, 8)
-        EG_ROW_CASE(7, 2048, 8, false, 5)
+        EG_ROW_CASE(1, 2048, 4, false, 6, 0)
+        EG_ROW_CASE(2, 2048, 4, true, 5, 0)
+        EG_ROW_CASE(3, 1024, 4, true, 6, 0)
+        EG_ROW_CASE(4, 512, 4, true, 5, 0)
+        EG_ROW_CASE(5, 1024, 8, true, 4, 0)
+        EG_ROW_CASE(6, 1024, 4, false, 8, 0)
+        EG_ROW_CASE(7, 2048, 8, false, 5, 0)
+        EG_ROW_CASE(8, 1024, 4, true, 5, 1)
+        EG_ROW_CASE(9, 2048, 4, true, 5, 1)
         default: return coo_launch_t<Op, 1024, 4, REDUCE, true, 5>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
     }
 #undef EG_ROW_CASE
@@ -537,6 +543,7 @@ extern "C" int eg_graph_tune(eg_graph *g, eg_tune_result *out) {
         r.entries_per_lane[c] = kRowCfg[c].u;
         r.prefetch[c] = kRowCfg[c].pf;
         r.min_blocks[c] = kRowCfg[c].minb;
+        r.cache_hint[c] = kRowCfg[c].hint;
         r.ms[c] = st.row_kernel_ms;
         if (st.row_kernel_ms < r.ms[best]) best = c;
     }

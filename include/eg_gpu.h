@@ -170,16 +170,20 @@ int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out, eg_pr_stat
  * eg_graph_tune times every schedule on this graph (two 6-iteration PageRank
  * runs each, CUDA events around the row kernel) and keeps the fastest for
  * eg_pagerank, eg_ppr and eg_spmv on this graph; eg_graph_set_row_schedule
- * picks one by index (0 = 1024 x 4 with prefetch, the default).  Schedules change only
- * how rows are split between warps, i.e. the fp32 summation order. */
+ * picks one by index (0 = 1024 x 4 with prefetch, the default).  cache_hint
+ * keeps the streamed row ids and columns out of L1 and first in line for L2
+ * eviction.  Schedules change only how rows are split between warps, i.e.
+ * the fp32 summation order. */
+#define EG_ROW_SCHEDULES_MAX 16
 typedef struct {
     int ncand;
     int chosen;               /* index of the schedule kept */
-    int tile_entries[8];
-    int entries_per_lane[8];
-    int prefetch[8];
-    int min_blocks[8];
-    float ms[8];              /* mean row-kernel time per iteration */
+    int tile_entries[EG_ROW_SCHEDULES_MAX];
+    int entries_per_lane[EG_ROW_SCHEDULES_MAX];
+    int prefetch[EG_ROW_SCHEDULES_MAX];
+    int min_blocks[EG_ROW_SCHEDULES_MAX];
+    int cache_hint[EG_ROW_SCHEDULES_MAX];
+    float ms[EG_ROW_SCHEDULES_MAX]; /* mean row-kernel time per iteration */
     /* BFS level loop (when the graph has a CSR): mean ms per BFS over 4
      * sampled roots for the CUDA-graph and the host-driven loop, and the
      * form kept for eg_bfs's host_loop = -1 */

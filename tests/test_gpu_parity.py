@@ -163,7 +163,8 @@ def test_row_schedules_and_autotuner(case):
     vals = oracle.hash_values(adj.in_col, adj.in_dst(), 9)
     y_ref = oracle.spmv_f64(n, adj.in_ptr, adj.in_col, vals, x)
     cands, chosen = g.tune()
-    assert len(cands) == 8 and 0 <= chosen < 8
+    assert len(cands) == 10 and 0 <= chosen < 10
+    assert sum(c["cache_hint"] for c in cands) == 2
     if n > 1000:
         assert all(c["ms"] > 0 for c in cands)
     assert cands[chosen]["ms"] == min(c["ms"] for c in cands)
@@ -176,7 +177,7 @@ def test_row_schedules_and_autotuner(case):
         l1, mx = rel_errors(y, y_ref)
         assert l1 <= PR_REL_L1, (cands[idx], l1)
     with pytest.raises(RuntimeError):
-        g.set_row_schedule(8)
+        g.set_row_schedule(len(cands))
     g.set_row_schedule(0)
 
 
