@@ -20,71 +20,124 @@ struct PprQ {  // per-query state (device)
     int active;  // lane in use
 };
 
+__device__ __forceinline__ float4 eg_f4add(float4 a, float4 b) {
+    return make_float4(a.x + b.x, a.y + b.y, a.z + b.z, a.w + b.w);
+}
+__device__ __forceinline__ float4 eg_f4shfl(unsigned mask, float4 v, int src) {
+    return make_float4(__shfl_sync(mask, v.x, src), __shfl_sync(mask, v.y, src), __shfl_sync(mask, v.z, src),
+                       __shfl_sync(mask, v.w, src));
+}
+
 // Y[v][q] = sum over CSC entries of row v of X[u][q], for the rows whose
 // entries lie in this warp's tile; rows open at the tile ends go to carries.
-__global__ void __launch_bounds__(256) k_ppr_rows(const uint32_t *__restrict__ rid, const uint32_t *__restrict__ col,
-                                                  uint32_t m, uint32_t ntiles, const float *__restrict__ X,
-                                                  float *__restrict__ Y, float *__restrict__ head_val,
-                                                  float *__restrict__ tail_val, uint32_t *__restrict__ head_row) {
-    const uint32_t lane = threadIdx.x & 31;
+//
+// The warp is four groups of 8 lanes; lane s of a group holds queries
+// 4s..4s+3 (one 16-byte load brings a group a whole 128-byte row of X), and
+// group g walks quarter g of the tile on its own, 8 entries per step with
+// their 8 row loads in flight.  A row is summed in entry order inside a
+// group; a row crossing quarter boundaries is completed by the merge at the
+// end, which adds the groups' parts in quarter order.
+__global__ void __launch_bounds__(256, 3) k_ppr_rows(const uint32_t *__restrict__ rid,
+                                                     const uint32_t *__restrict__ col, uint32_t m, uint32_t ntiles,
+                                                     const float *__restrict__ X, float *__restrict__ Y,
+                                                     float *__restrict__ head_val, float *__restrict__ tail_val,
+                                                     uint32_t *__restrict__ head_row) {
+    constexpr uint32_t SUB = EG_PPR_TILE / 4;
+    const uint32_t lane = threadIdx.x & 31, grp = lane >> 3, sl = lane & 7;
     const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     if (t >= ntiles) return;
+    const float4 *__restrict__ X4 = reinterpret_cast<const float4 *>(X);
+    float4 *__restrict__ Y4 = reinterpret_cast<float4 *>(Y);
     const uint32_t E0 = t * EG_PPR_TILE, E1 = min(E0 + EG_PPR_TILE, m);
-    const uint32_t first = __ldg(rid + E0);
-    const uint32_t hrow = (E0 > 0 && __ldg(rid + E0 - 1) == first) ? first : EG_PPR_NONE;
+    const uint32_t hrow = (E0 > 0 && __ldg(rid + E0 - 1) == __ldg(rid + E0)) ? __ldg(rid + E0) : EG_PPR_NONE;
     const uint32_t tnext = E1 < m ? __ldg(rid + E1) : EG_PPR_NONE;
-    float acc = 0.f;
+    const uint32_t S0 = min(E0 + grp * SUB, E1), S1 = min(S0 + SUB, E1);
+    const unsigned gmask = 0xffu << (grp * 8);
+    const float4 zero = make_float4(0.f, 0.f, 0.f, 0.f);
+    // group state: its first row (and that row's sum if it ended inside the
+    // quarter), its open last row and partial sum
+    const uint32_t first = S0 < S1 ? __ldg(rid + S0) : EG_PPR_NONE;
+    bool fclosed = false;
+    float4 fval = zero, acc = zero;
     uint32_t cur = first;
-    bool hdone = false;
-    float hval = 0.f;
-    for (uint32_t base = E0; base < E1; base += 32) {
-        const uint32_t e = base + lane;
-        const uint32_t my_r = e < E1 ? __ldg(rid + e) : EG_PPR_NONE;
-        const uint32_t my_c = e < E1 ? __ldg(col + e) : 0u;
-        const uint32_t cnt = min(32u, E1 - base);
-        // 8 entries per step: their 8 row loads are issued before any is
-        // added, then added in entry order (the same order as one at a time)
-        for (uint32_t j0 = 0; j0 < cnt; j0 += 8) {
-            uint32_t rr[8];
-            float xv[8];
+    for (uint32_t base = S0; base < S1; base += 8) {
+        const uint32_t e = base + sl;
+        const uint32_t my_r = e < S1 ? __ldg(rid + e) : EG_PPR_NONE;
+        const uint32_t my_c = e < S1 ? __ldg(col + e) : 0u;
+        const uint32_t cnt = min(8u, S1 - base);
+        uint32_t rr[8];
+        float4 xv[8];
 #pragma unroll
-            for (uint32_t q = 0; q < 8; q++) {
-                const uint32_t j = j0 + q;
-                rr[q] = __shfl_sync(EG_FULL_MASK, my_r, j & 31);
-                const uint32_t u = __shfl_sync(EG_FULL_MASK, my_c, j & 31);
-                xv[q] = j < cnt ? __ldg(X + (uint64_t)u * EG_PPR_LANES + lane) : 0.f;
-            }
+        for (uint32_t q = 0; q < 8; q++) {
+            rr[q] = __shfl_sync(gmask, my_r, q, 8);
+            const uint32_t u = __shfl_sync(gmask, my_c, q, 8);
+            xv[q] = q < cnt ? __ldg(X4 + (uint64_t)u * (EG_PPR_LANES / 4) + sl) : zero;
+        }
 #pragma unroll
-            for (uint32_t q = 0; q < 8; q++) {
-                if (j0 + q >= cnt) break;
-                if (rr[q] != cur) {  // row `cur` ended inside the tile
-                    if (cur == hrow) {
-                        hdone = true;
-                        hval = acc;
-                    } else {
-                        Y[(uint64_t)cur * EG_PPR_LANES + lane] = acc;
-                    }
-                    acc = 0.f;
-                    cur = rr[q];
+        for (uint32_t q = 0; q < 8; q++) {
+            if (q >= cnt) break;
+            if (rr[q] != cur) {  // row `cur` ended inside the quarter
+                if (cur == first) {
+                    fclosed = true;
+                    fval = acc;
+                } else {
+                    Y4[(uint64_t)cur * (EG_PPR_LANES / 4) + sl] = acc;
                 }
-                acc += xv[q];
+                acc = zero;
+                cur = rr[q];
             }
+            acc = eg_f4add(acc, xv[q]);
         }
     }
-    // the last row: complete if the next tile starts another row
-    if (tnext != cur) {
-        if (cur == hrow) {
+    // merge the quarters in order: (orow, oval) is the row open so far
+    uint32_t orow = EG_PPR_NONE;
+    float4 oval = zero;
+    bool hdone = false;
+    float4 hval = zero;
+    auto emit = [&](uint32_t row, float4 v) {  // every group holds the merged values: group 0 writes
+        if (row == hrow) {
             hdone = true;
-            hval = acc;
-        } else {
-            Y[(uint64_t)cur * EG_PPR_LANES + lane] = acc;
+            hval = v;
+        } else if (lane < 8) {
+            Y4[(uint64_t)row * (EG_PPR_LANES / 4) + sl] = v;
         }
-        tail_val[(uint64_t)t * EG_PPR_LANES + lane] = 0.f;
-    } else {
-        tail_val[(uint64_t)t * EG_PPR_LANES + lane] = acc;
+    };
+#pragma unroll
+    for (uint32_t gq = 0; gq < 4; gq++) {
+        const int src = (int)(gq * 8 + sl);
+        const uint32_t f = __shfl_sync(EG_FULL_MASK, first, src);
+        if (f == EG_PPR_NONE) continue;  // empty quarter (short last tile)
+        const bool fc = __shfl_sync(EG_FULL_MASK, fclosed, src);
+        const uint32_t c = __shfl_sync(EG_FULL_MASK, cur, src);
+        const float4 fv = eg_f4shfl(EG_FULL_MASK, fval, src);
+        const float4 av = eg_f4shfl(EG_FULL_MASK, acc, src);
+        if (fc) {  // the quarter's first row ended inside it
+            if (orow == f) {
+                emit(f, eg_f4add(oval, fv));
+            } else {
+                if (orow != EG_PPR_NONE) emit(orow, oval);
+                emit(f, fv);
+            }
+            orow = c;
+            oval = av;
+        } else if (orow == f) {  // one row through the whole quarter
+            oval = eg_f4add(oval, av);
+        } else {
+            if (orow != EG_PPR_NONE) emit(orow, oval);
+            orow = f;
+            oval = av;
+        }
+    }
+    float4 *tv = reinterpret_cast<float4 *>(tail_val) + (uint64_t)t * (EG_PPR_LANES / 4);
+    // the last row: complete if the next tile starts another row
+    if (tnext != orow) {
+        emit(orow, oval);
+        if (lane < 8) tv[sl] = zero;
+    } else if (lane < 8) {
+        tv[sl] = oval;
     }
     if (lane == 0) head_row[t] = hdone ? hrow : EG_PPR_NONE;
-    if (hdone) head_val[(uint64_t)t * EG_PPR_LANES + lane] = hval;
+    if (hdone && lane < 8) reinterpret_cast<float4 *>(head_val)[(uint64_t)t * (EG_PPR_LANES / 4) + sl] = hval;
 }
 
 // Rows split between tiles: a warp per tile with a head row adds the tails of
