@@ -207,19 +207,21 @@ __global__ void k_sv_sssp_admit(const uint32_t *roots, const uint32_t *slots, in
     }
 }
 
-// Records v in the next frontier for slots of word j (eg_mrelax's Sink);
-// actmask collects the slots that improved anything this round.
+// Records v in the next frontier for slots of word j (eg_mrelax's Sink).
+// The slots that improved anything collect in lane 0's registers (am) and
+// reach cnt->actmask once per warp (flush), not once per improved edge.
 struct SvSink {
     uint32_t j;
     uint32_t *next_act, *next_inq, *next_queue;
     SvCounters *cnt;
+    uint32_t am[2];
     __device__ __forceinline__ bool enqueue_bit(uint32_t v) {
         const uint32_t bit = 1u << (v & 31);
         return !(atomicOr(next_inq + (v >> 5), bit) & bit);
     }
     __device__ __forceinline__ void row(uint32_t v, uint32_t ball) {
         atomicOr(next_act + (uint64_t)v * 2 + j, ball);
-        atomicOr(&cnt->actmask[j], (unsigned long long)ball);
+        am[j] |= ball;
         if (enqueue_bit(v)) next_queue[atomicAdd(&cnt->qsize, 1u)] = v;
     }
     __device__ __forceinline__ bool mark(uint32_t v, uint32_t bit) {
@@ -234,7 +236,12 @@ struct SvSink {
         base = __shfl_sync(EG_FULL_MASK, base, 0);
         if (q) next_queue[base + __popc(ball & eg_lanemask_lt())] = v;
     }
-    __device__ __forceinline__ void any(uint32_t bit) { atomicOr(&cnt->actmask[j], (unsigned long long)bit); }
+    __device__ __forceinline__ void any(uint32_t bit) { am[j] |= bit; }
+    __device__ __forceinline__ void flush() {
+        if ((threadIdx.x & 31) != 0) return;
+        if (am[0]) atomicOr(&cnt->actmask[0], (unsigned long long)am[0]);
+        if (am[1]) atomicOr(&cnt->actmask[1], (unsigned long long)am[1]);
+    }
 };
 
 __global__ void __launch_bounds__(256) k_sv_sssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
@@ -245,11 +252,12 @@ __global__ void __launch_bounds__(256) k_sv_sssp_push(const uint32_t *__restrict
     const uint32_t qlen = qc->qsize;
     const uint64_t warps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
     unsigned long long scanned = 0;
-    SvSink sink{0, next_act, next_inq, next_queue, cnt};
+    SvSink sink{0, next_act, next_inq, next_queue, cnt, {0u, 0u}};
     for (uint64_t base = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * 32; base < 2ull * qlen;
          base += warps * 32)
         eg_mrelax_items(base, 2ull * qlen, queue, 2u, ptr, col, wts, w, SV_SSSP_SLOTS, dist, act, SV_BIG_DEG, big,
                         &cnt->nbig, sink, scanned);
+    sink.flush();
 }
 
 // Deferred (hub, word) items in chunks of SV_SSSP_CHUNK edges, one CTA per
@@ -266,6 +274,7 @@ __global__ void __launch_bounds__(256) k_sv_sssp_push_big(const uint32_t *__rest
     if (!nbig) return;
     const uint32_t total = bigoff[nbig];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    SvSink sink{0, next_act, next_inq, next_queue, cnt, {0u, 0u}};
     for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
         const uint32_t i = eg_big_item(bigoff, nbig, c);
         const uint32_t u = big[i] >> 1, j = big[i] & 1;
@@ -276,10 +285,11 @@ __global__ void __launch_bounds__(256) k_sv_sssp_push_big(const uint32_t *__rest
         const uint32_t ve = ptr[u + 1];
         const uint32_t b = ptr[u] + (c - bigoff[i]) * SV_SSSP_CHUNK + 32u * warp;
         if (b < ve) {
-            SvSink sink{j, next_act, next_inq, next_queue, cnt};
+            sink.j = j;
             eg_mrelax(u, b, ve - b > 32 ? b + 32 : ve, col, wts, w, a, du, j, SV_SSSP_SLOTS, dist, sink);
         }
     }
+    sink.flush();
 }
 
 __global__ void k_sv_sssp_clear_frontier(const uint32_t *__restrict__ queue, const SvCounters *qc, uint32_t *act,
