@@ -11,10 +11,30 @@
 //
 // An item is vertex * per + word (per = 1 for one source, the number of
 // 32-source words for the batched kernels).
+//
+// eg_warp_grab / eg_cta_grab hand out work units from a counter zeroed
+// before the launch, so that a grid with more CTAs than fit on the SMs at
+// once, or units of uneven cost, leave no tail of idle SMs.
 #pragma once
 #include "eg_internal.cuh"
 
 namespace {
+
+// Next unit for the calling warp (lane 0 takes it, every lane gets it).
+__device__ __forceinline__ uint32_t eg_warp_grab(uint32_t *counter) {
+    uint32_t c = 0;
+    if ((threadIdx.x & 31) == 0) c = atomicAdd(counter, 1u);
+    return __shfl_sync(EG_FULL_MASK, c, 0);
+}
+
+// Next unit for the calling CTA (every thread calls it).
+__device__ __forceinline__ uint32_t eg_cta_grab(uint32_t *counter) {
+    __shared__ uint32_t s_unit;
+    __syncthreads();  // every thread has read the previous unit
+    if (threadIdx.x == 0) s_unit = atomicAdd(counter, 1u);
+    __syncthreads();
+    return s_unit;
+}
 
 __global__ void __launch_bounds__(1024) k_big_offsets(const uint32_t *__restrict__ items,
                                                       const uint32_t *__restrict__ count, uint32_t per,

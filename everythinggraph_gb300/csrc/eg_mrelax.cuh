@@ -14,6 +14,13 @@
 //    per active source (scattered 4-byte distance accesses), so a word with
 //    2 active sources costs 2 warp steps per 32 edges instead of 32.
 //
+// An update counts as an improvement when nd is below the distance read just
+// before it; the atomicMin's old value is not awaited.  When another
+// relaxation of the same (vertex, source) got below nd in between, that one
+// improved and marks the same frontier bit, so the next frontier is the same
+// set as with the old value tested, and one memory round trip leaves each
+// relaxation's critical path.
+//
 // The Sink records the next frontier:
 //   row(v, ball)      lane 0: sources `ball` of word j improved at v
 //   mark(v, bit)      one lane: source bit `bit` improved at v; returns true
@@ -49,9 +56,10 @@ __device__ __forceinline__ void eg_mrelax_rows(uint32_t u, uint32_t p0, uint32_t
                 cur[q] = (on && vv[q] != u) ? __ldcg(dist + (uint64_t)vv[q] * K + s) : 0u;
 #pragma unroll
             for (int q = 0; q < 4; q++) {
-                bool improved = false;
-                if (on && vv[q] != u && nd[q] < cur[q])  // self-loops skipped (sssp_pushpull.c:80)
-                    improved = nd[q] < atomicMin(dist + (uint64_t)vv[q] * K + s, nd[q]);
+                // self-loops skipped (sssp_pushpull.c:80); the atomic's old
+                // value is not awaited (see the header)
+                const bool improved = on && vv[q] != u && nd[q] < cur[q];
+                if (improved) atomicMin(dist + (uint64_t)vv[q] * K + s, nd[q]);
                 const uint32_t ball = __ballot_sync(EG_FULL_MASK, improved);
                 if (ball && lane == 0) sink.row(vv[q], ball);
             }
@@ -77,7 +85,10 @@ __device__ __forceinline__ void eg_mrelax_edges(uint32_t u, uint32_t p0, uint32_
             bool improved = false;
             if (v != u) {  // self-loops (and lanes past the end) skipped
                 uint32_t *dp = dist + (uint64_t)v * K + s;
-                if (nd < __ldcg(dp)) improved = nd < atomicMin(dp, nd);
+                if (nd < __ldcg(dp)) {
+                    atomicMin(dp, nd);
+                    improved = true;
+                }
             }
             const bool q = improved && sink.mark(v, 1u << sl);
             if (__ballot_sync(EG_FULL_MASK, improved) && lane == 0) sink.any(1u << sl);

@@ -47,6 +47,7 @@ struct SvCounters {
     uint32_t count;                 // vertices in the new frontier
     uint32_t qsize;
     uint32_t nbig;
+    uint32_t grab, grab_big;  // SSSP work units handed out this step
     uint32_t pad;
 };
 
@@ -250,18 +251,19 @@ __global__ void __launch_bounds__(256) k_sv_sssp_push(const uint32_t *__restrict
                                                       uint32_t *next_act, uint32_t *next_inq, uint32_t *next_queue,
                                                       SvW w, SvCounters *cnt, uint32_t *big) {
     const uint32_t qlen = qc->qsize;
-    const uint64_t warps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
     unsigned long long scanned = 0;
     SvSink sink{0, next_act, next_inq, next_queue, cnt, {0u, 0u}};
-    for (uint64_t base = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * 32; base < 2ull * qlen;
-         base += warps * 32)
+    for (;;) {  // 32 items per unit
+        const uint64_t base = (uint64_t)eg_warp_grab(&cnt->grab) * 32;
+        if (base >= 2ull * qlen) break;
         eg_mrelax_items(base, 2ull * qlen, queue, 2u, ptr, col, wts, w, SV_SSSP_SLOTS, dist, act, SV_BIG_DEG, big,
                         &cnt->nbig, sink, scanned);
+    }
     sink.flush();
 }
 
-// Deferred (hub, word) items in chunks of SV_SSSP_CHUNK edges, one CTA per
-// chunk, one warp per 32 edges of it.
+// Deferred (hub, word) items in chunks of SV_SSSP_CHUNK edges handed out to
+// the CTAs, one warp per 32 edges of a chunk.
 #define SV_SSSP_CHUNK 256u
 __global__ void __launch_bounds__(256) k_sv_sssp_push_big(const uint32_t *__restrict__ ptr,
                                                           const uint32_t *__restrict__ col,
@@ -275,7 +277,9 @@ __global__ void __launch_bounds__(256) k_sv_sssp_push_big(const uint32_t *__rest
     const uint32_t total = bigoff[nbig];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     SvSink sink{0, next_act, next_inq, next_queue, cnt, {0u, 0u}};
-    for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
+    for (;;) {
+        const uint32_t c = eg_cta_grab(&cnt->grab_big);
+        if (c >= total) break;
         const uint32_t i = eg_big_item(bigoff, nbig, c);
         const uint32_t u = big[i] >> 1, j = big[i] & 1;
         const uint32_t a = act[(uint64_t)u * 2 + j];

@@ -25,6 +25,7 @@ struct SsspCounters {
     uint32_t qsize;
     uint32_t nbig;             // frontier vertices deferred to the grid-wide kernel
     unsigned long long reached;
+    uint32_t grab, grab_big;   // work units handed out (batched kernels), zeroed per round
 };
 
 // Frontier vertices with more out-edges than this are relaxed by the whole
@@ -50,8 +51,9 @@ __device__ __forceinline__ bool sssp_relax(uint32_t u, uint32_t du, uint32_t v, 
     if (v == u) return false;  // self-loops skipped (sssp_pushpull.c:80)
     const uint32_t nd = w.add(du, wt);
     if (nd >= __ldcg(dist + v)) return false;
-    const uint32_t old = atomicMin(dist + v, nd);
-    if (nd >= old) return false;
+    // no wait for the old value: when another relaxation got below nd first,
+    // that one marks v, so the frontier is the same set either way
+    atomicMin(dist + v, nd);
     const uint32_t bit = 1u << (v & 31);
     return !(atomicOr(next_bm + (v >> 5), bit) & bit);
 }
@@ -333,19 +335,21 @@ __global__ void __launch_bounds__(256) k_msssp_push(const uint32_t *__restrict__
                                                     uint32_t *next_act, uint32_t *next_inq, uint32_t *next_queue,
                                                     WRule w, SsspCounters *cnt, uint32_t *big) {
     const uint32_t lane = threadIdx.x & 31;
-    const uint64_t warps = (gridDim.x * (uint64_t)blockDim.x) >> 5;
     unsigned long long scanned = 0;
     const uint64_t items = (uint64_t)qlen * kw;
     MsSink sink{0, kw, next_act, next_inq, next_queue, cnt};
-    for (uint64_t base = ((blockIdx.x * (uint64_t)blockDim.x + threadIdx.x) >> 5) * 32; base < items; base += warps * 32)
+    for (;;) {  // 32 items per unit
+        const uint64_t base = (uint64_t)eg_warp_grab(&cnt->grab) * 32;
+        if (base >= items) break;
         eg_mrelax_items(base, items, queue, kw, ptr, col, wts, w, (uint32_t)k, dist, act, EG_SSSP_BIG_DEG, big,
                         &cnt->nbig, sink, scanned);
+    }
     if (lane == 0 && scanned) atomicAdd(&cnt->relax, scanned);
 }
 
 // The deferred (high-degree vertex, source word) items: chunks of
-// EG_MSSSP_CHUNK edges shared out over the grid, one CTA per chunk, one warp
-// per 32 edges of it.
+// EG_MSSSP_CHUNK edges handed out to the CTAs, one warp per 32 edges of a
+// chunk.
 #define EG_MSSSP_CHUNK 256u
 __global__ void __launch_bounds__(256) k_msssp_push_big(const uint32_t *__restrict__ ptr,
                                                         const uint32_t *__restrict__ col,
@@ -359,7 +363,9 @@ __global__ void __launch_bounds__(256) k_msssp_push_big(const uint32_t *__restri
     const uint32_t total = bigoff[nbig];
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     unsigned long long scanned = 0;
-    for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
+    for (;;) {
+        const uint32_t c = eg_cta_grab(&cnt->grab_big);
+        if (c >= total) break;
         const uint32_t i = eg_big_item(bigoff, nbig, c);
         const uint32_t item = big[i];
         const uint32_t u = item / kw, j = item % kw;
@@ -448,6 +454,7 @@ extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg
     while (qlen > 0) {
         const int nxt = cur ^ 1;
         EG_CUDA(cudaMemsetAsync(&cnt->qsize, 0, 8, ctx->stream));  // qsize and nbig
+        EG_CUDA(cudaMemsetAsync(&cnt->grab, 0, 8, ctx->stream));   // grab and grab_big
         k_msssp_push<<<blocks_for(ctx, (uint64_t)qlen * kw), 256, 0, ctx->stream>>>(
             bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), wts, q[cur], qlen, k, kw, dist, act[cur], act[nxt], inq[nxt],
             q[nxt], w, cnt, big);
