@@ -31,6 +31,7 @@ struct BfsCounters {
 // grid (k_bfs_push_big) instead of one warp: an RMAT hub has 10^5..10^6.
 #define EG_BFS_BIG_DEG 2048u
 #define EG_BFS_CHUNK 4096u  // edges of a deferred hub per CTA work unit
+#define EG_BFS_SMALL_BIG 64u  // the deferral threshold of levels with few frontier vertices
 
 // Block-level reduction of per-thread counters: one atomic per block.
 __device__ __forceinline__ void block_add_counters(BfsCounters *c, uint32_t cnt, unsigned long long deg) {
@@ -114,13 +115,14 @@ __device__ __forceinline__ void warp_append(bool claimed, uint32_t v, uint32_t *
 }
 
 // Top-down step: one warp per frontier vertex, lanes over its out-list.
-// Vertices with more than EG_BFS_BIG_DEG out-edges go to a side list that
+// Vertices with more than big_deg out-edges go to a side list that
 // k_bfs_push_big expands with every thread of the grid.
 __global__ void __launch_bounds__(256) k_bfs_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
                                                   const uint32_t *__restrict__ deg, const uint32_t *__restrict__ queue,
                                                   uint32_t qlen, uint32_t *visited, uint32_t *next_bm,
                                                   uint32_t *next_queue, int32_t *level, int32_t *parent,
-                                                  int32_t next_level, BfsCounters *cnt, uint32_t *big) {
+                                                  int32_t next_level, BfsCounters *cnt, uint32_t *big,
+                                                  uint32_t big_deg) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     uint32_t my_cnt = 0;
@@ -129,7 +131,7 @@ __global__ void __launch_bounds__(256) k_bfs_push(const uint32_t *__restrict__ p
     for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < qlen; qi += warps) {
         const uint32_t u = queue[qi];
         const uint32_t b = ptr[u], e = ptr[u + 1];
-        if (e - b > EG_BFS_BIG_DEG) {
+        if (e - b > big_deg) {
             if (lane == 0) big[atomicAdd(&cnt->nbig, 1u)] = u;
             continue;
         }
@@ -147,14 +149,16 @@ __global__ void __launch_bounds__(256) k_bfs_push(const uint32_t *__restrict__ p
     block_add_counters(cnt, my_cnt, my_deg);
 }
 
-// Expands the deferred high-degree frontier vertices: all threads of the
-// grid stride over each one's out-list in turn.
+// Expands the deferred high-degree frontier vertices: their out-lists cut
+// into chunks of `chunk` edges (as k_big_offsets counted them), one CTA per
+// chunk.
 __global__ void __launch_bounds__(256) k_bfs_push_big(const uint32_t *__restrict__ ptr,
                                                       const uint32_t *__restrict__ col,
                                                       const uint32_t *__restrict__ deg, const uint32_t *big,
                                                       const uint32_t *__restrict__ bigoff, uint32_t *visited,
                                                       uint32_t *next_bm, uint32_t *next_queue, int32_t *level,
-                                                      int32_t *parent, int32_t next_level, BfsCounters *cnt) {
+                                                      int32_t *parent, int32_t next_level, BfsCounters *cnt,
+                                                      uint32_t chunk) {
     const uint32_t nbig = *(volatile uint32_t *)&cnt->nbig;
     uint32_t my_cnt = 0;
     unsigned long long my_deg = 0;
@@ -162,7 +166,7 @@ __global__ void __launch_bounds__(256) k_bfs_push_big(const uint32_t *__restrict
     for (uint32_t c = blockIdx.x; c < total; c += gridDim.x) {
         const uint32_t i = eg_big_item(bigoff, nbig, c);
         const uint32_t u = big[i];
-        const uint32_t b = ptr[u] + (c - bigoff[i]) * EG_BFS_CHUNK, e = min(ptr[u + 1], b + EG_BFS_CHUNK);
+        const uint32_t b = ptr[u] + (c - bigoff[i]) * chunk, e = min(ptr[u + 1], b + chunk);
         // warp-uniform trip count: each warp covers 32 consecutive entries
         for (uint32_t p0 = b + (threadIdx.x & ~31u); p0 < e; p0 += blockDim.x) {
             const uint32_t p = p0 + (threadIdx.x & 31);
@@ -693,17 +697,29 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
                 EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(BfsCounters), ctx->stream));
             }
             EG_CUDA(cudaMemsetAsync(bm[nxt], 0, (uint64_t)nw * 4, ctx->stream));
+            // A frontier with fewer vertices than a full grid has warps (the
+            // first levels: a root and its hubs' neighbours) would leave most
+            // SMs idle behind the warps walking long lists: there every list
+            // over EG_BFS_SMALL_BIG edges goes to the chunked kernel, with
+            // chunks sized to spread the level's edges over the grid.
+            const uint32_t grid_ctas = (uint32_t)ctx->sm_count * 8;
+            uint32_t big_deg = EG_BFS_BIG_DEG, chunk = EG_BFS_CHUNK;
+            if ((uint64_t)qlen < (uint64_t)grid_ctas * 8) {
+                big_deg = EG_BFS_SMALL_BIG;
+                const uint64_t per = (fdeg / grid_ctas + 255) & ~255ull;
+                chunk = (uint32_t)(per < 256 ? 256 : (per > EG_BFS_CHUNK ? EG_BFS_CHUNK : per));
+            }
             k_bfs_push<<<blocks_for(ctx, (uint64_t)qlen * 32), 256, 0, ctx->stream>>>(
                 bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, q[cur], qlen, visited, bm[nxt], q[nxt], level,
-                parent, lvl + 1, cnt, big);
+                parent, lvl + 1, cnt, big, big_deg);
             EG_LAUNCHED(ctx);
-            if (fdeg > EG_BFS_BIG_DEG) {  // a frontier vertex may exceed the threshold
-                k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, 1u, bp<uint32_t>(g->csr.ptr), EG_BFS_CHUNK,
+            if (fdeg > big_deg) {  // a frontier vertex may exceed the threshold
+                k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, 1u, bp<uint32_t>(g->csr.ptr), chunk,
                                                            bigoff);
                 EG_LAUNCHED(ctx);
-                k_bfs_push_big<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
-                    bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, big, bigoff, visited, bm[nxt], q[nxt],
-                    level, parent, lvl + 1, cnt);
+                k_bfs_push_big<<<grid_ctas, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col),
+                                                                   deg, big, bigoff, visited, bm[nxt], q[nxt], level,
+                                                                   parent, lvl + 1, cnt, chunk);
                 EG_LAUNCHED(ctx);
             }
             have_queue = true;
