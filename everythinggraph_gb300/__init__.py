@@ -33,6 +33,40 @@ def lib():
     return L.load()
 
 
+class _PinnedOwner:
+    """Frees one eg_host_alloc block when the last array over it goes."""
+
+    def __init__(self, p):
+        self.p = p
+
+    def __del__(self):
+        try:
+            lib().eg_host_free(ctypes.c_void_p(self.p))
+        except Exception:
+            pass
+
+
+def pinned_empty(shape, dtype):
+    """Uninitialised numpy array in page-locked host memory (eg_host_alloc):
+    the *_out copies of the graph calls land in it at the full host-link rate.
+    Reuse it across calls; it is freed with the last array that views it."""
+    dt = np.dtype(dtype)
+    count = int(np.prod(shape))
+    nbytes = max(count * dt.itemsize, 1)
+    p = ctypes.c_void_p()
+    L.check(lib().eg_host_alloc(nbytes, ctypes.byref(p)))
+    buf = (ctypes.c_char * nbytes).from_address(p.value)
+    buf._eg_owner = _PinnedOwner(p.value)
+    return np.frombuffer(buf, dtype=dt, count=count).reshape(shape)
+
+
+def _out(a, n, dtype, name):
+    """A caller-supplied output array: n elements of dtype, C-contiguous."""
+    if a.dtype != np.dtype(dtype) or a.size != n or not a.flags["C_CONTIGUOUS"] or not a.flags["WRITEABLE"]:
+        raise ValueError("%s must be a writeable C-contiguous %s array of %d elements" % (name, np.dtype(dtype), n))
+    return a
+
+
 def weights(rule="ref", seed=0, lo=1, hi=255):
     """SSSP weight rule: "ref" (src%10+dst%10), "hash" (u32 in [lo, hi]),
     "unit", or "f32" (fp32 in (0, 1]; distances come back as float32)."""
@@ -227,15 +261,22 @@ class Graph:
         L.check(lib().eg_spmv(self._h, ctypes.byref(o), _ptr(x), _ptr(y), ctypes.byref(ms)))
         return y, ms.value
 
-    def bfs(self, root, direction="auto", switch_divisor=20.0, parents=False, copy_out=True, host_loop=None):
+    def bfs(self, root, direction="auto", switch_divisor=20.0, parents=False, copy_out=True, host_loop=None,
+            level_out=None, parent_out=None):
         """host_loop: None = the form eg_graph_tune kept (else the CUDA graph),
-        False = CUDA-graph level loop, True = host-driven level loop."""
+        False = CUDA-graph level loop, True = host-driven level loop.
+        level_out / parent_out: int32 arrays of n elements to fill (e.g. from
+        pinned_empty) instead of new ones."""
         hl = -1 if host_loop is None else int(bool(host_loop))
         o = L.BfsOpts({"auto": L.EG_BFS_AUTO, "push": L.EG_BFS_PUSH_ONLY, "pull": L.EG_BFS_PULL_ONLY}[direction],
                       switch_divisor, int(parents), hl)
         n = self.n
-        lv = np.empty(n, dtype=np.int32) if copy_out else None
-        par = np.empty(n, dtype=np.int32) if (parents and copy_out) else None
+        lv = par = None
+        if copy_out:
+            lv = _out(level_out, n, np.int32, "level_out") if level_out is not None else np.empty(n, dtype=np.int32)
+            if parents:
+                par = (_out(parent_out, n, np.int32, "parent_out") if parent_out is not None
+                       else np.empty(n, dtype=np.int32))
         st = L.BfsStats()
         L.check(lib().eg_bfs(self._h, root, ctypes.byref(o), _ptr(lv), _ptr(par), ctypes.byref(st)))
         return (lv, par, st) if parents else (lv, st)
@@ -295,8 +336,11 @@ class Graph:
         L.check(lib().eg_ppr(self._h, _ptr(seeds), len(seeds), ctypes.byref(o), _ptr(out), ctypes.byref(st)))
         return out, st
 
-    def wcc(self, copy_out=True):
-        out = np.empty(self.n, dtype=np.int64) if copy_out else None
+    def wcc(self, copy_out=True, out=None):
+        if copy_out:
+            out = _out(out, self.n, np.int64, "out") if out is not None else np.empty(self.n, dtype=np.int64)
+        else:
+            out = None
         st = L.WccStats()
         L.check(lib().eg_wcc(self._h, _ptr(out), ctypes.byref(st)))
         return out, st

@@ -108,6 +108,8 @@ SIGNATURES = {
     "eg_version": (c_char_p, []),
     "eg_open": (c_int, [c_int, c_u64, P(c_void_p)]),
     "eg_close": (c_int, [c_void_p]),
+    "eg_host_alloc": (c_int, [c_u64, P(c_void_p)]),
+    "eg_host_free": (c_int, [c_void_p]),
     "eg_stream": (c_void_p, [c_void_p]),
     "eg_sync": (c_int, [c_void_p]),
     "eg_bytes_in_use": (c_u64, [c_void_p]),

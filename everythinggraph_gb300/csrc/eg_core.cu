@@ -48,6 +48,25 @@ extern "C" int eg_open(int device, uint64_t hbm_budget_bytes, eg_ctx **out) {
     return EG_OK;
 }
 
+extern "C" int eg_host_alloc(uint64_t bytes, void **out) {
+    if (!out) return eg_fail(EG_EINVAL, "NULL argument");
+    *out = nullptr;
+    if (bytes == 0) return EG_OK;
+    const cudaError_t e = cudaHostAlloc(out, bytes, cudaHostAllocPortable);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        *out = nullptr;
+        return eg_fail(EG_ENOMEM, "cudaHostAlloc(%llu): %s", (unsigned long long)bytes, cudaGetErrorString(e));
+    }
+    return EG_OK;
+}
+
+extern "C" int eg_host_free(void *p) {
+    if (!p) return EG_OK;
+    EG_CUDA(cudaFreeHost(p));
+    return EG_OK;
+}
+
 extern "C" int eg_close(eg_ctx *c) {
     if (!c) return EG_OK;
     if (c->live_graphs > 0) return eg_fail(EG_EINVAL, "eg_close: %d graphs are still open", c->live_graphs);

@@ -57,6 +57,13 @@ uint64_t eg_bytes_in_use(eg_ctx *ctx);
 /* Number of kernels this context has launched so far. */
 uint64_t eg_kernel_launches(eg_ctx *ctx);
 
+/* Page-locked host memory for the *_out buffers of the calls below: a
+ * device-to-host copy into it runs at the full host-link rate (NVLink-C2C on
+ * GB300) instead of being staged through the driver.  Freed by eg_host_free;
+ * independent of any context. */
+int eg_host_alloc(uint64_t bytes, void **out);
+int eg_host_free(void *p);
+
 /* ---- graph input (replaces init(): init_all.c:791-893) ----------------- */
 #define EG_UNDIRECTED 1u /* -u: append reversed copies of every edge
                             (init_all.c:171-175), doubling m (init_all.c:636) */

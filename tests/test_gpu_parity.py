@@ -277,6 +277,25 @@ def test_bfs_levels_bit_exact(case):
     assert st.reached == int((lvu > 0).sum())
 
 
+def test_outputs_into_pinned_buffers(case):
+    # caller-supplied page-locked outputs, reused across calls, hold the same
+    # results as freshly allocated ones
+    import everythinggraph_gb300 as eg
+    name, n, pairs, rec, g, gu, adj, adju = case
+    lv_h = eg.pinned_empty(n, np.int32)
+    par_h = eg.pinned_empty(n, np.int32)
+    lab_h = eg.pinned_empty(n, np.int64)
+    for r in rec["roots"][:2]:
+        lv, par, st = g.bfs(int(r), parents=True, level_out=lv_h, parent_out=par_h)
+        assert lv is lv_h and par is par_h
+        np.testing.assert_array_equal(lv_h.astype(np.uint32), rec["bfsgrid_m0_p%d" % r])
+        assert oracle.bfs_tree_ok(n, adj.out_ptr, adj.out_col, int(r), lv_h, par_h)
+    lab, _ = g.wcc(out=lab_h)
+    np.testing.assert_array_equal(lab_h, g.wcc()[0])
+    with pytest.raises(ValueError):
+        g.bfs(0, level_out=np.empty(n, dtype=np.int64))
+
+
 def test_bfs_multi_matches_single(case):
     name, n, pairs, rec, g, gu, adj, adju = case
     od = adju.out_deg()
