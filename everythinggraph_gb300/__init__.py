@@ -281,6 +281,27 @@ class Graph:
         L.check(lib().eg_bfs(self._h, root, ctypes.byref(o), _ptr(lv), _ptr(par), ctypes.byref(st)))
         return (lv, par, st) if parents else (lv, st)
 
+    def bfs_batch(self, roots, direction="auto", switch_divisor=20.0, parents=False, host_loop=None,
+                  level_out=None, parent_out=None):
+        """eg_bfs from each root in turn with the copies of one root overlapped
+        with the next traversal; returns (levels[k, n], parents[k, n] or None,
+        [BfsStats] * k).  level_out / parent_out: int32 arrays of k * n
+        elements to fill (pinned_empty for full-rate copies)."""
+        roots = np.ascontiguousarray(roots, dtype=np.uint32)
+        k, n = len(roots), self.n
+        hl = -1 if host_loop is None else int(bool(host_loop))
+        o = L.BfsOpts({"auto": L.EG_BFS_AUTO, "push": L.EG_BFS_PUSH_ONLY, "pull": L.EG_BFS_PULL_ONLY}[direction],
+                      switch_divisor, int(parents), hl)
+        lv = (_out(level_out, k * n, np.int32, "level_out") if level_out is not None
+              else np.empty(k * n, dtype=np.int32)).reshape(k, n)
+        par = None
+        if parents:
+            par = (_out(parent_out, k * n, np.int32, "parent_out") if parent_out is not None
+                   else np.empty(k * n, dtype=np.int32)).reshape(k, n)
+        st = (L.BfsStats * max(k, 1))()
+        L.check(lib().eg_bfs_batch(self._h, _ptr(roots), k, ctypes.byref(o), _ptr(lv), _ptr(par), st))
+        return lv, par, [st[i] for i in range(k)]
+
     def bfs_multi(self, roots, copy_out=True):
         roots = np.ascontiguousarray(roots, dtype=np.uint32)
         n = self.n

@@ -132,6 +132,7 @@ SIGNATURES = {
     "eg_spmv": (c_int, [c_void_p, P(SpmvOpts), c_void_p, c_void_p, P(c_f32)]),
     "eg_bfs_opts_default": (None, [P(BfsOpts)]),
     "eg_bfs": (c_int, [c_void_p, c_u32, P(BfsOpts), c_void_p, c_void_p, P(BfsStats)]),
+    "eg_bfs_batch": (c_int, [c_void_p, c_void_p, c_u32, P(BfsOpts), c_void_p, c_void_p, c_void_p]),
     "eg_bfs_multi": (c_int, [c_void_p, c_void_p, c_int, c_void_p, P(BfsStats)]),
     "eg_sssp": (c_int, [c_void_p, c_u32, P(Weights), c_void_p, P(SsspStats)]),
     "eg_sssp_multi": (c_int, [c_void_p, c_void_p, c_int, P(Weights), c_void_p, P(SsspStats)]),

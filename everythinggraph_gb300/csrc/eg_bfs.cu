@@ -583,15 +583,22 @@ static int bfs_graph_build(eg_graph *g, eg_bfs_graph &bg, const void *const key[
     return EG_OK;
 }
 
-extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32_t *level_out, int32_t *parent_out,
-                      eg_bfs_stats *stats) {
+static int bfs_check(eg_graph *g, const eg_bfs_opts *opts, eg_bfs_opts &o) {
     if (!g) return eg_fail(EG_EINVAL, "NULL graph");
-    if (root >= g->n) return eg_fail(EG_EINVAL, "root %u >= n %u", root, g->n);
     if (!(g->built & EG_LAYOUT_CSR)) return eg_fail(EG_ENOTBUILT, "BFS needs the CSR");
-    eg_bfs_opts o;
     if (opts) o = *opts;
     else eg_bfs_opts_default(&o);
     if (o.direction < EG_BFS_AUTO || o.direction > EG_BFS_PULL_ONLY) return eg_fail(EG_EINVAL, "bad direction");
+    return EG_OK;
+}
+
+// One BFS from `root` into the device arrays of output slot `slot` (g->level
+// / g->parent, or g->level2 / g->parent2), on the context stream.  When
+// level_out / parent_out are given, the copies to them are queued before the
+// final wait; returns once the traversal (and those copies) are done.
+static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, bool want_parent, int32_t *level_out,
+                    int32_t *parent_out, eg_bfs_stats *stats) {
+    if (root >= g->n) return eg_fail(EG_EINVAL, "root %u >= n %u", root, g->n);
     const bool undirected = (g->flags & EG_UNDIRECTED) != 0;
     // in-lists: the CSC when built (sorted by source id, so RMAT hubs come first
     // and bottom-up scans stop early); an undirected CSR is its own transpose
@@ -602,9 +609,9 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
     EG_CUDA(cudaSetDevice(ctx->device));
     const uint32_t n = g->n;
     const uint32_t nw = (n + 31) >> 5;
-    const bool want_parent = parent_out != nullptr || o.device_parents;
-    EG_TRY(eg_buf_ensure(ctx, g->level, (uint64_t)n * 4));
-    if (want_parent) EG_TRY(eg_buf_ensure(ctx, g->parent, (uint64_t)n * 4));
+    eg_buf &lbuf = slot ? g->level2 : g->level, &pbuf = slot ? g->parent2 : g->parent;
+    EG_TRY(eg_buf_ensure(ctx, lbuf, (uint64_t)n * 4));
+    if (want_parent) EG_TRY(eg_buf_ensure(ctx, pbuf, (uint64_t)n * 4));
     // work: visited | bm0 | bm1 | queue0 | queue1 | big list | counters | graph state
     const uint64_t off_bm0 = (uint64_t)nw, off_bm1 = 2ull * nw, off_q0 = 3ull * nw, off_q1 = off_q0 + n,
                    off_big = off_q1 + n, off_bigoff = off_big + n, off_cnt = (off_bigoff + n + 1 + 7) & ~7ull,
@@ -615,14 +622,14 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
     uint32_t *big = wk + off_big, *bigoff = wk + off_bigoff;
     BfsCounters *cnt = reinterpret_cast<BfsCounters *>(wk + off_cnt);
     BfsGState *gst = reinterpret_cast<BfsGState *>(wk + off_st);
-    int32_t *level = bp<int32_t>(g->level);
-    int32_t *parent = want_parent ? bp<int32_t>(g->parent) : nullptr;
+    int32_t *level = bp<int32_t>(lbuf);
+    int32_t *parent = want_parent ? bp<int32_t>(pbuf) : nullptr;
     const uint32_t *deg = bp<uint32_t>(g->out_deg);
     const double threshold = o.switch_divisor > 0 ? (double)g->m / o.switch_divisor : 0.0;
 
     const bool host_loop = o.host_loop < 0 ? g->bfs_host_loop != 0 : o.host_loop != 0;
     if (!host_loop) {
-        eg_bfs_graph &bg = g->bfsg[want_parent ? 1 : 0];
+        eg_bfs_graph &bg = g->bfsg[slot * 2 + (want_parent ? 1 : 0)];
         const void *key[8] = {wk, level, parent, deg, g->csr.col.p, in_adj ? in_adj->col.p : nullptr, g->csr.ptr.p,
                               (const void *)(uintptr_t)ctx->stream};
         bool fresh = bg.exec != nullptr;
@@ -645,7 +652,7 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
         if (parent_out)
             EG_CUDA(cudaMemcpyAsync(parent_out, parent, (uint64_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream));
         BfsGState *hs = h + 1;
-        EG_CUDA(cudaMemcpyAsync(hs, gst, sizeof(BfsGState), cudaMemcpyDeviceToHost, ctx->stream));
+        EG_TRY(eg_readback(ctx, hs, gst, sizeof(BfsGState), ctx->stream));
         EG_CUDA(cudaStreamSynchronize(ctx->stream));
         if (hs->err) return eg_fail(EG_ETIMEOUT, "BFS did not terminate");
         if (stats) {
@@ -665,7 +672,7 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
     EG_LAUNCHED(ctx);
     uint32_t count = 1, qlen = 1;
     unsigned long long fdeg = 0;
-    EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(BfsCounters), cudaMemcpyDeviceToHost, ctx->stream));
+    EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream));
     EG_CUDA(cudaStreamSynchronize(ctx->stream));
     fdeg = h->next_deg;
     int cur = 0;
@@ -679,7 +686,7 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
         else if (o.direction == EG_BFS_PULL_ONLY) pull = true;
         else pull = (double)count + (double)fdeg > threshold;
         const int nxt = cur ^ 1;
-        EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(BfsCounters), ctx->stream));
+        EG_TRY(eg_zero(ctx, cnt, sizeof(BfsCounters), ctx->stream));
         if (pull) {
             k_bfs_pull<<<blocks_for(ctx, (uint64_t)nw * 32), 256, 0, ctx->stream>>>(
                 bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col), deg, n, bm[cur], visited, bm[nxt], level, parent,
@@ -691,12 +698,12 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
             if (!have_queue) {
                 k_bm_to_queue<<<blocks_for(ctx, (uint64_t)nw * 32), 256, 0, ctx->stream>>>(bm[cur], n, q[cur], cnt);
                 EG_LAUNCHED(ctx);
-                EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(BfsCounters), cudaMemcpyDeviceToHost, ctx->stream));
+                EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream));
                 EG_CUDA(cudaStreamSynchronize(ctx->stream));
                 qlen = h->qsize;
-                EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(BfsCounters), ctx->stream));
+                EG_TRY(eg_zero(ctx, cnt, sizeof(BfsCounters), ctx->stream));
             }
-            EG_CUDA(cudaMemsetAsync(bm[nxt], 0, (uint64_t)nw * 4, ctx->stream));
+            EG_TRY(eg_zero(ctx, bm[nxt], (uint64_t)nw * 4, ctx->stream));
             // A frontier with fewer vertices than a full grid has warps (the
             // first levels: a root and its hubs' neighbours) would leave most
             // SMs idle behind the warps walking long lists: there every list
@@ -724,7 +731,7 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
             }
             have_queue = true;
         }
-        EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(BfsCounters), cudaMemcpyDeviceToHost, ctx->stream));
+        EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream));
         EG_CUDA(cudaStreamSynchronize(ctx->stream));
         count = h->next_count;
         fdeg = h->next_deg;
@@ -747,6 +754,52 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
         EG_CUDA(cudaEventElapsedTime(&stats->ms, ctx->ev0, ctx->ev1));
     }
     return EG_OK;
+}
+
+extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32_t *level_out, int32_t *parent_out,
+                      eg_bfs_stats *stats) {
+    eg_bfs_opts o;
+    EG_TRY(bfs_check(g, opts, o));
+    EG_CUDA(cudaSetDevice(g->ctx->device));
+    return bfs_core(g, root, o, 0, parent_out != nullptr || o.device_parents, level_out, parent_out, stats);
+}
+
+// BFS from each root in turn; root i's levels (and parents) go to
+// level_out + i * n (parent_out + i * n).  The copies of root i run on the
+// copy stream while root i + 1 is traversed into the other output slot.
+extern "C" int eg_bfs_batch(eg_graph *g, const uint32_t *roots, uint32_t k, const eg_bfs_opts *opts,
+                            int32_t *level_out, int32_t *parent_out, eg_bfs_stats *stats) {
+    eg_bfs_opts o;
+    EG_TRY(bfs_check(g, opts, o));
+    if (!roots && k) return eg_fail(EG_EINVAL, "NULL roots");
+    for (uint32_t i = 0; i < k; i++)
+        if (roots[i] >= g->n) return eg_fail(EG_EINVAL, "root %u >= n %u", roots[i], g->n);
+    eg_ctx *ctx = g->ctx;
+    EG_CUDA(cudaSetDevice(ctx->device));
+    const uint64_t n = g->n;
+    const bool want_parent = parent_out != nullptr || o.device_parents;
+    int rc = EG_OK;
+    for (uint32_t i = 0; i < k && rc == EG_OK; i++) {
+        const int slot = (int)(i & 1);
+        // the slot's arrays are rewritten only after their previous copy-out
+        if (i >= 2) EG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_out[2 + slot], 0));
+        rc = bfs_core(g, roots[i], o, slot, want_parent, nullptr, nullptr, stats ? stats + i : nullptr);
+        if (rc != EG_OK) break;
+        if (level_out || parent_out) {
+            const int32_t *level = bp<int32_t>(slot ? g->level2 : g->level);
+            const int32_t *parent = want_parent ? bp<int32_t>(slot ? g->parent2 : g->parent) : nullptr;
+            EG_CUDA(cudaEventRecord(ctx->ev_out[slot], ctx->stream));
+            EG_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_out[slot], 0));
+            if (level_out)
+                EG_CUDA(cudaMemcpyAsync(level_out + i * n, level, n * 4, cudaMemcpyDeviceToHost, ctx->copy_stream));
+            if (parent_out)
+                EG_CUDA(cudaMemcpyAsync(parent_out + i * n, parent, n * 4, cudaMemcpyDeviceToHost, ctx->copy_stream));
+            EG_CUDA(cudaEventRecord(ctx->ev_out[2 + slot], ctx->copy_stream));
+        }
+    }
+    const cudaError_t e = cudaStreamSynchronize(ctx->copy_stream);
+    if (rc == EG_OK && e != cudaSuccess) return eg_fail(EG_ECUDA, "BFS batch copies: %s", cudaGetErrorString(e));
+    return rc;
 }
 
 // ============================================================== multi-source

@@ -41,10 +41,45 @@ extern "C" int eg_open(int device, uint64_t hbm_budget_bytes, eg_ctx **out) {
     EG_CUDA(cudaDeviceGetAttribute(&c->sm_count, cudaDevAttrMultiProcessorCount, device));
     EG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     EG_CUDA(cudaMallocHost(&c->h_pinned, 1 << 20));
+    EG_CUDA(cudaHostGetDevicePointer(&c->h_pinned_dev, c->h_pinned, 0));
     EG_CUDA(cudaEventCreate(&c->ev0));
     EG_CUDA(cudaEventCreate(&c->ev1));
     for (cudaEvent_t &e : c->evk) EG_CUDA(cudaEventCreate(&e));
+    EG_CUDA(cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+    for (cudaEvent_t &e : c->ev_out) EG_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     *out = c;
+    return EG_OK;
+}
+
+namespace {
+__global__ void k_readback(const uint32_t *__restrict__ src, uint32_t *dst, uint32_t words) {
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+}
+__global__ void k_zero(uint32_t *p, uint64_t words) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < words; i += (uint64_t)gridDim.x * blockDim.x)
+        p[i] = 0u;
+}
+}  // namespace
+
+int eg_zero(eg_ctx *c, void *dev, uint64_t bytes, cudaStream_t st) {
+    if ((bytes & 3) || ((uintptr_t)dev & 3)) return eg_fail(EG_EINVAL, "eg_zero: unaligned");
+    const uint64_t words = bytes / 4;
+    if (!words) return EG_OK;
+    uint64_t blocks = (words + 255) / 256;
+    if (blocks > (uint64_t)c->sm_count * 8) blocks = (uint64_t)c->sm_count * 8;
+    k_zero<<<(uint32_t)blocks, 256, 0, st>>>(static_cast<uint32_t *>(dev), words);
+    EG_LAUNCHED(c);
+    return EG_OK;
+}
+
+int eg_readback(eg_ctx *c, void *host_dst, const void *dev_src, uint32_t bytes, cudaStream_t st) {
+    const uintptr_t off = (uintptr_t)host_dst - (uintptr_t)c->h_pinned;
+    if ((uintptr_t)host_dst < (uintptr_t)c->h_pinned || off + bytes > (1u << 20) || (off & 3) || ((uintptr_t)dev_src & 3))
+        return eg_fail(EG_EINVAL, "readback outside the pinned staging area");
+    k_readback<<<1, 32, 0, st>>>(static_cast<const uint32_t *>(dev_src),
+                                 reinterpret_cast<uint32_t *>(static_cast<char *>(c->h_pinned_dev) + off),
+                                 (bytes + 3) / 4);
+    EG_LAUNCHED(c);
     return EG_OK;
 }
 
@@ -72,10 +107,13 @@ extern "C" int eg_close(eg_ctx *c) {
     if (c->live_graphs > 0) return eg_fail(EG_EINVAL, "eg_close: %d graphs are still open", c->live_graphs);
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
+    cudaStreamSynchronize(c->copy_stream);
     cudaEventDestroy(c->ev0);
     cudaEventDestroy(c->ev1);
     for (cudaEvent_t e : c->evk) cudaEventDestroy(e);
+    for (cudaEvent_t e : c->ev_out) cudaEventDestroy(e);
     cudaFreeHost(c->h_pinned);
+    cudaStreamDestroy(c->copy_stream);
     cudaStreamDestroy(c->stream);
     delete c;
     return EG_OK;
@@ -310,6 +348,7 @@ extern "C" void eg_graph_free(eg_graph *g) {
                       &g->out_deg,      &g->in_deg,      &g->cell_ptr,       &g->gsrc,         &g->gdst,
                       &g->rank,    &g->contrib0,     &g->contrib1,
                       &g->pr_part,      &g->pr_stats,    &g->mp_carry,    &g->errflag,     &g->rank_p,    &g->rank_q,    &g->level,          &g->parent,       &g->dist,
+                      &g->level2,       &g->parent2,
                       &g->label,        &g->spmv_x,      &g->spmv_y,      &g->spmv_vals,      &g->bfs_work,     &g->msbfs_work,
                       &g->sssp_work,    &g->ppr_work,    &g->wts,
                       &g->grid_order,   &g->grid_units,  &g->grid_off,    &g->grid_vals,   &g->grid_acc};

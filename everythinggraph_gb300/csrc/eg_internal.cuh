@@ -44,10 +44,13 @@ struct eg_ctx {
     uint64_t budget;
     uint64_t in_use;
     uint64_t launches;
-    void *h_pinned;  // 1 MiB pinned staging for small readbacks
+    void *h_pinned;      // 1 MiB pinned staging for small readbacks
+    void *h_pinned_dev;  // the same memory as the device addresses it
     cudaEvent_t ev0, ev1;
     cudaEvent_t evk[2 * EG_KEV];  // begin/end pairs around single kernel launches
     int live_graphs;              // eg_close refuses while graphs are alive
+    cudaStream_t copy_stream;     // device-to-host copies overlapped with the next traversal
+    cudaEvent_t ev_out[4];        // [slot]: outputs ready, [2 + slot]: outputs copied out
 };
 
 int eg_dmalloc(eg_ctx *ctx, void **p, uint64_t bytes);
@@ -59,6 +62,14 @@ struct eg_buf {
     uint64_t bytes = 0;
 };
 int eg_buf_ensure(eg_ctx *ctx, eg_buf &b, uint64_t bytes);  // grows (contents lost)
+// Small device-to-host readback into ctx->h_pinned (host_dst lies in it) by a
+// one-warp kernel on `st` instead of a copy engine, so that it does not queue
+// behind large copies another stream has on the engine.  Valid on the host
+// after `st` is synchronised.
+int eg_readback(eg_ctx *ctx, void *host_dst, const void *dev_src, uint32_t bytes, cudaStream_t st);
+// Zeroes `bytes` (a multiple of 4, 4-byte aligned) of device memory with a
+// kernel, for the same reason: a memset may be carried out by a copy engine.
+int eg_zero(eg_ctx *ctx, void *dev, uint64_t bytes, cudaStream_t st);
 void eg_buf_free(eg_ctx *ctx, eg_buf &b);
 template <class T>
 static inline T *bp(const eg_buf &b) {
@@ -109,13 +120,14 @@ struct eg_graph {
     // algorithm state, allocated on first use and reused
     eg_buf rank, rank_p, rank_q, contrib0, contrib1, pr_part, pr_stats, mp_carry, errflag;
     eg_buf level, parent, dist, label, spmv_x, spmv_y, spmv_vals;
+    eg_buf level2, parent2;  // second output slot of eg_bfs_batch
     uint64_t spmv_vals_seed;
     int spmv_vals_kind;
     eg_buf bfs_work;  // bitmaps, queues, counters
     eg_buf msbfs_work;
     eg_buf sssp_work;
     eg_buf ppr_work;
-    eg_bfs_graph bfsg[2];  // without / with parents
+    eg_bfs_graph bfsg[4];  // [slot * 2 + with parents]
     eg_bfs_graph prg;      // PageRank iterations (key: options and buffers)
     eg_bfs_graph msg;      // multi-source BFS level loop
     int row_cfg = 0;       // row-kernel schedule (entries per warp tile, per lane)

@@ -262,6 +262,14 @@ typedef struct {
 void eg_bfs_opts_default(eg_bfs_opts *o);
 int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32_t *level_out, int32_t *parent_out,
            eg_bfs_stats *stats);
+/* eg_bfs from each of k roots in turn (the reference's per-root benchmark
+ * loop, bfs_simple.c's main): root i's levels go to level_out + i*n and its
+ * parents to parent_out + i*n (either may be NULL); stats, if given, holds k
+ * entries.  The copies of root i run on a second stream while root i+1 is
+ * traversed, so with page-locked outputs (eg_host_alloc) they overlap the
+ * traversals. */
+int eg_bfs_batch(eg_graph *g, const uint32_t *roots, uint32_t k, const eg_bfs_opts *opts, int32_t *level_out,
+                 int32_t *parent_out, eg_bfs_stats *stats);
 
 /* Multi-source BFS, bit-sliced: up to 64 sources per 64-bit word per vertex,
  * all advanced by one level per sweep.  levels_out: k*n int32, row s holds

@@ -22,6 +22,10 @@ CASES = ["tiny", "rmat10", "rmat12", "rmat16"]
 PR_REL_L1 = 1e-6
 PR_MAX_REL = 1e-5
 PR_VS_REF32_MAX_REL = 2e-5
+# the grid-layout kernels add fp32 contributions with atomics in arbitrary
+# order and without compensation: the rel L1 bound is the same, the largest
+# single-row error (a hub row of 10^4 terms, ~sqrt(terms) * 2^-24) is looser
+GRID_MAX_REL = 5e-5
 
 
 def load(name):
@@ -210,7 +214,7 @@ def test_grid_spmv_and_pagerank(case):
     np.testing.assert_allclose(y64, ref, rtol=1e-12, atol=1e-300)
     y32, _ = g.spmv(xf, "f32", value_seed=9, grid=True)
     l1, mx = rel_errors(y32, ref)
-    assert l1 <= PR_REL_L1 and mx <= PR_MAX_REL, (l1, mx)
+    assert l1 <= PR_REL_L1 and mx <= GRID_MAX_REL, (l1, mx)
     with pytest.raises(RuntimeError):
         g.spmv(xf, "f32_comp", grid=True)
     got, st = g.pagerank(iterations=10, prev_init=0.15, swap=True, deg_multiplier=2, grid=True)
@@ -219,7 +223,7 @@ def test_grid_spmv_and_pagerank(case):
     ref = oracle.pagerank_f64(adj, adj.out_deg(), 1.0 / n, 10, dangling=True)
     got, st = g.pagerank(iterations=10, dangling=True, grid=True)
     l1, mx = rel_errors(got, ref)
-    assert l1 <= PR_REL_L1 and mx <= PR_MAX_REL, (l1, mx)
+    assert l1 <= PR_REL_L1 and mx <= GRID_MAX_REL, (l1, mx)
     got, st = g.pagerank(iterations=200, tolerance=1e-6, dangling=True, grid=True)
     assert 1 <= st.iterations_run < 200 and st.residual < 1e-6
 
@@ -292,6 +296,20 @@ def test_outputs_into_pinned_buffers(case):
         assert oracle.bfs_tree_ok(n, adj.out_ptr, adj.out_col, int(r), lv_h, par_h)
     lab, _ = g.wcc(out=lab_h)
     np.testing.assert_array_equal(lab_h, g.wcc()[0])
+    # batched roots: copies of one root overlap the next traversal, results
+    # equal root-by-root BFS; both level-loop forms
+    roots = np.array(list(rec["roots"]) * 3, dtype=np.uint32)
+    k = len(roots)
+    lvb = eg.pinned_empty(k * n, np.int32)
+    pab = eg.pinned_empty(k * n, np.int32)
+    for host_loop in (False, True):
+        lvs, pas, sts = g.bfs_batch(roots, parents=True, host_loop=host_loop, level_out=lvb, parent_out=pab)
+        for i, r in enumerate(roots):
+            np.testing.assert_array_equal(lvs[i].astype(np.uint32), rec["bfsgrid_m0_p%d" % r])
+            assert oracle.bfs_tree_ok(n, adj.out_ptr, adj.out_col, int(r), lvs[i], pas[i])
+            assert sts[i].reached == int((lvs[i] > 0).sum())
+    lvs, pas, sts = g.bfs_batch(roots[:3])
+    assert pas is None and lvs.shape == (3, n)
     with pytest.raises(ValueError):
         g.bfs(0, level_out=np.empty(n, dtype=np.int64))
 
