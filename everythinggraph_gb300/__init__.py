@@ -225,7 +225,8 @@ class Graph:
         cands = [{"tile": r.tile_entries[i], "per_lane": r.entries_per_lane[i], "prefetch": r.prefetch[i],
                   "min_blocks": r.min_blocks[i], "cache_hint": r.cache_hint[i],
                   "ms": r.ms[i]} for i in range(r.ncand)]
-        self.bfs_tuning = {"graph_ms": r.bfs_graph_ms, "host_ms": r.bfs_host_ms, "host_loop": r.bfs_host_loop}
+        self.bfs_tuning = {"graph_ms": r.bfs_graph_ms, "host_ms": r.bfs_host_ms, "host_loop": r.bfs_host_loop,
+                           "switch_divisor": r.bfs_switch_divisor}
         return cands, r.chosen
 
     def set_row_schedule(self, index):
@@ -261,15 +262,17 @@ class Graph:
         L.check(lib().eg_spmv(self._h, ctypes.byref(o), _ptr(x), _ptr(y), ctypes.byref(ms)))
         return y, ms.value
 
-    def bfs(self, root, direction="auto", switch_divisor=20.0, parents=False, copy_out=True, host_loop=None,
+    def bfs(self, root, direction="auto", switch_divisor=None, parents=False, copy_out=True, host_loop=None,
             level_out=None, parent_out=None):
         """host_loop: None = the form eg_graph_tune kept (else the CUDA graph),
         False = CUDA-graph level loop, True = host-driven level loop.
+        switch_divisor: None = the divisor eg_graph_tune kept (else 20, the
+        reference's).
         level_out / parent_out: int32 arrays of n elements to fill (e.g. from
         pinned_empty) instead of new ones."""
         hl = -1 if host_loop is None else int(bool(host_loop))
         o = L.BfsOpts({"auto": L.EG_BFS_AUTO, "push": L.EG_BFS_PUSH_ONLY, "pull": L.EG_BFS_PULL_ONLY}[direction],
-                      switch_divisor, int(parents), hl)
+                      -1.0 if switch_divisor is None else switch_divisor, int(parents), hl)
         n = self.n
         lv = par = None
         if copy_out:
@@ -281,7 +284,7 @@ class Graph:
         L.check(lib().eg_bfs(self._h, root, ctypes.byref(o), _ptr(lv), _ptr(par), ctypes.byref(st)))
         return (lv, par, st) if parents else (lv, st)
 
-    def bfs_batch(self, roots, direction="auto", switch_divisor=20.0, parents=False, host_loop=None,
+    def bfs_batch(self, roots, direction="auto", switch_divisor=None, parents=False, host_loop=None,
                   level_out=None, parent_out=None):
         """eg_bfs from each root in turn with the copies of one root overlapped
         with the next traversal; returns (levels[k, n], parents[k, n] or None,
@@ -291,7 +294,7 @@ class Graph:
         k, n = len(roots), self.n
         hl = -1 if host_loop is None else int(bool(host_loop))
         o = L.BfsOpts({"auto": L.EG_BFS_AUTO, "push": L.EG_BFS_PUSH_ONLY, "pull": L.EG_BFS_PULL_ONLY}[direction],
-                      switch_divisor, int(parents), hl)
+                      -1.0 if switch_divisor is None else switch_divisor, int(parents), hl)
         lv = (_out(level_out, k * n, np.int32, "level_out") if level_out is not None
               else np.empty(k * n, dtype=np.int32)).reshape(k, n)
         par = None

@@ -32,6 +32,7 @@ struct BfsCounters {
 #define EG_BFS_BIG_DEG 2048u
 #define EG_BFS_CHUNK 4096u  // edges of a deferred hub per CTA work unit
 #define EG_BFS_SMALL_BIG 64u  // the deferral threshold of levels with few frontier vertices
+#define EG_BFS_QUEUE_EDGES (1u << 18)  // push levels over more edges build no next queue
 
 // Block-level reduction of per-thread counters: one atomic per block.
 __device__ __forceinline__ void block_add_counters(BfsCounters *c, uint32_t cnt, unsigned long long deg) {
@@ -96,10 +97,20 @@ __device__ __forceinline__ bool bfs_claim(uint32_t v, uint32_t u, uint32_t *visi
     return true;
 }
 
-// Appends the claimed vertices of a warp to the next queue (one atomic per warp).
+// Appends the claimed vertices of a warp to the next queue (one atomic per
+// warp) and counts them.  next_queue NULL: count only — the next frontier is
+// the next_bm bitmap alone (a level with many claims would otherwise meet on
+// the one queue counter).
 __device__ __forceinline__ void warp_append(bool claimed, uint32_t v, uint32_t *next_queue, BfsCounters *cnt,
                                             const uint32_t *__restrict__ deg, uint32_t &my_cnt,
                                             unsigned long long &my_deg) {
+    if (!next_queue) {
+        if (claimed) {
+            my_cnt++;
+            my_deg += deg[v];
+        }
+        return;
+    }
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t ball = __ballot_sync(EG_FULL_MASK, claimed);
     if (ball) {
@@ -517,7 +528,7 @@ __global__ void k_bfsg_end(BfsGState *st, BfsCounters *cnt, cudaGraphConditional
 extern "C" void eg_bfs_opts_default(eg_bfs_opts *o) {
     if (!o) return;
     o->direction = EG_BFS_AUTO;
-    o->switch_divisor = 20.0;
+    o->switch_divisor = -1.0;
     o->device_parents = 0;
     o->host_loop = -1;
 }
@@ -625,7 +636,8 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
     int32_t *level = bp<int32_t>(lbuf);
     int32_t *parent = want_parent ? bp<int32_t>(pbuf) : nullptr;
     const uint32_t *deg = bp<uint32_t>(g->out_deg);
-    const double threshold = o.switch_divisor > 0 ? (double)g->m / o.switch_divisor : 0.0;
+    const double divisor = o.switch_divisor < 0 ? g->bfs_divisor : o.switch_divisor;
+    const double threshold = divisor > 0 ? (double)g->m / divisor : 0.0;
 
     const bool host_loop = o.host_loop < 0 ? g->bfs_host_loop != 0 : o.host_loop != 0;
     if (!host_loop) {
@@ -710,6 +722,9 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
             // over EG_BFS_SMALL_BIG edges goes to the chunked kernel, with
             // chunks sized to spread the level's edges over the grid.
             const uint32_t grid_ctas = (uint32_t)ctx->sm_count * 8;
+            // a level over many edges leaves the next frontier as a bitmap
+            // only; a push level after it rebuilds the queue (k_bm_to_queue)
+            const bool make_queue = fdeg <= EG_BFS_QUEUE_EDGES;
             uint32_t big_deg = EG_BFS_BIG_DEG, chunk = EG_BFS_CHUNK;
             if ((uint64_t)qlen < (uint64_t)grid_ctas * 8) {
                 big_deg = EG_BFS_SMALL_BIG;
@@ -717,19 +732,19 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
                 chunk = (uint32_t)(per < 256 ? 256 : (per > EG_BFS_CHUNK ? EG_BFS_CHUNK : per));
             }
             k_bfs_push<<<blocks_for(ctx, (uint64_t)qlen * 32), 256, 0, ctx->stream>>>(
-                bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, q[cur], qlen, visited, bm[nxt], q[nxt], level,
-                parent, lvl + 1, cnt, big, big_deg);
+                bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, q[cur], qlen, visited, bm[nxt],
+                make_queue ? q[nxt] : nullptr, level, parent, lvl + 1, cnt, big, big_deg);
             EG_LAUNCHED(ctx);
             if (fdeg > big_deg) {  // a frontier vertex may exceed the threshold
                 k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, 1u, bp<uint32_t>(g->csr.ptr), chunk,
                                                            bigoff);
                 EG_LAUNCHED(ctx);
-                k_bfs_push_big<<<grid_ctas, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col),
-                                                                   deg, big, bigoff, visited, bm[nxt], q[nxt], level,
-                                                                   parent, lvl + 1, cnt, chunk);
+                k_bfs_push_big<<<grid_ctas, 256, 0, ctx->stream>>>(
+                    bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, big, bigoff, visited, bm[nxt],
+                    make_queue ? q[nxt] : nullptr, level, parent, lvl + 1, cnt, chunk);
                 EG_LAUNCHED(ctx);
             }
-            have_queue = true;
+            have_queue = make_queue;
         }
         EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream));
         EG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1127,25 +1142,37 @@ extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *
     return EG_OK;
 }
 
-int eg_bfs_tune(eg_graph *g, float *ms_graph, float *ms_host, int *host_loop) {
+int eg_bfs_tune(eg_graph *g, float *ms_graph, float *ms_host, int *host_loop, double *divisor) {
+    static const double kDiv[5] = {20.0, 40.0, 80.0, 160.0, 320.0};
     uint32_t roots[4];
     EG_TRY(eg_sample_roots(g, 4, 12345, roots));
-    float t[2] = {0.f, 0.f};
+    float best[2] = {0.f, 0.f};
+    double best_div[2] = {20.0, 20.0};
     for (int form = 0; form < 2; form++) {
-        eg_bfs_opts o;
-        eg_bfs_opts_default(&o);
-        o.host_loop = form;
-        o.device_parents = 1;
-        eg_bfs_stats st;
-        EG_TRY(eg_bfs(g, roots[0], &o, nullptr, nullptr, &st));  // warm-up (graph capture, buffers)
-        for (int r = 0; r < 4; r++) {
-            EG_TRY(eg_bfs(g, roots[r], &o, nullptr, nullptr, &st));
-            t[form] += st.ms / 4.f;
+        for (int d = 0; d < 5; d++) {
+            eg_bfs_opts o;
+            eg_bfs_opts_default(&o);
+            o.host_loop = form;
+            o.switch_divisor = kDiv[d];
+            o.device_parents = 1;
+            eg_bfs_stats st;
+            EG_TRY(eg_bfs(g, roots[0], &o, nullptr, nullptr, &st));  // warm-up (graph capture, buffers)
+            float t = 0.f;
+            for (int r = 0; r < 4; r++) {
+                EG_TRY(eg_bfs(g, roots[r], &o, nullptr, nullptr, &st));
+                t += st.ms / 4.f;
+            }
+            if (d == 0 || t < best[form]) {
+                best[form] = t;
+                best_div[form] = kDiv[d];
+            }
         }
     }
-    g->bfs_host_loop = t[1] < t[0] ? 1 : 0;
-    *ms_graph = t[0];
-    *ms_host = t[1];
+    g->bfs_host_loop = best[1] < best[0] ? 1 : 0;
+    g->bfs_divisor = best_div[g->bfs_host_loop];
+    *ms_graph = best[0];
+    *ms_host = best[1];
     *host_loop = g->bfs_host_loop;
+    *divisor = g->bfs_divisor;
     return EG_OK;
 }

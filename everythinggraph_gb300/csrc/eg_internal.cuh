@@ -132,6 +132,7 @@ struct eg_graph {
     eg_bfs_graph msg;      // multi-source BFS level loop
     int row_cfg = 0;       // row-kernel schedule (entries per warp tile, per lane)
     int bfs_host_loop = 0; // BFS level-loop form eg_bfs uses by default (eg_graph_tune)
+    double bfs_divisor = 20.0;  // push/pull switch divisor eg_bfs uses by default (eg_graph_tune)
     // SSSP edge weights of the CSR entries for one rule, materialised on first
     // use (the reference stores them in its edge records, init_all.c:661-686)
     eg_buf wts;
@@ -241,7 +242,7 @@ struct eg_wrule {
 };
 struct eg_graph;
 // Times eg_bfs's two level-loop forms on a few sampled roots (eg_bfs.cu).
-int eg_bfs_tune(eg_graph *g, float *ms_graph, float *ms_host, int *host_loop);
+int eg_bfs_tune(eg_graph *g, float *ms_graph, float *ms_host, int *host_loop, double *divisor);
 // SpMV / PageRank over the 2-D grid layout (eg_grid.cu).
 int eg_grid_spmv(eg_graph *g, int kind, uint64_t value_seed, int unit_values, const void *d_x, void *d_y);
 int eg_grid_pagerank(eg_graph *g, const eg_pr_opts &o, float *rank_out, eg_pr_stats *stats);

@@ -549,7 +549,8 @@ extern "C" int eg_graph_tune(eg_graph *g, eg_tune_result *out) {
     }
     g->row_cfg = best;
     r.chosen = best;
-    if (g->built & EG_LAYOUT_CSR) EG_TRY(eg_bfs_tune(g, &r.bfs_graph_ms, &r.bfs_host_ms, &r.bfs_host_loop));
+    if (g->built & EG_LAYOUT_CSR)
+        EG_TRY(eg_bfs_tune(g, &r.bfs_graph_ms, &r.bfs_host_ms, &r.bfs_host_loop, &r.bfs_switch_divisor));
     if (out) *out = r;
     return EG_OK;
 }

@@ -192,10 +192,12 @@ typedef struct {
     int cache_hint[EG_ROW_SCHEDULES_MAX];
     float ms[EG_ROW_SCHEDULES_MAX]; /* mean row-kernel time per iteration */
     /* BFS level loop (when the graph has a CSR): mean ms per BFS over 4
-     * sampled roots for the CUDA-graph and the host-driven loop, and the
-     * form kept for eg_bfs's host_loop = -1 */
+     * sampled roots for the CUDA-graph and the host-driven loop (each at its
+     * best switch divisor of 20, 40, 80, 160, 320), and the form and the
+     * divisor kept for eg_bfs's host_loop = -1 and switch_divisor < 0 */
     float bfs_graph_ms, bfs_host_ms;
     int bfs_host_loop;
+    double bfs_switch_divisor; /* the push/pull switch divisor kept */
 } eg_tune_result;
 int eg_graph_tune(eg_graph *g, eg_tune_result *out);
 int eg_graph_set_row_schedule(eg_graph *g, int index);
@@ -240,7 +242,10 @@ int eg_spmv(eg_graph *g, const eg_spmv_opts *opts, const void *x, void *y, float
 typedef struct {
     int direction;
     /* auto switches to pull when frontier size + frontier out-degree
-     * > m / switch_divisor (the reference uses 20, bfs_simple.c:191-197) */
+     * > m / switch_divisor (the reference uses 20, bfs_simple.c:191-197).
+     * The direction changes how a level is computed, never its levels.
+     * < 0 (default): the graph's divisor, which eg_graph_tune picks by
+     * timing (20 until then) */
     double switch_divisor;
     /* 1: compute parents on the device even when parent_out is NULL (read
      * them later through eg_graph_device_ptr(g, EG_DEV_PARENT)) */

@@ -168,6 +168,7 @@ def test_row_schedules_and_autotuner(case):
     y_ref = oracle.spmv_f64(n, adj.in_ptr, adj.in_col, vals, x)
     cands, chosen = g.tune()
     assert len(cands) == 10 and 0 <= chosen < 10
+    assert g.bfs_tuning["switch_divisor"] in (20.0, 40.0, 80.0, 160.0, 320.0)
     assert sum(c["cache_hint"] for c in cands) == 2
     if n > 1000:
         assert all(c["ms"] > 0 for c in cands)
@@ -274,6 +275,12 @@ def test_bfs_levels_bit_exact(case):
                 np.testing.assert_array_equal(lv.astype(np.uint32), rec["bfsgrid_m0_p%d" % r])
                 assert oracle.bfs_tree_ok(n, adj.out_ptr, adj.out_col, int(r), lv, par)
                 assert st.reached == int((lv > 0).sum())
+    # the push/pull switch point changes how levels are computed, not them
+    r = int(rec["roots"][0])
+    for div in (2.0, 80.0, 320.0, 1e9):
+        lv, par, st = g.bfs(r, switch_divisor=div, parents=True)
+        np.testing.assert_array_equal(lv.astype(np.uint32), rec["bfsgrid_m0_p%d" % r])
+        assert oracle.bfs_tree_ok(n, adj.out_ptr, adj.out_col, r, lv, par)
     lv, st = g.bfs(0)
     np.testing.assert_array_equal(lv.astype(np.uint32), rec["bfs_simple_m8"])
     lvu, st = gu.bfs(0)
