@@ -94,7 +94,7 @@ def dist_env():
     return rank, world, local
 
 
-E2E_BATCH = 16  # roots per eg_bfs_batch call in the end-to-end step
+E2E_BATCH = 32  # roots per eg_bfs_batch call in the end-to-end step
 
 
 def run_ours(args):
@@ -220,7 +220,7 @@ def run_ours(args):
         "config": dict(W, n=n, m_adjacency=2 * m_in, l2="inputs larger than L2 (CSR 2.1 GB)",
                        parallelism="replicas" if world > 1 else "single"),
         "e2e": {"value": e_edges * world / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "host_buffers": "page-locked (eg_host_alloc), reused by every call",
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3 / args.steps, "host_buffers": "page-locked (eg_host_alloc), reused by every call",
                 "api": "eg_bfs_batch (%d roots per call, copies overlapped with the next traversal) + eg_wcc" % E2E_BATCH},
         "gpu_launches": launches,
         "load": {"build_ms": build_ms, "bfs_tuning": g.bfs_tuning},

@@ -604,7 +604,7 @@ static int bfs_check(eg_graph *g, const eg_bfs_opts *opts, eg_bfs_opts &o) {
 }
 
 // One BFS from `root` into the device arrays of output slot `slot` (g->level
-// / g->parent, or g->level2 / g->parent2), on the context stream.  When
+// / g->parent, or g->level_s / g->parent_s), on the context stream.  When
 // level_out / parent_out are given, the copies to them are queued before the
 // final wait; returns once the traversal (and those copies) are done.
 static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, bool want_parent, int32_t *level_out,
@@ -620,7 +620,7 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
     EG_CUDA(cudaSetDevice(ctx->device));
     const uint32_t n = g->n;
     const uint32_t nw = (n + 31) >> 5;
-    eg_buf &lbuf = slot ? g->level2 : g->level, &pbuf = slot ? g->parent2 : g->parent;
+    eg_buf &lbuf = slot ? g->level_s[slot - 1] : g->level, &pbuf = slot ? g->parent_s[slot - 1] : g->parent;
     EG_TRY(eg_buf_ensure(ctx, lbuf, (uint64_t)n * 4));
     if (want_parent) EG_TRY(eg_buf_ensure(ctx, pbuf, (uint64_t)n * 4));
     // work: visited | bm0 | bm1 | queue0 | queue1 | big list | counters | graph state
@@ -780,8 +780,10 @@ extern "C" int eg_bfs(eg_graph *g, uint32_t root, const eg_bfs_opts *opts, int32
 }
 
 // BFS from each root in turn; root i's levels (and parents) go to
-// level_out + i * n (parent_out + i * n).  The copies of root i run on the
-// copy stream while root i + 1 is traversed into the other output slot.
+// level_out + i * n (parent_out + i * n).  Root i is traversed into output
+// slot i % EG_OUT_SLOTS and copied out on the copy stream while the next
+// roots are traversed into the other slots; a slot is rewritten only after
+// its previous copy-out.
 extern "C" int eg_bfs_batch(eg_graph *g, const uint32_t *roots, uint32_t k, const eg_bfs_opts *opts,
                             int32_t *level_out, int32_t *parent_out, eg_bfs_stats *stats) {
     eg_bfs_opts o;
@@ -795,21 +797,20 @@ extern "C" int eg_bfs_batch(eg_graph *g, const uint32_t *roots, uint32_t k, cons
     const bool want_parent = parent_out != nullptr || o.device_parents;
     int rc = EG_OK;
     for (uint32_t i = 0; i < k && rc == EG_OK; i++) {
-        const int slot = (int)(i & 1);
-        // the slot's arrays are rewritten only after their previous copy-out
-        if (i >= 2) EG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_out[2 + slot], 0));
+        const int slot = (int)(i % EG_OUT_SLOTS);
+        if (i >= EG_OUT_SLOTS) EG_CUDA(cudaStreamWaitEvent(ctx->stream, ctx->ev_out[EG_OUT_SLOTS + slot], 0));
         rc = bfs_core(g, roots[i], o, slot, want_parent, nullptr, nullptr, stats ? stats + i : nullptr);
         if (rc != EG_OK) break;
         if (level_out || parent_out) {
-            const int32_t *level = bp<int32_t>(slot ? g->level2 : g->level);
-            const int32_t *parent = want_parent ? bp<int32_t>(slot ? g->parent2 : g->parent) : nullptr;
+            const int32_t *level = bp<int32_t>(slot ? g->level_s[slot - 1] : g->level);
+            const int32_t *parent = want_parent ? bp<int32_t>(slot ? g->parent_s[slot - 1] : g->parent) : nullptr;
             EG_CUDA(cudaEventRecord(ctx->ev_out[slot], ctx->stream));
             EG_CUDA(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_out[slot], 0));
             if (level_out)
                 EG_CUDA(cudaMemcpyAsync(level_out + i * n, level, n * 4, cudaMemcpyDeviceToHost, ctx->copy_stream));
             if (parent_out)
                 EG_CUDA(cudaMemcpyAsync(parent_out + i * n, parent, n * 4, cudaMemcpyDeviceToHost, ctx->copy_stream));
-            EG_CUDA(cudaEventRecord(ctx->ev_out[2 + slot], ctx->copy_stream));
+            EG_CUDA(cudaEventRecord(ctx->ev_out[EG_OUT_SLOTS + slot], ctx->copy_stream));
         }
     }
     const cudaError_t e = cudaStreamSynchronize(ctx->copy_stream);

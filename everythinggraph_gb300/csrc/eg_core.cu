@@ -348,7 +348,8 @@ extern "C" void eg_graph_free(eg_graph *g) {
                       &g->out_deg,      &g->in_deg,      &g->cell_ptr,       &g->gsrc,         &g->gdst,
                       &g->rank,    &g->contrib0,     &g->contrib1,
                       &g->pr_part,      &g->pr_stats,    &g->mp_carry,    &g->errflag,     &g->rank_p,    &g->rank_q,    &g->level,          &g->parent,       &g->dist,
-                      &g->level2,       &g->parent2,
+                      &g->level_s[0],   &g->level_s[1],  &g->level_s[2],  &g->parent_s[0], &g->parent_s[1],
+                      &g->parent_s[2],
                       &g->label,        &g->spmv_x,      &g->spmv_y,      &g->spmv_vals,      &g->bfs_work,     &g->msbfs_work,
                       &g->sssp_work,    &g->ppr_work,    &g->wts,
                       &g->grid_order,   &g->grid_units,  &g->grid_off,    &g->grid_vals,   &g->grid_acc};

@@ -36,7 +36,8 @@ void eg_clear_error();
     } while (0)
 
 // ---------------------------------------------------------------- context
-#define EG_KEV 8  // kernel launches timed individually per call
+#define EG_KEV 8        // kernel launches timed individually per call
+#define EG_OUT_SLOTS 4  // device output slots of eg_bfs_batch (copy-out pipeline depth)
 struct eg_ctx {
     int device;
     int sm_count;
@@ -50,7 +51,7 @@ struct eg_ctx {
     cudaEvent_t evk[2 * EG_KEV];  // begin/end pairs around single kernel launches
     int live_graphs;              // eg_close refuses while graphs are alive
     cudaStream_t copy_stream;     // device-to-host copies overlapped with the next traversal
-    cudaEvent_t ev_out[4];        // [slot]: outputs ready, [2 + slot]: outputs copied out
+    cudaEvent_t ev_out[2 * EG_OUT_SLOTS];  // [slot]: outputs ready, [EG_OUT_SLOTS + slot]: copied out
 };
 
 int eg_dmalloc(eg_ctx *ctx, void **p, uint64_t bytes);
@@ -120,14 +121,14 @@ struct eg_graph {
     // algorithm state, allocated on first use and reused
     eg_buf rank, rank_p, rank_q, contrib0, contrib1, pr_part, pr_stats, mp_carry, errflag;
     eg_buf level, parent, dist, label, spmv_x, spmv_y, spmv_vals;
-    eg_buf level2, parent2;  // second output slot of eg_bfs_batch
+    eg_buf level_s[EG_OUT_SLOTS - 1], parent_s[EG_OUT_SLOTS - 1];  // output slots 1.. of eg_bfs_batch
     uint64_t spmv_vals_seed;
     int spmv_vals_kind;
     eg_buf bfs_work;  // bitmaps, queues, counters
     eg_buf msbfs_work;
     eg_buf sssp_work;
     eg_buf ppr_work;
-    eg_bfs_graph bfsg[4];  // [slot * 2 + with parents]
+    eg_bfs_graph bfsg[2 * EG_OUT_SLOTS];  // [slot * 2 + with parents]
     eg_bfs_graph prg;      // PageRank iterations (key: options and buffers)
     eg_bfs_graph msg;      // multi-source BFS level loop
     int row_cfg = 0;       // row-kernel schedule (entries per warp tile, per lane)
