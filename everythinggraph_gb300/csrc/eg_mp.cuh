@@ -471,7 +471,7 @@ __device__ __forceinline__ void eg_coov_reduce(const eg_red2 &redf, double2 *s_r
 
 // One warp tile t of the row-id stream (the body of k_coov_rows);
 // `gather(e, u)` returns the value of entry e, source u.
-template <class Op, int TILE_E, int U, bool REDUCE, bool PF, int HINT, class G>
+template <class Op, int TILE_E, int U, bool REDUCE, int PF, int HINT, class G>
 __device__ __forceinline__ void eg_coov_tile(uint32_t t, const uint32_t *__restrict__ rid,
                                              const uint32_t *__restrict__ col, uint32_t m,
                                              eg_mp_carry<typename Op::A> *__restrict__ carry, const Op &op,
@@ -499,24 +499,52 @@ __device__ __forceinline__ void eg_coov_tile(uint32_t t, const uint32_t *__restr
         const float2 d = op.emit(row, val);
         if (REDUCE) redf.add(d);
     };
-    uint32_t rn[U], un[U];  // prefetched next chunk (PF)
+    uint32_t rn[U], un[U];  // prefetched next chunk (PF >= 1)
+    uint32_t rg[U];         // PF 2: rows of the chunk whose gathers are in flight
+    V vg[U];                // PF 2: its gathered values
     if (PF) eg_coov_load<U, HINT>(rid, col, E0, E1, lane, rn, un, pol);
+    if constexpr (PF == 2) {  // prologue: the first chunk's gathers, the second chunk's words
+#pragma unroll
+        for (int k = 0; k < U; k++) {
+            rg[k] = rn[k];
+            vg[k] = rn[k] != EG_MP_NONE ? gather(E0 + U * lane + k, un[k]) : V();
+        }
+        if (E0 + CH < E1) eg_coov_load<U, HINT>(rid, col, E0 + CH, E1, lane, rn, un, pol);
+    }
     for (uint32_t base = E0; base < E1; base += CH) {
         const uint32_t e = base + U * lane;
         uint32_t r[U], u[U];
-        if (PF) {
+        V v[U];
+        if constexpr (PF == 2) {
+            // this chunk's values arrived during the previous chunk's scan;
+            // issue the next chunk's gathers and load the one after, then scan
 #pragma unroll
             for (int k = 0; k < U; k++) {
-                r[k] = rn[k];
-                u[k] = un[k];
+                r[k] = rg[k];
+                v[k] = vg[k];
             }
-            if (base + CH < E1) eg_coov_load<U, HINT>(rid, col, base + CH, E1, lane, rn, un, pol);
-        } else {
-            eg_coov_load<U, HINT>(rid, col, base, E1, lane, r, u, pol);
-        }
-        V v[U];
+            if (base + CH < E1) {
 #pragma unroll
-        for (int k = 0; k < U; k++) v[k] = r[k] != EG_MP_NONE ? gather(e + k, u[k]) : V();
+                for (int k = 0; k < U; k++) {
+                    rg[k] = rn[k];
+                    vg[k] = rn[k] != EG_MP_NONE ? gather(e + CH + k, un[k]) : V();
+                }
+                if (base + 2 * CH < E1) eg_coov_load<U, HINT>(rid, col, base + 2 * CH, E1, lane, rn, un, pol);
+            }
+        } else {
+            if (PF) {
+#pragma unroll
+                for (int k = 0; k < U; k++) {
+                    r[k] = rn[k];
+                    u[k] = un[k];
+                }
+                if (base + CH < E1) eg_coov_load<U, HINT>(rid, col, base + CH, E1, lane, rn, un, pol);
+            } else {
+                eg_coov_load<U, HINT>(rid, col, base, E1, lane, r, u, pol);
+            }
+#pragma unroll
+            for (int k = 0; k < U; k++) v[k] = r[k] != EG_MP_NONE ? gather(e + k, u[k]) : V();
+        }
         // row of the entry after this lane's last one
         uint32_t nxt = __shfl_down_sync(EG_FULL_MASK, r[0], 1);
         if (lane == 31) nxt = base + CH < E1 ? __ldg(rid + base + CH) : tile_next;
@@ -588,12 +616,13 @@ __device__ __forceinline__ void eg_coov_tile(uint32_t t, const uint32_t *__restr
 // entries, so only the last tile has padding entries (row EG_MP_NONE, never
 // emitted).
 //
-// PF: the next chunk's rid/col words are loaded before the current chunk's
+// PF 1: the next chunk's rid/col words are loaded before the current chunk's
 // gathers, so the streaming loads of one chunk overlap the gathers and scan
-// of the previous one.  MINB: resident CTAs per SM asked of the compiler,
+// of the previous one.  PF 2: in addition the next chunk's gathers are issued
+// before the current chunk's scan, so their latency hides behind the scan.  MINB: resident CTAs per SM asked of the compiler,
 // which bounds the registers per thread (6: 42, 8: every warp slot, 32).
 // HINT: cache hints on the streamed words (eg_stream_ld4).
-template <class Op, int TILE_E, int U, bool REDUCE, bool PF = false, int MINB = 6, int HINT = 0>
+template <class Op, int TILE_E, int U, bool REDUCE, int PF = 0, int MINB = 6, int HINT = 0>
 __global__ void __launch_bounds__(256, MINB) k_coov_rows(const uint32_t *__restrict__ rid,
                                                          const uint32_t *__restrict__ col, uint32_t m, uint32_t ntiles,
                                                          eg_mp_carry<typename Op::A> *__restrict__ carry,

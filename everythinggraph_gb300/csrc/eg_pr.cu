@@ -235,17 +235,20 @@ __global__ void k_pr_reduce(const double2 *__restrict__ part, uint32_t nparts, e
 #define EG_COO_TILE_MIN 512
 #define EG_PR_CHECK 4  // iterations between reads of the stop flag
 #define EG_PR_RES_BLOCKS 1024
-#define EG_ROW_CFGS 10
+#define EG_ROW_CFGS 12
 struct RowCfg {
     int tile, u, pf, minb, hint;
 };
-// min_blocks bounds the registers: 6 resident CTAs of 256 threads leave 42
-// registers per thread, 5 leave 51, 4 leave 64, 8 leave 32.
+// pf: 0 no prefetch, 1 next chunk's words loaded ahead, 2 also its gathers
+// issued before the current chunk's scan.  min_blocks bounds the registers:
+// 6 resident CTAs of 256 threads leave 42 registers per thread, 5 leave 51,
+// 4 leave 64, 8 leave 32.
 static const RowCfg kRowCfg[EG_ROW_CFGS] = {
     {1024, 4, 1, 5, 0}, {2048, 4, 0, 6, 0}, {2048, 4, 1, 5, 0}, {1024, 4, 1, 6, 0}, {512, 4, 1, 5, 0},
-    {1024, 8, 1, 4, 0}, {1024, 4, 0, 8, 0}, {2048, 8, 0, 5, 0}, {1024, 4, 1, 5, 1}, {2048, 4, 1, 5, 1}};
+    {1024, 8, 1, 4, 0}, {1024, 4, 0, 8, 0}, {2048, 8, 0, 5, 0}, {1024, 4, 1, 5, 1}, {2048, 4, 1, 5, 1},
+    {1024, 4, 2, 4, 0}, {2048, 4, 2, 4, 0}};
 
-template <class Op, int TILE, int U, bool REDUCE, bool PF, int MINB, int HINT = 0>
+template <class Op, int TILE, int U, bool REDUCE, int PF, int MINB, int HINT = 0>
 static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts,
                         cudaEvent_t ev_begin, cudaEvent_t ev_end) {
     eg_ctx *ctx = g->ctx;
@@ -291,6 +294,8 @@ static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part
         EG_ROW_CASE(7, 2048, 8, false, 5, 0)
         EG_ROW_CASE(8, 1024, 4, true, 5, 1)
         EG_ROW_CASE(9, 2048, 4, true, 5, 1)
+        EG_ROW_CASE(10, 1024, 4, 2, 4, 0)
+        EG_ROW_CASE(11, 2048, 4, 2, 4, 0)
         default: return coo_launch_t<Op, 1024, 4, REDUCE, true, 5>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
     }
 #undef EG_ROW_CASE

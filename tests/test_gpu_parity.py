@@ -167,7 +167,7 @@ def test_row_schedules_and_autotuner(case):
     vals = oracle.hash_values(adj.in_col, adj.in_dst(), 9)
     y_ref = oracle.spmv_f64(n, adj.in_ptr, adj.in_col, vals, x)
     cands, chosen = g.tune()
-    assert len(cands) == 10 and 0 <= chosen < 10
+    assert len(cands) == 12 and 0 <= chosen < 12
     assert g.bfs_tuning["switch_divisor"] in (20.0, 40.0, 80.0, 160.0, 320.0)
     assert sum(c["cache_hint"] for c in cands) == 2
     if n > 1000:
