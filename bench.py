@@ -124,6 +124,9 @@ def run_ours(args):
     g.tune()  # row schedule and BFS level-loop form for this graph (untimed setup)
     roots = g.sample_roots(W["roots"], W["root_seed"])
     stream = torch.cuda.ExternalStream(ctx.stream)
+    # the BFS level-loop form: the tuner's (default), or fixed (a profiler
+    # slows per-level host round trips, so its own tuning would differ)
+    bfs_form = {"auto": None, "graph": False, "host": True}[args.bfs_form]
 
     # host outputs of the end-to-end step: page-locked, allocated once and
     # reused by every call (what a serving process holds); eg_bfs_batch takes
@@ -137,11 +140,12 @@ def run_ours(args):
         traversed = 0
         if copy_out:
             for c in range(0, len(roots), E2E_BATCH):
-                _, _, sts = g.bfs_batch(roots[c:c + E2E_BATCH], parents=True, level_out=lv_h, parent_out=par_h)
+                _, _, sts = g.bfs_batch(roots[c:c + E2E_BATCH], parents=True, level_out=lv_h, parent_out=par_h,
+                                        host_loop=bfs_form)
                 traversed += sum(st.edges_traversed for st in sts)
         else:
             for r in roots:
-                lv, par, st = g.bfs(int(r), parents=True, copy_out=False)
+                lv, par, st = g.bfs(int(r), parents=True, copy_out=False, host_loop=bfs_form)
                 traversed += st.edges_traversed
         lab, wst = g.wcc(copy_out=copy_out, out=lab_h)
         return traversed + m_in, wst
@@ -577,6 +581,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--scale", type=int, default=0)
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--bfs-form", choices=["auto", "graph", "host"], default="auto",
+                    help="BFS level loop: the form eg_graph_tune keeps (auto), or a fixed one")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--pr-only", action="store_true", help="only the PageRank pull report (profiling)")
     ap.add_argument("--serve-only", action="store_true", help="only the serving report")

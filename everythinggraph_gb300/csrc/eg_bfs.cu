@@ -31,7 +31,8 @@ struct BfsCounters {
 // grid (k_bfs_push_big) instead of one warp: an RMAT hub has 10^5..10^6.
 #define EG_BFS_BIG_DEG 2048u
 #define EG_BFS_CHUNK 4096u  // edges of a deferred hub per CTA work unit
-#define EG_BFS_SMALL_BIG 64u  // the deferral threshold of levels with few frontier vertices
+#define EG_BFS_SMALL_BIG 64u     // the deferral threshold of levels with few frontier vertices
+#define EG_BFS_WARP_EDGES 256u   // k_bfs_push's threshold otherwise (32 such lists: 8192 edges per warp)
 #define EG_BFS_QUEUE_EDGES (1u << 18)  // push levels over more edges build no next queue
 
 // Block-level reduction of per-thread counters: one atomic per block.
@@ -125,7 +126,11 @@ __device__ __forceinline__ void warp_append(bool claimed, uint32_t v, uint32_t *
     }
 }
 
-// Top-down step: one warp per frontier vertex, lanes over its out-list.
+// Top-down step: a warp takes 32 frontier vertices (one per lane) and walks
+// their out-lists together, 32 edges per step: an inclusive scan of the
+// lanes' degrees gives each edge slot its owner by a 5-step shuffle search, so
+// every lane has an edge whatever the degrees (one warp per vertex left most
+// lanes idle on the low-degree frontiers that follow the pull levels).
 // Vertices with more than big_deg out-edges go to a side list that
 // k_bfs_push_big expands with every thread of the grid.
 __global__ void __launch_bounds__(256) k_bfs_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
@@ -138,21 +143,43 @@ __global__ void __launch_bounds__(256) k_bfs_push(const uint32_t *__restrict__ p
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     uint32_t my_cnt = 0;
     unsigned long long my_deg = 0;
-    // uniform trip count per warp (qi is the same for all lanes)
-    for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < qlen; qi += warps) {
-        const uint32_t u = queue[qi];
-        const uint32_t b = ptr[u], e = ptr[u + 1];
-        if (e - b > big_deg) {
-            if (lane == 0) big[atomicAdd(&cnt->nbig, 1u)] = u;
-            continue;
+    // uniform trip count per warp (q0 is the same for all lanes)
+    for (uint32_t q0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; q0 < qlen; q0 += warps * 32) {
+        const uint32_t qi = q0 + lane;
+        uint32_t u = 0, b = 0, d = 0;
+        if (qi < qlen) {
+            u = queue[qi];
+            b = ptr[u];
+            d = ptr[u + 1] - b;
+            if (d > big_deg) {
+                big[atomicAdd(&cnt->nbig, 1u)] = u;
+                d = 0;
+            }
         }
-        for (uint32_t p0 = b; p0 < e; p0 += 32) {
-            const uint32_t p = p0 + lane;
+        uint32_t inc = d;  // inclusive scan of the degrees
+#pragma unroll
+        for (uint32_t o = 1; o < 32; o <<= 1) {
+            const uint32_t y = __shfl_up_sync(EG_FULL_MASK, inc, o);
+            if (lane >= o) inc += y;
+        }
+        const uint32_t total = __shfl_sync(EG_FULL_MASK, inc, 31);
+        const uint32_t exc = inc - d;
+        for (uint32_t p0 = 0; p0 < total; p0 += 32) {
+            const uint32_t x = p0 + lane;
+            uint32_t lo = 0;  // owner of edge slot x: the first lane whose inclusive sum exceeds x
+#pragma unroll
+            for (uint32_t step = 16; step > 0; step >>= 1) {
+                const uint32_t probe = __shfl_sync(EG_FULL_MASK, inc, lo + step - 1);
+                if (probe <= x) lo += step;
+            }
+            const uint32_t ob = __shfl_sync(EG_FULL_MASK, b, lo);
+            const uint32_t oe = __shfl_sync(EG_FULL_MASK, exc, lo);
+            const uint32_t ou = __shfl_sync(EG_FULL_MASK, u, lo);
             bool claimed = false;
             uint32_t v = 0;
-            if (p < e) {
-                v = col[p];
-                claimed = bfs_claim(v, u, visited, next_bm, level, parent, next_level);
+            if (x < total) {
+                v = col[ob + (x - oe)];
+                claimed = bfs_claim(v, ou, visited, next_bm, level, parent, next_level);
             }
             warp_append(claimed, v, next_queue, cnt, deg, my_cnt, my_deg);
         }
@@ -725,13 +752,13 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
             // a level over many edges leaves the next frontier as a bitmap
             // only; a push level after it rebuilds the queue (k_bm_to_queue)
             const bool make_queue = fdeg <= EG_BFS_QUEUE_EDGES;
-            uint32_t big_deg = EG_BFS_BIG_DEG, chunk = EG_BFS_CHUNK;
+            uint32_t big_deg = EG_BFS_WARP_EDGES, chunk = EG_BFS_CHUNK;
             if ((uint64_t)qlen < (uint64_t)grid_ctas * 8) {
                 big_deg = EG_BFS_SMALL_BIG;
                 const uint64_t per = (fdeg / grid_ctas + 255) & ~255ull;
                 chunk = (uint32_t)(per < 256 ? 256 : (per > EG_BFS_CHUNK ? EG_BFS_CHUNK : per));
             }
-            k_bfs_push<<<blocks_for(ctx, (uint64_t)qlen * 32), 256, 0, ctx->stream>>>(
+            k_bfs_push<<<blocks_for(ctx, qlen), 256, 0, ctx->stream>>>(
                 bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, q[cur], qlen, visited, bm[nxt],
                 make_queue ? q[nxt] : nullptr, level, parent, lvl + 1, cnt, big, big_deg);
             EG_LAUNCHED(ctx);
@@ -1144,9 +1171,12 @@ extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *
 }
 
 int eg_bfs_tune(eg_graph *g, float *ms_graph, float *ms_host, int *host_loop, double *divisor) {
+    // per-root times vary several-fold (a late switch to pull costs a few
+    // roots a lot), so the mean is taken over 16 sampled roots
     static const double kDiv[5] = {20.0, 40.0, 80.0, 160.0, 320.0};
-    uint32_t roots[4];
-    EG_TRY(eg_sample_roots(g, 4, 12345, roots));
+    constexpr int R = 16;
+    uint32_t roots[R];
+    EG_TRY(eg_sample_roots(g, R, 12345, roots));
     float best[2] = {0.f, 0.f};
     double best_div[2] = {20.0, 20.0};
     for (int form = 0; form < 2; form++) {
@@ -1159,9 +1189,9 @@ int eg_bfs_tune(eg_graph *g, float *ms_graph, float *ms_host, int *host_loop, do
             eg_bfs_stats st;
             EG_TRY(eg_bfs(g, roots[0], &o, nullptr, nullptr, &st));  // warm-up (graph capture, buffers)
             float t = 0.f;
-            for (int r = 0; r < 4; r++) {
+            for (int r = 0; r < R; r++) {
                 EG_TRY(eg_bfs(g, roots[r], &o, nullptr, nullptr, &st));
-                t += st.ms / 4.f;
+                t += st.ms / (float)R;
             }
             if (d == 0 || t < best[form]) {
                 best[form] = t;
