@@ -27,13 +27,13 @@ struct BfsCounters {
     uint32_t pad;
 };
 
-// Frontier vertices with more out-edges than this are expanded by the whole
-// grid (k_bfs_push_big) instead of one warp: an RMAT hub has 10^5..10^6.
-#define EG_BFS_BIG_DEG 2048u
-#define EG_BFS_CHUNK 4096u  // edges of a deferred hub per CTA work unit
-#define EG_BFS_SMALL_BIG 64u     // the deferral threshold of levels with few frontier vertices
-#define EG_BFS_WARP_EDGES 256u   // k_bfs_push's threshold otherwise (32 such lists: 8192 edges per warp)
-#define EG_BFS_QUEUE_EDGES (1u << 18)  // push levels over more edges build no next queue
+// Frontier vertices with more out-edges than a threshold are expanded by the
+// whole grid (k_*_push_big) instead of one warp: an RMAT hub has 10^5..10^6.
+#define EG_BFS_BIG_DEG 2048u            // multi-source push (one warp per vertex)
+#define EG_BFS_WARP_EDGES 256u          // single-source push (32 lists per warp: 8192 edges at most)
+#define EG_BFS_SMALL_BIG 64u            // single-source levels with few frontier vertices
+#define EG_BFS_CHUNK 4096u              // edges of a deferred hub per CTA work unit
+#define EG_BFS_QUEUE_EDGES (1u << 18)   // push levels over more edges build no next queue
 
 // Block-level reduction of per-thread counters: one atomic per block.
 __device__ __forceinline__ void block_add_counters(BfsCounters *c, uint32_t cnt, unsigned long long deg) {
@@ -126,13 +126,51 @@ __device__ __forceinline__ void warp_append(bool claimed, uint32_t v, uint32_t *
     }
 }
 
-// Top-down step: a warp takes 32 frontier vertices (one per lane) and walks
-// their out-lists together, 32 edges per step: an inclusive scan of the
-// lanes' degrees gives each edge slot its owner by a 5-step shuffle search, so
-// every lane has an edge whatever the degrees (one warp per vertex left most
-// lanes idle on the low-degree frontiers that follow the pull levels).
-// Vertices with more than big_deg out-edges go to a side list that
-// k_bfs_push_big expands with every thread of the grid.
+// Expands the out-lists of a warp's 32 lanes' vertices together (lane i:
+// vertex u, list start b, length d; d = 0 for none), 32 edges per step: an
+// inclusive scan of the lengths gives each edge slot its owner by a 5-step
+// shuffle search, so every lane has an edge whatever the degrees (one warp per
+// vertex left most lanes idle on the low-degree frontiers that follow the
+// pull levels).
+__device__ __forceinline__ void bfs_expand_warp(uint32_t u, uint32_t b, uint32_t d, const uint32_t *__restrict__ col,
+                                                const uint32_t *__restrict__ deg, uint32_t *visited,
+                                                uint32_t *next_bm, uint32_t *next_queue, int32_t *level,
+                                                int32_t *parent, int32_t next_level, BfsCounters *cnt,
+                                                uint32_t &my_cnt, unsigned long long &my_deg) {
+    const uint32_t lane = threadIdx.x & 31;
+    uint32_t inc = d;  // inclusive scan of the lengths
+#pragma unroll
+    for (uint32_t o = 1; o < 32; o <<= 1) {
+        const uint32_t y = __shfl_up_sync(EG_FULL_MASK, inc, o);
+        if (lane >= o) inc += y;
+    }
+    const uint32_t total = __shfl_sync(EG_FULL_MASK, inc, 31);
+    const uint32_t exc = inc - d;
+    for (uint32_t p0 = 0; p0 < total; p0 += 32) {
+        const uint32_t x = p0 + lane;
+        uint32_t lo = 0;  // owner of edge slot x: the first lane whose inclusive sum exceeds x
+#pragma unroll
+        for (uint32_t step = 16; step > 0; step >>= 1) {
+            const uint32_t probe = __shfl_sync(EG_FULL_MASK, inc, lo + step - 1);
+            if (probe <= x) lo += step;
+        }
+        const uint32_t ob = __shfl_sync(EG_FULL_MASK, b, lo);
+        const uint32_t oe = __shfl_sync(EG_FULL_MASK, exc, lo);
+        const uint32_t ou = __shfl_sync(EG_FULL_MASK, u, lo);
+        bool claimed = false;
+        uint32_t v = 0;
+        if (x < total) {
+            v = col[ob + (x - oe)];
+            claimed = bfs_claim(v, ou, visited, next_bm, level, parent, next_level);
+        }
+        warp_append(claimed, v, next_queue, cnt, deg, my_cnt, my_deg);
+    }
+}
+
+// Top-down step: a warp takes 32 frontier vertices (one per lane) and
+// expands them together (bfs_expand_warp).  Vertices with more than big_deg
+// out-edges go to a side list that k_bfs_push_big expands with every thread
+// of the grid.
 __global__ void __launch_bounds__(256) k_bfs_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
                                                   const uint32_t *__restrict__ deg, const uint32_t *__restrict__ queue,
                                                   uint32_t qlen, uint32_t *visited, uint32_t *next_bm,
@@ -156,33 +194,8 @@ __global__ void __launch_bounds__(256) k_bfs_push(const uint32_t *__restrict__ p
                 d = 0;
             }
         }
-        uint32_t inc = d;  // inclusive scan of the degrees
-#pragma unroll
-        for (uint32_t o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(EG_FULL_MASK, inc, o);
-            if (lane >= o) inc += y;
-        }
-        const uint32_t total = __shfl_sync(EG_FULL_MASK, inc, 31);
-        const uint32_t exc = inc - d;
-        for (uint32_t p0 = 0; p0 < total; p0 += 32) {
-            const uint32_t x = p0 + lane;
-            uint32_t lo = 0;  // owner of edge slot x: the first lane whose inclusive sum exceeds x
-#pragma unroll
-            for (uint32_t step = 16; step > 0; step >>= 1) {
-                const uint32_t probe = __shfl_sync(EG_FULL_MASK, inc, lo + step - 1);
-                if (probe <= x) lo += step;
-            }
-            const uint32_t ob = __shfl_sync(EG_FULL_MASK, b, lo);
-            const uint32_t oe = __shfl_sync(EG_FULL_MASK, exc, lo);
-            const uint32_t ou = __shfl_sync(EG_FULL_MASK, u, lo);
-            bool claimed = false;
-            uint32_t v = 0;
-            if (x < total) {
-                v = col[ob + (x - oe)];
-                claimed = bfs_claim(v, ou, visited, next_bm, level, parent, next_level);
-            }
-            warp_append(claimed, v, next_queue, cnt, deg, my_cnt, my_deg);
-        }
+        bfs_expand_warp(u, b, d, col, deg, visited, next_bm, next_queue, level, parent, next_level, cnt, my_cnt,
+                        my_deg);
     }
     block_add_counters(cnt, my_cnt, my_deg);
 }
@@ -423,23 +436,20 @@ __global__ void __launch_bounds__(256) k_bfsg_push(const BfsGState *st, const ui
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     uint32_t my_cnt = 0;
     unsigned long long my_deg = 0;
-    for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < qlen; qi += warps) {
-        const uint32_t u = queue[qi];
-        const uint32_t b = ptr[u], e = ptr[u + 1];
-        if (e - b > EG_BFS_BIG_DEG) {
-            if (lane == 0) big[atomicAdd(&cnt->nbig, 1u)] = u;
-            continue;
-        }
-        for (uint32_t p0 = b; p0 < e; p0 += 32) {
-            const uint32_t p = p0 + lane;
-            bool claimed = false;
-            uint32_t v = 0;
-            if (p < e) {
-                v = col[p];
-                claimed = bfs_claim(v, u, visited, next_bm, level, parent, next_level);
+    for (uint32_t q0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; q0 < qlen; q0 += warps * 32) {
+        const uint32_t qi = q0 + lane;
+        uint32_t u = 0, b = 0, d = 0;
+        if (qi < qlen) {
+            u = queue[qi];
+            b = ptr[u];
+            d = ptr[u + 1] - b;
+            if (d > EG_BFS_WARP_EDGES) {
+                big[atomicAdd(&cnt->nbig, 1u)] = u;
+                d = 0;
             }
-            warp_append(claimed, v, next_queue, cnt, deg, my_cnt, my_deg);
         }
+        bfs_expand_warp(u, b, d, col, deg, visited, next_bm, next_queue, level, parent, next_level, cnt, my_cnt,
+                        my_deg);
     }
     block_add_counters(cnt, my_cnt, my_deg);
 }
@@ -1171,10 +1181,10 @@ extern "C" int eg_bfs_multi(eg_graph *g, const uint32_t *roots, int k, int32_t *
 }
 
 int eg_bfs_tune(eg_graph *g, float *ms_graph, float *ms_host, int *host_loop, double *divisor) {
-    // per-root times vary several-fold (a late switch to pull costs a few
-    // roots a lot), so the mean is taken over 16 sampled roots
+    // per-root times vary several-fold (an early switch to pull costs a few
+    // roots a lot), so the mean is taken over 48 sampled roots
     static const double kDiv[5] = {20.0, 40.0, 80.0, 160.0, 320.0};
-    constexpr int R = 16;
+    constexpr int R = 48;
     uint32_t roots[R];
     EG_TRY(eg_sample_roots(g, R, 12345, roots));
     float best[2] = {0.f, 0.f};

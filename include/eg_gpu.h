@@ -191,7 +191,7 @@ typedef struct {
     int min_blocks[EG_ROW_SCHEDULES_MAX];
     int cache_hint[EG_ROW_SCHEDULES_MAX];
     float ms[EG_ROW_SCHEDULES_MAX]; /* mean row-kernel time per iteration */
-    /* BFS level loop (when the graph has a CSR): mean ms per BFS over 16
+    /* BFS level loop (when the graph has a CSR): mean ms per BFS over 48
      * sampled roots for the CUDA-graph and the host-driven loop (each at its
      * best switch divisor of 20, 40, 80, 160, 320), and the form and the
      * divisor kept for eg_bfs's host_loop = -1 and switch_divisor < 0 */
