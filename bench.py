@@ -176,7 +176,10 @@ def run_ours(args):
         ms = float(t.item())
     ms_step = ms / args.steps
     value = edges * world / (ms / 1e3) / 1e9
-    # ---- end-to-end through the C ABI with host outputs (levels, parents, labels)
+    # ---- end-to-end through the C ABI with host outputs (levels, parents, labels),
+    # after one untimed step of its own (first use of the output slots and of
+    # the page-locked buffers)
+    step(True)
     torch.cuda.synchronize()
     te0 = time.perf_counter()
     e_edges = 0
