@@ -14,6 +14,7 @@
 #include <string.h>
 
 #include "eg_bigwork.cuh"
+#include "eg_frontier.cuh"
 #include "eg_internal.cuh"
 #include "eg_mspull.cuh"
 
@@ -126,45 +127,22 @@ __device__ __forceinline__ void warp_append(bool claimed, uint32_t v, uint32_t *
     }
 }
 
-// Expands the out-lists of a warp's 32 lanes' vertices together (lane i:
-// vertex u, list start b, length d; d = 0 for none), 32 edges per step: an
-// inclusive scan of the lengths gives each edge slot its owner by a 5-step
-// shuffle search, so every lane has an edge whatever the degrees (one warp per
-// vertex left most lanes idle on the low-degree frontiers that follow the
-// pull levels).
+// Expands the out-lists of a warp's 32 lanes' vertices together
+// (eg_warp_lists): claims the unvisited targets for the next level.
 __device__ __forceinline__ void bfs_expand_warp(uint32_t u, uint32_t b, uint32_t d, const uint32_t *__restrict__ col,
                                                 const uint32_t *__restrict__ deg, uint32_t *visited,
                                                 uint32_t *next_bm, uint32_t *next_queue, int32_t *level,
                                                 int32_t *parent, int32_t next_level, BfsCounters *cnt,
                                                 uint32_t &my_cnt, unsigned long long &my_deg) {
-    const uint32_t lane = threadIdx.x & 31;
-    uint32_t inc = d;  // inclusive scan of the lengths
-#pragma unroll
-    for (uint32_t o = 1; o < 32; o <<= 1) {
-        const uint32_t y = __shfl_up_sync(EG_FULL_MASK, inc, o);
-        if (lane >= o) inc += y;
-    }
-    const uint32_t total = __shfl_sync(EG_FULL_MASK, inc, 31);
-    const uint32_t exc = inc - d;
-    for (uint32_t p0 = 0; p0 < total; p0 += 32) {
-        const uint32_t x = p0 + lane;
-        uint32_t lo = 0;  // owner of edge slot x: the first lane whose inclusive sum exceeds x
-#pragma unroll
-        for (uint32_t step = 16; step > 0; step >>= 1) {
-            const uint32_t probe = __shfl_sync(EG_FULL_MASK, inc, lo + step - 1);
-            if (probe <= x) lo += step;
-        }
-        const uint32_t ob = __shfl_sync(EG_FULL_MASK, b, lo);
-        const uint32_t oe = __shfl_sync(EG_FULL_MASK, exc, lo);
-        const uint32_t ou = __shfl_sync(EG_FULL_MASK, u, lo);
+    eg_warp_lists(u, b, d, [&](bool valid, uint32_t, uint32_t ou, uint32_t p) {
         bool claimed = false;
         uint32_t v = 0;
-        if (x < total) {
-            v = col[ob + (x - oe)];
+        if (valid) {
+            v = col[p];
             claimed = bfs_claim(v, ou, visited, next_bm, level, parent, next_level);
         }
         warp_append(claimed, v, next_queue, cnt, deg, my_cnt, my_deg);
-    }
+    });
 }
 
 // Top-down step: a warp takes 32 frontier vertices (one per lane) and
@@ -278,48 +256,6 @@ __global__ void __launch_bounds__(256) k_bfs_pull(const uint32_t *__restrict__ p
     }
     block_add_counters(cnt, my_cnt, my_deg);
 }
-
-// Bitmap -> id queue: each thread owns one word, a block-wide exclusive scan
-// of the words' popcounts places them, one atomic per block reserves space.
-__global__ void __launch_bounds__(256) k_bm_to_queue(const uint32_t *__restrict__ bm, uint32_t n, uint32_t *queue,
-                                                     BfsCounters *cnt) {
-    __shared__ uint32_t s_warp[8];
-    __shared__ uint32_t s_base;
-    const uint32_t nw = (n + 31) >> 5;
-    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    for (uint32_t w0 = blockIdx.x * blockDim.x; w0 < nw; w0 += gridDim.x * blockDim.x) {
-        const uint32_t w = w0 + threadIdx.x;
-        const uint32_t word = w < nw ? bm[w] : 0u;
-        const uint32_t c = __popc(word);
-        uint32_t x = c;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t y = __shfl_up_sync(EG_FULL_MASK, x, o);
-            if (lane >= (uint32_t)o) x += y;
-        }
-        if (lane == 31) s_warp[warp] = x;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            uint32_t t = 0;
-            for (int i = 0; i < 8; i++) {
-                const uint32_t v = s_warp[i];
-                s_warp[i] = t;
-                t += v;
-            }
-            s_base = t ? atomicAdd(&cnt->qsize, t) : 0u;
-        }
-        __syncthreads();
-        uint32_t pos = s_base + s_warp[warp] + x - c;
-        uint32_t bits = word;
-        while (bits) {
-            const int b = __ffs(bits) - 1;
-            bits &= bits - 1;
-            queue[pos++] = (w << 5) + (uint32_t)b;
-        }
-        __syncthreads();
-    }
-}
-
 
 // ---------------------------------------------------------------- device-driven levels
 // The level loop as a CUDA graph: a start kernel, then a while node whose
@@ -745,7 +681,7 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
             have_queue = false;
         } else {
             if (!have_queue) {
-                k_bm_to_queue<<<blocks_for(ctx, (uint64_t)nw * 32), 256, 0, ctx->stream>>>(bm[cur], n, q[cur], cnt);
+                k_bm_queue<<<blocks_for(ctx, (uint64_t)nw * 32), 256, 0, ctx->stream>>>(bm[cur], n, q[cur], &cnt->qsize, 0);
                 EG_LAUNCHED(ctx);
                 EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream));
                 EG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -760,7 +696,7 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
             // chunks sized to spread the level's edges over the grid.
             const uint32_t grid_ctas = (uint32_t)ctx->sm_count * 8;
             // a level over many edges leaves the next frontier as a bitmap
-            // only; a push level after it rebuilds the queue (k_bm_to_queue)
+            // only; a push level after it rebuilds the queue (k_bm_queue)
             const bool make_queue = fdeg <= EG_BFS_QUEUE_EDGES;
             uint32_t big_deg = EG_BFS_WARP_EDGES, chunk = EG_BFS_CHUNK;
             if ((uint64_t)qlen < (uint64_t)grid_ctas * 8) {

@@ -14,6 +14,7 @@
 
 #include "eg_internal.cuh"
 #include "eg_bigwork.cuh"
+#include "eg_frontier.cuh"
 #include "eg_mrelax.cuh"
 
 namespace {
@@ -43,30 +44,18 @@ __global__ void k_sssp_init(uint32_t n, uint32_t *dist, uint32_t root, uint32_t 
     }
 }
 
-// One warp per frontier vertex; lanes relax its out-edges.  A vertex whose
-// distance drops is queued once per round (claimed through the next bitmap).
-__device__ __forceinline__ bool sssp_relax(uint32_t u, uint32_t du, uint32_t v, uint32_t wt, const WRule &w,
-                                           uint32_t *dist,
-                                           uint32_t *next_bm) {
-    if (v == u) return false;  // self-loops skipped (sssp_pushpull.c:80)
+// A relaxation that lowers dist[v] marks v in the next frontier bitmap; the
+// next queue is built from the bitmap afterwards (k_bm_queue), so no warp
+// waits on a shared queue counter.  The atomicMin's old value is not
+// awaited: when another relaxation got below nd first, that one marks v, so
+// the frontier is the same set either way.
+__device__ __forceinline__ void sssp_relax(uint32_t u, uint32_t du, uint32_t v, uint32_t wt, const WRule &w,
+                                           uint32_t *dist, uint32_t *next_bm) {
+    if (v == u) return;  // self-loops skipped (sssp_pushpull.c:80)
     const uint32_t nd = w.add(du, wt);
-    if (nd >= __ldcg(dist + v)) return false;
-    // no wait for the old value: when another relaxation got below nd first,
-    // that one marks v, so the frontier is the same set either way
+    if (nd >= __ldcg(dist + v)) return;
     atomicMin(dist + v, nd);
-    const uint32_t bit = 1u << (v & 31);
-    return !(atomicOr(next_bm + (v >> 5), bit) & bit);
-}
-
-__device__ __forceinline__ void sssp_append(bool q, uint32_t v, uint32_t *next_queue, SsspCounters *cnt) {
-    const uint32_t lane = threadIdx.x & 31;
-    const uint32_t ball = __ballot_sync(EG_FULL_MASK, q);
-    if (ball) {
-        uint32_t base = 0;
-        if (lane == 0) base = atomicAdd(&cnt->qsize, __popc(ball));
-        base = __shfl_sync(EG_FULL_MASK, base, 0);
-        if (q) next_queue[base + __popc(ball & eg_lanemask_lt())] = v;
-    }
+    atomicOr(next_bm + (v >> 5), 1u << (v & 31));
 }
 
 // Relaxes the deferred high-degree frontier vertices: chunks of
@@ -76,8 +65,7 @@ __global__ void __launch_bounds__(256) k_sssp_push_big(const uint32_t *__restric
                                                        const uint32_t *__restrict__ col,
                                                        const uint32_t *__restrict__ wts, const uint32_t *big,
                                                        const uint32_t *__restrict__ bigoff, uint32_t *dist,
-                                                       uint32_t *next_bm, uint32_t *next_queue, WRule w,
-                                                       SsspCounters *cnt) {
+                                                       uint32_t *next_bm, WRule w, SsspCounters *cnt) {
     const uint32_t nbig = *(volatile uint32_t *)&cnt->nbig;
     if (!nbig) return;
     const uint32_t total = bigoff[nbig];
@@ -90,56 +78,46 @@ __global__ void __launch_bounds__(256) k_sssp_push_big(const uint32_t *__restric
         const uint32_t b = vb + (c - bigoff[i]) * EG_SSSP_CHUNK;
         const uint32_t e = ve - b > EG_SSSP_CHUNK ? b + EG_SSSP_CHUNK : ve;
         if (threadIdx.x == 0) scanned += e - b;
-        for (uint32_t p0 = b + (threadIdx.x & ~31u); p0 < e; p0 += blockDim.x) {
-            const uint32_t p = p0 + (threadIdx.x & 31);
-            bool q = false;
-            uint32_t v = 0;
-            if (p < e) {
-                v = col[p];
-                q = sssp_relax(u, du, v, __ldg(wts + p), w, dist, next_bm);
-            }
-            sssp_append(q, v, next_queue, cnt);
-        }
+        for (uint32_t p = b + threadIdx.x; p < e; p += blockDim.x)
+            sssp_relax(u, du, __ldg(col + p), __ldg(wts + p), w, dist, next_bm);
     }
     if (scanned) atomicAdd(&cnt->relax, scanned);
 }
 
+// A warp takes 32 frontier vertices (one per lane) and relaxes their
+// out-lists together (eg_warp_lists); lists over EG_SSSP_WARP_EDGES go to
+// the side list for k_sssp_push_big.
+#define EG_SSSP_WARP_EDGES 256u
 __global__ void __launch_bounds__(256) k_sssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
-                                                   const uint32_t *__restrict__ wts, const uint32_t *__restrict__ queue, uint32_t qlen, uint32_t *dist,
-                                                   uint32_t *next_bm, uint32_t *next_queue, WRule w,
-                                                   SsspCounters *cnt, uint32_t *big) {
+                                                   const uint32_t *__restrict__ wts,
+                                                   const uint32_t *__restrict__ queue, uint32_t qlen, uint32_t *dist,
+                                                   uint32_t *next_bm, WRule w, SsspCounters *cnt, uint32_t *big) {
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
     unsigned long long scanned = 0;
-    for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < qlen; qi += warps) {
-        const uint32_t u = queue[qi];
-        const uint32_t du = __ldcg(dist + u);
-        const uint32_t b = ptr[u], e = ptr[u + 1];
-        if (e - b > EG_SSSP_BIG_DEG) {
-            if (lane == 0) big[atomicAdd(&cnt->nbig, 1u)] = u;
-            continue;
-        }
-        scanned += e - b;
-        for (uint32_t p0 = b; p0 < e; p0 += 32) {
-            const uint32_t p = p0 + lane;
-            bool q = false;
-            uint32_t v = 0;
-            if (p < e) {
-                v = col[p];
-                q = sssp_relax(u, du, v, __ldg(wts + p), w, dist, next_bm);
+    for (uint32_t q0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; q0 < qlen; q0 += warps * 32) {
+        const uint32_t qi = q0 + lane;
+        uint32_t u = 0, b = 0, d = 0, du = 0;
+        if (qi < qlen) {
+            u = queue[qi];
+            b = ptr[u];
+            d = ptr[u + 1] - b;
+            if (d > EG_SSSP_WARP_EDGES) {
+                big[atomicAdd(&cnt->nbig, 1u)] = u;
+                d = 0;
+            } else {
+                du = __ldcg(dist + u);
+                scanned += d;
             }
-            sssp_append(q, v, next_queue, cnt);
         }
+        eg_warp_lists(u, b, d, [&](bool valid, uint32_t lo, uint32_t ou, uint32_t p) {
+            const uint32_t odu = __shfl_sync(EG_FULL_MASK, du, lo);
+            if (valid) sssp_relax(ou, odu, __ldg(col + p), __ldg(wts + p), w, dist, next_bm);
+        });
     }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) scanned += __shfl_down_sync(EG_FULL_MASK, scanned, o);
     if (lane == 0 && scanned) atomicAdd(&cnt->relax, scanned);
-}
-
-// Clears the bitmap bits of the vertices in a queue.
-__global__ void k_clear_bits(const uint32_t *__restrict__ queue, uint32_t qlen, uint32_t *bm) {
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < qlen; i += gridDim.x * blockDim.x) {
-        uint32_t v = queue[i];
-        atomicAnd(bm + (v >> 5), ~(1u << (v & 31)));
-    }
 }
 
 __global__ void k_count_reached(const uint32_t *__restrict__ dist, uint64_t len, unsigned long long *out,
@@ -230,25 +208,22 @@ extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wrule_in, u
     while (qlen > 0) {
         const int nxt = cur ^ 1;
         EG_CUDA(cudaMemsetAsync(&cnt->qsize, 0, 8, ctx->stream));  // qsize and nbig
-        k_sssp_push<<<blocks_for(ctx, (uint64_t)qlen * 32), 256, 0, ctx->stream>>>(
-            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), wts, q[cur], qlen, dist, bm, q[nxt], w, cnt, big);
+        k_sssp_push<<<blocks_for(ctx, qlen), 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col),
+                                                                   wts, q[cur], qlen, dist, bm, w, cnt, big);
         EG_LAUNCHED(ctx);
         k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, 1u, bp<uint32_t>(g->csr.ptr), EG_SSSP_CHUNK,
                                                    bigoff);
         EG_LAUNCHED(ctx);
-        k_sssp_push_big<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr),
-                                                                              bp<uint32_t>(g->csr.col), wts, big, bigoff,
-                                                                              dist, bm, q[nxt], w, cnt);
+        k_sssp_push_big<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
+            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), wts, big, bigoff, dist, bm, w, cnt);
+        EG_LAUNCHED(ctx);
+        // the marked vertices become the next queue; their bits are cleared
+        k_bm_queue<<<blocks_for(ctx, (uint64_t)nw * 32), 256, 0, ctx->stream>>>(bm, n, q[nxt], &cnt->qsize, 1);
         EG_LAUNCHED(ctx);
         EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(SsspCounters), cudaMemcpyDeviceToHost, ctx->stream));
         EG_CUDA(cudaStreamSynchronize(ctx->stream));
         qlen = h->qsize;
         relax = h->relax;
-        // the new queue's bits must be clear before it produces the next one
-        if (qlen) {
-            k_clear_bits<<<blocks_for(ctx, qlen), 256, 0, ctx->stream>>>(q[nxt], qlen, bm);
-            EG_LAUNCHED(ctx);
-        }
         cur = nxt;
         rounds++;
         if (rounds > (int)(4 * (uint64_t)n + 16)) return eg_fail(EG_ETIMEOUT, "SSSP did not converge");
