@@ -30,8 +30,7 @@ struct BfsCounters {
 
 // Frontier vertices with more out-edges than a threshold are expanded by the
 // whole grid (k_*_push_big) instead of one warp: an RMAT hub has 10^5..10^6.
-#define EG_BFS_BIG_DEG 2048u            // multi-source push (one warp per vertex)
-#define EG_BFS_WARP_EDGES 256u          // single-source push (32 lists per warp: 8192 edges at most)
+#define EG_BFS_WARP_EDGES 256u          // pushes with 32 lists per warp (8192 edges at most)
 #define EG_BFS_SMALL_BIG 64u            // single-source levels with few frontier vertices
 #define EG_BFS_CHUNK 4096u              // edges of a deferred hub per CTA work unit
 #define EG_BFS_QUEUE_EDGES (1u << 18)   // push levels over more edges build no next queue
@@ -879,8 +878,8 @@ __global__ void k_msg_prep(MsGState *st, MsCounters *cnt) {
 
 // Pull: a vertex ORs the frontier words of its in-neighbours, stopping early
 // once every source it still lacks has been found.
-// Push: one warp per vertex with a nonzero frontier word; vertices with more
-// than EG_BFS_BIG_DEG out-edges go to a side list for k_ms_push_big.
+// Push: 32 vertices with a nonzero frontier word per warp (eg_warp_lists); lists with more
+// than EG_BFS_WARP_EDGES out-edges go to a side list for k_ms_push_big.
 __global__ void __launch_bounds__(256) k_ms_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
                                                  const uint32_t *__restrict__ queue, const MsGState *st,
                                                  const unsigned long long *__restrict__ seen,
@@ -891,19 +890,30 @@ __global__ void __launch_bounds__(256) k_ms_push(const uint32_t *__restrict__ pt
     const uint32_t qlen = st->count;
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-    for (uint32_t qi = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; qi < qlen; qi += warps) {
-        const uint32_t u = queue[qi];
-        const uint32_t b = ptr[u], e = ptr[u + 1];
-        if (e - b > EG_BFS_BIG_DEG) {
-            if (lane == 0) big[atomicAdd(&cnt->nbig, 1u)] = u;
-            continue;
+    // 32 frontier vertices per warp, their lists walked together (eg_warp_lists)
+    for (uint32_t q0 = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 32; q0 < qlen; q0 += warps * 32) {
+        const uint32_t qi = q0 + lane;
+        uint32_t u = 0, b = 0, d = 0;
+        unsigned long long f = 0ull;
+        if (qi < qlen) {
+            u = queue[qi];
+            b = ptr[u];
+            d = ptr[u + 1] - b;
+            if (d > EG_BFS_WARP_EDGES) {
+                big[atomicAdd(&cnt->nbig, 1u)] = u;
+                d = 0;
+            } else {
+                f = front[u];
+            }
         }
-        const unsigned long long f = front[u];
-        for (uint32_t p = b + lane; p < e; p += 32) {
-            const uint32_t v = col[p];
-            const unsigned long long add = f & ~__ldcg(seen + v);
-            if (add && (__ldcg(next + v) & add) != add) atomicOr(next + v, add);
-        }
+        eg_warp_lists(u, b, d, [&](bool valid, uint32_t lo, uint32_t, uint32_t p) {
+            const unsigned long long of = __shfl_sync(EG_FULL_MASK, f, lo);
+            if (valid) {
+                const uint32_t v = col[p];
+                const unsigned long long add = of & ~__ldcg(seen + v);
+                if (add && (__ldcg(next + v) & add) != add) atomicOr(next + v, add);
+            }
+        });
     }
 }
 
