@@ -34,6 +34,7 @@ struct BfsCounters {
 #define EG_BFS_SMALL_BIG 64u            // single-source levels with few frontier vertices
 #define EG_BFS_CHUNK 4096u              // edges of a deferred hub per CTA work unit
 #define EG_BFS_QUEUE_EDGES (1u << 18)   // push levels over more edges build no next queue
+#define EG_NO_VERTEX 0xffffffffu
 
 // Block-level reduction of per-thread counters: one atomic per block.
 __device__ __forceinline__ void block_add_counters(BfsCounters *c, uint32_t cnt, unsigned long long deg) {
@@ -210,10 +211,53 @@ __global__ void __launch_bounds__(256) k_bfs_push_big(const uint32_t *__restrict
     block_add_counters(cnt, my_cnt, my_deg);
 }
 
+// An unvisited vertex's bottom-up scan: the first in-neighbour comes from
+// first[] (one coalesced word per vertex: in-lists sorted by source id put
+// the RMAT hubs first, so it is most often the parent), the rest of the list
+// only when that one is not in the frontier.  Sets level and parent of the
+// first in-neighbour (in list order) in the frontier, as a scan of the whole
+// list would.
+__device__ __forceinline__ bool pull_scan(uint32_t v, const uint32_t *__restrict__ ptr,
+                                          const uint32_t *__restrict__ col, const uint32_t *__restrict__ first,
+                                          const uint32_t *cur_bm, int32_t *level, int32_t *parent,
+                                          int32_t next_level) {
+    const uint32_t f0 = __ldg(first + v);
+    if (f0 == EG_NO_VERTEX) return false;  // no in-neighbours
+    // the frontier bitmap is not written during a pull level: read through L1,
+    // which keeps the words of the hub ids
+    uint32_t u = f0;
+    bool hit = (__ldg(cur_bm + (u >> 5)) >> (u & 31)) & 1u;
+    if (!hit) {
+        const uint32_t e = ptr[v + 1];
+        for (uint32_t p = ptr[v] + 1; p < e; p++) {
+            u = col[p];
+            if ((__ldg(cur_bm + (u >> 5)) >> (u & 31)) & 1u) {
+                hit = true;
+                break;
+            }
+        }
+    }
+    if (hit) {
+        level[v] = next_level;
+        if (parent) parent[v] = (int32_t)u;
+    }
+    return hit;
+}
+
+// first[v] = the first entry of v's in-list, EG_NO_VERTEX when it is empty.
+__global__ void k_first_in(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col, uint32_t n,
+                           uint32_t *__restrict__ first) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
+        const uint32_t b = ptr[v];
+        first[v] = b < ptr[v + 1] ? col[b] : EG_NO_VERTEX;
+    }
+}
+
 // Bottom-up step: one thread per vertex, warps over 32 consecutive vertices
 // (one bitmap word).  An unvisited vertex scans its in-list and stops at the
 // first neighbour in the frontier.  The new frontier word is the warp ballot.
 __global__ void __launch_bounds__(256) k_bfs_pull(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+                                                  const uint32_t *__restrict__ first,
                                                   const uint32_t *__restrict__ deg, uint32_t n,
                                                   const uint32_t *__restrict__ cur_bm, uint32_t *visited,
                                                   uint32_t *next_bm, int32_t *level, int32_t *parent,
@@ -231,18 +275,8 @@ __global__ void __launch_bounds__(256) k_bfs_pull(const uint32_t *__restrict__ p
         }
         const uint32_t v = (w << 5) + lane;
         bool found = false;
-        if (v < n && !(vis & (1u << lane))) {
-            const uint32_t b = ptr[v], e = ptr[v + 1];
-            for (uint32_t p = b; p < e; p++) {
-                const uint32_t u = col[p];
-                if (__ldg(cur_bm + (u >> 5)) & (1u << (u & 31))) {
-                    found = true;
-                    level[v] = next_level;
-                    if (parent) parent[v] = (int32_t)u;
-                    break;
-                }
-            }
-        }
+        if (v < n && !(vis & (1u << lane)))
+            found = pull_scan(v, ptr, col, first, cur_bm, level, parent, next_level);
         const uint32_t ball = __ballot_sync(EG_FULL_MASK, found);
         if (lane == 0) {
             next_bm[w] = ball;
@@ -423,7 +457,8 @@ __global__ void __launch_bounds__(256) k_bfsg_push_big(const BfsGState *st, cons
 }
 
 __global__ void __launch_bounds__(256) k_bfsg_pull(const BfsGState *st, const uint32_t *__restrict__ ptr,
-                                                   const uint32_t *__restrict__ col, const uint32_t *__restrict__ deg,
+                                                   const uint32_t *__restrict__ col,
+                                                   const uint32_t *__restrict__ first, const uint32_t *__restrict__ deg,
                                                    uint32_t *bm0, uint32_t *bm1, uint32_t *visited, int32_t *level,
                                                    int32_t *parent, BfsCounters *cnt) {
     if (!st->pull) return;
@@ -445,18 +480,8 @@ __global__ void __launch_bounds__(256) k_bfsg_pull(const BfsGState *st, const ui
         }
         const uint32_t v = (w << 5) + lane;
         bool found = false;
-        if (v < n && !(vis & (1u << lane))) {
-            const uint32_t b = ptr[v], e = ptr[v + 1];
-            for (uint32_t p = b; p < e; p++) {
-                const uint32_t u = col[p];
-                if (__ldcg(cur_bm + (u >> 5)) & (1u << (u & 31))) {
-                    found = true;
-                    level[v] = next_level;
-                    if (parent) parent[v] = (int32_t)u;
-                    break;
-                }
-            }
-        }
+        if (v < n && !(vis & (1u << lane)))
+            found = pull_scan(v, ptr, col, first, cur_bm, level, parent, next_level);
         const uint32_t ball = __ballot_sync(EG_FULL_MASK, found);
         if (lane == 0) {
             next_bm[w] = ball;
@@ -555,7 +580,9 @@ static int bfs_graph_build(eg_graph *g, eg_bfs_graph &bg, const void *const key[
     k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, 1u, bp<uint32_t>(g->csr.ptr), EG_BFS_CHUNK, bigoff);
     k_bfsg_push_big<<<blocks, 256, 0, ctx->stream>>>(st, bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, big,
                                                     bigoff, q0, q1, bm0, bm1, visited, level, parent, cnt);
-    if (iptr) k_bfsg_pull<<<blocks, 256, 0, ctx->stream>>>(st, iptr, icol, deg, bm0, bm1, visited, level, parent, cnt);
+    if (iptr)
+        k_bfsg_pull<<<blocks, 256, 0, ctx->stream>>>(st, iptr, icol, bp<uint32_t>(g->first_in), deg, bm0, bm1, visited,
+                                                     level, parent, cnt);
     k_bfsg_end<<<1, 1, 0, ctx->stream>>>(st, cnt, handle);
     ce = cudaStreamEndCapture(ctx->stream, &body);
     if (ce != cudaSuccess) return eg_fail(EG_ECUDA, "BFS level capture: %s", cudaGetErrorString(ce));
@@ -592,6 +619,13 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
     EG_CUDA(cudaSetDevice(ctx->device));
     const uint32_t n = g->n;
     const uint32_t nw = (n + 31) >> 5;
+    if (in_adj && g->first_in_src != in_adj->col.p) {  // once per graph and in-list array
+        EG_TRY(eg_buf_ensure(ctx, g->first_in, (uint64_t)n * 4));
+        k_first_in<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col), n,
+                                                              bp<uint32_t>(g->first_in));
+        EG_LAUNCHED(ctx);
+        g->first_in_src = in_adj->col.p;
+    }
     eg_buf &lbuf = slot ? g->level_s[slot - 1] : g->level, &pbuf = slot ? g->parent_s[slot - 1] : g->parent;
     EG_TRY(eg_buf_ensure(ctx, lbuf, (uint64_t)n * 4));
     if (want_parent) EG_TRY(eg_buf_ensure(ctx, pbuf, (uint64_t)n * 4));
@@ -673,8 +707,8 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
         EG_TRY(eg_zero(ctx, cnt, sizeof(BfsCounters), ctx->stream));
         if (pull) {
             k_bfs_pull<<<blocks_for(ctx, (uint64_t)nw * 32), 256, 0, ctx->stream>>>(
-                bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col), deg, n, bm[cur], visited, bm[nxt], level, parent,
-                lvl + 1, cnt);
+                bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col), bp<uint32_t>(g->first_in), deg, n, bm[cur],
+                visited, bm[nxt], level, parent, lvl + 1, cnt);
             EG_LAUNCHED(ctx);
             pull_levels++;
             have_queue = false;

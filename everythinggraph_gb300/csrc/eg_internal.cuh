@@ -122,6 +122,8 @@ struct eg_graph {
     eg_buf rank, rank_p, rank_q, contrib0, contrib1, pr_part, pr_stats, mp_carry, errflag;
     eg_buf level, parent, dist, label, spmv_x, spmv_y, spmv_vals;
     eg_buf level_s[EG_OUT_SLOTS - 1], parent_s[EG_OUT_SLOTS - 1];  // output slots 1.. of eg_bfs_batch
+    eg_buf first_in;                  // BFS pull: each vertex's first in-neighbour (0xffffffff: none)
+    const void *first_in_src = nullptr;  // the in-list column array first_in was taken from
     uint64_t spmv_vals_seed;
     int spmv_vals_kind;
     eg_buf bfs_work;  // bitmaps, queues, counters

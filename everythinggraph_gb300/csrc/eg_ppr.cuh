@@ -6,6 +6,8 @@
 #define EG_PPR_LANES 32
 #define EG_PPR_TILE 1024
 #define EG_PPR_NONE 0xffffffffu
+#define EG_PPR_INFLIGHT 8  // row loads in flight per lane in k_ppr_rows
+#define EG_PPR_MINB 4      // resident CTAs per SM asked of the compiler (64 registers)
 
 namespace {
 
@@ -36,8 +38,9 @@ __device__ __forceinline__ float4 eg_f4shfl(unsigned mask, float4 v, int src) {
 // group g walks quarter g of the tile on its own, 8 entries per step with
 // their 8 row loads in flight.  A row is summed in entry order inside a
 // group; a row crossing quarter boundaries is completed by the merge at the
-// end, which adds the groups' parts in quarter order.
-__global__ void __launch_bounds__(256, 3) k_ppr_rows(const uint32_t *__restrict__ rid,
+// end, which adds the groups' parts in quarter order.  EG_PPR_INFLIGHT rows
+// (8 or 4) are loaded before any of them is added.
+__global__ void __launch_bounds__(256, EG_PPR_MINB) k_ppr_rows(const uint32_t *__restrict__ rid,
                                                      const uint32_t *__restrict__ col, uint32_t m, uint32_t ntiles,
                                                      const float *__restrict__ X, float *__restrict__ Y,
                                                      float *__restrict__ head_val, float *__restrict__ tail_val,
@@ -60,22 +63,26 @@ __global__ void __launch_bounds__(256, 3) k_ppr_rows(const uint32_t *__restrict_
     bool fclosed = false;
     float4 fval = zero, acc = zero;
     uint32_t cur = first;
+    constexpr uint32_t NB = EG_PPR_INFLIGHT;
+    static_assert(NB == 4 || NB == 8, "a group's 8 lanes load 8 entries' ids at once");
     for (uint32_t base = S0; base < S1; base += 8) {
         const uint32_t e = base + sl;
         const uint32_t my_r = e < S1 ? __ldg(rid + e) : EG_PPR_NONE;
         const uint32_t my_c = e < S1 ? __ldg(col + e) : 0u;
         const uint32_t cnt = min(8u, S1 - base);
-        uint32_t rr[8];
-        float4 xv[8];
 #pragma unroll
-        for (uint32_t q = 0; q < 8; q++) {
-            rr[q] = __shfl_sync(gmask, my_r, q, 8);
-            const uint32_t u = __shfl_sync(gmask, my_c, q, 8);
-            xv[q] = q < cnt ? __ldg(X4 + (uint64_t)u * (EG_PPR_LANES / 4) + sl) : zero;
+        for (uint32_t h = 0; h < 8; h += NB) {
+        uint32_t rr[NB];
+        float4 xv[NB];
+#pragma unroll
+        for (uint32_t q = 0; q < NB; q++) {
+            rr[q] = __shfl_sync(gmask, my_r, h + q, 8);
+            const uint32_t u = __shfl_sync(gmask, my_c, h + q, 8);
+            xv[q] = h + q < cnt ? __ldg(X4 + (uint64_t)u * (EG_PPR_LANES / 4) + sl) : zero;
         }
 #pragma unroll
-        for (uint32_t q = 0; q < 8; q++) {
-            if (q >= cnt) break;
+        for (uint32_t q = 0; q < NB; q++) {
+            if (h + q >= cnt) break;
             if (rr[q] != cur) {  // row `cur` ended inside the quarter
                 if (cur == first) {
                     fclosed = true;
@@ -87,6 +94,7 @@ __global__ void __launch_bounds__(256, 3) k_ppr_rows(const uint32_t *__restrict_
                 cur = rr[q];
             }
             acc = eg_f4add(acc, xv[q]);
+        }
         }
     }
     // merge the quarters in order: (orow, oval) is the row open so far
