@@ -31,6 +31,7 @@
 #include "eg_internal.cuh"
 
 #define EG_MRELAX_SPARSE 8  // at most this many active sources: edge form
+#define EG_MSSSP_MINB 8     // resident CTAs per SM asked of the compiler for the item kernels (32 registers)
 
 template <class Sink>
 __device__ __forceinline__ void eg_mrelax_rows(uint32_t u, uint32_t p0, uint32_t p1, const uint32_t *__restrict__ col,

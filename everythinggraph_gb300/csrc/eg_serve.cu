@@ -245,7 +245,7 @@ struct SvSink {
     }
 };
 
-__global__ void __launch_bounds__(256) k_sv_sssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+__global__ void __launch_bounds__(256, EG_MSSSP_MINB) k_sv_sssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
                                                       const uint32_t *__restrict__ wts, const uint32_t *__restrict__ queue, const SvCounters *qc,
                                                       uint32_t *dist, const uint32_t *__restrict__ act,
                                                       uint32_t *next_act, uint32_t *next_inq, uint32_t *next_queue,

@@ -304,7 +304,7 @@ struct MsSink {
     __device__ __forceinline__ void any(uint32_t) {}
 };
 
-__global__ void __launch_bounds__(256) k_msssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+__global__ void __launch_bounds__(256, EG_MSSSP_MINB) k_msssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
                                                     const uint32_t *__restrict__ wts, const uint32_t *__restrict__ queue, uint32_t qlen, int k,
                                                     uint32_t kw, uint32_t *dist, const uint32_t *__restrict__ act,
                                                     uint32_t *next_act, uint32_t *next_inq, uint32_t *next_queue,
