@@ -690,7 +690,7 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
     EG_LAUNCHED(ctx);
     uint32_t count = 1, qlen = 1;
     unsigned long long fdeg = 0;
-    EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream));
+    EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream, true));  // and clears them
     EG_CUDA(cudaStreamSynchronize(ctx->stream));
     fdeg = h->next_deg;
     int cur = 0;
@@ -704,7 +704,6 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
         else if (o.direction == EG_BFS_PULL_ONLY) pull = true;
         else pull = (double)count + (double)fdeg > threshold;
         const int nxt = cur ^ 1;
-        EG_TRY(eg_zero(ctx, cnt, sizeof(BfsCounters), ctx->stream));
         if (pull) {
             k_bfs_pull<<<blocks_for(ctx, (uint64_t)nw * 32), 256, 0, ctx->stream>>>(
                 bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col), bp<uint32_t>(g->first_in), deg, n, bm[cur],
@@ -716,10 +715,9 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
             if (!have_queue) {
                 k_bm_queue<<<blocks_for(ctx, (uint64_t)nw * 32), 256, 0, ctx->stream>>>(bm[cur], n, q[cur], &cnt->qsize, 0);
                 EG_LAUNCHED(ctx);
-                EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream));
+                EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream, true));  // and clears them
                 EG_CUDA(cudaStreamSynchronize(ctx->stream));
                 qlen = h->qsize;
-                EG_TRY(eg_zero(ctx, cnt, sizeof(BfsCounters), ctx->stream));
             }
             EG_TRY(eg_zero(ctx, bm[nxt], (uint64_t)nw * 4, ctx->stream));
             // A frontier with fewer vertices than a full grid has warps (the
@@ -752,7 +750,7 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
             }
             have_queue = make_queue;
         }
-        EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream));
+        EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream, true));  // and clears them
         EG_CUDA(cudaStreamSynchronize(ctx->stream));
         count = h->next_count;
         fdeg = h->next_deg;

@@ -52,8 +52,11 @@ extern "C" int eg_open(int device, uint64_t hbm_budget_bytes, eg_ctx **out) {
 }
 
 namespace {
-__global__ void k_readback(const uint32_t *__restrict__ src, uint32_t *dst, uint32_t words) {
-    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) dst[i] = src[i];
+__global__ void k_readback(uint32_t *src, uint32_t *dst, uint32_t words, int clear) {
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) {
+        dst[i] = src[i];
+        if (clear) src[i] = 0u;
+    }
 }
 __global__ void k_zero(uint32_t *p, uint64_t words) {
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < words; i += (uint64_t)gridDim.x * blockDim.x)
@@ -72,13 +75,13 @@ int eg_zero(eg_ctx *c, void *dev, uint64_t bytes, cudaStream_t st) {
     return EG_OK;
 }
 
-int eg_readback(eg_ctx *c, void *host_dst, const void *dev_src, uint32_t bytes, cudaStream_t st) {
+int eg_readback(eg_ctx *c, void *host_dst, const void *dev_src, uint32_t bytes, cudaStream_t st, bool clear) {
     const uintptr_t off = (uintptr_t)host_dst - (uintptr_t)c->h_pinned;
     if ((uintptr_t)host_dst < (uintptr_t)c->h_pinned || off + bytes > (1u << 20) || (off & 3) || ((uintptr_t)dev_src & 3))
         return eg_fail(EG_EINVAL, "readback outside the pinned staging area");
-    k_readback<<<1, 32, 0, st>>>(static_cast<const uint32_t *>(dev_src),
+    k_readback<<<1, 32, 0, st>>>(static_cast<uint32_t *>(const_cast<void *>(dev_src)),
                                  reinterpret_cast<uint32_t *>(static_cast<char *>(c->h_pinned_dev) + off),
-                                 (bytes + 3) / 4);
+                                 (bytes + 3) / 4, clear ? 1 : 0);
     EG_LAUNCHED(c);
     return EG_OK;
 }

@@ -67,7 +67,9 @@ int eg_buf_ensure(eg_ctx *ctx, eg_buf &b, uint64_t bytes);  // grows (contents l
 // one-warp kernel on `st` instead of a copy engine, so that it does not queue
 // behind large copies another stream has on the engine.  Valid on the host
 // after `st` is synchronised.
-int eg_readback(eg_ctx *ctx, void *host_dst, const void *dev_src, uint32_t bytes, cudaStream_t st);
+// With `clear` the kernel also zeroes the device words after reading them.
+int eg_readback(eg_ctx *ctx, void *host_dst, const void *dev_src, uint32_t bytes, cudaStream_t st,
+                bool clear = false);
 // Zeroes `bytes` (a multiple of 4, 4-byte aligned) of device memory with a
 // kernel, for the same reason: a memset may be carried out by a copy engine.
 int eg_zero(eg_ctx *ctx, void *dev, uint64_t bytes, cudaStream_t st);
