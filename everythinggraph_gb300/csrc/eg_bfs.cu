@@ -178,6 +178,119 @@ __global__ void __launch_bounds__(256) k_bfs_push(const uint32_t *__restrict__ p
     block_add_counters(cnt, my_cnt, my_deg);
 }
 
+// Small push levels back to back in one CTA (1024 threads): the root's level
+// and the tail levels after the pull levels have a few hundred to a few
+// thousand frontier vertices, and as separate launches each paid ~25 us of
+// launches and host round trip for a few us of work.  The frontier lives in
+// shared memory (two queues of EG_SMALL_Q ids); a level runs here only while
+// its frontier has at most EG_SMALL_Q vertices and out-edges (so the next
+// frontier, at most one id per edge, always fits) and, in auto mode, the
+// switch rule still asks for push.  Larger caps lose: one SM walking 4K-16K
+// edges per level with dependent claims took longer than a full grid plus
+// its launch overhead (RMAT-24: 1K 0.637 ms per BFS, 4K 0.650, 16K 0.728,
+// none 0.651).  Block barriers only; the frontier is
+// handed back through `queue` and the host loop continues from it.
+#define EG_SMALL_Q 1024u
+struct BfsSmallOut {
+    uint32_t qlen;     // frontier size handed back
+    uint32_t levels;   // levels run
+    int32_t lvl;       // level number of the frontier handed back
+    uint32_t pad;
+    unsigned long long fdeg, reached, traversed;
+};
+
+__global__ void __launch_bounds__(1024) k_bfs_small(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+                                                    const uint32_t *__restrict__ deg, uint32_t *visited,
+                                                    int32_t *level, int32_t *parent, uint32_t *queue, uint32_t qlen,
+                                                    unsigned long long fdeg, int32_t lvl, double threshold,
+                                                    int auto_dir, BfsSmallOut *out) {
+    __shared__ uint32_t s_q[2 * EG_SMALL_Q];
+    __shared__ uint32_t s_n;
+    __shared__ unsigned long long s_deg;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (uint32_t i = threadIdx.x; i < qlen; i += blockDim.x) s_q[i] = queue[i];
+    int c = 0;
+    uint32_t levels = 0;
+    unsigned long long reached = 0, traversed = 0;
+    __syncthreads();
+    for (;;) {
+        if (threadIdx.x == 0) {
+            s_n = 0;
+            s_deg = 0;
+        }
+        __syncthreads();
+        const uint32_t *cq = s_q + (c ? EG_SMALL_Q : 0u);
+        uint32_t *nq = s_q + (c ? 0u : EG_SMALL_Q);
+        const int32_t next_level = lvl + 1;
+        unsigned long long my_deg = 0;
+        for (uint32_t q0 = warp * 32; q0 < qlen; q0 += nwarps * 32) {  // uniform per warp
+            const uint32_t qi = q0 + lane;
+            uint32_t u = 0, b = 0, d = 0;
+            if (qi < qlen) {
+                u = cq[qi];
+                b = ptr[u];
+                d = ptr[u + 1] - b;
+            }
+            eg_warp_lists(u, b, d, [&](bool valid, uint32_t, uint32_t ou, uint32_t p) {
+                bool claimed = false;
+                uint32_t v = 0;
+                if (valid) {
+                    v = col[p];
+                    const uint32_t bit = 1u << (v & 31);
+                    if (!(__ldcg(visited + (v >> 5)) & bit) && !(atomicOr(visited + (v >> 5), bit) & bit)) {
+                        claimed = true;
+                        level[v] = next_level;
+                        if (parent) parent[v] = (int32_t)ou;
+                    }
+                }
+                const uint32_t ball = __ballot_sync(EG_FULL_MASK, claimed);
+                if (ball) {
+                    uint32_t base = 0;
+                    if (lane == 0) base = atomicAdd(&s_n, (uint32_t)__popc(ball));
+                    base = __shfl_sync(EG_FULL_MASK, base, 0);
+                    if (claimed) {
+                        nq[base + __popc(ball & eg_lanemask_lt())] = v;
+                        my_deg += deg[v];
+                    }
+                }
+            });
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) my_deg += __shfl_down_sync(EG_FULL_MASK, my_deg, o);
+        if (lane == 0 && my_deg) atomicAdd(&s_deg, my_deg);
+        __syncthreads();
+        qlen = s_n;
+        fdeg = s_deg;
+        __syncthreads();  // every thread has read s_n and s_deg before the next level resets them
+        levels++;
+        lvl++;
+        reached += qlen;
+        traversed += fdeg;
+        c ^= 1;
+        if (qlen == 0 || qlen > EG_SMALL_Q || fdeg > EG_SMALL_Q ||
+            (auto_dir && (double)qlen + (double)fdeg > threshold))
+            break;
+    }
+    const uint32_t *cq = s_q + (c ? EG_SMALL_Q : 0u);
+    for (uint32_t i = threadIdx.x; i < qlen; i += blockDim.x) queue[i] = cq[i];
+    if (threadIdx.x == 0) {
+        out->qlen = qlen;
+        out->levels = levels;
+        out->lvl = lvl;
+        out->fdeg = fdeg;
+        out->reached = reached;
+        out->traversed = traversed;
+    }
+}
+
+// Frontier queue -> bitmap (the bitmap zeroed before).
+__global__ void k_queue_bm(const uint32_t *__restrict__ queue, uint32_t qlen, uint32_t *bm) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < qlen; i += gridDim.x * blockDim.x) {
+        const uint32_t v = queue[i];
+        atomicOr(bm + (v >> 5), 1u << (v & 31));
+    }
+}
+
 // Expands the deferred high-degree frontier vertices: their out-lists cut
 // into chunks of `chunk` edges (as k_big_offsets counted them), one CTA per
 // chunk.
@@ -630,9 +743,11 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
     EG_TRY(eg_buf_ensure(ctx, lbuf, (uint64_t)n * 4));
     if (want_parent) EG_TRY(eg_buf_ensure(ctx, pbuf, (uint64_t)n * 4));
     // work: visited | bm0 | bm1 | queue0 | queue1 | big list | counters | graph state
+    // (the counters are followed by a BfsSmallOut: 16 words leave room for both)
     const uint64_t off_bm0 = (uint64_t)nw, off_bm1 = 2ull * nw, off_q0 = 3ull * nw, off_q1 = off_q0 + n,
                    off_big = off_q1 + n, off_bigoff = off_big + n, off_cnt = (off_bigoff + n + 1 + 7) & ~7ull,
                    off_st = off_cnt + 16;
+    static_assert(sizeof(BfsCounters) + sizeof(BfsSmallOut) <= 16 * 4, "counter area");
     EG_TRY(eg_buf_ensure(ctx, g->bfs_work, (off_st + 64) * 4));
     uint32_t *wk = bp<uint32_t>(g->bfs_work);
     uint32_t *visited = wk, *bm[2] = {wk + off_bm0, wk + off_bm1}, *q[2] = {wk + off_q0, wk + off_q1};
@@ -698,12 +813,38 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
     int32_t lvl = 1;
     int pull_levels = 0;
     uint64_t reached = 1, traversed = fdeg;
+    bool bm_valid = true;  // bm[cur] holds the frontier (not so after k_bfs_small)
+    BfsSmallOut *hsm = reinterpret_cast<BfsSmallOut *>(h + 1);
+    BfsSmallOut *dsm = reinterpret_cast<BfsSmallOut *>(cnt + 1);
     while (count > 0) {
         bool pull;
         if (o.direction == EG_BFS_PUSH_ONLY) pull = false;
         else if (o.direction == EG_BFS_PULL_ONLY) pull = true;
         else pull = (double)count + (double)fdeg > threshold;
+        if (!pull && have_queue && qlen <= EG_SMALL_Q && fdeg <= EG_SMALL_Q) {
+            // small levels back to back in one CTA
+            k_bfs_small<<<1, 1024, 0, ctx->stream>>>(
+                bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, visited, level, parent, q[cur], qlen, fdeg,
+                lvl, threshold, o.direction == EG_BFS_AUTO ? 1 : 0, dsm);
+            EG_LAUNCHED(ctx);
+            EG_TRY(eg_readback(ctx, hsm, dsm, sizeof(BfsSmallOut), ctx->stream));
+            EG_CUDA(cudaStreamSynchronize(ctx->stream));
+            count = qlen = hsm->qlen;
+            fdeg = hsm->fdeg;
+            reached += hsm->reached;
+            traversed += hsm->traversed;
+            lvl = hsm->lvl;
+            bm_valid = false;
+            if (lvl > (int32_t)n + 1) return eg_fail(EG_ETIMEOUT, "BFS did not terminate");
+            continue;  // the frontier in q[cur] left the small range, needs pull, or is empty
+        }
         const int nxt = cur ^ 1;
+        if (pull && !bm_valid) {  // the frontier is a queue only: set its bits
+            EG_TRY(eg_zero(ctx, bm[cur], (uint64_t)nw * 4, ctx->stream));
+            k_queue_bm<<<blocks_for(ctx, qlen), 256, 0, ctx->stream>>>(q[cur], qlen, bm[cur]);
+            EG_LAUNCHED(ctx);
+        }
+        bm_valid = true;
         if (pull) {
             k_bfs_pull<<<blocks_for(ctx, (uint64_t)nw * 32), 256, 0, ctx->stream>>>(
                 bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col), bp<uint32_t>(g->first_in), deg, n, bm[cur],
