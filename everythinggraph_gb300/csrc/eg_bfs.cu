@@ -324,12 +324,10 @@ __global__ void __launch_bounds__(256) k_bfs_push_big(const uint32_t *__restrict
     block_add_counters(cnt, my_cnt, my_deg);
 }
 
-// An unvisited vertex's bottom-up scan: the first in-neighbour comes from
-// first[] (one coalesced word per vertex: in-lists sorted by source id put
-// the RMAT hubs first, so it is most often the parent), the rest of the list
-// only when that one is not in the frontier.  Sets level and parent of the
-// first in-neighbour (in list order) in the frontier, as a scan of the whole
-// list would.
+// An unvisited vertex's bottom-up scan: first[] (one coalesced word per
+// vertex) names the in-neighbour with the largest out-degree, most often in
+// the frontier; the list is read, in order, only when that one is not.  The
+// parent is that in-neighbour or the first one in list order in the frontier.
 __device__ __forceinline__ bool pull_scan(uint32_t v, const uint32_t *__restrict__ ptr,
                                           const uint32_t *__restrict__ col, const uint32_t *__restrict__ first,
                                           const uint32_t *cur_bm, int32_t *level, int32_t *parent,
@@ -342,7 +340,7 @@ __device__ __forceinline__ bool pull_scan(uint32_t v, const uint32_t *__restrict
     bool hit = (__ldg(cur_bm + (u >> 5)) >> (u & 31)) & 1u;
     if (!hit) {
         const uint32_t e = ptr[v + 1];
-        for (uint32_t p = ptr[v] + 1; p < e; p++) {
+        for (uint32_t p = ptr[v]; p < e; p++) {
             u = col[p];
             if ((__ldg(cur_bm + (u >> 5)) >> (u & 31)) & 1u) {
                 hit = true;
@@ -357,12 +355,28 @@ __device__ __forceinline__ bool pull_scan(uint32_t v, const uint32_t *__restrict
     return hit;
 }
 
-// first[v] = the first entry of v's in-list, EG_NO_VERTEX when it is empty.
-__global__ void k_first_in(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col, uint32_t n,
-                           uint32_t *__restrict__ first) {
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-        const uint32_t b = ptr[v];
-        first[v] = b < ptr[v + 1] ? col[b] : EG_NO_VERTEX;
+// first[v] = v's in-neighbour with the largest out-degree (the smallest id
+// among equals), EG_NO_VERTEX when the in-list is empty: the in-neighbour
+// most likely to be in a large frontier, checked before the list is read.
+// One warp per vertex, 32 entries per step.
+__global__ void k_first_in(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+                           const uint32_t *__restrict__ deg, uint32_t n, uint32_t *__restrict__ first) {
+    const uint32_t lane = threadIdx.x & 31;
+    const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+    for (uint32_t v = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; v < n; v += warps) {
+        const uint32_t b = ptr[v], e = ptr[v + 1];
+        unsigned long long best = 0ull;  // (degree << 32) | ~id: the max is the largest degree, then the smallest id
+        for (uint32_t p = b + lane; p < e; p += 32) {
+            const uint32_t u = col[p];
+            const unsigned long long key = ((unsigned long long)deg[u] << 32) | (uint32_t)~u;
+            best = key > best ? key : best;
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const unsigned long long y = __shfl_down_sync(EG_FULL_MASK, best, o);
+            best = y > best ? y : best;
+        }
+        if (lane == 0) first[v] = b < e ? ~(uint32_t)best : EG_NO_VERTEX;
     }
 }
 
@@ -734,8 +748,8 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
     const uint32_t nw = (n + 31) >> 5;
     if (in_adj && g->first_in_src != in_adj->col.p) {  // once per graph and in-list array
         EG_TRY(eg_buf_ensure(ctx, g->first_in, (uint64_t)n * 4));
-        k_first_in<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col), n,
-                                                              bp<uint32_t>(g->first_in));
+        k_first_in<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
+            bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col), bp<uint32_t>(g->out_deg), n, bp<uint32_t>(g->first_in));
         EG_LAUNCHED(ctx);
         g->first_in_src = in_adj->col.p;
     }
