@@ -25,7 +25,7 @@ struct BfsCounters {
     uint32_t next_count;          // vertices in the new frontier
     uint32_t qsize;               // entries in the next queue
     uint32_t nbig;                // frontier vertices deferred to the cooperative kernel
-    uint32_t pad;
+    uint32_t qbuilt;              // ids written by k_bm_queue (the frontier count is known already)
 };
 
 // Frontier vertices with more out-edges than a threshold are expanded by the
@@ -191,28 +191,66 @@ __global__ void __launch_bounds__(256) k_bfs_push(const uint32_t *__restrict__ p
 // none 0.651).  Block barriers only; the frontier is
 // handed back through `queue` and the host loop continues from it.
 #define EG_SMALL_Q 1024u
+#define EG_FDEG_UNKNOWN (~0ull)
 struct BfsSmallOut {
     uint32_t qlen;     // frontier size handed back
-    uint32_t levels;   // levels run
+    uint32_t levels;   // levels run (0: the incoming frontier was not small)
     int32_t lvl;       // level number of the frontier handed back
     uint32_t pad;
     unsigned long long fdeg, reached, traversed;
+    unsigned long long fdeg_in;  // out-degree sum of the incoming frontier
 };
 
+// fdeg = EG_FDEG_UNKNOWN: the kernel sums the incoming frontier's degrees
+// itself (the root's level, launched right after k_bfs_init without a host
+// round trip).  The level counters `cnt` are cleared for the next level.
 __global__ void __launch_bounds__(1024) k_bfs_small(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
                                                     const uint32_t *__restrict__ deg, uint32_t *visited,
                                                     int32_t *level, int32_t *parent, uint32_t *queue, uint32_t qlen,
                                                     unsigned long long fdeg, int32_t lvl, double threshold,
-                                                    int auto_dir, BfsSmallOut *out) {
+                                                    int auto_dir, BfsSmallOut *out, BfsCounters *cnt) {
     __shared__ uint32_t s_q[2 * EG_SMALL_Q];
     __shared__ uint32_t s_n;
     __shared__ unsigned long long s_deg;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-    for (uint32_t i = threadIdx.x; i < qlen; i += blockDim.x) s_q[i] = queue[i];
+    const bool fits = qlen <= EG_SMALL_Q;
+    if (fits)
+        for (uint32_t i = threadIdx.x; i < qlen; i += blockDim.x) s_q[i] = queue[i];
+    if (threadIdx.x == 0) {
+        s_deg = 0;
+        cnt->next_deg = 0;
+        cnt->next_count = 0;
+        cnt->qsize = 0;
+        cnt->nbig = 0;
+        cnt->qbuilt = 0;
+    }
+    __syncthreads();
+    if (fits && fdeg == EG_FDEG_UNKNOWN) {
+        unsigned long long my = 0;
+        for (uint32_t i = threadIdx.x; i < qlen; i += blockDim.x) my += deg[s_q[i]];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) my += __shfl_down_sync(EG_FULL_MASK, my, o);
+        if (lane == 0 && my) atomicAdd(&s_deg, my);
+        __syncthreads();
+        fdeg = s_deg;
+        __syncthreads();
+    }
+    const unsigned long long fdeg_in = fdeg;
+    if (!fits || fdeg > EG_SMALL_Q || (auto_dir && (double)qlen + (double)fdeg > threshold)) {
+        if (threadIdx.x == 0) {  // not a small level: nothing run
+            out->qlen = qlen;
+            out->levels = 0;
+            out->lvl = lvl;
+            out->fdeg = fdeg;
+            out->reached = 0;
+            out->traversed = 0;
+            out->fdeg_in = fdeg_in;
+        }
+        return;
+    }
     int c = 0;
     uint32_t levels = 0;
     unsigned long long reached = 0, traversed = 0;
-    __syncthreads();
     for (;;) {
         if (threadIdx.x == 0) {
             s_n = 0;
@@ -280,6 +318,7 @@ __global__ void __launch_bounds__(1024) k_bfs_small(const uint32_t *__restrict__
         out->fdeg = fdeg;
         out->reached = reached;
         out->traversed = traversed;
+        out->fdeg_in = fdeg_in;
     }
 }
 
@@ -757,11 +796,11 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
     EG_TRY(eg_buf_ensure(ctx, lbuf, (uint64_t)n * 4));
     if (want_parent) EG_TRY(eg_buf_ensure(ctx, pbuf, (uint64_t)n * 4));
     // work: visited | bm0 | bm1 | queue0 | queue1 | big list | counters | graph state
-    // (the counters are followed by a BfsSmallOut: 16 words leave room for both)
+    // (the counters are followed by a BfsSmallOut: 24 words leave room for both)
     const uint64_t off_bm0 = (uint64_t)nw, off_bm1 = 2ull * nw, off_q0 = 3ull * nw, off_q1 = off_q0 + n,
                    off_big = off_q1 + n, off_bigoff = off_big + n, off_cnt = (off_bigoff + n + 1 + 7) & ~7ull,
-                   off_st = off_cnt + 16;
-    static_assert(sizeof(BfsCounters) + sizeof(BfsSmallOut) <= 16 * 4, "counter area");
+                   off_st = off_cnt + 24;
+    static_assert(sizeof(BfsCounters) + sizeof(BfsSmallOut) <= 24 * 4, "counter area");
     EG_TRY(eg_buf_ensure(ctx, g->bfs_work, (off_st + 64) * 4));
     uint32_t *wk = bp<uint32_t>(g->bfs_work);
     uint32_t *visited = wk, *bm[2] = {wk + off_bm0, wk + off_bm1}, *q[2] = {wk + off_q0, wk + off_q1};
@@ -819,17 +858,35 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
     EG_LAUNCHED(ctx);
     uint32_t count = 1, qlen = 1;
     unsigned long long fdeg = 0;
-    EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream, true));  // and clears them
-    EG_CUDA(cudaStreamSynchronize(ctx->stream));
-    fdeg = h->next_deg;
     int cur = 0;
     bool have_queue = true;  // q[cur] lists the frontier
     int32_t lvl = 1;
     int pull_levels = 0;
-    uint64_t reached = 1, traversed = fdeg;
+    uint64_t reached = 1, traversed = 0;
     bool bm_valid = true;  // bm[cur] holds the frontier (not so after k_bfs_small)
     BfsSmallOut *hsm = reinterpret_cast<BfsSmallOut *>(h + 1);
     BfsSmallOut *dsm = reinterpret_cast<BfsSmallOut *>(cnt + 1);
+    if (o.direction != EG_BFS_PULL_ONLY) {
+        // the root's level goes straight to the small-level kernel, which
+        // finds the root's degree itself (no round trip after k_bfs_init)
+        k_bfs_small<<<1, 1024, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, visited,
+                                                 level, parent, q[0], 1u, EG_FDEG_UNKNOWN, 1, threshold,
+                                                 o.direction == EG_BFS_AUTO ? 1 : 0, dsm, cnt);
+        EG_LAUNCHED(ctx);
+        EG_TRY(eg_readback(ctx, hsm, dsm, sizeof(BfsSmallOut), ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        count = qlen = hsm->qlen;
+        fdeg = hsm->fdeg;
+        reached += hsm->reached;
+        traversed = hsm->fdeg_in + hsm->traversed;
+        lvl = hsm->lvl;
+        bm_valid = hsm->levels == 0;  // else bm[0] still holds only the root
+    } else {
+        EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream, true));  // and clears them
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        fdeg = h->next_deg;
+        traversed = fdeg;
+    }
     while (count > 0) {
         bool pull;
         if (o.direction == EG_BFS_PUSH_ONLY) pull = false;
@@ -839,7 +896,7 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
             // small levels back to back in one CTA
             k_bfs_small<<<1, 1024, 0, ctx->stream>>>(
                 bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, visited, level, parent, q[cur], qlen, fdeg,
-                lvl, threshold, o.direction == EG_BFS_AUTO ? 1 : 0, dsm);
+                lvl, threshold, o.direction == EG_BFS_AUTO ? 1 : 0, dsm, cnt);
             EG_LAUNCHED(ctx);
             EG_TRY(eg_readback(ctx, hsm, dsm, sizeof(BfsSmallOut), ctx->stream));
             EG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -867,12 +924,11 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
             pull_levels++;
             have_queue = false;
         } else {
-            if (!have_queue) {
-                k_bm_queue<<<blocks_for(ctx, (uint64_t)nw * 32), 256, 0, ctx->stream>>>(bm[cur], n, q[cur], &cnt->qsize, 0);
+            if (!have_queue) {  // the queue from the bitmap; its length is the frontier count
+                k_bm_queue<<<blocks_for(ctx, (uint64_t)nw * 32), 256, 0, ctx->stream>>>(bm[cur], n, q[cur],
+                                                                                       &cnt->qbuilt, 0);
                 EG_LAUNCHED(ctx);
-                EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream, true));  // and clears them
-                EG_CUDA(cudaStreamSynchronize(ctx->stream));
-                qlen = h->qsize;
+                qlen = count;
             }
             EG_TRY(eg_zero(ctx, bm[nxt], (uint64_t)nw * 4, ctx->stream));
             // A frontier with fewer vertices than a full grid has warps (the
