@@ -251,13 +251,16 @@ class Graph:
         L.check(lib().eg_pagerank(self._h, ctypes.byref(o), _ptr(out), ctypes.byref(st)))
         return out, st
 
-    def spmv(self, x, kind="u32_pull", value_seed=0, unit_values=False, copy_out=True, grid=False):
+    def spmv(self, x, kind="u32_pull", value_seed=0, unit_values=False, copy_out=True, grid=False,
+             source_block_log2=0):
+        """source_block_log2: fp32 over graphs with more vertices than 2^k
+        runs one pass per source block of 2^k vertices (0: k = 24)."""
         k = SPMV_KINDS[kind]
         xd = np.uint32 if kind.startswith("u32") else np.float32
         x = np.ascontiguousarray(x, dtype=xd)
         yd = np.float64 if kind == "f64" else xd
         y = np.empty(self.n, dtype=yd) if copy_out else None
-        o = L.SpmvOpts(k, value_seed, int(unit_values), int(grid))
+        o = L.SpmvOpts(k, value_seed, int(unit_values), int(grid), int(source_block_log2))
         ms = ctypes.c_float()
         L.check(lib().eg_spmv(self._h, ctypes.byref(o), _ptr(x), _ptr(y), ctypes.byref(ms)))
         return y, ms.value

@@ -53,7 +53,8 @@ class TuneResult(ctypes.Structure):
 
 
 class SpmvOpts(ctypes.Structure):
-    _fields_ = [("kind", c_int), ("value_seed", c_u64), ("unit_values", c_int), ("grid", c_int)]
+    _fields_ = [("kind", c_int), ("value_seed", c_u64), ("unit_values", c_int), ("grid", c_int),
+                ("source_block_log2", c_int)]
 
 
 class BfsOpts(ctypes.Structure):

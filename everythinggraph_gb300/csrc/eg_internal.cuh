@@ -38,6 +38,7 @@ void eg_clear_error();
 // ---------------------------------------------------------------- context
 #define EG_KEV 8        // kernel launches timed individually per call
 #define EG_OUT_SLOTS 4  // device output slots of eg_bfs_batch (copy-out pipeline depth)
+#define EG_SB_MAX 64    // source blocks of the blocked CSC at most
 struct eg_ctx {
     int device;
     int sm_count;
@@ -128,6 +129,16 @@ struct eg_graph {
     const void *first_in_src = nullptr;  // the in-list column array first_in was taken from
     uint64_t spmv_vals_seed;
     int spmv_vals_kind;
+    // source-blocked copy of the CSC (fp32 SpMV over an x larger than L2):
+    // block b holds the sb_len[b] entries with source in [b << sb_shift,
+    // (b+1) << sb_shift), in CSC order, from entry sb_start[b] (a multiple of
+    // 4: the row kernel reads 16-byte vectors from the block's base);
+    // sb_ptr holds one row-pointer array of n + 1 per block
+    uint32_t sb_shift = 0, sb_blocks = 0;
+    eg_buf sb_ptr, sb_rid, sb_col, sb_perm, sb_vals, sb_yerr;
+    uint64_t sb_start[EG_SB_MAX] = {}, sb_len[EG_SB_MAX] = {};
+    int sb_vals_kind = 0;
+    uint64_t sb_vals_seed = 0;
     eg_buf bfs_work;  // bitmaps, queues, counters
     eg_buf msbfs_work;
     eg_buf sssp_work;

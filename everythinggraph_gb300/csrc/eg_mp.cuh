@@ -417,6 +417,14 @@ __device__ __forceinline__ uint4 eg_stream_ld4(const uint32_t *p, uint64_t pol) 
     }
 }
 
+// One streamed 4-byte value (read once per pass): not kept in L1, first in
+// line for L2 eviction, so the caches stay with the gathered vector.
+__device__ __forceinline__ float eg_stream_ldf(const float *p, uint64_t pol) {
+    float v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
 __device__ __forceinline__ uint64_t eg_l2_evict_first_policy() {
     uint64_t pol;
     asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));

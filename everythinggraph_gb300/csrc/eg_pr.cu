@@ -233,6 +233,8 @@ __global__ void k_pr_reduce(const double2 *__restrict__ part, uint32_t nparts, e
 // keeps the streamed row ids and columns out of L1 and first in line for L2
 // eviction.
 #define EG_COO_TILE_MIN 512
+#define EG_ALL_ENTRIES (~0ull)
+#define EG_SB_LOG2 24  // source-block size by default: 2^24 vertices, a 64 MB slice of x
 #define EG_PR_CHECK 4  // iterations between reads of the stop flag
 #define EG_PR_RES_BLOCKS 1024
 #define EG_ROW_CFGS 12
@@ -250,10 +252,10 @@ static const RowCfg kRowCfg[EG_ROW_CFGS] = {
 
 template <class Op, int TILE, int U, bool REDUCE, int PF, int MINB, int HINT = 0>
 static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts,
-                        cudaEvent_t ev_begin, cudaEvent_t ev_end) {
+                        cudaEvent_t ev_begin, cudaEvent_t ev_end, uint64_t m_entries, bool empty_rows) {
     eg_ctx *ctx = g->ctx;
     using A = typename Op::A;
-    const uint32_t m = (uint32_t)g->m;
+    const uint32_t m = (uint32_t)(m_entries == EG_ALL_ENTRIES ? g->m : m_entries);
     const uint32_t ntiles = m ? eg_div_up(m, TILE) : 0;
     EG_TRY(eg_buf_ensure(ctx, carry_buf, ((uint64_t)ntiles + 1) * sizeof(eg_mp_carry<A>)));
     const uint32_t gf = ntiles ? eg_div_up((uint64_t)ntiles * 32, 256) : 0;  // one warp per tile
@@ -267,9 +269,11 @@ static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *pa
         EG_LAUNCHED(ctx);
         if (ev_end) EG_CUDA(cudaEventRecord(ev_end, ctx->stream));
     }
-    k_coo_empty_rows<Op, REDUCE><<<g2, 256, 0, ctx->stream>>>(bp<uint32_t>(adj.ptr), g->n, part ? part + g1 : nullptr,
-                                                              op);
-    EG_LAUNCHED(ctx);
+    if (empty_rows) {
+        k_coo_empty_rows<Op, REDUCE><<<g2, 256, 0, ctx->stream>>>(bp<uint32_t>(adj.ptr), g->n,
+                                                                  part ? part + g1 : nullptr, op);
+        EG_LAUNCHED(ctx);
+    }
     if (gf) {
         k_coo_fixup<Op, TILE, REDUCE><<<gf, 256, 0, ctx->stream>>>(
             bp<uint32_t>(adj.ptr), ntiles, bp<eg_mp_carry<A>>(carry_buf), part ? part + g1 + g2 : nullptr, op);
@@ -279,11 +283,16 @@ static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *pa
     return EG_OK;
 }
 
+// m_entries: the entries of `adj` (EG_ALL_ENTRIES: the graph's m); without
+// empty_rows the rows that have no entries in `adj` are left as they are.
 template <class Op, bool REDUCE>
 static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts,
-                      cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr) {
-#define EG_ROW_CASE(i, T, U, PF, MB, H) \
-    case i: return coo_launch_t<Op, T, U, REDUCE, PF, MB, H>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
+                      cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr,
+                      uint64_t m_entries = EG_ALL_ENTRIES, bool empty_rows = true) {
+#define EG_ROW_CASE(i, T, U, PF, MB, H)                                                                         \
+    case i:                                                                                                     \
+        return coo_launch_t<Op, T, U, REDUCE, PF, MB, H>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end, \
+                                                          m_entries, empty_rows);
     switch (g->row_cfg) {
         EG_ROW_CASE(1, 2048, 4, false, 6, 0)
         EG_ROW_CASE(2, 2048, 4, true, 5, 0)
@@ -296,7 +305,9 @@ static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part
         EG_ROW_CASE(9, 2048, 4, true, 5, 1)
         EG_ROW_CASE(10, 1024, 4, 2, 4, 0)
         EG_ROW_CASE(11, 2048, 4, 2, 4, 0)
-        default: return coo_launch_t<Op, 1024, 4, REDUCE, true, 5>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end);
+        default:
+            return coo_launch_t<Op, 1024, 4, REDUCE, true, 5>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end,
+                                                              m_entries, empty_rows);
     }
 #undef EG_ROW_CASE
 }
@@ -645,9 +656,14 @@ struct SpmvF32Op {
     const float *__restrict__ x;
     const float *__restrict__ vals;
     float *__restrict__ y;
+    int accum;     // 1: y[v] += the row sum (source blocks after the first)
+    uint64_t pol;  // L2 evict-first for the streamed values
+    float *yerr;   // COMP over source blocks: the rows' error terms between passes
     __device__ __forceinline__ bool active() const { return true; }
-    __device__ __forceinline__ void setup() {}
-    __device__ __forceinline__ V gather(uint32_t j, uint32_t u) const { return __fmul_rn(__ldg(vals + j), __ldg(x + u)); }
+    __device__ __forceinline__ void setup() { pol = eg_l2_evict_first_policy(); }
+    __device__ __forceinline__ V gather(uint32_t j, uint32_t u) const {
+        return __fmul_rn(eg_stream_ldf(vals + j, pol), __ldg(x + u));
+    }
     __device__ __forceinline__ A zero() const {
         if constexpr (COMP) return make_float2(0.f, 0.f);
         else return 0.f;
@@ -661,8 +677,18 @@ struct SpmvF32Op {
         else return a + b;
     }
     __device__ __forceinline__ float2 emit(uint32_t v, A s) const {
-        if constexpr (COMP) y[v] = s.x + s.y;
-        else y[v] = s;
+        if constexpr (COMP) {
+            float2 t = s;
+            if (accum) t = eg_f2sum::merge(make_float2(y[v], yerr[v]), t);
+            if (yerr) {  // the pair goes on to the next block (k_pair_finish adds it up)
+                y[v] = t.x;
+                yerr[v] = t.y;
+            } else {
+                y[v] = t.x + t.y;
+            }
+        } else {
+            y[v] = accum ? y[v] + s : s;
+        }
         return make_float2(0.f, 0.f);
     }
 };
@@ -673,10 +699,11 @@ struct SpmvF64Op {
     const float *__restrict__ x;
     const float *__restrict__ vals;
     double *__restrict__ y;
+    uint64_t pol;  // L2 evict-first for the streamed values
     __device__ __forceinline__ bool active() const { return true; }
-    __device__ __forceinline__ void setup() {}
+    __device__ __forceinline__ void setup() { pol = eg_l2_evict_first_policy(); }
     __device__ __forceinline__ V gather(uint32_t j, uint32_t u) const {
-        return __dmul_rn((double)__ldg(vals + j), (double)__ldg(x + u));
+        return __dmul_rn((double)eg_stream_ldf(vals + j, pol), (double)__ldg(x + u));
     }
     __device__ __forceinline__ A zero() const { return 0.0; }
     __device__ __forceinline__ A add(A a, V v) const { return __dadd_rn(a, v); }
@@ -698,6 +725,173 @@ __global__ void k_csc_values(const uint32_t *__restrict__ ptr, const uint32_t *_
             if (unit) vals[p] = 1.0f;
             else vals[p] = (float)(eg_edge_hash(seed, col[p], v) >> 40) * (1.0f / 16777216.0f);
         }
+}
+
+// ---- source-blocked CSC for fp32 SpMV over an x larger than L2
+// With x beyond L2 (ER 2^25: 134 MB) every gather that misses goes to DRAM at
+// random.  The CSC's entries are split by source block (a stable sort on
+// source >> shift keeps CSC order inside a block), each block with its own
+// row pointers; one row-kernel pass per block then gathers from an x slice
+// that L2 holds: the first pass writes y, the others add to it.
+namespace {
+__global__ void k_sb_keys(const uint32_t *__restrict__ col, uint64_t M, uint32_t shift, uint32_t *keys,
+                          uint32_t *idx) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < M; i += (uint64_t)gridDim.x * blockDim.x) {
+        keys[i] = col[i] >> shift;
+        idx[i] = (uint32_t)i;
+    }
+}
+__global__ void k_sb_gather(const uint32_t *__restrict__ perm, const uint32_t *__restrict__ rid,
+                            const uint32_t *__restrict__ col, uint64_t M, uint32_t *orid, uint32_t *ocol) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < M; i += (uint64_t)gridDim.x * blockDim.x) {
+        const uint32_t e = perm[i];
+        orid[i] = rid[e];
+        ocol[i] = col[e];
+    }
+}
+__global__ void k_pair_finish(float *y, const float *__restrict__ err, uint32_t n) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) y[v] = y[v] + err[v];
+}
+__global__ void k_sb_vals(const uint32_t *__restrict__ perm, const float *__restrict__ vals, uint64_t M,
+                          float *out) {
+    for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < M; i += (uint64_t)gridDim.x * blockDim.x)
+        out[i] = vals[perm[i]];
+}
+}  // namespace
+
+static uint32_t sb_grid(eg_ctx *ctx, uint64_t work) {
+    uint64_t b = (work + 255) / 256;
+    const uint64_t cap = (uint64_t)ctx->sm_count * 8;
+    return (uint32_t)(b > cap ? cap : (b ? b : 1));
+}
+
+static int sb_prepare(eg_graph *g, uint32_t shift) {
+    if (g->sb_blocks && g->sb_shift == shift) return EG_OK;
+    eg_ctx *ctx = g->ctx;
+    const uint32_t n = g->n;
+    const uint64_t M = g->m;
+    const uint32_t B = (uint32_t)(((uint64_t)n + (1ull << shift) - 1) >> shift);
+    if (B > EG_SB_MAX) return eg_fail(EG_EINVAL, "source blocks of 2^%u vertices: %u blocks, at most %d", shift, B, EG_SB_MAX);
+    g->sb_blocks = 0;
+    eg_buf ka, va, kb, vb, cnt;
+    int rc = EG_OK;
+    auto cleanup = [&]() {
+        cudaStreamSynchronize(ctx->stream);
+        eg_buf_free(ctx, ka);
+        eg_buf_free(ctx, va);
+        eg_buf_free(ctx, kb);
+        eg_buf_free(ctx, vb);
+        eg_buf_free(ctx, cnt);
+    };
+#define STRY(x)            \
+    do {                   \
+        rc = (x);          \
+        if (rc != EG_OK) { \
+            cleanup();     \
+            return rc;     \
+        }                  \
+    } while (0)
+    STRY(eg_buf_ensure(ctx, ka, (M + 1) * 4));
+    STRY(eg_buf_ensure(ctx, va, (M + 1) * 4));
+    STRY(eg_buf_ensure(ctx, kb, (M + 1) * 4));
+    STRY(eg_buf_ensure(ctx, vb, (M + 1) * 4));
+    STRY(eg_buf_ensure(ctx, cnt, ((uint64_t)n + EG_SB_MAX + 1) * 4));
+    const uint64_t MP = M + 4ull * EG_SB_MAX;  // room for the blocks' alignment padding
+    STRY(eg_buf_ensure(ctx, g->sb_rid, MP * 4 + 16));
+    STRY(eg_buf_ensure(ctx, g->sb_col, MP * 4 + 16));
+    STRY(eg_buf_ensure(ctx, g->sb_perm, MP * 4 + 16));
+    STRY(eg_buf_ensure(ctx, g->sb_ptr, (uint64_t)B * ((uint64_t)n + 1) * 4));
+    uint32_t *ks = bp<uint32_t>(ka), *vs = bp<uint32_t>(va);
+    if (M) {
+        k_sb_keys<<<sb_grid(ctx, M), 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.col), M, shift, bp<uint32_t>(ka),
+                                                            bp<uint32_t>(va));
+        EG_LAUNCHED(ctx);
+        const int bits = B <= 1 ? 1 : 32 - __builtin_clz(B - 1);
+        STRY(eg_radix_sort(ctx, bp<uint32_t>(ka), bp<uint32_t>(va), bp<uint32_t>(kb), bp<uint32_t>(vb), M, bits, &ks,
+                           &vs));
+    }
+    // entries per block (sorted by block: block b is vs[s_b, s_b + len_b))
+    uint32_t *bcnt = bp<uint32_t>(cnt) + n;
+    if (cudaMemsetAsync(bcnt, 0, (EG_SB_MAX + 1) * 4, ctx->stream) != cudaSuccess) STRY(eg_fail(EG_ECUDA, "memset"));
+    STRY(eg_histogram(ctx, ks, M, bcnt));
+    uint32_t hc[EG_SB_MAX + 1];
+    if (cudaMemcpyAsync(hc, bcnt, (EG_SB_MAX + 1) * 4, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        STRY(eg_fail(EG_ECUDA, "source-block counts"));
+    uint64_t sorted_at = 0, placed_at = 0;
+    for (uint32_t b = 0; b < B; b++) {
+        const uint64_t len = hc[b];
+        g->sb_start[b] = placed_at;  // a multiple of 4 entries
+        g->sb_len[b] = len;
+        if (len) {
+            k_sb_gather<<<sb_grid(ctx, len), 256, 0, ctx->stream>>>(
+                vs + sorted_at, bp<uint32_t>(g->csc.rid), bp<uint32_t>(g->csc.col), len,
+                bp<uint32_t>(g->sb_rid) + placed_at, bp<uint32_t>(g->sb_col) + placed_at);
+            EG_LAUNCHED(ctx);
+            if (cudaMemcpyAsync(bp<uint32_t>(g->sb_perm) + placed_at, vs + sorted_at, len * 4, cudaMemcpyDeviceToDevice,
+                                ctx->stream) != cudaSuccess)
+                STRY(eg_fail(EG_ECUDA, "source-block copy"));
+        }
+        // the block's row pointers: histogram of its rows, exclusive scan
+        if (cudaMemsetAsync(cnt.p, 0, (uint64_t)n * 4, ctx->stream) != cudaSuccess) STRY(eg_fail(EG_ECUDA, "memset"));
+        STRY(eg_histogram(ctx, bp<uint32_t>(g->sb_rid) + placed_at, len, bp<uint32_t>(cnt)));
+        STRY(eg_exscan_u32(ctx, bp<uint32_t>(cnt), bp<uint32_t>(g->sb_ptr) + (uint64_t)b * ((uint64_t)n + 1), n));
+        sorted_at += len;
+        placed_at = (placed_at + len + 3) & ~3ull;
+    }
+    cleanup();
+#undef STRY
+    g->sb_shift = shift;
+    g->sb_blocks = B;
+    g->sb_vals_kind = 0;
+    return EG_OK;
+}
+
+// fp32 SpMV over the source blocks (values already in g->spmv_vals, CSC
+// order): one pass per block, the first writing y, the others adding to it
+// (EG_SPMV_F32_COMP carries each row's (sum, error) pair between passes).
+static int sb_spmv(eg_graph *g, int kind, int vk, uint64_t seed) {
+    eg_ctx *ctx = g->ctx;
+    const uint32_t n = g->n;
+    const uint64_t M = g->m;
+    if (g->sb_vals_kind != vk || (vk == 2 && g->sb_vals_seed != seed)) {
+        EG_TRY(eg_buf_ensure(ctx, g->sb_vals, (M + 4ull * EG_SB_MAX) * 4 + 16));
+        for (uint32_t b = 0; b < g->sb_blocks; b++) {
+            const uint64_t s0 = g->sb_start[b], len = g->sb_len[b];
+            if (!len) continue;
+            k_sb_vals<<<sb_grid(ctx, len), 256, 0, ctx->stream>>>(bp<uint32_t>(g->sb_perm) + s0,
+                                                                  bp<float>(g->spmv_vals), len,
+                                                                  bp<float>(g->sb_vals) + s0);
+            EG_LAUNCHED(ctx);
+        }
+        g->sb_vals_kind = vk;
+        g->sb_vals_seed = seed;
+    }
+    if (kind == EG_SPMV_F32_COMP) EG_TRY(eg_buf_ensure(ctx, g->sb_yerr, (uint64_t)n * 4));
+    uint32_t np = 0;
+    for (uint32_t b = 0; b < g->sb_blocks; b++) {
+        const uint64_t s0 = g->sb_start[b], len = g->sb_len[b];
+        eg_adj view;  // pointers into the blocked arrays (owned by the graph)
+        view.ptr.p = bp<uint32_t>(g->sb_ptr) + (uint64_t)b * ((uint64_t)n + 1);
+        view.col.p = bp<uint32_t>(g->sb_col) + s0;
+        view.rid.p = bp<uint32_t>(g->sb_rid) + s0;
+        const int acc = b > 0 ? 1 : 0;
+        if (kind == EG_SPMV_F32) {
+            SpmvF32Op<false> op{bp<float>(g->spmv_x), bp<float>(g->sb_vals) + s0, bp<float>(g->spmv_y), acc};
+            EG_TRY((coo_launch<SpmvF32Op<false>, false>(g, view, g->mp_carry, nullptr, op, &np, nullptr, nullptr, len,
+                                                         b == 0)));
+        } else {
+            SpmvF32Op<true> op{bp<float>(g->spmv_x), bp<float>(g->sb_vals) + s0, bp<float>(g->spmv_y), acc, 0,
+                               bp<float>(g->sb_yerr)};
+            EG_TRY((coo_launch<SpmvF32Op<true>, false>(g, view, g->mp_carry, nullptr, op, &np, nullptr, nullptr, len,
+                                                        b == 0)));
+        }
+    }
+    if (kind == EG_SPMV_F32_COMP) {
+        k_pair_finish<<<sb_grid(ctx, n), 256, 0, ctx->stream>>>(bp<float>(g->spmv_y), bp<float>(g->sb_yerr), n);
+        EG_LAUNCHED(ctx);
+    }
+    return EG_OK;
 }
 
 extern "C" int eg_spmv(eg_graph *g, const eg_spmv_opts *opts, const void *x, void *y, float *ms) {
@@ -736,6 +930,12 @@ extern "C" int eg_spmv(eg_graph *g, const eg_spmv_opts *opts, const void *x, voi
             g->spmv_vals_seed = opts->value_seed;
         }
     }
+    // fp32 kinds over x beyond the source-block size: the source-blocked CSC
+    const uint32_t sb_log2 = opts->source_block_log2 ? (uint32_t)opts->source_block_log2 : EG_SB_LOG2;
+    // (not FP64: its time is in the FP64 arithmetic, which a second pass only adds to)
+    const bool blocked = (kind == EG_SPMV_F32 || kind == EG_SPMV_F32_COMP) && sb_log2 < 32 &&
+                         (uint64_t)n > (1ull << sb_log2);
+    if (blocked) EG_TRY(sb_prepare(g, sb_log2));
     eg_buf &carry = g->mp_carry;
     uint32_t np = 0;
     EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
@@ -752,12 +952,20 @@ extern "C" int eg_spmv(eg_graph *g, const eg_spmv_opts *opts, const void *x, voi
             break;
         }
         case EG_SPMV_F32: {
-            SpmvF32Op<false> op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<float>(g->spmv_y)};
+            if (blocked) {
+                EG_TRY(sb_spmv(g, kind, opts->unit_values ? 1 : 2, opts->value_seed));
+                break;
+            }
+            SpmvF32Op<false> op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<float>(g->spmv_y), 0};
             EG_TRY((coo_launch<SpmvF32Op<false>, false>(g, adj, carry, nullptr, op, &np)));
             break;
         }
         case EG_SPMV_F32_COMP: {
-            SpmvF32Op<true> op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<float>(g->spmv_y)};
+            if (blocked) {
+                EG_TRY(sb_spmv(g, kind, opts->unit_values ? 1 : 2, opts->value_seed));
+                break;
+            }
+            SpmvF32Op<true> op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<float>(g->spmv_y), 0};
             EG_TRY((coo_launch<SpmvF32Op<true>, false>(g, adj, carry, nullptr, op, &np)));
             break;
         }

@@ -225,6 +225,11 @@ typedef struct {
     int grid;            /* 1: over the 2-D grid layout (spmv.c's grid modes):
                             cells in L2-sized blocks, y by atomic adds (u32
                             exact; f32/f64 not in a fixed order; no F32_COMP) */
+    int source_block_log2; /* EG_SPMV_F32(_COMP) with n > 2^k (k = this, 0: 24):
+                            the entries are split by source block of 2^k
+                            vertices (a copy of the CSC built once) and summed
+                            one block per pass, so each pass gathers from an
+                            x slice that L2 holds; a fixed order */
 } eg_spmv_opts;
 /* x: host array of n (u32 for U32 kinds, f32 otherwise); y: host array of n
  * (u32, f32 or f64 for EG_SPMV_F64), or NULL to keep y on the device. */

@@ -265,6 +265,40 @@ def test_spmv_float_vs_fp64(case):
         assert np.all(y[~nz] == 0)
 
 
+def test_spmv_source_blocks(case):
+    # fp32 SpMV one source block per pass (blocks of 2^k vertices; the default
+    # 2^24 only splits larger graphs): within the FP64 tolerance, rows without
+    # entries zero, values re-gathered when the seed or the rule changes
+    name, n, pairs, rec, g, gu, adj, adju = case
+    x = oracle.uniform_f32(n, 11)
+    for seed in (9, 3):
+        vals = oracle.hash_values(adj.in_col, adj.in_dst(), seed)
+        ref = oracle.spmv_f64(n, adj.in_ptr, adj.in_col, vals, x)
+        nz = ref != 0
+        y_one, _ = g.spmv(x, "f32", value_seed=seed)
+        for k in (10, 3, 2):
+            if n > (64 << k):  # at most 64 blocks
+                continue
+            y, _ = g.spmv(x, "f32", value_seed=seed, source_block_log2=k)
+            l1, mx = rel_errors(y[nz], ref[nz])
+            assert l1 <= 1e-6 and mx <= 1e-5, (k, l1, mx)
+            assert np.all(y[~nz] == 0)
+            if n <= (1 << k):  # one block: the same pass as without blocks
+                np.testing.assert_array_equal(y, y_one)
+            y2, _ = g.spmv(x, "f32", value_seed=seed, source_block_log2=k)
+            np.testing.assert_array_equal(y, y2)  # a fixed order
+            yc, _ = g.spmv(x, "f32_comp", value_seed=seed, source_block_log2=k)
+            l1, mx = rel_errors(yc[nz], ref[nz])
+            assert l1 <= 1e-6 and mx <= 1e-5, ("comp", k, l1, mx)
+            assert np.all(yc[~nz] == 0)
+    ones = oracle.spmv_f64(n, adj.in_ptr, adj.in_col, np.ones(adj.m, np.float32), x)
+    k = max(2, int(np.ceil(np.log2(max(n, 2)))) - 2)
+    y, _ = g.spmv(x, "f32", unit_values=True, source_block_log2=k)
+    nz = ones != 0
+    l1, mx = rel_errors(y[nz], ones[nz])
+    assert l1 <= 1e-6 and mx <= 1e-5, (l1, mx)
+
+
 # ------------------------------------------------------------------ BFS
 def test_bfs_levels_bit_exact(case):
     name, n, pairs, rec, g, gu, adj, adju = case
