@@ -239,13 +239,14 @@ class Graph:
 
     # ---------------------------------------------------------------- algorithms
     def pagerank(self, iterations=10, damping=0.85, prev_init=-1.0, swap=True, deg_multiplier=1, dangling=False,
-                 compensated=False, tolerance=0.0, copy_out=True, use_graph=False, grid=False):
+                 compensated=False, tolerance=0.0, copy_out=True, use_graph=False, grid=False, source_block_log2=0):
         o = L.PrOpts()
         lib().eg_pr_opts_default(ctypes.byref(o))
         o.iterations, o.damping, o.prev_init, o.swap = iterations, damping, prev_init, int(swap)
         o.deg_multiplier, o.dangling, o.compensated, o.tolerance = deg_multiplier, int(dangling), int(compensated), tolerance
         o.use_graph = int(use_graph)
         o.grid = int(grid)
+        o.source_block_log2 = int(source_block_log2)
         st = L.PrStats()
         out = np.empty(self.n, dtype=np.float32) if copy_out else None
         L.check(lib().eg_pagerank(self._h, ctypes.byref(o), _ptr(out), ctypes.byref(st)))

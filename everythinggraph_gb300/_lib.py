@@ -33,7 +33,7 @@ class GraphInfo(ctypes.Structure):
 class PrOpts(ctypes.Structure):
     _fields_ = [("iterations", c_int), ("damping", c_f32), ("prev_init", c_f32), ("swap", c_int),
                 ("deg_multiplier", c_u32), ("dangling", c_int), ("compensated", c_int), ("tolerance", c_f64),
-                ("use_graph", c_int), ("grid", c_int)]
+                ("use_graph", c_int), ("grid", c_int), ("source_block_log2", c_int)]
 
 
 class PrStats(ctypes.Structure):

@@ -352,8 +352,9 @@ extern "C" void eg_graph_free(eg_graph *g) {
                       &g->rank,    &g->contrib0,     &g->contrib1,
                       &g->pr_part,      &g->pr_stats,    &g->mp_carry,    &g->errflag,     &g->rank_p,    &g->rank_q,    &g->level,          &g->parent,       &g->dist,
                       &g->level_s[0],   &g->level_s[1],  &g->level_s[2],  &g->parent_s[0], &g->parent_s[1],
-                      &g->parent_s[2],   &g->first_in,    &g->sb_ptr,      &g->sb_rid,      &g->sb_col,
-                      &g->sb_perm,       &g->sb_vals,     &g->sb_yerr,
+                      &g->parent_s[2],   &g->first_in,    &g->sb.ptr,      &g->sb.rid,      &g->sb.col,
+                      &g->sb.perm,       &g->sb.vals,     &g->sb.yerr,     &g->sbp.ptr,     &g->sbp.rid,
+                      &g->sbp.col,       &g->sbp.perm,    &g->sbp.vals,    &g->sbp.yerr,    &g->pr_acc,
                       &g->label,        &g->spmv_x,      &g->spmv_y,      &g->spmv_vals,      &g->bfs_work,     &g->msbfs_work,
                       &g->sssp_work,    &g->ppr_work,    &g->wts,
                       &g->grid_order,   &g->grid_units,  &g->grid_off,    &g->grid_vals,   &g->grid_acc};
@@ -747,8 +748,10 @@ static int build_adj_pair(eg_graph *g, bool want_csc) {
             BTRY(eg_fail(EG_ECUDA, "copy rid"));
         g->built |= EG_LAYOUT_CSC;
         g->first_in_src = nullptr;
-        g->sb_blocks = 0;  // the source-blocked copy follows the CSC
-        g->sb_shift = 0;
+        g->sb.blocks = 0;  // the source-blocked copies follow the CSC
+        g->sb.shift = 0;
+        g->sbp.blocks = 0;
+        g->sbp.shift = 0;
     }
     if (cudaStreamSynchronize(ctx->stream) != cudaSuccess)
         BTRY(eg_fail(EG_ECUDA, "build: %s", cudaGetErrorString(cudaGetLastError())));

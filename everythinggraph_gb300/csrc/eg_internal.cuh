@@ -96,6 +96,20 @@ struct eg_bfs_graph {
     const void *key[8] = {};
 };
 
+// A copy of an adjacency with its entries split by source block (for row
+// sums over an x larger than L2): block b holds the len[b] entries with
+// source in [b << shift, (b+1) << shift), in the adjacency's order, from
+// entry start[b] (a multiple of 4: the row kernel reads 16-byte vectors from
+// the block's base); ptr holds one row-pointer array of n + 1 per block;
+// perm[i] is the adjacency entry placed at i (for values kept per entry).
+struct eg_sblocks {
+    uint32_t shift = 0, blocks = 0;
+    eg_buf ptr, rid, col, perm, vals, yerr;
+    uint64_t start[EG_SB_MAX] = {}, len[EG_SB_MAX] = {};
+    int vals_kind = 0;
+    uint64_t vals_seed = 0;
+};
+
 struct eg_graph {
     eg_ctx *ctx;
     uint32_t n;
@@ -123,22 +137,15 @@ struct eg_graph {
     uint64_t grid_vals_seed = 0;
     // algorithm state, allocated on first use and reused
     eg_buf rank, rank_p, rank_q, contrib0, contrib1, pr_part, pr_stats, mp_carry, errflag;
+    eg_buf pr_acc;  // PageRank over source blocks: the row sums of the blocks before the last
     eg_buf level, parent, dist, label, spmv_x, spmv_y, spmv_vals;
     eg_buf level_s[EG_OUT_SLOTS - 1], parent_s[EG_OUT_SLOTS - 1];  // output slots 1.. of eg_bfs_batch
     eg_buf first_in;                  // BFS pull: each vertex's first in-neighbour (0xffffffff: none)
     const void *first_in_src = nullptr;  // the in-list column array first_in was taken from
     uint64_t spmv_vals_seed;
     int spmv_vals_kind;
-    // source-blocked copy of the CSC (fp32 SpMV over an x larger than L2):
-    // block b holds the sb_len[b] entries with source in [b << sb_shift,
-    // (b+1) << sb_shift), in CSC order, from entry sb_start[b] (a multiple of
-    // 4: the row kernel reads 16-byte vectors from the block's base);
-    // sb_ptr holds one row-pointer array of n + 1 per block
-    uint32_t sb_shift = 0, sb_blocks = 0;
-    eg_buf sb_ptr, sb_rid, sb_col, sb_perm, sb_vals, sb_yerr;
-    uint64_t sb_start[EG_SB_MAX] = {}, sb_len[EG_SB_MAX] = {};
-    int sb_vals_kind = 0;
-    uint64_t sb_vals_seed = 0;
+    eg_sblocks sb;   // source-blocked copy of the CSC (fp32 SpMV over an x larger than L2)
+    eg_sblocks sbp;  // the same of the relabelled CSC (PageRank)
     eg_buf bfs_work;  // bitmaps, queues, counters
     eg_buf msbfs_work;
     eg_buf sssp_work;

@@ -86,6 +86,7 @@ struct PrOp {
     float damping;
     float base;
     PprSeeds seeds;
+    const float *__restrict__ acc_in;  // source blocks: the earlier blocks' row sums (else NULL)
     __device__ __forceinline__ bool active() const { return st->done == 0; }
     __device__ __forceinline__ void setup() { base = st->base; }
     __device__ __forceinline__ V gather(uint32_t, uint32_t u) const { return __ldg(cin + u); }
@@ -105,6 +106,7 @@ struct PrOp {
         float sum;
         if constexpr (COMP) sum = s.x + s.y;
         else sum = s;
+        if (acc_in) sum = acc_in[v] + sum;
         // teleport: base on every vertex, or base x multiplicity on the seeds
         const float b = seeds.count ? base * seeds.weight(v) : base;
         float r = fmaf(damping, sum, b);
@@ -112,6 +114,27 @@ struct PrOp {
         uint32_t d = deg[v] * mult;
         cout[v] = d ? __fdiv_rn(r, (float)d) : 0.f;
         return make_float2(0.f, d ? 0.f : r);  // (residual: k_pr_residual, dangling mass)
+    }
+};
+
+// PageRank's row sums over the source blocks before the last one: acc[v] =
+// the sum of contrib[u] over v's entries in the blocks so far.
+struct PrAccOp {
+    using V = float;
+    using A = float;
+    const float *__restrict__ cin;
+    float *__restrict__ acc;
+    const eg_pr_dev *st;
+    int accum;  // 1: add to acc (blocks after the first)
+    __device__ __forceinline__ bool active() const { return st->done == 0; }
+    __device__ __forceinline__ void setup() {}
+    __device__ __forceinline__ V gather(uint32_t, uint32_t u) const { return __ldg(cin + u); }
+    __device__ __forceinline__ A zero() const { return 0.f; }
+    __device__ __forceinline__ A add(A a, V x) const { return a + x; }
+    __device__ __forceinline__ A merge(A a, A b) const { return a + b; }
+    __device__ __forceinline__ float2 emit(uint32_t v, A s) const {
+        acc[v] = accum ? acc[v] + s : s;
+        return make_float2(0.f, 0.f);
     }
 };
 
@@ -324,6 +347,16 @@ extern "C" void eg_pr_opts_default(eg_pr_opts *o) {
     o->tolerance = 0.0;
     o->use_graph = 0;
     o->grid = 0;
+    o->source_block_log2 = 0;
+}
+
+static int sb_prepare(eg_graph *g, eg_sblocks &sb, const eg_adj &adj, uint32_t shift);
+
+// PageRank's source-block size for these options, 0 when it runs in one pass
+static uint32_t pr_block_log2(const eg_graph *g, const eg_pr_opts &o) {
+    const uint32_t k = o.source_block_log2 > 0 ? (uint32_t)o.source_block_log2 : EG_SB_LOG2;
+    if (o.compensated || o.grid || k >= 32 || (uint64_t)g->n <= (1ull << k)) return 0;
+    return k;
 }
 
 // Launches every iteration; with `timed`, the row kernels of the first
@@ -346,10 +379,38 @@ static int pr_iterations(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, d
         op.damping = o.damping;
         op.base = 0.f;
         op.seeds = ps;
+        op.acc_in = nullptr;
         uint32_t nparts = 0;
         const bool t = timed && it < EG_KEV;
-        EG_TRY((coo_launch<PrOp<COMP>, REDUCE>(g, g->csc_p, carry, part, op, &nparts, t ? ctx->evk[2 * it] : nullptr,
-                                                t ? ctx->evk[2 * it + 1] : nullptr)));
+        const eg_sblocks &sb = g->sbp;
+        const uint32_t kb = pr_block_log2(g, o);
+        if (!COMP && kb && sb.blocks > 1 && sb.shift == kb) {
+            // contributions beyond L2: one pass per source block (eg_sblocks),
+            // the earlier blocks' row sums into pr_acc, the last block's
+            // pass finishing the ranks from them
+            if (t) EG_CUDA(cudaEventRecord(ctx->evk[2 * it], ctx->stream));
+            const uint32_t n1 = g->n + 1;
+            for (uint32_t b = 0; b < sb.blocks; b++) {
+                eg_adj view;  // pointers into the blocked arrays (owned by the graph)
+                view.ptr.p = bp<uint32_t>(sb.ptr) + (uint64_t)b * n1;
+                view.col.p = bp<uint32_t>(sb.col) + sb.start[b];
+                view.rid.p = bp<uint32_t>(sb.rid) + sb.start[b];
+                if (b + 1 < sb.blocks) {
+                    uint32_t np = 0;
+                    PrAccOp aop{op.cin, bp<float>(g->pr_acc), st, b > 0 ? 1 : 0};
+                    EG_TRY((coo_launch<PrAccOp, false>(g, view, carry, nullptr, aop, &np, nullptr, nullptr,
+                                                        sb.len[b], b == 0)));
+                } else {
+                    op.acc_in = bp<float>(g->pr_acc);
+                    EG_TRY((coo_launch<PrOp<COMP>, REDUCE>(g, view, carry, part, op, &nparts, nullptr,
+                                                            t ? ctx->evk[2 * it + 1] : nullptr, sb.len[b], true)));
+                }
+            }
+        } else {
+            EG_TRY((coo_launch<PrOp<COMP>, REDUCE>(g, g->csc_p, carry, part, op, &nparts,
+                                                    t ? ctx->evk[2 * it] : nullptr,
+                                                    t ? ctx->evk[2 * it + 1] : nullptr)));
+        }
         if (o.tolerance > 0.0) {  // the L1 change, after the row kernels (coalesced, 8 bytes per vertex)
             k_pr_residual<<<EG_PR_RES_BLOCKS, 256, 0, ctx->stream>>>(rank_new, rank_old, g->n, st, part + nparts);
             EG_LAUNCHED(ctx);
@@ -394,7 +455,7 @@ static int pr_graph(eg_graph *g, const eg_pr_opts &o, bool reduce, eg_pr_dev *st
     key[11] = (uint64_t)(uintptr_t)g->csc_p.rid.p;
     key[12] = (uint64_t)(uintptr_t)g->csc_p.col.p;
     key[13] = (uint64_t)(uintptr_t)g->csc_p.ptr.p;
-    key[14] = g->m ^ ((uint64_t)g->row_cfg << 56);
+    key[14] = g->m ^ ((uint64_t)g->row_cfg << 56) ^ ((uint64_t)pr_block_log2(g, o) << 48);
     key[15] = (uint64_t)ctx->stream ^ 0x5052ull;
     if (g->prg.exec && !memcmp(key, g->prk, sizeof(key))) return EG_OK;
     if (g->prg.exec) cudaGraphExecDestroy(g->prg.exec);
@@ -505,12 +566,19 @@ static int pr_run(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, uint32_t
     return EG_OK;
 }
 
-static int pr_prepare(eg_graph *g) {
+static int pr_prepare(eg_graph *g, const eg_pr_opts *o = nullptr) {
     if (!(g->built & EG_LAYOUT_CSC) || !(g->built & EG_LAYOUT_CSR))
         return eg_fail(EG_ENOTBUILT, "PageRank needs the CSC (in-lists) and CSR (out-degrees)");
     EG_CUDA(cudaSetDevice(g->ctx->device));
     EG_TRY(eg_build_relabeled_csc(g));
     EG_TRY(eg_buf_ensure(g->ctx, g->pr_stats, 512));
+    eg_pr_opts d;
+    eg_pr_opts_default(&d);
+    const uint32_t kb = pr_block_log2(g, o ? *o : d);
+    if (kb) {  // contributions beyond L2: the source-blocked copy
+        EG_TRY(sb_prepare(g, g->sbp, g->csc_p, kb));
+        EG_TRY(eg_buf_ensure(g->ctx, g->pr_acc, (uint64_t)g->n * 4));
+    }
     return EG_OK;
 }
 
@@ -524,7 +592,7 @@ extern "C" int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out,
         EG_CUDA(cudaSetDevice(g->ctx->device));
         return eg_grid_pagerank(g, o, rank_out, stats);
     }
-    EG_TRY(pr_prepare(g));
+    EG_TRY(pr_prepare(g, &o));
     PprSeeds none;
     memset(&none, 0, sizeof(none));
     return pr_run(g, o, none, 0, rank_out, stats);
@@ -765,14 +833,14 @@ static uint32_t sb_grid(eg_ctx *ctx, uint64_t work) {
     return (uint32_t)(b > cap ? cap : (b ? b : 1));
 }
 
-static int sb_prepare(eg_graph *g, uint32_t shift) {
-    if (g->sb_blocks && g->sb_shift == shift) return EG_OK;
+static int sb_prepare(eg_graph *g, eg_sblocks &sb, const eg_adj &adj, uint32_t shift) {
+    if (sb.blocks && sb.shift == shift) return EG_OK;
     eg_ctx *ctx = g->ctx;
     const uint32_t n = g->n;
     const uint64_t M = g->m;
     const uint32_t B = (uint32_t)(((uint64_t)n + (1ull << shift) - 1) >> shift);
     if (B > EG_SB_MAX) return eg_fail(EG_EINVAL, "source blocks of 2^%u vertices: %u blocks, at most %d", shift, B, EG_SB_MAX);
-    g->sb_blocks = 0;
+    sb.blocks = 0;
     eg_buf ka, va, kb, vb, cnt;
     int rc = EG_OK;
     auto cleanup = [&]() {
@@ -797,13 +865,13 @@ static int sb_prepare(eg_graph *g, uint32_t shift) {
     STRY(eg_buf_ensure(ctx, vb, (M + 1) * 4));
     STRY(eg_buf_ensure(ctx, cnt, ((uint64_t)n + EG_SB_MAX + 1) * 4));
     const uint64_t MP = M + 4ull * EG_SB_MAX;  // room for the blocks' alignment padding
-    STRY(eg_buf_ensure(ctx, g->sb_rid, MP * 4 + 16));
-    STRY(eg_buf_ensure(ctx, g->sb_col, MP * 4 + 16));
-    STRY(eg_buf_ensure(ctx, g->sb_perm, MP * 4 + 16));
-    STRY(eg_buf_ensure(ctx, g->sb_ptr, (uint64_t)B * ((uint64_t)n + 1) * 4));
+    STRY(eg_buf_ensure(ctx, sb.rid, MP * 4 + 16));
+    STRY(eg_buf_ensure(ctx, sb.col, MP * 4 + 16));
+    STRY(eg_buf_ensure(ctx, sb.perm, MP * 4 + 16));
+    STRY(eg_buf_ensure(ctx, sb.ptr, (uint64_t)B * ((uint64_t)n + 1) * 4));
     uint32_t *ks = bp<uint32_t>(ka), *vs = bp<uint32_t>(va);
     if (M) {
-        k_sb_keys<<<sb_grid(ctx, M), 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.col), M, shift, bp<uint32_t>(ka),
+        k_sb_keys<<<sb_grid(ctx, M), 256, 0, ctx->stream>>>(bp<uint32_t>(adj.col), M, shift, bp<uint32_t>(ka),
                                                             bp<uint32_t>(va));
         EG_LAUNCHED(ctx);
         const int bits = B <= 1 ? 1 : 32 - __builtin_clz(B - 1);
@@ -821,29 +889,29 @@ static int sb_prepare(eg_graph *g, uint32_t shift) {
     uint64_t sorted_at = 0, placed_at = 0;
     for (uint32_t b = 0; b < B; b++) {
         const uint64_t len = hc[b];
-        g->sb_start[b] = placed_at;  // a multiple of 4 entries
-        g->sb_len[b] = len;
+        sb.start[b] = placed_at;  // a multiple of 4 entries
+        sb.len[b] = len;
         if (len) {
             k_sb_gather<<<sb_grid(ctx, len), 256, 0, ctx->stream>>>(
-                vs + sorted_at, bp<uint32_t>(g->csc.rid), bp<uint32_t>(g->csc.col), len,
-                bp<uint32_t>(g->sb_rid) + placed_at, bp<uint32_t>(g->sb_col) + placed_at);
+                vs + sorted_at, bp<uint32_t>(adj.rid), bp<uint32_t>(adj.col), len,
+                bp<uint32_t>(sb.rid) + placed_at, bp<uint32_t>(sb.col) + placed_at);
             EG_LAUNCHED(ctx);
-            if (cudaMemcpyAsync(bp<uint32_t>(g->sb_perm) + placed_at, vs + sorted_at, len * 4, cudaMemcpyDeviceToDevice,
+            if (cudaMemcpyAsync(bp<uint32_t>(sb.perm) + placed_at, vs + sorted_at, len * 4, cudaMemcpyDeviceToDevice,
                                 ctx->stream) != cudaSuccess)
                 STRY(eg_fail(EG_ECUDA, "source-block copy"));
         }
         // the block's row pointers: histogram of its rows, exclusive scan
         if (cudaMemsetAsync(cnt.p, 0, (uint64_t)n * 4, ctx->stream) != cudaSuccess) STRY(eg_fail(EG_ECUDA, "memset"));
-        STRY(eg_histogram(ctx, bp<uint32_t>(g->sb_rid) + placed_at, len, bp<uint32_t>(cnt)));
-        STRY(eg_exscan_u32(ctx, bp<uint32_t>(cnt), bp<uint32_t>(g->sb_ptr) + (uint64_t)b * ((uint64_t)n + 1), n));
+        STRY(eg_histogram(ctx, bp<uint32_t>(sb.rid) + placed_at, len, bp<uint32_t>(cnt)));
+        STRY(eg_exscan_u32(ctx, bp<uint32_t>(cnt), bp<uint32_t>(sb.ptr) + (uint64_t)b * ((uint64_t)n + 1), n));
         sorted_at += len;
         placed_at = (placed_at + len + 3) & ~3ull;
     }
     cleanup();
 #undef STRY
-    g->sb_shift = shift;
-    g->sb_blocks = B;
-    g->sb_vals_kind = 0;
+    sb.shift = shift;
+    sb.blocks = B;
+    sb.vals_kind = 0;
     return EG_OK;
 }
 
@@ -851,44 +919,45 @@ static int sb_prepare(eg_graph *g, uint32_t shift) {
 // order): one pass per block, the first writing y, the others adding to it
 // (EG_SPMV_F32_COMP carries each row's (sum, error) pair between passes).
 static int sb_spmv(eg_graph *g, int kind, int vk, uint64_t seed) {
+    eg_sblocks &sb = g->sb;
     eg_ctx *ctx = g->ctx;
     const uint32_t n = g->n;
     const uint64_t M = g->m;
-    if (g->sb_vals_kind != vk || (vk == 2 && g->sb_vals_seed != seed)) {
-        EG_TRY(eg_buf_ensure(ctx, g->sb_vals, (M + 4ull * EG_SB_MAX) * 4 + 16));
-        for (uint32_t b = 0; b < g->sb_blocks; b++) {
-            const uint64_t s0 = g->sb_start[b], len = g->sb_len[b];
+    if (sb.vals_kind != vk || (vk == 2 && sb.vals_seed != seed)) {
+        EG_TRY(eg_buf_ensure(ctx, sb.vals, (M + 4ull * EG_SB_MAX) * 4 + 16));
+        for (uint32_t b = 0; b < sb.blocks; b++) {
+            const uint64_t s0 = sb.start[b], len = sb.len[b];
             if (!len) continue;
-            k_sb_vals<<<sb_grid(ctx, len), 256, 0, ctx->stream>>>(bp<uint32_t>(g->sb_perm) + s0,
+            k_sb_vals<<<sb_grid(ctx, len), 256, 0, ctx->stream>>>(bp<uint32_t>(sb.perm) + s0,
                                                                   bp<float>(g->spmv_vals), len,
-                                                                  bp<float>(g->sb_vals) + s0);
+                                                                  bp<float>(sb.vals) + s0);
             EG_LAUNCHED(ctx);
         }
-        g->sb_vals_kind = vk;
-        g->sb_vals_seed = seed;
+        sb.vals_kind = vk;
+        sb.vals_seed = seed;
     }
-    if (kind == EG_SPMV_F32_COMP) EG_TRY(eg_buf_ensure(ctx, g->sb_yerr, (uint64_t)n * 4));
+    if (kind == EG_SPMV_F32_COMP) EG_TRY(eg_buf_ensure(ctx, sb.yerr, (uint64_t)n * 4));
     uint32_t np = 0;
-    for (uint32_t b = 0; b < g->sb_blocks; b++) {
-        const uint64_t s0 = g->sb_start[b], len = g->sb_len[b];
+    for (uint32_t b = 0; b < sb.blocks; b++) {
+        const uint64_t s0 = sb.start[b], len = sb.len[b];
         eg_adj view;  // pointers into the blocked arrays (owned by the graph)
-        view.ptr.p = bp<uint32_t>(g->sb_ptr) + (uint64_t)b * ((uint64_t)n + 1);
-        view.col.p = bp<uint32_t>(g->sb_col) + s0;
-        view.rid.p = bp<uint32_t>(g->sb_rid) + s0;
+        view.ptr.p = bp<uint32_t>(sb.ptr) + (uint64_t)b * ((uint64_t)n + 1);
+        view.col.p = bp<uint32_t>(sb.col) + s0;
+        view.rid.p = bp<uint32_t>(sb.rid) + s0;
         const int acc = b > 0 ? 1 : 0;
         if (kind == EG_SPMV_F32) {
-            SpmvF32Op<false> op{bp<float>(g->spmv_x), bp<float>(g->sb_vals) + s0, bp<float>(g->spmv_y), acc};
+            SpmvF32Op<false> op{bp<float>(g->spmv_x), bp<float>(sb.vals) + s0, bp<float>(g->spmv_y), acc};
             EG_TRY((coo_launch<SpmvF32Op<false>, false>(g, view, g->mp_carry, nullptr, op, &np, nullptr, nullptr, len,
                                                          b == 0)));
         } else {
-            SpmvF32Op<true> op{bp<float>(g->spmv_x), bp<float>(g->sb_vals) + s0, bp<float>(g->spmv_y), acc, 0,
-                               bp<float>(g->sb_yerr)};
+            SpmvF32Op<true> op{bp<float>(g->spmv_x), bp<float>(sb.vals) + s0, bp<float>(g->spmv_y), acc, 0,
+                               bp<float>(sb.yerr)};
             EG_TRY((coo_launch<SpmvF32Op<true>, false>(g, view, g->mp_carry, nullptr, op, &np, nullptr, nullptr, len,
                                                         b == 0)));
         }
     }
     if (kind == EG_SPMV_F32_COMP) {
-        k_pair_finish<<<sb_grid(ctx, n), 256, 0, ctx->stream>>>(bp<float>(g->spmv_y), bp<float>(g->sb_yerr), n);
+        k_pair_finish<<<sb_grid(ctx, n), 256, 0, ctx->stream>>>(bp<float>(g->spmv_y), bp<float>(sb.yerr), n);
         EG_LAUNCHED(ctx);
     }
     return EG_OK;
@@ -935,7 +1004,7 @@ extern "C" int eg_spmv(eg_graph *g, const eg_spmv_opts *opts, const void *x, voi
     // (not FP64: its time is in the FP64 arithmetic, which a second pass only adds to)
     const bool blocked = (kind == EG_SPMV_F32 || kind == EG_SPMV_F32_COMP) && sb_log2 < 32 &&
                          (uint64_t)n > (1ull << sb_log2);
-    if (blocked) EG_TRY(sb_prepare(g, sb_log2));
+    if (blocked) EG_TRY(sb_prepare(g, g->sb, g->csc, sb_log2));
     eg_buf &carry = g->mp_carry;
     uint32_t np = 0;
     EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));

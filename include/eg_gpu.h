@@ -157,6 +157,11 @@ typedef struct {
     int grid;      /* 1: iterate over the 2-D grid layout (prgrid_cilk.c:62-141):
                       cells in L2-sized blocks, sums by atomic adds (not in a
                       fixed order); needs eg_graph_build_grid and the CSR */
+    int source_block_log2; /* not compensated, n > 2^k (k = this, 0: 24): the
+                      contributions are gathered one source block of 2^k
+                      vertices per pass (a copy of the relabelled CSC split by
+                      source, built once), each pass from a slice that L2
+                      holds; the earlier blocks' row sums feed the last pass */
 } eg_pr_opts;
 typedef struct {
     int iterations_run;

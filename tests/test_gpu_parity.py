@@ -186,6 +186,32 @@ def test_row_schedules_and_autotuner(case):
     g.set_row_schedule(0)
 
 
+def test_pagerank_source_blocks(case):
+    # PageRank gathering its contributions one source block per pass (blocks
+    # of 2^k vertices; the default 2^24 only splits larger graphs): within the
+    # FP64 tolerance, graph replay = stream launch, the tolerance stop works
+    name, n, pairs, rec, g, gu, adj, adju = case
+    ref = oracle.pagerank_f64(adj, adj.out_deg(), 1.0 / n, 10, dangling=True)
+    ran = 0
+    for k in (10, 8, 3):
+        if n > (64 << k) or n <= (1 << k):
+            continue
+        ran += 1
+        got, st = g.pagerank(iterations=10, dangling=True, source_block_log2=k)
+        l1, mx = rel_errors(got, ref)
+        assert l1 <= PR_REL_L1 and mx <= PR_MAX_REL, (k, l1, mx)
+        a, _ = g.pagerank(iterations=7, source_block_log2=k)
+        b, _ = g.pagerank(iterations=7, source_block_log2=k, use_graph=True)
+        np.testing.assert_array_equal(a, b)
+        got, st = g.pagerank(iterations=200, tolerance=1e-6, dangling=True, source_block_log2=k)
+        assert 1 <= st.iterations_run < 200 and st.residual < 1e-6
+    assert ran >= 1
+    # back to one pass on the same graph
+    got, _ = g.pagerank(iterations=10, dangling=True)
+    l1, mx = rel_errors(got, ref)
+    assert l1 <= PR_REL_L1 and mx <= PR_MAX_REL
+
+
 def test_pagerank_tolerance_stops_early(case):
     name, n, pairs, rec, g, gu, adj, adju = case
     got, st = g.pagerank(iterations=200, tolerance=1e-6, dangling=True)
