@@ -402,10 +402,12 @@ static int pr_iterations(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, d
                                                         sb.len[b], b == 0)));
                 } else {
                     op.acc_in = bp<float>(g->pr_acc);
-                    EG_TRY((coo_launch<PrOp<COMP>, REDUCE>(g, view, carry, part, op, &nparts, nullptr,
-                                                            t ? ctx->evk[2 * it + 1] : nullptr, sb.len[b], true)));
+                    EG_TRY((coo_launch<PrOp<COMP>, REDUCE>(g, view, carry, part, op, &nparts, nullptr, nullptr,
+                                                            sb.len[b], true)));
                 }
             }
+            // after the last pass (a block may have no entries, and so no row kernel)
+            if (t) EG_CUDA(cudaEventRecord(ctx->evk[2 * it + 1], ctx->stream));
         } else {
             EG_TRY((coo_launch<PrOp<COMP>, REDUCE>(g, g->csc_p, carry, part, op, &nparts,
                                                     t ? ctx->evk[2 * it] : nullptr,

@@ -200,6 +200,7 @@ def test_pagerank_source_blocks(case):
         got, st = g.pagerank(iterations=10, dangling=True, source_block_log2=k)
         l1, mx = rel_errors(got, ref)
         assert l1 <= PR_REL_L1 and mx <= PR_MAX_REL, (k, l1, mx)
+        assert st.row_kernel_ms > 0  # timed over all passes, also when a block has no entries
         a, _ = g.pagerank(iterations=7, source_block_log2=k)
         b, _ = g.pagerank(iterations=7, source_block_log2=k, use_graph=True)
         np.testing.assert_array_equal(a, b)
