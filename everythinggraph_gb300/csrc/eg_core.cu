@@ -748,6 +748,7 @@ static int build_adj_pair(eg_graph *g, bool want_csc) {
             BTRY(eg_fail(EG_ECUDA, "copy rid"));
         g->built |= EG_LAYOUT_CSC;
         g->first_in_src = nullptr;
+        g->relabeled = false;  // so do PageRank's relabelled copy
         g->sb.blocks = 0;  // the source-blocked copies follow the CSC
         g->sb.shift = 0;
         g->sbp.blocks = 0;
@@ -894,11 +895,21 @@ extern "C" int eg_graph_build_grid(eg_graph *g, uint32_t P) {
 }
 
 // ---------------------------------------------------------------- relabelled CSC
-__global__ void k_relabel_keys(const uint32_t *__restrict__ deg, uint32_t n, uint32_t *keys, uint32_t *vals) {
+// Ascending key: vertices with in-edges first, then descending out-degree;
+// ties keep ascending id (stable sort).  `rows` counts the vertices with
+// in-edges, so the rows of the relabelled CSC that have entries are [0, rows).
+__global__ void k_relabel_keys(const uint32_t *__restrict__ deg, const uint32_t *__restrict__ in_deg, uint32_t n,
+                               uint32_t *keys, uint32_t *vals, uint32_t *rows) {
+    uint32_t cnt = 0;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-        keys[v] = ~deg[v];  // ascending key = descending degree; ties keep ascending id (stable sort)
+        const uint32_t d = deg[v] < 0x7fffffffu ? deg[v] : 0x7fffffffu;
+        const bool in = in_deg[v] != 0;
+        keys[v] = (in ? 0u : 0x80000000u) | (0x7fffffffu - d);
         vals[v] = v;
+        cnt += in;
     }
+    cnt = __reduce_add_sync(EG_FULL_MASK, cnt);
+    if ((threadIdx.x & 31) == 0 && cnt) atomicAdd(rows, cnt);
 }
 __global__ void k_relabel_perm(const uint32_t *__restrict__ order, const uint32_t *__restrict__ deg, uint32_t n,
                                uint32_t *perm, uint32_t *deg_p) {
@@ -949,9 +960,17 @@ int eg_build_relabeled_csc(eg_graph *g) {
     RTRY(eg_buf_ensure(ctx, g->perm, (uint64_t)n * 4));
     RTRY(eg_buf_ensure(ctx, g->deg_p, (uint64_t)n * 4));
     uint32_t *ks, *vs;
-    k_relabel_keys<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(bp<uint32_t>(g->out_deg), n, bp<uint32_t>(ka),
-                                                             bp<uint32_t>(va));
+    // the count of rows with entries goes to the word after the key array
+    // (the buffers hold len + 1 words; the sorts use the first n)
+    uint32_t *rows_dev = bp<uint32_t>(kb) + len;
+    if (cudaMemsetAsync(rows_dev, 0, 4, ctx->stream) != cudaSuccess) RTRY(eg_fail(EG_ECUDA, "memset"));
+    k_relabel_keys<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(bp<uint32_t>(g->out_deg), bp<uint32_t>(g->in_deg), n,
+                                                             bp<uint32_t>(ka), bp<uint32_t>(va), rows_dev);
     ctx->launches++;
+    uint32_t rows_host = 0;
+    if (cudaMemcpyAsync(&rows_host, rows_dev, 4, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+        cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+        RTRY(eg_fail(EG_ECUDA, "relabel count"));
     RTRY(eg_radix_sort(ctx, bp<uint32_t>(ka), bp<uint32_t>(va), bp<uint32_t>(kb), bp<uint32_t>(vb), n, 32, &ks, &vs));
     k_relabel_perm<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(vs, bp<uint32_t>(g->out_deg), n, bp<uint32_t>(g->perm),
                                                              bp<uint32_t>(g->deg_p));
@@ -986,6 +1005,7 @@ int eg_build_relabeled_csc(eg_graph *g) {
 #undef RTRY
     cleanup();
     g->relabeled = true;
+    g->csc_p_rows = rows_host;
     return EG_OK;
 }
 

@@ -122,10 +122,12 @@ struct eg_graph {
     eg_adj csr, csc;
     eg_buf out_deg, in_deg;  // uint32[n]
     // PageRank's copy of the CSC with vertices relabelled by descending
-    // out-degree (hot sources contiguous): perm[old] = new, deg_p[new]
+    // out-degree (hot sources contiguous), the vertices without in-edges
+    // last: perm[old] = new, deg_p[new]; rows [csc_p_rows, n) have no entries
     eg_adj csc_p;
     eg_buf perm, deg_p;
     bool relabeled = false;
+    uint32_t csc_p_rows = 0;
     // grid
     uint32_t grid_p;
     eg_buf cell_ptr, gsrc, gdst;

@@ -315,10 +315,37 @@ struct eg_f2sum {
 // per graph), so a warp can own a fixed range of entries and find row
 // boundaries by comparing neighbouring row ids.  Rows split between warps are
 // finished by k_coo_fixup (same head/tail scheme as the merge-path kernels);
-// rows without entries are written by k_coo_empty_rows.
+// rows without entries are written by k_coo_empty_rows (or, when they are
+// known to form the range at the end, k_coo_empty_range).
 
-// Rows split between warp tiles: one warp per tile with a head row adds the
-// tails of the preceding tiles, 32 per step (as k_mp_fixup).
+// The block's share of the emitted (residual, dangling) partials into part[blockIdx.x].
+template <bool REDUCE>
+__device__ __forceinline__ void eg_block_part(const eg_red2 &redf, double2 *__restrict__ part, double2 *s_red) {
+    if (!REDUCE) return;
+    double2 red = redf.wide();
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        red.x += __shfl_down_sync(EG_FULL_MASK, red.x, o);
+        red.y += __shfl_down_sync(EG_FULL_MASK, red.y, o);
+    }
+    if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = red;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double2 t = make_double2(0.0, 0.0);
+        for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
+            t.x += s_red[w].x;
+            t.y += s_red[w].y;
+        }
+        part[blockIdx.x] = t;
+    }
+}
+
+// Rows split between warp tiles, finished from the tiles' head and tail
+// partials: one thread per tile.  A head row that began in the tile before
+// is finished by the tile's thread (that tile's tail + this tile's head);
+// a row spanning more tiles is finished by the whole warp, which adds the
+// tails of the preceding tiles 32 per step.  Both give the same bits (the
+// tail and head are merged in that order either way).
 template <class Op, int TILE_E, bool REDUCE>
 __global__ void k_coo_fixup(const uint32_t *__restrict__ ptr, uint32_t ntiles,
                             const eg_mp_carry<typename Op::A> *__restrict__ carry, double2 *__restrict__ part,
@@ -328,77 +355,100 @@ __global__ void k_coo_fixup(const uint32_t *__restrict__ ptr, uint32_t ntiles,
     if (!op.active()) return;
     op.setup();
     const uint32_t lane = threadIdx.x & 31;
-    const uint32_t c = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t c = blockIdx.x * blockDim.x + threadIdx.x;
     eg_red2 redf;
+    uint32_t row = EG_MP_NONE, rstart = 0;
+    bool wide = false;
     if (c < ntiles) {
-        const uint32_t row = carry[c].head_row;
+        row = carry[c].head_row;  // never set in tile 0
         if (row != EG_MP_NONE) {
-            A tot = carry[c].head_val;
-            const uint32_t rstart = ptr[row];
-            for (int base = (int)c - 1; base >= 0; base -= 32) {
-                const int k = base - (int)lane;
-                const bool valid = k >= 0;
-                const bool began = valid && rstart >= (uint32_t)k * (uint32_t)TILE_E;
-                const uint32_t stop_mask = __ballot_sync(EG_FULL_MASK, began || !valid);
-                const int last = stop_mask ? __ffs(stop_mask) - 1 : 31;
-                A x = (valid && (int)lane <= last) ? carry[k].tail_val : op.zero();
+            rstart = ptr[row];
+            if (c >= 1 && rstart >= (c - 1) * (uint32_t)TILE_E) {
+                const float2 d = op.emit(row, op.merge(carry[c - 1].tail_val, carry[c].head_val));
+                if (REDUCE) redf.add(d);
+            } else {
+                wide = true;
+            }
+        }
+    }
+    uint32_t todo = __ballot_sync(EG_FULL_MASK, wide);
+    while (todo) {
+        const int src = __ffs(todo) - 1;
+        todo &= todo - 1;
+        const uint32_t cw = __shfl_sync(EG_FULL_MASK, c, src);
+        const uint32_t rw = __shfl_sync(EG_FULL_MASK, row, src);
+        const uint32_t sw = __shfl_sync(EG_FULL_MASK, rstart, src);
+        A tot = carry[cw].head_val;
+        for (int base = (int)cw - 1; base >= 0; base -= 32) {
+            const int k = base - (int)lane;
+            const bool valid = k >= 0;
+            const bool began = valid && sw >= (uint32_t)k * (uint32_t)TILE_E;
+            const uint32_t stop_mask = __ballot_sync(EG_FULL_MASK, began || !valid);
+            const int last = stop_mask ? __ffs(stop_mask) - 1 : 31;
+            A x = (valid && (int)lane <= last) ? carry[k].tail_val : op.zero();
 #pragma unroll
-                for (int off = 16; off > 0; off >>= 1) {
-                    const A y = eg_shfl_down(x, off);
-                    x = op.merge(y, x);
-                }
-                x = eg_shfl_idx(x, 0);
-                tot = op.merge(x, tot);
-                if (stop_mask) break;
+            for (int off = 16; off > 0; off >>= 1) {
+                const A y = eg_shfl_down(x, off);
+                x = op.merge(y, x);
             }
-            if (lane == 0) redf.add(op.emit(row, tot));
+            x = eg_shfl_idx(x, 0);
+            tot = op.merge(x, tot);
+            if (stop_mask) break;
         }
-    }
-    if (REDUCE) {
-        if (lane == 0) s_red[threadIdx.x >> 5] = redf.wide();
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double2 s = make_double2(0.0, 0.0);
-            for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
-                s.x += s_red[w].x;
-                s.y += s_red[w].y;
-            }
-            part[blockIdx.x] = s;
-        }
-    }
-}
-
-// Rows without entries: emitted with an empty sum.
-template <class Op, bool REDUCE>
-__global__ void k_coo_empty_rows(const uint32_t *__restrict__ ptr, uint32_t n, double2 *__restrict__ part, Op op) {
-    __shared__ double2 s_red[8];
-    if (!op.active()) return;
-    op.setup();
-    eg_red2 redf;
-    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x) {
-        if (__ldg(ptr + v) == __ldg(ptr + v + 1)) {
-            const float2 d = op.emit(v, op.zero());
+        if ((int)lane == src) {
+            const float2 d = op.emit(rw, tot);
             if (REDUCE) redf.add(d);
         }
     }
-    if (REDUCE) {
-        double2 red = redf.wide();
+    eg_block_part<REDUCE>(redf, part, s_red);
+}
+
+// Rows without entries: emitted with an empty sum.  Four rows per thread and
+// step, their row pointers loaded before any is tested.
+template <class Op, bool REDUCE>
+__global__ void k_coo_empty_rows(const uint32_t *__restrict__ ptr, uint32_t n, double2 *__restrict__ part, Op op) {
+    __shared__ double2 s_red[32];
+    if (!op.active()) return;
+    op.setup();
+    eg_red2 redf;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t v0 = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v0 < n; v0 += 4 * stride) {
+        uint32_t lo[4], hi[4];
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            red.x += __shfl_down_sync(EG_FULL_MASK, red.x, o);
-            red.y += __shfl_down_sync(EG_FULL_MASK, red.y, o);
-        }
-        if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = red;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            double2 s = make_double2(0.0, 0.0);
-            for (int w = 0; w < (int)(blockDim.x >> 5); w++) {
-                s.x += s_red[w].x;
-                s.y += s_red[w].y;
+        for (int j = 0; j < 4; j++) {
+            const uint64_t v = v0 + j * stride;
+            lo[j] = 0;
+            hi[j] = 1;
+            if (v < n) {
+                lo[j] = __ldg(ptr + v);
+                hi[j] = __ldg(ptr + v + 1);
             }
-            part[blockIdx.x] = s;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+            if (lo[j] == hi[j]) {
+                const float2 d = op.emit((uint32_t)(v0 + j * stride), op.zero());
+                if (REDUCE) redf.add(d);
+            }
         }
     }
+    eg_block_part<REDUCE>(redf, part, s_red);
+}
+
+// Rows [lo, hi), known to have no entries (the relabelled CSC keeps them
+// last): emitted with an empty sum, without reading row pointers.
+template <class Op, bool REDUCE>
+__global__ void k_coo_empty_range(uint32_t lo, uint32_t hi, double2 *__restrict__ part, Op op) {
+    __shared__ double2 s_red[32];
+    if (!op.active()) return;
+    op.setup();
+    eg_red2 redf;
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+    for (uint64_t v = (uint64_t)lo + (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; v < hi; v += stride) {
+        const float2 d = op.emit((uint32_t)v, op.zero());
+        if (REDUCE) redf.add(d);
+    }
+    eg_block_part<REDUCE>(redf, part, s_red);
 }
 
 // 128-bit streaming load of the row-id / column words.  HINT 1: the words

@@ -10,11 +10,13 @@
 // descending out-degree (built once, eg_build_relabeled_csc): the most
 // gathered contrib entries are then contiguous, so they share cache sectors
 // and stay in L1; ranks are mapped back to the original ids at the end.
+// Vertices without in-edges come last in that order, so the rows without
+// entries are one range that needs no row-pointer scan.
 // Per PageRank iteration the device runs:
 //   k_coov_rows<PrOp>      rank[v] = base + d * sum_{u in in(v)} contrib[u],
 //                          contrib'[v] = rank[v] / deg[v] (fused into the write);
 //                          warp tiles of row-id/column pairs (eg_mp.cuh)
-//   k_coo_empty_rows, k_coo_fixup   rows without entries, rows split between tiles
+//   k_coo_empty_range, k_coo_fixup  rows without entries, rows split between tiles
 //   k_pr_residual          (with a tolerance) the L1 change, coalesced
 //   k_pr_reduce            FP64 residual / dangling mass -> next base, stop flag
 // contrib[u] = prev[u] / (float)deg[u] is the reference's per-edge quotient
@@ -257,6 +259,7 @@ __global__ void k_pr_reduce(const double2 *__restrict__ part, uint32_t nparts, e
 // eviction.
 #define EG_COO_TILE_MIN 512
 #define EG_ALL_ENTRIES (~0ull)
+#define EG_NO_RANGE 0xffffffffu  // coo_launch: rows without entries found from the row pointers
 #define EG_SB_LOG2 24  // source-block size by default: 2^24 vertices, a 64 MB slice of x
 #define EG_PR_CHECK 4  // iterations between reads of the stop flag
 #define EG_PR_RES_BLOCKS 1024
@@ -275,15 +278,20 @@ static const RowCfg kRowCfg[EG_ROW_CFGS] = {
 
 template <class Op, int TILE, int U, bool REDUCE, int PF, int MINB, int HINT = 0>
 static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts,
-                        cudaEvent_t ev_begin, cudaEvent_t ev_end, uint64_t m_entries, bool empty_rows) {
+                        cudaEvent_t ev_begin, cudaEvent_t ev_end, uint64_t m_entries, bool empty_rows,
+                        uint32_t empty_from) {
     eg_ctx *ctx = g->ctx;
     using A = typename Op::A;
     const uint32_t m = (uint32_t)(m_entries == EG_ALL_ENTRIES ? g->m : m_entries);
     const uint32_t ntiles = m ? eg_div_up(m, TILE) : 0;
     EG_TRY(eg_buf_ensure(ctx, carry_buf, ((uint64_t)ntiles + 1) * sizeof(eg_mp_carry<A>)));
-    const uint32_t gf = ntiles ? eg_div_up((uint64_t)ntiles * 32, 256) : 0;  // one warp per tile
-    const uint32_t g1 = gf;
-    uint32_t g2 = eg_div_up(g->n, 256);
+    const uint32_t g1 = ntiles ? eg_div_up((uint64_t)ntiles * 32, 256) : 0;  // one warp per tile
+    const uint32_t gf = ntiles ? eg_div_up(ntiles, 256) : 0;                 // one thread per tile
+    // rows without entries: the range [empty_from, n) when the layout keeps
+    // them last, else found from the row pointers
+    const bool ranged = empty_from <= g->n;
+    const uint32_t empty_n = ranged ? g->n - empty_from : g->n;
+    uint32_t g2 = empty_rows ? eg_div_up(empty_n, 256) : 0;
     if (g2 > (uint32_t)ctx->sm_count * 8) g2 = (uint32_t)ctx->sm_count * 8;
     if (g1) {
         if (ev_begin) EG_CUDA(cudaEventRecord(ev_begin, ctx->stream));
@@ -292,7 +300,10 @@ static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *pa
         EG_LAUNCHED(ctx);
         if (ev_end) EG_CUDA(cudaEventRecord(ev_end, ctx->stream));
     }
-    if (empty_rows) {
+    if (g2 && ranged) {
+        k_coo_empty_range<Op, REDUCE><<<g2, 256, 0, ctx->stream>>>(empty_from, g->n, part ? part + g1 : nullptr, op);
+        EG_LAUNCHED(ctx);
+    } else if (g2) {
         k_coo_empty_rows<Op, REDUCE><<<g2, 256, 0, ctx->stream>>>(bp<uint32_t>(adj.ptr), g->n,
                                                                   part ? part + g1 : nullptr, op);
         EG_LAUNCHED(ctx);
@@ -308,14 +319,15 @@ static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *pa
 
 // m_entries: the entries of `adj` (EG_ALL_ENTRIES: the graph's m); without
 // empty_rows the rows that have no entries in `adj` are left as they are.
+// empty_from <= n: the rows without entries are exactly [empty_from, n).
 template <class Op, bool REDUCE>
 static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts,
                       cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr,
-                      uint64_t m_entries = EG_ALL_ENTRIES, bool empty_rows = true) {
+                      uint64_t m_entries = EG_ALL_ENTRIES, bool empty_rows = true, uint32_t empty_from = EG_NO_RANGE) {
 #define EG_ROW_CASE(i, T, U, PF, MB, H)                                                                         \
     case i:                                                                                                     \
         return coo_launch_t<Op, T, U, REDUCE, PF, MB, H>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end, \
-                                                          m_entries, empty_rows);
+                                                          m_entries, empty_rows, empty_from);
     switch (g->row_cfg) {
         EG_ROW_CASE(1, 2048, 4, false, 6, 0)
         EG_ROW_CASE(2, 2048, 4, true, 5, 0)
@@ -330,7 +342,7 @@ static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part
         EG_ROW_CASE(11, 2048, 4, 2, 4, 0)
         default:
             return coo_launch_t<Op, 1024, 4, REDUCE, true, 5>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end,
-                                                              m_entries, empty_rows);
+                                                              m_entries, empty_rows, empty_from);
     }
 #undef EG_ROW_CASE
 }
@@ -411,7 +423,8 @@ static int pr_iterations(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, d
         } else {
             EG_TRY((coo_launch<PrOp<COMP>, REDUCE>(g, g->csc_p, carry, part, op, &nparts,
                                                     t ? ctx->evk[2 * it] : nullptr,
-                                                    t ? ctx->evk[2 * it + 1] : nullptr)));
+                                                    t ? ctx->evk[2 * it + 1] : nullptr, EG_ALL_ENTRIES, true,
+                                                    g->csc_p_rows)));
         }
         if (o.tolerance > 0.0) {  // the L1 change, after the row kernels (coalesced, 8 bytes per vertex)
             k_pr_residual<<<EG_PR_RES_BLOCKS, 256, 0, ctx->stream>>>(rank_new, rank_old, g->n, st, part + nparts);
@@ -441,7 +454,7 @@ static int pr_dispatch(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, dou
 static int pr_graph(eg_graph *g, const eg_pr_opts &o, bool reduce, eg_pr_dev *st, double2 *part, eg_buf &carry) {
     eg_ctx *ctx = g->ctx;
     uint64_t key[16] = {};
-    key[0] = (uint64_t)o.iterations;
+    key[0] = (uint32_t)o.iterations | ((uint64_t)g->csc_p_rows << 32);
     key[1] = (uint64_t)o.swap | ((uint64_t)o.compensated << 1) | ((uint64_t)reduce << 2) | ((uint64_t)o.dangling << 3);
     uint32_t dbits;
     memcpy(&dbits, &o.damping, 4);

@@ -213,6 +213,39 @@ def test_pagerank_source_blocks(case):
     assert l1 <= PR_REL_L1 and mx <= PR_MAX_REL
 
 
+def test_pagerank_rows_without_in_edges(ctx):
+    # vertices without in-edges (a quarter of them, plus isolated ones) are
+    # the rows PageRank writes apart from the row kernel: their ranks, the
+    # dangling mass of the isolated ones, and a personalised seed among them
+    import everythinggraph_gb300 as eg
+    n = 6000
+    rng = np.random.default_rng(5)
+    m = 60000
+    src = rng.integers(0, 4000, size=m)
+    dst = rng.integers(1500, 4000, size=m)  # [0, 1500) and [4000, n) have no in-edges
+    src[:50] = 4500  # one out-only vertex above the isolated range [4000, 4500), (4500, n)
+    pairs = np.stack([src, dst], axis=1).astype(np.uint32).reshape(-1)
+    g = ctx.from_pairs(n, pairs).build(eg.CSR | eg.CSC)
+    adj = oracle.build_adj(n, pairs)
+    try:
+        for dangling in (False, True):
+            ref = oracle.pagerank_f64(adj, adj.out_deg(), 1.0 / n, 10, dangling=dangling)
+            got, st = g.pagerank(iterations=10, dangling=dangling)
+            l1, mx = rel_errors(got, ref)
+            assert l1 <= PR_REL_L1 and mx <= PR_MAX_REL, (dangling, l1, mx)
+            a, _ = g.pagerank(iterations=7, dangling=dangling)
+            b, _ = g.pagerank(iterations=7, dangling=dangling, use_graph=True)
+            np.testing.assert_array_equal(a, b)
+        for seeds in (np.array([4500], np.uint32), np.array([10, 2000, 10], np.uint32)):
+            ref, it_ref = oracle.ppr_f64(adj, adj.out_deg(), seeds, tol=1e-7, max_iters=50)
+            got, st = g.ppr_single(seeds, tolerance=1e-7, max_iters=50)
+            l1 = np.abs(got - ref).sum() / np.abs(ref).sum()
+            assert l1 <= 1e-5, (seeds, l1)
+            assert abs(st.iterations[0] - it_ref) <= 1
+    finally:
+        g.free()
+
+
 def test_pagerank_tolerance_stops_early(case):
     name, n, pairs, rec, g, gu, adj, adju = case
     got, st = g.pagerank(iterations=200, tolerance=1e-6, dangling=True)
