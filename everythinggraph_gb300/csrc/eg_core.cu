@@ -347,7 +347,7 @@ extern "C" void eg_graph_free(eg_graph *g) {
     cudaStreamSynchronize(c->stream);
     eg_buf *bufs[] = {&g->pairs,        &g->csr.ptr,     &g->csr.col,        &g->csc.ptr,      &g->csc.col,
                       &g->csr.rid,      &g->csc.rid,     &g->csc_p.ptr,      &g->csc_p.col,    &g->csc_p.rid,
-                      &g->perm,         &g->deg_p,
+                      &g->perm,         &g->deg_p,       &g->csc_p_starts,   &g->csc_p_trow,
                       &g->out_deg,      &g->in_deg,      &g->cell_ptr,       &g->gsrc,         &g->gdst,
                       &g->rank,    &g->contrib0,     &g->contrib1,
                       &g->pr_part,      &g->pr_stats,    &g->mp_carry,    &g->errflag,     &g->rank_p,    &g->rank_q,    &g->level,          &g->parent,       &g->dist,
@@ -928,6 +928,24 @@ __global__ void k_relabel_entries(const uint32_t *__restrict__ rid, const uint32
     }
 }
 
+// Row-start bits of the relabelled CSC: bit e of word e/32 is set when entry
+// e begins a row (its row differs from entry e-1's); words past the entries
+// are 0.  One warp per word, the bits from a ballot.
+__global__ void k_row_starts(const uint32_t *__restrict__ rid, uint64_t m, uint64_t nbits, uint32_t *starts) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;  // a multiple of 32: warps stay whole
+    for (uint64_t e = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; e < nbits; e += stride) {
+        const bool s = e < m && (e == 0 || rid[e] != rid[e - 1]);
+        const uint32_t b = __ballot_sync(EG_FULL_MASK, s);
+        if ((threadIdx.x & 31) == 0) starts[e >> 5] = b;
+    }
+}
+// Row of every EG_TROW_SPAN-th entry.
+__global__ void k_trow(const uint32_t *__restrict__ rid, uint64_t m, uint32_t *trow) {
+    const uint64_t nt = (m + EG_TROW_SPAN - 1) / EG_TROW_SPAN;
+    for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += (uint64_t)gridDim.x * blockDim.x)
+        trow[i] = rid[i * EG_TROW_SPAN];
+}
+
 int eg_build_relabeled_csc(eg_graph *g) {
     if (g->relabeled) return EG_OK;
     if (!(g->built & EG_LAYOUT_CSC) || !(g->built & EG_LAYOUT_CSR))
@@ -1000,6 +1018,19 @@ int eg_build_relabeled_csc(eg_graph *g) {
     if (cudaMemsetAsync(hist, 0, (uint64_t)n * 4, ctx->stream) != cudaSuccess) RTRY(eg_fail(EG_ECUDA, "memset"));
     RTRY(eg_histogram(ctx, bp<uint32_t>(g->csc_p.rid), M, hist));
     RTRY(eg_exscan_u32(ctx, hist, bp<uint32_t>(g->csc_p.ptr), n));
+    // row-start bits and the row of every 512th entry: with the rows that
+    // have entries numbered 0 .. rows-1, they give every entry's row
+    const uint64_t nwords = (M + 31) / 32 + EG_STARTS_PAD;
+    RTRY(eg_buf_ensure(ctx, g->csc_p_starts, nwords * 4));
+    RTRY(eg_buf_ensure(ctx, g->csc_p_trow, ((M + EG_TROW_SPAN - 1) / EG_TROW_SPAN + 1) * 4));
+    k_row_starts<<<grid_for(ctx, nwords * 32), 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc_p.rid), M, nwords * 32,
+                                                                      bp<uint32_t>(g->csc_p_starts));
+    ctx->launches++;
+    if (M) {
+        k_trow<<<grid_for(ctx, (M + EG_TROW_SPAN - 1) / EG_TROW_SPAN), 256, 0, ctx->stream>>>(
+            bp<uint32_t>(g->csc_p.rid), M, bp<uint32_t>(g->csc_p_trow));
+        ctx->launches++;
+    }
     if (cudaStreamSynchronize(ctx->stream) != cudaSuccess)
         RTRY(eg_fail(EG_ECUDA, "relabel: %s", cudaGetErrorString(cudaGetLastError())));
 #undef RTRY

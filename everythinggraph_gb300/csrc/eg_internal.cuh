@@ -8,6 +8,8 @@
 #include "eg_gpu.h"
 
 #define EG_FULL_MASK 0xffffffffu
+#define EG_TROW_SPAN 512  // entries per row-of-entry sample (eg_graph::csc_p_trow)
+#define EG_STARTS_PAD 8   // zero words after the row-start bits
 
 // ---------------------------------------------------------------- errors
 int eg_fail(int code, const char *fmt, ...);
@@ -128,6 +130,11 @@ struct eg_graph {
     eg_buf perm, deg_p;
     bool relabeled = false;
     uint32_t csc_p_rows = 0;
+    // csc_p's rows as row-start bits (1 per entry, EG_STARTS_PAD zero words
+    // after them) and the row of every EG_TROW_SPAN-th entry: the row kernel's
+    // compact form of the row-id stream (valid because rows 0 .. csc_p_rows-1
+    // all have entries)
+    eg_buf csc_p_starts, csc_p_trow;
     // grid
     uint32_t grid_p;
     eg_buf cell_ptr, gsrc, gdst;

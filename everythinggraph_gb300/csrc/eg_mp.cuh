@@ -527,11 +527,56 @@ __device__ __forceinline__ void eg_coov_reduce(const eg_red2 &redf, double2 *s_r
     }
 }
 
+// Masked form of the row-id stream: the rows of lane l's entries base+U*l ..
+// base+U*l+U-1 from the row-start bits (one word per lane, bits U*l..U*l+U-1
+// of the chunk's U words) and `rbefore`, the row of the entry before the
+// chunk.  Valid when every row between the first and the last has entries,
+// so that a row start always means the next row.  Entries past E1 get
+// EG_MP_NONE.
+template <int U>
+__device__ __forceinline__ void eg_mask_rows(uint32_t mw, uint32_t lane, uint32_t base, uint32_t E1, uint32_t rbefore,
+                                             uint32_t (&r)[U]) {
+    const uint32_t bits = (mw >> ((U * lane) & 31)) & ((1u << U) - 1u);
+    const uint32_t c = __popc(bits);
+    uint32_t incl = c;  // starts up to this lane's last entry, within the chunk
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        const uint32_t y = __shfl_up_sync(EG_FULL_MASK, incl, off);
+        if (lane >= (uint32_t)off) incl += y;
+    }
+    const uint32_t r0 = rbefore + (incl - c);
+    const uint32_t e = base + U * lane;
+#pragma unroll
+    for (int k = 0; k < U; k++) r[k] = e + k < E1 ? r0 + __popc(bits & ((2u << k) - 1u)) : EG_MP_NONE;
+}
+
+// The columns of a chunk (as eg_coov_load) and, masked, the lane's row-start word.
+template <int U, int HINT>
+__device__ __forceinline__ void eg_coom_load(const uint32_t *__restrict__ col, const uint32_t *__restrict__ starts,
+                                             uint32_t cb, uint32_t E1, uint32_t lane, uint32_t &mw,
+                                             uint32_t (&u)[U], uint64_t pol) {
+    const uint32_t e = cb + U * lane;
+    mw = e < E1 ? __ldg(starts + (e >> 5)) : 0u;  // lanes past the last entry read nothing
+    if (e + U - 1 < E1) {
+#pragma unroll
+        for (int h = 0; h < U / 4; h++) {
+            const uint4 cc = eg_stream_ld4<HINT>(col + e + 4 * h, pol);
+            u[4 * h] = cc.x; u[4 * h + 1] = cc.y; u[4 * h + 2] = cc.z; u[4 * h + 3] = cc.w;
+        }
+    } else {
+#pragma unroll
+        for (int k = 0; k < U; k++) u[k] = e + k < E1 ? __ldg(col + e + k) : 0u;
+    }
+}
+
 // One warp tile t of the row-id stream (the body of k_coov_rows);
-// `gather(e, u)` returns the value of entry e, source u.
-template <class Op, int TILE_E, int U, bool REDUCE, int PF, int HINT, class G>
+// `gather(e, u)` returns the value of entry e, source u.  MK: rows from the
+// row-start bits `starts` and the row of every EG_TROW_SPAN-th entry `trow`
+// instead of the row ids (rid unused).
+template <class Op, int TILE_E, int U, bool REDUCE, int PF, int HINT, bool MK, class G>
 __device__ __forceinline__ void eg_coov_tile(uint32_t t, const uint32_t *__restrict__ rid,
-                                             const uint32_t *__restrict__ col, uint32_t m,
+                                             const uint32_t *__restrict__ col, const uint32_t *__restrict__ starts,
+                                             const uint32_t *__restrict__ trow, uint32_t m,
                                              eg_mp_carry<typename Op::A> *__restrict__ carry, const Op &op,
                                              eg_red2 &redf, const G &gather, uint64_t pol) {
     constexpr uint32_t CH = 32u * U;  // entries per chunk
@@ -540,9 +585,21 @@ __device__ __forceinline__ void eg_coov_tile(uint32_t t, const uint32_t *__restr
     const uint32_t lane = threadIdx.x & 31;
     const uint32_t E0 = t * (uint32_t)TILE_E;
     const uint32_t E1 = min(E0 + (uint32_t)TILE_E, m);
-    const uint32_t first = __ldg(rid + E0);
-    const uint32_t head_row = (E0 > 0 && __ldg(rid + E0 - 1) == first) ? first : EG_MP_NONE;
-    const uint32_t tile_next = E1 < m ? __ldg(rid + E1) : EG_MP_NONE;
+    uint32_t head_row, tile_next;
+    uint32_t rbefore = 0;  // MK: row of the entry before the current chunk
+    uint32_t sb_end = 0;   // MK: entry E1 begins a row
+    if constexpr (MK) {
+        const uint32_t first = __ldg(trow + E0 / EG_TROW_SPAN);
+        const uint32_t sb0 = __ldg(starts + (E0 >> 5)) & 1u;  // E0 is a multiple of 32
+        head_row = (E0 > 0 && !sb0) ? first : EG_MP_NONE;
+        rbefore = first - sb0;  // wraps to 0xffffffff before entry 0: + 1 gives row 0
+        sb_end = E1 < m ? __ldg(starts + (E1 >> 5)) & 1u : 0u;
+        tile_next = EG_MP_NONE;  // (not used: rows are found from the bits)
+    } else {
+        const uint32_t first = __ldg(rid + E0);
+        head_row = (E0 > 0 && __ldg(rid + E0 - 1) == first) ? first : EG_MP_NONE;
+        tile_next = E1 < m ? __ldg(rid + E1) : EG_MP_NONE;
+    }
     uint32_t crow = EG_MP_NONE;
     A cval = op.zero();
     bool head_done = false;
@@ -557,55 +614,81 @@ __device__ __forceinline__ void eg_coov_tile(uint32_t t, const uint32_t *__restr
         const float2 d = op.emit(row, val);
         if (REDUCE) redf.add(d);
     };
-    uint32_t rn[U], un[U];  // prefetched next chunk (PF >= 1)
-    uint32_t rg[U];         // PF 2: rows of the chunk whose gathers are in flight
-    V vg[U];                // PF 2: its gathered values
-    if (PF) eg_coov_load<U, HINT>(rid, col, E0, E1, lane, rn, un, pol);
+    // prefetched next chunk (PF >= 1): row ids (or MK: row-start word) and columns
+    uint32_t rn[U], un[U], mwn = 0;
+    uint32_t rg[U], mwg = 0;  // PF 2: rows (MK: row-start word) of the chunk whose gathers are in flight
+    V vg[U];                  // PF 2: its gathered values
+    auto load = [&](uint32_t cb, uint32_t (&rr)[U], uint32_t &mw, uint32_t (&uu)[U]) {
+        if constexpr (MK) eg_coom_load<U, HINT>(col, starts, cb, E1, lane, mw, uu, pol);
+        else eg_coov_load<U, HINT>(rid, col, cb, E1, lane, rr, uu, pol);
+    };
+    if (PF) load(E0, rn, mwn, un);
     if constexpr (PF == 2) {  // prologue: the first chunk's gathers, the second chunk's words
 #pragma unroll
         for (int k = 0; k < U; k++) {
-            rg[k] = rn[k];
-            vg[k] = rn[k] != EG_MP_NONE ? gather(E0 + U * lane + k, un[k]) : V();
+            const bool in = MK ? E0 + U * lane + k < E1 : rn[k] != EG_MP_NONE;
+            if constexpr (!MK) rg[k] = rn[k];
+            vg[k] = in ? gather(E0 + U * lane + k, un[k]) : V();
         }
-        if (E0 + CH < E1) eg_coov_load<U, HINT>(rid, col, E0 + CH, E1, lane, rn, un, pol);
+        mwg = mwn;
+        if (E0 + CH < E1) load(E0 + CH, rn, mwn, un);
     }
     for (uint32_t base = E0; base < E1; base += CH) {
         const uint32_t e = base + U * lane;
-        uint32_t r[U], u[U];
+        uint32_t r[U], u[U], mw = 0;
         V v[U];
         if constexpr (PF == 2) {
             // this chunk's values arrived during the previous chunk's scan;
             // issue the next chunk's gathers and load the one after, then scan
 #pragma unroll
             for (int k = 0; k < U; k++) {
-                r[k] = rg[k];
+                if constexpr (!MK) r[k] = rg[k];
                 v[k] = vg[k];
             }
+            mw = mwg;
             if (base + CH < E1) {
 #pragma unroll
                 for (int k = 0; k < U; k++) {
-                    rg[k] = rn[k];
-                    vg[k] = rn[k] != EG_MP_NONE ? gather(e + CH + k, un[k]) : V();
+                    const bool in = MK ? e + CH + k < E1 : rn[k] != EG_MP_NONE;
+                    if constexpr (!MK) rg[k] = rn[k];
+                    vg[k] = in ? gather(e + CH + k, un[k]) : V();
                 }
-                if (base + 2 * CH < E1) eg_coov_load<U, HINT>(rid, col, base + 2 * CH, E1, lane, rn, un, pol);
+                mwg = mwn;
+                if (base + 2 * CH < E1) load(base + 2 * CH, rn, mwn, un);
             }
+            if constexpr (MK) eg_mask_rows<U>(mw, lane, base, E1, rbefore, r);
         } else {
             if (PF) {
 #pragma unroll
                 for (int k = 0; k < U; k++) {
-                    r[k] = rn[k];
+                    if constexpr (!MK) r[k] = rn[k];
                     u[k] = un[k];
                 }
-                if (base + CH < E1) eg_coov_load<U, HINT>(rid, col, base + CH, E1, lane, rn, un, pol);
+                mw = mwn;
+                if (base + CH < E1) load(base + CH, rn, mwn, un);
             } else {
-                eg_coov_load<U, HINT>(rid, col, base, E1, lane, r, u, pol);
+                load(base, r, mw, u);
             }
+            if constexpr (MK) {
+                // gathers first: the row computation waits on nothing they need
 #pragma unroll
-            for (int k = 0; k < U; k++) v[k] = r[k] != EG_MP_NONE ? gather(e + k, u[k]) : V();
+                for (int k = 0; k < U; k++) v[k] = e + k < E1 ? gather(e + k, u[k]) : V();
+                eg_mask_rows<U>(mw, lane, base, E1, rbefore, r);
+            } else {
+#pragma unroll
+                for (int k = 0; k < U; k++) v[k] = r[k] != EG_MP_NONE ? gather(e + k, u[k]) : V();
+            }
         }
         // row of the entry after this lane's last one
         uint32_t nxt = __shfl_down_sync(EG_FULL_MASK, r[0], 1);
-        if (lane == 31) nxt = base + CH < E1 ? __ldg(rid + base + CH) : tile_next;
+        if (lane == 31) {
+            if constexpr (MK) {
+                if (base + CH < E1) nxt = r[U - 1] + (__ldg(starts + ((base + CH) >> 5)) & 1u);
+                else nxt = E1 < m ? r[U - 1] + sb_end : EG_MP_NONE;
+            } else {
+                nxt = base + CH < E1 ? __ldg(rid + base + CH) : tile_next;
+            }
+        }
         const uint32_t prev_last = __shfl_up_sync(EG_FULL_MASK, r[U - 1], 1);
         // local runs: head run (from entry 0), middle runs, tail run (to entry U-1)
         A hsum = op.add(op.zero(), v[0]);
@@ -650,10 +733,11 @@ __device__ __forceinline__ void eg_coov_tile(uint32_t t, const uint32_t *__restr
         if (nxt != r[U - 1]) finish(r[U - 1], x);
         crow = __shfl_sync(EG_FULL_MASK, r[U - 1], 31);
         cval = eg_shfl_idx(x, 31);
+        rbefore = crow;  // MK: the next chunk starts after this row's entry
     }
     const uint32_t hmask = __ballot_sync(EG_FULL_MASK, head_done);
     if (lane == 0) {
-        const bool tail_open = E1 < m && crow != EG_MP_NONE && tile_next == crow;
+        const bool tail_open = E1 < m && crow != EG_MP_NONE && (MK ? sb_end == 0u : tile_next == crow);
         carry[t].tail_row = tail_open ? crow : EG_MP_NONE;
         carry[t].tail_val = cval;
         carry[t].head_row = hmask ? head_row : EG_MP_NONE;
@@ -680,13 +764,19 @@ __device__ __forceinline__ void eg_coov_tile(uint32_t t, const uint32_t *__restr
 // before the current chunk's scan, so their latency hides behind the scan.  MINB: resident CTAs per SM asked of the compiler,
 // which bounds the registers per thread (6: 42, 8: every warp slot, 32).
 // HINT: cache hints on the streamed words (eg_stream_ld4).
-template <class Op, int TILE_E, int U, bool REDUCE, int PF = 0, int MINB = 6, int HINT = 0>
+// MK: rows from the row-start bits `starts` and the row samples `trow`
+// (eg_mask_rows) instead of the row ids: 4.1 instead of 8 streamed bytes per
+// entry, for layouts whose rows 0 .. last all have entries.
+template <class Op, int TILE_E, int U, bool REDUCE, int PF = 0, int MINB = 6, int HINT = 0, bool MK = false>
 __global__ void __launch_bounds__(256, MINB) k_coov_rows(const uint32_t *__restrict__ rid,
                                                          const uint32_t *__restrict__ col, uint32_t m, uint32_t ntiles,
                                                          eg_mp_carry<typename Op::A> *__restrict__ carry,
-                                                         double2 *__restrict__ part, Op op) {
+                                                         double2 *__restrict__ part, Op op,
+                                                         const uint32_t *__restrict__ starts = nullptr,
+                                                         const uint32_t *__restrict__ trow = nullptr) {
     static_assert(U == 4 || U == 8, "4 or 8 entries per lane");
     static_assert(TILE_E % (32 * U) == 0, "tiles hold whole chunks");
+    static_assert(!MK || TILE_E % EG_TROW_SPAN == 0, "tiles start at a row sample");
     __shared__ double2 s_red[8];
     if (!op.active()) return;
     op.setup();
@@ -694,7 +784,8 @@ __global__ void __launch_bounds__(256, MINB) k_coov_rows(const uint32_t *__restr
     const uint64_t pol = HINT ? eg_l2_evict_first_policy() : 0;
     eg_red2 redf;
     if (t < ntiles)
-        eg_coov_tile<Op, TILE_E, U, REDUCE, PF, HINT>(
-            t, rid, col, m, carry, op, redf, [&](uint32_t e, uint32_t u) { return op.gather(e, u); }, pol);
+        eg_coov_tile<Op, TILE_E, U, REDUCE, PF, HINT, MK>(
+            t, rid, col, starts, trow, m, carry, op, redf, [&](uint32_t e, uint32_t u) { return op.gather(e, u); },
+            pol);
     if (REDUCE) eg_coov_reduce(redf, s_red, 8, part);
 }

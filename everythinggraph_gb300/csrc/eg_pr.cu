@@ -276,10 +276,11 @@ static const RowCfg kRowCfg[EG_ROW_CFGS] = {
     {1024, 8, 1, 4, 0}, {1024, 4, 0, 8, 0}, {2048, 8, 0, 5, 0}, {1024, 4, 1, 5, 1}, {2048, 4, 1, 5, 1},
     {1024, 4, 2, 4, 0}, {2048, 4, 2, 4, 0}};
 
-template <class Op, int TILE, int U, bool REDUCE, int PF, int MINB, int HINT = 0>
+template <class Op, int TILE, int U, bool REDUCE, int PF, int MINB, int HINT = 0, bool MK = false>
 static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts,
                         cudaEvent_t ev_begin, cudaEvent_t ev_end, uint64_t m_entries, bool empty_rows,
                         uint32_t empty_from) {
+    static_assert(!MK || TILE % EG_TROW_SPAN == 0, "masked tiles start at a row sample");
     eg_ctx *ctx = g->ctx;
     using A = typename Op::A;
     const uint32_t m = (uint32_t)(m_entries == EG_ALL_ENTRIES ? g->m : m_entries);
@@ -295,8 +296,10 @@ static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *pa
     if (g2 > (uint32_t)ctx->sm_count * 8) g2 = (uint32_t)ctx->sm_count * 8;
     if (g1) {
         if (ev_begin) EG_CUDA(cudaEventRecord(ev_begin, ctx->stream));
-        k_coov_rows<Op, TILE, U, REDUCE, PF, MINB, HINT><<<g1, 256, 0, ctx->stream>>>(
-                bp<uint32_t>(adj.rid), bp<uint32_t>(adj.col), m, ntiles, bp<eg_mp_carry<A>>(carry_buf), part, op);
+        // MK: the relabelled CSC's row-start bits stand in for its row ids
+        k_coov_rows<Op, TILE, U, REDUCE, PF, MINB, HINT, MK><<<g1, 256, 0, ctx->stream>>>(
+                bp<uint32_t>(adj.rid), bp<uint32_t>(adj.col), m, ntiles, bp<eg_mp_carry<A>>(carry_buf), part, op,
+                MK ? bp<uint32_t>(g->csc_p_starts) : nullptr, MK ? bp<uint32_t>(g->csc_p_trow) : nullptr);
         EG_LAUNCHED(ctx);
         if (ev_end) EG_CUDA(cudaEventRecord(ev_end, ctx->stream));
     }
@@ -320,14 +323,15 @@ static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *pa
 // m_entries: the entries of `adj` (EG_ALL_ENTRIES: the graph's m); without
 // empty_rows the rows that have no entries in `adj` are left as they are.
 // empty_from <= n: the rows without entries are exactly [empty_from, n).
-template <class Op, bool REDUCE>
+// MK: `adj` is the relabelled CSC, read through its row-start bits.
+template <class Op, bool REDUCE, bool MK = false>
 static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts,
                       cudaEvent_t ev_begin = nullptr, cudaEvent_t ev_end = nullptr,
                       uint64_t m_entries = EG_ALL_ENTRIES, bool empty_rows = true, uint32_t empty_from = EG_NO_RANGE) {
-#define EG_ROW_CASE(i, T, U, PF, MB, H)                                                                         \
-    case i:                                                                                                     \
-        return coo_launch_t<Op, T, U, REDUCE, PF, MB, H>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end, \
-                                                          m_entries, empty_rows, empty_from);
+#define EG_ROW_CASE(i, T, U, PF, MB, H)                                                                             \
+    case i:                                                                                                         \
+        return coo_launch_t<Op, T, U, REDUCE, PF, MB, H, MK>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end, \
+                                                              m_entries, empty_rows, empty_from);
     switch (g->row_cfg) {
         EG_ROW_CASE(1, 2048, 4, false, 6, 0)
         EG_ROW_CASE(2, 2048, 4, true, 5, 0)
@@ -341,8 +345,8 @@ static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part
         EG_ROW_CASE(10, 1024, 4, 2, 4, 0)
         EG_ROW_CASE(11, 2048, 4, 2, 4, 0)
         default:
-            return coo_launch_t<Op, 1024, 4, REDUCE, true, 5>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end,
-                                                              m_entries, empty_rows, empty_from);
+            return coo_launch_t<Op, 1024, 4, REDUCE, true, 5, 0, MK>(g, adj, carry_buf, part, op, nparts, ev_begin,
+                                                                     ev_end, m_entries, empty_rows, empty_from);
     }
 #undef EG_ROW_CASE
 }
@@ -421,10 +425,10 @@ static int pr_iterations(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, d
             // after the last pass (a block may have no entries, and so no row kernel)
             if (t) EG_CUDA(cudaEventRecord(ctx->evk[2 * it + 1], ctx->stream));
         } else {
-            EG_TRY((coo_launch<PrOp<COMP>, REDUCE>(g, g->csc_p, carry, part, op, &nparts,
-                                                    t ? ctx->evk[2 * it] : nullptr,
-                                                    t ? ctx->evk[2 * it + 1] : nullptr, EG_ALL_ENTRIES, true,
-                                                    g->csc_p_rows)));
+            EG_TRY((coo_launch<PrOp<COMP>, REDUCE, true>(g, g->csc_p, carry, part, op, &nparts,
+                                                          t ? ctx->evk[2 * it] : nullptr,
+                                                          t ? ctx->evk[2 * it + 1] : nullptr, EG_ALL_ENTRIES, true,
+                                                          g->csc_p_rows)));
         }
         if (o.tolerance > 0.0) {  // the L1 change, after the row kernels (coalesced, 8 bytes per vertex)
             k_pr_residual<<<EG_PR_RES_BLOCKS, 256, 0, ctx->stream>>>(rank_new, rank_old, g->n, st, part + nparts);
@@ -467,8 +471,8 @@ static int pr_graph(eg_graph *g, const eg_pr_opts &o, bool reduce, eg_pr_dev *st
     key[8] = (uint64_t)(uintptr_t)st;
     key[9] = (uint64_t)(uintptr_t)part;
     key[10] = (uint64_t)(uintptr_t)carry.p;
-    key[11] = (uint64_t)(uintptr_t)g->csc_p.rid.p;
-    key[12] = (uint64_t)(uintptr_t)g->csc_p.col.p;
+    key[11] = (uint64_t)(uintptr_t)g->csc_p.rid.p ^ ((uint64_t)(uintptr_t)g->csc_p_starts.p << 17);
+    key[12] = (uint64_t)(uintptr_t)g->csc_p.col.p ^ ((uint64_t)(uintptr_t)g->csc_p_trow.p << 17);
     key[13] = (uint64_t)(uintptr_t)g->csc_p.ptr.p;
     key[14] = g->m ^ ((uint64_t)g->row_cfg << 56) ^ ((uint64_t)pr_block_log2(g, o) << 48);
     key[15] = (uint64_t)ctx->stream ^ 0x5052ull;
