@@ -32,7 +32,7 @@ METRIC, UNIT = "GTEPS", "GTEPS"
 # ncu capture of PageRank on directed RMAT-22 (the kernel's traffic grows with
 # the entries); the summary and its command are in
 # profiles/k_coov_rows_pagerank_rmat22.md.
-PR_ROWS_DRAM_BYTES_PER_ENTRY = (557.354e6 + 6.059e6) / 67108864
+PR_ROWS_DRAM_BYTES_PER_ENTRY = (294.009e6 + 3.622e6) / 67108864
 
 
 def peaks():
@@ -262,7 +262,7 @@ def kernel_reports(ctx, eg, scale, args):
         "ms_per_iter": it_ms, "gbps": bytes_it / (it_ms / 1e3) / 1e9, "gteps": m / (it_ms / 1e3) / 1e9,
         "row_kernel_ms": st.row_kernel_ms, "row_kernel_gbps": bytes_it / (st.row_kernel_ms / 1e3) / 1e9,
         "ms_per_iter_graph_replay": stg.ms / 10, "bytes_per_iter": bytes_it,
-        "bytes_rule": "8 per CSC entry (row id + column) + 16 per vertex (contribution, degree, rank, next contribution)",
+        "bytes_rule": "8 per CSC entry (column + gathered contribution) + 16 per vertex (row start, degree, rank and next-contribution writes)",
         "build_ms": g.info().build_ms, "m": m,
         "schedule": dict(cands[chosen], candidates=cands)}
     g.free()
