@@ -97,6 +97,26 @@ def dist_env():
 E2E_BATCH = 32  # roots per eg_bfs_batch call in the end-to-end step
 
 
+def rank_reduce(x, op="max", device=None):
+    """x reduced over the ranks of the default process group ("max" or
+    "sum"); x itself without a group or with one rank."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(x)
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX if op == "max" else dist.ReduceOp.SUM)
+    return float(t.item())
+
+
+def replica_throughput(units, seconds, device=None):
+    """Whole-job rate of independent replicas: the units every rank processed
+    over the slowest rank's time, in 10^9 units per second; and that time."""
+    total = rank_reduce(units, "sum", device)
+    slowest = rank_reduce(seconds, "max", device)
+    return total / slowest / 1e9, slowest
+
+
 def run_ours(args):
     import torch
 
@@ -168,26 +188,23 @@ def run_ours(args):
         e1.record(stream)
         torch.cuda.synchronize()
     launches = ctx.kernel_launches - l0
-    ms = e0.elapsed_time(e1)
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    ms_step = ms / args.steps
-    value = edges * world / (ms / 1e3) / 1e9
+    # all ranks' edges over the slowest rank's device time
+    value, slowest_s = replica_throughput(edges, e0.elapsed_time(e1) / 1e3, device="cuda")
+    ms_step = slowest_s * 1e3 / args.steps
     # ---- end-to-end through the C ABI with host outputs (levels, parents, labels),
     # after one untimed step of its own (first use of the output slots and of
     # the page-locked buffers)
     step(True)
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     te0 = time.perf_counter()
     e_edges = 0
     for _ in range(args.steps):
         te, _ = step(True)
         e_edges += te
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - te0
+    e2e_value, e2e_s = replica_throughput(e_edges, time.perf_counter() - te0, device="cuda")
     d2h = (W["roots"] * 2 * 4 * n + 8 * n)
     h2d = W["roots"] * 4
     # ---- per-kernel reports on the same graph size
@@ -226,7 +243,7 @@ def run_ours(args):
         "vs_baseline": None, "dtype": "u32", "data": "synthetic (device RMAT generator)",
         "config": dict(W, n=n, m_adjacency=2 * m_in, l2="inputs larger than L2 (CSR 2.1 GB)",
                        parallelism="replicas" if world > 1 else "single"),
-        "e2e": {"value": e_edges * world / e2e_s / 1e9, "unit": UNIT, "h2d_bytes_per_step": h2d,
+        "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3 / args.steps, "host_buffers": "page-locked (eg_host_alloc), reused by every call",
                 "api": "eg_bfs_batch (%d roots per call, copies overlapped with the next traversal) + eg_wcc" % E2E_BATCH},
         "gpu_launches": launches,
