@@ -425,10 +425,15 @@ static int pr_iterations(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, d
             // after the last pass (a block may have no entries, and so no row kernel)
             if (t) EG_CUDA(cudaEventRecord(ctx->evk[2 * it + 1], ctx->stream));
         } else {
+            // rows without in-edges get base (the teleport) alone: with no
+            // dangling mass or seed weights moving it, base is the same every
+            // iteration, so once both rank buffers and the contribution
+            // buffer(s) hold it (iterations 0 and 1) those rows stay written
+            const bool fixed_base = !o.dangling && ps.count == 0;
             EG_TRY((coo_launch<PrOp<COMP>, REDUCE, true>(g, g->csc_p, carry, part, op, &nparts,
                                                           t ? ctx->evk[2 * it] : nullptr,
-                                                          t ? ctx->evk[2 * it + 1] : nullptr, EG_ALL_ENTRIES, true,
-                                                          g->csc_p_rows)));
+                                                          t ? ctx->evk[2 * it + 1] : nullptr, EG_ALL_ENTRIES,
+                                                          !fixed_base || it < 2, g->csc_p_rows)));
         }
         if (o.tolerance > 0.0) {  // the L1 change, after the row kernels (coalesced, 8 bytes per vertex)
             k_pr_residual<<<EG_PR_RES_BLOCKS, 256, 0, ctx->stream>>>(rank_new, rank_old, g->n, st, part + nparts);
