@@ -970,7 +970,7 @@ static int sb_spmv(eg_graph *g, int kind, int vk, uint64_t seed) {
         view.rid.p = bp<uint32_t>(sb.rid) + s0;
         const int acc = b > 0 ? 1 : 0;
         if (kind == EG_SPMV_F32) {
-            SpmvF32Op<false> op{bp<float>(g->spmv_x), bp<float>(sb.vals) + s0, bp<float>(g->spmv_y), acc};
+            SpmvF32Op<false> op{bp<float>(g->spmv_x), bp<float>(sb.vals) + s0, bp<float>(g->spmv_y), acc, 0, nullptr};
             EG_TRY((coo_launch<SpmvF32Op<false>, false>(g, view, g->mp_carry, nullptr, op, &np, nullptr, nullptr, len,
                                                          b == 0)));
         } else {
@@ -1049,7 +1049,7 @@ extern "C" int eg_spmv(eg_graph *g, const eg_spmv_opts *opts, const void *x, voi
                 EG_TRY(sb_spmv(g, kind, opts->unit_values ? 1 : 2, opts->value_seed));
                 break;
             }
-            SpmvF32Op<false> op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<float>(g->spmv_y), 0};
+            SpmvF32Op<false> op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<float>(g->spmv_y), 0, 0, nullptr};
             EG_TRY((coo_launch<SpmvF32Op<false>, false>(g, adj, carry, nullptr, op, &np)));
             break;
         }
@@ -1058,12 +1058,12 @@ extern "C" int eg_spmv(eg_graph *g, const eg_spmv_opts *opts, const void *x, voi
                 EG_TRY(sb_spmv(g, kind, opts->unit_values ? 1 : 2, opts->value_seed));
                 break;
             }
-            SpmvF32Op<true> op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<float>(g->spmv_y), 0};
+            SpmvF32Op<true> op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<float>(g->spmv_y), 0, 0, nullptr};
             EG_TRY((coo_launch<SpmvF32Op<true>, false>(g, adj, carry, nullptr, op, &np)));
             break;
         }
         case EG_SPMV_F64: {
-            SpmvF64Op op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<double>(g->spmv_y)};
+            SpmvF64Op op{bp<float>(g->spmv_x), bp<float>(g->spmv_vals), bp<double>(g->spmv_y), 0};
             EG_TRY((coo_launch<SpmvF64Op, false>(g, adj, carry, nullptr, op, &np)));
             break;
         }
