@@ -15,7 +15,7 @@ static void s_reset(struct node *n) { (void)n; }
 static void s_main(struct node *n) {
     (void)n;
     for (uint32_t i = 0; i < NB_NODES; i++) x[i] = i;
-    eg_spmv_opts o = {EG_SPMV_U32_PUSH, 0, 0};
+    eg_spmv_opts o = {.kind = EG_SPMV_U32_PUSH}; /* the other fields 0: CSR/CSC path, u32 x */
     if (load_mode == 8) o.kind = EG_SPMV_U32_EDGE;
     else if (mode == PULL) o.kind = EG_SPMV_U32_PULL;
     float ms = 0;
