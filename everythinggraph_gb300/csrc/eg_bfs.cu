@@ -873,8 +873,7 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
                                                  level, parent, q[0], 1u, EG_FDEG_UNKNOWN, 1, threshold,
                                                  o.direction == EG_BFS_AUTO ? 1 : 0, dsm, cnt);
         EG_LAUNCHED(ctx);
-        EG_TRY(eg_readback(ctx, hsm, dsm, sizeof(BfsSmallOut), ctx->stream));
-        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        EG_TRY(eg_readback_wait(ctx, hsm, dsm, sizeof(BfsSmallOut), ctx->stream));
         count = qlen = hsm->qlen;
         fdeg = hsm->fdeg;
         reached += hsm->reached;
@@ -882,8 +881,7 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
         lvl = hsm->lvl;
         bm_valid = hsm->levels == 0;  // else bm[0] still holds only the root
     } else {
-        EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream, true));  // and clears them
-        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        EG_TRY(eg_readback_wait(ctx, h, cnt, sizeof(BfsCounters), ctx->stream, true));  // and clears them
         fdeg = h->next_deg;
         traversed = fdeg;
     }
@@ -898,8 +896,7 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
                 bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), deg, visited, level, parent, q[cur], qlen, fdeg,
                 lvl, threshold, o.direction == EG_BFS_AUTO ? 1 : 0, dsm, cnt);
             EG_LAUNCHED(ctx);
-            EG_TRY(eg_readback(ctx, hsm, dsm, sizeof(BfsSmallOut), ctx->stream));
-            EG_CUDA(cudaStreamSynchronize(ctx->stream));
+            EG_TRY(eg_readback_wait(ctx, hsm, dsm, sizeof(BfsSmallOut), ctx->stream));
             count = qlen = hsm->qlen;
             fdeg = hsm->fdeg;
             reached += hsm->reached;
@@ -961,8 +958,7 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
             }
             have_queue = make_queue;
         }
-        EG_TRY(eg_readback(ctx, h, cnt, sizeof(BfsCounters), ctx->stream, true));  // and clears them
-        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        EG_TRY(eg_readback_wait(ctx, h, cnt, sizeof(BfsCounters), ctx->stream, true));  // and clears them
         count = h->next_count;
         fdeg = h->next_deg;
         qlen = h->qsize;

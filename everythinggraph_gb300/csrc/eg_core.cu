@@ -10,6 +10,8 @@
 #include <string.h>
 #include <sys/stat.h>
 
+#include <time.h>
+
 #include "eg_internal.cuh"
 
 // ============================================================== errors
@@ -42,6 +44,7 @@ extern "C" int eg_open(int device, uint64_t hbm_budget_bytes, eg_ctx **out) {
     EG_CUDA(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
     EG_CUDA(cudaMallocHost(&c->h_pinned, 1 << 20));
     EG_CUDA(cudaHostGetDevicePointer(&c->h_pinned_dev, c->h_pinned, 0));
+    *reinterpret_cast<uint32_t *>(static_cast<char *>(c->h_pinned) + EG_RB_FLAG_OFF) = 0;  // no readback yet
     EG_CUDA(cudaEventCreate(&c->ev0));
     EG_CUDA(cudaEventCreate(&c->ev1));
     for (cudaEvent_t &e : c->evk) EG_CUDA(cudaEventCreate(&e));
@@ -52,10 +55,18 @@ extern "C" int eg_open(int device, uint64_t hbm_budget_bytes, eg_ctx **out) {
 }
 
 namespace {
-__global__ void k_readback(uint32_t *src, uint32_t *dst, uint32_t words, int clear) {
+// One warp copies `words` to pinned host memory (and clears them); with a
+// flag, every lane's stores are made visible system-wide before lane 0
+// writes `seq` to the flag word.
+__global__ void k_readback(uint32_t *src, uint32_t *dst, uint32_t words, int clear, uint32_t *flag, uint32_t seq) {
     for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) {
         dst[i] = src[i];
         if (clear) src[i] = 0u;
+    }
+    if (flag) {
+        __threadfence_system();
+        __syncwarp();
+        if (threadIdx.x == 0) *(volatile uint32_t *)flag = seq;
     }
 }
 __global__ void k_zero(uint32_t *p, uint64_t words) {
@@ -75,14 +86,43 @@ int eg_zero(eg_ctx *c, void *dev, uint64_t bytes, cudaStream_t st) {
     return EG_OK;
 }
 
-int eg_readback(eg_ctx *c, void *host_dst, const void *dev_src, uint32_t bytes, cudaStream_t st, bool clear) {
+static int readback_launch(eg_ctx *c, void *host_dst, const void *dev_src, uint32_t bytes, cudaStream_t st, bool clear,
+                           uint32_t *flag_dev, uint32_t seq) {
     const uintptr_t off = (uintptr_t)host_dst - (uintptr_t)c->h_pinned;
-    if ((uintptr_t)host_dst < (uintptr_t)c->h_pinned || off + bytes > (1u << 20) || (off & 3) || ((uintptr_t)dev_src & 3))
+    if ((uintptr_t)host_dst < (uintptr_t)c->h_pinned || off + bytes > EG_RB_FLAG_OFF || (off & 3) ||
+        ((uintptr_t)dev_src & 3))
         return eg_fail(EG_EINVAL, "readback outside the pinned staging area");
     k_readback<<<1, 32, 0, st>>>(static_cast<uint32_t *>(const_cast<void *>(dev_src)),
                                  reinterpret_cast<uint32_t *>(static_cast<char *>(c->h_pinned_dev) + off),
-                                 (bytes + 3) / 4, clear ? 1 : 0);
+                                 (bytes + 3) / 4, clear ? 1 : 0, flag_dev, seq);
     EG_LAUNCHED(c);
+    return EG_OK;
+}
+
+int eg_readback(eg_ctx *c, void *host_dst, const void *dev_src, uint32_t bytes, cudaStream_t st, bool clear) {
+    return readback_launch(c, host_dst, dev_src, bytes, st, clear, nullptr, 0);
+}
+
+int eg_readback_wait(eg_ctx *c, void *host_dst, const void *dev_src, uint32_t bytes, cudaStream_t st, bool clear) {
+    uint32_t seq = ++c->rb_seq;
+    if (seq == 0) seq = ++c->rb_seq;  // 0 is the flag's value before any readback
+    uint32_t *flag_dev = reinterpret_cast<uint32_t *>(static_cast<char *>(c->h_pinned_dev) + EG_RB_FLAG_OFF);
+    uint32_t *flag = reinterpret_cast<uint32_t *>(static_cast<char *>(c->h_pinned) + EG_RB_FLAG_OFF);
+    // the flag holds an earlier value; make sure of it before the launch
+    __atomic_store_n(flag, seq - 1u, __ATOMIC_SEQ_CST);
+    __atomic_thread_fence(__ATOMIC_SEQ_CST);
+    EG_TRY(readback_launch(c, host_dst, dev_src, bytes, st, clear, flag_dev, seq));
+    timespec t0, t1;
+    clock_gettime(CLOCK_MONOTONIC, &t0);
+    for (uint32_t i = 1;; i++) {
+        if (__atomic_load_n(flag, __ATOMIC_ACQUIRE) == seq) return EG_OK;  // the words before it are visible
+        if ((i & 4095u) == 0) {
+            clock_gettime(CLOCK_MONOTONIC, &t1);
+            if ((t1.tv_sec - t0.tv_sec) + 1e-9 * (double)(t1.tv_nsec - t0.tv_nsec) > 1.0) break;
+        }
+    }
+    EG_CUDA(cudaStreamSynchronize(st));  // a device error surfaces here
+    if (__atomic_load_n(flag, __ATOMIC_ACQUIRE) != seq) return eg_fail(EG_ETIMEOUT, "readback flag not raised");
     return EG_OK;
 }
 
@@ -277,9 +317,10 @@ extern "C" int eg_graph_from_file(eg_ctx *ctx, const char *path, uint32_t n, uns
         return rc;
     }
     eg_graph *g = *out;
-    // stream the file through the 1 MiB pinned staging; 12-byte records are
-    // compacted to [src][dst] pairs in place (pair i lands at 8i <= 12i)
-    const uint64_t per = (1u << 20) / rec;  // records per piece
+    // stream the file through the pinned staging (short of its readback flag
+    // word); 12-byte records are compacted to [src][dst] pairs in place
+    // (pair i lands at 8i <= 12i)
+    const uint64_t per = EG_RB_FLAG_OFF / rec;  // records per piece
     uint64_t done = 0;
     while (done < m) {
         const uint64_t cnt = m - done < per ? m - done : per;

@@ -55,7 +55,10 @@ struct eg_ctx {
     int live_graphs;              // eg_close refuses while graphs are alive
     cudaStream_t copy_stream;     // device-to-host copies overlapped with the next traversal
     cudaEvent_t ev_out[2 * EG_OUT_SLOTS];  // [slot]: outputs ready, [EG_OUT_SLOTS + slot]: copied out
+    uint32_t rb_seq = 0;                   // eg_readback_wait: the last flag value asked for
 };
+// eg_readback_wait's flag word: the last 64 bytes of the pinned staging area
+#define EG_RB_FLAG_OFF ((1u << 20) - 64u)
 
 int eg_dmalloc(eg_ctx *ctx, void **p, uint64_t bytes);
 void eg_dfree(eg_ctx *ctx, void *p, uint64_t bytes);
@@ -73,6 +76,12 @@ int eg_buf_ensure(eg_ctx *ctx, eg_buf &b, uint64_t bytes);  // grows (contents l
 // With `clear` the kernel also zeroes the device words after reading them.
 int eg_readback(eg_ctx *ctx, void *host_dst, const void *dev_src, uint32_t bytes, cudaStream_t st,
                 bool clear = false);
+// The same, and returns once the words are on the host: the kernel raises a
+// flag in pinned memory after them and the host polls it (no stream
+// synchronisation per call).  The poll gives up after a second and falls back
+// to synchronising `st`, which reports any device error.
+int eg_readback_wait(eg_ctx *ctx, void *host_dst, const void *dev_src, uint32_t bytes, cudaStream_t st,
+                     bool clear = false);
 // Zeroes `bytes` (a multiple of 4, 4-byte aligned) of device memory with a
 // kernel, for the same reason: a memset may be carried out by a copy engine.
 int eg_zero(eg_ctx *ctx, void *dev, uint64_t bytes, cudaStream_t st);

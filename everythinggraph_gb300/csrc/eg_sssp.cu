@@ -220,8 +220,7 @@ extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wrule_in, u
         // the marked vertices become the next queue; their bits are cleared
         k_bm_queue<<<blocks_for(ctx, (uint64_t)nw * 32), 256, 0, ctx->stream>>>(bm, n, q[nxt], &cnt->qsize, 1);
         EG_LAUNCHED(ctx);
-        EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(SsspCounters), cudaMemcpyDeviceToHost, ctx->stream));
-        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        EG_TRY(eg_readback_wait(ctx, h, cnt, sizeof(SsspCounters), ctx->stream));
         qlen = h->qsize;
         relax = h->relax;
         cur = nxt;
@@ -444,8 +443,7 @@ extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg
         // the current frontier's words and bits are cleared for reuse as "next"
         k_msssp_clear<<<blocks_for(ctx, (uint64_t)qlen * kw), 256, 0, ctx->stream>>>(q[cur], qlen, kw, act[cur], inq[cur]);
         EG_LAUNCHED(ctx);
-        EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(SsspCounters), cudaMemcpyDeviceToHost, ctx->stream));
-        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        EG_TRY(eg_readback_wait(ctx, h, cnt, sizeof(SsspCounters), ctx->stream));
         qlen = h->qsize;
         relax = h->relax;
         cur = nxt;
