@@ -558,8 +558,7 @@ static int pr_run(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, uint32_t
             const int it1 = it0 + chunk < o.iterations ? it0 + chunk : o.iterations;
             EG_TRY(pr_dispatch(g, o, ps, tele_div, reduce, st, part, carry, true, it0, it1));
             if (o.tolerance > 0.0 && it1 < o.iterations) {
-                EG_CUDA(cudaMemcpyAsync(hdone, &st->done, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
-                EG_CUDA(cudaStreamSynchronize(ctx->stream));
+                EG_TRY(eg_readback_wait(ctx, hdone, &st->done, sizeof(int), ctx->stream));
                 if (*hdone) break;
             }
         }
