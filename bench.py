@@ -30,8 +30,7 @@ WORKLOAD = {"workload": "bfs64+wcc rmat24 undirected", "scale": 24, "edgefactor"
 METRIC, UNIT = "GTEPS", "GTEPS"
 # DRAM bytes (read + write) of one row-kernel launch per CSC entry, from an
 # ncu capture of PageRank on directed RMAT-22 (the kernel's traffic grows with
-# the entries); the summary and its command are in
-# profiles/k_coov_rows_pagerank_rmat22.md.
+# the entries).
 PR_ROWS_DRAM_BYTES_PER_ENTRY = (294.009e6 + 3.622e6) / 67108864
 
 
@@ -168,7 +167,7 @@ def run_ours(args):
                 lv, par, st = g.bfs(int(r), parents=True, copy_out=False, host_loop=bfs_form)
                 traversed += st.edges_traversed
         lab, wst = g.wcc(copy_out=copy_out, out=lab_h)
-        return traversed + m_in, wst
+        return traversed + m_in, traversed
 
     for _ in range(max(args.warmup, 0)):
         step(False)
@@ -179,18 +178,22 @@ def run_ours(args):
     l0 = ctx.kernel_launches
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    edges = 0
+    edges = bfs_entries = 0
     with Clocks(local) as clk:
         e0.record(stream)
         for _ in range(args.steps):
-            te, _ = step(False)
+            te, tb = step(False)
             edges += te
+            bfs_entries += tb
         e1.record(stream)
         torch.cuda.synchronize()
     launches = ctx.kernel_launches - l0
     # all ranks' edges over the slowest rank's device time
     value, slowest_s = replica_throughput(edges, e0.elapsed_time(e1) / 1e3, device="cuda")
     ms_step = slowest_s * 1e3 / args.steps
+    # Graph500 counts each undirected edge of the traversed component once:
+    # half the adjacency entries the BFS runs traverse (+ WCC's input edges)
+    g500 = (bfs_entries / 2 + (edges - bfs_entries)) / (edges / value) if edges else 0.0
     # ---- end-to-end through the C ABI with host outputs (levels, parents, labels),
     # after one untimed step of its own (first use of the output slots and of
     # the page-locked buffers)
@@ -210,58 +213,81 @@ def run_ours(args):
     # ---- per-kernel reports on the same graph size
     kernels = {}
     if not args.no_extras:
-        try:
-            kernels["msbfs_64_roots"] = msbfs_report(g, roots)
-        except Exception as ex:  # reported, not fatal for the headline
-            kernels["msbfs_64_roots"] = {"error": str(ex)}
-        try:
-            kernels["serve"] = serve_report(ctx, eg, scale, args.rate, args.queries, g=g, exclusive=args.serve_exclusive, gang=not args.serve_no_gang)
-        except Exception as ex:
-            kernels["serve"] = {"error": str(ex)}
+        for name, fn in (("msbfs64", lambda: msbfs_report(g, roots)),
+                         ("serve", lambda: serve_sweep(ctx, eg, scale, args, g))):
+            try:
+                kernels[name] = fn()
+            except Exception as ex:  # reported, not fatal for the headline
+                kernels[name] = {"error": str(ex)[:200]}
         kernels.update(kernel_reports(ctx, eg, scale, args))
         for name, fn in (("spmv_er25", lambda: spmv_report(ctx, eg, 25 if scale >= 24 else scale, 32)),
                          ("sssp_rmat23_256", lambda: sssp_report(ctx, eg, 23 if scale >= 24 else scale - 1)),
-                         ("ppr_32_queries", lambda: ppr_report(ctx, eg, scale))):
+                         ("ppr32", lambda: ppr_report(ctx, eg, scale))):
             try:
                 kernels[name] = fn()
             except Exception as ex:
-                kernels[name] = {"error": str(ex)}
+                kernels[name] = {"error": str(ex)[:200]}
     hbm, src = peaks()
-    dom = kernels.get("pagerank_pull_rmat%d" % scale)
+    dom = kernels.get("pr_rmat%d" % scale)
     roof = None
-    if dom:
-        roof = {"bound": "hbm", "achieved": dom["row_kernel_gbps"], "peak": hbm, "unit": "GB/s",
-                "frac": dom["row_kernel_gbps"] / hbm,
-                "traffic": PR_ROWS_DRAM_BYTES_PER_ENTRY * dom["m"] if PR_ROWS_DRAM_BYTES_PER_ENTRY else None,
-                "kernel": "k_coov_rows<PrOp<0>, %d, %d> prefetch=%d min_blocks=%d (PageRank pull, RMAT-%d directed)"
-                          % (dom["schedule"]["tile"], dom["schedule"]["per_lane"], dom["schedule"]["prefetch"],
-                             dom["schedule"]["min_blocks"], scale),
-                "algorithmic_bytes": dom["bytes_per_iter"], "peak_source": src}
+    if dom and "row_ms" in dom:
+        gbps = dom["bytes"] / (dom["row_ms"] / 1e3) / 1e9
+        roof = {"bound": "hbm", "achieved": r4(gbps), "peak": hbm, "unit": "GB/s", "frac": r4(gbps / hbm),
+                "traffic": r4(PR_ROWS_DRAM_BYTES_PER_ENTRY * dom["m"]),
+                "kernel": "k_coov_rows<PrOp<0>,%s> (PageRank pull, RMAT-%d directed)" % (dom["sched"], scale),
+                "algorithmic_bytes": dom["bytes"], "peak_source": src}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32", "data": "synthetic (device RMAT generator)",
         "config": dict(W, n=n, m_adjacency=2 * m_in, l2="inputs larger than L2 (CSR 2.1 GB)",
-                       parallelism="replicas" if world > 1 else "single"),
+                       parallelism="replicas" if world > 1 else "single",
+                       edges_counted="BFS: out-degrees of reached vertices; WCC: the input edges"),
+        "graph500_gteps": r4(g500),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3 / args.steps, "host_buffers": "page-locked (eg_host_alloc), reused by every call",
-                "api": "eg_bfs_batch (%d roots per call, copies overlapped with the next traversal) + eg_wcc" % E2E_BATCH},
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3 / args.steps,
+                "api": "eg_bfs_batch x%d roots/call into page-locked buffers + eg_wcc" % E2E_BATCH},
         "gpu_launches": launches,
-        "load": {"build_ms": build_ms, "bfs_tuning": g.bfs_tuning},
         "roofline": roof,
         "clocks": clk.summary(),
-        "kernels": kernels,
     }
     if not args.no_cpu and rank == 0:
-        out["cpu_baseline"] = cpu_baseline(g, eg, roots, n, m_in, args)
+        cb, parity = cpu_baseline(g, eg, roots, n, m_in, args, lv_h, par_h, lab_h)
+        out["cpu_baseline"] = cb
+        out["parity"] = parity
+    out["load_build_ms"] = r4(build_ms)
+    out["kernels"] = kernels
     g.free()
     ctx.close()
     if rank == 0:
-        print(json.dumps(out))
+        print(json.dumps(out, separators=(",", ":")))
+
+
+def r4(x):
+    """x to 4 significant digits (keeps the JSON line short)."""
+    return float("%.4g" % x) if x is not None else None
+
+
+class _Csc:
+    """The in-lists the FP64 PageRank oracle reads (n, in_ptr, in_col)."""
+
+    def __init__(self, n, ptr, col):
+        self.n, self.in_ptr, self.in_col = n, ptr, col
+
+
+def rel_errors(got, ref):
+    """(relative L1, max relative) error of got against the FP64 ref."""
+    got = got.astype(np.float64)
+    d = np.abs(got - ref)
+    nz = ref != 0
+    return r4(d.sum() / np.abs(ref).sum()), r4((d[nz] / np.abs(ref[nz])).max())
 
 
 def kernel_reports(ctx, eg, scale, args):
-    """PageRank pull on the directed RMAT graph of the same scale (10 iterations)."""
+    """PageRank pull on the directed RMAT graph of the same scale (seed 1):
+    10 iterations from 1/n after eg_graph_tune; relative L1 and max relative
+    error of the ranks against the CPU FP64 oracle run on the same in-lists."""
+    import oracle
     import torch
     rep = {}
     n = 1 << scale
@@ -273,67 +299,68 @@ def kernel_reports(ctx, eg, scale, args):
     _, st = g.pagerank(iterations=10, copy_out=False)
     _, stg = g.pagerank(iterations=10, copy_out=False, use_graph=True)
     _, stg = g.pagerank(iterations=10, copy_out=False, use_graph=True)
+    rank, _ = g.pagerank(iterations=10)
     it_ms = st.ms / 10
     bytes_it = 8 * m + 16 * n
-    rep["pagerank_pull_rmat%d" % scale] = {
-        "ms_per_iter": it_ms, "gbps": bytes_it / (it_ms / 1e3) / 1e9, "gteps": m / (it_ms / 1e3) / 1e9,
-        "row_kernel_ms": st.row_kernel_ms, "row_kernel_gbps": bytes_it / (st.row_kernel_ms / 1e3) / 1e9,
-        "ms_per_iter_graph_replay": stg.ms / 10, "bytes_per_iter": bytes_it,
-        "bytes_rule": "8 per CSC entry (column + gathered contribution) + 16 per vertex (row start, degree, rank and next-contribution writes)",
-        "build_ms": g.info().build_ms, "m": m,
-        "schedule": dict(cands[chosen], candidates=cands)}
+    c = cands[chosen]
+    rec = {"ms_iter": r4(it_ms), "ms_iter_graph": r4(stg.ms / 10), "row_ms": r4(st.row_kernel_ms),
+           "row_gbps": r4(bytes_it / (st.row_kernel_ms / 1e3) / 1e9), "gteps": r4(m / (it_ms / 1e3) / 1e9),
+           "bytes": bytes_it, "m": m,
+           "sched": "%d,%d pf%d mb%d ch%d" % (c["tile"], c["per_lane"], c["prefetch"], c["min_blocks"],
+                                             c["cache_hint"]),
+           "tuned_of": len(cands)}
+    try:
+        oracle.build()
+        ptr, col = g.adj(eg.CSC)
+        od, _ = g.degrees(True, False)
+        ref = oracle.pagerank_f64(_Csc(n, ptr, col), od, 1.0 / n, 10)
+        rec["l1_err"], rec["max_rel_err"] = rel_errors(rank, ref)
+        rec["err_vs"] = "CPU FP64 oracle"
+    except Exception as ex:
+        rec["err"] = str(ex)[:120]
     g.free()
+    rep["pr_rmat%d" % scale] = rec
     return rep
 
 
 def spmv_report(ctx, eg, log_n=25, degree=32):
     """SpMV over an Erdos-Renyi graph (2^25 vertices, 32 out-edges each, seed 4):
     fp32 values U[0,1) hashed from the endpoints, x U[0,1) (seed 11); fp32,
-    fp32 two-sum and fp64, with max-relative and L1 error against fp64 (x is
-    larger than 2^24 vertices, so the source-blocked CSC is used: two passes
-    over x slices L2 holds; its build is timed apart); the 64x64 grid layout
-    built on the device beside it."""
+    fp32 two-sum and fp64, with max-relative and L1 error against the CPU
+    FP64 oracle over the same in-lists (x is larger than 2^24 vertices, so the
+    source-blocked CSC is used: two passes over x slices L2 holds); PageRank
+    over the same graph; the 64x64 grid layout built on the device beside it."""
     import oracle
     n = 1 << log_n
     m = degree * n
     g = ctx.er(n, m, 4).build(eg.CSR | eg.CSC)
     g.tune()  # row-kernel schedule for this graph (untimed setup)
     x = oracle.uniform_f32(n, 11)
-    y64, _ = g.spmv(x, "f64", value_seed=9)
-    out = {"workload": "ER n=2^%d m=%d" % (log_n, m), "build_ms": g.info().build_ms}
-    nz = y64 != 0
+    oracle.build()
+    ptr, col = g.adj(eg.CSC)
+    y64 = oracle.spmv_f64_hashed(n, ptr, col, 9, x)
+    del ptr, col
+    out = {}
     for kind in ("f32", "f32_comp", "f64"):
         g.spmv(x, kind, value_seed=9, copy_out=False)
         y, ms = g.spmv(x, kind, value_seed=9)
         bytes_ = 12 * m + (16 if kind == "f64" else 12) * n
-        rec = {"ms": ms, "gbps": bytes_ / (ms / 1e3) / 1e9, "gflops": 2 * m / (ms / 1e3) / 1e9}
-        if kind != "f64":
-            d = np.abs(y.astype(np.float64) - y64)
-            rec["max_rel_err"] = float((d[nz] / np.abs(y64[nz])).max())
-            rec["l1_rel_err"] = float(d.sum() / np.abs(y64).sum())
+        rec = {"ms": r4(ms), "gbps": r4(bytes_ / (ms / 1e3) / 1e9)}
+        rec["l1_err"], rec["max_rel_err"] = rel_errors(y, y64)
         out[kind] = rec
-    # PageRank over the same graph, 10 iterations
     _, st = g.pagerank(iterations=10, copy_out=False)
-    out["pagerank_ms_per_iter"] = st.ms / 10
-    # the 64 x 64 grid layout and the grid kernels (cells in L2-sized blocks)
-    import time as _t
-    t0 = _t.perf_counter()
+    out["pr_ms_iter"] = r4(st.ms / 10)
+    # the 64 x 64 grid layout and the grid kernels
+    t0 = time.perf_counter()
     g.build_grid(64)
-    out["grid64_build_s"] = _t.perf_counter() - t0
-    grid = {}
-    for kind in ("f32", "f64"):
-        g.spmv(x, kind, value_seed=9, copy_out=False, grid=True)
-        y, ms = g.spmv(x, kind, value_seed=9, grid=True)
-        bytes_ = 12 * m + (16 if kind == "f64" else 12) * n
-        rec = {"ms": ms, "gbps": bytes_ / (ms / 1e3) / 1e9}
-        if kind == "f32":
-            d = np.abs(y.astype(np.float64) - y64)
-            rec["max_rel_err"] = float((d[nz] / np.abs(y64[nz])).max())
-            rec["l1_rel_err"] = float(d.sum() / np.abs(y64).sum())
-        grid[kind] = rec
+    out["grid64_build_s"] = r4(time.perf_counter() - t0)
+    g.spmv(x, "f32", value_seed=9, copy_out=False, grid=True)
+    y, ms = g.spmv(x, "f32", value_seed=9, grid=True)
+    gr = {"f32_ms": r4(ms), "f32_gbps": r4((12 * m + 12 * n) / (ms / 1e3) / 1e9)}
+    gr["l1_err"], gr["max_rel_err"] = rel_errors(y, y64)
     _, st = g.pagerank(iterations=10, copy_out=False, grid=True)
-    grid["pagerank_ms_per_iter"] = st.ms / 10
-    out["grid64"] = grid
+    gr["pr_ms_iter"] = r4(st.ms / 10)
+    out["grid64"] = gr
     g.free()
     return out
 
@@ -341,7 +368,7 @@ def spmv_report(ctx, eg, log_n=25, degree=32):
 def sssp_report(ctx, eg, scale=23, k=256, singles=16):
     """Batched SSSP on RMAT-23 (seed 5), u32 weights U[1,255] hashed from the
     endpoints: k sources in one batch versus single-source launches (a sample
-    of `singles`, scaled to k)."""
+    of `singles`, scaled to k); fp32 weights batched."""
     n = 1 << scale
     g = ctx.rmat(scale, 16 * n, 5).build(eg.CSR)
     roots = g.sample_roots(k, 6)
@@ -356,11 +383,8 @@ def sssp_report(ctx, eg, scale=23, k=256, singles=16):
     wf = eg.weights("f32", seed=6)
     _, stf = g.sssp_multi(roots, wf, copy_out=False)
     g.free()
-    return {"workload": "rmat%d, %d sources" % (scale, k), "batched_ms": stb.ms, "single_ms_each": per_single,
-            "runs_per_s_batched": k / (stb.ms / 1e3), "runs_per_s_single": 1e3 / per_single,
-            "speedup": per_single * k / stb.ms, "rounds_batched": stb.rounds,
-            "gteps_batched": stb.relaxations / (stb.ms / 1e3) / 1e9,
-            "f32_weights_batched_ms": stf.ms, "f32_rounds_batched": stf.rounds}
+    return {"batch_ms": r4(stb.ms), "single_ms": r4(per_single), "speedup": r4(per_single * k / stb.ms),
+            "rounds": stb.rounds, "f32_batch_ms": r4(stf.ms)}
 
 
 def msbfs_report(g, roots):
@@ -372,25 +396,12 @@ def msbfs_report(g, roots):
         _, st = g.bfs(int(r), copy_out=False)
         t1 += st.ms
     per_single = t1 / 16
-    return {"batched_ms": stm.ms, "single_ms_each": per_single, "gteps_batched": stm.edges_traversed / (stm.ms / 1e3) / 1e9,
-            "speedup": per_single * len(roots) / stm.ms}
+    return {"batch_ms": r4(stm.ms), "single_ms": r4(per_single), "speedup": r4(per_single * len(roots) / stm.ms)}
 
 
-def serve_report(ctx, eg, scale, rate, nq, seed=7, plain_sample=40, g=None, exclusive=False, gang=True):
-    """Serving workload: Poisson arrivals at `rate` qps of 60% BFS, 25% SSSP
-    (u32 weights U[1,255]), 15% personalised PageRank (1-8 seeds, tolerance
-    10^U(-7,-4), <= 50 iterations) on the resident undirected RMAT graph;
-    p50/p99 latency (arrival -> completion) and QPS, next to the QPS of the
-    plain one-query-at-a-time kernels on a sample of the same queries (BFS:
-    the direction-optimising BFS; SSSP: the single-source frontier
-    Bellman-Ford; PPR: the PageRank row kernel with a seed teleport)."""
-    import torch
-    n = 1 << scale
-    own = g is None
-    if own:
-        g = ctx.rmat(scale, 16 * n, 2, undirected=True).build(eg.CSR | eg.CSC)
-    od, _ = g.degrees(True, False)
-    nz = np.nonzero(od > 0)[0].astype(np.uint32)
+def serve_queries(nz, nq, rate, seed):
+    """The serving mix: arrival times (Poisson at `rate`) and queries, 60% BFS,
+    25% SSSP, 15% personalised PageRank (1-8 seeds, tolerance 10^U(-7,-4))."""
     rng = np.random.default_rng(seed)
     kinds = rng.choice(3, size=nq, p=[0.60, 0.25, 0.15])
     arrivals = np.cumsum(rng.exponential(1.0 / rate, size=nq))
@@ -403,79 +414,129 @@ def serve_report(ctx, eg, scale, rate, nq, seed=7, plain_sample=40, g=None, excl
         else:
             k = int(rng.integers(1, 9))
             qs.append(("ppr", 0, [int(x) for x in rng.choice(nz, size=k)], float(10 ** rng.uniform(-7, -4))))
-    w = eg.weights("hash", seed=6, lo=1, hi=255)
+    return arrivals, qs
+
+
+def serve_run(eg, g, w, arrivals, qs, exclusive=False, gang=True):
+    """Offers the queries at their arrival times to a fresh server; returns
+    (latencies in ms, span in s from the first arrival to the last completion)."""
+    import torch
+    nq = len(qs)
     srv = eg.Server(g, hbm_budget=64 << 30, weights_=w, exclusive=exclusive, gang=gang)
     torch.cuda.synchronize()
     t_start = srv.info()["clock_s"]
-    arrivals = arrivals + t_start
+    arr = arrivals - arrivals[0] + t_start
     done = []
     i = 0
     while len(done) < nq:
         now = srv.info()["clock_s"]
-        while i < nq and arrivals[i] <= now:
+        while i < nq and arr[i] <= now:
             kind, src, seeds, tol = qs[i]
             if kind == "ppr":
-                srv.submit("ppr", seeds=seeds, tol=tol, arrival=float(arrivals[i]))
+                srv.submit("ppr", seeds=seeds, tol=tol, arrival=float(arr[i]))
             else:
-                srv.submit(kind, source=src, arrival=float(arrivals[i]))
+                srv.submit(kind, source=src, arrival=float(arr[i]))
             i += 1
         active = srv.step()
         done.extend(srv.poll())
         if active == 0 and i < nq:  # idle: wait for the next arrival
-            time.sleep(max(0.0, min(0.001, arrivals[i] - srv.info()["clock_s"])))
-    info = srv.info()
-    info["stats"] = srv.stats()
+            time.sleep(max(0.0, min(0.001, arr[i] - srv.info()["clock_s"])))
     srv.close()
     lat = np.array([r.done_s - r.arrival_s for r in done]) * 1e3
-    span = max(r.done_s for r in done) - arrivals[0]
-    # plain kernels, one query at a time, on a sample of the same mix
-    samp = list(range(min(plain_sample, nq)))
+    return lat, max(r.done_s for r in done) - arr[0]
+
+
+def plain_qps(g, w, qs):
+    """The plain one-query-at-a-time kernels on the same queries: BFS (the
+    direction-optimising BFS), SSSP (single-source frontier Bellman-Ford),
+    PPR (the PageRank row kernel with a seed teleport)."""
     t0 = time.perf_counter()
-    for j in samp:
-        kind, src, seeds, tol = qs[j]
+    for kind, src, seeds, tol in qs:
         if kind == "bfs":
             g.bfs(src, copy_out=False)
         elif kind == "sssp":
             g.sssp(src, w, copy_out=False)
         else:
             g.ppr_single(seeds, tolerance=tol, copy_out=False)
-    plain_qps = len(samp) / (time.perf_counter() - t0)
-    if own:
-        g.free()
-    qps = nq / span
-    return {"workload": "serve rmat%d undirected, %d queries, Poisson %g qps offered" % (scale, nq, rate),
-            "engines": "exclusive" if exclusive else "concurrent", "sssp_gang": gang,
-            "qps": qps, "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-            "plain_qps": plain_qps, "speedup_vs_plain": qps / plain_qps, "slots": info}
+    return len(qs) / (time.perf_counter() - t0)
 
 
-def cpu_baseline(g, eg, roots, n, m_in, args):
+def serve_sweep(ctx, eg, scale, args, g):
+    """The serving workload on the resident undirected RMAT graph at several
+    offered Poisson rates (seed 7): per rate QPS achieved and p50/p99 latency
+    (arrival to completion); the plain one-query-at-a-time kernels' QPS on
+    a sample of the same queries."""
+    od, _ = g.degrees(True, False)
+    nz = np.nonzero(od > 0)[0].astype(np.uint32)
+    w = eg.weights("hash", seed=6, lo=1, hi=255)
+    rates = [float(r) for r in args.rates.split(",")] if args.rates else [args.rate]
+    out = {"rates": []}
+    for rate in rates:
+        nq = int(min(args.queries, max(200, rate * args.serve_seconds)))
+        arrivals, qs = serve_queries(nz, nq, rate, 7)
+        lat, span = serve_run(eg, g, w, arrivals, qs, exclusive=args.serve_exclusive, gang=not args.serve_no_gang)
+        out["rates"].append({"offered": rate, "n": nq, "qps": r4(nq / span), "p50_ms": r4(np.percentile(lat, 50)),
+                             "p99_ms": r4(np.percentile(lat, 99))})
+    _, qs = serve_queries(nz, args.plain_sample, 1000.0, 7)
+    out["plain_qps"] = r4(plain_qps(g, w, qs))
+    best = max(r["qps"] for r in out["rates"])
+    out["max_qps_vs_plain"] = r4(best / out["plain_qps"])
+    return out
+
+
+def cpu_baseline(g, eg, roots, n, m_in, args, lv_h=None, par_h=None, lab_h=None):
     """The multi-threaded CPU port of the reference loops (bfs_simple's
     direction-optimising iterator, wcc's label propagation) on a bounded
     sample of the same step: the first roots that fit in ~15 s plus one WCC,
-    on the same graph copied to the host."""
+    on the same graph copied to the host.  Outside the CPU timing, the GPU's
+    last end-to-end outputs (levels and parents of the last E2E_BATCH roots,
+    WCC labels, in the page-locked buffers) are compared with the port's:
+    levels and labels bit for bit, parents as a BFS tree."""
     import oracle
     oracle.build()
     ptr, col = g.adj(eg.CSR)
-    return cpu_sample(oracle, ptr, col, roots, m_in, budget_s=15.0)
+    first = len(roots) - E2E_BATCH
+    par = {"bfs_roots_checked": 0, "bfs_levels_bit_exact": True, "bfs_trees_valid": True}
+
+    def check(i, r, lv):
+        if lv_h is None or i < first:
+            return
+        j = i - first
+        par["bfs_roots_checked"] += 1
+        par["bfs_levels_bit_exact"] &= bool(np.array_equal(lv, lv_h[j * n:(j + 1) * n]))
+        if par["bfs_roots_checked"] <= 4:
+            par["bfs_trees_valid"] &= oracle.bfs_tree_check(n, ptr, col, int(r), lv_h[j * n:(j + 1) * n],
+                                                            par_h[j * n:(j + 1) * n]) == 0
+
+    cb, comp = cpu_sample(oracle, ptr, col, roots, m_in, budget_s=15.0, check=check)
+    if lab_h is not None:
+        par["wcc_bit_exact"] = bool(np.array_equal(comp, lab_h))
+    par["vs"] = "CPU port (bfs_do, wcc_lp) on the GPU's CSR"
+    return cb, par
 
 
-def cpu_sample(oracle, ptr, col, roots, m_in, budget_s):
+def cpu_sample(oracle, ptr, col, roots, m_in, budget_s, check=None):
+    """WCC plus BFS from the roots in turn until budget_s of CPU time; only the
+    oracle calls are timed.  Returns (the cpu_baseline record, WCC labels)."""
     od = np.diff(ptr.astype(np.int64))
     t0 = time.perf_counter()
     comp, rounds = oracle.wcc_lp(ptr, col)
+    dt = time.perf_counter() - t0
     edges = m_in
     k = 0
-    for r in roots:
+    for i, r in enumerate(roots):
+        t0 = time.perf_counter()
         lv = oracle.bfs_do(ptr, col, ptr, col, int(r))
+        dt += time.perf_counter() - t0
         edges += int(od[lv > 0].sum())
         k += 1
-        if time.perf_counter() - t0 > budget_s:
+        if check:
+            check(i, r, lv)
+        if dt > budget_s:
             break
-    dt = time.perf_counter() - t0
-    return {"value": edges / dt / 1e9, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
-            "sample": "WCC + %d of %d BFS roots on the same graph (OpenMP port of bfs_simple/wcc loops), %.1f s"
-                      % (k, len(roots), dt)}
+    return ({"value": edges / dt / 1e9, "unit": UNIT, "cores": oracle.num_threads(), "kind": "port",
+             "sample": "WCC + %d of %d BFS roots on the same graph (OpenMP port of bfs_simple/wcc loops), %.1f s"
+                       % (k, len(roots), dt)}, comp)
 
 
 def run_reference(args):
@@ -502,7 +563,7 @@ def run_reference(args):
     vals, samples = [], []
     t0 = time.perf_counter()
     for _ in range(args.steps):
-        r = cpu_sample(oracle, adj.out_ptr, adj.out_col, roots, m_in, budget_s=20.0)
+        r, _ = cpu_sample(oracle, adj.out_ptr, adj.out_col, roots, m_in, budget_s=20.0)
         vals.append(r["value"])
         samples.append(r["sample"])
     dt = time.perf_counter() - t0
@@ -537,9 +598,8 @@ def ppr_report(ctx, eg, scale=24, nq=32, seed=7):
         its += st.sweeps
     g.free()
     per_single = t1 / 8
-    return {"workload": "ppr rmat%d undirected, %d queries" % (scale, nq), "batched_ms": stb.ms,
-            "sweeps": stb.sweeps, "ms_per_sweep": stb.ms / max(stb.sweeps, 1), "single_ms_each": per_single,
-            "single_iters_each": its / 8, "speedup": per_single * nq / stb.ms}
+    return {"batch_ms": r4(stb.ms), "sweeps": stb.sweeps, "single_ms": r4(per_single),
+            "single_iters": r4(its / 8), "speedup": r4(per_single * nq / stb.ms)}
 
 
 def bfs_report(ctx, eg, scale=24, roots=16):
@@ -576,7 +636,11 @@ def only_report(name, args):
     ctx = eg.Context(0)
     scale = args.scale or 24
     if name == "serve":
-        out = serve_report(ctx, eg, scale, args.rate, args.queries, exclusive=args.serve_exclusive, gang=not args.serve_no_gang)
+        n = 1 << scale
+        g = ctx.rmat(scale, 16 * n, 2, undirected=True).build(eg.CSR | eg.CSC)
+        g.tune()
+        out = serve_sweep(ctx, eg, scale, args, g)
+        g.free()
     elif name == "pr":
         out = kernel_reports(ctx, eg, scale, args)
     elif name == "spmv":
@@ -611,8 +675,14 @@ def main():
     ap.add_argument("--serve-only", action="store_true", help="only the serving report")
     ap.add_argument("--only", choices=["pr", "spmv", "sssp", "msbfs", "ppr", "bfs", "serve"],
                     help="only one kernel report (profiling)")
-    ap.add_argument("--rate", type=float, default=20000.0)
-    ap.add_argument("--queries", type=int, default=1000)
+    ap.add_argument("--rate", type=float, default=20000.0, help="offered rate when --rates is empty")
+    ap.add_argument("--rates", default="250,1000,5000,50000",
+                    help="comma-separated offered Poisson rates (qps) of the serving sweep")
+    ap.add_argument("--serve-seconds", type=float, default=2.0,
+                    help="offered arrival span per rate (queries = rate x seconds, 200..--queries)")
+    ap.add_argument("--queries", type=int, default=1500, help="most queries per offered rate")
+    ap.add_argument("--plain-sample", type=int, default=40,
+                    help="queries of the same mix run one at a time on the plain kernels")
     ap.add_argument("--serve-no-gang", action="store_true",
                     help="query server admits SSSP queries into any free slot instead of 32-source gangs")
     ap.add_argument("--serve-exclusive", action="store_true",

@@ -2,9 +2,9 @@
 // (degree histogram, scan, stable radix sort, CSR/CSC and 2-D grid).
 //
 // The builders replace the reference loader (init_all.c): preload_graph
-// (init_all.c:150-179), init_adj_sort (init_all.c:629-790) with its Ligra
+// (init_all.c:81-110), init_adj_sort (init_all.c:629-790) with its Ligra
 // radix sort (radixSort_ligra.h:290-358) and offset back-fill
-// (utils_ligra.h:212-214), and init_grid_sort (init_all.c:321-430).
+// (utils_ligra.h:212-214), and init_grid_sort (init_all.c:252-361).
 #include <stdarg.h>
 #include <stdlib.h>
 #include <string.h>
@@ -56,17 +56,21 @@ extern "C" int eg_open(int device, uint64_t hbm_budget_bytes, eg_ctx **out) {
 
 namespace {
 // One warp copies `words` to pinned host memory (and clears them); with a
-// flag, every lane's stores are made visible system-wide before lane 0
-// writes `seq` to the flag word.
+// flag, lane 0 releases `seq` to the flag word after every lane's stores:
+// the warp barrier orders the other lanes' stores before lane 0's
+// system-scope fence (cumulativity), and the fence orders them before the
+// flag store that the host reads with acquire semantics.
 __global__ void k_readback(uint32_t *src, uint32_t *dst, uint32_t words, int clear, uint32_t *flag, uint32_t seq) {
     for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) {
         dst[i] = src[i];
         if (clear) src[i] = 0u;
     }
     if (flag) {
-        __threadfence_system();
         __syncwarp();
-        if (threadIdx.x == 0) *(volatile uint32_t *)flag = seq;
+        if (threadIdx.x == 0) {
+            __threadfence_system();
+            *(volatile uint32_t *)flag = seq;
+        }
     }
 }
 __global__ void k_zero(uint32_t *p, uint64_t words) {
@@ -688,7 +692,7 @@ int eg_radix_sort(eg_ctx *ctx, uint32_t *k_in, uint32_t *v_in, uint32_t *k_tmp, 
 // ============================================================== builders
 // Unpacks the input pairs into (key, value) arrays: the file's edges in file
 // order, then (undirected) the reversed copies, as preload_graph lays out
-// memblock (init_all.c:150-179).  by_src selects key=src,value=dst.
+// memblock (init_all.c:81-110).  by_src selects key=src,value=dst.
 __global__ void k_unpack(const uint32_t *pairs, uint64_t m_in, int undirected, uint32_t n, uint32_t *keys,
                          uint32_t *vals, uint32_t *bad) {
     uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
@@ -826,7 +830,7 @@ extern "C" int eg_graph_build(eg_graph *g, unsigned layouts) {
 }
 
 // ---------------------------------------------------------------- grid
-// Partition id of the reference (init_all.c:123-129, sizes from 838-842).
+// Partition id of the reference (init_all.c:54-60, sizes from 838-842).
 __device__ __forceinline__ uint32_t part_of(uint32_t v, uint32_t psz, uint32_t mod, uint32_t split) {
     if (mod == 0) return v / psz;
     return v < split ? v / psz : (v - split) / (psz - 1) + mod;

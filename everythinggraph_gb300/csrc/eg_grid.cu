@@ -1,7 +1,7 @@
 // SpMV and PageRank over the 2-D grid layout (eg_graph_build_grid): the
 // reference's prgrid_algo / iterator (prgrid_cilk.c:62-141) and the grid
 // modes of spmv.c, which walk the P x P cells of init_grid_sort
-// (init_all.c:321-430).
+// (init_all.c:252-361).
 //
 // A cell (i, j) holds the edges from source partition i to destination
 // partition j.  The cells are visited in B x B blocks (block-row-major), so

@@ -66,7 +66,7 @@ int eg_host_free(void *p);
 
 /* ---- graph input (replaces init(): init_all.c:791-893) ----------------- */
 #define EG_UNDIRECTED 1u /* -u: append reversed copies of every edge
-                            (init_all.c:171-175), doubling m (init_all.c:636) */
+                            (init_all.c:102-106), doubling m (init_all.c:636) */
 #define EG_WEIGHTED_FILE 2u /* -w: the file holds 12-byte [src][dst][f32 weight]
                                records (struct input, init_all.h:8-14;
                                item_size, init_all.c:43-49).  The weights are
@@ -92,13 +92,13 @@ int eg_graph_generate_er(eg_ctx *ctx, uint32_t n, uint64_t m, uint64_t seed, uns
 void eg_graph_free(eg_graph *g);
 
 /* ---- layouts (replaces init_adj_sort, init_all.c:629-790, and
- * init_grid_sort, init_all.c:321-430) ------------------------------------ */
+ * init_grid_sort, init_all.c:252-361) ------------------------------------ */
 #define EG_LAYOUT_CSR 1u /* out-lists, stable by src: each list in file order */
 #define EG_LAYOUT_CSC 2u /* in-lists: ascending src, ties in file order */
 #define EG_LAYOUT_GRID 4u
 
 int eg_graph_build(eg_graph *g, unsigned layouts);
-/* 2-D grid of P x P cells (reference partitioning, init_all.c:123-129):
+/* 2-D grid of P x P cells (reference partitioning, init_all.c:54-60):
  * cells row-major by (src partition, dst partition), ascending src inside. */
 int eg_graph_build_grid(eg_graph *g, uint32_t P);
 
@@ -451,8 +451,10 @@ int eg_serve_close(eg_server *s);
  * cudaGetSymbolAddress; make that first call before any stream capture.
  * Every call on a device shares the array (it keeps the last call's
  * contents; each call writes all it reads), so calls that overlap on the GPU
- * race: serialise them on one stream.  Results equal eg_spmv's EG_SPMV_F32
- * row sums (same kernel, same schedule). */
+ * race: serialise them on one stream.  Rows are summed over merge-path
+ * tiles of 2048 items (row ends + entries), a different fp32 summation order
+ * from eg_spmv's EG_SPMV_F32, so the two agree within fp32 rounding (relative
+ * L1 <= 1e-6 in the tests), not bit for bit. */
 #define EG_NOALLOC_MAX_ITEMS (65536ull * 2048ull)
 int eg_spmv_f32_noalloc(const uint32_t *d_ptr, const uint32_t *d_col, const float *d_vals, const float *d_x,
                         float *d_y, uint32_t n, uint64_t m, void *stream);

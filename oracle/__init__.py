@@ -34,6 +34,7 @@ def lib():
         _lib.or_partition_id.restype = ctypes.c_uint32
         _lib.or_default_p.restype = ctypes.c_uint32
         _lib.or_ppr_f64.restype = ctypes.c_int
+        _lib.or_bfs_tree_check.restype = ctypes.c_int
     return _lib
 
 
@@ -111,6 +112,21 @@ class Adj:
 
     def in_dst(self):
         return np.repeat(np.arange(self.n, dtype=np.uint32), self.in_deg())
+
+
+def build_csr(n, pairs, undirected=False):
+    """The CSR (out-lists) of build_adj alone: (ptr, col), without the CSC and
+    the entry ids (for graphs of 10^8-10^9 entries)."""
+    pairs = np.ascontiguousarray(pairs, dtype=np.uint32)
+    m = len(pairs) // 2
+    M = 2 * m if undirected else m
+    ptr = np.empty(n + 1, dtype=np.uint32)
+    col = np.empty(M, dtype=np.uint32)
+    rc = lib().or_build_adj(u32(n), u64(m), _p(pairs), ctypes.c_int(int(undirected)), _p(ptr), _p(col),
+                            None, None, None, None)
+    if rc != 0:
+        raise ValueError("edge endpoint out of range" if rc == -1 else "allocation failed")
+    return ptr, col
 
 
 def build_adj(n, pairs, undirected=False):
@@ -195,6 +211,15 @@ def ppr_f64(adj, deg, seeds, damping=0.85, tol=1e-10, max_iters=50):
 SPMV_PULL, SPMV_PUSH, SPMV_EDGE = 0, 1, 2
 
 
+def spmv_f64_hashed(n, ptr, col, value_seed, x):
+    """fp64 SpMV with the edge values of hash_values(col, row, value_seed),
+    computed per entry (no value array)."""
+    x = np.ascontiguousarray(x, dtype=np.float32)
+    y = np.empty(n, dtype=np.float64)
+    lib().or_spmv_f64_hval(u32(n), _p(ptr), _p(col), u64(value_seed), _p(x), _p(y))
+    return y
+
+
 def spmv_u32(n, ptr, col, x, mode):
     x = np.ascontiguousarray(x, dtype=np.uint32)
     y = np.empty(n, dtype=np.uint32)
@@ -257,27 +282,24 @@ def ref_weights(adj, which="out"):
     return (s % 10 + d % 10).astype(np.uint32)
 
 
+def bfs_tree_check(n, out_ptr, out_col, root, level, parent):
+    """0 when `parent` is a BFS tree for `level` (root = 1 convention) over the
+    CSR out-lists: the root is its own parent, unreached vertices have parent
+    -1, every other reached vertex has a parent one level up with an edge
+    parent -> v.  Else the negative code of the first rule that failed
+    (-1 root, -2 unreached, -3 level, -4 edge)."""
+    out_ptr = np.ascontiguousarray(out_ptr, dtype=np.uint32)
+    out_col = np.ascontiguousarray(out_col, dtype=np.uint32)
+    level = np.ascontiguousarray(level, dtype=np.int32)
+    parent = np.ascontiguousarray(parent, dtype=np.int32)
+    if len(level) != n or len(parent) != n:
+        raise ValueError("level and parent need n entries")
+    return lib().or_bfs_tree_check(u32(n), _p(out_ptr), _p(out_col), u32(root), _p(level), _p(parent))
+
+
 def bfs_tree_ok(n, out_ptr, out_col, root, level, parent):
-    """Checks a BFS parent array against levels (root=1 convention): the root is
-    its own parent, every other reached vertex has a parent one level up with an
-    edge parent->v, unreached vertices have parent -1."""
-    level = np.asarray(level)
-    parent = np.asarray(parent)
-    if parent[root] != root or level[root] != 1:
-        return False
-    reached = level > 0
-    if np.any(parent[~reached] != -1):
-        return False
-    vs = np.nonzero(reached)[0]
-    vs = vs[vs != root]
-    ps = parent[vs]
-    if np.any(ps < 0) or np.any(level[ps] != level[vs] - 1):
-        return False
-    # edge existence: p -> v must be in p's out-list
-    src = np.repeat(np.arange(n, dtype=np.int64), np.diff(out_ptr.astype(np.int64)))
-    keys = np.unique(src * n + out_col.astype(np.int64))
-    q = ps.astype(np.int64) * n + vs.astype(np.int64)
-    return bool(np.all(np.isin(q, keys)))
+    """True when `parent` is a BFS tree for `level` (see bfs_tree_check)."""
+    return bfs_tree_check(n, out_ptr, out_col, root, level, parent) == 0
 
 
 def hash_weights(u, v, seed, lo, hi):

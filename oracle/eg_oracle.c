@@ -122,9 +122,9 @@ int or_sample_roots(uint32_t n, const uint32_t *deg, int k, uint64_t seed, uint3
 /* Layout builders.
  *
  * or_build_adj restates init_adj_sort (init_all.c:629-790) with the loader in
- * front of it (preload_graph, init_all.c:150-179):
+ * front of it (preload_graph, init_all.c:81-110):
  *  - memblock holds the file's edges in file order; with `undirected` the
- *    reversed copies follow at positions m..2m-1 (init_all.c:171-175) and the
+ *    reversed copies follow at positions m..2m-1 (init_all.c:102-106) and the
  *    edge count doubles (init_all.c:636);
  *  - the out-lists (CSR) are a stable sort of memblock by src (init_all.c:640),
  *    so a list keeps memblock order;
@@ -174,7 +174,7 @@ int or_build_adj(uint32_t n, uint64_t m, const uint32_t *pairs, int undirected,
     return 0;
 }
 
-/* Grid partitioning, restating get_partition_id (init_all.c:123-129) with the
+/* Grid partitioning, restating get_partition_id (init_all.c:54-60) with the
  * partition sizes set in init (init_all.c:838-842): the first n mod P
  * partitions hold ceil(n/P) vertices, the rest floor(n/P). */
 static inline uint32_t or_part(uint32_t v, uint32_t n, uint32_t P) {
@@ -194,7 +194,7 @@ uint32_t or_default_p(uint32_t n) {
     return P;
 }
 
-/* or_build_grid restates init_grid_sort (init_all.c:321-430, load mode 0):
+/* or_build_grid restates init_grid_sort (init_all.c:252-361, load mode 0):
  * stable sort by src, then a stable sort of each src-partition row by dst
  * partition.  Cells are laid out row-major (src partition i, dst partition j);
  * inside a cell edges are in ascending src, ties in file order.
@@ -543,7 +543,7 @@ int or_wcc(uint32_t n, uint64_t m, const uint32_t *pairs, int64_t *labels) {
 }
 
 /* Degree histogram of the file's edges (preload_graph's count,
- * init_all.c:160-163). */
+ * init_all.c:91-94). */
 void or_degrees(uint32_t n, uint64_t m, const uint32_t *pairs, uint32_t *out_deg, uint32_t *in_deg) {
     memset(out_deg, 0, (size_t)n * sizeof(uint32_t));
     if (in_deg) memset(in_deg, 0, (size_t)n * sizeof(uint32_t));
@@ -591,6 +591,61 @@ void or_hash_values(uint64_t count, const uint32_t *u, const uint32_t *v, uint64
 #pragma omp parallel for schedule(static)
     for (int64_t i = 0; i < (int64_t)count; i++)
         out[i] = (float)(or_edge_hash(seed, u[i], v[i]) >> 40) * (1.0f / 16777216.0f);
+}
+
+/* fp64 SpMV whose edge values follow the rule of or_hash_values, computed per
+ * entry instead of stored: y[v] = sum over in-entries p of row v of
+ * val(col[p], v) * x[col[p]] (the FP64 error reference for graphs whose value
+ * array would not fit beside the CSC in host memory). */
+void or_spmv_f64_hval(uint32_t n, const uint32_t *ptr, const uint32_t *col, uint64_t seed, const float *x,
+                      double *y) {
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t v = 0; v < (int64_t)n; v++) {
+        double acc = 0.0;
+        for (uint32_t p = ptr[v]; p < ptr[v + 1]; p++) {
+            const float val = (float)(or_edge_hash(seed, col[p], (uint32_t)v) >> 40) * (1.0f / 16777216.0f);
+            acc += (double)val * (double)x[col[p]];
+        }
+        y[v] = acc;
+    }
+}
+
+/* BFS tree check for a parent array (the parents that bfs_numa's top-down
+ * step records with a CAS, bfs_numa.c:234-278), against levels in the root = 1
+ * convention, in O(n + m):
+ *   parent[root] = root and level[root] = 1;
+ *   an unreached vertex (level 0) has parent -1;
+ *   every other reached v has a parent p with level[p] = level[v] - 1 and an
+ *   out-entry p -> v in the CSR.
+ * The edge test marks, for every CSR entry u -> w with parent[w] = u, that w's
+ * tree edge exists.  Returns 0 when the tree is valid, else a negative code
+ * naming the first rule that failed (-1 root, -2 unreached, -3 level, -4 edge). */
+int or_bfs_tree_check(uint32_t n, const uint32_t *ptr, const uint32_t *col, uint32_t root, const int32_t *level,
+                      const int32_t *parent) {
+    if (root >= n || parent[root] != (int32_t)root || level[root] != 1) return -1;
+    int bad2 = 0, bad3 = 0, bad4 = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad2, bad3)
+    for (int64_t v = 0; v < (int64_t)n; v++) {
+        if (level[v] == 0) {
+            if (parent[v] != -1) bad2 = 1;
+        } else if (v != (int64_t)root) {
+            const int32_t p = parent[v];
+            if (p < 0 || (uint32_t)p >= n || level[p] != level[v] - 1) bad3 = 1;
+        }
+    }
+    if (bad2) return -2;
+    if (bad3) return -3;
+    uint8_t *found = (uint8_t *)calloc(n, 1);
+    if (!found) return -5;
+#pragma omp parallel for schedule(dynamic, 1024)
+    for (int64_t u = 0; u < (int64_t)n; u++)
+        for (uint32_t p = ptr[u]; p < ptr[u + 1]; p++)
+            if (parent[col[p]] == (int32_t)u) found[col[p]] = 1;
+#pragma omp parallel for schedule(static) reduction(| : bad4)
+    for (int64_t v = 0; v < (int64_t)n; v++)
+        if (level[v] > 0 && v != (int64_t)root && !found[v]) bad4 = 1;
+    free(found);
+    return bad4 ? -4 : 0;
 }
 
 /* ------------------------------------------------------------------------ */

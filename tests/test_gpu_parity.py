@@ -553,10 +553,14 @@ def test_big_bfs_properties(big):
 def test_big_wcc_and_sssp_properties(big):
     import everythinggraph_gb300 as eg
     ptr, col = big.adj(eg.CSR)
-    src = np.repeat(np.arange(len(ptr) - 1, dtype=np.int64), np.diff(ptr.astype(np.int64)))
+    n = len(ptr) - 1
+    src = np.repeat(np.arange(n, dtype=np.int64), np.diff(ptr.astype(np.int64)))
     lab, st = big.wcc()
     assert np.all(lab[src] == lab[col])
     assert np.all(lab <= np.arange(len(lab))) and np.all(lab[lab] == lab)
+    # the labels are the oracle's min-id labels (a merge of two components
+    # under the smaller id would pass the closure checks above)
+    np.testing.assert_array_equal(lab, oracle.wcc(n, oracle.rmat_edges(20, 16 << 20, 2)))
     w = eg.weights("hash", seed=6, lo=1, hi=255)
     wa = oracle.hash_weights(src.astype(np.uint32), col, 6, 1, 255).astype(np.int64)
     r = int(big.sample_roots(1, 5)[0])
@@ -566,6 +570,13 @@ def test_big_wcc_and_sssp_properties(big):
     ok = (d[src] != INF) & (src != col)
     assert np.all(d[col][ok] <= d[src][ok] + wa[ok])  # no edge can still be relaxed
     assert d[r] == 0
+    # every reached vertex's distance is attained by an in-edge (too-small
+    # distances would pass the relaxation check above)
+    attained = np.zeros(n, dtype=bool)
+    attained[col[ok & (d[src] + wa == d[col])]] = True
+    reached = np.nonzero(d != INF)[0]
+    assert np.all(attained[reached[reached != r]])
+    np.testing.assert_array_equal(d.astype(np.uint32), oracle.sssp(n, ptr, col, wa.astype(np.uint32), r))
 
 
 # ------------------------------------------------------------------ personalised PageRank

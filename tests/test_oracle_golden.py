@@ -83,6 +83,48 @@ def test_bfs_parents_form_tree(case):
         assert oracle.bfs_tree_ok(n, adj.out_ptr, adj.out_col, int(r), lv, par)
 
 
+def test_bfs_tree_check_rejects_planted_mistakes(case):
+    # mistakes planted in the oracle's own tree (CPU): each rule must fire
+    name, n, pairs, rec = case
+    adj = oracle.build_adj(n, pairs)
+    r = int(rec["roots"][0])
+    lv, par = oracle.bfs_levels(n, adj.out_ptr, adj.out_col, r, parents=True)
+    assert oracle.bfs_tree_check(n, adj.out_ptr, adj.out_col, r, lv, par) == 0
+    deep = np.nonzero(lv > 2)[0]
+    if len(deep) == 0:
+        pytest.skip("tree too shallow")
+    v = int(deep[0])
+    bad = par.copy()
+    bad[r] = -1
+    assert oracle.bfs_tree_check(n, adj.out_ptr, adj.out_col, r, lv, bad) == -1
+    unreached = np.nonzero(lv == 0)[0]
+    if len(unreached):
+        bad = par.copy()
+        bad[unreached[0]] = r
+        assert oracle.bfs_tree_check(n, adj.out_ptr, adj.out_col, r, lv, bad) == -2
+    bad = par.copy()
+    bad[v] = r  # root is two or more levels up
+    assert oracle.bfs_tree_check(n, adj.out_ptr, adj.out_col, r, lv, bad) == -3
+    # a parent one level up that has no edge to v
+    same = np.nonzero(lv == lv[v] - 1)[0]
+    src = adj.out_src()
+    into_v = set(src[adj.out_col == v].tolist())
+    cand = [int(p) for p in same if int(p) not in into_v]
+    if cand:
+        bad = par.copy()
+        bad[v] = cand[0]
+        assert oracle.bfs_tree_check(n, adj.out_ptr, adj.out_col, r, lv, bad) == -4
+
+
+def test_spmv_f64_hashed_equals_stored_values(case):
+    name, n, pairs, rec = case
+    adj = oracle.build_adj(n, pairs)
+    x = oracle.uniform_f32(n, 11)
+    vals = oracle.hash_values(adj.in_col, adj.in_dst(), 9)
+    np.testing.assert_array_equal(oracle.spmv_f64_hashed(n, adj.in_ptr, adj.in_col, 9, x),
+                                  oracle.spmv_f64(n, adj.in_ptr, adj.in_col, vals, x))
+
+
 def test_sssp(case):
     name, n, pairs, rec = case
     adj = oracle.build_adj(n, pairs)
