@@ -17,7 +17,8 @@ import numpy as np
 from . import _lib as L
 from ._lib import EGError  # noqa: F401
 
-CSR, CSC, GRID = L.EG_LAYOUT_CSR, L.EG_LAYOUT_CSC, L.EG_LAYOUT_GRID
+CSR, CSC, GRID, EDGES = L.EG_LAYOUT_CSR, L.EG_LAYOUT_CSC, L.EG_LAYOUT_GRID, L.EG_LAYOUT_EDGES
+EDGE_ORDERS = {"file": L.EG_EDGES_FILE_ORDER, "src": L.EG_EDGES_BY_SRC, "src_dst": L.EG_EDGES_BY_SRC_DST}
 UNDIRECTED = L.EG_UNDIRECTED
 UNREACHED_SSSP = 0xFFFFFFFE
 
@@ -177,6 +178,47 @@ class Graph:
     def build_grid(self, P):
         L.check(lib().eg_graph_build_grid(self._h, P))
         return self
+
+    def build_edges(self, order="src"):
+        """The edge array of load modes 9 ("file": input order), 7 ("src":
+        stable by source) or 8 ("src_dst": by source, then destination),
+        without any CSR or CSC."""
+        L.check(lib().eg_graph_build_edges(self._h, EDGE_ORDERS[order]))
+        return self
+
+    def edges(self):
+        """(src, dst) of the edge array, m entries each."""
+        m = self.m
+        s = np.empty(m, dtype=np.uint32)
+        d = np.empty(m, dtype=np.uint32)
+        L.check(lib().eg_graph_copy_edges(self._h, _ptr(s), _ptr(d)))
+        return s, d
+
+    def edges_bfs(self, root, parents=False, copy_out=True):
+        n = self.n
+        lv = np.empty(n, dtype=np.int32) if copy_out else None
+        par = np.empty(n, dtype=np.int32) if (copy_out and parents) else None
+        st = L.BfsStats()
+        L.check(lib().eg_edges_bfs(self._h, root, _ptr(lv), _ptr(par), ctypes.byref(st)))
+        return (lv, par, st) if parents else (lv, st)
+
+    def edges_pagerank(self, iterations=10, damping=0.85, prev_init=-1.0, swap=True, deg_multiplier=1,
+                       dangling=False, tolerance=0.0, copy_out=True):
+        o = L.PrOpts()
+        lib().eg_pr_opts_default(ctypes.byref(o))
+        o.iterations, o.damping, o.prev_init, o.swap = iterations, damping, prev_init, int(swap)
+        o.deg_multiplier, o.dangling, o.tolerance = deg_multiplier, int(dangling), tolerance
+        st = L.PrStats()
+        out = np.empty(self.n, dtype=np.float32) if copy_out else None
+        L.check(lib().eg_edges_pagerank(self._h, ctypes.byref(o), _ptr(out), ctypes.byref(st)))
+        return out, st
+
+    def edges_spmv(self, x, copy_out=True):
+        x = np.ascontiguousarray(x, dtype=np.uint32)
+        y = np.empty(self.n, dtype=np.uint32) if copy_out else None
+        ms = ctypes.c_float()
+        L.check(lib().eg_edges_spmv_u32(self._h, _ptr(x), _ptr(y), ctypes.byref(ms)))
+        return y, ms.value
 
     def info(self):
         i = L.GraphInfo()

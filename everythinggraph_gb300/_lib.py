@@ -15,8 +15,10 @@ c_u32, c_u64, c_i32, c_f32, c_f64, c_int, c_void_p, c_char_p = (
 
 EG_OK, EG_EINVAL, EG_ECUDA, EG_ENOMEM, EG_EIO, EG_ETIMEOUT, EG_ENOTBUILT, EG_ERANGE = 0, -1, -2, -3, -4, -5, -6, -7
 EG_UNDIRECTED = 1
-EG_LAYOUT_CSR, EG_LAYOUT_CSC, EG_LAYOUT_GRID = 1, 2, 4
+EG_LAYOUT_CSR, EG_LAYOUT_CSC, EG_LAYOUT_GRID, EG_LAYOUT_EDGES = 1, 2, 4, 8
+EG_EDGES_FILE_ORDER, EG_EDGES_BY_SRC, EG_EDGES_BY_SRC_DST = 0, 1, 2
 EG_DEV_CSR_PTR, EG_DEV_CSR_COL, EG_DEV_CSC_PTR, EG_DEV_CSC_COL, EG_DEV_OUT_DEG = 1, 2, 3, 4, 5
+EG_DEV_EDGE_SRC, EG_DEV_EDGE_DST = 6, 7
 EG_DEV_RANK, EG_DEV_LEVEL, EG_DEV_PARENT, EG_DEV_DIST, EG_DEV_LABEL, EG_DEV_SPMV_Y = 10, 11, 12, 13, 14, 15
 EG_SPMV_U32_PULL, EG_SPMV_U32_PUSH, EG_SPMV_U32_EDGE, EG_SPMV_F32, EG_SPMV_F32_COMP, EG_SPMV_F64 = 0, 1, 2, 3, 4, 5
 EG_BFS_AUTO, EG_BFS_PUSH_ONLY, EG_BFS_PULL_ONLY = 0, 1, 2
@@ -153,6 +155,11 @@ SIGNATURES = {
     "eg_serve_info": (c_int, [c_void_p, P(c_int), P(c_int), P(c_int), P(c_f64)]),
     "eg_serve_close": (c_int, [c_void_p]),
     "eg_spmv_f32_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_u32, c_u64, c_void_p]),
+    "eg_graph_build_edges": (c_int, [c_void_p, c_int]),
+    "eg_graph_copy_edges": (c_int, [c_void_p, c_void_p, c_void_p]),
+    "eg_edges_bfs": (c_int, [c_void_p, c_u32, c_void_p, c_void_p, c_void_p]),
+    "eg_edges_pagerank": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
+    "eg_edges_spmv_u32": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),
 }
 
 _lib = None

@@ -402,7 +402,8 @@ extern "C" void eg_graph_free(eg_graph *g) {
                       &g->sbp.col,       &g->sbp.perm,    &g->sbp.vals,    &g->sbp.yerr,    &g->pr_acc,
                       &g->label,        &g->spmv_x,      &g->spmv_y,      &g->spmv_vals,      &g->bfs_work,     &g->msbfs_work,
                       &g->sssp_work,    &g->ppr_work,    &g->wts,
-                      &g->grid_order,   &g->grid_units,  &g->grid_off,    &g->grid_vals,   &g->grid_acc};
+                      &g->grid_order,   &g->grid_units,  &g->grid_off,    &g->grid_vals,   &g->grid_acc,
+                      &g->esrc,         &g->edst,        &g->edge_work};
     for (eg_buf *b : bufs) eg_buf_free(c, *b);
     for (eg_bfs_graph &bg : g->bfsg) {
         if (bg.exec) cudaGraphExecDestroy(bg.exec);
@@ -1126,11 +1127,11 @@ extern "C" int eg_graph_copy_degrees(eg_graph *g, uint32_t *out_deg, uint32_t *i
     if (!g) return eg_fail(EG_EINVAL, "NULL graph");
     eg_ctx *ctx = g->ctx;
     if (out_deg) {
-        if (!(g->built & EG_LAYOUT_CSR)) return eg_fail(EG_ENOTBUILT, "CSR not built");
+        if (!(g->built & (EG_LAYOUT_CSR | EG_LAYOUT_EDGES))) return eg_fail(EG_ENOTBUILT, "CSR not built");
         EG_CUDA(cudaMemcpyAsync(out_deg, g->out_deg.p, (uint64_t)g->n * 4, cudaMemcpyDeviceToHost, ctx->stream));
     }
     if (in_deg) {
-        if (!(g->built & EG_LAYOUT_CSC)) return eg_fail(EG_ENOTBUILT, "CSC not built");
+        if (!(g->built & (EG_LAYOUT_CSC | EG_LAYOUT_EDGES))) return eg_fail(EG_ENOTBUILT, "CSC not built");
         EG_CUDA(cudaMemcpyAsync(in_deg, g->in_deg.p, (uint64_t)g->n * 4, cudaMemcpyDeviceToHost, ctx->stream));
     }
     EG_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -1145,6 +1146,8 @@ extern "C" void *eg_graph_device_ptr(eg_graph *g, int which) {
         case EG_DEV_CSC_PTR: return g->csc.ptr.p;
         case EG_DEV_CSC_COL: return g->csc.col.p;
         case EG_DEV_OUT_DEG: return g->out_deg.p;
+        case EG_DEV_EDGE_SRC: return g->esrc.p;
+        case EG_DEV_EDGE_DST: return g->edst.p;
         case EG_DEV_RANK: return g->rank.p;
         case EG_DEV_LEVEL: return g->level.p;
         case EG_DEV_PARENT: return g->parent.p;

@@ -144,6 +144,11 @@ struct eg_graph {
     // compact form of the row-id stream (valid because rows 0 .. csc_p_rows-1
     // all have entries)
     eg_buf csc_p_starts, csc_p_trow;
+    // edge array (load modes 7, 8, 9): sources and destinations of every
+    // adjacency entry in the order edge_order (EG_EDGES_*), and the
+    // edge-centric BFS's bitmaps and counters
+    eg_buf esrc, edst, edge_work;
+    int edge_order = -1;
     // grid
     uint32_t grid_p;
     eg_buf cell_ptr, gsrc, gdst;

@@ -23,7 +23,11 @@ static void pr_main(struct node *n) {
     o.prev_init = 0.15f;
     o.swap = !(mode == PULL && load_mode <= 6);
     eg_pr_stats st;
-    if (eg_pagerank(eg_g, &o, rank_h, &st) != EG_OK) eg_die("pagerank");
+    if (load_mode > 6) {  // pr_algo_edgecentric over the edge array (pagerank_simple.c:40-61)
+        if (eg_edges_pagerank(eg_g, &o, rank_h, &st) != EG_OK) eg_die("pagerank");
+    } else if (eg_pagerank(eg_g, &o, rank_h, &st) != EG_OK) {
+        eg_die("pagerank");
+    }
     printf("#Algo time ( %.3f sec) \n", st.ms / 1000.0);
     for (uint32_t i = 0; i < NB_NODES; i++) prev_h[i] = o.swap ? rank_h[i] : 0.15f;
     for (int i = 0; i < 10 && i < (int)NB_NODES; i++) printf("Rank[%d] = %.5f\n", i, prev_h[i]);

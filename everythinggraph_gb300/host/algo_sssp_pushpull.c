@@ -15,6 +15,7 @@ static void s_main(struct node *n) {
     eg_weights w = {EG_W_REF, 0, 0, 0};
     if (!switch_mode && mode == PUSH) w.rule = EG_W_UNIT;
     eg_sssp_stats st;
+    eg_need_adjacency(EG_LAYOUT_CSR);  // the edge-array modes build none
     if (eg_sssp(eg_g, BFS_ROOT, &w, dist_h, &st) != EG_OK) eg_die("sssp");
     printf("#Algo time ( %.3f sec) \n", st.ms / 1000.0);
     uint32_t t = 0;

@@ -48,6 +48,9 @@ extern eg_graph *eg_g;
 /* loader: mmap-free read of the [src][dst] file into HBM, then the device
  * layout builder selected by load_mode (init_all.c:855-888). */
 void init(int full);
+/* Builds the adjacency layouts an algorithm needs when the load mode did not
+ * (the edge-array modes 7, 8, 9 build none). */
+void eg_need_adjacency(unsigned layouts);
 
 double eg_now(void);
 void eg_die(const char *what);

@@ -6,7 +6,9 @@
  *             per-cell realloc lists are a host-side construction method)
  *   2, 3      CSR + CSC by stable device radix sort (init_adj_sort)
  *   4, 5      count sort / dynamic lists: the same device CSR + CSC
- *   7, 8, 9   edge array: the device CSR (edge array sorted by src)
+ *   7, 8, 9   edge array only, no adjacency (init_edgelist,
+ *             init_all.c:573-628): 7 sorted by src, 8 by src then dst,
+ *             9 in file order (eg_graph_build_edges)
  * -u appends the reversed edges for the adjacency modes only, as in the
  * reference (init_all.c:636 doubles nb_edges only in init_adj_sort).
  */
@@ -27,6 +29,13 @@ void init(int full) {
     eg_graph_get_info(eg_g, &info);
     nb_edges = info.m;
     printf("#NB edges = %llu\n", (unsigned long long)info.m_input);
+    if (load_mode >= 7 && load_mode <= 9) {
+        const int order = load_mode == 7 ? EG_EDGES_BY_SRC : load_mode == 8 ? EG_EDGES_BY_SRC_DST : EG_EDGES_FILE_ORDER;
+        if (eg_graph_build_edges(eg_g, order) != EG_OK) eg_die("edge array build");
+        eg_graph_get_info(eg_g, &info);
+        printf("#Device edge array build time ( %f s )\n", info.build_ms / 1000.0);
+        return;
+    }
     unsigned layouts = EG_LAYOUT_CSR | EG_LAYOUT_CSC;
     if (isSymmetric && adjacency_mode) layouts = EG_LAYOUT_CSR;
     if (eg_graph_build(eg_g, layouts) != EG_OK) eg_die("build");
@@ -35,4 +44,11 @@ void init(int full) {
     }
     eg_graph_get_info(eg_g, &info);
     printf("#Device layout build time ( %f s )\n", info.build_ms / 1000.0);
+}
+
+void eg_need_adjacency(unsigned layouts) {
+    eg_graph_info info;
+    eg_graph_get_info(eg_g, &info);
+    if ((info.layouts & layouts) == layouts) return;
+    if (eg_graph_build(eg_g, layouts) != EG_OK) eg_die("adjacency build");
 }

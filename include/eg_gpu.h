@@ -96,6 +96,7 @@ void eg_graph_free(eg_graph *g);
 #define EG_LAYOUT_CSR 1u /* out-lists, stable by src: each list in file order */
 #define EG_LAYOUT_CSC 2u /* in-lists: ascending src, ties in file order */
 #define EG_LAYOUT_GRID 4u
+#define EG_LAYOUT_EDGES 8u /* the edge array of eg_graph_build_edges */
 
 int eg_graph_build(eg_graph *g, unsigned layouts);
 /* 2-D grid of P x P cells (reference partitioning, init_all.c:54-60):
@@ -125,6 +126,8 @@ int eg_graph_copy_degrees(eg_graph *g, uint32_t *out_deg, uint32_t *in_deg);
 #define EG_DEV_CSC_PTR 3
 #define EG_DEV_CSC_COL 4
 #define EG_DEV_OUT_DEG 5
+#define EG_DEV_EDGE_SRC 6 /* uint32[m], the edge array's sources (eg_graph_build_edges) */
+#define EG_DEV_EDGE_DST 7 /* uint32[m], its destinations */
 #define EG_DEV_RANK 10   /* float[n], last eg_pagerank */
 #define EG_DEV_LEVEL 11  /* int32[n], last eg_bfs */
 #define EG_DEV_PARENT 12 /* int32[n], last eg_bfs with parents */
@@ -331,6 +334,38 @@ typedef struct {
     float ms;
 } eg_wcc_stats;
 int eg_wcc(eg_graph *g, int64_t *labels_out, eg_wcc_stats *stats);
+
+/* ---- edge array (replaces init_edgelist, init_all.c:573-628: load modes
+ * 7, 8, 9) ------------------------------------------------------------------
+ * Builds the device edge array without any CSR or CSC: the input's edges
+ * (reversed copies after them with EG_UNDIRECTED) as two uint32 arrays,
+ * sources and destinations, in one of three orders, plus the out- and
+ * in-degree counts (count_degree, init_all.c:425-443).  The edge-centric
+ * calls below stream it; eg_wcc on a graph without a CSR hooks the input
+ * edges directly (the WCC edge loop, wcc.c:235-261). */
+#define EG_EDGES_FILE_ORDER 0  /* mode 9: input order, no sort */
+#define EG_EDGES_BY_SRC 1      /* mode 7: stable sort by source */
+#define EG_EDGES_BY_SRC_DST 2  /* mode 8: by source, then by destination */
+int eg_graph_build_edges(eg_graph *g, int order);
+/* Copies the edge array to the host (src and dst have m entries; either may
+ * be NULL). */
+int eg_graph_copy_edges(eg_graph *g, uint32_t *src, uint32_t *dst);
+/* Edge-centric BFS (bfs_edgecentric, bfs_simple.c:58-103): every level
+ * streams the whole edge array and each edge whose source is in the frontier
+ * claims its unvisited destination.  Same levels (root 1, unreached 0) and
+ * parent convention as eg_bfs. */
+int eg_edges_bfs(eg_graph *g, uint32_t root, int32_t *level_out, int32_t *parent_out, eg_bfs_stats *stats);
+/* Edge-centric PageRank (pr_algo_edgecentric, pagerank_simple.c:40-61, and
+ * prgrid_algo_col, prgrid_cilk.c:79-88): every iteration adds
+ * prev[src]/deg[src] into rank[dst] for every edge with fp32 atomic adds
+ * (not in a fixed order), then rank = (1-d)/n + d * sum.  Uses iterations,
+ * damping, prev_init, swap, deg_multiplier, dangling and tolerance of the
+ * options (swap = 0 keeps prev at prev_init).  stats->row_kernel_ms is 0. */
+int eg_edges_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out, eg_pr_stats *stats);
+/* The SpMV edge loop (spmv.c:130-135): y[src] += x[dst] over every edge,
+ * u32 wrapping adds (exact in any order).  x: host array of n; y: host array
+ * of n or NULL (kept on the device, EG_DEV_SPMV_Y). */
+int eg_edges_spmv_u32(eg_graph *g, const uint32_t *x, uint32_t *y, float *ms);
 
 /* ---- personalised PageRank, batched ---------------------------------------
  * No counterpart in the reference (which runs one global PageRank; the

@@ -60,6 +60,12 @@ def make(name, n, pairs, store_pairs, roots, tmp):
     rec["prgrid_m0"] = run_ref("prgrid_cilk", f + ["-m", "0"], np.float32, n, tmp)
     rec["bfs_simple_m2u"] = run_ref("bfs_simple", f + ["-m", "2", "-u"], np.uint32, n, tmp)
     rec["bfs_simple_m8"] = run_ref("bfs_simple", f + ["-m", "8"], np.uint32, n, tmp)
+    # the edge-array load modes: 7 (sorted by src), 9 (file order); prgrid's
+    # column loop over the edge array (degrees counted twice in mode 9)
+    rec["bfs_simple_m7"] = run_ref("bfs_simple", f + ["-m", "7"], np.uint32, n, tmp)
+    rec["bfs_simple_m9"] = run_ref("bfs_simple", f + ["-m", "9"], np.uint32, n, tmp)
+    for mode in ("7", "8", "9"):
+        rec["prgrid_m" + mode] = run_ref("prgrid_cilk", f + ["-m", mode], np.float32, n, tmp)
     for r in roots:
         rec["bfsgrid_m0_p%d" % r] = run_ref("bfsgrid_cilk", f + ["-m", "0", "-p", str(r)], np.uint32, n, tmp)
         rec["sssp_pull_p%d" % r] = run_ref("sssp_pushpull", f + ["-m", "2", "-a", "1", "-r", "-p", str(r)],

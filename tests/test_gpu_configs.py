@@ -9,7 +9,8 @@ oracle (which the golden tests pin to the reference's dumps).
   eg_sssp_multi batch; fp32 weights bit-exact too;
 * directed RMAT-20 (seed 1): 10 PageRank iterations from 1/n within relative
   L1 1e-6 and max relative 1e-5 of FP64; the reference's pull quirk
-  (prev = 0.15, never swapped) within 2e-5 of the fp32 restatement;
+  (prev = 0.15, never swapped) within the same bounds of FP64 and within
+  2e-5 (plus the serial sum's own error) of the fp32 restatement;
 * directed RMAT-24 (seed 1): the headline PageRank within the same FP64
   bounds;
 * Erdos-Renyi 2^25 x 32 (seed 4): fp32 and fp32 two-sum SpMV with hashed
@@ -151,11 +152,18 @@ def test_rmat20_pagerank_config(ctx):
     rank, st = g.pagerank(iterations=10)
     l1, mx, _ = rel_errors(rank, ref)
     assert l1 <= REL_L1 and mx <= MAX_REL, (l1, mx)
-    # the reference's pull mode: prev = 0.15, never swapped (one effective step)
+    # the reference's pull mode: prev = 0.15, never swapped (one effective
+    # step).  Against FP64 within the bounds above; against the reference's
+    # serial fp32 row sums within 2e-5 plus that serial sum's own error (a
+    # hub row of 10^5 terms summed serially in fp32 is off FP64 by more
+    # than 2e-5 itself)
+    r64 = oracle.pagerank_f64(adj, adj.out_deg(), 0.15, 1)
     r32 = oracle.pagerank_f32(adj, adj.out_deg(), 0.15, 10, swap=False)
     got, _ = g.pagerank(iterations=10, prev_init=0.15, swap=False)
-    _, mx32, _ = rel_errors(got, r32)
-    assert mx32 <= VS_REF32_MAX_REL, mx32
+    l1, mx, _ = rel_errors(got, r64)
+    assert l1 <= REL_L1 and mx <= MAX_REL, ("quirk vs fp64", l1, mx)
+    own = np.abs(r32.astype(np.float64) - r64)
+    assert np.all(np.abs(got.astype(np.float64) - r32) <= own + VS_REF32_MAX_REL * np.abs(r64))
     g.free()
 
 

@@ -60,6 +60,18 @@ def test_prgrid(case):
     np.testing.assert_array_equal(got2.view(np.uint32), rec["prgrid_m0"].view(np.uint32))
 
 
+def test_prgrid_edge_array(case):
+    # prgrid_cilk -m 7/8/9: prgrid_algo_col over the edge array with atomic
+    # fp32 adds (no fixed order, so a tolerance, as for the GPU), degrees
+    # counted once in modes 7/8 (init_edgelist rewrites them) and twice in 9
+    name, n, pairs, rec = case
+    adj = oracle.build_adj(n, pairs)
+    for mode, mult in ((7, 1), (8, 1), (9, 2)):
+        ref = oracle.pagerank_f64(adj, mult * adj.out_deg(), 0.15, 10)
+        got = rec["prgrid_m%d" % mode].astype(np.float64)
+        assert np.max(np.abs(got - ref) / np.maximum(np.abs(ref), 1e-30)) <= 5e-5, mode
+
+
 def test_bfs(case):
     name, n, pairs, rec = case
     adj = oracle.build_adj(n, pairs)
@@ -69,6 +81,8 @@ def test_bfs(case):
     # bfs_simple -m 8 (edge-centric): levels from root 0
     lv0 = oracle.bfs_levels(n, adj.out_ptr, adj.out_col, 0)
     np.testing.assert_array_equal(lv0.astype(np.uint32), rec["bfs_simple_m8"])
+    np.testing.assert_array_equal(lv0.astype(np.uint32), rec["bfs_simple_m7"])
+    np.testing.assert_array_equal(lv0.astype(np.uint32), rec["bfs_simple_m9"])
     # bfs_simple -m 2 -u: visited counters; the visited set is the -u BFS reach
     adju = oracle.build_adj(n, pairs, undirected=True)
     lvu = oracle.bfs_levels(n, adju.out_ptr, adju.out_col, 0)
