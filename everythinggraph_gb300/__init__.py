@@ -68,6 +68,13 @@ def _out(a, n, dtype, name):
     return a
 
 
+def _grid_mode(grid):
+    """grid option: False (0), True (1: the fixed-order row kernel in the
+    grid's order when the adjacency is built) or "cells" (2: the cell kernel
+    with atomic adds)."""
+    return 2 if grid == "cells" else int(bool(grid))
+
+
 def weights(rule="ref", seed=0, lo=1, hi=255):
     """SSSP weight rule: "ref" (src%10+dst%10), "hash" (u32 in [lo, hi]),
     "unit", or "f32" (fp32 in (0, 1]; distances come back as float32)."""
@@ -186,6 +193,17 @@ class Graph:
         L.check(lib().eg_graph_build_edges(self._h, EDGE_ORDERS[order]))
         return self
 
+    def save_layouts(self, path):
+        """Writes the built layouts to an on-disk cache file (eg_graph_save_layouts)."""
+        L.check(lib().eg_graph_save_layouts(self._h, path.encode()))
+
+    def load_layouts(self, path):
+        """Fills the layouts from a cache file written for the same input;
+        True on a hit, False when the file is absent or for another input."""
+        hit = ctypes.c_int()
+        L.check(lib().eg_graph_load_layouts(self._h, path.encode(), ctypes.byref(hit)))
+        return bool(hit.value)
+
     def edges(self):
         """(src, dst) of the edge array, m entries each."""
         m = self.m
@@ -287,7 +305,7 @@ class Graph:
         o.iterations, o.damping, o.prev_init, o.swap = iterations, damping, prev_init, int(swap)
         o.deg_multiplier, o.dangling, o.compensated, o.tolerance = deg_multiplier, int(dangling), int(compensated), tolerance
         o.use_graph = int(use_graph)
-        o.grid = int(grid)
+        o.grid = _grid_mode(grid)
         o.source_block_log2 = int(source_block_log2)
         st = L.PrStats()
         out = np.empty(self.n, dtype=np.float32) if copy_out else None
@@ -303,7 +321,7 @@ class Graph:
         x = np.ascontiguousarray(x, dtype=xd)
         yd = np.float64 if kind == "f64" else xd
         y = np.empty(self.n, dtype=yd) if copy_out else None
-        o = L.SpmvOpts(k, value_seed, int(unit_values), int(grid), int(source_block_log2))
+        o = L.SpmvOpts(k, value_seed, int(unit_values), _grid_mode(grid), int(source_block_log2))
         ms = ctypes.c_float()
         L.check(lib().eg_spmv(self._h, ctypes.byref(o), _ptr(x), _ptr(y), ctypes.byref(ms)))
         return y, ms.value

@@ -156,6 +156,8 @@ SIGNATURES = {
     "eg_serve_close": (c_int, [c_void_p]),
     "eg_spmv_f32_noalloc": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p, c_void_p, c_u32, c_u64, c_void_p]),
     "eg_graph_build_edges": (c_int, [c_void_p, c_int]),
+    "eg_graph_save_layouts": (c_int, [c_void_p, c_char_p]),
+    "eg_graph_load_layouts": (c_int, [c_void_p, c_char_p, c_void_p]),
     "eg_graph_copy_edges": (c_int, [c_void_p, c_void_p, c_void_p]),
     "eg_edges_bfs": (c_int, [c_void_p, c_u32, c_void_p, c_void_p, c_void_p]),
     "eg_edges_pagerank": (c_int, [c_void_p, c_void_p, c_void_p, c_void_p]),

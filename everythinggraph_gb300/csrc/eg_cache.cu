@@ -1,0 +1,227 @@
+// On-disk cache of built layouts.
+//
+// The reference reads a raw edge file on every run and rebuilds its layout;
+// its pre-processed-file path (not_processed, random.c:6, and the header
+// arithmetic of init_all.c:823-824) is dead code.  eg_graph_save_layouts
+// writes every layout a graph has built (CSR, CSC with their row ids and
+// degrees, the grid, the edge array) after a header that names the input:
+// n, the input edge count, the flags, and a 64-bit digest of the input edges
+// computed on the device.  eg_graph_load_layouts fills a graph loaded from
+// the same input straight from the file, skipping the sorts; a file for
+// another input (or of another version) is a miss, not an error.
+//
+// The digest is an order-sensitive sum over the input edges e of
+// mix(key(e) ^ (src << 32 | dst)): any change of an endpoint or of the edge
+// order changes it with probability about 1 - 2^-64 per change.  It is a
+// cache key, not a cryptographic hash.
+#include <stdio.h>
+#include <string.h>
+
+#include "eg_internal.cuh"
+
+#define EG_CACHE_MAGIC "EGLAYT01"
+#define EG_CACHE_CHUNK (64ull << 20)  // bytes per staged copy
+
+namespace {
+
+struct CacheHeader {
+    char magic[8];
+    uint32_t n;
+    uint32_t flags;
+    uint64_t m_in;
+    uint64_t m;
+    uint64_t digest;
+    uint32_t layouts;
+    uint32_t grid_p;
+    int32_t edge_order;
+    uint32_t nbufs;
+};
+
+__global__ void k_pairs_digest(const uint32_t *__restrict__ pairs, uint64_t m, unsigned long long *out) {
+    unsigned long long h = 0;
+    for (uint64_t e = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; e < m; e += (uint64_t)gridDim.x * blockDim.x) {
+        const uint2 p = reinterpret_cast<const uint2 *>(pairs)[e];
+        h += eg_mix64(eg_key(0x6c61796f7574ull, e) ^ (((uint64_t)p.x << 32) | p.y));
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) h += __shfl_down_sync(EG_FULL_MASK, h, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(out, h);
+}
+
+int pairs_digest(eg_graph *g, uint64_t *out) {
+    eg_ctx *ctx = g->ctx;
+    unsigned long long *d = nullptr;
+    EG_TRY(eg_dmalloc(ctx, (void **)&d, 8));
+    int rc = eg_zero(ctx, d, 8, ctx->stream);
+    if (rc == EG_OK && g->m_in) {
+        uint64_t blocks = (g->m_in + 255) / 256;
+        if (blocks > (uint64_t)ctx->sm_count * 8) blocks = (uint64_t)ctx->sm_count * 8;
+        k_pairs_digest<<<(uint32_t)blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->pairs), g->m_in, d);
+        ctx->launches++;
+        if (cudaGetLastError() != cudaSuccess) rc = eg_fail(EG_ECUDA, "digest launch");
+    }
+    if (rc == EG_OK) {
+        unsigned long long h = 0;
+        cudaError_t e = cudaMemcpyAsync(&h, d, 8, cudaMemcpyDeviceToHost, ctx->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+        if (e != cudaSuccess) rc = eg_fail(EG_ECUDA, "digest: %s", cudaGetErrorString(e));
+        *out = h ^ ((uint64_t)g->n << 1) ^ g->m_in;
+    }
+    eg_dfree(ctx, d, 8);
+    return rc;
+}
+
+// The device arrays of each built layout, in file order.
+struct CacheBuf {
+    eg_buf *b;
+    uint64_t bytes;
+};
+int cache_bufs(eg_graph *g, unsigned layouts, CacheBuf *out) {
+    const uint64_t n = g->n, m = g->m;
+    int k = 0;
+    if (layouts & EG_LAYOUT_CSR) {
+        out[k++] = {&g->csr.ptr, (n + 1) * 4};
+        out[k++] = {&g->csr.col, m * 4};
+        out[k++] = {&g->csr.rid, m * 4};
+    }
+    if (layouts & EG_LAYOUT_CSC) {
+        out[k++] = {&g->csc.ptr, (n + 1) * 4};
+        out[k++] = {&g->csc.col, m * 4};
+        out[k++] = {&g->csc.rid, m * 4};
+    }
+    if (layouts & EG_LAYOUT_GRID) {
+        out[k++] = {&g->cell_ptr, ((uint64_t)g->grid_p * g->grid_p + 1) * 4};
+        out[k++] = {&g->gsrc, m * 4};
+        out[k++] = {&g->gdst, m * 4};
+    }
+    if (layouts & EG_LAYOUT_EDGES) {
+        out[k++] = {&g->esrc, m * 4};
+        out[k++] = {&g->edst, m * 4};
+    }
+    if (layouts & (EG_LAYOUT_CSR | EG_LAYOUT_EDGES)) out[k++] = {&g->out_deg, n * 4};
+    if (layouts & (EG_LAYOUT_CSC | EG_LAYOUT_EDGES)) out[k++] = {&g->in_deg, n * 4};
+    return k;
+}
+
+// Copies device <-> file through a pinned staging buffer, one chunk at a time.
+int stage_out(eg_ctx *ctx, const void *dev, uint64_t bytes, FILE *f, void *stage) {
+    for (uint64_t off = 0; off < bytes; off += EG_CACHE_CHUNK) {
+        const uint64_t c = bytes - off < EG_CACHE_CHUNK ? bytes - off : EG_CACHE_CHUNK;
+        EG_CUDA(cudaMemcpyAsync(stage, (const char *)dev + off, c, cudaMemcpyDeviceToHost, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        if (fwrite(stage, 1, c, f) != c) return eg_fail(EG_EIO, "layout cache: short write");
+    }
+    return EG_OK;
+}
+int stage_in(eg_ctx *ctx, void *dev, uint64_t bytes, FILE *f, void *stage) {
+    for (uint64_t off = 0; off < bytes; off += EG_CACHE_CHUNK) {
+        const uint64_t c = bytes - off < EG_CACHE_CHUNK ? bytes - off : EG_CACHE_CHUNK;
+        if (fread(stage, 1, c, f) != c) return eg_fail(EG_EIO, "layout cache: short read");
+        EG_CUDA(cudaMemcpyAsync((char *)dev + off, stage, c, cudaMemcpyHostToDevice, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    return EG_OK;
+}
+
+struct Stage {
+    void *p = nullptr;
+    ~Stage() {
+        if (p) cudaFreeHost(p);
+    }
+};
+
+}  // namespace
+
+extern "C" int eg_graph_save_layouts(eg_graph *g, const char *path) {
+    if (!g || !path) return eg_fail(EG_EINVAL, "NULL argument");
+    eg_ctx *ctx = g->ctx;
+    EG_CUDA(cudaSetDevice(ctx->device));
+    const unsigned layouts = g->built & (EG_LAYOUT_CSR | EG_LAYOUT_CSC | EG_LAYOUT_GRID | EG_LAYOUT_EDGES);
+    if (!layouts) return eg_fail(EG_ENOTBUILT, "no layout built");
+    CacheHeader h;
+    memset(&h, 0, sizeof(h));
+    memcpy(h.magic, EG_CACHE_MAGIC, 8);
+    h.n = g->n;
+    h.flags = g->flags;
+    h.m_in = g->m_in;
+    h.m = g->m;
+    EG_TRY(pairs_digest(g, &h.digest));
+    h.layouts = layouts;
+    h.grid_p = g->grid_p;
+    h.edge_order = g->edge_order;
+    CacheBuf bufs[16];
+    h.nbufs = (uint32_t)cache_bufs(g, layouts, bufs);
+    Stage stage;
+    EG_CUDA(cudaMallocHost(&stage.p, EG_CACHE_CHUNK));
+    // written under a temporary name and renamed, so a reader never sees a
+    // half-written file
+    char tmp[4096];
+    if (snprintf(tmp, sizeof(tmp), "%s.tmp", path) >= (int)sizeof(tmp)) return eg_fail(EG_EINVAL, "path too long");
+    FILE *f = fopen(tmp, "wb");
+    if (!f) return eg_fail(EG_EIO, "cannot create %s", tmp);
+    int rc = fwrite(&h, sizeof(h), 1, f) == 1 ? EG_OK : eg_fail(EG_EIO, "layout cache: short write");
+    for (uint32_t i = 0; i < h.nbufs && rc == EG_OK; i++) rc = stage_out(ctx, bufs[i].b->p, bufs[i].bytes, f, stage.p);
+    if (fclose(f) != 0 && rc == EG_OK) rc = eg_fail(EG_EIO, "layout cache: close failed");
+    if (rc == EG_OK && rename(tmp, path) != 0) rc = eg_fail(EG_EIO, "cannot rename %s", tmp);
+    if (rc != EG_OK) remove(tmp);
+    return rc;
+}
+
+extern "C" int eg_graph_load_layouts(eg_graph *g, const char *path, int *hit) {
+    if (!g || !path || !hit) return eg_fail(EG_EINVAL, "NULL argument");
+    *hit = 0;
+    eg_ctx *ctx = g->ctx;
+    EG_CUDA(cudaSetDevice(ctx->device));
+    FILE *f = fopen(path, "rb");
+    if (!f) return EG_OK;  // no cache yet
+    CacheHeader h;
+    bool match = fread(&h, sizeof(h), 1, f) == 1 && memcmp(h.magic, EG_CACHE_MAGIC, 8) == 0 && h.n == g->n &&
+                 h.flags == g->flags && h.m_in == g->m_in && h.m == g->m && h.nbufs <= 16 &&
+                 !(h.layouts & ~(EG_LAYOUT_CSR | EG_LAYOUT_CSC | EG_LAYOUT_GRID | EG_LAYOUT_EDGES));
+    if (match) {
+        uint64_t d = 0;
+        int rc = pairs_digest(g, &d);
+        if (rc != EG_OK) {
+            fclose(f);
+            return rc;
+        }
+        match = d == h.digest;
+    }
+    if (!match) {
+        fclose(f);
+        return EG_OK;  // another input's layouts: a miss
+    }
+    // the buffers this header names, sized as a build would size them
+    const uint32_t saved_p = g->grid_p;
+    g->grid_p = h.grid_p;
+    CacheBuf bufs[16];
+    const int nb = cache_bufs(g, h.layouts, bufs);
+    int rc = nb == (int)h.nbufs ? EG_OK : eg_fail(EG_EIO, "layout cache: %u buffers, expected %d", h.nbufs, nb);
+    Stage stage;
+    if (rc == EG_OK && cudaMallocHost(&stage.p, EG_CACHE_CHUNK) != cudaSuccess)
+        rc = eg_fail(EG_ENOMEM, "layout cache: no pinned staging");
+    for (int i = 0; i < nb && rc == EG_OK; i++) {
+        // +16: the row kernels read 16-byte vectors past the last entry
+        rc = eg_buf_ensure(ctx, *bufs[i].b, bufs[i].bytes + 16);
+        if (rc == EG_OK) rc = stage_in(ctx, bufs[i].b->p, bufs[i].bytes, f, stage.p);
+    }
+    if (rc == EG_OK && fgetc(f) != EOF) rc = eg_fail(EG_EIO, "layout cache: trailing bytes in %s", path);
+    fclose(f);
+    if (rc != EG_OK) {
+        g->grid_p = saved_p;
+        return rc;
+    }
+    g->built |= h.layouts;
+    g->edge_order = h.edge_order;
+    // derived copies follow the layouts they were made from
+    g->first_in_src = nullptr;
+    g->relabeled = false;
+    g->sb.blocks = g->sb.shift = 0;
+    g->sbp.blocks = g->sbp.shift = 0;
+    g->grid_order_p = 0;
+    g->grid_vals_kind = 0;
+    g->spmv_vals_kind = 0;
+    for (uint64_t &k : g->wts_key) k = ~0ull;
+    *hit = 1;
+    return EG_OK;
+}

@@ -409,7 +409,7 @@ extern "C" void eg_graph_free(eg_graph *g) {
         if (bg.exec) cudaGraphExecDestroy(bg.exec);
         if (bg.graph) cudaGraphDestroy(bg.graph);
     }
-    for (eg_bfs_graph *bg : {&g->prg, &g->msg}) {
+    for (eg_bfs_graph *bg : {&g->prg, &g->msg, &g->ssg, &g->ppg}) {
         if (bg->exec) cudaGraphExecDestroy(bg->exec);
         if (bg->graph) cudaGraphDestroy(bg->graph);
     }

@@ -176,6 +176,8 @@ struct eg_graph {
     eg_bfs_graph bfsg[2 * EG_OUT_SLOTS];  // [slot * 2 + with parents]
     eg_bfs_graph prg;      // PageRank iterations (key: options and buffers)
     eg_bfs_graph msg;      // multi-source BFS level loop
+    eg_bfs_graph ssg;      // batched SSSP round loop
+    eg_bfs_graph ppg;      // batched personalised PageRank sweep loop
     int row_cfg = 0;       // row-kernel schedule (entries per warp tile, per lane)
     int bfs_host_loop = 0; // BFS level-loop form eg_bfs uses by default (eg_graph_tune)
     double bfs_divisor = 20.0;  // push/pull switch divisor eg_bfs uses by default (eg_graph_tune)

@@ -23,6 +23,80 @@
 #include "eg_ppr.cuh"
 
 
+namespace {
+// Sweep-loop state of the batched PageRank graph.
+struct PprLoop {
+    int sweeps;
+    int max_sweeps;
+    int nq;
+    int pad;
+};
+
+__global__ void k_ppr_loop_init(PprLoop *st, int max_sweeps, int nq) {
+    st->sweeps = 0;
+    st->max_sweeps = max_sweeps;
+    st->nq = nq;
+}
+
+// Sweep end: the while node runs another sweep while a query of the batch is
+// still running (and fewer than max_iters sweeps ran).
+__global__ void k_ppr_loop_end(PprLoop *st, const PprQ *qs, cudaGraphConditionalHandle handle) {
+    st->sweeps += 1;
+    bool all = true;
+    for (int q = 0; q < st->nq; q++) all &= qs[q].done != 0;
+    cudaGraphSetConditional(handle, (!all && st->sweeps < st->max_sweeps) ? 1u : 0u);
+}
+
+// The sweep loop of eg_ppr_multi as one CUDA graph: a while node whose body
+// is one sweep (row sums of the 32 lanes, fix-up of rows split between
+// warps, rows without entries, seeds' teleport, finish and the per-query
+// FP64 reductions) and the loop test.  Valid while the buffers, nq and the
+// options it was captured with (key) stay the same.
+int ppr_graph_build(eg_graph *g, const void *const key[8], uint32_t ntiles, uint32_t row_blocks, uint32_t fin_blocks,
+                    const eg_ppr_opts &o, int nq, float *R, float *X, float *Y, float *hv, float *tvv, uint32_t *hr,
+                    double2 *part, const uint32_t *d_seeds, const uint32_t *d_soff, PprQ *qs, PprLoop *lst) {
+    eg_ctx *ctx = g->ctx;
+    eg_bfs_graph &bg = g->ppg;
+    if (bg.exec) cudaGraphExecDestroy(bg.exec);
+    if (bg.graph) cudaGraphDestroy(bg.graph);
+    bg.exec = nullptr;
+    bg.graph = nullptr;
+    const uint32_t n = g->n, m = (uint32_t)g->m;
+    const uint32_t *deg = bp<uint32_t>(g->out_deg);
+    cudaGraph_t graph = nullptr;
+    EG_CUDA(cudaGraphCreate(&graph, 0));
+    bg.graph = graph;
+    cudaGraphConditionalHandle handle;
+    EG_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    EG_CUDA(cudaGraphAddNode(&wnode, graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    EG_CUDA(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    if (row_blocks) {
+        k_ppr_rows<<<row_blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.rid), bp<uint32_t>(g->csc.col), m, ntiles,
+                                                        X, Y, hv, tvv, hr);
+        k_ppr_fixup<<<row_blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), ntiles, hr, hv, tvv, Y);
+    }
+    k_ppr_empty<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), n, Y);
+    k_ppr_seeds<<<1, EG_PPR_LANES, 0, ctx->stream>>>(d_seeds, d_soff, d_soff + 1, nq, qs, o.damping, Y);
+    k_ppr_finish<<<fin_blocks, 256, 0, ctx->stream>>>(Y, deg, n, o.damping, qs, R, X, part);
+    k_ppr_reduce<<<1, EG_PPR_LANES, 0, ctx->stream>>>(part, fin_blocks, qs, 1);
+    k_ppr_loop_end<<<1, 1, 0, ctx->stream>>>(lst, qs, handle);
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &body);
+    if (ce != cudaSuccess) return eg_fail(EG_ECUDA, "batched PageRank capture: %s", cudaGetErrorString(ce));
+    cudaGraphExec_t exec = nullptr;
+    EG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    bg.exec = exec;
+    for (int i = 0; i < 8; i++) bg.key[i] = key[i];
+    return EG_OK;
+}
+}  // namespace
+
 extern "C" int eg_ppr_multi(eg_graph *g, const uint32_t *seeds, const uint32_t *seed_offsets, int nq,
                             const eg_ppr_opts *opts, float *ranks_out, eg_ppr_stats *stats) {
     if (!g || !seeds || !seed_offsets) return eg_fail(EG_EINVAL, "NULL argument");
@@ -54,8 +128,9 @@ extern "C" int eg_ppr_multi(eg_graph *g, const uint32_t *seeds, const uint32_t *
     const uint64_t tv = (uint64_t)ntiles * EG_PPR_LANES;
     const uint64_t off_X = vec, off_Y = 2 * vec, off_hv = 3 * vec, off_tv = off_hv + tv, off_hr = off_tv + tv,
                    off_part = (off_hr + ntiles + 63) & ~63ull, off_seeds = off_part + (uint64_t)fin_blocks * 32 * 4,
-                   off_soff = off_seeds + nseeds_total + 8, off_q = (off_soff + 40 + 63) & ~63ull;
-    EG_TRY(eg_buf_ensure(ctx, g->ppr_work, (off_q + 32 * sizeof(PprQ) / 4 + 64) * 4));
+                   off_soff = off_seeds + nseeds_total + 8, off_q = (off_soff + 40 + 63) & ~63ull,
+                   off_loop = off_q + 32 * sizeof(PprQ) / 4;
+    EG_TRY(eg_buf_ensure(ctx, g->ppr_work, (off_loop + 64) * 4));
     float *W = bp<float>(g->ppr_work);
     float *R = W, *X = W + off_X, *Y = W + off_Y, *hv = W + off_hv, *tvv = W + off_tv;
     uint32_t *hr = reinterpret_cast<uint32_t *>(W + off_hr);
@@ -63,6 +138,7 @@ extern "C" int eg_ppr_multi(eg_graph *g, const uint32_t *seeds, const uint32_t *
     uint32_t *d_seeds = reinterpret_cast<uint32_t *>(W + off_seeds);
     uint32_t *d_soff = reinterpret_cast<uint32_t *>(W + off_soff);
     PprQ *qs = reinterpret_cast<PprQ *>(W + off_q);
+    PprLoop *lst = reinterpret_cast<PprLoop *>(W + off_loop);
     PprQ hq[EG_PPR_LANES];
     memset(hq, 0, sizeof(hq));
     for (int q = 0; q < nq; q++) {
@@ -85,36 +161,26 @@ extern "C" int eg_ppr_multi(eg_graph *g, const uint32_t *seeds, const uint32_t *
     EG_LAUNCHED(ctx);
     PprQ *hqs = (PprQ *)ctx->h_pinned;
     const uint32_t row_blocks = ntiles ? eg_div_up((uint64_t)ntiles * 32, 256) : 0;
-    const uint32_t empty_blocks = (uint32_t)ctx->sm_count * 8;
-    int it;
-    for (it = 0; it < o.max_iters; it++) {
-        if (row_blocks) {
-            k_ppr_rows<<<row_blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.rid), bp<uint32_t>(g->csc.col), m, ntiles,
-                                                            X, Y, hv, tvv, hr);
-            EG_LAUNCHED(ctx);
-            k_ppr_fixup<<<row_blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), ntiles, hr, hv, tvv, Y);
-            EG_LAUNCHED(ctx);
-        }
-        k_ppr_empty<<<empty_blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), n, Y);
-        EG_LAUNCHED(ctx);
-        k_ppr_seeds<<<1, EG_PPR_LANES, 0, ctx->stream>>>(d_seeds, d_soff, d_soff + 1, nq, qs, o.damping, Y);
-        EG_LAUNCHED(ctx);
-        k_ppr_finish<<<fin_blocks, 256, 0, ctx->stream>>>(Y, deg, n, o.damping, qs, R, X, part);
-        EG_LAUNCHED(ctx);
-        k_ppr_reduce<<<1, EG_PPR_LANES, 0, ctx->stream>>>(part, fin_blocks, qs, 1);
-        EG_LAUNCHED(ctx);
-        // every 4 iterations: stop once every query is done
-        if ((it & 3) == 3 || it + 1 == o.max_iters) {
-            EG_CUDA(cudaMemcpyAsync(hqs, qs, sizeof(PprQ) * EG_PPR_LANES, cudaMemcpyDeviceToHost, ctx->stream));
-            EG_CUDA(cudaStreamSynchronize(ctx->stream));
-            bool all = true;
-            for (int q = 0; q < nq; q++) all &= hqs[q].done != 0;
-            if (all) {
-                it++;
-                break;
-            }
-        }
-    }
+    // the sweeps: one CUDA graph launch (a while node over one sweep)
+    k_ppr_loop_init<<<1, 1, 0, ctx->stream>>>(lst, o.max_iters, nq);
+    EG_LAUNCHED(ctx);
+    uint32_t dmg;
+    memcpy(&dmg, &o.damping, 4);
+    // n and m are the graph's own; the seed offsets' place follows the seed count
+    const void *key[8] = {W, g->csc.col.p, g->csc.rid.p, (const void *)(uintptr_t)nq,
+                          (const void *)(uintptr_t)dmg, d_soff, g->csc.ptr.p, g->out_deg.p};
+    eg_bfs_graph &bg = g->ppg;
+    bool same = bg.exec != nullptr;
+    for (int i = 0; i < 8 && same; i++) same = bg.key[i] == key[i];
+    if (!same)
+        EG_TRY(ppr_graph_build(g, key, ntiles, row_blocks, fin_blocks, o, nq, R, X, Y, hv, tvv, hr, part, d_seeds,
+                               d_soff, qs, lst));
+    EG_CUDA(cudaGraphLaunch(bg.exec, ctx->stream));
+    ctx->launches += 1;
+    PprLoop *hl = reinterpret_cast<PprLoop *>(hqs + EG_PPR_LANES);
+    EG_TRY(eg_readback(ctx, hl, lst, sizeof(PprLoop), ctx->stream));
+    EG_CUDA(cudaStreamSynchronize(ctx->stream));
+    const int it = hl->sweeps;
     EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     if (ranks_out) {
         EG_TRY(eg_buf_ensure(ctx, g->rank, (uint64_t)n * 4));

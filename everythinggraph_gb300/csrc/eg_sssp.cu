@@ -192,7 +192,7 @@ extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wrule_in, u
     EG_TRY(eg_buf_ensure(ctx, g->dist, (uint64_t)n * 4));
     const uint64_t off_q0 = nw, off_q1 = off_q0 + n, off_big = off_q1 + n, off_bigoff = off_big + n,
                    off_cnt = (off_bigoff + n + 1 + 7) & ~7ull;
-    EG_TRY(eg_buf_ensure(ctx, g->sssp_work, (off_cnt + 8) * 4));
+    EG_TRY(eg_buf_ensure(ctx, g->sssp_work, (off_cnt + 16) * 4));
     uint32_t *wk = bp<uint32_t>(g->sssp_work);
     uint32_t *bm = wk, *q[2] = {wk + off_q0, wk + off_q1}, *big = wk + off_big, *bigoff = wk + off_bigoff;
     SsspCounters *cnt = reinterpret_cast<SsspCounters *>(wk + off_cnt);
@@ -252,6 +252,35 @@ extern "C" int eg_sssp(eg_graph *g, uint32_t root, const eg_weights *wrule_in, u
 // one (frontier vertex, source word) and walks the vertex's out-list; its 32
 // lanes relax 32 sources of the same edge (coalesced 128-byte rows).
 namespace {
+// Round-loop state of the batched SSSP graph: the current frontier's length,
+// the rounds run, and an error flag when the round bound was hit.
+struct MsState {
+    uint32_t qlen;
+    uint32_t rounds;
+    uint32_t limit;
+    uint32_t err;
+};
+
+// Round start: the counters the round's kernels accumulate into are cleared.
+__global__ void k_msssp_prep(SsspCounters *cnt) {
+    cnt->qsize = 0;
+    cnt->nbig = 0;
+    cnt->grab = 0;
+    cnt->grab_big = 0;
+}
+
+// Round end: the next frontier becomes the current one; the while node runs
+// the body (two rounds) again while a frontier is left and the bound allows.
+__global__ void k_msssp_end(MsState *st, const SsspCounters *cnt, cudaGraphConditionalHandle handle, int last) {
+    if (st->qlen) st->rounds += 1;
+    st->qlen = cnt->qsize;
+    if (st->qlen && st->rounds >= st->limit) {
+        st->err = 1;
+        st->qlen = 0;
+    }
+    if (last) cudaGraphSetConditional(handle, st->qlen ? 1u : 0u);
+}
+
 __global__ void k_msssp_init(uint32_t n, int k, uint32_t kw, uint32_t *dist, uint32_t *act0, uint32_t *act1,
                              uint32_t inf) {
     uint64_t total = (uint64_t)n * k;
@@ -304,13 +333,14 @@ struct MsSink {
 };
 
 __global__ void __launch_bounds__(256, EG_MSSSP_MINB) k_msssp_push(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
-                                                    const uint32_t *__restrict__ wts, const uint32_t *__restrict__ queue, uint32_t qlen, int k,
+                                                    const uint32_t *__restrict__ wts, const uint32_t *__restrict__ queue,
+                                                    const MsState *st, int k,
                                                     uint32_t kw, uint32_t *dist, const uint32_t *__restrict__ act,
                                                     uint32_t *next_act, uint32_t *next_inq, uint32_t *next_queue,
                                                     WRule w, SsspCounters *cnt, uint32_t *big) {
     const uint32_t lane = threadIdx.x & 31;
     unsigned long long scanned = 0;
-    const uint64_t items = (uint64_t)qlen * kw;
+    const uint64_t items = (uint64_t)st->qlen * kw;
     MsSink sink{0, kw, next_act, next_inq, next_queue, cnt};
     for (;;) {  // 32 items per unit
         const uint64_t base = (uint64_t)eg_warp_grab(&cnt->grab) * 32;
@@ -360,8 +390,9 @@ __global__ void __launch_bounds__(256) k_msssp_push_big(const uint32_t *__restri
 }
 
 // Clears the frontier words and queued bits of the vertices in a queue.
-__global__ void k_msssp_clear(const uint32_t *__restrict__ queue, uint32_t qlen, uint32_t kw, uint32_t *act,
+__global__ void k_msssp_clear(const uint32_t *__restrict__ queue, const MsState *st, uint32_t kw, uint32_t *act,
                               uint32_t *inq) {
+    const uint32_t qlen = st->qlen;
     for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < (uint64_t)qlen * kw;
          i += (uint64_t)gridDim.x * blockDim.x) {
         uint32_t v = queue[i / kw];
@@ -385,6 +416,70 @@ __global__ void k_transpose_dist(const uint32_t *__restrict__ dvk, uint32_t n, i
 }
 }  // namespace
 
+namespace {
+// Loop state from the roots' queue: qlen = the roots' frontier, no rounds yet.
+__global__ void k_msssp_state(MsState *st, const SsspCounters *cnt, uint32_t limit) {
+    st->qlen = cnt->qsize;
+    st->rounds = 0;
+    st->limit = limit;
+    st->err = 0;
+}
+}  // namespace
+
+// The round loop of eg_sssp_multi as one CUDA graph: a while node whose body
+// runs two rounds (frontier buffers 0 -> 1, then 1 -> 0), each round = clear
+// the counters, relax the frontier's (vertex, source word) items, cut the
+// hubs' deferred items into chunks and relax them, clear the old frontier,
+// and move the next frontier's length into the state.  Every kernel takes
+// its work from counters (fixed grids), so a round with an empty frontier
+// does nothing.  Valid while the buffers, k and the weight array it was
+// captured with (key) stay the same.
+static int msssp_graph_build(eg_graph *g, const void *const key[8], const uint32_t *wts, int k, uint32_t kw, WRule w,
+                             uint32_t *dist, uint32_t *const act[2], uint32_t *const inq[2], uint32_t *const q[2],
+                             uint32_t *big, uint32_t *bigoff, MsState *st, SsspCounters *cnt) {
+    eg_ctx *ctx = g->ctx;
+    eg_bfs_graph &bg = g->ssg;
+    if (bg.exec) cudaGraphExecDestroy(bg.exec);
+    if (bg.graph) cudaGraphDestroy(bg.graph);
+    bg.exec = nullptr;
+    bg.graph = nullptr;
+    cudaGraph_t graph = nullptr;
+    EG_CUDA(cudaGraphCreate(&graph, 0));
+    bg.graph = graph;
+    cudaGraphConditionalHandle handle;
+    EG_CUDA(cudaGraphConditionalHandleCreate(&handle, graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = handle;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t wnode;
+    EG_CUDA(cudaGraphAddNode(&wnode, graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    const uint32_t blocks = (uint32_t)ctx->sm_count * 8;
+    const uint32_t *ptr = bp<uint32_t>(g->csr.ptr), *col = bp<uint32_t>(g->csr.col);
+    EG_CUDA(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    for (int cur = 0; cur < 2; cur++) {
+        const int nxt = cur ^ 1;
+        k_msssp_prep<<<1, 1, 0, ctx->stream>>>(cnt);
+        k_msssp_push<<<blocks, 256, 0, ctx->stream>>>(ptr, col, wts, q[cur], st, k, kw, dist, act[cur], act[nxt],
+                                                       inq[nxt], q[nxt], w, cnt, big);
+        k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, kw, ptr, EG_MSSSP_CHUNK, bigoff);
+        k_msssp_push_big<<<blocks, 256, 0, ctx->stream>>>(ptr, col, wts, k, kw, dist, act[cur], act[nxt], inq[nxt],
+                                                           q[nxt], w, cnt, big, bigoff);
+        // the current frontier's words and bits are cleared for reuse as "next"
+        k_msssp_clear<<<blocks, 256, 0, ctx->stream>>>(q[cur], st, kw, act[cur], inq[cur]);
+        k_msssp_end<<<1, 1, 0, ctx->stream>>>(st, cnt, handle, cur);
+    }
+    cudaError_t ce = cudaStreamEndCapture(ctx->stream, &body);
+    if (ce != cudaSuccess) return eg_fail(EG_ECUDA, "batched SSSP capture: %s", cudaGetErrorString(ce));
+    cudaGraphExec_t exec = nullptr;
+    EG_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    bg.exec = exec;
+    for (int i = 0; i < 8; i++) bg.key[i] = key[i];
+    return EG_OK;
+}
+
 extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg_weights *wrule_in,
                              uint32_t *dist_out, eg_sssp_stats *stats) {
     if (!g || !roots) return eg_fail(EG_EINVAL, "NULL argument");
@@ -405,12 +500,13 @@ extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg
                    off_inq1 = off_inq0 + nw, off_q0 = off_inq1 + nw, off_q1 = off_q0 + n, off_big = off_q1 + n,
                    off_bigoff = off_big + (uint64_t)n * kw, off_roots = off_bigoff + (uint64_t)n * kw + 1,
                    off_cnt = (off_roots + 1024 + 7) & ~7ull;
-    EG_TRY(eg_buf_ensure(ctx, g->sssp_work, (off_cnt + 8) * 4));
+    EG_TRY(eg_buf_ensure(ctx, g->sssp_work, (off_cnt + 16) * 4));
     uint32_t *wk = bp<uint32_t>(g->sssp_work);
     uint32_t *dist = wk, *act[2] = {wk + off_act0, wk + off_act1}, *inq[2] = {wk + off_inq0, wk + off_inq1},
              *q[2] = {wk + off_q0, wk + off_q1}, *d_roots = wk + off_roots, *big = wk + off_big,
              *bigoff = wk + off_bigoff;
     SsspCounters *cnt = reinterpret_cast<SsspCounters *>(wk + off_cnt);
+    MsState *st = reinterpret_cast<MsState *>(wk + off_cnt + 8);
     SsspCounters *h = (SsspCounters *)ctx->h_pinned;
     EG_CUDA(cudaMemcpyAsync(d_roots, roots, (uint64_t)k * 4, cudaMemcpyHostToDevice, ctx->stream));
     EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
@@ -420,36 +516,26 @@ extern "C" int eg_sssp_multi(eg_graph *g, const uint32_t *roots, int k, const eg
     EG_CUDA(cudaMemsetAsync(cnt, 0, sizeof(SsspCounters), ctx->stream));
     k_msssp_roots<<<1, 256, 0, ctx->stream>>>(d_roots, k, kw, dist, act[0], inq[0], q[0], cnt);
     EG_LAUNCHED(ctx);
-    EG_CUDA(cudaMemcpyAsync(h, cnt, sizeof(SsspCounters), cudaMemcpyDeviceToHost, ctx->stream));
+    // the round loop: one CUDA graph launch (built once per graph, buffers,
+    // k and weight array; a while node over a body of two rounds, so that
+    // each half keeps its frontier buffers fixed)
+    k_msssp_state<<<1, 1, 0, ctx->stream>>>(st, cnt, (uint32_t)(4 * (uint64_t)n + 16));
+    EG_LAUNCHED(ctx);
+    const void *key[8] = {wk, wts, g->csr.col.p, (const void *)(uintptr_t)k, (const void *)(uintptr_t)kw,
+                          (const void *)(uintptr_t)w.rule, (const void *)(uintptr_t)n, nullptr};
+    eg_bfs_graph &bg = g->ssg;
+    bool same = bg.exec != nullptr;
+    for (int i = 0; i < 8 && same; i++) same = bg.key[i] == key[i];
+    if (!same) EG_TRY(msssp_graph_build(g, key, wts, k, kw, w, dist, act, inq, q, big, bigoff, st, cnt));
+    EG_CUDA(cudaGraphLaunch(bg.exec, ctx->stream));
+    ctx->launches += 1;
+    EG_TRY(eg_readback(ctx, h + 1, st, sizeof(MsState), ctx->stream));
+    EG_TRY(eg_readback(ctx, h, cnt, sizeof(SsspCounters), ctx->stream));
     EG_CUDA(cudaStreamSynchronize(ctx->stream));
-    uint32_t qlen = h->qsize;
-    int cur = 0, rounds = 0;
-    unsigned long long relax = 0;
-    while (qlen > 0) {
-        const int nxt = cur ^ 1;
-        EG_CUDA(cudaMemsetAsync(&cnt->qsize, 0, 8, ctx->stream));  // qsize and nbig
-        EG_CUDA(cudaMemsetAsync(&cnt->grab, 0, 8, ctx->stream));   // grab and grab_big
-        k_msssp_push<<<blocks_for(ctx, (uint64_t)qlen * kw), 256, 0, ctx->stream>>>(
-            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), wts, q[cur], qlen, k, kw, dist, act[cur], act[nxt], inq[nxt],
-            q[nxt], w, cnt, big);
-        EG_LAUNCHED(ctx);
-        k_big_offsets<<<1, 1024, 0, ctx->stream>>>(big, &cnt->nbig, kw, bp<uint32_t>(g->csr.ptr), EG_MSSSP_CHUNK,
-                                                   bigoff);
-        EG_LAUNCHED(ctx);
-        k_msssp_push_big<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
-            bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), wts, k, kw, dist, act[cur], act[nxt], inq[nxt], q[nxt], w,
-            cnt, big, bigoff);
-        EG_LAUNCHED(ctx);
-        // the current frontier's words and bits are cleared for reuse as "next"
-        k_msssp_clear<<<blocks_for(ctx, (uint64_t)qlen * kw), 256, 0, ctx->stream>>>(q[cur], qlen, kw, act[cur], inq[cur]);
-        EG_LAUNCHED(ctx);
-        EG_TRY(eg_readback_wait(ctx, h, cnt, sizeof(SsspCounters), ctx->stream));
-        qlen = h->qsize;
-        relax = h->relax;
-        cur = nxt;
-        rounds++;
-        if (rounds > (int)(4 * (uint64_t)n + 16)) return eg_fail(EG_ETIMEOUT, "batched SSSP did not converge");
-    }
+    const MsState *hst = reinterpret_cast<const MsState *>(h + 1);
+    if (hst->err) return eg_fail(EG_ETIMEOUT, "batched SSSP did not converge");
+    const int rounds = (int)hst->rounds;
+    const unsigned long long relax = h->relax;
     EG_CUDA(cudaEventRecord(ctx->ev1, ctx->stream));
     if (dist_out) {
         EG_TRY(eg_buf_ensure(ctx, g->dist, (uint64_t)n * k * 4));

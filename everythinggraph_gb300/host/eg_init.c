@@ -11,10 +11,25 @@
  *             9 in file order (eg_graph_build_edges)
  * -u appends the reversed edges for the adjacency modes only, as in the
  * reference (init_all.c:636 doubles nb_edges only in init_adj_sort).
+ * With EG_LAYOUT_CACHE=<directory> set, the built layouts are kept in
+ * <directory>/<file name>.m<mode>[u][P].eglayout and a later run on the same
+ * input fills them from there instead of sorting (the file's header carries
+ * a digest of the input edges, so a changed input is rebuilt).
  */
 #include <string.h>
 
 #include "eg_host.h"
+
+/* <EG_LAYOUT_CACHE>/<base name of the input>.m<mode>[u]p<P>.eglayout, or ""
+ * without the variable. */
+static void cache_path(char *out, size_t len) {
+    const char *dir = getenv("EG_LAYOUT_CACHE");
+    out[0] = 0;
+    if (!dir || !*dir) return;
+    const char *base = strrchr(filename, '/');
+    base = base ? base + 1 : filename;
+    snprintf(out, len, "%s/%s.m%d%sp%u.eglayout", dir, base, load_mode, createUndir ? "u" : "", (unsigned)P);
+}
 
 void init(int full) {
     (void)full;
@@ -29,11 +44,23 @@ void init(int full) {
     eg_graph_get_info(eg_g, &info);
     nb_edges = info.m;
     printf("#NB edges = %llu\n", (unsigned long long)info.m_input);
+    char cpath[4096];
+    cache_path(cpath, sizeof(cpath));
+    if (cpath[0]) {
+        int hit = 0;
+        double t0 = eg_now();
+        if (eg_graph_load_layouts(eg_g, cpath, &hit) != EG_OK) eg_die("layout cache");
+        if (hit) {
+            printf("#Layout cache hit %s ( %f s )\n", cpath, eg_now() - t0);
+            return;
+        }
+    }
     if (load_mode >= 7 && load_mode <= 9) {
         const int order = load_mode == 7 ? EG_EDGES_BY_SRC : load_mode == 8 ? EG_EDGES_BY_SRC_DST : EG_EDGES_FILE_ORDER;
         if (eg_graph_build_edges(eg_g, order) != EG_OK) eg_die("edge array build");
         eg_graph_get_info(eg_g, &info);
         printf("#Device edge array build time ( %f s )\n", info.build_ms / 1000.0);
+        if (cpath[0] && eg_graph_save_layouts(eg_g, cpath) != EG_OK) eg_die("layout cache save");
         return;
     }
     unsigned layouts = EG_LAYOUT_CSR | EG_LAYOUT_CSC;
@@ -44,6 +71,7 @@ void init(int full) {
     }
     eg_graph_get_info(eg_g, &info);
     printf("#Device layout build time ( %f s )\n", info.build_ms / 1000.0);
+    if (cpath[0] && eg_graph_save_layouts(eg_g, cpath) != EG_OK) eg_die("layout cache save");
 }
 
 void eg_need_adjacency(unsigned layouts) {

@@ -157,9 +157,14 @@ typedef struct {
     int compensated;
     double tolerance;
     int use_graph; /* 1: replay the iteration as a captured CUDA graph */
-    int grid;      /* 1: iterate over the 2-D grid layout (prgrid_cilk.c:62-141):
-                      cells in L2-sized blocks, sums by atomic adds (not in a
-                      fixed order); needs eg_graph_build_grid and the CSR */
+    int grid;      /* the grid load modes (prgrid_cilk.c:62-141); need
+                      eg_graph_build_grid.  1: with the CSR and CSC built,
+                      the row kernel over the CSC, whose per-destination
+                      order is the order in which prgrid visits a
+                      destination's cells (fixed-order sums, source blocks
+                      when n > 2^24); otherwise as 2.  2: the cell kernel:
+                      cells in L2-sized blocks, sums by atomic adds (not in
+                      a fixed order) */
     int source_block_log2; /* not compensated, n > 2^k (k = this, 0: 24): the
                       contributions are gathered one source block of 2^k
                       vertices per pass (a copy of the relabelled CSC split by
@@ -230,9 +235,14 @@ typedef struct {
     int kind;
     uint64_t value_seed; /* val(e) = U[0,1) hashed from (seed, min(u,v), max(u,v)) */
     int unit_values;     /* 1: val(e) = 1 */
-    int grid;            /* 1: over the 2-D grid layout (spmv.c's grid modes):
-                            cells in L2-sized blocks, y by atomic adds (u32
-                            exact; f32/f64 not in a fixed order; no F32_COMP) */
+    int grid;            /* spmv.c's grid modes; need the grid.  1: with the
+                            adjacency the kind reads (CSC for pull and fp
+                            kinds, CSR for push and edge) built, its fixed-
+                            order row kernel, which sums in the grid's
+                            per-row order; otherwise as 2.  2: the cell
+                            kernel: cells in L2-sized blocks, y by atomic
+                            adds (u32 exact; f32/f64 not in a fixed order;
+                            no F32_COMP) */
     int source_block_log2; /* EG_SPMV_F32(_COMP) with n > 2^k (k = this, 0: 24):
                             the entries are split by source block of 2^k
                             vertices (a copy of the CSC built once) and summed
@@ -366,6 +376,19 @@ int eg_edges_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out, eg_p
  * u32 wrapping adds (exact in any order).  x: host array of n; y: host array
  * of n or NULL (kept on the device, EG_DEV_SPMV_Y). */
 int eg_edges_spmv_u32(eg_graph *g, const uint32_t *x, uint32_t *y, float *ms);
+
+/* ---- layout cache (no working counterpart: the reference's pre-processed
+ * file path, random.c:6 and init_all.c:823-824, is dead code) --------------
+ * eg_graph_save_layouts writes every layout the graph has built (CSR and CSC
+ * with their row ids, the grid, the edge array, the degree arrays) to `path`
+ * behind a header naming the input: n, the input edge count, the flags and a
+ * 64-bit digest of the input edges computed on the device.  The file is
+ * written under path + ".tmp" and renamed.  eg_graph_load_layouts fills a
+ * graph loaded from the same input from such a file instead of sorting:
+ * *hit = 1 when it did; *hit = 0 (and EG_OK) when the file is absent or
+ * belongs to another input; EG_EIO when a matching file is truncated. */
+int eg_graph_save_layouts(eg_graph *g, const char *path);
+int eg_graph_load_layouts(eg_graph *g, const char *path, int *hit);
 
 /* ---- personalised PageRank, batched ---------------------------------------
  * No counterpart in the reference (which runs one global PageRank; the

@@ -255,38 +255,48 @@ def test_pagerank_tolerance_stops_early(case):
 
 
 def test_grid_spmv_and_pagerank(case):
-    # the grid-layout kernels (cells in L2-sized blocks, atomic sums): integer
-    # SpMV exact, float within tolerance, prgrid's PageRank against the
-    # reference's own dumps and FP64
+    # grid modes: grid=True runs the fixed-order row kernel (the grid's
+    # per-destination order is the CSC's), bit-identical to the plain call;
+    # grid="cells" the cell kernel (cells in L2-sized blocks, atomic sums):
+    # integer SpMV exact, float within tolerance, prgrid's PageRank against
+    # the reference's own dumps and FP64
     name, n, pairs, rec, g, gu, adj, adju = case
     P = oracle.default_p(n) if n > 100 else 3
     g.build_grid(P)
     x = np.arange(n, dtype=np.uint32)
-    y, _ = g.spmv(x, "u32_pull", grid=True)
-    np.testing.assert_array_equal(y, rec["spmv_pull"])
-    y, _ = g.spmv(x, "u32_push", grid=True)
-    np.testing.assert_array_equal(y, rec["spmv_push"])
-    y, _ = g.spmv(x, "u32_edge", grid=True)
-    np.testing.assert_array_equal(y, rec["spmv_m8"])
     xf = oracle.uniform_f32(n, 11)
     vals = oracle.hash_values(adj.in_col, adj.in_dst(), 9)
     ref = oracle.spmv_f64(n, adj.in_ptr, adj.in_col, vals, xf)
-    y64, _ = g.spmv(xf, "f64", value_seed=9, grid=True)
-    np.testing.assert_allclose(y64, ref, rtol=1e-12, atol=1e-300)
-    y32, _ = g.spmv(xf, "f32", value_seed=9, grid=True)
-    l1, mx = rel_errors(y32, ref)
-    assert l1 <= PR_REL_L1 and mx <= GRID_MAX_REL, (l1, mx)
+    for mode in (True, "cells"):
+        y, _ = g.spmv(x, "u32_pull", grid=mode)
+        np.testing.assert_array_equal(y, rec["spmv_pull"])
+        y, _ = g.spmv(x, "u32_push", grid=mode)
+        np.testing.assert_array_equal(y, rec["spmv_push"])
+        y, _ = g.spmv(x, "u32_edge", grid=mode)
+        np.testing.assert_array_equal(y, rec["spmv_m8"])
+        y64, _ = g.spmv(xf, "f64", value_seed=9, grid=mode)
+        np.testing.assert_allclose(y64, ref, rtol=1e-12, atol=1e-300)
+        y32, _ = g.spmv(xf, "f32", value_seed=9, grid=mode)
+        l1, mx = rel_errors(y32, ref)
+        assert l1 <= PR_REL_L1 and mx <= GRID_MAX_REL, (mode, l1, mx)
+        got, st = g.pagerank(iterations=10, prev_init=0.15, swap=True, deg_multiplier=2, grid=mode)
+        l1, mx = rel_errors(got, rec["prgrid_m0"])
+        assert mx <= PR_VS_REF32_MAX_REL, (mode, l1, mx)
+        ref_pr = oracle.pagerank_f64(adj, adj.out_deg(), 1.0 / n, 10, dangling=True)
+        got, st = g.pagerank(iterations=10, dangling=True, grid=mode)
+        l1, mx = rel_errors(got, ref_pr)
+        assert l1 <= PR_REL_L1 and mx <= GRID_MAX_REL, (mode, l1, mx)
+        got, st = g.pagerank(iterations=200, tolerance=1e-6, dangling=True, grid=mode)
+        assert 1 <= st.iterations_run < 200 and st.residual < 1e-6
     with pytest.raises(RuntimeError):
-        g.spmv(xf, "f32_comp", grid=True)
-    got, st = g.pagerank(iterations=10, prev_init=0.15, swap=True, deg_multiplier=2, grid=True)
-    l1, mx = rel_errors(got, rec["prgrid_m0"])
-    assert mx <= PR_VS_REF32_MAX_REL, (l1, mx)
-    ref = oracle.pagerank_f64(adj, adj.out_deg(), 1.0 / n, 10, dangling=True)
-    got, st = g.pagerank(iterations=10, dangling=True, grid=True)
-    l1, mx = rel_errors(got, ref)
-    assert l1 <= PR_REL_L1 and mx <= GRID_MAX_REL, (l1, mx)
-    got, st = g.pagerank(iterations=200, tolerance=1e-6, dangling=True, grid=True)
-    assert 1 <= st.iterations_run < 200 and st.residual < 1e-6
+        g.spmv(xf, "f32_comp", grid="cells")
+    # the fixed-order grid path is the row kernel itself: the same bits
+    y1, _ = g.spmv(xf, "f32", value_seed=9, grid=True)
+    y0, _ = g.spmv(xf, "f32", value_seed=9)
+    np.testing.assert_array_equal(y1.view(np.uint32), y0.view(np.uint32))
+    yc, _ = g.spmv(xf, "f32_comp", value_seed=9, grid=True)
+    l1, mx = rel_errors(yc, ref)
+    assert l1 <= PR_REL_L1 and mx <= PR_MAX_REL, (l1, mx)
 
 
 # ------------------------------------------------------------------ SpMV
