@@ -117,7 +117,7 @@ class Adj:
 def build_csr(n, pairs, undirected=False):
     """The CSR (out-lists) of build_adj alone: (ptr, col), without the CSC and
     the entry ids (for graphs of 10^8-10^9 entries)."""
-    pairs = np.ascontiguousarray(pairs, dtype=np.uint32)
+    pairs = np.ascontiguousarray(pairs, dtype=np.uint32).reshape(-1)
     m = len(pairs) // 2
     M = 2 * m if undirected else m
     ptr = np.empty(n + 1, dtype=np.uint32)

@@ -173,7 +173,7 @@ def test_rmat24_pagerank_headline(ctx):
     pairs = oracle.rmat_edges(scale, 16 * n, 1)
     out_deg, _ = oracle.degrees(n, pairs)
     # in-lists: the CSR of the reversed edges (list order does not matter in FP64)
-    iptr, icol = oracle.build_csr(n, np.ascontiguousarray(pairs.reshape(-1, 2)[:, ::-1]))
+    iptr, icol = oracle.build_csr(n, np.ascontiguousarray(pairs.reshape(-1, 2)[:, ::-1]).reshape(-1))
     del pairs
     ref = oracle.pagerank_f64(_Csc(n, iptr, icol), out_deg, 1.0 / n, 10)
     g = ctx.rmat(scale, 16 * n, 1).build(eg.CSR | eg.CSC)

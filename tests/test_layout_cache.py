@@ -29,10 +29,11 @@ def test_cache_round_trip_adjacency_and_grid(ctx, tmp_path):
     z = np.load(os.path.join(GOLDEN, "rmat12.npz"))
     n, pairs = int(z["n"]), z["pairs"]
     path = str(tmp_path / "g.eglayout")
-    g = ctx.from_pairs(n, pairs, undirected=True).build(eg.CSR | eg.CSC).build_grid(17)
+    # the grid is built from directed input (its load modes take no -u)
+    g = ctx.from_pairs(n, pairs).build(eg.CSR | eg.CSC).build_grid(17)
     g.save_layouts(path)
     assert os.path.exists(path) and not os.path.exists(path + ".tmp")
-    h = ctx.from_pairs(n, pairs, undirected=True)
+    h = ctx.from_pairs(n, pairs)
     assert h.load_layouts(path)
     info = h.info()
     assert info.layouts & (eg.CSR | eg.CSC | eg.GRID) == eg.CSR | eg.CSC | eg.GRID and info.grid_p == 17
@@ -49,9 +50,9 @@ def test_cache_round_trip_adjacency_and_grid(ctx, tmp_path):
     # another input of the same size is a miss (the digest differs)
     other = pairs.copy()
     other[5] = (other[5] + 1) % n
-    assert not ctx.from_pairs(n, other, undirected=True).load_layouts(path)
-    assert not ctx.from_pairs(n, pairs, undirected=False).load_layouts(path)  # other flags
-    assert not ctx.from_pairs(n, pairs, undirected=True).load_layouts(str(tmp_path / "absent"))
+    assert not ctx.from_pairs(n, other).load_layouts(path)
+    assert not ctx.from_pairs(n, pairs, undirected=True).load_layouts(path)  # other flags
+    assert not ctx.from_pairs(n, pairs).load_layouts(str(tmp_path / "absent"))
     # a truncated file that matches the header is an error, not a miss
     with open(path, "rb") as f:
         head = f.read(os.path.getsize(path) // 2)
@@ -59,8 +60,18 @@ def test_cache_round_trip_adjacency_and_grid(ctx, tmp_path):
     with open(cut, "wb") as f:
         f.write(head)
     with pytest.raises(eg.EGError) as e:
-        ctx.from_pairs(n, pairs, undirected=True).load_layouts(cut)
+        ctx.from_pairs(n, pairs).load_layouts(cut)
     assert e.value.code == -4
+    g.free()
+    h.free()
+    # undirected adjacency
+    g = ctx.from_pairs(n, pairs, undirected=True).build(eg.CSR)
+    g.save_layouts(path)
+    h = ctx.from_pairs(n, pairs, undirected=True)
+    assert h.load_layouts(path)
+    for a, b in zip(g.adj(eg.CSR), h.adj(eg.CSR)):
+        np.testing.assert_array_equal(a, b)
+    np.testing.assert_array_equal(g.wcc()[0], h.wcc()[0])
     g.free()
     h.free()
 
