@@ -608,6 +608,33 @@ def ppr_report(ctx, eg, scale=24, nq=32, seed=7):
             "single_iters": r4(its / 8), "speedup": r4(per_single * nq / stb.ms)}
 
 
+def cache_report(ctx, eg, scale=24, path=None):
+    """The layout cache on the undirected RMAT graph: device build (CSR +
+    CSC) against writing the layouts to a file and filling a fresh graph
+    from it."""
+    import tempfile
+    n = 1 << scale
+    g = ctx.rmat(scale, 16 * n, 2, undirected=True).build(eg.CSR | eg.CSC)
+    build_ms = g.info().build_ms
+    d = tempfile.mkdtemp()
+    path = path or os.path.join(d, "g.eglayout")
+    t0 = time.perf_counter()
+    g.save_layouts(path)
+    save_s = time.perf_counter() - t0
+    size = os.path.getsize(path)
+    h = ctx.rmat(scale, 16 * n, 2, undirected=True)
+    t0 = time.perf_counter()
+    hit = h.load_layouts(path)
+    load_s = time.perf_counter() - t0
+    same = bool(np.array_equal(g.adj(eg.CSR)[1], h.adj(eg.CSR)[1]))
+    g.free()
+    h.free()
+    os.remove(path)
+    os.rmdir(d)
+    return {"build_ms": r4(build_ms), "file_gb": r4(size / 1e9), "save_s": r4(save_s), "load_s": r4(load_s),
+            "hit": hit, "same_csr": same}
+
+
 def bfs_report(ctx, eg, scale=24, roots=16):
     """Single-source BFS (levels + parents) on the undirected RMAT graph: the
     CUDA-graph level loop and the host-driven loop (the same kernels launched
@@ -657,6 +684,8 @@ def only_report(name, args):
         out = ppr_report(ctx, eg, scale)
     elif name == "bfs":
         out = bfs_report(ctx, eg, scale)
+    elif name == "cache":
+        out = cache_report(ctx, eg, scale)
     else:  # msbfs
         n = 1 << scale
         g = ctx.rmat(scale, 16 * n, 2, undirected=True).build(eg.CSR | eg.CSC)
@@ -679,7 +708,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--pr-only", action="store_true", help="only the PageRank pull report (profiling)")
     ap.add_argument("--serve-only", action="store_true", help="only the serving report")
-    ap.add_argument("--only", choices=["pr", "spmv", "sssp", "msbfs", "ppr", "bfs", "serve"],
+    ap.add_argument("--only", choices=["pr", "spmv", "sssp", "msbfs", "ppr", "bfs", "serve", "cache"],
                     help="only one kernel report (profiling)")
     ap.add_argument("--rate", type=float, default=20000.0, help="offered rate when --rates is empty")
     ap.add_argument("--rates", default="250,1000,5000,50000",

@@ -748,45 +748,6 @@ __device__ __forceinline__ void eg_coov_tile(uint32_t t, const uint32_t *__restr
     }
 }
 
-// Persistent form with a shared-memory hot set: one CTA of 1024 threads per
-// SM stages hot[0 .. nhot) (the gathered vector's first nhot words) in
-// shared memory once, then its 32 warps walk tiles blockIdx.x * 32 + warp,
-// + gridDim.x * 32, ...  A gather of source u < nhot reads shared memory,
-// the others read through L1/L2 as in k_coov_rows.  With vertices numbered
-// by descending out-degree (PageRank's relabelled CSC) the first ~56K
-// sources carry about half of an RMAT graph's entries, so half of the
-// scattered L1 requests become shared-memory reads.  The tiles, carries and
-// per-tile order are those of k_coov_rows (same sums, bit for bit).
-template <class Op, int TILE_E, int U, bool REDUCE, int PF = 0, int HINT = 0, bool MK = false>
-__global__ void __launch_bounds__(1024, 1) k_coov_rows_hot(const uint32_t *__restrict__ rid,
-                                                           const uint32_t *__restrict__ col, uint32_t m,
-                                                           uint32_t ntiles,
-                                                           eg_mp_carry<typename Op::A> *__restrict__ carry,
-                                                           double2 *__restrict__ part, Op op,
-                                                           const uint32_t *__restrict__ starts,
-                                                           const uint32_t *__restrict__ trow,
-                                                           const float *__restrict__ hot, uint32_t nhot) {
-    static_assert(U == 4 || U == 8, "4 or 8 entries per lane");
-    static_assert(TILE_E % (32 * U) == 0, "tiles hold whole chunks");
-    static_assert(!MK || TILE_E % EG_TROW_SPAN == 0, "tiles start at a row sample");
-    extern __shared__ __align__(16) float s_hot[];
-    __shared__ double2 s_red[32];
-    if (!op.active()) return;
-    op.setup();
-    // nhot is a multiple of 4 and hot 16-byte aligned
-    for (uint32_t i = threadIdx.x; i < nhot / 4; i += blockDim.x)
-        reinterpret_cast<float4 *>(s_hot)[i] = __ldg(reinterpret_cast<const float4 *>(hot) + i);
-    __syncthreads();
-    const uint32_t warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    const uint64_t pol = HINT ? eg_l2_evict_first_policy() : 0;
-    eg_red2 redf;
-    for (uint32_t t = blockIdx.x * nw + warp; t < ntiles; t += gridDim.x * nw)
-        eg_coov_tile<Op, TILE_E, U, REDUCE, PF, HINT, MK>(
-            t, rid, col, starts, trow, m, carry, op, redf,
-            [&](uint32_t e, uint32_t u) { return u < nhot ? s_hot[u] : op.gather(e, u); }, pol);
-    if (REDUCE) eg_coov_reduce(redf, s_red, nw, part);
-}
-
 // U entries per lane (U = 4 or 8): lane l of a warp holds entries
 // base+U*l .. base+U*l+U-1 (128-bit loads of rid and col), sums the runs of
 // equal rows among them locally, and one segmented scan per 32*U entries

@@ -27,8 +27,6 @@
 #include <stdlib.h>
 #include <string.h>
 
-#include <type_traits>
-
 #include "eg_mp.cuh"
 
 // ============================================================== merge-path schedule (eg_noalloc.cu)
@@ -89,7 +87,6 @@ struct PrOp {
     float base;
     PprSeeds seeds;
     const float *__restrict__ acc_in;  // source blocks: the earlier blocks' row sums (else NULL)
-    __host__ __device__ const float *hot_src() const { return cin; }  // the gathered vector (hot-set form)
     __device__ __forceinline__ bool active() const { return st->done == 0; }
     __device__ __forceinline__ void setup() { base = st->base; }
     __device__ __forceinline__ V gather(uint32_t, uint32_t u) const { return __ldg(cin + u); }
@@ -264,39 +261,23 @@ __global__ void k_pr_reduce(const double2 *__restrict__ part, uint32_t nparts, e
 #define EG_SB_LOG2 24  // source-block size by default: 2^24 vertices, a 64 MB slice of x
 #define EG_PR_CHECK 4  // iterations between reads of the stop flag
 #define EG_PR_RES_BLOCKS 1024
-#define EG_ROW_CFGS 14
+#define EG_ROW_CFGS 12
 struct RowCfg {
     int tile, u, pf, minb, hint;
 };
 // pf: 0 no prefetch, 1 next chunk's words loaded ahead, 2 also its gathers
 // issued before the current chunk's scan.  min_blocks bounds the registers:
 // 6 resident CTAs of 256 threads leave 42 registers per thread, 5 leave 51,
-// 4 leave 64, 8 leave 32; min_blocks 1: the persistent form with the hot
-// set in shared memory (k_coov_rows_hot, one CTA of 1024 threads per SM,
-// 64 registers), for ops that gather one float per source.
+// 4 leave 64, 8 leave 32.
 static const RowCfg kRowCfg[EG_ROW_CFGS] = {
     {1024, 4, 1, 5, 0}, {2048, 4, 0, 6, 0}, {2048, 4, 1, 5, 0}, {1024, 4, 1, 6, 0}, {512, 4, 1, 5, 0},
     {1024, 8, 1, 4, 0}, {1024, 4, 0, 8, 0}, {2048, 8, 0, 5, 0}, {1024, 4, 1, 5, 1}, {2048, 4, 1, 5, 1},
-    {1024, 4, 2, 4, 0}, {2048, 4, 2, 4, 0}, {2048, 4, 1, 1, 1}, {1024, 4, 1, 1, 1}};
-// shared memory of the hot set: 224 KiB of the 227 KiB a CTA may hold
-#define EG_HOT_WORDS (56u * 1024u)
-
-// Ops whose gather is one float per source, hot_src() giving the gathered
-// vector, can run the persistent hot-set form (MINB 1).
-template <class Op, class = void>
-struct HasHot : std::false_type {};
-template <class Op>
-struct HasHot<Op, std::void_t<decltype(std::declval<const Op &>().hot_src())>> : std::true_type {};
+    {1024, 4, 2, 4, 0}, {2048, 4, 2, 4, 0}};
 
 template <class Op, int TILE, int U, bool REDUCE, int PF, int MINB, int HINT = 0, bool MK = false>
 static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part, const Op &op, uint32_t *nparts,
                         cudaEvent_t ev_begin, cudaEvent_t ev_end, uint64_t m_entries, bool empty_rows,
                         uint32_t empty_from) {
-    if constexpr (MINB == 1 && !HasHot<Op>::value) {
-        // no hot-set form for this op: the default schedule
-        return coo_launch_t<Op, 1024, 4, REDUCE, 1, 5, 0, MK>(g, adj, carry_buf, part, op, nparts, ev_begin, ev_end,
-                                                              m_entries, empty_rows, empty_from);
-    }
     static_assert(!MK || TILE % EG_TROW_SPAN == 0, "masked tiles start at a row sample");
     eg_ctx *ctx = g->ctx;
     using A = typename Op::A;
@@ -311,33 +292,13 @@ static int coo_launch_t(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *pa
     const uint32_t empty_n = ranged ? g->n - empty_from : g->n;
     uint32_t g2 = empty_rows ? eg_div_up(empty_n, 256) : 0;
     if (g2 > (uint32_t)ctx->sm_count * 8) g2 = (uint32_t)ctx->sm_count * 8;
-    uint32_t g1_parts = g1;
+    const uint32_t g1_parts = g1;
     if (g1) {
         if (ev_begin) EG_CUDA(cudaEventRecord(ev_begin, ctx->stream));
         // MK: the relabelled CSC's row-start bits stand in for its row ids
-        if constexpr (MINB == 1 && HasHot<Op>::value) {
-            const uint32_t nhot = (g->n < EG_HOT_WORDS ? g->n : EG_HOT_WORDS) & ~3u;
-            const uint32_t smem = nhot * 4;
-            auto kern = k_coov_rows_hot<Op, TILE, U, REDUCE, PF, HINT, MK>;
-            static bool attr_set = false;  // once per instantiation, before any capture uses it
-            if (!attr_set) {
-                EG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)(EG_HOT_WORDS * 4)));
-                attr_set = true;
-            }
-            uint32_t blocks = (uint32_t)ctx->sm_count;
-            const uint32_t need = eg_div_up(ntiles, 32);
-            if (blocks > need) blocks = need;
-            kern<<<blocks, 1024, smem, ctx->stream>>>(
-                bp<uint32_t>(adj.rid), bp<uint32_t>(adj.col), m, ntiles, bp<eg_mp_carry<A>>(carry_buf), part, op,
-                MK ? bp<uint32_t>(g->csc_p_starts) : nullptr, MK ? bp<uint32_t>(g->csc_p_trow) : nullptr,
-                op.hot_src(), nhot);
-            g1_parts = blocks;
-        } else {
-            k_coov_rows<Op, TILE, U, REDUCE, PF, MINB, HINT, MK><<<g1, 256, 0, ctx->stream>>>(
-                bp<uint32_t>(adj.rid), bp<uint32_t>(adj.col), m, ntiles, bp<eg_mp_carry<A>>(carry_buf), part, op,
-                MK ? bp<uint32_t>(g->csc_p_starts) : nullptr, MK ? bp<uint32_t>(g->csc_p_trow) : nullptr);
-        }
+        k_coov_rows<Op, TILE, U, REDUCE, PF, MINB, HINT, MK><<<g1, 256, 0, ctx->stream>>>(
+            bp<uint32_t>(adj.rid), bp<uint32_t>(adj.col), m, ntiles, bp<eg_mp_carry<A>>(carry_buf), part, op,
+            MK ? bp<uint32_t>(g->csc_p_starts) : nullptr, MK ? bp<uint32_t>(g->csc_p_trow) : nullptr);
         EG_LAUNCHED(ctx);
         if (ev_end) EG_CUDA(cudaEventRecord(ev_end, ctx->stream));
     }
@@ -383,8 +344,6 @@ static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part
         EG_ROW_CASE(9, 2048, 4, true, 5, 1)
         EG_ROW_CASE(10, 1024, 4, 2, 4, 0)
         EG_ROW_CASE(11, 2048, 4, 2, 4, 0)
-        EG_ROW_CASE(12, 2048, 4, 1, 1, 1)
-        EG_ROW_CASE(13, 1024, 4, 1, 1, 1)
         default:
             return coo_launch_t<Op, 1024, 4, REDUCE, true, 5, 0, MK>(g, adj, carry_buf, part, op, nparts, ev_begin,
                                                                      ev_end, m_entries, empty_rows, empty_from);

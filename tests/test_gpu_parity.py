@@ -167,9 +167,9 @@ def test_row_schedules_and_autotuner(case):
     vals = oracle.hash_values(adj.in_col, adj.in_dst(), 9)
     y_ref = oracle.spmv_f64(n, adj.in_ptr, adj.in_col, vals, x)
     cands, chosen = g.tune()
-    assert len(cands) == 14 and 0 <= chosen < 14
+    assert len(cands) == 12 and 0 <= chosen < 12
     assert g.bfs_tuning["switch_divisor"] in (20.0, 40.0, 80.0, 160.0, 320.0)
-    assert sum(c["cache_hint"] for c in cands) == 4
+    assert sum(c["cache_hint"] for c in cands) == 2
     if n > 1000:
         assert all(c["ms"] > 0 for c in cands)
     assert cands[chosen]["ms"] == min(c["ms"] for c in cands)
@@ -181,20 +181,6 @@ def test_row_schedules_and_autotuner(case):
         y, _ = g.spmv(x, "f32_comp", value_seed=9)
         l1, mx = rel_errors(y, y_ref)
         assert l1 <= PR_REL_L1, (cands[idx], l1)
-    # the persistent hot-set schedules (min_blocks 1) walk the same tiles in
-    # the same order as their per-tile twins: the same bits
-    hot = [i for i, c in enumerate(cands) if c["min_blocks"] == 1]
-    assert len(hot) == 2
-    for i in hot:
-        twin = [j for j, c in enumerate(cands) if c["min_blocks"] != 1 and c["cache_hint"] == 1
-                and (c["tile"], c["per_lane"], c["prefetch"]) == (cands[i]["tile"], cands[i]["per_lane"],
-                                                                  cands[i]["prefetch"])]
-        assert len(twin) == 1
-        g.set_row_schedule(i)
-        a, _ = g.pagerank(iterations=10, dangling=True)
-        g.set_row_schedule(twin[0])
-        b, _ = g.pagerank(iterations=10, dangling=True)
-        np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
     with pytest.raises(RuntimeError):
         g.set_row_schedule(len(cands))
     g.set_row_schedule(0)
