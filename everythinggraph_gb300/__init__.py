@@ -330,7 +330,7 @@ class Graph:
             level_out=None, parent_out=None):
         """host_loop: None = the form eg_graph_tune kept (else the CUDA graph),
         False = CUDA-graph level loop, True = host-driven level loop.
-        switch_divisor: None = the divisor eg_graph_tune kept (else 20, the
+        switch_divisor: None = the divisor eg_graph_tune kept (else 40, the
         reference's).
         level_out / parent_out: int32 arrays of n elements to fill (e.g. from
         pinned_empty) instead of new ones."""

@@ -180,7 +180,7 @@ struct eg_graph {
     eg_bfs_graph ppg;      // batched personalised PageRank sweep loop
     int row_cfg = 0;       // row-kernel schedule (entries per warp tile, per lane)
     int bfs_host_loop = 0; // BFS level-loop form eg_bfs uses by default (eg_graph_tune)
-    double bfs_divisor = 20.0;  // push/pull switch divisor eg_bfs uses by default (eg_graph_tune)
+    double bfs_divisor = 40.0;  // push/pull switch divisor eg_bfs uses by default (the reference's rule; eg_graph_tune)
     // SSSP edge weights of the CSR entries for one rule, materialised on first
     // use (the reference stores them in its edge records, init_all.c:661-686)
     eg_buf wts;

@@ -265,10 +265,12 @@ int eg_spmv(eg_graph *g, const eg_spmv_opts *opts, const void *x, void *y, float
 typedef struct {
     int direction;
     /* auto switches to pull when frontier size + frontier out-degree
-     * > m / switch_divisor (the reference uses 20, bfs_simple.c:191-197).
+     * > m / switch_divisor.  The reference's rule (bfs_simple.c:191-197)
+     * counts 2 * deg + 1 per frontier vertex against m / 20
+     * (nb_cleaning, buffer.c:272-282), which is divisor 40 here.
      * The direction changes how a level is computed, never its levels.
      * < 0 (default): the graph's divisor, which eg_graph_tune picks by
-     * timing (20 until then) */
+     * timing (40 until then) */
     double switch_divisor;
     /* 1: compute parents on the device even when parent_out is NULL (read
      * them later through eg_graph_device_ptr(g, EG_DEV_PARENT)) */

@@ -657,8 +657,11 @@ int or_bfs_tree_check(uint32_t n, const uint32_t *ptr, const uint32_t *col, uint
  * frontier's out-lists with a CAS on the next-frontier flag (bfs_push,
  * 121-134), pull steps over unvisited vertices that stop at the first
  * in-neighbour in the frontier (bfs_pull, 104-120), and the switch rule
- * "pull iff items + frontier degree > m/20" (191-197).  Frontiers are byte
- * maps as in random.c:74-77.  Writes levels (root = 1). */
+ * "pull iff items + degree_in_frontier > m/20" (191-197), where
+ * degree_in_frontier is the work queue's nb_cleaning, 2 * deg + 1 per
+ * frontier vertex (thread_add_task, buffer.c:272-282): pull iff
+ * 2 * (items + frontier out-degree) > m/20.  Frontiers are byte maps as in
+ * random.c:74-77.  Writes levels (root = 1). */
 int or_bfs_do(uint32_t n, const uint32_t *out_ptr, const uint32_t *out_col, const uint32_t *in_ptr,
               const uint32_t *in_col, uint32_t root, int32_t *level) {
     if (root >= n) return -1;
@@ -674,7 +677,7 @@ int or_bfs_do(uint32_t n, const uint32_t *out_ptr, const uint32_t *out_col, cons
     int pull = 0, have_q = 1;
     int32_t lvl = 1;
     while (items) {
-        pull = (double)items + (double)fdeg > (double)m / 20.0;
+        pull = 2.0 * ((double)items + (double)fdeg) > (double)m / 20.0;
         uint64_t cnt = 0, deg = 0, qn2 = 0;
         if (!pull) {
             if (!have_q) {
