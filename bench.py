@@ -32,6 +32,8 @@ METRIC, UNIT = "GTEPS", "GTEPS"
 # ncu capture of PageRank on directed RMAT-22 (the kernel's traffic grows with
 # the entries).
 PR_ROWS_DRAM_BYTES_PER_ENTRY = (294.009e6 + 3.622e6) / 67108864
+# the same for the partition kernel (k_pcol_rows); None until captured
+PR_PCOL_DRAM_BYTES_PER_ENTRY = None
 
 
 def peaks():
@@ -234,9 +236,12 @@ def run_ours(args):
     roof = None
     if dom and "row_ms" in dom:
         gbps = dom["bytes"] / (dom["row_ms"] / 1e3) / 1e9
+        pcol = dom["sched"].startswith("partitions")
+        per_entry = PR_PCOL_DRAM_BYTES_PER_ENTRY if pcol else PR_ROWS_DRAM_BYTES_PER_ENTRY
+        kname = "k_pcol_rows<PrOp<0>,14>" if pcol else "k_coov_rows<PrOp<0>,%s>" % dom["sched"]
         roof = {"bound": "hbm", "achieved": r4(gbps), "peak": hbm, "unit": "GB/s", "frac": r4(gbps / hbm),
-                "traffic": r4(PR_ROWS_DRAM_BYTES_PER_ENTRY * dom["m"]),
-                "kernel": "k_coov_rows<PrOp<0>,%s> (PageRank pull, RMAT-%d directed)" % (dom["sched"], scale),
+                "traffic": r4(per_entry * dom["m"]) if per_entry else None,
+                "kernel": "%s (PageRank pull, RMAT-%d directed)" % (kname, scale),
                 "algorithmic_bytes": dom["bytes"], "peak_source": src}
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -308,8 +313,9 @@ def kernel_reports(ctx, eg, scale, args):
     rec = {"ms_iter": r4(it_ms), "ms_iter_graph": r4(stg.ms / 10), "row_ms": r4(st.row_kernel_ms),
            "row_gbps": r4(bytes_it / (st.row_kernel_ms / 1e3) / 1e9), "gteps": r4(m / (it_ms / 1e3) / 1e9),
            "bytes": bytes_it, "m": m,
-           "sched": "%d,%d pf%d mb%d ch%d" % (c["tile"], c["per_lane"], c["prefetch"], c["min_blocks"],
-                                             c["cache_hint"]),
+           "sched": ("partitions 2^%d, %d-entry chunks" % (c["partition_log2"], c["tile"]) if c["partition_log2"]
+                     else "%d,%d pf%d mb%d ch%d" % (c["tile"], c["per_lane"], c["prefetch"], c["min_blocks"],
+                                                    c["cache_hint"])),
            "cand_ms": [round(x["ms"], 3) for x in cands]}
     try:
         oracle.build()

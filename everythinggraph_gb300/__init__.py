@@ -284,7 +284,7 @@ class Graph:
         L.check(lib().eg_graph_tune(self._h, ctypes.byref(r)))
         cands = [{"tile": r.tile_entries[i], "per_lane": r.entries_per_lane[i], "prefetch": r.prefetch[i],
                   "min_blocks": r.min_blocks[i], "cache_hint": r.cache_hint[i],
-                  "ms": r.ms[i]} for i in range(r.ncand)]
+                  "partition_log2": r.partition_log2[i], "ms": r.ms[i]} for i in range(r.ncand)]
         self.bfs_tuning = {"graph_ms": r.bfs_graph_ms, "host_ms": r.bfs_host_ms, "host_loop": r.bfs_host_loop,
                            "switch_divisor": r.bfs_switch_divisor}
         return cands, r.chosen

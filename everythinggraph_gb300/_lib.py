@@ -50,7 +50,8 @@ class ServeStats(ctypes.Structure):
 
 class TuneResult(ctypes.Structure):
     _fields_ = [("ncand", c_int), ("chosen", c_int), ("tile_entries", c_int * 16), ("entries_per_lane", c_int * 16),
-                ("prefetch", c_int * 16), ("min_blocks", c_int * 16), ("cache_hint", c_int * 16), ("ms", c_f32 * 16), ("bfs_graph_ms", c_f32),
+                ("prefetch", c_int * 16), ("min_blocks", c_int * 16), ("cache_hint", c_int * 16), ("ms", c_f32 * 16),
+                ("partition_log2", c_int * 16), ("bfs_graph_ms", c_f32),
                 ("bfs_host_ms", c_f32), ("bfs_host_loop", c_int), ("bfs_switch_divisor", c_f64)]
 
 

@@ -403,7 +403,9 @@ extern "C" void eg_graph_free(eg_graph *g) {
                       &g->label,        &g->spmv_x,      &g->spmv_y,      &g->spmv_vals,      &g->bfs_work,     &g->msbfs_work,
                       &g->sssp_work,    &g->ppr_work,    &g->wts,
                       &g->grid_order,   &g->grid_units,  &g->grid_off,    &g->grid_vals,   &g->grid_acc,
-                      &g->esrc,         &g->edst,        &g->edge_work};
+                      &g->esrc,         &g->edst,        &g->edge_work,
+                      &g->pcol.dst,     &g->pcol.flags,  &g->pcol.crun,   &g->pcol.rsrc,   &g->pcol.seg,
+                      &g->pcol.acc,     &g->pcol.ticket};
     for (eg_buf *b : bufs) eg_buf_free(c, *b);
     for (eg_bfs_graph &bg : g->bfsg) {
         if (bg.exec) cudaGraphExecDestroy(bg.exec);
@@ -996,6 +998,7 @@ int eg_build_relabeled_csc(eg_graph *g) {
     if (g->relabeled) return EG_OK;
     if (!(g->built & EG_LAYOUT_CSC) || !(g->built & EG_LAYOUT_CSR))
         return eg_fail(EG_ENOTBUILT, "relabelled CSC needs the CSC and the out-degrees");
+    g->pcol.shift = 0;  // the partition layout is made from this copy
     eg_ctx *ctx = g->ctx;
     const uint32_t n = g->n;
     const uint64_t M = g->m;

@@ -121,6 +121,27 @@ struct eg_sblocks {
     uint64_t vals_seed = 0;
 };
 
+// PageRank's destination-partition layout of the relabelled CSC (eg_pcol.cu):
+// the rows with entries are cut into partitions of 2^shift rows; inside a
+// partition the entries are ordered by source (then row), so each source's
+// entries into the partition form one run whose contribution is gathered
+// once.  Partitions start at chunk boundaries (EG_PC_CHUNK entries); the
+// entries past a partition's last (up to the next chunk) are padding that
+// adds into row 2^shift, a slot outside the partition.
+#define EG_PC_CHUNK 256
+struct eg_pcols {
+    uint32_t shift = 0;  // 0: not built
+    uint32_t parts = 0, segs = 0;
+    uint64_t chunks = 0, runs = 0;
+    eg_buf dst;     // uint16[chunks * EG_PC_CHUNK]: the entry's row within its partition
+    eg_buf flags;   // uint32[chunks * EG_PC_CHUNK / 32]: bit set where a run begins (at every chunk's first entry too)
+    eg_buf crun;    // uint32[chunks]: run of each chunk's first entry
+    eg_buf rsrc;    // uint32[runs]: source of each run
+    eg_buf seg;     // uint4[segs] (first chunk, end chunk, partition, segments of that partition), longest first
+    eg_buf acc;     // uint64[rows with entries]: sums of the partitions split over several segments
+    eg_buf ticket;  // uint32[parts + 2]: segments finished per partition; [parts]: the next segment to take; [parts + 1]: CTAs done
+};
+
 struct eg_graph {
     eg_ctx *ctx;
     uint32_t n;
@@ -169,6 +190,8 @@ struct eg_graph {
     int spmv_vals_kind;
     eg_sblocks sb;   // source-blocked copy of the CSC (fp32 SpMV over an x larger than L2)
     eg_sblocks sbp;  // the same of the relabelled CSC (PageRank)
+    eg_pcols pcol;   // the relabelled CSC by destination partition and source (PageRank)
+    int pr_kernel = 0;  // PageRank's one-pass kernel: 0 the row kernel (row_cfg), 1 the partition kernel
     eg_buf bfs_work;  // bitmaps, queues, counters
     eg_buf msbfs_work;
     eg_buf sssp_work;
@@ -202,6 +225,8 @@ int eg_radix_sort(eg_ctx *ctx, uint32_t *k_in, uint32_t *v_in, uint32_t *k_tmp, 
                   int bits, uint32_t **k_out, uint32_t **v_out);
 // builds g->csc_p / perm / deg_p from the CSC and out-degrees (once)
 int eg_build_relabeled_csc(eg_graph *g);
+// builds g->pcol with partitions of 2^shift rows from g->csc_p (once per shift)
+int eg_build_pcols(eg_graph *g, uint32_t shift);
 
 // ---------------------------------------------------------------- device utils
 #ifdef __CUDACC__

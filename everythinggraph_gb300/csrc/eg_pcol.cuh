@@ -1,0 +1,190 @@
+// Row sums over the destination-partition layout (eg_pcols, built by
+// eg_pcol.cu): PageRank's pull iteration with the contribution of each
+// source gathered once per partition instead of once per entry.
+//
+// The row kernel (eg_mp.cuh) walks the CSC in row order, so consecutive
+// entries name unrelated sources and nearly every entry gathers its own
+// 32-byte sector (0.98 sectors per entry on directed RMAT-24 before L1).
+// Here a partition's entries are ordered by source: all entries of source
+// u into the partition form one run, whose contribution is loaded once and
+// added into the rows of the run's entries, and consecutive runs are
+// ascending sources, so the loads of a warp share sectors (0.15 sectors per
+// entry for partitions of 16K rows).  The streamed words are 2 bytes per
+// entry (the row within the partition) plus a run-start bit, and 4 bytes per
+// run (its source).
+//
+// A CTA owns one segment of a partition's chunks at a time (persistent CTAs
+// take segments from a queue, longest first) and sums into the partition's
+// rows held in shared memory.  Sums are kept as unsigned 64-bit fixed point
+// (unit 2^-(62 - E), with 2^(E-1) above the rank mass, which bounds every
+// row sum; a contribution c becomes round(c / unit), an error of at most
+// half a unit per term): integer adds give the same bits in any order, so
+// the result does not depend on which warp or CTA added first.  A partition covered by one
+// segment is finished from shared memory; the segments of a longer partition
+// add their sums into a global accumulator, and the last to finish (a ticket
+// per partition) finishes the rows and clears the accumulator.
+#pragma once
+#include "eg_mp.cuh"
+
+#define EG_PC_THREADS 1024
+#define EG_PC_WARPS (EG_PC_THREADS / 32)
+
+// Shared memory of k_pcol_rows with partitions of 2^SHIFT rows: the row
+// sums as 64-bit fixed point (one slot more for the padding entries), the
+// low 32-bit words of every row, then the high words, and each warp's run
+// values (64-bit) for the chunk in hand.  A term is added to the low word
+// with a 32-bit integer atomic; when that add wraps, the high word gets one
+// more with the term's high half: every sum is exact, so its bits do not
+// depend on the order of the adds (and 32-bit integer adds are the shared
+// memory atomics that the hardware carries out natively).
+template <int SHIFT>
+struct eg_pc_smem {
+    static constexpr size_t word_bytes = (((size_t)(1u << SHIFT) + 1) * 4 + 15) & ~(size_t)15;
+    static constexpr size_t acc_bytes = 2 * word_bytes;
+    static constexpr size_t bytes = acc_bytes + (size_t)EG_PC_WARPS * EG_PC_CHUNK * 8;
+};
+
+// A warp's chunk: the rows of entries lane, lane + 32, ..., lane + 224 (one
+// 16-byte word per lane: the layout stores each chunk transposed), the
+// chunk's 8 words of run-start bits (word j: entries 32j .. 32j + 31), the
+// chunk's first run.
+struct eg_pc_chunk {
+    uint4 d8;
+    uint4 f0, f1;
+    uint32_t rb;
+};
+__device__ __forceinline__ void eg_pc_load(const uint32_t *__restrict__ dst, const uint32_t *__restrict__ flags,
+                                           const uint32_t *__restrict__ crun, uint64_t c, uint32_t lane,
+                                           uint64_t pol, eg_pc_chunk &k) {
+    k.d8 = eg_stream_ld4<1>(dst + c * (EG_PC_CHUNK / 2) + 4 * lane, pol);
+    k.f0 = __ldg(reinterpret_cast<const uint4 *>(flags + c * (EG_PC_CHUNK / 32)));
+    k.f1 = __ldg(reinterpret_cast<const uint4 *>(flags + c * (EG_PC_CHUNK / 32) + 4));
+    k.rb = __ldg(crun + c);
+}
+
+template <class Op, int SHIFT, bool REDUCE>
+__global__ void __launch_bounds__(EG_PC_THREADS, 1)
+    k_pcol_rows(const uint4 *__restrict__ seg, uint32_t nseg, const uint32_t *__restrict__ dst,
+                const uint32_t *__restrict__ flags, const uint32_t *__restrict__ crun,
+                const uint32_t *__restrict__ rsrc, unsigned long long *__restrict__ gacc,
+                uint32_t *__restrict__ ticket, uint32_t parts, uint32_t rows, double2 *__restrict__ part, Op op,
+                float fx, float fx_inv) {
+    using T = unsigned long long;
+    constexpr uint32_t D = 1u << SHIFT;
+    extern __shared__ __align__(16) unsigned char eg_pc_sm[];
+    using SM = eg_pc_smem<SHIFT>;
+    uint32_t *slo = reinterpret_cast<uint32_t *>(eg_pc_sm);                    // low words
+    uint32_t *shi = reinterpret_cast<uint32_t *>(eg_pc_sm + SM::word_bytes);  // high words
+    auto row_sum = [&](uint32_t l) -> float { return __ull2float_rn(((T)shi[l] << 32) | (T)slo[l]) * fx_inv; };
+    __shared__ double2 s_red[32];
+    __shared__ uint32_t s_seg;
+    __shared__ int s_last;
+    if (!op.active()) return;
+    op.setup();
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    T *wv = reinterpret_cast<T *>(eg_pc_sm + SM::acc_bytes) + warp * EG_PC_CHUNK;
+    const uint64_t pol = eg_l2_evict_first_policy();
+    eg_red2 redf;
+    for (;;) {
+        if (tid == 0) s_seg = atomicAdd(ticket + parts, 1u);
+        __syncthreads();
+        const uint32_t si = s_seg;
+        if (si >= nseg) break;
+        const uint4 sg = seg[si];
+        const uint32_t c1 = sg.y, p = sg.z, nsp = sg.w;
+        for (uint32_t i = tid; i <= D; i += EG_PC_THREADS) {
+            slo[i] = 0u;
+            shi[i] = 0u;
+        }
+        __syncthreads();
+        uint64_t c = (uint64_t)sg.x + warp;
+        eg_pc_chunk k;
+        if (c < c1) eg_pc_load(dst, flags, crun, c, lane, pol, k);
+        while (c < c1) {
+            const uint64_t cn = c + EG_PC_WARPS;
+            eg_pc_chunk kn = k;
+            if (cn < c1) eg_pc_load(dst, flags, crun, cn, lane, pol, kn);
+            const uint32_t fw[8] = {k.f0.x, k.f0.y, k.f0.z, k.f0.w, k.f1.x, k.f1.y, k.f1.z, k.f1.w};
+            uint32_t nr = 0;
+#pragma unroll
+            for (int j = 0; j < 8; j++) nr += __popc(fw[j]);
+            // one contribution per run (consecutive runs: ascending sources)
+            for (uint32_t i = lane; i < nr; i += 64) {
+                const uint32_t i2 = i + 32;
+                const uint32_t u1 = __ldg(rsrc + k.rb + i);
+                const uint32_t u2 = i2 < nr ? __ldg(rsrc + k.rb + i2) : 0u;
+                const float v1 = op.gather(0u, u1);
+                const float v2 = i2 < nr ? op.gather(0u, u2) : 0.f;
+                wv[i] = __float2ull_rn(v1 * fx);
+                if (i2 < nr) wv[i2] = __float2ull_rn(v2 * fx);
+            }
+            __syncwarp();
+            // entry 32j + lane: its run is the last one that began at or
+            // before it (every chunk begins with a run)
+            const uint32_t h[4] = {k.d8.x, k.d8.y, k.d8.z, k.d8.w};
+            const uint32_t le = 0xffffffffu >> (31 - lane);
+            uint32_t base = 0;
+#pragma unroll
+            for (int j0 = 0; j0 < 8; j0 += 4) {
+                uint32_t rw[4], old[4];
+                T val[4];
+#pragma unroll
+                for (int jj = 0; jj < 4; jj++) {
+                    const int j = j0 + jj;
+                    const uint32_t q = base + __popc(fw[j] & le);
+                    base += __popc(fw[j]);
+                    rw[jj] = (j & 1) ? (h[j >> 1] >> 16) : (h[j >> 1] & 0xffffu);
+                    val[jj] = wv[q - 1];
+                    old[jj] = atomicAdd(slo + rw[jj], (uint32_t)val[jj]);
+                }
+#pragma unroll
+                for (int jj = 0; jj < 4; jj++) {
+                    const uint32_t lo = (uint32_t)val[jj];
+                    const uint32_t hv = (uint32_t)(val[jj] >> 32) + (old[jj] + lo < old[jj] ? 1u : 0u);
+                    if (hv) atomicAdd(shi + rw[jj], hv);
+                }
+            }
+            __syncwarp();
+            c = cn;
+            k = kn;
+        }
+        __syncthreads();
+        const uint32_t row0 = p << SHIFT;
+        const uint32_t nrows = rows - row0 < D ? rows - row0 : D;
+        if (nsp == 1) {
+            for (uint32_t l = tid; l < nrows; l += EG_PC_THREADS) {
+                const float2 d = op.emit(row0 + l, row_sum(l));
+                if (REDUCE) redf.add(d);
+            }
+        } else {
+            for (uint32_t l = tid; l < nrows; l += EG_PC_THREADS) {
+                const T a = ((T)shi[l] << 32) | (T)slo[l];
+                if (a) atomicAdd(gacc + row0 + l, a);
+            }
+            __threadfence();
+            __syncthreads();
+            if (tid == 0) s_last = atomicAdd(ticket + p, 1u) == nsp - 1;
+            __syncthreads();
+            if (s_last) {
+                __threadfence();
+                for (uint32_t l = tid; l < nrows; l += EG_PC_THREADS) {
+                    const T a = __ldcg(gacc + row0 + l);
+                    gacc[row0 + l] = 0ull;
+                    const float2 d = op.emit(row0 + l, __ull2float_rn(a) * fx_inv);
+                    if (REDUCE) redf.add(d);
+                }
+                if (tid == 0) ticket[p] = 0u;
+            }
+        }
+        __syncthreads();  // s_seg and the shared sums are reused by the next segment
+    }
+    // the last CTA to leave resets the segment queue for the next launch
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(ticket + parts + 1, 1u) == gridDim.x - 1) {
+            ticket[parts] = 0u;
+            ticket[parts + 1] = 0u;
+        }
+    }
+    eg_block_part<REDUCE>(redf, part, s_red);
+}

@@ -28,6 +28,7 @@
 #include <string.h>
 
 #include "eg_mp.cuh"
+#include "eg_pcol.cuh"
 
 // ============================================================== merge-path schedule (eg_noalloc.cu)
 __global__ void k_mp_schedule(const uint32_t *__restrict__ ptr, uint32_t n, uint32_t m, uint32_t items,
@@ -351,6 +352,57 @@ static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part
 #undef EG_ROW_CASE
 }
 
+// PageRank's one-pass iteration over the destination-partition layout
+// (k_pcol_rows, eg_pcol.cuh), then the rows without entries as in
+// coo_launch.  `mass` bounds the rank mass, and so every row sum: the
+// fixed-point unit is 2^-(62 - E) with 2 * mass < 2^E, so that sums stay
+// below 2^61 units.
+#define EG_PC_SHIFT 14  // 16K rows per partition: 128 KB of 64-bit sums in shared memory
+#define EG_PR_CANDS (EG_ROW_CFGS + 1)  // the tuner's candidates: the row schedules, then the partition kernel
+template <bool REDUCE>
+static int pcol_launch(eg_graph *g, const PrOp<false> &op, double2 *part, uint32_t *nparts, cudaEvent_t ev_begin,
+                       cudaEvent_t ev_end, bool empty_rows, double mass) {
+    eg_ctx *ctx = g->ctx;
+    eg_pcols &pc = g->pcol;
+    int E = 0;
+    frexp(2.0 * (mass > 1.0 ? mass : 1.0), &E);
+    const float fx = ldexpf(1.f, 62 - E), fx_inv = ldexpf(1.f, E - 62);
+    const size_t smem = eg_pc_smem<EG_PC_SHIFT>::bytes;  // allowed by pcol_prepare
+    auto kern = k_pcol_rows<PrOp<false>, EG_PC_SHIFT, REDUCE>;
+    const uint32_t g1 = pc.segs < (uint32_t)ctx->sm_count ? pc.segs : (uint32_t)ctx->sm_count;  // one CTA per SM
+    if (g1) {
+        if (ev_begin) EG_CUDA(cudaEventRecord(ev_begin, ctx->stream));
+        kern<<<g1, EG_PC_THREADS, smem, ctx->stream>>>(
+            bp<uint4>(pc.seg), pc.segs, bp<uint32_t>(pc.dst), bp<uint32_t>(pc.flags), bp<uint32_t>(pc.crun),
+            bp<uint32_t>(pc.rsrc), bp<unsigned long long>(pc.acc), bp<uint32_t>(pc.ticket), pc.parts, g->csc_p_rows,
+            part, op, fx, fx_inv);
+        EG_LAUNCHED(ctx);
+        if (ev_end) EG_CUDA(cudaEventRecord(ev_end, ctx->stream));
+    }
+    uint32_t g2 = 0;
+    if (empty_rows && g->csc_p_rows < g->n) {
+        g2 = eg_div_up(g->n - g->csc_p_rows, 256);
+        if (g2 > (uint32_t)ctx->sm_count * 8) g2 = (uint32_t)ctx->sm_count * 8;
+        k_coo_empty_range<PrOp<false>, REDUCE><<<g2, 256, 0, ctx->stream>>>(g->csc_p_rows, g->n,
+                                                                          part ? part + g1 : nullptr, op);
+        EG_LAUNCHED(ctx);
+    }
+    *nparts = g1 + g2;
+    return EG_OK;
+}
+
+// The partition layout, and the kernels' shared-memory allowance (set
+// outside any stream capture).
+static int pcol_prepare(eg_graph *g) {
+    EG_TRY(eg_build_pcols(g, EG_PC_SHIFT));
+    const int smem = (int)eg_pc_smem<EG_PC_SHIFT>::bytes;
+    EG_CUDA(cudaFuncSetAttribute(k_pcol_rows<PrOp<false>, EG_PC_SHIFT, false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    EG_CUDA(cudaFuncSetAttribute(k_pcol_rows<PrOp<false>, EG_PC_SHIFT, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    return EG_OK;
+}
+
 extern "C" void eg_pr_opts_default(eg_pr_opts *o) {
     if (!o) return;
     o->iterations = 10;
@@ -430,10 +482,22 @@ static int pr_iterations(eg_graph *g, const eg_pr_opts &o, const PprSeeds &ps, d
             // iteration, so once both rank buffers and the contribution
             // buffer(s) hold it (iterations 0 and 1) those rows stay written
             const bool fixed_base = !o.dangling && ps.count == 0;
-            EG_TRY((coo_launch<PrOp<COMP>, REDUCE, true>(g, g->csc_p, carry, part, op, &nparts,
-                                                          t ? ctx->evk[2 * it] : nullptr,
-                                                          t ? ctx->evk[2 * it + 1] : nullptr, EG_ALL_ENTRIES,
-                                                          !fixed_base || it < 2, g->csc_p_rows)));
+            bool done = false;
+            if constexpr (!COMP) {
+                if (g->pr_kernel == 1 && ps.count == 0 && g->pcol.shift == EG_PC_SHIFT) {
+                    // the rank mass bound: the start vector's, or 1 (an
+                    // iteration maps mass B to at most (1 - d) + d B)
+                    const double mass = o.prev_init < 0.f ? 1.0 : (double)o.prev_init * (double)g->n;
+                    EG_TRY(pcol_launch<REDUCE>(g, op, part, &nparts, t ? ctx->evk[2 * it] : nullptr,
+                                               t ? ctx->evk[2 * it + 1] : nullptr, !fixed_base || it < 2, mass));
+                    done = true;
+                }
+            }
+            if (!done)
+                EG_TRY((coo_launch<PrOp<COMP>, REDUCE, true>(g, g->csc_p, carry, part, op, &nparts,
+                                                              t ? ctx->evk[2 * it] : nullptr,
+                                                              t ? ctx->evk[2 * it + 1] : nullptr, EG_ALL_ENTRIES,
+                                                              !fixed_base || it < 2, g->csc_p_rows)));
         }
         if (o.tolerance > 0.0) {  // the L1 change, after the row kernels (coalesced, 8 bytes per vertex)
             k_pr_residual<<<EG_PR_RES_BLOCKS, 256, 0, ctx->stream>>>(rank_new, rank_old, g->n, st, part + nparts);
@@ -478,8 +542,10 @@ static int pr_graph(eg_graph *g, const eg_pr_opts &o, bool reduce, eg_pr_dev *st
     key[10] = (uint64_t)(uintptr_t)carry.p;
     key[11] = (uint64_t)(uintptr_t)g->csc_p.rid.p ^ ((uint64_t)(uintptr_t)g->csc_p_starts.p << 17);
     key[12] = (uint64_t)(uintptr_t)g->csc_p.col.p ^ ((uint64_t)(uintptr_t)g->csc_p_trow.p << 17);
-    key[13] = (uint64_t)(uintptr_t)g->csc_p.ptr.p;
-    key[14] = g->m ^ ((uint64_t)g->row_cfg << 56) ^ ((uint64_t)pr_block_log2(g, o) << 48);
+    key[13] = (uint64_t)(uintptr_t)g->csc_p.ptr.p ^ ((uint64_t)(uintptr_t)g->pcol.seg.p << 7) ^
+              ((uint64_t)(uintptr_t)g->pcol.rsrc.p << 13) ^ ((uint64_t)(uintptr_t)g->pcol.dst.p << 19);
+    key[14] = g->m ^ ((uint64_t)g->row_cfg << 56) ^ ((uint64_t)pr_block_log2(g, o) << 48) ^
+              ((uint64_t)g->pr_kernel << 44) ^ ((uint64_t)g->pcol.shift << 36);
     key[15] = (uint64_t)ctx->stream ^ 0x5052ull;
     if (g->prg.exec && !memcmp(key, g->prk, sizeof(key))) return EG_OK;
     if (g->prg.exec) cudaGraphExecDestroy(g->prg.exec);
@@ -602,6 +668,7 @@ static int pr_prepare(eg_graph *g, const eg_pr_opts *o = nullptr) {
         EG_TRY(sb_prepare(g, g->sbp, g->csc_p, kb));
         EG_TRY(eg_buf_ensure(g->ctx, g->pr_acc, (uint64_t)g->n * 4));
     }
+    if (g->pr_kernel == 1) EG_TRY(pcol_prepare(g));
     return EG_OK;
 }
 
@@ -634,8 +701,13 @@ extern "C" int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out,
 // ============================================================== autotuner
 extern "C" int eg_graph_set_row_schedule(eg_graph *g, int index) {
     if (!g) return eg_fail(EG_EINVAL, "NULL graph");
-    if (index < 0 || index >= EG_ROW_CFGS) return eg_fail(EG_EINVAL, "row schedule %d of %d", index, EG_ROW_CFGS);
-    g->row_cfg = index;
+    if (index < 0 || index >= EG_PR_CANDS) return eg_fail(EG_EINVAL, "row schedule %d of %d", index, EG_PR_CANDS);
+    if (index < EG_ROW_CFGS) {
+        g->row_cfg = index;
+        g->pr_kernel = 0;
+    } else {
+        g->pr_kernel = 1;  // PageRank's partition kernel; the row kernels keep their schedule
+    }
     return EG_OK;
 }
 
@@ -649,8 +721,9 @@ extern "C" int eg_graph_tune(eg_graph *g, eg_tune_result *out) {
     memset(&none, 0, sizeof(none));
     eg_tune_result r;
     memset(&r, 0, sizeof(r));
-    r.ncand = EG_ROW_CFGS;
+    r.ncand = EG_PR_CANDS;
     int best = 0;
+    g->pr_kernel = 0;
     for (int c = 0; c < EG_ROW_CFGS; c++) {
         g->row_cfg = c;
         eg_pr_stats st;
@@ -666,6 +739,26 @@ extern "C" int eg_graph_tune(eg_graph *g, eg_tune_result *out) {
     }
     g->row_cfg = best;
     r.chosen = best;
+    {  // the partition kernel (PageRank only; SpMV keeps the row schedule)
+        const int c = EG_ROW_CFGS;
+        EG_TRY(pcol_prepare(g));
+        g->pr_kernel = 1;
+        eg_pr_stats st;
+        EG_TRY(pr_run(g, o, none, 0, nullptr, &st));
+        EG_TRY(pr_run(g, o, none, 0, nullptr, &st));
+        r.tile_entries[c] = EG_PC_CHUNK;
+        r.entries_per_lane[c] = 8;
+        r.prefetch[c] = 1;
+        r.min_blocks[c] = 1;
+        r.cache_hint[c] = 1;
+        r.partition_log2[c] = EG_PC_SHIFT;
+        r.ms[c] = st.row_kernel_ms;
+        if (st.row_kernel_ms < r.ms[best]) {
+            r.chosen = c;
+        } else {
+            g->pr_kernel = 0;
+        }
+    }
     if (g->built & EG_LAYOUT_CSR)
         EG_TRY(eg_bfs_tune(g, &r.bfs_graph_ms, &r.bfs_host_ms, &r.bfs_host_loop, &r.bfs_switch_divisor));
     if (out) *out = r;

@@ -193,7 +193,13 @@ int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out, eg_pr_stat
  * picks one by index (0 = 1024 x 4 with prefetch, the default).  cache_hint
  * keeps the streamed row ids and columns out of L1 and first in line for L2
  * eviction.  Schedules change only how rows are split between warps, i.e.
- * the fp32 summation order. */
+ * the fp32 summation order.
+ * The last candidate (index 12) is PageRank's partition kernel: the
+ * relabelled CSC cut into partitions of 2^14 rows whose entries are ordered
+ * by source, so each source's contribution is gathered once per partition,
+ * with 64-bit fixed-point row sums in shared memory (the same bits in any
+ * order of addition).  It is kept for eg_pagerank only when it is the
+ * fastest; eg_ppr and eg_spmv keep the fastest row schedule. */
 #define EG_ROW_SCHEDULES_MAX 16
 typedef struct {
     int ncand;
@@ -204,6 +210,9 @@ typedef struct {
     int min_blocks[EG_ROW_SCHEDULES_MAX];
     int cache_hint[EG_ROW_SCHEDULES_MAX];
     float ms[EG_ROW_SCHEDULES_MAX]; /* mean row-kernel time per iteration */
+    /* 0: a row-kernel schedule; k > 0: PageRank's partition kernel over
+     * partitions of 2^k rows (the last candidate) */
+    int partition_log2[EG_ROW_SCHEDULES_MAX];
     /* BFS level loop (when the graph has a CSR): mean ms per BFS over 48
      * sampled roots for the CUDA-graph and the host-driven loop (each at its
      * best switch divisor of 20, 40, 80, 160, 320), and the form and the

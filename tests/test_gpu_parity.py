@@ -167,9 +167,10 @@ def test_row_schedules_and_autotuner(case):
     vals = oracle.hash_values(adj.in_col, adj.in_dst(), 9)
     y_ref = oracle.spmv_f64(n, adj.in_ptr, adj.in_col, vals, x)
     cands, chosen = g.tune()
-    assert len(cands) == 12 and 0 <= chosen < 12
+    assert len(cands) == 13 and 0 <= chosen < 13
     assert g.bfs_tuning["switch_divisor"] in (20.0, 40.0, 80.0, 160.0, 320.0)
-    assert sum(c["cache_hint"] for c in cands) == 2
+    assert sum(c["cache_hint"] for c in cands) == 3
+    assert [c["partition_log2"] for c in cands] == [0] * 12 + [14]
     if n > 1000:
         assert all(c["ms"] > 0 for c in cands)
     assert cands[chosen]["ms"] == min(c["ms"] for c in cands)
@@ -184,6 +185,40 @@ def test_row_schedules_and_autotuner(case):
     with pytest.raises(RuntimeError):
         g.set_row_schedule(len(cands))
     g.set_row_schedule(0)
+
+
+def test_pagerank_partition_kernel(case):
+    # schedule 12: the relabelled CSC by destination partition and source,
+    # 64-bit fixed-point row sums (the same bits in any order of addition)
+    name, n, pairs, rec, g, gu, adj, adju = case
+    g.set_row_schedule(12)
+    try:
+        for dangling in (False, True):
+            ref = oracle.pagerank_f64(adj, adj.out_deg(), 1.0 / n, 10, dangling=dangling)
+            got, st = g.pagerank(iterations=10, dangling=dangling)
+            l1, mx = rel_errors(got, ref)
+            assert l1 <= PR_REL_L1 and mx <= PR_MAX_REL, (dangling, l1, mx)
+            assert st.iterations_run == 10 and st.row_kernel_ms > 0
+            again, _ = g.pagerank(iterations=10, dangling=dangling)
+            np.testing.assert_array_equal(got, again)  # run to run
+            replay, _ = g.pagerank(iterations=10, dangling=dangling, use_graph=True)
+            np.testing.assert_array_equal(got, replay)  # captured loop
+        # the reference's own semantics: pull mode (prev stays 0.15, rank mass
+        # 0.15 n) and prgrid (degrees counted twice)
+        got, _ = g.pagerank(iterations=10, prev_init=0.15, swap=False)
+        _, mx = rel_errors(got, rec["pr_simple_pull"])
+        assert mx <= PR_VS_REF32_MAX_REL, mx
+        got, _ = g.pagerank(iterations=10, prev_init=0.15, swap=True, deg_multiplier=2)
+        _, mx = rel_errors(got, rec["prgrid_m0"])
+        assert mx <= PR_VS_REF32_MAX_REL, mx
+        # the tolerance stop
+        ref = oracle.pagerank_f64(adj, adj.out_deg(), 1.0 / n, 50, dangling=True)
+        got, st = g.pagerank(iterations=50, dangling=True, tolerance=1e-9)
+        assert st.iterations_run <= 50
+        l1, _ = rel_errors(got, ref)
+        assert l1 <= 1e-5, l1
+    finally:
+        g.set_row_schedule(0)
 
 
 def test_pagerank_source_blocks(case):
