@@ -8,14 +8,16 @@
 // partition, with a bit per entry marking where a run (the entries of one
 // source) begins; a chunk always begins a run, so a warp can take any chunk
 // without looking at the one before.  The runs' sources are the words the
-// kernel gathers through.  Segments of at most EG_PC_SEG_CHUNKS chunks split
-// the long partitions, and are listed longest first for the kernel's queue.
+// kernel gathers through.  Segments of at most 256 .. 2048 chunks (by the
+// size of the graph) split the long partitions, and are listed longest first
+// for the kernel's queue.
 #include <algorithm>
 #include <vector>
 
 #include "eg_internal.cuh"
 
-#define EG_PC_SEG_CHUNKS 512  // chunks per segment at most (128K entries)
+#define EG_PC_SEG_MIN 256    // chunks per segment at most: 64K entries ..
+#define EG_PC_SEG_MAX 2048   // .. 512K entries
 
 namespace {
 __global__ void k_pc_keys(const uint32_t *__restrict__ rowid, uint64_t M, uint32_t shift, uint32_t *keys,
@@ -133,16 +135,22 @@ int eg_build_pcols(eg_graph *g, uint32_t shift) {
         cudaStreamSynchronize(ctx->stream) != cudaSuccess)
         PTRY(eg_fail(EG_ECUDA, "partition bounds: %s", cudaGetErrorString(cudaGetLastError())));
     uint64_t chunks = 0;
-    std::vector<uint4> segs;
     for (uint32_t p = 0; p < P; p++) {
         cb[p] = (uint32_t)chunks;
-        const uint64_t cnt = (uint64_t)eb[p + 1] - eb[p];
-        const uint64_t nch = (cnt + EG_PC_CHUNK - 1) / EG_PC_CHUNK;
-        const uint64_t ns = nch ? (nch + EG_PC_SEG_CHUNKS - 1) / EG_PC_SEG_CHUNKS : 1;
+        chunks += ((uint64_t)eb[p + 1] - eb[p] + EG_PC_CHUNK - 1) / EG_PC_CHUNK;
+    }
+    // segments: about four per SM of the whole work, so that the longest-
+    // first queue balances the SMs, but as long as that allows, since every
+    // segment zeroes and writes out a partition's row sums
+    uint64_t segc = EG_PC_SEG_MIN;
+    while (segc < EG_PC_SEG_MAX && segc * 4 * (uint64_t)ctx->sm_count < chunks) segc *= 2;
+    std::vector<uint4> segs;
+    for (uint32_t p = 0; p < P; p++) {
+        const uint64_t c0 = cb[p], nch = (p + 1 < P ? cb[p + 1] : chunks) - c0;
+        const uint64_t ns = nch ? (nch + segc - 1) / segc : 1;
         for (uint64_t s = 0; s < ns; s++)
-            segs.push_back(make_uint4((uint32_t)(chunks + s * nch / ns), (uint32_t)(chunks + (s + 1) * nch / ns), p,
+            segs.push_back(make_uint4((uint32_t)(c0 + s * nch / ns), (uint32_t)(c0 + (s + 1) * nch / ns), p,
                                       (uint32_t)ns));
-        chunks += nch;
     }
     cb[P] = (uint32_t)chunks;
     std::stable_sort(segs.begin(), segs.end(), [](const uint4 &a, const uint4 &b) { return a.y - a.x > b.y - b.x; });

@@ -44,6 +44,14 @@ struct eg_pc_smem {
     static constexpr size_t bytes = acc_bytes + (size_t)EG_PC_WARPS * EG_PC_CHUNK * 8;
 };
 
+// One streamed 4-byte word (read once per pass): not kept in L1, first in
+// line for L2 eviction.
+__device__ __forceinline__ uint32_t eg_stream_ldu(const uint32_t *p, uint64_t pol) {
+    uint32_t v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(p), "l"(pol));
+    return v;
+}
+
 // A warp's chunk: the rows of entries lane, lane + 32, ..., lane + 224 (one
 // 16-byte word per lane: the layout stores each chunk transposed), the
 // chunk's 8 words of run-start bits (word j: entries 32j .. 32j + 31), the
@@ -108,15 +116,36 @@ __global__ void __launch_bounds__(EG_PC_THREADS, 1)
             uint32_t nr = 0;
 #pragma unroll
             for (int j = 0; j < 8; j++) nr += __popc(fw[j]);
-            // one contribution per run (consecutive runs: ascending sources)
-            for (uint32_t i = lane; i < nr; i += 64) {
-                const uint32_t i2 = i + 32;
-                const uint32_t u1 = __ldg(rsrc + k.rb + i);
+            // one contribution per run (consecutive runs: ascending sources);
+            // a chunk with many runs loads all of the lane's source words
+            // first, then all its gathers, so that it waits for two memory
+            // round trips whatever its number of runs
+            if (nr <= 64) {
+                const uint32_t i2 = lane + 32;
+                const uint32_t u1 = lane < nr ? __ldg(rsrc + k.rb + lane) : 0u;
                 const uint32_t u2 = i2 < nr ? __ldg(rsrc + k.rb + i2) : 0u;
-                const float v1 = op.gather(0u, u1);
+                const float v1 = lane < nr ? op.gather(0u, u1) : 0.f;
                 const float v2 = i2 < nr ? op.gather(0u, u2) : 0.f;
-                wv[i] = __float2ull_rn(v1 * fx);
+                if (lane < nr) wv[lane] = __float2ull_rn(v1 * fx);
                 if (i2 < nr) wv[i2] = __float2ull_rn(v2 * fx);
+            } else {
+                uint32_t us[EG_PC_CHUNK / 32];
+                float vs[EG_PC_CHUNK / 32];
+#pragma unroll
+                for (int i = 0; i < EG_PC_CHUNK / 32; i++) {
+                    const uint32_t r = lane + 32u * i;
+                    us[i] = r < nr ? __ldg(rsrc + k.rb + r) : 0u;
+                }
+#pragma unroll
+                for (int i = 0; i < EG_PC_CHUNK / 32; i++) {
+                    const uint32_t r = lane + 32u * i;
+                    vs[i] = r < nr ? op.gather(0u, us[i]) : 0.f;
+                }
+#pragma unroll
+                for (int i = 0; i < EG_PC_CHUNK / 32; i++) {
+                    const uint32_t r = lane + 32u * i;
+                    if (r < nr) wv[r] = __float2ull_rn(vs[i] * fx);
+                }
             }
             __syncwarp();
             // entry 32j + lane: its run is the last one that began at or
