@@ -32,8 +32,9 @@ METRIC, UNIT = "GTEPS", "GTEPS"
 # ncu capture of PageRank on directed RMAT-22 (the kernel's traffic grows with
 # the entries).
 PR_ROWS_DRAM_BYTES_PER_ENTRY = (294.009e6 + 3.622e6) / 67108864
-# the same for the partition kernel (k_pcol_rows); None until captured
-PR_PCOL_DRAM_BYTES_PER_ENTRY = None
+# the same for the partition kernel (k_pcol_rows), from a one-pass capture
+# on directed RMAT-24 itself
+PR_PCOL_DRAM_BYTES_PER_ENTRY = (991.200768e6 + 47.771392e6) / 268435456
 
 
 def peaks():
