@@ -718,7 +718,7 @@ def main():
     ap.add_argument("--only", choices=["pr", "spmv", "sssp", "msbfs", "ppr", "bfs", "serve", "cache"],
                     help="only one kernel report (profiling)")
     ap.add_argument("--rate", type=float, default=20000.0, help="offered rate when --rates is empty")
-    ap.add_argument("--rates", default="250,1000,5000,50000",
+    ap.add_argument("--rates", default="100,250,1000,5000,50000",
                     help="comma-separated offered Poisson rates (qps) of the serving sweep")
     ap.add_argument("--serve-seconds", type=float, default=2.0,
                     help="offered arrival span per rate (queries = rate x seconds, 200..--queries)")
