@@ -378,13 +378,26 @@ __device__ __forceinline__ bool pull_scan(uint32_t v, const uint32_t *__restrict
     uint32_t u = f0;
     bool hit = (__ldg(cur_bm + (u >> 5)) >> (u & 31)) & 1u;
     if (!hit) {
+        // four entries per step, their loads all in flight before the tests
+        // (a long list is a chain of dependent loads otherwise); the first
+        // hit in list order is kept
+        uint32_t p = ptr[v];
         const uint32_t e = ptr[v + 1];
-        for (uint32_t p = ptr[v]; p < e; p++) {
-            u = col[p];
-            if ((__ldg(cur_bm + (u >> 5)) >> (u & 31)) & 1u) {
+        for (; p + 4 <= e; p += 4) {
+            const uint32_t u0 = col[p], u1 = col[p + 1], u2 = col[p + 2], u3 = col[p + 3];
+            const uint32_t w0 = __ldg(cur_bm + (u0 >> 5)), w1 = __ldg(cur_bm + (u1 >> 5));
+            const uint32_t w2 = __ldg(cur_bm + (u2 >> 5)), w3 = __ldg(cur_bm + (u3 >> 5));
+            const bool h0 = (w0 >> (u0 & 31)) & 1u, h1 = (w1 >> (u1 & 31)) & 1u;
+            const bool h2 = (w2 >> (u2 & 31)) & 1u, h3 = (w3 >> (u3 & 31)) & 1u;
+            if (h0 | h1 | h2 | h3) {
+                u = h0 ? u0 : (h1 ? u1 : (h2 ? u2 : u3));
                 hit = true;
                 break;
             }
+        }
+        for (; !hit && p < e; p++) {
+            u = col[p];
+            hit = (__ldg(cur_bm + (u >> 5)) >> (u & 31)) & 1u;
         }
     }
     if (hit) {
