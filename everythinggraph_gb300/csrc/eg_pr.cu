@@ -741,17 +741,23 @@ extern "C" int eg_graph_tune(eg_graph *g, eg_tune_result *out) {
     r.chosen = best;
     {  // the partition kernel (PageRank only; SpMV keeps the row schedule)
         const int c = EG_ROW_CFGS;
-        EG_TRY(pcol_prepare(g));
-        g->pr_kernel = 1;
-        eg_pr_stats st;
-        EG_TRY(pr_run(g, o, none, 0, nullptr, &st));
-        EG_TRY(pr_run(g, o, none, 0, nullptr, &st));
         r.tile_entries[c] = EG_PC_CHUNK;
         r.entries_per_lane[c] = 8;
         r.prefetch[c] = 1;
         r.min_blocks[c] = 1;
         r.cache_hint[c] = 1;
         r.partition_log2[c] = EG_PC_SHIFT;
+        r.ms[c] = -1.f;  // not timed: its layout does not fit the context's budget
+        const int prc = pcol_prepare(g);
+        if (prc == EG_ENOMEM) {
+            eg_clear_error();
+            goto tuned;
+        }
+        EG_TRY(prc);
+        g->pr_kernel = 1;
+        eg_pr_stats st;
+        EG_TRY(pr_run(g, o, none, 0, nullptr, &st));
+        EG_TRY(pr_run(g, o, none, 0, nullptr, &st));
         r.ms[c] = st.row_kernel_ms;
         if (st.row_kernel_ms < r.ms[best]) {
             r.chosen = c;
@@ -759,6 +765,7 @@ extern "C" int eg_graph_tune(eg_graph *g, eg_tune_result *out) {
             g->pr_kernel = 0;
         }
     }
+tuned:
     if (g->built & EG_LAYOUT_CSR)
         EG_TRY(eg_bfs_tune(g, &r.bfs_graph_ms, &r.bfs_host_ms, &r.bfs_host_loop, &r.bfs_switch_divisor));
     if (out) *out = r;

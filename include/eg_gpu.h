@@ -199,7 +199,8 @@ int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out, eg_pr_stat
  * by source, so each source's contribution is gathered once per partition,
  * with 64-bit fixed-point row sums in shared memory (the same bits in any
  * order of addition).  It is kept for eg_pagerank only when it is the
- * fastest; eg_ppr and eg_spmv keep the fastest row schedule. */
+ * fastest; eg_ppr and eg_spmv keep the fastest row schedule.  Its ms is -1
+ * when its layout did not fit the context's HBM budget (it is then skipped). */
 #define EG_ROW_SCHEDULES_MAX 16
 typedef struct {
     int ncand;
