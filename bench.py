@@ -154,15 +154,16 @@ def run_ours(args):
     # reused by every call (what a serving process holds); eg_bfs_batch takes
     # E2E_BATCH roots per call and copies one root's levels and parents out
     # while it traverses the next
-    lv_h = eg.pinned_empty(E2E_BATCH * n, np.int32)
-    par_h = eg.pinned_empty(E2E_BATCH * n, np.int32)
+    eb = args.e2e_batch
+    lv_h = eg.pinned_empty(eb * n, np.int32)
+    par_h = eg.pinned_empty(eb * n, np.int32)
     lab_h = eg.pinned_empty(n, np.int64)
 
     def step(copy_out):
         traversed = 0
         if copy_out:
-            for c in range(0, len(roots), E2E_BATCH):
-                _, _, sts = g.bfs_batch(roots[c:c + E2E_BATCH], parents=True, level_out=lv_h, parent_out=par_h,
+            for c in range(0, len(roots), eb):
+                _, _, sts = g.bfs_batch(roots[c:c + eb], parents=True, level_out=lv_h, parent_out=par_h,
                                         host_loop=bfs_form)
                 traversed += sum(st.edges_traversed for st in sts)
         else:
@@ -254,13 +255,13 @@ def run_ours(args):
         "graph500_gteps": r4(g500),
         "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_s * 1e3 / args.steps,
-                "api": "eg_bfs_batch x%d roots/call into page-locked buffers + eg_wcc" % E2E_BATCH},
+                "api": "eg_bfs_batch x%d roots/call into page-locked buffers + eg_wcc" % eb},
         "gpu_launches": launches,
         "roofline": roof,
         "clocks": clk.summary(),
     }
     if not args.no_cpu and rank == 0:
-        cb, parity = cpu_baseline(g, eg, roots, n, m_in, args, lv_h, par_h, lab_h)
+        cb, parity = cpu_baseline(g, eg, roots, n, m_in, args, lv_h, par_h, lab_h, eb)
         out["cpu_baseline"] = cb
         out["parity"] = parity
     out["load_build_ms"] = r4(build_ms)
@@ -497,18 +498,18 @@ def serve_sweep(ctx, eg, scale, args, g):
     return out
 
 
-def cpu_baseline(g, eg, roots, n, m_in, args, lv_h=None, par_h=None, lab_h=None):
+def cpu_baseline(g, eg, roots, n, m_in, args, lv_h=None, par_h=None, lab_h=None, eb=E2E_BATCH):
     """The multi-threaded CPU port of the reference loops (bfs_simple's
     direction-optimising iterator, wcc's label propagation) on a bounded
     sample of the same step: the first roots that fit in ~15 s plus one WCC,
     on the same graph copied to the host.  Outside the CPU timing, the GPU's
-    last end-to-end outputs (levels and parents of the last E2E_BATCH roots,
+    last end-to-end outputs (levels and parents of the last `eb` roots,
     WCC labels, in the page-locked buffers) are compared with the port's:
     levels and labels bit for bit, parents as a BFS tree."""
     import oracle
     oracle.build()
     ptr, col = g.adj(eg.CSR)
-    first = len(roots) - E2E_BATCH
+    first = len(roots) - eb
     par = {"bfs_roots_checked": 0, "bfs_levels_bit_exact": True, "bfs_trees_valid": True}
 
     def check(i, r, lv):
@@ -713,6 +714,7 @@ def main():
     ap.add_argument("--bfs-form", choices=["auto", "graph", "host"], default="auto",
                     help="BFS level loop: the form eg_graph_tune keeps (auto), or a fixed one")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--e2e-batch", type=int, default=E2E_BATCH, help="roots per eg_bfs_batch call in the end-to-end step")
     ap.add_argument("--pr-only", action="store_true", help="only the PageRank pull report (profiling)")
     ap.add_argument("--serve-only", action="store_true", help="only the serving report")
     ap.add_argument("--only", choices=["pr", "spmv", "sssp", "msbfs", "ppr", "bfs", "serve", "cache"],
