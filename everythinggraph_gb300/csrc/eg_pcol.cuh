@@ -44,6 +44,36 @@ struct eg_pc_smem {
     static constexpr size_t bytes = acc_bytes + (size_t)EG_PC_WARPS * EG_PC_CHUNK * 8;
 };
 
+// round(x) for 0 <= x < 2^64 as an unsigned 64-bit integer, from 32-bit
+// conversions only (a 64-bit float-to-integer conversion runs on the FP64
+// pipe, which is narrow on this GPU).  hi = floor(x / 2^32) and
+// x - hi * 2^32 (exact: both are multiples of x's ulp) are floats; the low
+// part has a fraction only when x < 2^24, where hi = 0, so rounding it to
+// the nearest integer rounds x.
+__device__ __forceinline__ unsigned long long eg_f2u64_rn(float x) {
+    const float hf = truncf(x * 2.3283064365386963e-10f);  // x / 2^32
+    const float lf = fmaf(-hf, 4294967296.0f, x);           // x - hi * 2^32
+    return ((unsigned long long)__float2uint_rz(hf) << 32) | __float2uint_rn(lf);
+}
+
+// The unsigned 64-bit value hi * 2^32 + lo rounded to the nearest float
+// (ties to even), from 32-bit integer operations for the same reason.
+__device__ __forceinline__ float eg_u642f_rn(uint32_t hi, uint32_t lo) {
+    if (hi == 0u) return __uint2float_rn(lo);
+    const int lz = __clz(hi);
+    const int sh = 40 - lz;  // bits below the 24-bit significand (9 .. 40)
+    const unsigned long long v = ((unsigned long long)hi << 32) | lo;
+    uint32_t mant = (uint32_t)(v >> sh);
+    const unsigned long long rem = v & ((1ull << sh) - 1ull), half = 1ull << (sh - 1);
+    int e = 63 - lz;  // exponent of the leading bit
+    if (rem > half || (rem == half && (mant & 1u))) mant++;
+    if (mant == (1u << 24)) {
+        mant >>= 1;
+        e++;
+    }
+    return __uint_as_float(((uint32_t)(e + 127) << 23) | (mant & 0x7fffffu));
+}
+
 // One streamed 4-byte word (read once per pass): not kept in L1, first in
 // line for L2 eviction.
 __device__ __forceinline__ uint32_t eg_stream_ldu(const uint32_t *p, uint64_t pol) {
@@ -54,20 +84,32 @@ __device__ __forceinline__ uint32_t eg_stream_ldu(const uint32_t *p, uint64_t po
 
 // A warp's chunk: the rows of entries lane, lane + 32, ..., lane + 224 (one
 // 16-byte word per lane: the layout stores each chunk transposed), the
-// chunk's 8 words of run-start bits (word j: entries 32j .. 32j + 31), the
-// chunk's first run.
+// chunk's run-start word `lane` for lanes 0..7 (word j: entries 32j ..
+// 32j + 31), the chunk's first run.
 struct eg_pc_chunk {
     uint4 d8;
-    uint4 f0, f1;
+    uint32_t fw;
     uint32_t rb;
 };
 __device__ __forceinline__ void eg_pc_load(const uint32_t *__restrict__ dst, const uint32_t *__restrict__ flags,
                                            const uint32_t *__restrict__ crun, uint64_t c, uint32_t lane,
                                            uint64_t pol, eg_pc_chunk &k) {
     k.d8 = eg_stream_ld4<1>(dst + c * (EG_PC_CHUNK / 2) + 4 * lane, pol);
-    k.f0 = __ldg(reinterpret_cast<const uint4 *>(flags + c * (EG_PC_CHUNK / 32)));
-    k.f1 = __ldg(reinterpret_cast<const uint4 *>(flags + c * (EG_PC_CHUNK / 32) + 4));
+    k.fw = lane < EG_PC_CHUNK / 32 ? __ldg(flags + c * (EG_PC_CHUNK / 32) + lane) : 0u;
     k.rb = __ldg(crun + c);
+}
+
+// The chunk's run count and, when it has at most 64 runs, the sources of
+// runs lane and lane + 32.
+__device__ __forceinline__ uint32_t eg_pc_sources(const eg_pc_chunk &k, const uint32_t *__restrict__ rsrc,
+                                                  uint32_t lane, uint32_t &u1, uint32_t &u2) {
+    const uint32_t nr = __reduce_add_sync(EG_FULL_MASK, __popc(k.fw));
+    u1 = u2 = 0u;
+    if (nr <= 64) {
+        if (lane < nr) u1 = __ldg(rsrc + k.rb + lane);
+        if (lane + 32 < nr) u2 = __ldg(rsrc + k.rb + lane + 32);
+    }
+    return nr;
 }
 
 template <class Op, int SHIFT, bool REDUCE>
@@ -83,7 +125,7 @@ __global__ void __launch_bounds__(EG_PC_THREADS, 1)
     using SM = eg_pc_smem<SHIFT>;
     uint32_t *slo = reinterpret_cast<uint32_t *>(eg_pc_sm);                    // low words
     uint32_t *shi = reinterpret_cast<uint32_t *>(eg_pc_sm + SM::word_bytes);  // high words
-    auto row_sum = [&](uint32_t l) -> float { return __ull2float_rn(((T)shi[l] << 32) | (T)slo[l]) * fx_inv; };
+    auto row_sum = [&](uint32_t l) -> float { return eg_u642f_rn(shi[l], slo[l]) * fx_inv; };
     __shared__ double2 s_red[32];
     __shared__ uint32_t s_seg;
     __shared__ int s_last;
@@ -105,29 +147,32 @@ __global__ void __launch_bounds__(EG_PC_THREADS, 1)
             shi[i] = 0u;
         }
         __syncthreads();
-        uint64_t c = (uint64_t)sg.x + warp;
-        eg_pc_chunk k;
-        if (c < c1) eg_pc_load(dst, flags, crun, c, lane, pol, k);
+        // a two-stage pipeline per warp: while chunk c is summed, the words
+        // of chunk c + 2W are in flight and the run sources of chunk c + W
+        // are loaded, so that c's gathers wait for one memory round trip
+        uint64_t c = (uint64_t)sg.x + warp, cn = c + EG_PC_WARPS;
+        eg_pc_chunk k = {}, kn = {};
+        uint32_t nr = 0, u1 = 0, u2 = 0;
+        if (c < c1) {
+            eg_pc_load(dst, flags, crun, c, lane, pol, k);
+            nr = eg_pc_sources(k, rsrc, lane, u1, u2);
+        }
+        if (cn < c1) eg_pc_load(dst, flags, crun, cn, lane, pol, kn);
         while (c < c1) {
-            const uint64_t cn = c + EG_PC_WARPS;
-            eg_pc_chunk kn = k;
-            if (cn < c1) eg_pc_load(dst, flags, crun, cn, lane, pol, kn);
-            const uint32_t fw[8] = {k.f0.x, k.f0.y, k.f0.z, k.f0.w, k.f1.x, k.f1.y, k.f1.z, k.f1.w};
-            uint32_t nr = 0;
-#pragma unroll
-            for (int j = 0; j < 8; j++) nr += __popc(fw[j]);
+            const uint64_t cnn = cn + EG_PC_WARPS;
+            eg_pc_chunk knn = kn;
+            if (cnn < c1) eg_pc_load(dst, flags, crun, cnn, lane, pol, knn);
+            uint32_t nrn = 0, un1 = 0, un2 = 0;
+            if (cn < c1) nrn = eg_pc_sources(kn, rsrc, lane, un1, un2);
             // one contribution per run (consecutive runs: ascending sources);
-            // a chunk with many runs loads all of the lane's source words
-            // first, then all its gathers, so that it waits for two memory
-            // round trips whatever its number of runs
+            // a chunk with more than 64 runs loads all of the lane's source
+            // words, then all its gathers
             if (nr <= 64) {
                 const uint32_t i2 = lane + 32;
-                const uint32_t u1 = lane < nr ? __ldg(rsrc + k.rb + lane) : 0u;
-                const uint32_t u2 = i2 < nr ? __ldg(rsrc + k.rb + i2) : 0u;
                 const float v1 = lane < nr ? op.gather(0u, u1) : 0.f;
                 const float v2 = i2 < nr ? op.gather(0u, u2) : 0.f;
-                if (lane < nr) wv[lane] = __float2ull_rn(v1 * fx);
-                if (i2 < nr) wv[i2] = __float2ull_rn(v2 * fx);
+                if (lane < nr) wv[lane] = eg_f2u64_rn(v1 * fx);
+                if (i2 < nr) wv[i2] = eg_f2u64_rn(v2 * fx);
             } else {
                 uint32_t us[EG_PC_CHUNK / 32];
                 float vs[EG_PC_CHUNK / 32];
@@ -144,10 +189,13 @@ __global__ void __launch_bounds__(EG_PC_THREADS, 1)
 #pragma unroll
                 for (int i = 0; i < EG_PC_CHUNK / 32; i++) {
                     const uint32_t r = lane + 32u * i;
-                    if (r < nr) wv[r] = __float2ull_rn(vs[i] * fx);
+                    if (r < nr) wv[r] = eg_f2u64_rn(vs[i] * fx);
                 }
             }
             __syncwarp();
+            uint32_t fw[EG_PC_CHUNK / 32];
+#pragma unroll
+            for (int j = 0; j < EG_PC_CHUNK / 32; j++) fw[j] = __shfl_sync(EG_FULL_MASK, k.fw, j);
             // entry 32j + lane: its run is the last one that began at or
             // before it (every chunk begins with a run)
             const uint32_t h[4] = {k.d8.x, k.d8.y, k.d8.z, k.d8.w};
@@ -175,7 +223,12 @@ __global__ void __launch_bounds__(EG_PC_THREADS, 1)
             }
             __syncwarp();
             c = cn;
+            cn = cnn;
             k = kn;
+            kn = knn;
+            nr = nrn;
+            u1 = un1;
+            u2 = un2;
         }
         __syncthreads();
         const uint32_t row0 = p << SHIFT;
@@ -199,7 +252,7 @@ __global__ void __launch_bounds__(EG_PC_THREADS, 1)
                 for (uint32_t l = tid; l < nrows; l += EG_PC_THREADS) {
                     const T a = __ldcg(gacc + row0 + l);
                     gacc[row0 + l] = 0ull;
-                    const float2 d = op.emit(row0 + l, __ull2float_rn(a) * fx_inv);
+                    const float2 d = op.emit(row0 + l, eg_u642f_rn((uint32_t)(a >> 32), (uint32_t)a) * fx_inv);
                     if (REDUCE) redf.add(d);
                 }
                 if (tid == 0) ticket[p] = 0u;
