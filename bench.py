@@ -457,7 +457,8 @@ def serve_run(eg, g, w, arrivals, qs, exclusive=False, gang=True):
             time.sleep(max(0.0, min(0.001, arr[i] - srv.info()["clock_s"])))
     srv.close()
     lat = np.array([r.done_s - r.arrival_s for r in done]) * 1e3
-    return lat, max(r.done_s for r in done) - arr[0]
+    kinds = np.array([r.kind for r in done])
+    return lat, max(r.done_s for r in done) - arr[0], kinds
 
 
 def plain_qps(g, w, qs):
@@ -488,9 +489,12 @@ def serve_sweep(ctx, eg, scale, args, g):
     for rate in rates:
         nq = int(min(args.queries, max(200, rate * args.serve_seconds)))
         arrivals, qs = serve_queries(nz, nq, rate, 7)
-        lat, span = serve_run(eg, g, w, arrivals, qs, exclusive=args.serve_exclusive, gang=not args.serve_no_gang)
+        lat, span, kinds = serve_run(eg, g, w, arrivals, qs, exclusive=args.serve_exclusive,
+                                     gang=not args.serve_no_gang)
+        # p50 per query kind: BFS, SSSP, PPR
+        p50k = [r4(np.percentile(lat[kinds == k], 50)) if np.any(kinds == k) else None for k in (1, 2, 3)]
         out["rates"].append({"offered": rate, "n": nq, "qps": r4(nq / span), "p50_ms": r4(np.percentile(lat, 50)),
-                             "p99_ms": r4(np.percentile(lat, 99))})
+                             "p99_ms": r4(np.percentile(lat, 99)), "p50_bfs_sssp_ppr": p50k})
     _, qs = serve_queries(nz, args.plain_sample, 1000.0, 7)
     out["plain_qps"] = r4(plain_qps(g, w, qs))
     best = max(r["qps"] for r in out["rates"])

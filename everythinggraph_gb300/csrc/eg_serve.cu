@@ -524,8 +524,16 @@ extern "C" int eg_serve_open(eg_graph *g, const eg_serve_opts *opts, eg_server *
     if (rc == EG_OK) rc = eg_buf_ensure(ctx, s->wts_buf, g->m * 4 + 16);
     if (rc == EG_OK) rc = eg_fill_weights(g, eg_make_wrule(&o.weights), bp<uint32_t>(s->wts_buf));
     if (rc == EG_OK) s->wts = bp<uint32_t>(s->wts_buf);
+    // stream priorities by step length: the blocks of a BFS level (~1 ms)
+    // are scheduled ahead of those of a Bellman-Ford round or a PPR sweep
+    // (~13 ms), so that the short queries do not queue behind long steps;
+    // SSSP and PPR share the lower priority
+    int lo_prio = 0, hi_prio = 0;
+    if (rc == EG_OK && cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio) != cudaSuccess)
+        rc = eg_fail(EG_ECUDA, "stream priority range");
+    const int prio[3] = {hi_prio, lo_prio, lo_prio};  // BFS, SSSP, PPR
     for (int e = 0; e < 3 && rc == EG_OK; e++) {
-        if (cudaStreamCreateWithFlags(&s->st[e], cudaStreamNonBlocking) != cudaSuccess ||
+        if (cudaStreamCreateWithPriority(&s->st[e], cudaStreamNonBlocking, prio[e]) != cudaSuccess ||
             cudaEventCreate(&s->ev_begin[e]) != cudaSuccess || cudaEventCreate(&s->ev_end[e]) != cudaSuccess)
             rc = eg_fail(EG_ECUDA, "server streams/events");
     }
