@@ -215,6 +215,7 @@ extern "C" int eg_graph_load_layouts(eg_graph *g, const char *path, int *hit) {
     g->edge_order = h.edge_order;
     // derived copies follow the layouts they were made from
     g->first_in_src = nullptr;
+    g->wcc_list_src = nullptr;
     g->relabeled = false;
     g->sb.blocks = g->sb.shift = 0;
     g->sbp.blocks = g->sbp.shift = 0;

@@ -405,7 +405,7 @@ extern "C" void eg_graph_free(eg_graph *g) {
                       &g->grid_order,   &g->grid_units,  &g->grid_off,    &g->grid_vals,   &g->grid_acc,
                       &g->esrc,         &g->edst,        &g->edge_work,
                       &g->pcol.dst,     &g->pcol.flags,  &g->pcol.crun,   &g->pcol.rsrc,   &g->pcol.seg,
-                      &g->pcol.acc,     &g->pcol.ticket};
+                      &g->pcol.acc,     &g->pcol.ticket,  &g->wcc_list};
     for (eg_buf *b : bufs) eg_buf_free(c, *b);
     for (eg_bfs_graph &bg : g->bfsg) {
         if (bg.exec) cudaGraphExecDestroy(bg.exec);
@@ -775,6 +775,7 @@ static int build_adj_pair(eg_graph *g, bool want_csc) {
         BTRY(eg_fail(EG_ECUDA, "copy rid"));
     g->built |= EG_LAYOUT_CSR;
     g->first_in_src = nullptr;
+    g->wcc_list_src = nullptr;
     if (want_csc) {
         // CSC: stable sort of the CSR entries by dst, value src.  The sorted
         // src keys become the values; the CSR cols (a copy) become the keys.
@@ -796,6 +797,7 @@ static int build_adj_pair(eg_graph *g, bool want_csc) {
             BTRY(eg_fail(EG_ECUDA, "copy rid"));
         g->built |= EG_LAYOUT_CSC;
         g->first_in_src = nullptr;
+        g->wcc_list_src = nullptr;
         g->relabeled = false;  // so do PageRank's relabelled copy
         g->sb.blocks = 0;  // the source-blocked copies follow the CSC
         g->sb.shift = 0;

@@ -186,6 +186,11 @@ struct eg_graph {
     eg_buf level_s[EG_OUT_SLOTS - 1], parent_s[EG_OUT_SLOTS - 1];  // output slots 1.. of eg_bfs_batch
     eg_buf first_in;                  // BFS pull: each vertex's first in-neighbour (0xffffffff: none)
     const void *first_in_src = nullptr;  // the in-list column array first_in was taken from
+    // WCC: the vertices with an edge (out- or in-list not empty), listed once
+    // per layout so that the hooking rounds give no thread to an isolated one
+    eg_buf wcc_list;
+    uint32_t wcc_list_n = 0;
+    const void *wcc_list_src = nullptr;  // the CSR row pointers the list was taken from
     uint64_t spmv_vals_seed;
     int spmv_vals_kind;
     eg_sblocks sb;   // source-blocked copy of the CSC (fp32 SpMV over an x larger than L2)

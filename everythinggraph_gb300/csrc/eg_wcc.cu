@@ -53,10 +53,13 @@ __device__ __forceinline__ void uf_link(uint32_t *par, uint32_t x, uint32_t y) {
 }
 
 // Hooks entries [lo, hi) of every list (first round: lo=0, hi=2) or, with
-// skip_root set, entries [lo, end) of vertices whose root is not skip_root.
-__global__ void k_wcc_lists(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col, uint32_t n,
-                            uint32_t lo, uint32_t hi, uint32_t skip_root, uint32_t *par) {
-    for (uint32_t u = blockIdx.x * blockDim.x + threadIdx.x; u < n; u += gridDim.x * blockDim.x) {
+// skip_root set, entries [lo, end) of vertices whose root is not skip_root;
+// the vertices are list[0 .. count) (those with an edge).
+__global__ void k_wcc_lists(const uint32_t *__restrict__ ptr, const uint32_t *__restrict__ col,
+                            const uint32_t *__restrict__ list, uint32_t count, uint32_t lo, uint32_t hi,
+                            uint32_t skip_root, uint32_t *par) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t u = __ldg(list + i);
         if (skip_root != EG_WCC_NONE && uf_find(par, u) == skip_root) continue;
         const uint32_t b = ptr[u], e = ptr[u + 1];
         const uint32_t pe = (hi == EG_WCC_NONE || b + hi > e) ? e : b + hi;
@@ -69,6 +72,19 @@ __global__ void k_wcc_lists(const uint32_t *__restrict__ ptr, const uint32_t *__
 __global__ void k_wcc_sample(const uint32_t *__restrict__ par, uint32_t n, uint32_t *out) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < 1024) out[i] = par[(uint32_t)(((eg_mix64((uint64_t)i + 0x51ed) >> 32) * (uint64_t)n) >> 32)];
+}
+
+// The vertices with a non-empty out-list (or in-list), in id order: a
+// flag per vertex, then each warp's ballot placed at its exclusive prefix.
+__global__ void k_wcc_has_edge(const uint32_t *__restrict__ optr, const uint32_t *__restrict__ iptr, uint32_t n,
+                               uint32_t *flag) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        flag[v] = (optr[v + 1] > optr[v]) || (iptr && iptr[v + 1] > iptr[v]);
+}
+__global__ void k_wcc_place(const uint32_t *__restrict__ flag, const uint32_t *__restrict__ pos, uint32_t n,
+                            uint32_t *list) {
+    for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += gridDim.x * blockDim.x)
+        if (flag[v]) list[pos[v]] = v;
 }
 
 __global__ void k_wcc_flatten(uint32_t n, uint32_t *par) {
@@ -143,14 +159,32 @@ extern "C" int eg_wcc(eg_graph *g, int64_t *labels_out, eg_wcc_stats *stats) {
     const bool sym = (g->flags & EG_UNDIRECTED) != 0;
     const bool have_csc = (g->built & EG_LAYOUT_CSC) != 0;
     int rounds = 1;
+    if (have_csr && (sym || have_csc) && n >= 1024 && g->wcc_list_src != g->csr.ptr.p) {
+        // once per layout: the vertices with an edge (flags, scan, placement)
+        EG_TRY(eg_buf_ensure(ctx, g->wcc_list, ((uint64_t)n + 1) * 4 * 3));
+        uint32_t *flag = bp<uint32_t>(g->wcc_list) + (uint64_t)n + 1, *pos = flag + (uint64_t)n + 1;
+        k_wcc_has_edge<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr), sym ? nullptr : bp<uint32_t>(g->csc.ptr),
+                                                        n, flag);
+        EG_LAUNCHED(ctx);
+        EG_TRY(eg_exscan_u32(ctx, flag, pos, n));
+        k_wcc_place<<<blocks, 256, 0, ctx->stream>>>(flag, pos, n, bp<uint32_t>(g->wcc_list));
+        EG_LAUNCHED(ctx);
+        uint32_t cnt = 0;
+        EG_CUDA(cudaMemcpyAsync(&cnt, pos + n, 4, cudaMemcpyDeviceToHost, ctx->stream));
+        EG_CUDA(cudaStreamSynchronize(ctx->stream));
+        g->wcc_list_n = cnt;
+        g->wcc_list_src = g->csr.ptr.p;
+    }
+    const uint32_t *wl = bp<uint32_t>(g->wcc_list);
+    const uint32_t wn = g->wcc_list_n;
     if (have_csr && (sym || have_csc) && n >= 1024) {
         // round 1: two entries per list (both directions for a directed graph)
-        k_wcc_lists<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), n, 0, 2,
+        k_wcc_lists<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), wl, wn, 0, 2,
                                                      EG_WCC_NONE, par);
         EG_LAUNCHED(ctx);
         if (!sym) {
-            k_wcc_lists<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), bp<uint32_t>(g->csc.col), n, 0, 2,
-                                                         EG_WCC_NONE, par);
+            k_wcc_lists<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), bp<uint32_t>(g->csc.col), wl, wn, 0,
+                                                         2, EG_WCC_NONE, par);
             EG_LAUNCHED(ctx);
         }
         k_wcc_flatten<<<blocks, 256, 0, ctx->stream>>>(n, par);
@@ -177,11 +211,11 @@ extern "C" int eg_wcc(eg_graph *g, int64_t *labels_out, eg_wcc_stats *stats) {
             i = j;
         }
         // round 2: remaining entries of vertices outside the sampled component
-        k_wcc_lists<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), n, 2,
+        k_wcc_lists<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csr.ptr), bp<uint32_t>(g->csr.col), wl, wn, 2,
                                                      EG_WCC_NONE, best, par);
         EG_LAUNCHED(ctx);
         if (!sym) {
-            k_wcc_lists<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), bp<uint32_t>(g->csc.col), n, 2,
+            k_wcc_lists<<<blocks, 256, 0, ctx->stream>>>(bp<uint32_t>(g->csc.ptr), bp<uint32_t>(g->csc.col), wl, wn, 2,
                                                          EG_WCC_NONE, best, par);
             EG_LAUNCHED(ctx);
         }
