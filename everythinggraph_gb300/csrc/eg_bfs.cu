@@ -65,8 +65,13 @@ __device__ __forceinline__ void block_add_counters(BfsCounters *c, uint32_t cnt,
     }
 }
 
+// noin (may be NULL): a bit per vertex without in-neighbours.  Such a vertex
+// can only be the root, so it starts out visited: the pull levels then skip
+// it, and skip whole words of them (on undirected RMAT about half the ids
+// are isolated).  Its level and parent stay those of an unreached vertex.
 __global__ void k_bfs_init(uint32_t n, int32_t *level, int32_t *parent, uint32_t *visited, uint32_t *cur_bm,
-                           uint32_t nw, uint32_t root, uint32_t *queue, const uint32_t *deg, BfsCounters *cnt) {
+                           uint32_t nw, uint32_t root, uint32_t *queue, const uint32_t *deg, BfsCounters *cnt,
+                           const uint32_t *__restrict__ noin) {
     uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
         level[v] = v == root ? 1 : 0;
@@ -74,7 +79,7 @@ __global__ void k_bfs_init(uint32_t n, int32_t *level, int32_t *parent, uint32_t
     }
     for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += stride) {
         uint32_t bit = (root >> 5) == w ? 1u << (root & 31) : 0u;
-        visited[w] = bit;
+        visited[w] = bit | (noin ? noin[w] : 0u);
         cur_bm[w] = bit;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -432,6 +437,16 @@ __global__ void k_first_in(const uint32_t *__restrict__ ptr, const uint32_t *__r
     }
 }
 
+// bits[w]: bit l set when vertex 32w + l has no in-neighbours (ids past n: set)
+__global__ void k_no_in_bits(const uint32_t *__restrict__ first, uint32_t n, uint32_t nw, uint32_t *bits) {
+    const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;  // a multiple of 32: warps stay whole
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < (uint64_t)nw * 32; v += stride) {
+        const bool none = v >= n || first[v] == EG_NO_VERTEX;
+        const uint32_t b = __ballot_sync(EG_FULL_MASK, none);
+        if ((threadIdx.x & 31) == 0) bits[v >> 5] = b;
+    }
+}
+
 // Bottom-up step: one thread per vertex, warps over 32 consecutive vertices
 // (one bitmap word).  An unvisited vertex scans its in-list and stops at the
 // first neighbour in the frontier.  The new frontier word is the warp ballot.
@@ -490,7 +505,8 @@ struct BfsGState {
 };
 
 __global__ void k_bfsg_start(BfsGState *st, const uint32_t *__restrict__ deg, int32_t *level, int32_t *parent,
-                             uint32_t *visited, uint32_t *bm0, uint32_t nw, uint32_t *q0, BfsCounters *cnt) {
+                             uint32_t *visited, uint32_t *bm0, uint32_t nw, uint32_t *q0, BfsCounters *cnt,
+                             const uint32_t *__restrict__ noin) {
     const uint32_t n = st->n, root = st->root;
     const uint32_t stride = gridDim.x * blockDim.x;
     for (uint32_t v = blockIdx.x * blockDim.x + threadIdx.x; v < n; v += stride) {
@@ -499,7 +515,7 @@ __global__ void k_bfsg_start(BfsGState *st, const uint32_t *__restrict__ deg, in
     }
     for (uint32_t w = blockIdx.x * blockDim.x + threadIdx.x; w < nw; w += stride) {
         const uint32_t bit = (root >> 5) == w ? 1u << (root & 31) : 0u;
-        visited[w] = bit;
+        visited[w] = bit | (noin ? noin[w] : 0u);  // as in k_bfs_init
         bm0[w] = bit;
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -733,7 +749,8 @@ static int bfs_graph_build(eg_graph *g, eg_bfs_graph &bg, const void *const key[
     const uint32_t blocks = (uint32_t)ctx->sm_count * 8;
     // start kernel
     EG_CUDA(cudaStreamBeginCaptureToGraph(ctx->stream, graph, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
-    k_bfsg_start<<<blocks, 256, 0, ctx->stream>>>(st, deg, level, parent, visited, bm0, nw, q0, cnt);
+    k_bfsg_start<<<blocks, 256, 0, ctx->stream>>>(st, deg, level, parent, visited, bm0, nw, q0, cnt,
+                                                  in_adj ? bp<uint32_t>(g->first_in) + n : nullptr);
     cudaError_t ce = cudaStreamEndCapture(ctx->stream, &graph);
     if (ce != cudaSuccess) return eg_fail(EG_ECUDA, "BFS graph capture: %s", cudaGetErrorString(ce));
     cudaGraphNode_t start_node;
@@ -799,9 +816,13 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
     const uint32_t n = g->n;
     const uint32_t nw = (n + 31) >> 5;
     if (in_adj && g->first_in_src != in_adj->col.p) {  // once per graph and in-list array
-        EG_TRY(eg_buf_ensure(ctx, g->first_in, (uint64_t)n * 4));
+        // first_in[0 .. n), then the bit per vertex without in-neighbours
+        EG_TRY(eg_buf_ensure(ctx, g->first_in, ((uint64_t)n + nw) * 4));
         k_first_in<<<(uint32_t)ctx->sm_count * 8, 256, 0, ctx->stream>>>(
             bp<uint32_t>(in_adj->ptr), bp<uint32_t>(in_adj->col), bp<uint32_t>(g->out_deg), n, bp<uint32_t>(g->first_in));
+        EG_LAUNCHED(ctx);
+        k_no_in_bits<<<blocks_for(ctx, (uint64_t)nw * 32), 256, 0, ctx->stream>>>(bp<uint32_t>(g->first_in), n, nw,
+                                                                                  bp<uint32_t>(g->first_in) + n);
         EG_LAUNCHED(ctx);
         g->first_in_src = in_adj->col.p;
     }
@@ -829,7 +850,8 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
     const bool host_loop = o.host_loop < 0 ? g->bfs_host_loop != 0 : o.host_loop != 0;
     if (!host_loop) {
         eg_bfs_graph &bg = g->bfsg[slot * 2 + (want_parent ? 1 : 0)];
-        const void *key[8] = {wk, level, parent, deg, g->csr.col.p, in_adj ? in_adj->col.p : nullptr, g->csr.ptr.p,
+        const void *key[8] = {wk, level, parent, (const void *)((uintptr_t)deg ^ ((uintptr_t)g->first_in.p << 1)),
+                              g->csr.col.p, in_adj ? in_adj->col.p : nullptr, g->csr.ptr.p,
                               (const void *)(uintptr_t)ctx->stream};
         bool fresh = bg.exec != nullptr;
         for (int i = 0; i < 8 && fresh; i++) fresh = bg.key[i] == key[i];
@@ -867,7 +889,8 @@ static int bfs_core(eg_graph *g, uint32_t root, const eg_bfs_opts &o, int slot, 
     // host-driven level loop
     BfsCounters *h = (BfsCounters *)ctx->h_pinned;
     EG_CUDA(cudaEventRecord(ctx->ev0, ctx->stream));
-    k_bfs_init<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(n, level, parent, visited, bm[0], nw, root, q[0], deg, cnt);
+    k_bfs_init<<<blocks_for(ctx, n), 256, 0, ctx->stream>>>(n, level, parent, visited, bm[0], nw, root, q[0], deg, cnt,
+                                                            in_adj ? bp<uint32_t>(g->first_in) + n : nullptr);
     EG_LAUNCHED(ctx);
     uint32_t count = 1, qlen = 1;
     unsigned long long fdeg = 0;
