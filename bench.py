@@ -34,7 +34,7 @@ METRIC, UNIT = "GTEPS", "GTEPS"
 PR_ROWS_DRAM_BYTES_PER_ENTRY = (294.009e6 + 3.622e6) / 67108864
 # the same for the partition kernel (k_pcol_rows), from a one-pass capture
 # on directed RMAT-24 itself
-PR_PCOL_DRAM_BYTES_PER_ENTRY = (991.200768e6 + 47.771392e6) / 268435456
+PR_PCOL_DRAM_BYTES_PER_ENTRY = (1060.849152e6 + 41.525504e6) / 268435456
 
 
 def peaks():
@@ -240,7 +240,8 @@ def run_ours(args):
         gbps = dom["bytes"] / (dom["row_ms"] / 1e3) / 1e9
         pcol = dom["sched"].startswith("partitions")
         per_entry = PR_PCOL_DRAM_BYTES_PER_ENTRY if pcol else PR_ROWS_DRAM_BYTES_PER_ENTRY
-        kname = "k_pcol_rows<PrOp<0>,14>" if pcol else "k_coov_rows<PrOp<0>,%s>" % dom["sched"]
+        kname = ("k_pcol_rows<PrOp<0>,%s>" % dom["sched"].split()[1].rstrip(",").split("^")[1] if pcol
+                 else "k_coov_rows<PrOp<0>,%s>" % dom["sched"])
         roof = {"bound": "hbm", "achieved": r4(gbps), "peak": hbm, "unit": "GB/s", "frac": r4(gbps / hbm),
                 "traffic": r4(per_entry * dom["m"]) if per_entry else None,
                 "kernel": "%s (PageRank pull, RMAT-%d directed)" % (kname, scale),

@@ -8,8 +8,8 @@
 // Here a partition's entries are ordered by source: all entries of source
 // u into the partition form one run, whose contribution is loaded once and
 // added into the rows of the run's entries, and consecutive runs are
-// ascending sources, so the loads of a warp share sectors (0.15 sectors per
-// entry for partitions of 16K rows).  The streamed words are 2 bytes per
+// ascending sources, so the loads of a warp share sectors (0.19 sectors per
+// entry for partitions of 8K rows on directed RMAT-24).  The streamed words are 2 bytes per
 // entry (the row within the partition) plus a run-start bit, and 4 bytes per
 // run (its source).
 //
@@ -26,7 +26,10 @@
 #pragma once
 #include "eg_mp.cuh"
 
-#define EG_PC_THREADS 1024
+#ifndef EG_PC_THREADS
+#define EG_PC_THREADS 1024  // (512 with two CTAs per SM: 0.553 against 0.505 ms on RMAT-24)
+#endif
+#define EG_PC_CTAS (1024 / EG_PC_THREADS)  // resident CTAs per SM (64 registers a thread)
 #define EG_PC_WARPS (EG_PC_THREADS / 32)
 
 // Shared memory of k_pcol_rows with partitions of 2^SHIFT rows: the row
@@ -113,7 +116,7 @@ __device__ __forceinline__ uint32_t eg_pc_sources(const eg_pc_chunk &k, const ui
 }
 
 template <class Op, int SHIFT, bool REDUCE>
-__global__ void __launch_bounds__(EG_PC_THREADS, 1)
+__global__ void __launch_bounds__(EG_PC_THREADS, EG_PC_CTAS)
     k_pcol_rows(const uint4 *__restrict__ seg, uint32_t nseg, const uint32_t *__restrict__ dst,
                 const uint32_t *__restrict__ flags, const uint32_t *__restrict__ crun,
                 const uint32_t *__restrict__ rsrc, unsigned long long *__restrict__ gacc,

@@ -357,7 +357,12 @@ static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part
 // coo_launch.  `mass` bounds the rank mass, and so every row sum: the
 // fixed-point unit is 2^-(62 - E) with 2 * mass < 2^E, so that sums stay
 // below 2^61 units.
-#define EG_PC_SHIFT 14  // 16K rows per partition: 128 KB of 64-bit sums in shared memory
+#ifndef EG_PC_SHIFT
+// 8K rows per partition (64 KB of 64-bit sums in shared memory); measured on
+// directed RMAT-24 / RMAT-22 per row pass: 2^14 rows 0.525 / 0.179 ms, 2^13
+// 0.505 / 0.144, 2^12 0.546 / 0.151, 2^11 0.617 / 0.160
+#define EG_PC_SHIFT 13
+#endif
 #define EG_PR_CANDS (EG_ROW_CFGS + 1)  // the tuner's candidates: the row schedules, then the partition kernel
 template <bool REDUCE>
 static int pcol_launch(eg_graph *g, const PrOp<false> &op, double2 *part, uint32_t *nparts, cudaEvent_t ev_begin,
@@ -369,7 +374,8 @@ static int pcol_launch(eg_graph *g, const PrOp<false> &op, double2 *part, uint32
     const float fx = ldexpf(1.f, 62 - E), fx_inv = ldexpf(1.f, E - 62);
     const size_t smem = eg_pc_smem<EG_PC_SHIFT>::bytes;  // allowed by pcol_prepare
     auto kern = k_pcol_rows<PrOp<false>, EG_PC_SHIFT, REDUCE>;
-    const uint32_t g1 = pc.segs < (uint32_t)ctx->sm_count ? pc.segs : (uint32_t)ctx->sm_count;  // one CTA per SM
+    const uint32_t gmax = (uint32_t)ctx->sm_count * EG_PC_CTAS;
+    const uint32_t g1 = pc.segs < gmax ? pc.segs : gmax;  // the resident CTAs
     if (g1) {
         if (ev_begin) EG_CUDA(cudaEventRecord(ev_begin, ctx->stream));
         kern<<<g1, EG_PC_THREADS, smem, ctx->stream>>>(

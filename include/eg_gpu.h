@@ -195,7 +195,7 @@ int eg_pagerank(eg_graph *g, const eg_pr_opts *opts, float *rank_out, eg_pr_stat
  * eviction.  Schedules change only how rows are split between warps, i.e.
  * the fp32 summation order.
  * The last candidate (index 12) is PageRank's partition kernel: the
- * relabelled CSC cut into partitions of 2^14 rows whose entries are ordered
+ * relabelled CSC cut into partitions of 2^13 rows whose entries are ordered
  * by source, so each source's contribution is gathered once per partition,
  * with 64-bit fixed-point row sums in shared memory (the same bits in any
  * order of addition).  It is kept for eg_pagerank only when it is the

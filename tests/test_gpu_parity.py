@@ -170,7 +170,7 @@ def test_row_schedules_and_autotuner(case):
     assert len(cands) == 13 and 0 <= chosen < 13
     assert g.bfs_tuning["switch_divisor"] in (20.0, 40.0, 80.0, 160.0, 320.0)
     assert sum(c["cache_hint"] for c in cands) == 3
-    assert [c["partition_log2"] for c in cands] == [0] * 12 + [14]
+    assert [c["partition_log2"] for c in cands] == [0] * 12 + [13]
     if n > 1000:
         assert all(c["ms"] > 0 for c in cands)
     assert cands[chosen]["ms"] == min(c["ms"] for c in cands)
