@@ -16,8 +16,15 @@
 
 #include "eg_internal.cuh"
 
+#ifndef EG_PC_SEG_MIN
 #define EG_PC_SEG_MIN 256    // chunks per segment at most: 64K entries ..
+#endif
+#ifndef EG_PC_SEG_MAX
 #define EG_PC_SEG_MAX 2048   // .. 512K entries
+#endif
+#ifndef EG_PC_SEG_PER_SM
+#define EG_PC_SEG_PER_SM 4   // segments per SM the size aims at
+#endif
 
 namespace {
 __global__ void k_pc_keys(const uint32_t *__restrict__ rowid, uint64_t M, uint32_t shift, uint32_t *keys,
@@ -143,7 +150,7 @@ int eg_build_pcols(eg_graph *g, uint32_t shift) {
     // first queue balances the SMs, but as long as that allows, since every
     // segment zeroes and writes out a partition's row sums
     uint64_t segc = EG_PC_SEG_MIN;
-    while (segc < EG_PC_SEG_MAX && segc * 4 * (uint64_t)ctx->sm_count < chunks) segc *= 2;
+    while (segc < EG_PC_SEG_MAX && segc * EG_PC_SEG_PER_SM * (uint64_t)ctx->sm_count < chunks) segc *= 2;
     std::vector<uint4> segs;
     for (uint32_t p = 0; p < P; p++) {
         const uint64_t c0 = cb[p], nch = (p + 1 < P ? cb[p + 1] : chunks) - c0;
