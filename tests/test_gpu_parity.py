@@ -221,6 +221,34 @@ def test_pagerank_partition_kernel(case):
         g.set_row_schedule(0)
 
 
+def test_pagerank_partition_kernel_hub_rows(ctx):
+    # one row with most of the entries (its 64-bit sums carry out of the low
+    # words many times and its partition spans many segments), rows spread
+    # over several partitions, an undirected copy: partition kernel against
+    # FP64, bit-identical from run to run and with the graph replay
+    import everythinggraph_gb300 as eg
+    rng = np.random.default_rng(21)
+    n = 40000
+    m_star, m_rand = 300000, 200000
+    pairs = np.empty(2 * (m_star + m_rand), dtype=np.uint32)
+    pairs[0:2 * m_star:2] = rng.integers(1, n, m_star)
+    pairs[1:2 * m_star:2] = 0  # everything points at vertex 0
+    pairs[2 * m_star::2] = rng.integers(0, n, m_rand)
+    pairs[2 * m_star + 1::2] = rng.integers(0, n, m_rand)
+    for undirected in (False, True):
+        g = ctx.from_pairs(n, pairs, undirected=undirected).build(eg.CSR | eg.CSC)
+        adj = oracle.build_adj(n, pairs, undirected=undirected)
+        g.set_row_schedule(12)
+        for dangling in (False, True):
+            ref = oracle.pagerank_f64(adj, adj.out_deg(), 1.0 / n, 10, dangling=dangling)
+            got, st = g.pagerank(iterations=10, dangling=dangling)
+            l1, mx = rel_errors(got, ref)
+            assert l1 <= PR_REL_L1 and mx <= PR_MAX_REL, (undirected, dangling, l1, mx)
+            again, _ = g.pagerank(iterations=10, dangling=dangling, use_graph=True)
+            np.testing.assert_array_equal(got, again)
+        g.free()
+
+
 def test_pagerank_source_blocks(case):
     # PageRank gathering its contributions one source block per pass (blocks
     # of 2^k vertices; the default 2^24 only splits larger graphs): within the
