@@ -481,6 +481,9 @@ typedef struct {
                             of 32 source slots is refilled only once all of
                             its sources have finished, so the sources that
                             share a word stay in step and relax dense rows;
+                            BFS queries enter only while no BFS slot is live,
+                            so that the 64 bit-sliced sources advance level
+                            by level together;
                             0: a free slot takes the next query at once
                             (lower latency under light load) */
 } eg_serve_opts;
