@@ -30,7 +30,12 @@
 #pragma once
 #include "eg_internal.cuh"
 
-#define EG_MRELAX_SPARSE 8  // at most this many active sources: edge form
+#ifndef EG_MRELAX_SPARSE
+// at most this many active sources: edge form.  Directed RMAT-23, 256
+// sources (u32 / fp32 weights): 0 (row form always) 325 / 635 ms, 1 296 / 590,
+// 2 290 / 560, 3 291 / 568, 4 294 / 585, 8 339 / 725, 16 506 / 1055
+#define EG_MRELAX_SPARSE 2
+#endif
 #define EG_MSSSP_MINB 8     // resident CTAs per SM asked of the compiler for the item kernels (32 registers)
 
 template <class Sink>
