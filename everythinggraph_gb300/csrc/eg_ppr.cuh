@@ -4,10 +4,16 @@
 #include "eg_internal.cuh"
 
 #define EG_PPR_LANES 32
+#ifndef EG_PPR_TILE
 #define EG_PPR_TILE 1024
+#endif
 #define EG_PPR_NONE 0xffffffffu
+#ifndef EG_PPR_INFLIGHT
 #define EG_PPR_INFLIGHT 8  // row loads in flight per lane in k_ppr_rows
+#endif
+#ifndef EG_PPR_MINB
 #define EG_PPR_MINB 4      // resident CTAs per SM asked of the compiler (64 registers)
+#endif
 
 namespace {
 
