@@ -264,7 +264,7 @@ __global__ void __launch_bounds__(256, EG_MSSSP_MINB) k_sv_sssp_push(const uint3
 
 // Deferred (hub, word) items in chunks of SV_SSSP_CHUNK edges handed out to
 // the CTAs, one warp per 32 edges of a chunk.
-#define SV_SSSP_CHUNK 256u
+#define SV_SSSP_CHUNK 256u  // one CTA work unit: its 8 warps take 32 edges each
 __global__ void __launch_bounds__(256) k_sv_sssp_push_big(const uint32_t *__restrict__ ptr,
                                                           const uint32_t *__restrict__ col,
                                                           const uint32_t *__restrict__ wts, uint32_t *dist,

@@ -31,7 +31,9 @@ struct SsspCounters {
 
 // Frontier vertices with more out-edges than this are relaxed by the whole
 // grid instead of one warp (RMAT hubs have 10^5..10^6 out-edges).
+#ifndef EG_SSSP_BIG_DEG
 #define EG_SSSP_BIG_DEG 2048u
+#endif
 
 __global__ void k_sssp_init(uint32_t n, uint32_t *dist, uint32_t root, uint32_t *queue, SsspCounters *cnt,
                             uint32_t inf) {
@@ -354,7 +356,7 @@ __global__ void __launch_bounds__(256, EG_MSSSP_MINB) k_msssp_push(const uint32_
 // The deferred (high-degree vertex, source word) items: chunks of
 // EG_MSSSP_CHUNK edges handed out to the CTAs, one warp per 32 edges of a
 // chunk.
-#define EG_MSSSP_CHUNK 256u
+#define EG_MSSSP_CHUNK 256u  // one CTA work unit: its 8 warps take 32 edges each
 __global__ void __launch_bounds__(256) k_msssp_push_big(const uint32_t *__restrict__ ptr,
                                                         const uint32_t *__restrict__ col,
                                                         const uint32_t *__restrict__ wts, int k, uint32_t kw,
