@@ -16,9 +16,9 @@
 // A CTA owns one segment of a partition's chunks at a time (persistent CTAs
 // take segments from a queue, longest first) and sums into the partition's
 // rows held in shared memory.  Sums are kept as unsigned 64-bit fixed point
-// (unit 2^-(62 - E), with 2^(E-1) above the rank mass, which bounds every
-// row sum; a contribution c becomes round(c / unit), an error of at most
-// half a unit per term): integer adds give the same bits in any order, so
+// (a power-of-two unit chosen by the host so that no sum reaches 2^61 units;
+// a contribution c becomes round(c / unit), an error of at most half a unit
+// per term): integer adds give the same bits in any order, so
 // the result does not depend on which warp or CTA added first.  A partition covered by one
 // segment is finished from shared memory; the segments of a longer partition
 // add their sums into a global accumulator, and the last to finish (a ticket

@@ -355,8 +355,8 @@ static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part
 // PageRank's one-pass iteration over the destination-partition layout
 // (k_pcol_rows, eg_pcol.cuh), then the rows without entries as in
 // coo_launch.  `mass` bounds the rank mass, and so every row sum: the
-// fixed-point unit is 2^-(62 - E) with 2 * mass < 2^E, so that sums stay
-// below 2^61 units.
+// fixed-point unit is 2^-S with S at most 62 - E, 2 * mass < 2^E, so that
+// sums stay below 2^61 units.
 #ifndef EG_PC_SHIFT
 // 8K rows per partition (64 KB of 64-bit sums in shared memory); measured on
 // directed RMAT-24 / RMAT-22 per row pass: 2^14 rows 0.525 / 0.179 ms, 2^13
@@ -369,9 +369,27 @@ static int pcol_launch(eg_graph *g, const PrOp<false> &op, double2 *part, uint32
                        cudaEvent_t ev_end, bool empty_rows, double mass) {
     eg_ctx *ctx = g->ctx;
     eg_pcols &pc = g->pcol;
-    int E = 0;
+    int E = 0, Em = 0, Lm = 0, Eb = 0;
     frexp(2.0 * (mass > 1.0 ? mass : 1.0), &E);
-    const float fx = ldexpf(1.f, 62 - E), fx_inv = ldexpf(1.f, E - 62);
+    frexp(mass, &Em);                       // mass < 2^Em
+    frexp((double)(g->m ? g->m : 1), &Lm);  // m < 2^Lm
+    // 2^-S with S = 62 - E keeps every sum below 2^61 units.  A coarser unit
+    // leaves most entries' high words alone: S_mean puts the mean
+    // contribution (at most mass / m) below 2^28 units, so that a row's high
+    // word takes a carry about every 16th add.  S_rank keeps the unit below
+    // 2^-27 of b = (1 - d) / n, the least rank any vertex gets, so that the
+    // rounding of a row of k entries (half a unit each) moves its rank by at
+    // most k * 2^-28 of it, 1/16 of the bound for a serial fp32 sum of the
+    // row.  No rank floor (d = 1): the finest unit.
+    const double b = (1.0 - (double)op.damping) / (double)(g->n ? g->n : 1);
+    int S = 62 - E;
+    if (b > 0.0) {
+        frexp(b, &Eb);  // b >= 2^(Eb - 1)
+        const int s_mean = 27 + Lm - Em, s_rank = 28 - Eb;
+        const int s = s_mean > s_rank ? s_mean : s_rank;
+        if (s < S) S = s;
+    }
+    const float fx = ldexpf(1.f, S), fx_inv = ldexpf(1.f, -S);
     const size_t smem = eg_pc_smem<EG_PC_SHIFT>::bytes;  // allowed by pcol_prepare
     auto kern = k_pcol_rows<PrOp<false>, EG_PC_SHIFT, REDUCE>;
     const uint32_t gmax = (uint32_t)ctx->sm_count * EG_PC_CTAS;
