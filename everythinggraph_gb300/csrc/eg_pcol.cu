@@ -23,7 +23,7 @@
 #define EG_PC_SEG_MAX 2048   // .. 512K entries
 #endif
 #ifndef EG_PC_SEG_PER_SM
-#define EG_PC_SEG_PER_SM 4   // segments per SM the size aims at
+#define EG_PC_SEG_PER_SM 4   // segments per SM the size aims at (RMAT-24 row pass: 2 or 4 0.484 ms, 8 0.516)
 #endif
 
 namespace {

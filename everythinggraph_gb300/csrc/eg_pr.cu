@@ -359,8 +359,9 @@ static int coo_launch(eg_graph *g, eg_adj &adj, eg_buf &carry_buf, double2 *part
 // sums stay below 2^61 units.
 #ifndef EG_PC_SHIFT
 // 8K rows per partition (64 KB of 64-bit sums in shared memory); measured on
-// directed RMAT-24 / RMAT-22 per row pass: 2^14 rows 0.525 / 0.179 ms, 2^13
-// 0.505 / 0.144, 2^12 0.546 / 0.151, 2^11 0.617 / 0.160
+// directed RMAT-24 / RMAT-22 per row pass with the finest unit: 2^14 rows
+// 0.525 / 0.179 ms, 2^13 0.505 / 0.144, 2^12 0.546 / 0.151, 2^11 0.617 /
+// 0.160; with the coarser unit (RMAT-24): 2^14 0.503, 2^13 0.484, 2^12 0.521
 #define EG_PC_SHIFT 13
 #endif
 #define EG_PR_CANDS (EG_ROW_CFGS + 1)  // the tuner's candidates: the row schedules, then the partition kernel
