@@ -211,6 +211,13 @@ def test_pagerank_partition_kernel(case):
         got, _ = g.pagerank(iterations=10, prev_init=0.15, swap=True, deg_multiplier=2)
         _, mx = rel_errors(got, rec["prgrid_m0"])
         assert mx <= PR_VS_REF32_MAX_REL, mx
+        # the fixed-point unit follows the least rank (1 - d) / n: other
+        # dampings, and d = 1 (no rank floor: the finest unit)
+        for d in (0.5, 0.99, 1.0):
+            ref = oracle.pagerank_f64(adj, adj.out_deg(), 1.0 / n, 10, dangling=True, damping=d)
+            got, _ = g.pagerank(iterations=10, dangling=True, damping=d)
+            l1, mx = rel_errors(got, ref)
+            assert l1 <= PR_REL_L1 and mx <= PR_MAX_REL, (d, l1, mx)
         # the tolerance stop
         ref = oracle.pagerank_f64(adj, adj.out_deg(), 1.0 / n, 50, dangling=True)
         got, st = g.pagerank(iterations=50, dangling=True, tolerance=1e-9)
