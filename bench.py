@@ -34,7 +34,7 @@ METRIC, UNIT = "GTEPS", "GTEPS"
 PR_ROWS_DRAM_BYTES_PER_ENTRY = (294.009e6 + 3.622e6) / 67108864
 # the same for the partition kernel (k_pcol_rows), from a one-pass capture
 # on directed RMAT-24 itself
-PR_PCOL_DRAM_BYTES_PER_ENTRY = (1061.336832e6 + 41.319168e6) / 268435456
+PR_PCOL_DRAM_BYTES_PER_ENTRY = (1290.110208e6 + 41.027584e6) / 268435456
 
 
 def peaks():

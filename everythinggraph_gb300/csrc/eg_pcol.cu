@@ -81,6 +81,20 @@ __global__ void k_pc_fill(const uint32_t *__restrict__ cbase, const uint32_t *__
     }
 }
 
+// Each entry's run within its chunk (the run starts at or before it, less
+// one), stored transposed like the rows: lane l's 8 bytes hold entries l,
+// l + 32, ..., l + 224.
+__global__ void k_pc_ridx(const uint32_t *__restrict__ flags, uint64_t npos, uint8_t *__restrict__ ridx) {
+    for (uint64_t o = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; o < npos; o += (uint64_t)gridDim.x * blockDim.x) {
+        const uint64_t c = o / EG_PC_CHUNK;
+        const uint32_t e = (uint32_t)(o % EG_PC_CHUNK), j = e >> 5, b = e & 31u;
+        const uint32_t *fw = flags + c * (EG_PC_CHUNK / 32);
+        uint32_t q = __popc(fw[j] & (0xffffffffu >> (31u - b)));
+        for (uint32_t i = 0; i < j; i++) q += __popc(fw[i]);
+        ridx[c * EG_PC_CHUNK + b * 8u + j] = (uint8_t)(q - 1u);
+    }
+}
+
 __global__ void k_pc_popc(const uint32_t *__restrict__ flags, uint64_t nwords, uint32_t *cnt) {
     for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwords; w += (uint64_t)gridDim.x * blockDim.x)
         cnt[w] = __popc(flags[w]);
@@ -198,9 +212,12 @@ int eg_build_pcols(eg_graph *g, uint32_t shift) {
     PTRY(eg_buf_ensure(ctx, pc.dst, npos * 2 + 16));
     PTRY(eg_buf_ensure(ctx, pc.flags, (npos / 32) * 4 + 16));
     PTRY(eg_buf_ensure(ctx, pc.crun, chunks * 4 + 16));
+    PTRY(eg_buf_ensure(ctx, pc.ridx, npos + 16));
     if (npos) {
         k_pc_fill<<<pc_grid(ctx, npos), 256, 0, ctx->stream>>>(cbase_d, ebase, P, shift, ord, ks, vs, npos,
                                                               bp<uint16_t>(pc.dst), bp<uint32_t>(pc.flags), spos);
+        ctx->launches++;
+        k_pc_ridx<<<pc_grid(ctx, npos), 256, 0, ctx->stream>>>(bp<uint32_t>(pc.flags), npos, bp<uint8_t>(pc.ridx));
         ctx->launches++;
     }
     // run numbers: an exclusive scan of the flag words' bit counts

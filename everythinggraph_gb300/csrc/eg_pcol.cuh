@@ -9,9 +9,9 @@
 // u into the partition form one run, whose contribution is loaded once and
 // added into the rows of the run's entries, and consecutive runs are
 // ascending sources, so the loads of a warp share sectors (0.19 sectors per
-// entry for partitions of 8K rows on directed RMAT-24).  The streamed words are 2 bytes per
-// entry (the row within the partition) plus a run-start bit, and 4 bytes per
-// run (its source).
+// entry for partitions of 8K rows on directed RMAT-24).  The streamed words are 3 bytes per
+// entry (the row within the partition, and the entry's run within its
+// 256-entry chunk), and 4 bytes per run (its source).
 //
 // A CTA owns one segment of a partition's chunks at a time (persistent CTAs
 // take segments from a queue, longest first) and sums into the partition's
@@ -86,27 +86,35 @@ __device__ __forceinline__ uint32_t eg_stream_ldu(const uint32_t *p, uint64_t po
 }
 
 // A warp's chunk: the rows of entries lane, lane + 32, ..., lane + 224 (one
-// 16-byte word per lane: the layout stores each chunk transposed), the
-// chunk's run-start word `lane` for lanes 0..7 (word j: entries 32j ..
-// 32j + 31), the chunk's first run.
+// 16-byte word per lane: the layout stores each chunk transposed), the runs
+// (within the chunk) of the same entries (8 bytes per lane, byte j: entry
+// lane + 32j), the chunk's first run.
 struct eg_pc_chunk {
     uint4 d8;
-    uint32_t fw;
+    uint2 ri;
     uint32_t rb;
 };
-__device__ __forceinline__ void eg_pc_load(const uint32_t *__restrict__ dst, const uint32_t *__restrict__ flags,
+__device__ __forceinline__ uint2 eg_stream_ld2(const uint32_t *p, uint64_t pol) {
+    uint2 v;
+    asm("ld.global.nc.L1::no_allocate.L2::cache_hint.v2.u32 {%0, %1}, [%2], %3;"
+        : "=r"(v.x), "=r"(v.y)
+        : "l"(p), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ void eg_pc_load(const uint32_t *__restrict__ dst, const uint32_t *__restrict__ ridx,
                                            const uint32_t *__restrict__ crun, uint64_t c, uint32_t lane,
                                            uint64_t pol, eg_pc_chunk &k) {
     k.d8 = eg_stream_ld4<1>(dst + c * (EG_PC_CHUNK / 2) + 4 * lane, pol);
-    k.fw = lane < EG_PC_CHUNK / 32 ? __ldg(flags + c * (EG_PC_CHUNK / 32) + lane) : 0u;
+    k.ri = eg_stream_ld2(ridx + c * (EG_PC_CHUNK / 4) + 2 * lane, pol);
     k.rb = __ldg(crun + c);
 }
 
-// The chunk's run count and, when it has at most 64 runs, the sources of
-// runs lane and lane + 32.
+// The chunk's run count (the run of its last entry, lane 31's byte 7, plus
+// one: padding entries continue the last run) and, when it has at most 64
+// runs, the sources of runs lane and lane + 32.
 __device__ __forceinline__ uint32_t eg_pc_sources(const eg_pc_chunk &k, const uint32_t *__restrict__ rsrc,
                                                   uint32_t lane, uint32_t &u1, uint32_t &u2) {
-    const uint32_t nr = __reduce_add_sync(EG_FULL_MASK, __popc(k.fw));
+    const uint32_t nr = __shfl_sync(EG_FULL_MASK, k.ri.y >> 24, 31) + 1u;
     u1 = u2 = 0u;
     if (nr <= 64) {
         if (lane < nr) u1 = __ldg(rsrc + k.rb + lane);
@@ -118,7 +126,7 @@ __device__ __forceinline__ uint32_t eg_pc_sources(const eg_pc_chunk &k, const ui
 template <class Op, int SHIFT, bool REDUCE>
 __global__ void __launch_bounds__(EG_PC_THREADS, EG_PC_CTAS)
     k_pcol_rows(const uint4 *__restrict__ seg, uint32_t nseg, const uint32_t *__restrict__ dst,
-                const uint32_t *__restrict__ flags, const uint32_t *__restrict__ crun,
+                const uint32_t *__restrict__ ridx, const uint32_t *__restrict__ crun,
                 const uint32_t *__restrict__ rsrc, unsigned long long *__restrict__ gacc,
                 uint32_t *__restrict__ ticket, uint32_t parts, uint32_t rows, double2 *__restrict__ part, Op op,
                 float fx, float fx_inv) {
@@ -157,14 +165,14 @@ __global__ void __launch_bounds__(EG_PC_THREADS, EG_PC_CTAS)
         eg_pc_chunk k = {}, kn = {};
         uint32_t nr = 0, u1 = 0, u2 = 0;
         if (c < c1) {
-            eg_pc_load(dst, flags, crun, c, lane, pol, k);
+            eg_pc_load(dst, ridx, crun, c, lane, pol, k);
             nr = eg_pc_sources(k, rsrc, lane, u1, u2);
         }
-        if (cn < c1) eg_pc_load(dst, flags, crun, cn, lane, pol, kn);
+        if (cn < c1) eg_pc_load(dst, ridx, crun, cn, lane, pol, kn);
         while (c < c1) {
             const uint64_t cnn = cn + EG_PC_WARPS;
             eg_pc_chunk knn = kn;
-            if (cnn < c1) eg_pc_load(dst, flags, crun, cnn, lane, pol, knn);
+            if (cnn < c1) eg_pc_load(dst, ridx, crun, cnn, lane, pol, knn);
             uint32_t nrn = 0, un1 = 0, un2 = 0;
             if (cn < c1) nrn = eg_pc_sources(kn, rsrc, lane, un1, un2);
             // one contribution per run (consecutive runs: ascending sources);
@@ -196,14 +204,8 @@ __global__ void __launch_bounds__(EG_PC_THREADS, EG_PC_CTAS)
                 }
             }
             __syncwarp();
-            uint32_t fw[EG_PC_CHUNK / 32];
-#pragma unroll
-            for (int j = 0; j < EG_PC_CHUNK / 32; j++) fw[j] = __shfl_sync(EG_FULL_MASK, k.fw, j);
-            // entry 32j + lane: its run is the last one that began at or
-            // before it (every chunk begins with a run)
+            // entry 32j + lane: its row (16 bits) and its run (byte j)
             const uint32_t h[4] = {k.d8.x, k.d8.y, k.d8.z, k.d8.w};
-            const uint32_t le = 0xffffffffu >> (31 - lane);
-            uint32_t base = 0;
 #pragma unroll
             for (int j0 = 0; j0 < 8; j0 += 4) {
                 uint32_t rw[4], old[4];
@@ -211,10 +213,9 @@ __global__ void __launch_bounds__(EG_PC_THREADS, EG_PC_CTAS)
 #pragma unroll
                 for (int jj = 0; jj < 4; jj++) {
                     const int j = j0 + jj;
-                    const uint32_t q = base + __popc(fw[j] & le);
-                    base += __popc(fw[j]);
+                    const uint32_t q = ((j < 4 ? k.ri.x : k.ri.y) >> (8 * (j & 3))) & 0xffu;
                     rw[jj] = (j & 1) ? (h[j >> 1] >> 16) : (h[j >> 1] & 0xffffu);
-                    val[jj] = wv[q - 1];
+                    val[jj] = wv[q];
                     old[jj] = atomicAdd(slo + rw[jj], (uint32_t)val[jj]);
                 }
 #pragma unroll

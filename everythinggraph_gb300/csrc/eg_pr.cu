@@ -398,7 +398,7 @@ static int pcol_launch(eg_graph *g, const PrOp<false> &op, double2 *part, uint32
     if (g1) {
         if (ev_begin) EG_CUDA(cudaEventRecord(ev_begin, ctx->stream));
         kern<<<g1, EG_PC_THREADS, smem, ctx->stream>>>(
-            bp<uint4>(pc.seg), pc.segs, bp<uint32_t>(pc.dst), bp<uint32_t>(pc.flags), bp<uint32_t>(pc.crun),
+            bp<uint4>(pc.seg), pc.segs, bp<uint32_t>(pc.dst), bp<uint32_t>(pc.ridx), bp<uint32_t>(pc.crun),
             bp<uint32_t>(pc.rsrc), bp<unsigned long long>(pc.acc), bp<uint32_t>(pc.ticket), pc.parts, g->csc_p_rows,
             part, op, fx, fx_inv);
         EG_LAUNCHED(ctx);
@@ -568,7 +568,8 @@ static int pr_graph(eg_graph *g, const eg_pr_opts &o, bool reduce, eg_pr_dev *st
     key[11] = (uint64_t)(uintptr_t)g->csc_p.rid.p ^ ((uint64_t)(uintptr_t)g->csc_p_starts.p << 17);
     key[12] = (uint64_t)(uintptr_t)g->csc_p.col.p ^ ((uint64_t)(uintptr_t)g->csc_p_trow.p << 17);
     key[13] = (uint64_t)(uintptr_t)g->csc_p.ptr.p ^ ((uint64_t)(uintptr_t)g->pcol.seg.p << 7) ^
-              ((uint64_t)(uintptr_t)g->pcol.rsrc.p << 13) ^ ((uint64_t)(uintptr_t)g->pcol.dst.p << 19);
+              ((uint64_t)(uintptr_t)g->pcol.rsrc.p << 13) ^ ((uint64_t)(uintptr_t)g->pcol.dst.p << 19) ^
+              ((uint64_t)(uintptr_t)g->pcol.ridx.p << 25) ^ ((uint64_t)(uintptr_t)g->pcol.crun.p << 31);
     key[14] = g->m ^ ((uint64_t)g->row_cfg << 56) ^ ((uint64_t)pr_block_log2(g, o) << 48) ^
               ((uint64_t)g->pr_kernel << 44) ^ ((uint64_t)g->pcol.shift << 36);
     key[15] = (uint64_t)ctx->stream ^ 0x5052ull;
