@@ -404,7 +404,7 @@ extern "C" void eg_graph_free(eg_graph *g) {
                       &g->sssp_work,    &g->ppr_work,    &g->wts,
                       &g->grid_order,   &g->grid_units,  &g->grid_off,    &g->grid_vals,   &g->grid_acc,
                       &g->esrc,         &g->edst,        &g->edge_work,
-                      &g->pcol.dst,     &g->pcol.flags,  &g->pcol.ridx,  &g->pcol.crun,   &g->pcol.rsrc,   &g->pcol.seg,
+                      &g->pcol.dst,     &g->pcol.ridx,  &g->pcol.crun,   &g->pcol.rsrc,   &g->pcol.seg,
                       &g->pcol.acc,     &g->pcol.ticket,  &g->wcc_list};
     for (eg_buf *b : bufs) eg_buf_free(c, *b);
     for (eg_bfs_graph &bg : g->bfsg) {

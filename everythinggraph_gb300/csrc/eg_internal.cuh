@@ -134,7 +134,6 @@ struct eg_pcols {
     uint32_t parts = 0, segs = 0;
     uint64_t chunks = 0, runs = 0;
     eg_buf dst;     // uint16[chunks * EG_PC_CHUNK]: the entry's row within its partition
-    eg_buf flags;   // uint32[chunks * EG_PC_CHUNK / 32]: bit set where a run begins (at every chunk's first entry too)
     eg_buf ridx;    // uint8[chunks * EG_PC_CHUNK]: each entry's run within its chunk, transposed like dst
     eg_buf crun;    // uint32[chunks]: run of each chunk's first entry
     eg_buf rsrc;    // uint32[runs]: source of each run

@@ -132,11 +132,11 @@ int eg_build_pcols(eg_graph *g, uint32_t shift) {
         return eg_fail(EG_EINVAL, "partition layout: %llu entries, fewer than 2^32 needed", (unsigned long long)M);
     pc.shift = 0;
     const uint32_t P = rows ? ((rows - 1) >> shift) + 1 : 0;
-    eg_buf ka, va, kb, vb, kc, vc, bnd, sp, wcnt, wbase;
+    eg_buf ka, va, kb, vb, kc, vc, bnd, sp, wcnt, wbase, fl;  // fl: the run-start bits (build only)
     int rc = EG_OK;
     auto cleanup = [&]() {
         cudaStreamSynchronize(ctx->stream);
-        for (eg_buf *b : {&ka, &va, &kb, &vb, &kc, &vc, &bnd, &sp, &wcnt, &wbase}) eg_buf_free(ctx, *b);
+        for (eg_buf *b : {&ka, &va, &kb, &vb, &kc, &vc, &bnd, &sp, &wcnt, &wbase, &fl}) eg_buf_free(ctx, *b);
     };
 #define PTRY(x)            \
     do {                   \
@@ -210,14 +210,14 @@ int eg_build_pcols(eg_graph *g, uint32_t shift) {
     PTRY(eg_buf_ensure(ctx, sp, npos * 4 + 16));
     uint32_t *spos = bp<uint32_t>(sp);
     PTRY(eg_buf_ensure(ctx, pc.dst, npos * 2 + 16));
-    PTRY(eg_buf_ensure(ctx, pc.flags, (npos / 32) * 4 + 16));
+    PTRY(eg_buf_ensure(ctx, fl, (npos / 32) * 4 + 16));
     PTRY(eg_buf_ensure(ctx, pc.crun, chunks * 4 + 16));
     PTRY(eg_buf_ensure(ctx, pc.ridx, npos + 16));
     if (npos) {
         k_pc_fill<<<pc_grid(ctx, npos), 256, 0, ctx->stream>>>(cbase_d, ebase, P, shift, ord, ks, vs, npos,
-                                                              bp<uint16_t>(pc.dst), bp<uint32_t>(pc.flags), spos);
+                                                              bp<uint16_t>(pc.dst), bp<uint32_t>(fl), spos);
         ctx->launches++;
-        k_pc_ridx<<<pc_grid(ctx, npos), 256, 0, ctx->stream>>>(bp<uint32_t>(pc.flags), npos, bp<uint8_t>(pc.ridx));
+        k_pc_ridx<<<pc_grid(ctx, npos), 256, 0, ctx->stream>>>(bp<uint32_t>(fl), npos, bp<uint8_t>(pc.ridx));
         ctx->launches++;
     }
     // run numbers: an exclusive scan of the flag words' bit counts
@@ -226,7 +226,7 @@ int eg_build_pcols(eg_graph *g, uint32_t shift) {
     rc = eg_buf_ensure(ctx, wbase, (nwords + 1) * 4 + 16);
     uint32_t runs = 0;
     if (rc == EG_OK && nwords) {
-        k_pc_popc<<<pc_grid(ctx, nwords), 256, 0, ctx->stream>>>(bp<uint32_t>(pc.flags), nwords, bp<uint32_t>(wcnt));
+        k_pc_popc<<<pc_grid(ctx, nwords), 256, 0, ctx->stream>>>(bp<uint32_t>(fl), nwords, bp<uint32_t>(wcnt));
         ctx->launches++;
         rc = eg_exscan_u32(ctx, bp<uint32_t>(wcnt), bp<uint32_t>(wbase), nwords);
         if (rc == EG_OK &&
@@ -236,7 +236,7 @@ int eg_build_pcols(eg_graph *g, uint32_t shift) {
             rc = eg_fail(EG_ECUDA, "partition runs: %s", cudaGetErrorString(cudaGetLastError()));
         if (rc == EG_OK) rc = eg_buf_ensure(ctx, pc.rsrc, (uint64_t)runs * 4 + 16);
         if (rc == EG_OK) {
-            k_pc_runs<<<pc_grid(ctx, npos), 256, 0, ctx->stream>>>(bp<uint32_t>(pc.flags), bp<uint32_t>(wbase), spos,
+            k_pc_runs<<<pc_grid(ctx, npos), 256, 0, ctx->stream>>>(bp<uint32_t>(fl), bp<uint32_t>(wbase), spos,
                                                                   npos, bp<uint32_t>(pc.rsrc), bp<uint32_t>(pc.crun));
             ctx->launches++;
         }
